@@ -1,0 +1,148 @@
+#!/usr/bin/env python3
+"""Recipe that builds the UNMODIFIED reference solver functions as an oracle binary.
+
+Test infrastructure only: nothing in the shipped library imports or links this.
+
+The reference (jimmy3769tw/CFD_NSsolver_forHPC_flowPassingCylinder) fixes its grid,
+domain and cylinder position as compile-time ``const`` members, so every grid needs
+its own compile.  This recipe
+
+1. copies the reference's ``inc/`` tree into ``oracle/_ref/src/inc`` (git-ignored build
+   output; the repository never holds reference sources),
+2. rewrites exactly five literals so they read from ``-D`` macros instead:
+   ``inc/grid/structureGrid.hpp:20`` (Gridder), ``:28`` (lx, ly, lz),
+   ``:38-40`` (nxCal, nyCal, nzCal) and ``inc/dfib/setEta.hpp:145`` (center_x);
+   every other line is the reference's own,
+3. compiles ``oracle/ref_harness.cpp`` (our driver, which calls the reference's own
+   functions in the order of ``src/RUN_CPU.cpp:257-436``) once per grid into
+   ``oracle/_ref/bin/ref_<nx>x<ny>x<nz>_<tag>``.
+
+Two flavours are built per grid:
+
+* ``parity``: ``-O3 -fopenmp -ffp-contract=off`` so that its arithmetic is the plain
+  IEEE order of the source (the C restatement in ``oracle/cfd_oracle.c`` is built the
+  same way and matches it bit for bit at one OpenMP thread);
+* ``native``: the reference's own ``Makefile:7,24`` flags (``-O3 -fopenmp
+  -march=native``), used only to time the reference CPU path.
+
+When the reference tree is absent (the GPU host), the patched copy already under
+``oracle/_ref/src`` is compiled instead, if present.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("CFD_REFERENCE_ROOT", "/root/reference"))
+OUT = HERE / "_ref"
+SRC = OUT / "src"
+BIN = OUT / "bin"
+
+# (file, literal in the reference, replacement)
+PATCHES = [
+    ("inc/grid/structureGrid.hpp",
+     'const std::string Gridder = "non_uniform-SML";',
+     "const std::string Gridder = ORACLE_GRIDDER;"),
+    ("inc/grid/structureGrid.hpp",
+     "const double  lx = 17.0 ,      ly = 12.0 ,      lz = 3.0 ;",
+     "const double  lx = ORACLE_LX ,      ly = ORACLE_LY ,      lz = ORACLE_LZ ;"),
+    ("inc/grid/structureGrid.hpp",
+     "const int       nxCal = 190,     // nx should > 40",
+     "const int       nxCal = ORACLE_NX,"),
+    ("inc/grid/structureGrid.hpp",
+     "                        nyCal = 210,\n                        nzCal = 40;",
+     "                        nyCal = ORACLE_NY,\n                        nzCal = ORACLE_NZ;"),
+    ("inc/dfib/setEta.hpp",
+     "double  center_x    = 6.5, ",
+     "double  center_x    = ORACLE_CX, "),
+]
+
+
+def stage_sources(force: bool = False) -> Path:
+    """Copy + patch the reference headers into oracle/_ref/src (idempotent)."""
+    stamp = SRC / ".patched"
+    if stamp.exists() and not force:
+        return SRC
+    if not (REF_ROOT / "inc").is_dir():
+        if stamp.exists():
+            return SRC
+        raise FileNotFoundError(
+            f"reference tree not found at {REF_ROOT} and no staged copy in {SRC}")
+    if SRC.exists():
+        shutil.rmtree(SRC)
+    SRC.mkdir(parents=True)
+    # amgcl / yakutat are never included by the live path; skip them to keep the copy small
+    def _ignore(d, names):
+        if Path(d).resolve() == (REF_ROOT / "inc").resolve():
+            return [n for n in names if n in ("amgcl", "yakutat")]
+        return []
+    shutil.copytree(REF_ROOT / "inc", SRC / "inc", ignore=_ignore)
+    for rel, old, new in PATCHES:
+        f = SRC / rel
+        text = f.read_text()
+        n = text.count(old)
+        if n != 1:
+            raise RuntimeError(f"patch anchor found {n} times in {rel}: {old!r}")
+        f.write_text(text.replace(old, new))
+    stamp.write_text("patched\n")
+    return SRC
+
+
+def binary_name(nx: int, ny: int, nz: int, flavour: str) -> Path:
+    return BIN / f"ref_{nx}x{ny}x{nz}_{flavour}"
+
+
+def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
+          flavour: str = "parity", force: bool = False) -> Path:
+    """Compile the harness for one grid; returns the binary path."""
+    src = stage_sources()
+    BIN.mkdir(parents=True, exist_ok=True)
+    exe = binary_name(nx, ny, nz, flavour)
+    # the domain is part of the name only through a sidecar, so check it too
+    sidecar = exe.with_suffix(".cfg")
+    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r}\n"
+    harness = HERE / "ref_harness.cpp"
+    if (exe.exists() and not force and sidecar.exists() and sidecar.read_text() == cfg
+            and exe.stat().st_mtime >= harness.stat().st_mtime):
+        return exe
+    if flavour == "parity":
+        flags = ["-O3", "-fopenmp", "-ffp-contract=off"]
+    elif flavour == "native":
+        flags = ["-O3", "-fopenmp", "-march=native"]
+    else:
+        raise ValueError(flavour)
+    defs = [f"-DORACLE_NX={nx}", f"-DORACLE_NY={ny}", f"-DORACLE_NZ={nz}",
+            f"-DORACLE_LX={lx!r}", f"-DORACLE_LY={ly!r}", f"-DORACLE_LZ={lz!r}",
+            f"-DORACLE_CX={cx!r}", '-DORACLE_GRIDDER="uniform"']
+    cmd = (["g++", "-std=c++17", "-w"] + flags + defs +
+           ["-I", str(src / "inc"), str(harness), "-o", str(exe)])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and flavour == "native":
+        # e.g. a compiler without -march=native support: fall back to portable flags
+        cmd = [c for c in cmd if c != "-march=native"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference harness build failed:\n" + r.stderr[-4000:])
+    sidecar.write_text(cfg)
+    return exe
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--grid", nargs=3, type=int, default=[96, 48, 4])
+    ap.add_argument("--domain", nargs=3, type=float, default=[24.0, 12.0, 1.0])
+    ap.add_argument("--cx", type=float, default=6.0)
+    ap.add_argument("--flavour", default="parity", choices=["parity", "native"])
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args(argv)
+    exe = build(*a.grid, *a.domain, a.cx, flavour=a.flavour, force=a.force)
+    print(exe)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,724 @@
+/* CPU restatement of the reference projection step -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Each function follows one reference function (file:line cited) operation by operation,
+ * in the same left-to-right floating-point order, so that with -ffp-contract=off it
+ * agrees bit for bit with the reference compiled at one OpenMP thread (pinned by the
+ * golden vectors under tests/golden/, made by tests/golden/make_golden.py from the
+ * reference's own code).  Loops are serial: the checker favours exactness over speed.
+ * Paths are relative to the reference project's root. */
+#include "cfd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define IC(g, i, j, k) (((long)(i) * (g)->ny + (j)) * (g)->nz + (k))
+#define GC 2
+
+static double *dalloc(long n) { return (double *)calloc((size_t)n, sizeof(double)); }
+
+long og_padded(const og_grid *g) { return (long)g->nx * g->ny * g->nz; }
+long og_cells(const og_grid *g) { return (long)g->nxc * g->nyc * g->nzc; }
+
+/* inc/grid/structureGrid.hpp:336-367 (init_uniform); X[0] = -2dx, then running sums */
+int og_grid_init_uniform(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly,
+                         double lz, double cx, double cy, double radius) {
+  memset(g, 0, sizeof(*g));
+  if (nxc < 3 || nyc < 3 || nzc < 3) return -1;
+  g->nxc = nxc; g->nyc = nyc; g->nzc = nzc;
+  g->nx = nxc + 2 * GC; g->ny = nyc + 2 * GC; g->nz = nzc + 2 * GC;
+  g->lx = lx; g->ly = ly; g->lz = lz; g->cx = cx; g->cy = cy; g->radius = radius;
+  g->X = dalloc(g->nx + 1); g->Y = dalloc(g->ny + 1); g->Z = dalloc(g->nz + 1);
+  g->Dx = dalloc(g->nx); g->Dy = dalloc(g->ny); g->Dz = dalloc(g->nz);
+  g->Dxs = dalloc(g->nx); g->Dys = dalloc(g->ny); g->Dzs = dalloc(g->nz);
+  const double dx = lx / (g->nx - 2.0 * GC);
+  const double dy = ly / (g->ny - 2.0 * GC);
+  const double dz = lz / (g->nz - 2.0 * GC);
+  g->X[0] = 0.0 - 2.0 * dx;
+  for (int i = 1; i < g->nx + 1; ++i) g->X[i] = g->X[i - 1] + dx;
+  g->Y[0] = 0.0 - 2.0 * dy;
+  for (int j = 1; j < g->ny + 1; ++j) g->Y[j] = g->Y[j - 1] + dy;
+  g->Z[0] = 0.0 - 2.0 * dz;
+  for (int k = 1; k < g->nz + 1; ++k) g->Z[k] = g->Z[k - 1] + dz;
+  for (int i = 0; i < g->nx; ++i) { g->Dx[i] = dx; g->Dxs[i] = dx; }
+  for (int j = 0; j < g->ny; ++j) { g->Dy[j] = dy; g->Dys[j] = dy; }
+  for (int k = 0; k < g->nz; ++k) { g->Dz[k] = dz; g->Dzs[k] = dz; }
+  return 0;
+}
+
+void og_grid_free(og_grid *g) {
+  free(g->X); free(g->Y); free(g->Z);
+  free(g->Dx); free(g->Dy); free(g->Dz);
+  free(g->Dxs); free(g->Dys); free(g->Dzs);
+  memset(g, 0, sizeof(*g));
+}
+
+/* seeded perturbation added to the interior of u, then v, then w (icel order) */
+static uint64_t splitmix64(uint64_t *s) {
+  *s += 0x9E3779B97F4A7C15ULL;
+  uint64_t z = *s;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+void og_perturb(const og_grid *g, double *u, double *v, double *w, uint64_t seed, double amp) {
+  uint64_t s = seed;
+  double *f[3] = {u, v, w};
+  for (int c = 0; c < 3; ++c)
+    for (int i = GC; i < g->nx - GC; ++i)
+      for (int j = GC; j < g->ny - GC; ++j)
+        for (int k = GC; k < g->nz - GC; ++k) {
+          const double r = (double)(splitmix64(&s) >> 11) * (1.0 / 9007199254740992.0);
+          f[c][IC(g, i, j, k)] += amp * (2.0 * r - 1.0);
+        }
+}
+
+/* inc/source/Convection_Difussion.hpp:20-51 (QuickUnitA) */
+static void quick_a(double Up, double Un, long pp, long p, long ic, long n, long nn,
+                    const double *Di, const double *Ds, int I, const double *phi,
+                    double *P, double *N) {
+  if (Up > 0.0)
+    *P = 0.5 * (phi[ic] + phi[p]) - 0.125 * Di[I + 1] * Di[I + 1] / Ds[I] *
+             ((phi[p] - phi[ic]) / Di[I + 1] - (phi[ic] - phi[n]) / Di[I]);
+  else
+    *P = 0.5 * (phi[ic] + phi[p]) - 0.125 * Di[I + 1] * Di[I + 1] / Ds[I + 1] *
+             ((phi[pp] - phi[p]) / Di[I + 2] - (phi[p] - phi[ic]) / Di[I + 1]);
+  if (Un > 0.0)
+    *N = 0.5 * (phi[n] + phi[ic]) - 0.125 * Di[I] * Di[I] / Ds[I - 1] *
+             ((phi[ic] - phi[n]) / Di[I] - (phi[n] - phi[nn]) / Di[I - 1]);
+  else
+    *N = 0.5 * (phi[n] + phi[ic]) - 0.125 * Di[I] * Di[I] / Ds[I] *
+             ((phi[p] - phi[ic]) / Di[I + 1] - (phi[ic] - phi[n]) / Di[I]);
+}
+
+/* inc/source/Convection_Difussion.hpp:55-90 (QuickUnitB) */
+static void quick_b(double Up, double Un, long pp, long p, long ic, long n, long nn,
+                    const double *Di, const double *Ds, int I, const double *phi,
+                    double *P, double *N) {
+  if (Up > 0.0)
+    *P = 0.5 * (phi[ic] + phi[p]) - 0.125 * Ds[I] * Ds[I] / Di[I] *
+             ((phi[p] - phi[ic]) / Ds[I] - (phi[ic] - phi[n]) / Ds[I - 1]);
+  else
+    *P = 0.5 * (phi[ic] + phi[p]) - 0.125 * Ds[I] * Ds[I] / Di[I + 1] *
+             ((phi[pp] - phi[p]) / Ds[I + 1] - (phi[p] - phi[ic]) / Ds[I]);
+  if (Un > 0.0)
+    *N = 0.5 * (phi[n] + phi[ic]) - 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I - 1] *
+             ((phi[ic] - phi[n]) / Ds[I - 1] - (phi[n] - phi[nn]) / Ds[I - 2]);
+  else
+    *N = 0.5 * (phi[n] + phi[ic]) - 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I] *
+             ((phi[p] - phi[ic]) / Ds[I] - (phi[ic] - phi[n]) / Ds[I - 1]);
+}
+
+/* inc/source/Convection_Difussion.hpp:174-450 (ConvectionDifussion, QUICK, 1st order) */
+void og_convection_diffusion(const og_grid *g, double dt, double nu, const double *u,
+                             const double *v, const double *w, double *us, double *vs,
+                             double *ws) {
+  const long sx = (long)g->ny * g->nz, sy = g->nz, sz = 1;
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  /* u: last x face (i = nx-3) is a boundary face (:198-204) */
+  for (int i = GC; i < nx - GC - 1; ++i)
+    for (int j = GC; j < ny - GC; ++j)
+      for (int k = GC; k < nz - GC; ++k) {
+        const long ic = IC(g, i, j, k);
+        const long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz,
+                   zp = ic + sz;
+        const double IT = (g->Dxs[i] * 0.5) / g->Dx[i];
+        const double Up = 0.5 * (u[xp] + u[ic]);
+        const double Un = 0.5 * (u[xm] + u[ic]);
+        const double Vp = v[ic] + (v[xp] - v[ic]) * IT;
+        const double Vn = v[ym] + (v[ym + xp - ic] - v[ym]) * IT;
+        const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
+        const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
+        double uPx, uNx, uPy, uNy, uPz, uNz;
+        quick_a(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, u, &uPx, &uNx);
+        quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, u, &uPy, &uNy);
+        quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, u, &uPz, &uNz);
+        const double convection = -dt * ((uPx * uPx - uNx * uNx) / g->Dxs[i] +
+                                         (uPy * Vp - uNy * Vn) / g->Dy[j] +
+                                         (uPz * Wp - uNz * Wn) / g->Dz[k]);
+        const double difussion =
+            nu * dt *
+            (((u[xp] - u[ic]) / g->Dx[i + 1] - (u[ic] - u[xm]) / g->Dx[i]) / g->Dxs[i] +
+             ((u[yp] - u[ic]) / g->Dys[j] - (u[ic] - u[ym]) / g->Dys[j - 1]) / g->Dy[j] +
+             ((u[zp] - u[ic]) / g->Dzs[k] - (u[ic] - u[zm]) / g->Dzs[k - 1]) / g->Dz[k]);
+        us[ic] = u[ic] + convection + difussion;
+      }
+  /* v: :276-355 */
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC - 1; ++j)
+      for (int k = GC; k < nz - GC; ++k) {
+        const long ic = IC(g, i, j, k);
+        const long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz,
+                   zp = ic + sz;
+        const double IT = (g->Dys[j] * 0.5) / g->Dy[j];
+        const double Vp = 0.5 * (v[yp] + v[ic]);
+        const double Vn = 0.5 * (v[ym] + v[ic]);
+        const double Up = u[ic] + (u[yp] - u[ic]) * IT;
+        const double Un = u[xm] + (u[xm + yp - ic] - u[xm]) * IT;
+        const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
+        const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
+        double vPx, vNx, vPy, vNy, vPz, vNz;
+        quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, v, &vPx, &vNx);
+        quick_a(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, v, &vPy, &vNy);
+        quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, v, &vPz, &vNz);
+        const double convection = -dt * ((Up * vPx - Un * vNx) / g->Dx[i] +
+                                         (vPy * vPy - vNy * vNy) / g->Dys[j] +
+                                         (Wp * vPz - Wn * vNz) / g->Dz[k]);
+        const double difussion =
+            nu * dt *
+            (((v[xp] - v[ic]) / g->Dxs[i] - (v[ic] - v[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
+             ((v[yp] - v[ic]) / g->Dy[j + 1] - (v[ic] - v[ym]) / g->Dy[j]) / g->Dys[j] +
+             ((v[zp] - v[ic]) / g->Dzs[k] - (v[ic] - v[zm]) / g->Dzs[k - 1]) / g->Dz[k]);
+        vs[ic] = v[ic] + convection + difussion;
+      }
+  /* w: :359-438 */
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j)
+      for (int k = GC; k < nz - GC - 1; ++k) {
+        const long ic = IC(g, i, j, k);
+        const long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz,
+                   zp = ic + sz;
+        const double IT = (g->Dzs[k] * 0.5) / g->Dz[k];
+        const double Wp = 0.5 * (w[zp] + w[ic]);
+        const double Wn = 0.5 * (w[zm] + w[ic]);
+        const double Up = u[ic] + (u[zp] - u[ic]) * IT;
+        const double Un = u[xm] + (u[xm + zp - ic] - u[xm]) * IT;
+        const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
+        const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
+        double wPx, wNx, wPy, wNy, wPz, wNz;
+        quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, w, &wPx, &wNx);
+        quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, w, &wPy, &wNy);
+        quick_a(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, w, &wPz, &wNz);
+        const double convection = -dt * ((Up * wPx - Un * wNx) / g->Dx[i] +
+                                         (Vp * wPy - Vn * wNy) / g->Dy[j] +
+                                         (wPz * wPz - wNz * wNz) / g->Dzs[k]);
+        const double difussion =
+            nu * dt *
+            (((w[xp] - w[ic]) / g->Dxs[i] - (w[ic] - w[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
+             ((w[yp] - w[ic]) / g->Dys[j] - (w[ic] - w[ym]) / g->Dys[j - 1]) / g->Dy[j] +
+             ((w[zp] - w[ic]) / g->Dz[k + 1] - (w[ic] - w[zm]) / g->Dz[k]) / g->Dzs[k]);
+        ws[ic] = w[ic] + convection + difussion;
+      }
+}
+
+/* Dir/Num table of inc/BoundaryCondition/FLOWpassing.hpp:6-40: face 0 inlet u=1 with
+ * reflected (no-slip) v,w; every other face zero-gradient on u, v and w. */
+static const double kDir[6][3] = {{1, 0, 0}, {0, 0, 0}, {0, 0, 0},
+                                  {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+static const double kNum[6][3] = {{0, 0, 0}, {1, 1, 1}, {1, 1, 1},
+                                  {1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
+
+/* inc/BoundaryCondition/Boundary_Condition.hpp:37-176 (BC_staggered_main), in the
+ * order one thread executes it: faces 0..5 for u,v,w, then pressure. */
+void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  double *vel[3] = {u, v, w};
+  for (int j = GC; j < ny - GC; ++j)
+    for (int k = GC; k < nz - GC; ++k) { /* BC_0 */
+      u[IC(g, 1, j, k)] = u[IC(g, 0, j, k)] = kDir[0][0] + kNum[0][0] * u[IC(g, 2, j, k)];
+      v[IC(g, 1, j, k)] = v[IC(g, 0, j, k)] =
+          kDir[0][1] * 2. + (2.0 * kNum[0][1] - 1.0) * v[IC(g, 2, j, k)];
+      w[IC(g, 1, j, k)] = w[IC(g, 0, j, k)] =
+          kDir[0][2] * 2. + (2.0 * kNum[0][2] - 1.0) * w[IC(g, 2, j, k)];
+    }
+  for (int j = GC; j < ny - GC; ++j)
+    for (int k = GC; k < nz - GC; ++k) { /* BC_1 */
+      u[IC(g, nx - 1, j, k)] = u[IC(g, nx - 2, j, k)] = u[IC(g, nx - 3, j, k)] =
+          kDir[1][0] + kNum[1][0] * u[IC(g, nx - 4, j, k)];
+      v[IC(g, nx - 1, j, k)] = v[IC(g, nx - 2, j, k)] =
+          kDir[1][1] * 2. + (2.0 * kNum[1][1] - 1.0) * v[IC(g, nx - 3, j, k)];
+      w[IC(g, nx - 1, j, k)] = w[IC(g, nx - 2, j, k)] =
+          kDir[1][2] * 2. + (2.0 * kNum[1][2] - 1.0) * w[IC(g, nx - 3, j, k)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int k = GC; k < nz - GC; ++k) { /* BC_2 */
+      u[IC(g, i, 1, k)] = u[IC(g, i, 0, k)] =
+          kDir[2][0] * 2. + (2.0 * kNum[2][0] - 1.0) * u[IC(g, i, 2, k)];
+      v[IC(g, i, 1, k)] = v[IC(g, i, 0, k)] = kDir[2][1] + kNum[2][1] * v[IC(g, i, 2, k)];
+      w[IC(g, i, 1, k)] = w[IC(g, i, 0, k)] =
+          kDir[2][2] * 2. + (2.0 * kNum[2][2] - 1.0) * w[IC(g, i, 2, k)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int k = GC; k < nz - GC; ++k) { /* BC_3 */
+      v[IC(g, i, ny - 1, k)] = v[IC(g, i, ny - 2, k)] = v[IC(g, i, ny - 3, k)] =
+          kDir[3][1] + kNum[3][1] * v[IC(g, i, ny - 4, k)];
+      u[IC(g, i, ny - 1, k)] = u[IC(g, i, ny - 2, k)] =
+          kDir[3][0] * 2. + (2.0 * kNum[3][0] - 1.0) * u[IC(g, i, ny - 3, k)];
+      w[IC(g, i, ny - 1, k)] = w[IC(g, i, ny - 2, k)] =
+          kDir[3][2] * 2. + (2.0 * kNum[3][2] - 1.0) * w[IC(g, i, ny - 3, k)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j) { /* BC_4 */
+      u[IC(g, i, j, 1)] = u[IC(g, i, j, 0)] =
+          kDir[4][0] * 2. + (2.0 * kNum[4][0] - 1.0) * u[IC(g, i, j, 2)];
+      v[IC(g, i, j, 1)] = v[IC(g, i, j, 0)] =
+          kDir[4][1] * 2. + (2.0 * kNum[4][1] - 1.0) * v[IC(g, i, j, 2)];
+      w[IC(g, i, j, 1)] = w[IC(g, i, j, 0)] = kDir[4][2] + kNum[4][2] * w[IC(g, i, j, 2)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j) { /* BC_5 */
+      w[IC(g, i, j, nz - 1)] = w[IC(g, i, j, nz - 2)] = w[IC(g, i, j, nz - 3)] =
+          kDir[5][2] + kNum[5][2] * w[IC(g, i, j, nz - 4)];
+      u[IC(g, i, j, nz - 1)] = u[IC(g, i, j, nz - 2)] =
+          kDir[5][0] * 2. + (2.0 * kNum[5][0] - 1.0) * u[IC(g, i, j, nz - 3)];
+      v[IC(g, i, j, nz - 1)] = v[IC(g, i, j, nz - 2)] =
+          kDir[5][1] * 2. + (2.0 * kNum[5][1] - 1.0) * v[IC(g, i, j, nz - 3)];
+    }
+  (void)vel;
+  /* pressure: homogeneous Neumann, :148-172 */
+  for (int j = GC; j < ny - GC; ++j)
+    for (int k = GC; k < nz - GC; ++k) {
+      p[IC(g, 1, j, k)] = p[IC(g, 0, j, k)] = p[IC(g, 2, j, k)];
+      p[IC(g, nx - 2, j, k)] = p[IC(g, nx - 1, j, k)] = p[IC(g, nx - 3, j, k)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int k = GC; k < nz - GC; ++k) {
+      p[IC(g, i, 1, k)] = p[IC(g, i, 0, k)] = p[IC(g, i, 2, k)];
+      p[IC(g, i, ny - 2, k)] = p[IC(g, i, ny - 1, k)] = p[IC(g, i, ny - 3, k)];
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j) {
+      p[IC(g, i, j, 1)] = p[IC(g, i, j, 0)] = p[IC(g, i, j, 2)];
+      p[IC(g, i, j, nz - 2)] = p[IC(g, i, j, nz - 1)] = p[IC(g, i, j, nz - 3)];
+    }
+}
+
+/* inc/BoundaryCondition/updateBC.hpp:6-108 (BC_staggered_copy) */
+void og_bc_copy(const og_grid *g, const double *u, const double *v, const double *w,
+                double *us, double *vs, double *ws) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+#define CP(a, b, idx) (b)[idx] = (a)[idx]
+  for (int j = GC; j < ny - GC; ++j)
+    for (int k = GC; k < nz - GC; ++k) {
+      const int iu[5] = {0, 1, nx - 1, nx - 3, nx - 2};
+      for (int q = 0; q < 5; ++q) CP(u, us, IC(g, iu[q], j, k));
+      const int iv[4] = {0, 1, nx - 2, nx - 1};
+      for (int q = 0; q < 4; ++q) { CP(v, vs, IC(g, iv[q], j, k)); CP(w, ws, IC(g, iv[q], j, k)); }
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int k = GC; k < nz - GC; ++k) {
+      const int ju[4] = {0, 1, ny - 2, ny - 1};
+      for (int q = 0; q < 4; ++q) { CP(u, us, IC(g, i, ju[q], k)); CP(w, ws, IC(g, i, ju[q], k)); }
+      const int jv[5] = {0, 1, ny - 3, ny - 2, ny - 1};
+      for (int q = 0; q < 5; ++q) CP(v, vs, IC(g, i, jv[q], k));
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j) {
+      const int ku[4] = {0, 1, nz - 2, nz - 1};
+      for (int q = 0; q < 4; ++q) { CP(u, us, IC(g, i, j, ku[q])); CP(v, vs, IC(g, i, j, ku[q])); }
+      const int kw[5] = {0, 1, nz - 3, nz - 2, nz - 1};
+      for (int q = 0; q < 5; ++q) CP(w, ws, IC(g, i, j, kw[q]));
+    }
+#undef CP
+}
+
+/* inc/matrix/b_matrix.hpp:35-98 (createBMatrix_omp); jp == NULL is the unscaled branch */
+void og_rhs(const og_grid *g, double dt, const double *us, const double *vs,
+            const double *ws, const double *jp, double *b) {
+  const double ddt = 1.0 / dt;
+  const long sx = (long)g->ny * g->nz, sy = g->nz;
+  long row = 0;
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k, ++row) {
+        const long ic = IC(g, i, j, k);
+        const double div = (us[ic] - us[ic - sx]) / g->Dx[i] + (vs[ic] - vs[ic - sy]) / g->Dy[j] +
+                           (ws[ic] - ws[ic - 1]) / g->Dz[k];
+        if (jp)
+          b[row] = -jp[row] * ddt * div;
+        else
+          b[row] = -ddt * div;
+      }
+}
+
+/* coefficient helpers of inc/grid/structureGrid.hpp:560-566 and SPE_sparseMatrix.hpp:93-99 */
+static double cxp(const og_grid *g, int i) { return 1.0 / g->Dx[i + GC] / g->Dxs[i + GC]; }
+static double cyp(const og_grid *g, int j) { return 1.0 / g->Dy[j + GC] / g->Dys[j + GC]; }
+static double czp(const og_grid *g, int k) { return 1.0 / g->Dz[k + GC] / g->Dzs[k + GC]; }
+static double cxm(const og_grid *g, int i) { return 1.0 / g->Dx[i + GC] / g->Dxs[i + GC - 1]; }
+static double cym(const og_grid *g, int j) { return 1.0 / g->Dy[j + GC] / g->Dys[j + GC - 1]; }
+static double czm(const og_grid *g, int k) { return 1.0 / g->Dz[k + GC] / g->Dzs[k + GC - 1]; }
+
+/* inc/grid/structureGrid.hpp:583-603: jp = 1/diag of the Neumann operator */
+void og_jacobi_scale(const og_grid *g, double *jp) {
+  long row = 0;
+  for (int i = 0; i < g->nxc; ++i)
+    for (int j = 0; j < g->nyc; ++j)
+      for (int k = 0; k < g->nzc; ++k, ++row) {
+        double aa = 0.0, bb = 0.0, cc = 0.0;
+        if (i == 0) aa = -cxm(g, i);
+        if (i == g->nxc - 1) aa = -cxp(g, i);
+        if (j == 0) bb = -cym(g, j);
+        if (j == g->nyc - 1) bb = -cyp(g, j);
+        if (k == 0) cc = -czm(g, k);
+        if (k == g->nzc - 1) cc = -czp(g, k);
+        const double ijk = cxm(g, i) + cym(g, j) + czm(g, k) + cxp(g, i) + cyp(g, j) +
+                           czp(g, k) + aa + bb + cc;
+        jp[row] = 1.0 / ijk;
+      }
+}
+
+/* inc/matrix/SPE_sparseMatrix.hpp:42-88 (setupPressure), including the swapped
+ * y-coefficients of :79/:83 (identical on a uniform grid) */
+void og_spe_setup(const og_grid *g, double *val) {
+  const int nx = g->nxc, ny = g->nyc, nz = g->nzc;
+  memset(val, 0, sizeof(double) * 7 * (size_t)og_cells(g));
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        const long ic7 = ((long)k + (long)j * nz + (long)i * ny * nz) * 7;
+        double ijk = cxm(g, i) + cym(g, j) + czm(g, k) + cxp(g, i) + cyp(g, j) + czp(g, k);
+        if (i == 0) ijk -= cxm(g, i);
+        if (i == nx - 1) ijk -= cxp(g, i);
+        if (j == 0) ijk -= cym(g, j);
+        if (j == ny - 1) ijk -= cyp(g, j);
+        if (k == 0) ijk -= czm(g, k);
+        if (k == nz - 1) ijk -= czp(g, k);
+        if (i != 0) val[ic7 + 0] = -cxm(g, i);
+        if (j != 0) val[ic7 + 1] = -cyp(g, j);
+        if (k != 0) val[ic7 + 2] = -czm(g, k);
+        val[ic7 + 3] = ijk;
+        if (k != nz - 1) val[ic7 + 4] = -czp(g, k);
+        if (j != ny - 1) val[ic7 + 5] = -cym(g, j);
+        if (i != nx - 1) val[ic7 + 6] = -cxp(g, i);
+      }
+}
+
+/* inc/matrix/SPE_sparseMatrix.hpp:92-108 (multiply_omp; bounds tested on the row index) */
+void og_spe_multiply(const og_grid *g, const double *val, const double *x, double *r) {
+  const long n = og_cells(g), nz = g->nzc, nynz = (long)g->nyc * g->nzc;
+  for (long i = 0; i < n; ++i) {
+    double sum = 0.0;
+    const long i7 = i * 7;
+    if (i - nynz >= 0) sum += val[i7 + 0] * x[i - nynz];
+    if (i - nz >= 0) sum += val[i7 + 1] * x[i - nz];
+    if (i - 1 >= 0) sum += val[i7 + 2] * x[i - 1];
+    sum += val[i7 + 3] * x[i];
+    if (i + 1 < n) sum += val[i7 + 4] * x[i + 1];
+    if (i + nz < n) sum += val[i7 + 5] * x[i + nz];
+    if (i + nynz < n) sum += val[i7 + 6] * x[i + nynz];
+    r[i] = sum;
+  }
+}
+
+/* Jacobi-scaled CSR rows of inc/grid/structureGrid.hpp:557-654 multiplied as in
+ * inc/matrix/CSR_sparseMatrix.hpp:232-243; entries in the builder's order. */
+void og_csr_multiply(const og_grid *g, const double *jp, const double *x, double *r) {
+  const int nx = g->nxc, ny = g->nyc, nz = g->nzc;
+  const long nyz = (long)ny * nz;
+  long row = 0;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k, ++row) {
+        double aa = 0.0, bb = 0.0, cc = 0.0;
+        if (i == 0) aa = -cxm(g, i);
+        if (i == nx - 1) aa = -cxp(g, i);
+        if (j == 0) bb = -cym(g, j);
+        if (j == ny - 1) bb = -cyp(g, j);
+        if (k == 0) cc = -czm(g, k);
+        if (k == nz - 1) cc = -czp(g, k);
+        const double ijk = cxm(g, i) + cym(g, j) + czm(g, k) + cxp(g, i) + cyp(g, j) +
+                           czp(g, k) + aa + bb + cc;
+        const double s = jp[row];
+        double acc = 0.0;
+        if (i != 0) acc += (-cxm(g, i) * s) * x[row - nyz];
+        if (j != 0) acc += (-cym(g, j) * s) * x[row - nz];
+        if (k != 0) acc += (-czm(g, k) * s) * x[row - 1];
+        acc += (ijk * s) * x[row];
+        if (k != nz - 1) acc += (-czp(g, k) * s) * x[row + 1];
+        if (j != ny - 1) acc += (-cyp(g, j) * s) * x[row + nz];
+        if (i != nx - 1) acc += (-cxp(g, i) * s) * x[row + nyz];
+        r[row] = acc;
+      }
+}
+
+/* inc/solver/math.hpp:13-36 at one thread: serial sums */
+static double dot(long n, const double *a, const double *b) {
+  double r = 0.0;
+  for (long i = 0; i < n; ++i) r += a[i] * b[i];
+  return r;
+}
+static double l2norm(long n, const double *a) {
+  double r = 0.0;
+  for (long i = 0; i < n; ++i) r += a[i] * a[i];
+  return sqrt(r);
+}
+
+int og_bicg_init(og_bicg *s, const og_grid *g, int kind, double tol) {
+  memset(s, 0, sizeof(*s));
+  s->n = og_cells(g);
+  s->iters_max = 5000;           /* bicgstabRe2.hpp:47 */
+  s->tol = tol;
+  s->restart_factor = 1e-7;      /* :53 */
+  s->kind = kind;
+  s->g = g;
+  double **v[8] = {&s->r0, &s->r1, &s->p1, &s->s1, &s->ap, &s->as, &s->px1, &s->px2};
+  for (int q = 0; q < 8; ++q) *v[q] = dalloc(s->n);
+  if (kind == 0) {
+    s->val7 = dalloc(7 * s->n);
+    og_spe_setup(g, s->val7);
+  } else {
+    s->jp = dalloc(s->n);
+    og_jacobi_scale(g, s->jp);
+  }
+  return 0;
+}
+
+void og_bicg_free(og_bicg *s) {
+  free(s->r0); free(s->r1); free(s->p1); free(s->s1); free(s->ap); free(s->as);
+  free(s->px1); free(s->px2); free(s->val7); free(s->jp);
+  memset(s, 0, sizeof(*s));
+}
+
+static void apply(og_bicg *s, const double *x, double *y) {
+  if (s->kind == 0) og_spe_multiply(s->g, s->val7, x, y);
+  else og_csr_multiply(s->g, s->jp, x, y);
+}
+
+/* inc/solver/bicgstabRe2.hpp:84-180 (solve) */
+int og_bicg_solve(og_bicg *s, const double *rhs, double *x, double *relres) {
+  const long n = s->n;
+  s->timestep++;
+  double r1r0 = 0, r1r0l = 0, a = 0, w = 0, b = 0;
+  const double norm0 = l2norm(n, rhs);
+  apply(s, x, s->r0);
+  memcpy(s->px2, s->px1, sizeof(double) * n);
+  memcpy(s->px1, x, sizeof(double) * n);
+  for (long i = 0; i < n; ++i) s->r0[i] = rhs[i] - s->r0[i];
+  memcpy(s->r1, s->r0, sizeof(double) * n);
+  memcpy(s->p1, s->r0, sizeof(double) * n);
+  r1r0 = dot(n, s->r1, s->r0);
+  int it = 0;
+  for (;;) {
+    apply(s, s->p1, s->ap);
+    a = r1r0 / dot(n, s->ap, s->r0);
+    for (long i = 0; i < n; ++i) s->s1[i] = s->r1[i] - a * s->ap[i];
+    apply(s, s->s1, s->as);
+    w = dot(n, s->as, s->s1) / dot(n, s->as, s->as);
+    for (long i = 0; i < n; ++i) {
+      x[i] += a * s->p1[i] + w * s->s1[i];
+      s->r1[i] = s->s1[i] - w * s->as[i];
+    }
+    if ((l2norm(n, s->r1) / norm0) < s->tol) break;
+    if (it >= s->iters_max) {
+      long bad = 0;
+      for (long i = 0; i < n; ++i)
+        if (isnan(x[i]) || isinf(x[i])) { x[i] = s->px1[i]; ++bad; }
+      if (bad > n * 0.1)
+        for (long i = 0; i < n; ++i) x[i] = s->px2[i];
+      break;
+    }
+    r1r0l = r1r0;
+    r1r0 = dot(n, s->r1, s->r0);
+    b = (a / w) * (r1r0 / r1r0l);
+    if (s->timestep < 10 || fabs(r1r0l) > s->tol * s->restart_factor) {
+      for (long i = 0; i < n; ++i) s->p1[i] = s->r1[i] + b * (s->p1[i] - w * s->ap[i]);
+    } else {
+      for (long i = 0; i < n; ++i) { s->r0[i] = s->r1[i]; s->p1[i] = s->r1[i]; }
+    }
+    ++it;
+  }
+  *relres = l2norm(n, s->r1) / norm0;
+  return it;
+}
+
+/* inc/pressure/solver/SorPipeLine.omp.hpp:4-129 in one thread's (lexicographic) order;
+ * the coefficient cache cf[8] of :33-49 and the stop rule of :110 */
+int og_sor(const og_grid *g, double dt, double omega, double tol, int itmax,
+           const double *us, const double *vs, const double *ws, double *p, double *err) {
+  const long n = og_cells(g);
+  double *cf = dalloc(8 * n);
+  const double rdt = 1.0 / dt;
+  const long sx = (long)g->ny * g->nz, sy = g->nz;
+  long row = 0;
+  double norm_rhs = 0.0;
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k, ++row) {
+        double *c = cf + 8 * row;
+        const double *Dx = g->Dx, *Dy = g->Dy, *Dz = g->Dz;
+        c[0] = Dy[j] * Dz[k] / g->Dxs[i];
+        c[1] = Dy[j] * Dz[k] / g->Dxs[i - 1];
+        c[2] = Dx[i] * Dz[k] / g->Dys[j];
+        c[3] = Dx[i] * Dz[k] / g->Dys[j - 1];
+        c[4] = Dx[i] * Dy[j] / g->Dzs[k];
+        c[5] = Dx[i] * Dy[j] / g->Dzs[k - 1];
+        const double coef = Dy[j] * Dz[k] / g->Dxs[i] + Dy[j] * Dz[k] / g->Dxs[i - 1] +
+                            Dx[i] * Dz[k] / g->Dys[j] + Dx[i] * Dz[k] / g->Dys[j - 1] +
+                            Dx[i] * Dy[j] / g->Dzs[k] + Dx[i] * Dy[j] / g->Dzs[k - 1];
+        c[7] = -1.0 / coef;
+        const long ic = IC(g, i, j, k);
+        const double mChange = (us[ic] - us[ic - sx]) * Dy[j] * Dz[k] +
+                               (vs[ic] - vs[ic - sy]) * Dx[i] * Dz[k] +
+                               (ws[ic] - ws[ic - 1]) * Dx[i] * Dy[j];
+        c[6] = mChange * rdt;
+        norm_rhs += (mChange * rdt) * (mChange * rdt);
+      }
+  norm_rhs = sqrt(norm_rhs);
+  int it;
+  double residual = 0.0;
+  for (it = 0; it < itmax; ++it) {
+    residual = 0;
+    row = 0;
+    for (int i = GC; i < g->nx - GC; ++i)
+      for (int j = GC; j < g->ny - GC; ++j)
+        for (int k = GC; k < g->nz - GC; ++k, ++row) {
+          const long ic = IC(g, i, j, k);
+          const double *c = cf + 8 * row;
+          const double pNEW = (-p[ic + sx] * c[0] - p[ic - sx] * c[1] - p[ic + sy] * c[2] -
+                               p[ic - sy] * c[3] - p[ic + 1] * c[4] - p[ic - 1] * c[5] + c[6]) *
+                              c[7];
+          const double pChange = fabs(pNEW - p[ic]);
+          p[ic] += omega * (pNEW - p[ic]);
+          residual += pChange / norm_rhs;
+        }
+    if (sqrt(residual) < tol) break;
+  }
+  *err = sqrt(residual);
+  free(cf);
+  return it;
+}
+
+/* inc/pressure/Transform.hpp:8-20 */
+void og_transform(const og_grid *g, const double *x, double *p) {
+  long row = 0;
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k, ++row) p[IC(g, i, j, k)] = x[row];
+}
+
+/* inc/dfib/updateUandF.hpp:90-180 (update_UandF_omp); solid velocity 0 */
+void og_update_uf(const og_grid *g, double dt, const double *eta, const double *p,
+                  const double *us, const double *vs, const double *ws, double *u3,
+                  double *v3, double *w3, double *f) {
+  const long tot = og_padded(g);
+  const long sx = (long)g->ny * g->nz, sy = g->nz;
+  const double uS = 0.0, vS = 0.0, wS = 0.0;
+  for (int i = GC; i < g->nx - GC - 1; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k) {
+        const long ic = IC(g, i, j, k), icP = ic + sx;
+        const double T2u = us[ic] - dt * (p[icP] - p[ic]) / g->Dxs[i];
+        const double e = eta[ic] + (eta[icP] - eta[ic]) * ((g->Dxs[i] * 0.5) / g->Dx[i]);
+        u3[ic] = eta[ic] * uS + (1.0 - e) * T2u;
+        f[ic] = (u3[ic] - T2u) / dt;
+      }
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC - 1; ++j)
+      for (int k = GC; k < g->nz - GC; ++k) {
+        const long ic = IC(g, i, j, k), icP = ic + sy;
+        const double T2v = vs[ic] - dt * (p[icP] - p[ic]) / g->Dys[j];
+        const double e = eta[ic] + (eta[icP] - eta[ic]) * ((g->Dys[j] * 0.5) / g->Dy[j]);
+        v3[ic] = eta[ic] * vS + (1.0 - e) * T2v;
+        f[ic + tot] = (v3[ic] - T2v) / dt;
+      }
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC - 1; ++k) {
+        const long ic = IC(g, i, j, k), icP = ic + 1;
+        const double T2w = ws[ic] - dt * (p[icP] - p[ic]) / g->Dzs[k];
+        const double e = eta[ic] + (eta[icP] - eta[ic]) * ((g->Dzs[k] * 0.5) / g->Dz[k]);
+        w3[ic] = eta[ic] * wS + (1.0 - e) * T2w;
+        f[ic + 2 * tot] = (w3[ic] - T2w) / dt;
+      }
+}
+
+/* inc/dfib/setEta.hpp:136-204 (DFIB_CylinderZ): 100x100 sub-sampling of the cells within
+ * half a cell diagonal of the circle, then extrusion along z. */
+void og_dfib_cylinder_z(const og_grid *g, double *eta) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz, nsub = 100;
+  const double cx = g->cx, cy = g->cy, R = g->radius;
+  double sdx[101], sdy[101];
+  for (int i = GC; i < nx - GC; ++i)
+    for (int j = GC; j < ny - GC; ++j) {
+      const long icel = IC(g, i, j, 0);
+      const double Diagonal = sqrt(g->Dx[i] * g->Dx[i] + g->Dy[j] * g->Dy[j]) * 0.5;
+      const double ddx = ((g->X[i] + g->X[i + 1]) * 0.5) - cx;
+      const double ddy = ((g->Y[j] + g->Y[j + 1]) * 0.5) - cy;
+      const double Distance = sqrt(ddx * ddx + ddy * ddy);
+      if (fabs(Distance - R) < Diagonal) {
+        long xi = 0;
+        const double dyg = g->Dy[j] / (double)nsub;
+        const double dxg = g->Dx[i] / (double)nsub;
+        for (int q = 0; q < nsub + 1; ++q) {
+          sdy[q] = g->Y[j] + (double)q * dyg;
+          sdx[q] = g->X[i] + (double)q * dxg;
+        }
+        for (int ii = 0; ii < nsub; ++ii)
+          for (int jj = 0; jj < nsub; ++jj) {
+            const double a = (sdx[ii] + sdx[ii + 1]) * 0.5 - cx;
+            const double b = (sdy[jj] + sdy[jj + 1]) * 0.5 - cy;
+            if (sqrt(a * a + b * b) <= R) ++xi;
+          }
+        eta[icel] = (double)xi * (1.0 / ((double)nsub * (double)nsub));
+      } else if (Distance > R) {
+        eta[icel] = 0.;
+      } else {
+        eta[icel] = 1.;
+      }
+    }
+  for (int i = 0; i < nx - 1; ++i)
+    for (int j = 0; j < ny - 1; ++j)
+      for (int k = 1; k < nz - 1; ++k) eta[IC(g, i, j, k)] = eta[IC(g, i, j, 0)];
+}
+
+/* inc/dfib/virtualForceIntergrator.hpp:67-90 (virtualF_Int) */
+double og_force_sum(const og_grid *g, const double *f, int dir) {
+  const long tot = og_padded(g);
+  double s = 0.0;
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k)
+        s += f[IC(g, i, j, k) + tot * dir] * (g->Dx[i] * g->Dy[j] * g->Dz[k]);
+  return s;
+}
+
+int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
+           double omega, double *u, double *v, double *w, double *p, double *eta,
+           double *stats) {
+  const long tot = og_padded(g), n = og_cells(g);
+  const double nu = 1.0 / Re; /* 0_1_SimulationVariable.hpp:26-31 */
+  double *us = dalloc(tot), *vs = dalloc(tot), *ws = dalloc(tot);
+  double *u3 = dalloc(tot), *v3 = dalloc(tot), *w3 = dalloc(tot);
+  double *f = dalloc(3 * tot), *b = dalloc(n), *x = dalloc(n);
+  og_bicg bs;
+  int rc = 0;
+  /* src/RUN_CPU.cpp:104-109 */
+  memcpy(us, u, sizeof(double) * tot); memcpy(u3, u, sizeof(double) * tot);
+  memcpy(vs, v, sizeof(double) * tot); memcpy(v3, v, sizeof(double) * tot);
+  memcpy(ws, w, sizeof(double) * tot); memcpy(w3, w, sizeof(double) * tot);
+  og_bc_main(g, u, v, w, p);
+  og_bc_copy(g, u, v, w, us, vs, ws);
+  if (solver == 0 || solver == 1) og_bicg_init(&bs, g, solver, tol);
+  memset(eta, 0, sizeof(double) * tot);
+  og_dfib_cylinder_z(g, eta);
+  for (int s = 1; s <= steps; ++s) {
+    og_convection_diffusion(g, dt, nu, u, v, w, us, vs, ws);
+    int iters = 0;
+    double err = 0.0;
+    if (s > 1) { /* RUN_CPU.cpp:287/:303: no pressure solve at the first step */
+      if (solver == 2) {
+        iters = og_sor(g, dt, omega, tol, 5000, us, vs, ws, p, &err);
+      } else {
+        og_rhs(g, dt, us, vs, ws, solver == 1 ? bs.jp : NULL, b);
+        iters = og_bicg_solve(&bs, b, x, &err);
+        og_transform(g, x, p);
+      }
+    }
+    og_update_uf(g, dt, eta, p, us, vs, ws, u3, v3, w3, f);
+    memcpy(u, u3, sizeof(double) * tot); /* copyVel */
+    memcpy(v, v3, sizeof(double) * tot);
+    memcpy(w, w3, sizeof(double) * tot);
+    og_bc_main(g, u, v, w, p);
+    og_bc_copy(g, u, v, w, us, vs, ws);
+    if (stats) {
+      stats[4 * (s - 1) + 0] = iters;
+      stats[4 * (s - 1) + 1] = err;
+      stats[4 * (s - 1) + 2] = -2.0 * og_force_sum(g, f, 0) / g->lz;
+      stats[4 * (s - 1) + 3] = -2.0 * og_force_sum(g, f, 1) / g->lz;
+    }
+  }
+  if (solver == 0 || solver == 1) og_bicg_free(&bs);
+  free(us); free(vs); free(ws); free(u3); free(v3); free(w3); free(f); free(b); free(x);
+  return rc;
+}

@@ -1,0 +1,84 @@
+/* CPU restatement of the reference projection step (jimmy3769tw/CFD_NSsolver_forHPC_
+ * flowPassingCylinder) in plain C.  TEST INFRASTRUCTURE ONLY: the parity tests, the
+ * smoke check and bench.py's CPU-baseline leg call it as the checker; the shipped
+ * library never links it.
+ *
+ * Parity is pinned: with -ffp-contract=off it reproduces, bit for bit, the reference's
+ * own functions compiled from its sources by oracle/build_ref.py (one OpenMP thread),
+ * on the golden vectors under tests/golden/.
+ *
+ * Layout is the reference's: padded arrays of (nxc+4)(nyc+4)(nzc+4) doubles,
+ * icel = i*ny*nz + j*nz + k (inc/grid/structureGrid.hpp:154), interior i in [2, nx-2);
+ * compact Poisson vectors use icelCal = (i-2)*nyc*nzc + (j-2)*nzc + (k-2) (:178). */
+#ifndef CFD_ORACLE_H
+#define CFD_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct og_grid {
+  int nxc, nyc, nzc; /* interior cells */
+  int nx, ny, nz;    /* padded sizes, nxc + 4 */
+  double lx, ly, lz, cx, cy, radius;
+  double *X, *Y, *Z;           /* node coordinates, nx+1 / ny+1 / nz+1 */
+  double *Dx, *Dy, *Dz;        /* cell widths, nx / ny / nz */
+  double *Dxs, *Dys, *Dzs;     /* centre spacings */
+} og_grid;
+
+int og_grid_init_uniform(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly,
+                         double lz, double cx, double cy, double radius);
+void og_grid_free(og_grid *g);
+long og_padded(const og_grid *g);
+long og_cells(const og_grid *g);
+
+void og_perturb(const og_grid *g, double *u, double *v, double *w, uint64_t seed, double amp);
+void og_convection_diffusion(const og_grid *g, double dt, double nu, const double *u,
+                             const double *v, const double *w, double *us, double *vs,
+                             double *ws);
+void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p);
+void og_bc_copy(const og_grid *g, const double *u, const double *v, const double *w,
+                double *us, double *vs, double *ws);
+void og_rhs(const og_grid *g, double dt, const double *us, const double *vs,
+            const double *ws, const double *jp, double *b);
+void og_jacobi_scale(const og_grid *g, double *jp);
+void og_spe_setup(const og_grid *g, double *val7);
+void og_spe_multiply(const og_grid *g, const double *val7, const double *x, double *y);
+void og_csr_multiply(const og_grid *g, const double *jp, const double *x, double *y);
+
+typedef struct og_bicg {
+  long n;
+  int timestep, iters_max;
+  double tol, restart_factor;
+  double *r0, *r1, *p1, *s1, *ap, *as, *px1, *px2;
+  /* operator: 0 = SPE (unscaled), 1 = CSR rows scaled by jp */
+  int kind;
+  const og_grid *g;
+  double *val7, *jp;
+} og_bicg;
+int og_bicg_init(og_bicg *s, const og_grid *g, int kind, double tol);
+void og_bicg_free(og_bicg *s);
+int og_bicg_solve(og_bicg *s, const double *rhs, double *x, double *relres);
+
+int og_sor(const og_grid *g, double dt, double omega, double tol, int itmax,
+           const double *us, const double *vs, const double *ws, double *p, double *err);
+void og_transform(const og_grid *g, const double *x, double *p);
+void og_update_uf(const og_grid *g, double dt, const double *eta, const double *p,
+                  const double *us, const double *vs, const double *ws, double *u3,
+                  double *v3, double *w3, double *f);
+void og_dfib_cylinder_z(const og_grid *g, double *eta);
+double og_force_sum(const og_grid *g, const double *f, int dir);
+
+/* Whole run in the order of src/RUN_CPU.cpp:257-436.  solver: 0 SPE-BiCGSTAB,
+ * 1 CSR(Jacobi)-BiCGSTAB, 2 lexicographic SOR.  Fields in/out are padded; stats gets
+ * 4 doubles per step (iters, err, cd, cl).  u,v,w,p on entry: the initial state before
+ * the first ghost fill (uniform u=1 plus any perturbation); on exit: T0 and p after the
+ * last step. */
+int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
+           double omega, double *u, double *v, double *w, double *p, double *eta,
+           double *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

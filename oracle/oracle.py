@@ -1,0 +1,226 @@
+"""ctypes binding of the C restatement (oracle/cfd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY -- imported by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg as the checker; the library under test never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libcfd_oracle.so"
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> Path:
+    """Compile the restatement with the flags that keep IEEE source order."""
+    BUILD.mkdir(exist_ok=True)
+    src = HERE / "cfd_oracle.c"
+    hdr = HERE / "cfd_oracle.h"
+    newest = max(src.stat().st_mtime, hdr.stat().st_mtime)
+    if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
+        return LIB
+    tmp = LIB.with_suffix(f".so.{os.getpid()}")
+    cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+           "-shared", str(src), "-o", str(tmp), "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nxc", C.c_int), ("nyc", C.c_int), ("nzc", C.c_int),
+                ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+                ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)] + [
+        (n, C.POINTER(C.c_double)) for n in
+        ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")]
+
+
+class _Bicg(C.Structure):
+    _fields_ = [("n", C.c_long), ("timestep", C.c_int), ("iters_max", C.c_int),
+                ("tol", C.c_double), ("restart_factor", C.c_double)] + [
+        (n, C.POINTER(C.c_double)) for n in
+        ("r0", "r1", "p1", "s1", "ap", "as_", "px1", "px2")] + [
+        ("kind", C.c_int), ("g", C.c_void_p), ("val7", C.POINTER(C.c_double)),
+        ("jp", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(str(build()))
+        gp = C.POINTER(_Grid)
+        L.og_grid_init_uniform.argtypes = [gp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 6
+        L.og_grid_free.argtypes = [gp]
+        L.og_perturb.argtypes = [gp, _dp, _dp, _dp, C.c_uint64, C.c_double]
+        L.og_convection_diffusion.argtypes = [gp, C.c_double, C.c_double] + [_dp] * 6
+        L.og_bc_main.argtypes = [gp] + [_dp] * 4
+        L.og_bc_copy.argtypes = [gp] + [_dp] * 6
+        L.og_rhs.argtypes = [gp, C.c_double, _dp, _dp, _dp, C.c_void_p, _dp]
+        L.og_jacobi_scale.argtypes = [gp, _dp]
+        L.og_spe_setup.argtypes = [gp, _dp]
+        L.og_spe_multiply.argtypes = [gp, _dp, _dp, _dp]
+        L.og_csr_multiply.argtypes = [gp, _dp, _dp, _dp]
+        bp = C.POINTER(_Bicg)
+        L.og_bicg_init.argtypes = [bp, gp, C.c_int, C.c_double]
+        L.og_bicg_free.argtypes = [bp]
+        L.og_bicg_solve.argtypes = [bp, _dp, _dp, C.POINTER(C.c_double)]
+        L.og_sor.argtypes = [gp, C.c_double, C.c_double, C.c_double, C.c_int,
+                             _dp, _dp, _dp, _dp, C.POINTER(C.c_double)]
+        L.og_transform.argtypes = [gp, _dp, _dp]
+        L.og_update_uf.argtypes = [gp, C.c_double] + [_dp] * 9
+        L.og_dfib_cylinder_z.argtypes = [gp, _dp]
+        L.og_force_sum.argtypes = [gp, _dp, C.c_int]
+        L.og_force_sum.restype = C.c_double
+        L.og_run.argtypes = [gp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                             C.c_double, _dp, _dp, _dp, _dp, _dp, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+class Grid:
+    """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
+
+    def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5):
+        self._g = _Grid()
+        rc = lib().og_grid_init_uniform(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx,
+                                        ly / 2.0, radius)
+        if rc != 0:
+            raise ValueError("grid too small")
+        self.shape = (nxc + 4, nyc + 4, nzc + 4)
+        self.cells = nxc * nyc * nzc
+
+    @property
+    def ptr(self):
+        return C.byref(self._g)
+
+    def __del__(self):
+        try:
+            lib().og_grid_free(C.byref(self._g))
+        except Exception:
+            pass
+
+    def zeros(self):
+        return np.zeros(self.shape, dtype=np.float64)
+
+    def coords(self):
+        g = self._g
+        return (np.ctypeslib.as_array(g.X, (g.nx + 1,)).copy(),
+                np.ctypeslib.as_array(g.Y, (g.ny + 1,)).copy(),
+                np.ctypeslib.as_array(g.Z, (g.nz + 1,)).copy())
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def convection_diffusion(g: Grid, dt, nu, u, v, w, us, vs, ws):
+    lib().og_convection_diffusion(g.ptr, dt, nu, _c(u), _c(v), _c(w), us, vs, ws)
+
+
+def bc_main(g, u, v, w, p):
+    lib().og_bc_main(g.ptr, u, v, w, p)
+
+
+def bc_copy(g, u, v, w, us, vs, ws):
+    lib().og_bc_copy(g.ptr, _c(u), _c(v), _c(w), us, vs, ws)
+
+
+def rhs(g, dt, us, vs, ws, jp=None):
+    b = np.zeros(g.cells)
+    jpp = None if jp is None else _c(jp).ctypes.data_as(C.c_void_p)
+    lib().og_rhs(g.ptr, dt, _c(us), _c(vs), _c(ws), jpp, b)
+    return b
+
+
+def jacobi_scale(g):
+    jp = np.zeros(g.cells)
+    lib().og_jacobi_scale(g.ptr, jp)
+    return jp
+
+
+def spe_multiply(g, x):
+    val = np.zeros(7 * g.cells)
+    lib().og_spe_setup(g.ptr, val)
+    y = np.zeros(g.cells)
+    lib().og_spe_multiply(g.ptr, val, _c(x), y)
+    return y
+
+
+def csr_multiply(g, x):
+    y = np.zeros(g.cells)
+    lib().og_csr_multiply(g.ptr, jacobi_scale(g), _c(x), y)
+    return y
+
+
+class BiCGSTAB:
+    """bicgstabRe2 (inc/solver/bicgstabRe2.hpp) with kind 0 = SPE, 1 = Jacobi-scaled CSR."""
+
+    def __init__(self, g: Grid, kind: int, tol: float):
+        self._s = _Bicg()
+        self._g = g
+        lib().og_bicg_init(C.byref(self._s), g.ptr, kind, tol)
+
+    def solve(self, rhs_, x):
+        rr = C.c_double()
+        it = lib().og_bicg_solve(C.byref(self._s), _c(rhs_), x, C.byref(rr))
+        return it, rr.value
+
+    def __del__(self):
+        try:
+            lib().og_bicg_free(C.byref(self._s))
+        except Exception:
+            pass
+
+
+def sor(g, dt, omega, tol, itmax, us, vs, ws, p):
+    err = C.c_double()
+    it = lib().og_sor(g.ptr, dt, omega, tol, itmax, _c(us), _c(vs), _c(ws), p, C.byref(err))
+    return it, err.value
+
+
+def update_uf(g, dt, eta, p, us, vs, ws, u3, v3, w3, f):
+    lib().og_update_uf(g.ptr, dt, _c(eta), _c(p), _c(us), _c(vs), _c(ws), u3, v3, w3, f)
+
+
+def dfib_cylinder_z(g):
+    eta = g.zeros()
+    lib().og_dfib_cylinder_z(g.ptr, eta)
+    return eta
+
+
+def force_sum(g, f, d):
+    return lib().og_force_sum(g.ptr, _c(f), d)
+
+
+def perturb(g, u, v, w, seed, amp):
+    lib().og_perturb(g.ptr, u, v, w, seed, amp)
+
+
+SOLVERS = {"spe": 0, "bicgstab": 0, "jacobi": 1, "csr": 1, "sor": 2}
+
+
+def run(g: Grid, steps, Re, dt, tol, solver="spe", omega=1.8, seed=0, amp=0.0):
+    """Whole run (src/RUN_CPU.cpp:257-436 order); returns dict of final fields + stats."""
+    u = np.ones(g.shape)
+    v = g.zeros()
+    w = g.zeros()
+    if amp:
+        perturb(g, u, v, w, seed, amp)
+    p = g.zeros()
+    eta = g.zeros()
+    stats = np.zeros((steps, 4))
+    lib().og_run(g.ptr, steps, Re, dt, tol, SOLVERS[solver], omega, u, v, w, p, eta,
+                 stats.ctypes.data_as(C.c_void_p))
+    return {"u": u, "v": v, "w": w, "p": p, "eta": eta, "iters": stats[:, 0].astype(int),
+            "err": stats[:, 1], "cd": stats[:, 2], "cl": stats[:, 3]}

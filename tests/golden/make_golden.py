@@ -1,0 +1,99 @@
+#!/usr/bin/env python3
+"""Regenerate the golden vectors from the reference's OWN code.
+
+Builds the reference harness (oracle/build_ref.py: the reference's headers with only the
+grid/domain/cylinder literals turned into -D macros, driven by oracle/ref_harness.cpp)
+and runs it at ONE OpenMP thread, so that its in-place loops run in the sequential
+order.  Needs the reference tree (this container), not a GPU.
+
+Fixtures written next to this file:
+  unit_<grid>.npz   every hot-path function once on seeded random fields
+                    (inputs and outputs, padded layout)
+  run_<case>.npz    whole runs of the 96x48x4 flow-past-cylinder case (reference BCs,
+                    Re 100, dt 0.005): interior of the final u, v, w, p and the per-step
+                    iterations, residual, Cd and Cl.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+from oracle import build_ref  # noqa: E402
+
+UNIT_GRIDS = {
+    # name: (nxc, nyc, nzc, lx, ly, lz, cx)
+    "g10x8x6_h025": (10, 8, 6, 2.5, 2.0, 1.5, 1.25),
+    "g10x8x6_h030": (10, 8, 6, 3.0, 2.4, 1.8, 1.5),
+}
+C1 = (96, 48, 4, 24.0, 12.0, 1.0, 6.0)
+RUNS = {
+    # name: (steps, Re, dt, tol, solver, omega)
+    "c1_spe_tol1e-8_200": (200, 100.0, 0.005, 1e-8, "spe", 1.8),
+    "c1_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8),
+    "c1_csr_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "csr", 1.8),
+    "c1_sor_tol1e-3_4": (4, 100.0, 0.005, 1e-3, "sor", 1.8),
+}
+UNIT_SEED = 7
+UNIT_RE, UNIT_DT = 100.0, 0.005
+
+
+def _env():
+    e = dict(os.environ)
+    e["OMP_NUM_THREADS"] = "1"
+    return e
+
+
+def _load_dir(d: Path) -> dict:
+    out = {}
+    for f in sorted(d.glob("*.f64")):
+        out[f.stem] = np.fromfile(f, dtype="<f8")
+    return out
+
+
+def make_unit(name, spec):
+    nxc, nyc, nzc, lx, ly, lz, cx = spec
+    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity")
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([str(exe), "unit", str(UNIT_SEED), repr(UNIT_RE), repr(UNIT_DT), td],
+                       check=True, env=_env(), stdout=subprocess.DEVNULL, cwd=td)
+        arrs = _load_dir(Path(td))
+    meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, UNIT_RE, UNIT_DT, UNIT_SEED], dtype=np.float64)
+    np.savez_compressed(HERE / f"unit_{name}.npz", meta=meta, **arrs)
+
+
+def make_run(name, spec):
+    nxc, nyc, nzc, lx, ly, lz, cx = C1
+    steps, Re, dt, tol, solver, omega = spec
+    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity")
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([str(exe), "run", str(steps), repr(Re), repr(dt), repr(tol), solver,
+                        repr(omega), "0", "0", td], check=True, env=_env(),
+                       stdout=subprocess.DEVNULL, cwd=td)
+        shape = (nxc + 4, nyc + 4, nzc + 4)
+        fields = {k: np.fromfile(Path(td) / f"{k}.f64").reshape(shape)[2:-2, 2:-2, 2:-2].copy()
+                  for k in ("u", "v", "w", "p")}
+        stats = np.loadtxt(Path(td) / "stats.txt")
+    meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, steps, Re, dt, tol, omega], dtype=np.float64)
+    np.savez_compressed(HERE / f"run_{name}.npz", meta=meta, solver=np.array(solver),
+                        iters=stats[:, 2].astype(np.int64), err=stats[:, 3], cd=stats[:, 4],
+                        cl=stats[:, 5], **fields)
+
+
+def main():
+    for n, s in UNIT_GRIDS.items():
+        make_unit(n, s)
+        print("unit", n)
+    for n, s in RUNS.items():
+        make_run(n, s)
+        print("run", n)
+
+
+if __name__ == "__main__":
+    main()

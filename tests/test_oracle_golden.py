@@ -1,0 +1,117 @@
+"""Pins the C restatement (oracle/cfd_oracle.c) to golden vectors produced by the
+reference's own functions (tests/golden/make_golden.py).  The bar is bit-exact: both are
+compiled with -ffp-contract=off and the reference ran at one OpenMP thread."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+UNITS = ["unit_g10x8x6_h025.npz", "unit_g10x8x6_h030.npz"]
+
+
+def _grid(meta):
+    nxc, nyc, nzc = (int(x) for x in meta[:3])
+    lx, ly, lz, cx = meta[3:7]
+    return O.Grid(nxc, nyc, nzc, lx, ly, lz, cx)
+
+
+@pytest.fixture(params=UNITS)
+def unit(request, golden):
+    z = golden(request.param)
+    g = _grid(z["meta"])
+    sh = g.shape
+    padded = {k: v.reshape(sh) for k, v in z.items()
+              if v.size == g.shape[0] * g.shape[1] * g.shape[2]}
+    return z, g, padded
+
+
+def test_convection_diffusion_bit_exact(unit):
+    z, g, P = unit
+    Re, dt = z["meta"][7], z["meta"][8]
+    us, vs, ws = P["in_us"].copy(), P["in_vs"].copy(), P["in_ws"].copy()
+    O.convection_diffusion(g, dt, 1.0 / Re, P["in_u"], P["in_v"], P["in_w"], us, vs, ws)
+    np.testing.assert_array_equal(us, P["cd_u"])
+    np.testing.assert_array_equal(vs, P["cd_v"])
+    np.testing.assert_array_equal(ws, P["cd_w"])
+
+
+def test_bc_main_and_copy_bit_exact(unit):
+    z, g, P = unit
+    u, v, w, p = (P[k].copy() for k in ("in_u", "in_v", "in_w", "in_p"))
+    O.bc_main(g, u, v, w, p)
+    for a, k in ((u, "bc_u"), (v, "bc_v"), (w, "bc_w"), (p, "bc_p")):
+        np.testing.assert_array_equal(a, P[k])
+    us, vs, ws = P["in_us"].copy(), P["in_vs"].copy(), P["in_ws"].copy()
+    O.bc_copy(g, u, v, w, us, vs, ws)
+    for a, k in ((us, "bcc_u"), (vs, "bcc_v"), (ws, "bcc_w")):
+        np.testing.assert_array_equal(a, P[k])
+
+
+def test_rhs_and_jacobi_bit_exact(unit):
+    z, g, P = unit
+    dt = z["meta"][8]
+    np.testing.assert_array_equal(O.rhs(g, dt, P["in_us"], P["in_vs"], P["in_ws"]), z["b_spe"])
+    jp = O.jacobi_scale(g)
+    np.testing.assert_array_equal(jp, z["jp"])
+    np.testing.assert_array_equal(O.rhs(g, dt, P["in_us"], P["in_vs"], P["in_ws"], jp), z["b_jac"])
+
+
+def test_operators_bit_exact(unit):
+    z, g, P = unit
+    np.testing.assert_array_equal(O.spe_multiply(g, z["in_x"]), z["y_spe"])
+    np.testing.assert_array_equal(O.csr_multiply(g, z["in_x"]), z["y_csr"])
+
+
+def test_update_uf_and_drag_bit_exact(unit):
+    z, g, P = unit
+    dt = z["meta"][8]
+    u3, v3, w3 = P["in_u3"].copy(), P["in_v3"].copy(), P["in_w3"].copy()
+    f = np.zeros(3 * g.shape[0] * g.shape[1] * g.shape[2])
+    O.update_uf(g, dt, P["in_eta"], P["in_p"], P["in_us"], P["in_vs"], P["in_ws"], u3, v3, w3, f)
+    np.testing.assert_array_equal(u3, P["uf_u"])
+    np.testing.assert_array_equal(v3, P["uf_v"])
+    np.testing.assert_array_equal(w3, P["uf_w"])
+    np.testing.assert_array_equal(f, z["uf_f"])
+    cd = -2.0 * O.force_sum(g, f, 0) / g._g.lz
+    cl = -2.0 * O.force_sum(g, f, 1) / g._g.lz
+    np.testing.assert_array_equal(np.array([cd, cl]), z["cdcl"])
+
+
+def test_solid_fraction_bit_exact(unit):
+    z, g, P = unit
+    eta = O.dfib_cylinder_z(g)
+    np.testing.assert_array_equal(eta, P["eta_cyl"])
+    assert 0 < eta.max() <= 1.0 and eta.min() == 0.0
+
+
+def test_bicgstab_bit_exact(unit):
+    z, g, P = unit
+    s = O.BiCGSTAB(g, 0, 1e-10)
+    x = np.zeros(g.cells)
+    it, err = s.solve(z["bicg_rhs"], x)
+    np.testing.assert_array_equal(x, z["bicg_x"])
+    assert (it, err) == (int(z["bicg_it"][0]), z["bicg_it"][1])
+
+
+def test_sor_bit_exact(unit):
+    z, g, P = unit
+    dt = z["meta"][8]
+    p = P["in_p"].copy()
+    it, err = O.sor(g, dt, 1.7, 1e-30, 7, P["in_us"], P["in_vs"], P["in_ws"], p)
+    np.testing.assert_array_equal(p, P["sor_p"])
+    assert (it, err) == (int(z["sor_it"][0]), z["sor_it"][1])
+
+
+@pytest.mark.parametrize("case", ["c1_spe_tol1e-13_20", "c1_csr_tol1e-13_20",
+                                  "c1_sor_tol1e-3_4", "c1_spe_tol1e-8_200"])
+def test_whole_run_bit_exact(case, golden):
+    z = golden(f"run_{case}.npz")
+    m = z["meta"]
+    g = _grid(m)
+    steps, Re, dt, tol, omega = int(m[7]), m[8], m[9], m[10], m[11]
+    r = O.run(g, steps, Re, dt, tol, str(z["solver"]), omega)
+    np.testing.assert_array_equal(r["iters"], z["iters"])
+    np.testing.assert_array_equal(r["cd"], z["cd"])
+    np.testing.assert_array_equal(r["cl"], z["cl"])
+    for k in ("u", "v", "w", "p"):
+        np.testing.assert_array_equal(r[k][2:-2, 2:-2, 2:-2], z[k])
