@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark of the projection time step (cell-steps/s at Poisson residual 1e-8).
+
+Workload (default "c2"): the 512x256x64 uniform MAC grid over [0,32]x[0,16]x[0,4],
+cylinder D=1 at (8,8), Re 200, dt 0.002, the reference's own boundary conditions and
+initial state (u=1, v=w=0), Jacobi-scaled BiCGSTAB to relative residual 1e-8, FP64.
+A step is one projection step (convection-diffusion, Poisson solve, correction + DFIB
+forcing + drag, ghost fill).  Inputs (~1.5 GB of fields and Krylov vectors) are far
+larger than the 129 MB L2, so no flush is needed between steps.
+
+One JSON line on rank 0.  value: FP64 cell-steps/s over exactly --steps steps after
+--warmup steps, CUDA events on the library's stream, max over ranks (replicas: the
+path does not shard).  Beside it: the FP32+FP64-refined mode and red-black SOR on the
+same workload, e2e through the C ABI with host buffers, per-kernel live timing for the
+roofline, the CPU baseline (the reference's own OpenMP build, bounded sample) and SM
+clocks sampled during the timed region.
+
+--impl reference times the reference's own CPU implementation (oracle/_ref, built
+from the reference sources) on the host cores for the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # configs[1]-shaped workload: plain FP64 on the GPU at scale
+    "c2": dict(nx=512, ny=256, nz=64, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0, Re=200.0, dt=0.002),
+    # the reference's CPU-runnable case
+    "c1": dict(nx=96, ny=48, nz=4, lx=24.0, ly=12.0, lz=1.0, cx=6.0, cy=6.0, Re=100.0, dt=0.005),
+    # mixed-precision scale case (67M cells)
+    "c3": dict(nx=1024, ny=512, nz=128, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0, Re=300.0, dt=0.001),
+}
+TOL = 1e-8
+FALLBACK_HBM_GBS = 6800.0
+
+# algorithmic bytes per interior cell and launch (one word per array read or written,
+# neighbours assumed cached), FP64 = 8 B, FP32 = 4 B
+KERNEL_WORDS = {
+    "bicg_ap": 3,   # read p1, r0; write ap
+    "bicg_s": 3,    # read r1, ap; write s
+    "bicg_as": 2,   # read s; write as
+    "bicg_xr": 7,   # read x, p1, s, as, r0; write x, r1
+    "bicg_p": 4,    # read r1, p1, ap; write p1
+}
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows if len(r) >= 9 for q in range(4)
+                          if r[5 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.world, self.rank, self.local = _dist()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as tdist
+            tdist.init_process_group("nccl" if os.environ.get("BENCH_GLOO") is None else "gloo")
+            self.pg = tdist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def _timed_steps(s, steps, dist, torch):
+    """Exactly `steps` steps between two CUDA events on the solver's stream."""
+    stream = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    stats = s.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    return e0.elapsed_time(e1), stats
+
+
+def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True):
+    cfg = dict(WORKLOADS[wl])
+    with cg.Solver(solver=solver, precision=precision, tol=TOL, maxit=maxit, **cfg) as s:
+        s.init_fields()
+        s.step(warmup, allow_noconv=True)
+        s.reset_counters()
+        ms, stats = _timed_steps(s, steps, dist, torch)
+        launches = s.launch_count()
+        out = {"ms": ms, "stats": stats, "launches": launches, "cells": s.cells}
+        if profile:
+            # live per-kernel durations: the same number of further steps with every
+            # kernel bracketed by CUDA events on the library's stream
+            s.reset_counters()
+            s.set_kernel_timing(True)
+            s.step(steps, allow_noconv=True)
+            s.set_kernel_timing(False)
+            out["kernels"] = s.kernel_stats()
+        return out
+
+
+def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
+    """The public API with HOST buffers: per step, H2D of u,v,w,p from pinned memory,
+    one step, D2H of u,v,w,p; all on the library's stream inside the events."""
+    cfg = dict(WORKLOADS[wl])
+    with cg.Solver(solver=solver, precision=precision, tol=TOL, **cfg) as s:
+        s.init_fields()
+        s.step(warmup)
+        host = {k: torch.empty(s.shape, dtype=torch.float64, pin_memory=True).numpy() for k in "uvwp"}
+        s.get_fields(host)
+        stream = torch.cuda.ExternalStream(s.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            s.set_fields(host["u"], host["v"], host["w"], host["p"])
+            s.step(1)
+            s.get_fields(host)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = e0.elapsed_time(e1)
+        nbytes = 4 * int(host["u"].nbytes)
+        return ms, nbytes, s.cells
+
+
+def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file):
+    ks = {k[: -len(suffix)]: v for k, v in prof.items() if k.endswith(suffix) and k[: -len(suffix)] in KERNEL_WORDS}
+    ks = {k: v for k, v in ks.items() if v[1] > 0 and v[0] > 0}
+    if not ks:
+        return None, {}
+    total = sum(v[0] for v in prof.values())
+    dom = max(ks, key=lambda k: ks[k][0])
+    ms, n = ks[dom]
+    per_launch_s = ms / n / 1e3
+    alg = KERNEL_WORDS[dom] * word_bytes * cells
+    achieved = alg / per_launch_s / 1e9
+    traffic = None
+    if traffic_file.exists():
+        t = json.loads(traffic_file.read_text())
+        traffic = t.get(dom + suffix, {}).get("bytes_per_launch")
+    share = {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
+    r = {"kernel": dom + suffix, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+         "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(per_launch_s * 1e6, 2),
+         "peak_kind": peak_kind}
+    return r, share
+
+
+def cpu_reference_sample(wl, steps, cap, threads, iters_per_step):
+    """Run the reference's own build (oracle/_ref) for `steps` steps with its BiCGSTAB
+    capped at `cap` iterations; derive its time per iteration and per non-solve step
+    part, and from those its cell-steps/s at the iteration counts a full solve to 1e-8
+    needs (iters_per_step: list, one per step)."""
+    from oracle import build_ref
+    cfg = WORKLOADS[wl]
+    exe = build_ref.build(cfg["nx"], cfg["ny"], cfg["nz"], cfg["lx"], cfg["ly"], cfg["lz"], cfg["cx"], "native")
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="close", OMP_PLACES="cores")
+        t0 = time.perf_counter()
+        subprocess.run([str(exe), "run", str(steps), repr(cfg["Re"]), repr(cfg["dt"]), repr(TOL), "csr", "1.7",
+                        "0", "0", td, str(cap)], check=True, env=env, cwd=td, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        wall = time.perf_counter() - t0
+        rows = [list(map(float, l.split())) for l in (Path(td) / "stats.txt").read_text().splitlines()
+                if l and not l.startswith("#")]
+    solve_rows = [r for r in rows if r[0] > 1 and r[2] > 0]
+    t_iter = sum(r[7] for r in solve_rows) / sum(r[2] for r in solve_rows)
+    t_other = statistics.median(r[6] - r[7] for r in solve_rows)
+    cells = cfg["nx"] * cfg["ny"] * cfg["nz"]
+    per_step = [t_other + it * t_iter for it in iters_per_step]
+    value = cells * len(per_step) / sum(per_step)
+    return {"value": value, "t_iter_s": t_iter, "t_other_s": t_other, "wall_s": wall, "cells": cells}
+
+
+def reference_iteration_record(wl):
+    f = ROOT / "tests" / "golden" / f"reference_iters_{wl}.json"
+    if f.exists():
+        return json.loads(f.read_text())
+    return None
+
+
+def main_reference(args):
+    """--impl reference: the reference's own CPU implementation, host cores."""
+    world, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    rec = reference_iteration_record(args.workload)
+    threads = os.cpu_count() or 1
+    steps = args.warmup + args.steps
+    if rec is None:
+        iters = None
+    else:
+        its = rec["iters"]
+        mean = sum(its) / len(its)
+        iters = [its[i] if i < len(its) else mean for i in range(args.warmup + 1, steps + 1)][-args.steps:]
+    if iters is None:
+        print(json.dumps({"impl": "reference", "unavailable": "no recorded reference iteration counts"}))
+        return 0
+    r = cpu_reference_sample(args.workload, min(steps, 3), args.cap, threads, iters)
+    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "cell-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * r["cells"] / r["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state)",
+            "config": {"workload": args.workload, **WORKLOADS[args.workload], "solver": "jacobi_bicgstab",
+                       "tol": TOL},
+            "cpu_baseline": {"value": r["value"], "unit": "cell-steps/s", "cores": threads, "kind": "reference",
+                             "sample": SAMPLE_DOC.format(cap=args.cap, t_iter=r["t_iter_s"], t_other=r["t_other_s"])},
+            "e2e": {"value": r["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+METRIC = "cell-steps/s @resid 1e-8 (FP64 Jacobi-BiCGSTAB projection step)"
+SAMPLE_DOC = ("reference OpenMP build (-O3 -fopenmp -march=native) on the same grid, steps 1-3 with its "
+              "BiCGSTAB capped at {cap} iterations: {t_iter:.4f} s per iteration, {t_other:.3f} s per step "
+              "outside the solve; cell-steps/s at the iteration counts the reference itself needs to reach "
+              "1e-8 on these steps (recorded from full reference runs, tests/golden/reference_iters_<wl>.json)")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="projection-step benchmark")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cfdgb", choices=["cfdgb", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--modes", default="fp64,mixed,rbsor,e2e,cpu")
+    ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
+    ap.add_argument("--sor-steps", type=int, default=2)
+    ap.add_argument("--sor-maxit", type=int, default=20000)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return main_reference(args)
+
+    import torch
+    import cfd_nssolver_forhpc_flowpassingcylinder_gb300 as cg
+    dist = Dist()
+    torch.cuda.set_device(dist.local)
+    modes = set(args.modes.split(","))
+    hbm_peak, peak_kind = peaks()
+    wl = args.workload
+    traffic_file = ROOT / "profiles" / f"traffic_{wl}.json"
+
+    with Clocks(dist.local) as clk:
+        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64")
+    t64 = dist.max(fp64["ms"])
+    cells = fp64["cells"]
+    value = cells * args.steps * dist.world / (t64 / 1e3)
+    roof, share = roofline(fp64["kernels"], cells, 8, "64", hbm_peak, peak_kind, traffic_file)
+    iters64 = [r.iters for r in fp64["stats"]]
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t64 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state u=1, v=w=0)",
+        "config": {"workload": wl, **WORKLOADS[wl], "solver": "jacobi_bicgstab", "tol": TOL,
+                   "bc": "reference (FLOWpassing table)", "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs ~1.5 GB > 129 MB L2, no flush"},
+        "iters_per_step": iters64, "relres": max(r.relres for r in fp64["stats"]),
+        "gpu_launches": fp64["launches"], "roofline": roof, "kernel_share": share,
+        "clocks": clk.summary(),
+    }
+    if "mixed" in modes:
+        mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed")
+        tm = dist.max(mx["ms"])
+        r32, share32 = roofline(mx["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
+        line["mixed"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
+                         "iters_per_step": [r.iters for r in mx["stats"]],
+                         "outer_per_step": [r.outer for r in mx["stats"]],
+                         "relres": max(r.relres for r in mx["stats"]), "speedup_vs_fp64": t64 / tm,
+                         "gpu_launches": mx["launches"], "roofline": r32, "kernel_share": share32}
+    if "rbsor" in modes:
+        sr = run_mode(cg, torch, dist, wl, args.sor_steps, args.warmup, "rbsor", "fp64", maxit=args.sor_maxit,
+                      profile=False)
+        ts = dist.max(sr["ms"])
+        line["rbsor"] = {"value": cells * args.sor_steps * dist.world / (ts / 1e3), "steps": args.sor_steps,
+                         "omega": 1.7, "sweeps_per_step": [r.iters for r in sr["stats"]],
+                         "relres": [r.relres for r in sr["stats"]], "status": [r.status for r in sr["stats"]]}
+    if "e2e" in modes:
+        ms, nbytes, _ = e2e_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64")
+        te = dist.max(ms)
+        line["e2e"] = {"value": cells * args.steps * dist.world / (te / 1e3), "unit": "cell-steps/s",
+                       "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    if "cpu" in modes and dist.rank == 0:
+        rec = reference_iteration_record(wl)
+        try:
+            if rec is None:
+                raise RuntimeError("no recorded reference iteration counts")
+            its = rec["iters"]
+            mean = sum(its) / len(its)
+            want = [its[i] if i < len(its) else mean for i in range(args.warmup + 1, args.warmup + args.steps + 1)]
+            threads = os.cpu_count() or 1
+            cb = cpu_reference_sample(wl, 3, args.cap, threads, want)
+            line["cpu_baseline"] = {"value": cb["value"], "unit": "cell-steps/s", "cores": threads,
+                                    "kind": "reference",
+                                    "sample": SAMPLE_DOC.format(cap=args.cap, t_iter=cb["t_iter_s"],
+                                                                t_other=cb["t_other_s"])}
+        except Exception as e:  # reference binary or record unavailable on this host
+            line["cpu_baseline"] = {"value": None, "unit": "cell-steps/s", "cores": os.cpu_count(),
+                                    "kind": "reference", "sample": f"unavailable: {e}"}
+    if dist.rank == 0:
+        print(json.dumps(line))
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,919 @@
+// Host side of the C ABI (include/cfdgb.h): context set-up, the time-step driver and the
+// per-function entry points.  The driver enqueues everything on the context's stream;
+// the only host synchronisations are the Poisson solver's convergence polls (one per
+// chunk of iterations, each chunk a captured CUDA graph) and the per-step read-back of
+// the step scalars (iterations, residual, drag, lift).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cfdgb_internal.cuh"
+#include "kernels.h"
+
+using namespace cfdgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(e_ == cudaErrorMemoryAllocation ? CFDGB_ENOMEM : CFDGB_ECUDA, "%s: %s (%s:%d)", #call, \
+                  cudaGetErrorString(e_), __FILE__, __LINE__);                                \
+  } while (0)
+
+#define TRY(expr)            \
+  do {                       \
+    int rc_ = (expr);        \
+    if (rc_ < 0) return rc_; \
+  } while (0)
+
+uint64_t splitmix64(uint64_t &s) {
+  s += 0x9E3779B97F4A7C15ULL;
+  uint64_t z = s;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// Kernels the instrumentation tells apart (cfdgb_kernel_stat).
+enum KId {
+  K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_AP32, K_S32, K_AS32, K_XR32, K_P32,
+  K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA, K_COUNT
+};
+const char *const kKernelNames[K_COUNT] = {
+    "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
+    "bicg_p64", "bicg_ap32", "bicg_s32", "bicg_as32", "bicg_xr32", "bicg_p32", "residual64", "inner_setup32",
+    "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction"};
+
+struct PendingEv {
+  int id;
+  cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct cfdgb_ctx {
+  cfdgb_config cfg{};
+  int device = 0, nsm = 0, nblk = 0;
+  cudaStream_t stream = nullptr;
+  Geo g{};
+  long long npad = 0, ncell = 0;
+  // host grid (inc/grid/structureGrid.hpp:336-367)
+  std::vector<double> X, Y, Z, Dx, Dy, Dz, Dxs, Dys, Dzs;
+  Stencil<double> spe64{}, jac64{};
+  Stencil<float> spe32{}, jac32{};
+  // device buffers
+  double *metric = nullptr, *Xd = nullptr, *Yd = nullptr;
+  float *tab32 = nullptr;
+  double *u = nullptr, *v = nullptr, *w = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
+  double *ui = nullptr, *vi = nullptr, *wi = nullptr, *p = nullptr, *eta = nullptr;
+  double *b = nullptr, *x = nullptr, *px1 = nullptr, *px2 = nullptr, *r64 = nullptr;
+  KrylovVecs<double> k64{};
+  KrylovVecs<float> k32{};
+  double *part = nullptr;
+  SolverScal *sc = nullptr, *sc32 = nullptr;
+  StepScal *ss = nullptr;
+  // pinned host mirrors of the scalars
+  SolverScal *h_sc = nullptr;
+  StepScal *h_ss = nullptr;
+  // chunk graphs of solver iterations
+  cudaGraphExec_t chunk64 = nullptr, chunk32 = nullptr;
+  int chunk_len = 16;
+  // scratch for the per-function entry points (allocated on first use)
+  double *op[10] = {nullptr};
+  double *opc[3] = {nullptr};
+  std::vector<void *> allocs;
+  int loop = 0;  // steps taken since the last init_fields
+  bool have_fields = false;
+  // instrumentation
+  long long launches = 0;
+  bool timing = false;
+  double kms[K_COUNT] = {0};
+  long long kn[K_COUNT] = {0};
+  std::vector<cudaEvent_t> ev_free;
+  std::vector<PendingEv> ev_pending;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(cfdgb_ctx *c, T **p, size_t n) {
+  void *q = nullptr;
+  CK(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+  c->allocs.push_back(q);
+  *p = (T *)q;
+  return 0;
+}
+
+// Resolve recorded event pairs (the stream must have passed them).
+void resolve_events(cfdgb_ctx *c) {
+  for (auto &e : c->ev_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) c->kms[e.id] += ms;
+    c->ev_free.push_back(e.a);
+    c->ev_free.push_back(e.b);
+  }
+  c->ev_pending.clear();
+}
+
+// Every kernel launch of the driver goes through here: counts launches and, with timing
+// on, brackets the launch with a CUDA-event pair on the context's stream.
+template <class F>
+void L(cfdgb_ctx *c, int id, int nkernels, F &&launch) {
+  c->launches += nkernels;
+  c->kn[id] += nkernels;
+  if (!c->timing) {
+    launch();
+    return;
+  }
+  if (c->ev_free.size() < 2) {
+    if (c->ev_pending.size() >= 2048) {
+      cudaStreamSynchronize(c->stream);
+      resolve_events(c);
+    }
+    for (int q = 0; q < 64; ++q) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) == cudaSuccess) c->ev_free.push_back(e);
+    }
+  }
+  PendingEv pe{id, c->ev_free.back(), nullptr};
+  c->ev_free.pop_back();
+  pe.b = c->ev_free.back();
+  c->ev_free.pop_back();
+  cudaEventRecord(pe.a, c->stream);
+  launch();
+  cudaEventRecord(pe.b, c->stream);
+  c->ev_pending.push_back(pe);
+}
+
+// Reference coefficient helpers (structureGrid.hpp:560-566, SPE_sparseMatrix.hpp:93-99),
+// compact index a.
+struct Coef {
+  const cfdgb_ctx *c;
+  double xp(int i) const { return 1.0 / c->Dx[i + 2] / c->Dxs[i + 2]; }
+  double yp(int j) const { return 1.0 / c->Dy[j + 2] / c->Dys[j + 2]; }
+  double zp(int k) const { return 1.0 / c->Dz[k + 2] / c->Dzs[k + 2]; }
+  double xm(int i) const { return 1.0 / c->Dx[i + 2] / c->Dxs[i + 1]; }
+  double ym(int j) const { return 1.0 / c->Dy[j + 2] / c->Dys[j + 1]; }
+  double zm(int k) const { return 1.0 / c->Dz[k + 2] / c->Dzs[k + 1]; }
+};
+
+// 27 boundary classes: a representative compact index per class along each axis.
+int class_rep(int cls, int n) { return cls == 0 ? 0 : (cls == 2 ? n - 1 : 1); }
+
+void build_stencils(cfdgb_ctx *c) {
+  const Coef C{c};
+  const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+  for (int bx = 0; bx < 3; ++bx)
+    for (int by = 0; by < 3; ++by)
+      for (int bz = 0; bz < 3; ++bz) {
+        const int cls = bx * 9 + by * 3 + bz;
+        const int i = class_rep(bx, nx), j = class_rep(by, ny), k = class_rep(bz, nz);
+        // SPE values, SPE_sparseMatrix.hpp:101-126 (y coefficients swapped as there)
+        double ijk = C.xm(i) + C.ym(j) + C.zm(k) + C.xp(i) + C.yp(j) + C.zp(k);
+        if (i == 0) ijk -= C.xm(i);
+        if (i == nx - 1) ijk -= C.xp(i);
+        if (j == 0) ijk -= C.ym(j);
+        if (j == ny - 1) ijk -= C.yp(j);
+        if (k == 0) ijk -= C.zm(k);
+        if (k == nz - 1) ijk -= C.zp(k);
+        double *s = c->spe64.c[cls];
+        s[0] = i != 0 ? -C.xm(i) : 0.0;
+        s[1] = j != 0 ? -C.yp(j) : 0.0;
+        s[2] = k != 0 ? -C.zm(k) : 0.0;
+        s[3] = ijk;
+        s[4] = k != nz - 1 ? -C.zp(k) : 0.0;
+        s[5] = j != ny - 1 ? -C.ym(j) : 0.0;
+        s[6] = i != nx - 1 ? -C.xp(i) : 0.0;
+        // CSR rows scaled by jp, structureGrid.hpp:583-645
+        double aa = 0.0, bb = 0.0, cc = 0.0;
+        if (i == 0) aa = -C.xm(i);
+        if (i == nx - 1) aa = -C.xp(i);
+        if (j == 0) bb = -C.ym(j);
+        if (j == ny - 1) bb = -C.yp(j);
+        if (k == 0) cc = -C.zm(k);
+        if (k == nz - 1) cc = -C.zp(k);
+        const double dj = C.xm(i) + C.ym(j) + C.zm(k) + C.xp(i) + C.yp(j) + C.zp(k) + aa + bb + cc;
+        const double jp = 1.0 / dj;
+        double *q = c->jac64.c[cls];
+        q[0] = i != 0 ? -C.xm(i) * jp : 0.0;
+        q[1] = j != 0 ? -C.ym(j) * jp : 0.0;
+        q[2] = k != 0 ? -C.zm(k) * jp : 0.0;
+        q[3] = dj * jp;
+        q[4] = k != nz - 1 ? -C.zp(k) * jp : 0.0;
+        q[5] = j != ny - 1 ? -C.yp(j) * jp : 0.0;
+        q[6] = i != nx - 1 ? -C.xp(i) * jp : 0.0;
+        q[7] = jp;
+        s[7] = 1.0 / ijk;
+        for (int e = 0; e < 8; ++e) {
+          c->spe32.c[cls][e] = (float)s[e];
+          c->jac32.c[cls][e] = (float)q[e];
+        }
+      }
+}
+
+// FP32 per-axis tables for step_fast.cu (rows: 1/D, 1/Ds, interpolation factor, QUICK
+// coefficients of QuickUnitA and QuickUnitB for both upwind directions).
+std::vector<float> build_tab32(const cfdgb_ctx *c, int L) {
+  std::vector<float> t(3 * 11 * (size_t)L, 0.0f);
+  const std::vector<double> *D[3] = {&c->Dx, &c->Dy, &c->Dz}, *S[3] = {&c->Dxs, &c->Dys, &c->Dzs};
+  for (int a = 0; a < 3; ++a) {
+    const auto &d = *D[a], &s = *S[a];
+    const int n = (int)d.size();
+    auto at = [&](const std::vector<double> &v, int I) { return v[std::min(std::max(I, 0), n - 1)]; };
+    for (int I = 0; I < n; ++I) {
+      float *r = t.data() + (size_t)a * 11 * L;
+      r[0 * L + I] = (float)(1.0 / d[I]);
+      r[1 * L + I] = (float)(1.0 / s[I]);
+      r[2 * L + I] = (float)((s[I] * 0.5) / d[I]);
+      r[3 * L + I] = (float)(0.125 * at(d, I + 1) * at(d, I + 1) / s[I]);
+      r[4 * L + I] = (float)(0.125 * at(d, I + 1) * at(d, I + 1) / at(s, I + 1));
+      r[5 * L + I] = (float)(0.125 * d[I] * d[I] / at(s, I - 1));
+      r[6 * L + I] = (float)(0.125 * d[I] * d[I] / s[I]);
+      r[7 * L + I] = (float)(0.125 * s[I] * s[I] / d[I]);
+      r[8 * L + I] = (float)(0.125 * s[I] * s[I] / at(d, I + 1));
+      r[9 * L + I] = (float)(0.125 * at(s, I - 1) * at(s, I - 1) / at(d, I - 1));
+      r[10 * L + I] = (float)(0.125 * at(s, I - 1) * at(s, I - 1) / d[I]);
+    }
+  }
+  return t;
+}
+
+int validate(const cfdgb_config *c) {
+  if (!c) return fail(CFDGB_EINVAL, "null config");
+  if (c->nx < 3 || c->ny < 3 || c->nz < 3) return fail(CFDGB_EINVAL, "grid must be at least 3x3x3 interior cells");
+  const double cells = (double)(c->nx + 4) * (c->ny + 4) * (c->nz + 4);
+  if (cells > 4.0e9) return fail(CFDGB_EINVAL, "padded grid above 4e9 cells");
+  if (!(c->lx > 0 && c->ly > 0 && c->lz > 0)) return fail(CFDGB_EINVAL, "domain lengths must be positive");
+  if (!(c->Re > 0) || !(c->dt > 0)) return fail(CFDGB_EINVAL, "Re and dt must be positive");
+  if (c->solver < 0 || c->solver > 2) return fail(CFDGB_EINVAL, "unknown solver %d", c->solver);
+  if (c->precision < 0 || c->precision > 1) return fail(CFDGB_EINVAL, "unknown precision %d", c->precision);
+  if (!(c->tol > 0)) return fail(CFDGB_EINVAL, "tol must be positive");
+  if (c->maxit < 1) return fail(CFDGB_EINVAL, "maxit must be >= 1");
+  if (c->solver == CFDGB_RBSOR && !(c->omega > 0 && c->omega < 2)) return fail(CFDGB_EINVAL, "omega outside (0,2)");
+  if (c->precision == CFDGB_MIXED && c->solver == CFDGB_RBSOR)
+    return fail(CFDGB_EINVAL, "MIXED precision is implemented for the BiCGSTAB solvers");
+  if (c->precision == CFDGB_MIXED && !(c->inner_tol > 0 && c->inner_tol < 1))
+    return fail(CFDGB_EINVAL, "inner_tol outside (0,1)");
+  if (c->dfib && !(c->radius > 0)) return fail(CFDGB_EINVAL, "radius must be positive");
+  return 0;
+}
+
+int capture_chunk(cfdgb_ctx *c, bool fp32) {
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int m = 0; m < c->chunk_len; ++m) {
+    if (fp32)
+      launch_bicg_iter<float>(c->stream, c->nblk, c->g, c->cfg.solver == CFDGB_BICGSTAB_JACOBI ? c->jac32 : c->spe32,
+                              c->k32, c->part, c->sc32);
+    else
+      launch_bicg_iter<double>(c->stream, c->nblk, c->g, c->cfg.solver == CFDGB_BICGSTAB_JACOBI ? c->jac64 : c->spe64,
+                               c->k64, c->part, c->sc);
+  }
+  CK(cudaStreamEndCapture(c->stream, &graph));
+  cudaGraphExec_t exec;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  (fp32 ? c->chunk32 : c->chunk64) = exec;
+  return 0;
+}
+
+// Set the solve parameters in the device scalars (read by the set-up kernels' successors).
+int set_solver_params(cfdgb_ctx *c, SolverScal *dsc, double tol, int maxit) {
+  // tol, restart_thr, maxit live at fixed offsets; write them with small async copies
+  struct {
+    double tol, thr;
+  } t{tol, tol * 1e-7};  // bicgstabRe2.hpp:53 (pRestartFactor_)
+  CK(cudaMemcpyAsync(&dsc->tol, &t, sizeof(t), cudaMemcpyHostToDevice, c->stream));
+  // restart_thr follows tol in SolverScal
+  static_assert(offsetof(SolverScal, restart_thr) == offsetof(SolverScal, tol) + sizeof(double), "layout");
+  CK(cudaMemcpyAsync(&dsc->maxit, &maxit, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  return 0;
+}
+
+// Iterate chunks until the device says done.  Returns the scalars in *out.  Each chunk
+// is a captured graph of chunk_len iterations; with kernel timing on, the same kernels
+// are launched one by one between event pairs instead.
+int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
+  SolverScal *dsc = fp32 ? c->sc32 : c->sc;
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  if (!c->timing && !(fp32 ? c->chunk32 : c->chunk64)) TRY(capture_chunk(c, fp32));
+  const long long max_chunks = (long long)c->cfg.maxit / c->chunk_len + 3;
+  for (long long q = 0; q < max_chunks; ++q) {
+    if (c->timing) {
+      for (int m = 0; m < c->chunk_len; ++m)
+        for (int part = 0; part < 5; ++part) {
+          if (fp32)
+            L(c, K_AP32 + part, 1, [&] {
+              launch_bicg_part<float>(c->stream, part, c->nblk, c->g, jac ? c->jac32 : c->spe32, c->k32, c->part, c->sc32);
+            });
+          else
+            L(c, K_AP64 + part, 1, [&] {
+              launch_bicg_part<double>(c->stream, part, c->nblk, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
+            });
+        }
+    } else {
+      const int first = fp32 ? K_AP32 : K_AP64;
+      c->launches += 5LL * c->chunk_len;
+      for (int part = 0; part < 5; ++part) c->kn[first + part] += c->chunk_len;
+      CK(cudaGraphLaunch(fp32 ? c->chunk32 : c->chunk64, c->stream));
+    }
+    CK(cudaMemcpyAsync(c->h_sc, dsc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    resolve_events(c);
+    if (c->h_sc->done) {
+      *out = *c->h_sc;
+      return 0;
+    }
+  }
+  return fail(CFDGB_ECUDA, "solver did not report completion");
+}
+
+// createBMatrix + solve + (caller) transform, on the current u*.  Fills iters/relres.
+int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *status) {
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
+  L(c, K_RHS, 1, [&] { launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, jac, c->jac64, c->b); });
+  *iters = 0;
+  *outer = 0;
+  *status = 0;
+  if (c->cfg.solver == CFDGB_RBSOR) {
+    L(c, K_RNORM, 1, [&] { launch_vec_norm64(c->stream, c->nblk, c->g, c->b, c->part, c->ss); });
+    int sweeps = 0;
+    for (;;) {
+      L(c, K_RNORM, 1, [&] { launch_residual_norm64(c->stream, c->nblk, c->g, c->spe64, c->b, c->x, c->part, c->ss); });
+      CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      *relres = c->h_ss->relres;
+      if (c->h_ss->relres < c->cfg.tol) break;
+      if (sweeps >= c->cfg.maxit || !std::isfinite(c->h_ss->relres)) {
+        *status = std::isfinite(c->h_ss->relres) ? CFDGB_ENOCONV : CFDGB_ENAN;
+        break;
+      }
+      for (int q = 0; q < c->cfg.check_every; ++q)
+        L(c, K_RBSOR, 2, [&] { launch_rbsor_sweep(c->stream, c->nblk, c->g, c->spe64, c->b, c->x, c->cfg.omega); });
+      sweeps += c->cfg.check_every;
+    }
+    *iters = sweeps;
+    return 0;
+  }
+  if (c->cfg.precision == CFDGB_FP64) {
+    TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
+    L(c, K_SETUP64, 1, [&] { launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc); });
+    SolverScal r;
+    TRY(run_chunks(c, false, &r));
+    if (r.status == CFDGB_ENOCONV)
+      L(c, K_NANRESET, 2, [&] { launch_bicg_nan_reset(c->stream, c->nblk, c->g, c->x, c->px1, c->px2, c->part, c->sc); });
+    *iters = r.iter;
+    *relres = r.relres;
+    *status = r.status;
+    return 0;
+  }
+  // MIXED: FP64 defect correction around FP32 BiCGSTAB on the unit-scaled residual.
+  // Each inner solve is asked for the reduction that finishes the job with a 5x margin,
+  // but not below inner_tol (the FP32 floor).
+  static const bool trace = std::getenv("CFDGB_TRACE") != nullptr;
+  for (int o = 0;; ++o) {
+    L(c, K_RESID64, 1, [&] { launch_residual64(c->stream, c->nblk, c->g, st64, c->b, c->x, c->r64, c->part, c->ss, c->sc32, o == 0); });
+    CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const double rel = c->h_ss->relres;
+    *relres = rel;
+    if (trace) std::fprintf(stderr, "[cfdgb] step %d outer %d relres %.3e\n", c->loop, o, rel);
+    if (!std::isfinite(rel)) { *status = CFDGB_ENAN; break; }
+    if (rel < c->cfg.tol) break;
+    if (o >= c->cfg.max_outer) { *status = CFDGB_ENOCONV; break; }
+    const double itol = std::min(0.5, std::max(c->cfg.inner_tol, 0.2 * c->cfg.tol / rel));
+    TRY(set_solver_params(c, c->sc32, itol, c->cfg.maxit));
+    L(c, K_SETUP32, 1, [&] { launch_inner_setup32(c->stream, c->nblk, c->g, c->k32, c->r64, c->part, c->sc32); });
+    SolverScal r;
+    TRY(run_chunks(c, true, &r));
+    if (trace)
+      std::fprintf(stderr, "[cfdgb]   inner tol %.1e iters %d status %d relres %.3e\n", itol, r.iter, r.status, r.relres);
+    *iters += r.iter + 1;
+    *outer = o + 1;
+    if (!std::isfinite(r.relres)) { *status = CFDGB_ENAN; break; }  // never apply a broken correction
+    L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, c->sc32); });
+  }
+  return 0;
+}
+
+int apply_init_bc(cfdgb_ctx *c) {
+  // src/RUN_CPU.cpp:104-109: T1 = T3 = T0, then the first ghost fill and copy
+  const size_t bytes = c->npad * sizeof(double);
+  CK(cudaMemcpyAsync(c->ui, c->u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->vi, c->v, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->wi, c->w, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->us, c->u, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->vs, c->v, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->ws, c->w, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1);
+  CK(cudaMemsetAsync(c->x, 0, c->ncell * sizeof(double), c->stream));  // X_result = 0
+  CK(cudaMemsetAsync(c->px1, 0, c->ncell * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->px2, 0, c->ncell * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->sc, 0, sizeof(SolverScal), c->stream));
+  CK(cudaMemsetAsync(c->sc32, 0, sizeof(SolverScal), c->stream));
+  CK(cudaGetLastError());
+  c->loop = 0;
+  c->have_fields = true;
+  return 0;
+}
+
+int ensure_op_buffers(cfdgb_ctx *c) {
+  if (c->op[0]) return 0;
+  for (int q = 0; q < 7; ++q) TRY(dalloc(c, &c->op[q], c->npad));
+  TRY(dalloc(c, &c->op[7], 3 * c->npad));
+  TRY(dalloc(c, &c->op[8], c->npad));
+  for (int q = 0; q < 3; ++q) TRY(dalloc(c, &c->opc[q], c->ncell));
+  return 0;
+}
+
+int h2d(cfdgb_ctx *c, double *d, const double *h, size_t n) {
+  CK(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return 0;
+}
+int d2h(cfdgb_ctx *c, double *h, const double *d, size_t n) {
+  CK(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return 0;
+}
+int sync(cfdgb_ctx *c) {
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfdgb_abi_version(void) { return CFDGB_ABI_VERSION; }
+const char *cfdgb_last_error(void) { return g_last_error.c_str(); }
+
+int cfdgb_config_default(cfdgb_config *c) {
+  if (!c) return fail(CFDGB_EINVAL, "null config");
+  std::memset(c, 0, sizeof(*c));
+  c->nx = 96; c->ny = 48; c->nz = 4;
+  c->lx = 24.0; c->ly = 12.0; c->lz = 1.0;
+  c->cx = 6.0; c->cy = 6.0; c->radius = 0.5;
+  c->Re = 100.0; c->dt = 0.005;
+  c->solver = CFDGB_BICGSTAB;
+  c->precision = CFDGB_FP64;
+  c->tol = 1e-8;
+  c->maxit = 5000;
+  c->omega = 1.7;
+  c->inner_tol = 1e-4;
+  c->max_outer = 20;
+  c->check_every = 10;
+  c->dfib = 1;
+  c->seed = 0;
+  c->amp = 0.0;
+  return 0;
+}
+
+int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
+  if (!out) return fail(CFDGB_EINVAL, "null output pointer");
+  *out = nullptr;
+  TRY(validate(cfg));
+  cfdgb_ctx *c = new cfdgb_ctx();
+  c->cfg = *cfg;
+  auto bail = [&](int rc) { cfdgb_destroy(c); return rc; };
+  if (cudaGetDevice(&c->device) != cudaSuccess) return bail(fail(CFDGB_ECUDA, "no CUDA device"));
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) return bail(fail(CFDGB_ECUDA, "device query"));
+  c->nsm = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(CFDGB_ECUDA, "stream create"));
+  // grid (structureGrid.hpp:336-367): uniform, X[0] = -2 dx, running sums
+  const int nx = cfg->nx + 4, ny = cfg->ny + 4, nz = cfg->nz + 4;
+  auto axis = [](std::vector<double> &Xa, std::vector<double> &D, std::vector<double> &Ds, int n, double l) {
+    const double d = l / (n - 2.0 * 2);
+    Xa.assign(n + 1, 0.0);
+    Xa[0] = 0.0 - 2.0 * d;
+    for (int q = 1; q < n + 1; ++q) Xa[q] = Xa[q - 1] + d;
+    D.assign(n, d);
+    Ds.assign(n, d);
+  };
+  axis(c->X, c->Dx, c->Dxs, nx, cfg->lx);
+  axis(c->Y, c->Dy, c->Dys, ny, cfg->ly);
+  axis(c->Z, c->Dz, c->Dzs, nz, cfg->lz);
+  c->npad = (long long)nx * ny * nz;
+  c->ncell = (long long)cfg->nx * cfg->ny * cfg->nz;
+  build_stencils(c);
+  // reduction grid: a fixed number of resident blocks
+  c->nblk = (int)std::min<long long>((c->ncell + kBlock - 1) / kBlock, (long long)c->nsm * 8);
+  c->chunk_len = c->ncell > (1LL << 22) ? 8 : 32;
+  int rc = 0;
+  const int nmet = nx + ny + nz;
+  if ((rc = dalloc(c, &c->metric, 2 * (size_t)nmet))) return bail(rc);
+  std::vector<double> met;
+  for (auto *v : {&c->Dx, &c->Dy, &c->Dz, &c->Dxs, &c->Dys, &c->Dzs}) met.insert(met.end(), v->begin(), v->end());
+  if (cudaMemcpy(c->metric, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(CFDGB_ECUDA, "metric upload"));
+  if ((rc = dalloc(c, &c->Xd, nx + 1)) || (rc = dalloc(c, &c->Yd, ny + 1))) return bail(rc);
+  cudaMemcpy(c->Xd, c->X.data(), (nx + 1) * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->Yd, c->Y.data(), (ny + 1) * sizeof(double), cudaMemcpyHostToDevice);
+  const int L = std::max(nx, std::max(ny, nz)) + 1;
+  std::vector<float> tab = build_tab32(c, L);
+  if ((rc = dalloc(c, &c->tab32, tab.size()))) return bail(rc);
+  cudaMemcpy(c->tab32, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
+  Geo &g = c->g;
+  g.nxc = cfg->nx; g.nyc = cfg->ny; g.nzc = cfg->nz;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.sx = (long long)ny * nz; g.sy = nz;
+  g.ncell = c->ncell;
+  g.Dx = c->metric; g.Dy = g.Dx + nx; g.Dz = g.Dy + ny;
+  g.Dxs = g.Dz + nz; g.Dys = g.Dxs + nx; g.Dzs = g.Dys + ny;
+  // fields and solver vectors
+  double **pad[] = {&c->u, &c->v, &c->w, &c->us, &c->vs, &c->ws, &c->ui, &c->vi, &c->wi, &c->p, &c->eta};
+  for (auto **q : pad)
+    if ((rc = dalloc(c, q, c->npad))) return bail(rc);
+  double **cmp[] = {&c->b, &c->x, &c->px1, &c->px2};
+  for (auto **q : cmp)
+    if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
+  c->k64.x = c->x;
+  if (cfg->precision == CFDGB_FP64 && cfg->solver != CFDGB_RBSOR) {
+    double **kv[] = {&c->k64.r0, &c->k64.r1, &c->k64.p1, &c->k64.s, &c->k64.ap, &c->k64.as};
+    for (auto **q : kv)
+      if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
+  }
+  if (cfg->precision == CFDGB_MIXED) {
+    if ((rc = dalloc(c, &c->r64, c->ncell))) return bail(rc);
+    float **kv[] = {&c->k32.x, &c->k32.r0, &c->k32.r1, &c->k32.p1, &c->k32.s, &c->k32.ap, &c->k32.as};
+    for (auto **q : kv)
+      if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
+  }
+  if ((rc = dalloc(c, &c->part, 8 * (size_t)c->nblk))) return bail(rc);
+  if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc32, 1)) || (rc = dalloc(c, &c->ss, 1))) return bail(rc);
+  cudaMemset(c->sc, 0, sizeof(SolverScal));
+  cudaMemset(c->sc32, 0, sizeof(SolverScal));
+  cudaMemset(c->ss, 0, sizeof(StepScal));
+  if (cudaMallocHost(&c->h_sc, sizeof(SolverScal)) != cudaSuccess ||
+      cudaMallocHost(&c->h_ss, sizeof(StepScal)) != cudaSuccess)
+    return bail(fail(CFDGB_ENOMEM, "pinned scalars"));
+  // solid fraction (DFIB_CylinderZ, RUN_CPU.cpp:228-234)
+  cudaMemsetAsync(c->eta, 0, c->npad * sizeof(double), c->stream);
+  if (cfg->dfib) launch_eta(c->stream, c->nblk, c->g, c->Xd, c->Yd, cfg->cx, cfg->cy, cfg->radius, c->eta);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(CFDGB_ECUDA, "set-up kernels: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = c;
+  return 0;
+}
+
+int cfdgb_destroy(cfdgb_ctx *c) {
+  if (!c) return 0;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  resolve_events(c);
+  for (auto e : c->ev_free) cudaEventDestroy(e);
+  if (c->chunk64) cudaGraphExecDestroy(c->chunk64);
+  if (c->chunk32) cudaGraphExecDestroy(c->chunk32);
+  for (void *q : c->allocs) cudaFree(q);
+  if (c->h_sc) cudaFreeHost(c->h_sc);
+  if (c->h_ss) cudaFreeHost(c->h_ss);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return 0;
+}
+
+int cfdgb_padded_dims(const cfdgb_ctx *c, int *nxp, int *nyp, int *nzp) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (nxp) *nxp = c->g.nx;
+  if (nyp) *nyp = c->g.ny;
+  if (nzp) *nzp = c->g.nz;
+  return 0;
+}
+
+int cfdgb_stream(const cfdgb_ctx *c, void **s) {
+  if (!c || !s) return fail(CFDGB_EINVAL, "null argument");
+  *s = (void *)c->stream;
+  return 0;
+}
+
+int cfdgb_init_fields(cfdgb_ctx *c, const double *u, const double *v, const double *w, const double *p) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  const size_t n = c->npad;
+  std::vector<double> hu, hv, hw;
+  if (!u || !v || !w) {
+    // iniU(1, 0, 0) (RUN_CPU.cpp:66-76) plus the seeded perturbation of the interior
+    hu.assign(n, 1.0);
+    hv.assign(n, 0.0);
+    hw.assign(n, 0.0);
+    if (c->cfg.amp != 0.0) {
+      uint64_t s = c->cfg.seed;
+      std::vector<double> *f[3] = {&hu, &hv, &hw};
+      for (auto *fa : f)
+        for (int i = 2; i < c->g.nx - 2; ++i)
+          for (int j = 2; j < c->g.ny - 2; ++j)
+            for (int k = 2; k < c->g.nz - 2; ++k) {
+              const double r = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+              (*fa)[((size_t)i * c->g.ny + j) * c->g.nz + k] += c->cfg.amp * (2.0 * r - 1.0);
+            }
+    }
+    if (u) std::memcpy(hu.data(), u, n * sizeof(double));
+    if (v) std::memcpy(hv.data(), v, n * sizeof(double));
+    if (w) std::memcpy(hw.data(), w, n * sizeof(double));
+    u = hu.data(); v = hv.data(); w = hw.data();
+  }
+  TRY(h2d(c, c->u, u, n));
+  TRY(h2d(c, c->v, v, n));
+  TRY(h2d(c, c->w, w, n));
+  if (p) TRY(h2d(c, c->p, p, n));
+  else CK(cudaMemsetAsync(c->p, 0, n * sizeof(double), c->stream));
+  TRY(apply_init_bc(c));
+  return sync(c);
+}
+
+int cfdgb_set_fields(cfdgb_ctx *c, const double *u, const double *v, const double *w, const double *p) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!c->have_fields) return fail(CFDGB_ESTATE, "init_fields must come first");
+  const size_t n = c->npad;
+  if (u) TRY(h2d(c, c->u, u, n));
+  if (v) TRY(h2d(c, c->v, v, n));
+  if (w) TRY(h2d(c, c->w, w, n));
+  // p is the padded pressure (t1.p); the solver's warm start (X_result) is kept as is
+  if (p) TRY(h2d(c, c->p, p, n));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int cfdgb_get_fields(cfdgb_ctx *c, double *u, double *v, double *w, double *p) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  const size_t n = c->npad;
+  if (u) TRY(d2h(c, u, c->u, n));
+  if (v) TRY(d2h(c, v, c->v, n));
+  if (w) TRY(d2h(c, w, c->w, n));
+  if (p) TRY(d2h(c, p, c->p, n));
+  return sync(c);
+}
+
+int cfdgb_get_eta(cfdgb_ctx *c, double *eta) {
+  if (!c || !eta) return fail(CFDGB_EINVAL, "null argument");
+  TRY(d2h(c, eta, c->eta, c->npad));
+  return sync(c);
+}
+
+int cfdgb_set_eta(cfdgb_ctx *c, const double *eta) {
+  if (!c || !eta) return fail(CFDGB_EINVAL, "null argument");
+  TRY(h2d(c, c->eta, eta, c->npad));
+  return sync(c);
+}
+
+int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!c->have_fields) TRY(cfdgb_init_fields(c, nullptr, nullptr, nullptr, nullptr));
+  if (nsteps < 0) return fail(CFDGB_EINVAL, "negative step count");
+  const double nu = 1.0 / c->cfg.Re;  // 0_1_SimulationVariable.hpp:26-31
+  int worst = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    const int loop = ++c->loop;
+    // 1. u* (RUN_CPU.cpp:268)
+    L(c, K_CONVDIFF, 1, [&] {
+      if (c->cfg.precision == CFDGB_MIXED)
+        launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, c->u, c->v, c->w, c->us, c->vs, c->ws);
+      else
+        launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.dt, nu, c->u, c->v, c->w, c->us, c->vs, c->ws);
+    });
+    // 2. pressure, not at the first step (RUN_CPU.cpp:303)
+    int iters = 0, outer = 0, status = 0;
+    double relres = 0.0;
+    if (loop > 1) {
+      TRY(solve_pressure(c, &iters, &outer, &relres, &status));
+      L(c, K_TRANSFORM, 1, [&] { launch_transform(c->stream, c->nblk, c->g, c->x, c->p); });
+    }
+    // 3. correction + DFIB + drag, written straight into T0 (copyVel, RUN_CPU.cpp:369-391)
+    L(c, K_UPDATE, 1, [&] {
+      launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->cfg.lz, c->eta, c->p, c->us, c->vs, c->ws, c->u,
+                             c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part, c->ss);
+    });
+    // 4. ghost fill of T0 and p, copy into T1 (RUN_CPU.cpp:399-400)
+    L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1); });
+    CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    resolve_events(c);
+    if (c->h_ss->nan_flag && status == 0) status = CFDGB_ENAN;
+    if (stats) {
+      cfdgb_step_stats &st = stats[s];
+      st.step = loop;
+      st.iters = iters;
+      st.outer = outer;
+      st.status = status;
+      st.relres = relres;
+      st.cd = c->h_ss->cd;
+      st.cl = c->h_ss->cl;
+    }
+    if (status < worst) worst = status;
+  }
+  if (worst < 0) fail(worst, "step finished with status %d", worst);
+  return worst;
+}
+
+int cfdgb_pressure_solve(cfdgb_ctx *c, int *iters, double *relres) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!c->have_fields) return fail(CFDGB_ESTATE, "init_fields must come first");
+  int it = 0, outer = 0, status = 0;
+  double rr = 0.0;
+  TRY(solve_pressure(c, &it, &outer, &rr, &status));
+  launch_transform(c->stream, c->nblk, c->g, c->x, c->p);
+  TRY(sync(c));
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  return status;
+}
+
+int cfdgb_set_kernel_timing(cfdgb_ctx *c, int enable) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (c->timing) {
+    CK(cudaStreamSynchronize(c->stream));
+    resolve_events(c);
+  }
+  c->timing = enable != 0;
+  return 0;
+}
+
+int cfdgb_reset_counters(cfdgb_ctx *c) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  resolve_events(c);
+  c->launches = 0;
+  for (int q = 0; q < K_COUNT; ++q) { c->kms[q] = 0.0; c->kn[q] = 0; }
+  return 0;
+}
+
+int cfdgb_launch_count(const cfdgb_ctx *c, long long *launches) {
+  if (!c || !launches) return fail(CFDGB_EINVAL, "null argument");
+  *launches = c->launches;
+  return 0;
+}
+
+int cfdgb_kernel_stat(cfdgb_ctx *c, int idx, const char **name, double *total_ms, long long *launches) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (idx < 0 || idx >= K_COUNT) return fail(CFDGB_EINVAL, "kernel index out of range");
+  if (name) *name = kKernelNames[idx];
+  if (total_ms) *total_ms = c->kms[idx];
+  if (launches) *launches = c->kn[idx];
+  return 0;
+}
+
+// ---- per-function entry points ----
+
+int cfdgb_op_convection_diffusion(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *us,
+                                  double *vs, double *ws) {
+  if (!c || !u || !v || !w || !us || !vs || !ws) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n));
+  TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
+  if (c->cfg.precision == CFDGB_MIXED)
+    launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, 1.0 / c->cfg.Re, o[0], o[1], o[2], o[3], o[4], o[5]);
+  else
+    launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.dt, 1.0 / c->cfg.Re, o[0], o[1], o[2], o[3], o[4], o[5]);
+  TRY(d2h(c, us, o[3], n)); TRY(d2h(c, vs, o[4], n)); TRY(d2h(c, ws, o[5], n));
+  return sync(c);
+}
+
+int cfdgb_op_bc_main(cfdgb_ctx *c, double *u, double *v, double *w, double *p) {
+  if (!c || !u || !v || !w || !p) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n)); TRY(h2d(c, o[6], p, n));
+  launch_bc(c->stream, c->g, o[0], o[1], o[2], o[6], nullptr, nullptr, nullptr, 1);
+  TRY(d2h(c, u, o[0], n)); TRY(d2h(c, v, o[1], n)); TRY(d2h(c, w, o[2], n)); TRY(d2h(c, p, o[6], n));
+  return sync(c);
+}
+
+int cfdgb_op_bc_copy(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *us, double *vs,
+                     double *ws) {
+  if (!c || !u || !v || !w || !us || !vs || !ws) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n));
+  TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
+  launch_bc(c->stream, c->g, o[0], o[1], o[2], nullptr, o[3], o[4], o[5], 0);
+  TRY(d2h(c, us, o[3], n)); TRY(d2h(c, vs, o[4], n)); TRY(d2h(c, ws, o[5], n));
+  return sync(c);
+}
+
+int cfdgb_op_rhs(cfdgb_ctx *c, int jacobi, const double *us, const double *vs, const double *ws, double *b) {
+  if (!c || !us || !vs || !ws || !b) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
+  launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, o[3], o[4], o[5], jacobi != 0, c->jac64, c->opc[0]);
+  TRY(d2h(c, b, c->opc[0], c->ncell));
+  return sync(c);
+}
+
+int cfdgb_op_spmv(cfdgb_ctx *c, int jacobi, const double *x, double *y) {
+  if (!c || !x || !y) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  TRY(h2d(c, c->opc[0], x, c->ncell));
+  launch_spmv_exact(c->stream, c->nblk, c->g, jacobi ? c->jac64 : c->spe64, c->opc[0], c->opc[1]);
+  TRY(d2h(c, y, c->opc[1], c->ncell));
+  return sync(c);
+}
+
+int cfdgb_op_bicgstab(cfdgb_ctx *c, int solver, double tol, int maxit, const double *rhs, double *x, int *iters,
+                      double *relres) {
+  if (!c || !rhs || !x) return fail(CFDGB_EINVAL, "null argument");
+  if (solver != CFDGB_BICGSTAB && solver != CFDGB_BICGSTAB_JACOBI) return fail(CFDGB_EINVAL, "solver must be BiCGSTAB");
+  if (c->cfg.precision != CFDGB_FP64 || c->cfg.solver == CFDGB_RBSOR)
+    return fail(CFDGB_EINVAL, "op_bicgstab needs an FP64 BiCGSTAB context");
+  if (!(tol > 0) || maxit < 1) return fail(CFDGB_EINVAL, "bad tol/maxit");
+  // solve in the context's own Krylov buffers with the caller's rhs and warm start; the
+  // context's step state (x, history) is saved and restored around the call
+  std::vector<double> save_x(c->ncell), save_1(c->ncell), save_2(c->ncell);
+  TRY(d2h(c, save_x.data(), c->x, c->ncell));
+  TRY(d2h(c, save_1.data(), c->px1, c->ncell));
+  TRY(d2h(c, save_2.data(), c->px2, c->ncell));
+  SolverScal save_sc;
+  CK(cudaMemcpyAsync(&save_sc, c->sc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
+  TRY(sync(c));
+  TRY(h2d(c, c->b, rhs, c->ncell));
+  TRY(h2d(c, c->x, x, c->ncell));
+  CK(cudaMemsetAsync(c->sc, 0, sizeof(SolverScal), c->stream));  // a fresh solver object
+  const int keep_maxit = c->cfg.maxit;
+  c->cfg.maxit = maxit;
+  TRY(set_solver_params(c, c->sc, tol, maxit));
+  launch_bicg_setup64(c->stream, c->nblk, c->g, solver == CFDGB_BICGSTAB_JACOBI ? c->jac64 : c->spe64, c->k64, c->b,
+                      c->px1, c->px2, c->part, c->sc);
+  // the chunk graph bakes in the configured operator; use direct launches here
+  const Stencil<double> &st = solver == CFDGB_BICGSTAB_JACOBI ? c->jac64 : c->spe64;
+  SolverScal r{};
+  int rc = 0;
+  for (long long q = 0; q < (long long)maxit / 8 + 3; ++q) {
+    for (int m = 0; m < 8; ++m) launch_bicg_iter<double>(c->stream, c->nblk, c->g, st, c->k64, c->part, c->sc);
+    CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    if (c->h_sc->done) { r = *c->h_sc; break; }
+  }
+  c->cfg.maxit = keep_maxit;
+  if (r.status == CFDGB_ENOCONV) launch_bicg_nan_reset(c->stream, c->nblk, c->g, c->x, c->px1, c->px2, c->part, c->sc);
+  TRY(d2h(c, x, c->x, c->ncell));
+  TRY(sync(c));
+  if (iters) *iters = r.iter;
+  if (relres) *relres = r.relres;
+  rc = r.status;
+  TRY(h2d(c, c->x, save_x.data(), c->ncell));
+  TRY(h2d(c, c->px1, save_1.data(), c->ncell));
+  TRY(h2d(c, c->px2, save_2.data(), c->ncell));
+  CK(cudaMemcpyAsync(c->sc, &save_sc, sizeof(SolverScal), cudaMemcpyHostToDevice, c->stream));
+  TRY(sync(c));
+  if (rc < 0) fail(rc, "bicgstab hit its iteration cap");
+  return rc;
+}
+
+int cfdgb_op_update_uf(cfdgb_ctx *c, const double *eta, const double *p, const double *us, const double *vs,
+                       const double *ws, double *u3, double *v3, double *w3, double *f, double *cd, double *cl) {
+  if (!c || !eta || !p || !us || !vs || !ws || !u3 || !v3 || !w3) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[6], eta, n)); TRY(h2d(c, o[0], p, n));
+  TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
+  TRY(h2d(c, o[1], u3, n)); TRY(h2d(c, o[2], v3, n)); TRY(h2d(c, o[8], w3, n));
+  if (f) TRY(h2d(c, o[7], f, 3 * n));
+  launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->cfg.lz, o[6], o[0], o[3], o[4], o[5], o[1], o[2],
+                         o[8], f ? o[7] : nullptr, nullptr, nullptr, nullptr, c->part, c->ss);
+  TRY(d2h(c, u3, o[1], n)); TRY(d2h(c, v3, o[2], n)); TRY(d2h(c, w3, o[8], n));
+  if (f) TRY(d2h(c, f, o[7], 3 * n));
+  CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
+  TRY(sync(c));
+  if (cd) *cd = c->h_ss->cd;
+  if (cl) *cl = c->h_ss->cl;
+  return 0;
+}
+
+int cfdgb_op_solid_fraction(cfdgb_ctx *c, double *eta) {
+  if (!c || !eta) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  CK(cudaMemsetAsync(c->op[6], 0, c->npad * sizeof(double), c->stream));
+  launch_eta(c->stream, c->nblk, c->g, c->Xd, c->Yd, c->cfg.cx, c->cfg.cy, c->cfg.radius, c->op[6]);
+  TRY(d2h(c, eta, c->op[6], c->npad));
+  return sync(c);
+}
+
+}  // extern "C"

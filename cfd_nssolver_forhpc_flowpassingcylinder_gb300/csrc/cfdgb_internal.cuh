@@ -1,0 +1,103 @@
+// Internal types shared by the cfdgb translation units.
+//
+// Device data layout (all in HBM, one context = one grid):
+//   padded FP64 fields  (nx+4)(ny+4)(nz+4), k fastest: u,v,w (T0 = u^n), us,vs,ws
+//                       (T1 = u*), ui,vi,wi (initial T0, read only on the three
+//                       last-face planes), p, eta;
+//   compact Poisson vectors of nx*ny*nz (row = icelCal): b, x and the Krylov vectors,
+//   FP64 and (MIXED) FP32 copies;
+//   block partial sums [NV][nblk] for the deterministic two-stage reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cfdgb.h"
+
+namespace cfdgb {
+
+constexpr int kBlock = 256;  // threads per block of every grid-stride kernel
+
+// Geometry as the kernels see it.  Padded indices i,j,k run over [0, nx+4); interior
+// cells are [2, n+2).  Compact rows enumerate the interior with k fastest.
+struct Geo {
+  int nxc, nyc, nzc;    // interior cells
+  int nx, ny, nz;       // padded extents
+  long long sx, sy;     // padded strides: sx = ny*nz, sy = nz
+  long long ncell;      // nxc*nyc*nzc
+  const double *Dx, *Dy, *Dz, *Dxs, *Dys, *Dzs;  // metric arrays (padded lengths)
+};
+
+// compact row -> padded (i,j,k)
+__device__ __forceinline__ void row_ijk(const Geo &g, long long row, int &i, int &j, int &k) {
+  const long long nyz = (long long)g.nyc * g.nzc;
+  const int ic = (int)(row / nyz);
+  const long long rem = row - (long long)ic * nyz;
+  const int jc = (int)(rem / g.nzc);
+  k = (int)(rem - (long long)jc * g.nzc) + 2;
+  j = jc + 2;
+  i = ic + 2;
+}
+
+__device__ __forceinline__ long long pidx(const Geo &g, int i, int j, int k) {
+  return (long long)i * g.sx + (long long)j * g.sy + k;
+}
+
+// 7-point Neumann operator of the pressure Poisson problem, uniform grid.  A row's
+// coefficients depend only on whether the cell is first / inner / last along each axis
+// (27 classes).  c[cls][0..6] multiply x at -x,-y,-z,0,+z,+y,+x (the SPE column order,
+// inc/matrix/SPE_sparseMatrix.hpp:119-125); c[cls][7] = 1/diag of the unscaled operator.
+template <typename T>
+struct Stencil {
+  T c[27][8];
+};
+
+__device__ __forceinline__ int axis_class(int a, int n) { return a == 0 ? 0 : (a == n - 1 ? 2 : 1); }
+
+// y = (A x)[row] for compact row with compact coordinates (ic,jc,kc); bounds on the
+// coordinates, terms accumulated in SPE column order.
+template <typename T>
+__device__ __forceinline__ T stencil_row(const Stencil<T> &st, const T *__restrict__ x, long long row,
+                                         int ic, int jc, int kc, int nxc, int nyc, int nzc) {
+  const long long nyz = (long long)nyc * nzc;
+  const T *c = st.c[axis_class(ic, nxc) * 9 + axis_class(jc, nyc) * 3 + axis_class(kc, nzc)];
+  T sum = T(0);
+  if (ic > 0) sum += c[0] * x[row - nyz];
+  if (jc > 0) sum += c[1] * x[row - nzc];
+  if (kc > 0) sum += c[2] * x[row - 1];
+  sum += c[3] * x[row];
+  if (kc < nzc - 1) sum += c[4] * x[row + 1];
+  if (jc < nyc - 1) sum += c[5] * x[row + nzc];
+  if (ic < nxc - 1) sum += c[6] * x[row + nyz];
+  return sum;
+}
+
+__device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &ic, int &jc, int &kc) {
+  const long long nyz = (long long)nyc * nzc;
+  ic = (int)(row / nyz);
+  const long long rem = row - (long long)ic * nyz;
+  jc = (int)(rem / nzc);
+  kc = (int)(rem - (long long)jc * nzc);
+}
+
+// Device-resident scalars of one Krylov solve.  Written by the last block of a kernel,
+// read by the next kernel in stream order.
+struct SolverScal {
+  double rho, alpha, omega, beta, norm0, relres, tol, restart_thr;
+  double scale;              // MIXED: ||r|| of the outer residual the inner rhs is scaled by
+  int iter, maxit, done, status, timestep, restart, pad0, pad1;
+  unsigned cnt[8];           // last-block counters, one per kernel kind
+};
+
+// Per-step scalars (drag, lift, outer residual of the mixed solve)
+struct StepScal {
+  double cd, cl, fsum[2];
+  double bnorm, rnorm, relres;
+  int nan_flag, pad;
+  unsigned cnt[8];
+};
+
+// ---- launch helpers implemented in the .cu files ----
+struct Ctx;
+
+}  // namespace cfdgb

@@ -1,0 +1,65 @@
+// Kernel launchers shared between the translation units (all enqueue on stream s).
+#pragma once
+
+#include "cfdgb_internal.cuh"
+
+namespace cfdgb {
+
+// step_exact.cu (bit-exact FP64, reference operation order)
+void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u,
+                           const double *v, const double *w, double *us, double *vs, double *ws);
+void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
+                      const double *ws, int jacobi, const Stencil<double> &st, double *b);
+void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
+                       double *y);
+void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p);
+void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
+                            const double *p, const double *us, const double *vs, const double *ws, double *u3,
+                            double *v3, double *w3, double *f, const double *ui, const double *vi,
+                            const double *wi, double *part, StepScal *ss);
+void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
+               double *vs, double *ws, int do_main);
+void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
+                double R, double *eta);
+
+// step_fast.cu (MIXED: FP32 arithmetic on the FP64 state)
+void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
+                         const double *u, const double *v, const double *w, double *us, double *vs, double *ws);
+
+// solver.cu
+template <typename T>
+struct KrylovVecs {
+  T *x, *r0, *r1, *p1, *s, *ap, *as;
+};
+
+// FP64 BiCGSTAB (bicgstabRe2) set-up: r0 = b - A x, r1 = p1 = r0, history px2 <- px1 <- x
+void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st,
+                         KrylovVecs<double> v, const double *b, double *px1, double *px2, double *part,
+                         SolverScal *sc);
+// kernel `part` (0..4: ap, s, as, xr, p) of one iteration
+template <typename T>
+void launch_bicg_part(cudaStream_t s, int part, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v,
+                      double *part_buf, SolverScal *sc);
+// one iteration (five kernels, each a no-op once sc->done is set)
+template <typename T>
+void launch_bicg_iter(cudaStream_t s, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v,
+                      double *part, SolverScal *sc);
+// after the loop: NaN/Inf recovery of bicgstabRe2.hpp:133-153 when the cap was hit
+void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
+                           const double *px2, double *part, SolverScal *sc);
+
+// MIXED defect correction pieces
+void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first);
+void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, KrylovVecs<float> v, const double *r64,
+                          double *part, SolverScal *sc);
+void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, const SolverScal *sc);
+
+// red-black SOR on the same operator (FP64)
+void launch_rbsor_sweep(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+                        double *x, double omega);
+void launch_residual_norm64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+                            const double *x, double *part, StepScal *ss);
+void launch_vec_norm64(cudaStream_t s, int nblk, const Geo &g, const double *b, double *part, StepScal *ss);
+
+}  // namespace cfdgb

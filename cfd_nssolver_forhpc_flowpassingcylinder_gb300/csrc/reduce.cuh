@@ -1,0 +1,97 @@
+// Deterministic two-stage FP64 reductions for grid-stride kernels with a fixed grid.
+//
+// Stage 1: each block reduces its NV per-thread values (warp shuffles + shared memory)
+// and stores them to part[q * gridDim.x + blockIdx.x].  Stage 2: the last block to
+// finish (atomic ticket) sums the partials in a fixed order, so results do not depend
+// on block scheduling.  No block ever waits on another.
+#pragma once
+
+#include "cfdgb_internal.cuh"
+
+namespace cfdgb {
+
+template <int NV>
+__device__ __forceinline__ void warp_sum(double (&v)[NV]) {
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+}
+
+// Reduce v over the block; the result is valid in thread 0 only.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[NV][kBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  warp_sum<NV>(v);
+  __syncthreads();  // sh may still be read by a previous call
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q][wid] = v[q];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = lane < kBlock / 32 ? sh[q][lane] : 0.0;
+    warp_sum<NV>(v);
+  }
+}
+
+// Stage 1 + 2.  Returns true in every thread of the last block; out[] is then valid in
+// all of its threads.  *ticket is reset for the next launch.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, unsigned *ticket,
+                                         double (&out)[NV]) {
+  __shared__ bool last;
+  __shared__ double res[NV];
+  block_sum<NV>(v);
+  const int G = gridDim.x;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) part[q * G + blockIdx.x] = v[q];
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == (unsigned)(G - 1));
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double w[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < G; b += kBlock) s += __ldcg(part + q * G + b);
+    w[q] = s;
+  }
+  block_sum<NV>(w);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) res[q] = w[q];
+    *ticket = 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q] = res[q];
+  return true;
+}
+
+// FP32 products summed in short FP32 runs, each run added into an FP64 accumulator:
+// global sums stay FP64 while the per-element work stays FP32.
+struct AccF {
+  double d = 0.0;
+  float f = 0.0f;
+  int n = 0;
+  __device__ __forceinline__ void add(float x) {
+    f += x;
+    if (++n == 8) { d += (double)f; f = 0.0f; n = 0; }
+  }
+  __device__ __forceinline__ double get() const { return d + (double)f; }
+};
+struct AccD {
+  double d = 0.0;
+  __device__ __forceinline__ void add(double x) { d += x; }
+  __device__ __forceinline__ double get() const { return d; }
+};
+template <typename T> struct AccFor;
+template <> struct AccFor<double> { using type = AccD; };
+template <> struct AccFor<float> { using type = AccF; };
+
+}  // namespace cfdgb

@@ -1,0 +1,433 @@
+// FP64 projection-step kernels that reproduce the reference's arithmetic exactly.
+//
+// This translation unit is compiled with -fmad=false and IEEE division, so every
+// kernel performs the reference function's operations in the same order and rounding:
+// the results are bit-identical to the reference (checked against its golden vectors).
+// One thread per interior cell (grid-stride over compact rows, k fastest, so a warp
+// reads contiguous k runs of each padded array).
+#include "cfdgb_internal.cuh"
+#include "reduce.cuh"
+#include "kernels.h"
+
+namespace cfdgb {
+
+// inc/source/Convection_Difussion.hpp:20-51 (QuickUnitA)
+__device__ __forceinline__ void quick_a(double Up, double Un, long long pp, long long p, long long ic,
+                                        long long n, long long nn, const double *__restrict__ Di,
+                                        const double *__restrict__ Ds, int I,
+                                        const double *__restrict__ phi, double &P, double &N) {
+  const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  if (Up > 0.0)
+    P = 0.5 * (fc + fp) - 0.125 * Di[I + 1] * Di[I + 1] / Ds[I] * ((fp - fc) / Di[I + 1] - (fc - fn) / Di[I]);
+  else
+    P = 0.5 * (fc + fp) -
+        0.125 * Di[I + 1] * Di[I + 1] / Ds[I + 1] * ((phi[pp] - fp) / Di[I + 2] - (fp - fc) / Di[I + 1]);
+  if (Un > 0.0)
+    N = 0.5 * (fn + fc) -
+        0.125 * Di[I] * Di[I] / Ds[I - 1] * ((fc - fn) / Di[I] - (fn - phi[nn]) / Di[I - 1]);
+  else
+    N = 0.5 * (fn + fc) - 0.125 * Di[I] * Di[I] / Ds[I] * ((fp - fc) / Di[I + 1] - (fc - fn) / Di[I]);
+}
+
+// inc/source/Convection_Difussion.hpp:55-90 (QuickUnitB)
+__device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long long p, long long ic,
+                                        long long n, long long nn, const double *__restrict__ Di,
+                                        const double *__restrict__ Ds, int I,
+                                        const double *__restrict__ phi, double &P, double &N) {
+  const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  if (Up > 0.0)
+    P = 0.5 * (fc + fp) - 0.125 * Ds[I] * Ds[I] / Di[I] * ((fp - fc) / Ds[I] - (fc - fn) / Ds[I - 1]);
+  else
+    P = 0.5 * (fc + fp) -
+        0.125 * Ds[I] * Ds[I] / Di[I + 1] * ((phi[pp] - fp) / Ds[I + 1] - (fp - fc) / Ds[I]);
+  if (Un > 0.0)
+    N = 0.5 * (fn + fc) -
+        0.125 * Ds[I - 1] * Ds[I - 1] / Di[I - 1] * ((fc - fn) / Ds[I - 1] - (fn - phi[nn]) / Ds[I - 2]);
+  else
+    N = 0.5 * (fn + fc) - 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I] * ((fp - fc) / Ds[I] - (fc - fn) / Ds[I - 1]);
+}
+
+// inc/source/Convection_Difussion.hpp:174-450: explicit Euler QUICK convection + central
+// diffusion; the last face along a component's own axis is a boundary face and skipped.
+__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, double nu,
+                                                           const double *__restrict__ u,
+                                                           const double *__restrict__ v,
+                                                           const double *__restrict__ w,
+                                                           double *__restrict__ us,
+                                                           double *__restrict__ vs,
+                                                           double *__restrict__ ws) {
+  const long long sx = g.sx, sy = g.sy, sz = 1;
+  const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    const long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz, zp = ic + sz;
+    if (i < g.nx - 3) {  // u
+      const double IT = (Dxs[i] * 0.5) / Dx[i];
+      const double uc = u[ic], uxp = u[xp], uxm = u[xm];
+      const double Up = 0.5 * (uxp + uc);
+      const double Un = 0.5 * (uxm + uc);
+      const double Vp = v[ic] + (v[xp] - v[ic]) * IT;
+      const double Vn = v[ym] + (v[ym + xp - ic] - v[ym]) * IT;
+      const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
+      const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
+      double uPx, uNx, uPy, uNy, uPz, uNz;
+      quick_a(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, u, uPx, uNx);
+      quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, u, uPy, uNy);
+      quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, u, uPz, uNz);
+      const double convection = -dt * ((uPx * uPx - uNx * uNx) / Dxs[i] + (uPy * Vp - uNy * Vn) / Dy[j] +
+                                       (uPz * Wp - uNz * Wn) / Dz[k]);
+      const double difussion =
+          nu * dt *
+          (((uxp - uc) / Dx[i + 1] - (uc - uxm) / Dx[i]) / Dxs[i] +
+           ((u[yp] - uc) / Dys[j] - (uc - u[ym]) / Dys[j - 1]) / Dy[j] +
+           ((u[zp] - uc) / Dzs[k] - (uc - u[zm]) / Dzs[k - 1]) / Dz[k]);
+      us[ic] = uc + convection + difussion;
+    }
+    if (j < g.ny - 3) {  // v
+      const double IT = (Dys[j] * 0.5) / Dy[j];
+      const double vc = v[ic], vyp = v[yp], vym = v[ym];
+      const double Vp = 0.5 * (vyp + vc);
+      const double Vn = 0.5 * (vym + vc);
+      const double Up = u[ic] + (u[yp] - u[ic]) * IT;
+      const double Un = u[xm] + (u[xm + yp - ic] - u[xm]) * IT;
+      const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
+      const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
+      double vPx, vNx, vPy, vNy, vPz, vNz;
+      quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, v, vPx, vNx);
+      quick_a(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, v, vPy, vNy);
+      quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, v, vPz, vNz);
+      const double convection = -dt * ((Up * vPx - Un * vNx) / Dx[i] + (vPy * vPy - vNy * vNy) / Dys[j] +
+                                       (Wp * vPz - Wn * vNz) / Dz[k]);
+      const double difussion =
+          nu * dt *
+          (((v[xp] - vc) / Dxs[i] - (vc - v[xm]) / Dxs[i - 1]) / Dx[i] +
+           ((vyp - vc) / Dy[j + 1] - (vc - vym) / Dy[j]) / Dys[j] +
+           ((v[zp] - vc) / Dzs[k] - (vc - v[zm]) / Dzs[k - 1]) / Dz[k]);
+      vs[ic] = vc + convection + difussion;
+    }
+    if (k < g.nz - 3) {  // w
+      const double IT = (Dzs[k] * 0.5) / Dz[k];
+      const double wc = w[ic], wzp = w[zp], wzm = w[zm];
+      const double Wp = 0.5 * (wzp + wc);
+      const double Wn = 0.5 * (wzm + wc);
+      const double Up = u[ic] + (u[zp] - u[ic]) * IT;
+      const double Un = u[xm] + (u[xm + zp - ic] - u[xm]) * IT;
+      const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
+      const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
+      double wPx, wNx, wPy, wNy, wPz, wNz;
+      quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, w, wPx, wNx);
+      quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, w, wPy, wNy);
+      quick_a(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, w, wPz, wNz);
+      const double convection = -dt * ((Up * wPx - Un * wNx) / Dx[i] + (Vp * wPy - Vn * wNy) / Dy[j] +
+                                       (wPz * wPz - wNz * wNz) / Dzs[k]);
+      const double difussion =
+          nu * dt *
+          (((w[xp] - wc) / Dxs[i] - (wc - w[xm]) / Dxs[i - 1]) / Dx[i] +
+           ((w[yp] - wc) / Dys[j] - (wc - w[ym]) / Dys[j - 1]) / Dy[j] +
+           ((wzp - wc) / Dz[k + 1] - (wc - wzm) / Dz[k]) / Dzs[k]);
+      ws[ic] = wc + convection + difussion;
+    }
+  }
+}
+
+// inc/matrix/b_matrix.hpp:35-98: b = -(jp)(1/dt) div(u*), one-sided differences
+__global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt, const double *__restrict__ us,
+                                                      const double *__restrict__ vs,
+                                                      const double *__restrict__ ws, int jacobi,
+                                                      Stencil<double> st, double *__restrict__ b) {
+  const double ddt = 1.0 / dt;
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    const double div = (us[ic] - us[ic - g.sx]) / g.Dx[i] + (vs[ic] - vs[ic - g.sy]) / g.Dy[j] +
+                       (ws[ic] - ws[ic - 1]) / g.Dz[k];
+    if (jacobi) {
+      const int cls = axis_class(i - 2, g.nxc) * 9 + axis_class(j - 2, g.nyc) * 3 + axis_class(k - 2, g.nzc);
+      b[row] = -st.c[cls][7] * ddt * div;
+    } else {
+      b[row] = -ddt * div;
+    }
+  }
+}
+
+// SPE_matrix::multiply_omp / CSR_matrix::multiply_omp with the reference's entry values
+__global__ void __launch_bounds__(kBlock) k_spmv_exact(Geo g, Stencil<double> st, const double *__restrict__ x,
+                                                       double *__restrict__ y) {
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int ic, jc, kc;
+    row_cijk(row, g.nyc, g.nzc, ic, jc, kc);
+    y[row] = stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
+  }
+}
+
+// inc/pressure/Transform.hpp:8-20
+__global__ void __launch_bounds__(kBlock) k_transform(Geo g, const double *__restrict__ x, double *__restrict__ p) {
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    p[pidx(g, i, j, k)] = x[row];
+  }
+}
+
+// inc/dfib/updateUandF.hpp:90-180 (solid velocity 0), fused with the drag/lift sums of
+// virtualF_Int (inc/dfib/virtualForceIntergrator.hpp:67-90) and, in the time step, with
+// the part of copyVel (inc/source/copyVel.hpp:4) that matters: the faces update_UandF
+// never writes keep the initial values (ui, vi, wi) they hold in the reference's T3.
+__global__ void __launch_bounds__(kBlock) k_update_uf_exact(
+    Geo g, double dt, double lz, const double *__restrict__ eta, const double *__restrict__ p,
+    const double *__restrict__ us, const double *__restrict__ vs, const double *__restrict__ ws,
+    double *__restrict__ u3, double *__restrict__ v3, double *__restrict__ w3, double *__restrict__ f,
+    const double *__restrict__ ui, const double *__restrict__ vi, const double *__restrict__ wi,
+    double *part, StepScal *ss) {
+  const long long tot = (long long)g.nx * g.ny * g.nz;
+  const double uS = 0.0, vS = 0.0, wS = 0.0;
+  double acc[2] = {0.0, 0.0};
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    const double vol = g.Dx[i] * g.Dy[j] * g.Dz[k];
+    const double ec = eta[ic];
+    if (i < g.nx - 3) {
+      const long long icP = ic + g.sx;
+      const double T2u = us[ic] - dt * (p[icP] - p[ic]) / g.Dxs[i];
+      const double e = ec + (eta[icP] - ec) * ((g.Dxs[i] * 0.5) / g.Dx[i]);
+      const double nu3 = ec * uS + (1.0 - e) * T2u;
+      const double fx = (nu3 - T2u) / dt;
+      u3[ic] = nu3;
+      if (f) f[ic] = fx;
+      acc[0] += fx * vol;
+    } else if (ui) {
+      u3[ic] = ui[ic];
+    }
+    if (j < g.ny - 3) {
+      const long long icP = ic + g.sy;
+      const double T2v = vs[ic] - dt * (p[icP] - p[ic]) / g.Dys[j];
+      const double e = ec + (eta[icP] - ec) * ((g.Dys[j] * 0.5) / g.Dy[j]);
+      const double nv3 = ec * vS + (1.0 - e) * T2v;
+      const double fy = (nv3 - T2v) / dt;
+      v3[ic] = nv3;
+      if (f) f[ic + tot] = fy;
+      acc[1] += fy * vol;
+    } else if (vi) {
+      v3[ic] = vi[ic];
+    }
+    if (k < g.nz - 3) {
+      const long long icP = ic + 1;
+      const double T2w = ws[ic] - dt * (p[icP] - p[ic]) / g.Dzs[k];
+      const double e = ec + (eta[icP] - ec) * ((g.Dzs[k] * 0.5) / g.Dz[k]);
+      const double nw3 = ec * wS + (1.0 - e) * T2w;
+      w3[ic] = nw3;
+      if (f) f[ic + 2 * tot] = (nw3 - T2w) / dt;
+    } else if (wi) {
+      w3[ic] = wi[ic];
+    }
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &ss->cnt[0], out) && threadIdx.x == 0) {
+    ss->fsum[0] = out[0];
+    ss->fsum[1] = out[1];
+    ss->cd = -2.0 * out[0] / lz;  // CD_CL, virtualForceIntergrator.hpp:309-314
+    ss->cl = -2.0 * out[1] / lz;
+    ss->nan_flag = !(isfinite(out[0]) && isfinite(out[1]));
+  }
+}
+
+// ---- ghost fill: BC_staggered_main (Boundary_Condition.hpp:37-176) in three phases that
+// keep its one-thread order (x faces, then y, then z; each later phase reads cells the
+// earlier ones wrote), each fused with the matching part of BC_staggered_copy
+// (updateBC.hpp:6-108), whose cells no later phase touches.  bc: Dir/Num table
+// (FLOWpassing.hpp:6-40) as bc[face][comp] = {Dir, Num}.
+
+struct BcTable {
+  double dir[6][3], num[6][3];
+};
+
+__global__ void __launch_bounds__(kBlock) k_bc_x(Geo g, BcTable t, double *u, double *v, double *w, double *p,
+                                                 double *us, double *vs, double *ws, int do_main) {
+  const int nyc = g.nyc, nzc = g.nzc, nx = g.nx;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nyc * nzc; q += gridDim.x * kBlock) {
+    const int j = q / nzc + 2, k = q % nzc + 2;
+    auto I = [&](int i) { return pidx(g, i, j, k); };
+    if (do_main) {
+      u[I(1)] = u[I(0)] = t.dir[0][0] + t.num[0][0] * u[I(2)];
+      v[I(1)] = v[I(0)] = t.dir[0][1] * 2. + (2.0 * t.num[0][1] - 1.0) * v[I(2)];
+      w[I(1)] = w[I(0)] = t.dir[0][2] * 2. + (2.0 * t.num[0][2] - 1.0) * w[I(2)];
+      u[I(nx - 1)] = u[I(nx - 2)] = u[I(nx - 3)] = t.dir[1][0] + t.num[1][0] * u[I(nx - 4)];
+      v[I(nx - 1)] = v[I(nx - 2)] = t.dir[1][1] * 2. + (2.0 * t.num[1][1] - 1.0) * v[I(nx - 3)];
+      w[I(nx - 1)] = w[I(nx - 2)] = t.dir[1][2] * 2. + (2.0 * t.num[1][2] - 1.0) * w[I(nx - 3)];
+      if (p) {
+        p[I(1)] = p[I(0)] = p[I(2)];
+        p[I(nx - 2)] = p[I(nx - 1)] = p[I(nx - 3)];
+      }
+    }
+    if (us) {
+      const int iu[5] = {0, 1, nx - 1, nx - 3, nx - 2};
+#pragma unroll
+      for (int a = 0; a < 5; ++a) us[I(iu[a])] = u[I(iu[a])];
+      const int iv[4] = {0, 1, nx - 2, nx - 1};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { vs[I(iv[a])] = v[I(iv[a])]; ws[I(iv[a])] = w[I(iv[a])]; }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bc_y(Geo g, BcTable t, double *u, double *v, double *w, double *p,
+                                                 double *us, double *vs, double *ws, int do_main) {
+  const int nxc = g.nxc, nzc = g.nzc, ny = g.ny;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nzc; q += gridDim.x * kBlock) {
+    const int i = q / nzc + 2, k = q % nzc + 2;
+    auto J = [&](int j) { return pidx(g, i, j, k); };
+    if (do_main) {
+      u[J(1)] = u[J(0)] = t.dir[2][0] * 2. + (2.0 * t.num[2][0] - 1.0) * u[J(2)];
+      v[J(1)] = v[J(0)] = t.dir[2][1] + t.num[2][1] * v[J(2)];
+      w[J(1)] = w[J(0)] = t.dir[2][2] * 2. + (2.0 * t.num[2][2] - 1.0) * w[J(2)];
+      v[J(ny - 1)] = v[J(ny - 2)] = v[J(ny - 3)] = t.dir[3][1] + t.num[3][1] * v[J(ny - 4)];
+      u[J(ny - 1)] = u[J(ny - 2)] = t.dir[3][0] * 2. + (2.0 * t.num[3][0] - 1.0) * u[J(ny - 3)];
+      w[J(ny - 1)] = w[J(ny - 2)] = t.dir[3][2] * 2. + (2.0 * t.num[3][2] - 1.0) * w[J(ny - 3)];
+      if (p) {
+        p[J(1)] = p[J(0)] = p[J(2)];
+        p[J(ny - 2)] = p[J(ny - 1)] = p[J(ny - 3)];
+      }
+    }
+    if (us) {
+      const int ju[4] = {0, 1, ny - 2, ny - 1};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { us[J(ju[a])] = u[J(ju[a])]; ws[J(ju[a])] = w[J(ju[a])]; }
+      const int jv[5] = {0, 1, ny - 3, ny - 2, ny - 1};
+#pragma unroll
+      for (int a = 0; a < 5; ++a) vs[J(jv[a])] = v[J(jv[a])];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bc_z(Geo g, BcTable t, double *u, double *v, double *w, double *p,
+                                                 double *us, double *vs, double *ws, int do_main) {
+  const int nxc = g.nxc, nyc = g.nyc, nz = g.nz;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nyc; q += gridDim.x * kBlock) {
+    const int i = q / nyc + 2, j = q % nyc + 2;
+    const long long base = pidx(g, i, j, 0);
+    if (do_main) {
+      u[base + 1] = u[base + 0] = t.dir[4][0] * 2. + (2.0 * t.num[4][0] - 1.0) * u[base + 2];
+      v[base + 1] = v[base + 0] = t.dir[4][1] * 2. + (2.0 * t.num[4][1] - 1.0) * v[base + 2];
+      w[base + 1] = w[base + 0] = t.dir[4][2] + t.num[4][2] * w[base + 2];
+      w[base + nz - 1] = w[base + nz - 2] = w[base + nz - 3] = t.dir[5][2] + t.num[5][2] * w[base + nz - 4];
+      u[base + nz - 1] = u[base + nz - 2] = t.dir[5][0] * 2. + (2.0 * t.num[5][0] - 1.0) * u[base + nz - 3];
+      v[base + nz - 1] = v[base + nz - 2] = t.dir[5][1] * 2. + (2.0 * t.num[5][1] - 1.0) * v[base + nz - 3];
+      if (p) {
+        p[base + 1] = p[base + 0] = p[base + 2];
+        p[base + nz - 2] = p[base + nz - 1] = p[base + nz - 3];
+      }
+    }
+    if (us) {
+      const int ku[4] = {0, 1, nz - 2, nz - 1};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { us[base + ku[a]] = u[base + ku[a]]; vs[base + ku[a]] = v[base + ku[a]]; }
+      const int kw[5] = {0, 1, nz - 3, nz - 2, nz - 1};
+#pragma unroll
+      for (int a = 0; a < 5; ++a) ws[base + kw[a]] = w[base + kw[a]];
+    }
+  }
+}
+
+// inc/dfib/setEta.hpp:136-198: per (i,j) column, solid fraction at k = 0 by 100x100
+// sub-sampling of cells within half a cell diagonal of the circle.
+__global__ void __launch_bounds__(kBlock) k_eta_plane(Geo g, const double *__restrict__ X,
+                                                      const double *__restrict__ Y, double cx, double cy,
+                                                      double R, double *__restrict__ eta) {
+  const int nxc = g.nxc, nyc = g.nyc;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nyc; q += gridDim.x * kBlock) {
+    const int i = q / nyc + 2, j = q % nyc + 2;
+    const long long icel = pidx(g, i, j, 0);
+    const double Diagonal = sqrt(g.Dx[i] * g.Dx[i] + g.Dy[j] * g.Dy[j]) * 0.5;
+    const double ddx = ((X[i] + X[i + 1]) * 0.5) - cx;
+    const double ddy = ((Y[j] + Y[j + 1]) * 0.5) - cy;
+    const double Distance = sqrt(ddx * ddx + ddy * ddy);
+    if (fabs(Distance - R) < Diagonal) {
+      const int nsub = 100;
+      const double dyg = g.Dy[j] / (double)nsub;
+      const double dxg = g.Dx[i] / (double)nsub;
+      long long xi = 0;
+      for (int ii = 0; ii < nsub; ++ii) {
+        const double sx0 = X[i] + (double)ii * dxg, sx1 = X[i] + (double)(ii + 1) * dxg;
+        const double a = (sx0 + sx1) * 0.5 - cx;
+        for (int jj = 0; jj < nsub; ++jj) {
+          const double sy0 = Y[j] + (double)jj * dyg, sy1 = Y[j] + (double)(jj + 1) * dyg;
+          const double b = (sy0 + sy1) * 0.5 - cy;
+          if (sqrt(a * a + b * b) <= R) ++xi;
+        }
+      }
+      eta[icel] = (double)xi * (1.0 / ((double)nsub * (double)nsub));
+    } else if (Distance > R) {
+      eta[icel] = 0.;
+    } else {
+      eta[icel] = 1.;
+    }
+  }
+}
+
+// setEta.hpp:200-203: copy plane k = 0 to k in [1, nz-1) for i < nx-1, j < ny-1
+__global__ void __launch_bounds__(kBlock) k_eta_extrude(Geo g, double *__restrict__ eta) {
+  const long long n = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 2);
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock) {
+    const int k = (int)(q % (g.nz - 2)) + 1;
+    const long long ij = q / (g.nz - 2);
+    const int j = (int)(ij % (g.ny - 1)), i = (int)(ij / (g.ny - 1));
+    eta[pidx(g, i, j, k)] = eta[pidx(g, i, j, 0)];
+  }
+}
+
+// ---- launchers ----
+void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u,
+                           const double *v, const double *w, double *us, double *vs, double *ws) {
+  k_convdiff_exact<<<nblk, kBlock, 0, s>>>(g, dt, nu, u, v, w, us, vs, ws);
+}
+void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
+                      const double *ws, int jacobi, const Stencil<double> &st, double *b) {
+  k_rhs_exact<<<nblk, kBlock, 0, s>>>(g, dt, us, vs, ws, jacobi, st, b);
+}
+void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
+                       double *y) {
+  k_spmv_exact<<<nblk, kBlock, 0, s>>>(g, st, x, y);
+}
+void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p) {
+  k_transform<<<nblk, kBlock, 0, s>>>(g, x, p);
+}
+void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
+                            const double *p, const double *us, const double *vs, const double *ws, double *u3,
+                            double *v3, double *w3, double *f, const double *ui, const double *vi,
+                            const double *wi, double *part, StepScal *ss) {
+  k_update_uf_exact<<<nblk, kBlock, 0, s>>>(g, dt, lz, eta, p, us, vs, ws, u3, v3, w3, f, ui, vi, wi, part, ss);
+}
+static BcTable flowpassing_table() {
+  // inc/BoundaryCondition/FLOWpassing.hpp:6-40
+  BcTable t{};
+  for (int f = 0; f < 6; ++f)
+    for (int c = 0; c < 3; ++c) { t.dir[f][c] = 0.0; t.num[f][c] = 1.0; }
+  t.dir[0][0] = 1.0;
+  t.num[0][0] = t.num[0][1] = t.num[0][2] = 0.0;
+  return t;
+}
+void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
+               double *vs, double *ws, int do_main) {
+  const BcTable t = flowpassing_table();
+  auto blocks = [](long long n) { return (int)((n + kBlock - 1) / kBlock < 1024 ? (n + kBlock - 1) / kBlock : 1024); };
+  k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
+  k_bc_y<<<blocks((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
+  k_bc_z<<<blocks((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
+}
+void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
+                double R, double *eta) {
+  k_eta_plane<<<nblk, kBlock, 0, s>>>(g, X, Y, cx, cy, R, eta);
+  k_eta_extrude<<<nblk, kBlock, 0, s>>>(g, eta);
+}
+
+}  // namespace cfdgb

@@ -1,0 +1,164 @@
+/* cfdgb -- GB300-native (sm_103a) projection time step for incompressible flow past a
+ * circular cylinder on a staggered MAC grid: QUICK convection-diffusion, direct-forcing
+ * immersed boundary (DFIB), pressure Poisson solve and velocity correction.
+ *
+ * Drop-in for the projection step of jimmy3769tw/CFD_NSsolver_forHPC_flowPassingCylinder.
+ * Each entry point names the reference interface it replaces (paths relative to that
+ * project's root).  Field arrays use the reference's padded layout: doubles of
+ * (nx+4)*(ny+4)*(nz+4), index i*(ny+4)*(nz+4) + j*(nz+4) + k, two ghost layers per side,
+ * u stored at face i+1/2, v at j+1/2, w at k+1/2 (inc/grid/structureGrid.hpp:154).
+ * Poisson vectors are compact interior arrays, index (i-2)*ny*nz + (j-2)*nz + (k-2)
+ * (structureGrid.hpp:178).
+ *
+ * Every function returns an int status (cfdgb_status).  Calls on one context are not
+ * thread-safe; each context owns one CUDA stream on the current device.  Host pointers
+ * are caller-owned and only read or written during the call. */
+#ifndef CFDGB_H
+#define CFDGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CFDGB_ABI_VERSION 1
+
+typedef enum cfdgb_status {
+  CFDGB_OK = 0,
+  CFDGB_EINVAL = -1,     /* bad argument or configuration */
+  CFDGB_ECUDA = -2,      /* CUDA runtime error (message via cfdgb_last_error) */
+  CFDGB_ENOCONV = -3,    /* Poisson solver hit its iteration cap (solution still written,
+                            as the reference does: bicgstabRe2.hpp:133-153) */
+  CFDGB_ENAN = -4,       /* NaN/Inf detected in the solution or the drag */
+  CFDGB_ENOMEM = -5,     /* device allocation failed */
+  CFDGB_ESTATE = -6      /* call out of order (e.g. step before fields exist) */
+} cfdgb_status;
+
+typedef enum cfdgb_solver {
+  CFDGB_BICGSTAB = 0,        /* SPE operator, unscaled (P_SOLVER_BICG_SPE, the default) */
+  CFDGB_BICGSTAB_JACOBI = 1, /* rows and rhs scaled by 1/diag (P_SOLVER_BICG_CSR) */
+  CFDGB_RBSOR = 2            /* red-black SOR on the same Neumann operator */
+} cfdgb_solver;
+
+typedef enum cfdgb_precision {
+  CFDGB_FP64 = 0,  /* every kernel in FP64 */
+  CFDGB_MIXED = 1  /* FP32 stencil sweep and inner BiCGSTAB inside FP64 defect
+                      correction; FP64 outer residual, global dots and divergence */
+} cfdgb_precision;
+
+typedef struct cfdgb_config {
+  int nx, ny, nz;            /* interior cells (nxCal, nyCal, nzCal) */
+  double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; uniform spacing */
+  double cx, cy, radius;     /* cylinder axis along z (DFIB_CylinderZ, setEta.hpp:136) */
+  double Re, dt;             /* nu = 1/Re (0_1_SimulationVariable.hpp:26) */
+  int solver;                /* cfdgb_solver */
+  int precision;             /* cfdgb_precision */
+  double tol;                /* relative residual ||b-Ax||/||b|| (p_criteria) */
+  int maxit;                 /* iteration cap (5000: bicgstabRe2.hpp:47) */
+  double omega;              /* SOR relaxation */
+  double inner_tol;          /* MIXED: relative tolerance of each FP32 inner solve */
+  int max_outer;             /* MIXED: cap on defect-correction sweeps */
+  int check_every;           /* SOR: residual checked every this many sweeps */
+  int dfib;                  /* 1: cylinder solid fraction on; 0: no immersed body */
+  uint64_t seed;             /* perturbation seed (splitmix64), used when amp != 0 */
+  double amp;                /* uniform(-amp, amp) added to interior u, v, w at init */
+} cfdgb_config;
+
+typedef struct cfdgb_step_stats {
+  int step;          /* 1-based step number (simu.loop) */
+  int iters;         /* Poisson iterations (inner iterations summed for MIXED) */
+  int outer;         /* MIXED: defect-correction sweeps; 0 otherwise */
+  int status;        /* cfdgb_status of this step's solve */
+  double relres;     /* final relative residual of the solve (FP64) */
+  double cd, cl;     /* drag and lift coefficients (CD_CL, virtualForceIntergrator.hpp:92) */
+} cfdgb_step_stats;
+
+/* Library identity and last error text (thread-local). */
+int cfdgb_abi_version(void);
+const char *cfdgb_last_error(void);
+
+/* Defaults: the reference's config-1 case (96x48x4, [0,24]x[0,12]x[0,1], cylinder at
+ * (6,6), Re 100, dt 0.005, SPE BiCGSTAB, tol 1e-8, 5000 iterations). */
+int cfdgb_config_default(cfdgb_config *cfg);
+
+/* Context: grid, metrics, operator, solid fraction and all device buffers.  Replaces the
+ * set-up half of runSeqOmp (src/RUN_CPU.cpp:9-255): resize_variable, generateGride
+ * (uniform), SPE_matrix::setupPressure / createPressureMatrixCSR, DFIB_CylinderZ. */
+typedef struct cfdgb_ctx cfdgb_ctx;
+int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out);
+int cfdgb_destroy(cfdgb_ctx *ctx);
+int cfdgb_padded_dims(const cfdgb_ctx *ctx, int *nxp, int *nyp, int *nzp);
+/* cudaStream_t of the context, as void* (for events / interop). */
+int cfdgb_stream(const cfdgb_ctx *ctx, void **stream);
+
+/* Initial condition (src/RUN_CPU.cpp:66-109): u,v,w,p become T0 (and the T1/T3 copies),
+ * then BC_staggered_main and BC_staggered_copy run and the step counter restarts at 1
+ * (so the next step, like loop 1, has no pressure solve).  NULL fields select the
+ * reference's iniU(1,0,0) / p=0, plus the configured perturbation. */
+int cfdgb_init_fields(cfdgb_ctx *ctx, const double *u, const double *v, const double *w,
+                      const double *p);
+/* Overwrite the current state (T0 and p after a step) without restarting the run. */
+int cfdgb_set_fields(cfdgb_ctx *ctx, const double *u, const double *v, const double *w,
+                     const double *p);
+/* Copy the current state out; NULL skips a field. */
+int cfdgb_get_fields(cfdgb_ctx *ctx, double *u, double *v, double *w, double *p);
+int cfdgb_get_eta(cfdgb_ctx *ctx, double *eta);
+int cfdgb_set_eta(cfdgb_ctx *ctx, const double *eta);
+
+/* nsteps projection steps (the loop body src/RUN_CPU.cpp:257-436).  stats: NULL or
+ * nsteps entries.  Returns the worst status over the steps. */
+int cfdgb_step(cfdgb_ctx *ctx, int nsteps, cfdgb_step_stats *stats);
+
+/* ---- instrumentation (no reference counterpart: the reference times phases with
+ * std::chrono stopwatches, inc/profiling/STL_clock.hpp:8) ---- */
+/* Kernel timing: while enabled, every kernel the step driver launches is bracketed by a
+ * CUDA-event pair on the context's stream (the solver's iteration graphs are replaced by
+ * direct launches of the same kernels). */
+int cfdgb_set_kernel_timing(cfdgb_ctx *ctx, int enable);
+int cfdgb_reset_counters(cfdgb_ctx *ctx);
+/* Kernels launched by the step driver since the last reset (graph nodes counted). */
+int cfdgb_launch_count(const cfdgb_ctx *ctx, long long *launches);
+/* idx in [0, n): kernel name, summed device milliseconds (timing on), launches; returns
+ * CFDGB_EINVAL past the last kernel. */
+int cfdgb_kernel_stat(cfdgb_ctx *ctx, int idx, const char **name, double *total_ms, long long *launches);
+
+/* ---- per-function entry points on host buffers (one kernel each; for drop-in use of a
+ * single reference function and for parity tests) ---- */
+
+/* ConvectionDifussion (inc/source/Convection_Difussion.hpp:174): reads u,v,w, writes
+ * the interior faces of us,vs,ws (other entries of us,vs,ws are left as passed in). */
+int cfdgb_op_convection_diffusion(cfdgb_ctx *ctx, const double *u, const double *v,
+                                  const double *w, double *us, double *vs, double *ws);
+/* BC_staggered_main (inc/BoundaryCondition/Boundary_Condition.hpp:37), in place. */
+int cfdgb_op_bc_main(cfdgb_ctx *ctx, double *u, double *v, double *w, double *p);
+/* BC_staggered_copy (inc/BoundaryCondition/updateBC.hpp:6): ghosts of u,v,w into us,vs,ws. */
+int cfdgb_op_bc_copy(cfdgb_ctx *ctx, const double *u, const double *v, const double *w,
+                     double *us, double *vs, double *ws);
+/* createBMatrix_omp (inc/matrix/b_matrix.hpp:35): b (compact) from u*; jacobi != 0
+ * scales by jp = 1/diag as the CSR path does. */
+int cfdgb_op_rhs(cfdgb_ctx *ctx, int jacobi, const double *us, const double *vs,
+                 const double *ws, double *b);
+/* SPE_matrix::multiply_omp (inc/matrix/SPE_sparseMatrix.hpp:92) or, jacobi != 0, the
+ * scaled CSR_matrix::multiply_omp (inc/matrix/CSR_sparseMatrix.hpp:232); compact x, y. */
+int cfdgb_op_spmv(cfdgb_ctx *ctx, int jacobi, const double *x, double *y);
+/* bicgstabRe2::solve (inc/solver/bicgstabRe2.hpp:84) on compact rhs, x (x in: warm
+ * start, out: solution).  solver: CFDGB_BICGSTAB or CFDGB_BICGSTAB_JACOBI (rhs must then
+ * already be scaled, as createBMatrix_omp does). */
+int cfdgb_op_bicgstab(cfdgb_ctx *ctx, int solver, double tol, int maxit, const double *rhs,
+                      double *x, int *iters, double *relres);
+/* update_UandF_omp (inc/dfib/updateUandF.hpp:90): u3,v3,w3 interior faces from u*, p,
+ * eta; f (3*padded, may be NULL) gets the DFIB force; cd/cl (may be NULL) its CD_CL. */
+int cfdgb_op_update_uf(cfdgb_ctx *ctx, const double *eta, const double *p, const double *us,
+                       const double *vs, const double *ws, double *u3, double *v3,
+                       double *w3, double *f, double *cd, double *cl);
+/* DFIB_CylinderZ (inc/dfib/setEta.hpp:136): solid fraction of the context's cylinder. */
+int cfdgb_op_solid_fraction(cfdgb_ctx *ctx, double *eta);
+/* Pressure solve on the current u* of the context (createBMatrix + solve +
+ * Pressure_transform_X_result, src/RUN_CPU.cpp:310-320) with the configured solver. */
+int cfdgb_pressure_solve(cfdgb_ctx *ctx, int *iters, double *relres);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -2,7 +2,10 @@
 // patched copy that oracle/build_ref.py stages under oracle/_ref/src) and dumps FP64
 // fields as raw little-endian arrays.  Test infrastructure only.
 //
-//   ref_<grid> run  <steps> <Re> <dt> <tol> <spe|csr|sor> <omega> <seed> <amp> <outdir>
+//   ref_<grid> run  <steps> <Re> <dt> <tol> <spe|csr|sor> <omega> <seed> <amp> <outdir> [cap]
+// (cap: optional BiCGSTAB iteration cap in place of the reference's 5000, for bounded
+// timing samples; stats.txt then also carries per-step wall times of the whole step and
+// of the pressure solve.)
 //   ref_<grid> unit <seed> <Re> <dt> <outdir>
 //
 // "run" replays runSeqOmp (src/RUN_CPU.cpp:9-436) step by step: set-up :50-236, then
@@ -16,8 +19,30 @@
 //
 // "unit" calls each hot-path function once on seeded random fields of this grid and
 // dumps inputs and outputs (golden vectors for the per-function parity tests).
+// Standard headers first, so that the access override below reaches only the
+// reference's own classes: it lets the bounded CPU-baseline sample set bicgstabRe2's
+// private iteration cap (iters_max_, bicgstabRe2.hpp:47); no arithmetic changes.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <random>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+#include <omp.h>
+#define private public
 #include "0_General.hpp"
 #include "run/general.hpp"
+#undef private
 
 #include <cstdint>
 #include <cstdio>
@@ -71,6 +96,7 @@ int run_mode(int argc, char **argv) {
   const uint64_t seed = std::strtoull(argv[8], nullptr, 10);
   const double amp = std::atof(argv[9]);
   const std::string out = argv[10];
+  const int cap = argc > 11 ? std::atoi(argv[11]) : 0;
 
   grid gA;
   simpulationVariable simu;
@@ -106,10 +132,12 @@ int run_mode(int argc, char **argv) {
     Mx.matA_spe.setupPressure(gA.gC, gA.Dx, gA.Dy, gA.Dz, gA.Dxs, gA.Dys, gA.Dzs);
     spe.reset(new solver::bicgstabRe2<mat::SPE_matrix<double>>(Mx.matA_spe));
     spe->setTolerance(tol);
+    if (cap > 0) spe->iters_max_ = cap;
   } else if (solver == "csr") {
     Mx.matA_csr.set(gA.createPressureMatrixCSR());
     csr.reset(new solver::bicgstabRe2<mat::CSR_matrix<double>>(Mx.matA_csr));
     csr->setTolerance(tol);
+    if (cap > 0) csr->iters_max_ = cap;
   } else if (solver != "sor") {
     std::fprintf(stderr, "unknown solver %s\n", solver.c_str()); return 2;
   }
@@ -120,18 +148,23 @@ int run_mode(int argc, char **argv) {
 
   std::string stats = out + "/stats.txt";
   FILE *fs = std::fopen(stats.c_str(), "w");
-  std::fprintf(fs, "# step time iters err cd cl\n");
+  std::fprintf(fs, "# step time iters err cd cl t_step_s t_solve_s\n");
+  using clk = std::chrono::steady_clock;
   for (int s = 1; s <= steps; ++s) {
+    const auto t0 = clk::now();
     simu.loop = s;
     ConvectionDifussion(simu, T0, T1, Lo, gA);
     simu.iters = 0; simu.error = 0.0;
+    auto ts0 = clk::now(), ts1 = ts0;
     if (simu.loop > 1) {
       if (solver == "sor") {
         SorPipeLine_omp(ShareM, Sor, simu, T1, t1, Lo, gA);
       } else {
         createBMatrix_omp(T1, Mx, simu, Lo, gA);
+        ts0 = clk::now();
         if (spe) std::tie(simu.iters, simu.error) = spe->solve(Mx.matB, Mx.X_result);
         else std::tie(simu.iters, simu.error) = csr->solve(Mx.matB, Mx.X_result);
+        ts1 = clk::now();
         Pressure_transform_X_result(t1, Mx, Lo, gA);
       }
     }
@@ -144,7 +177,11 @@ int run_mode(int argc, char **argv) {
     virtualF_Int(Dfib, Lo, gA, 1);
     const double cD = -2.0 * Dfib.ValSum[0] / gA.lz;
     const double cL = -2.0 * Dfib.ValSum[1] / gA.lz;
-    std::fprintf(fs, "%d %.17g %d %.17g %.17g %.17g\n", s, simu.time, simu.iters, simu.error, cD, cL);
+    const double t_step = std::chrono::duration<double>(clk::now() - t0).count();
+    const double t_solve = std::chrono::duration<double>(ts1 - ts0).count();
+    std::fprintf(fs, "%d %.17g %d %.17g %.17g %.17g %.6e %.6e\n", s, simu.time, simu.iters, simu.error, cD, cL,
+                 t_step, t_solve);
+    std::fflush(fs);
     simu.finishloop();
   }
   std::fclose(fs);

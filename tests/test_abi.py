@@ -1,0 +1,79 @@
+"""CPU checks of the C-ABI library: it loads, exports every entry point include/cfdgb.h
+declares, and its host-side logic (defaults, validation, perturbation generator) is
+right.  No kernel runs here."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import cfd_nssolver_forhpc_flowpassingcylinder_gb300 as cg
+from oracle import oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    text = (ROOT / "include" / "cfdgb.h").read_text()
+    return sorted(set(re.findall(r"\b(cfdgb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not cg.LIB_PATH.exists():
+        from cfd_nssolver_forhpc_flowpassingcylinder_gb300 import build as B
+        B.build()
+    return cg.load_library()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    # and the binding covers exactly the declared surface
+    assert set(names) == set(cg.EXPORTS)
+
+
+def test_defaults_are_the_reference_case(lib):
+    cfg = cg.default_config()
+    assert (cfg.nx, cfg.ny, cfg.nz) == (96, 48, 4)
+    assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
+    assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
+    assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
+    assert lib.cfdgb_abi_version() == 1
+
+
+@pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
+                                         ("precision", 3), ("tol", 0.0), ("maxit", 0)])
+def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
+    cfg = cg.default_config()
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    rc = lib.cfdgb_create(C.byref(cfg), C.byref(h))
+    assert rc == cg.EINVAL
+    assert h.value is None
+    assert lib.cfdgb_last_error()
+
+
+def test_mixed_sor_combination_rejected(lib):
+    cfg = cg.default_config(solver="rbsor", precision="mixed")
+    h = C.c_void_p()
+    assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
+
+
+def test_null_arguments_are_errors(lib):
+    assert lib.cfdgb_create(None, None) == cg.EINVAL
+    assert lib.cfdgb_step(None, 1, None) == cg.EINVAL
+    assert lib.cfdgb_get_fields(None, None, None, None, None) == cg.EINVAL
+
+
+def test_perturbation_generator_matches_oracle():
+    g = O.Grid(10, 8, 6, 2.5, 2.0, 1.5, 1.25)
+    u, v, w = np.ones(g.shape), g.zeros(), g.zeros()
+    O.perturb(g, u, v, w, 1234, 1e-3)
+    du, dv, dw = cg.perturbation(g.shape, 1234, 1e-3)
+    np.testing.assert_array_equal(u, 1.0 + du)
+    np.testing.assert_array_equal(v, dv)
+    np.testing.assert_array_equal(w, dw)
