@@ -43,6 +43,11 @@ class Config(C.Structure):
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double)]
 
 
+class Objective(C.Structure):
+    """cfdgb_objective: mean drag over steps first..last of an nsteps run."""
+    _fields_ = [("nsteps", C.c_int), ("first", C.c_int), ("last", C.c_int), ("ckpt_every", C.c_int)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("step", C.c_int), ("iters", C.c_int), ("outer", C.c_int), ("status", C.c_int),
                 ("relres", C.c_double), ("cd", C.c_double), ("cl", C.c_double)]
@@ -67,6 +72,9 @@ EXPORTS = {
     "cfdgb_set_eta": (C.c_int, [C.c_void_p, _dp]),
     "cfdgb_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
     "cfdgb_pressure_solve": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _dp]),
+    "cfdgb_set_inlet": (C.c_int, [C.c_void_p, _dp]),
+    "cfdgb_forward": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
+    "cfdgb_backward": (C.c_int, [C.c_void_p, _dp, _dp]),
     "cfdgb_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "cfdgb_reset_counters": (C.c_int, [C.c_void_p]),
     "cfdgb_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
@@ -212,6 +220,28 @@ class Solver:
         it, rr = C.c_int(), C.c_double()
         _check(self._L.cfdgb_pressure_solve(self._h, C.byref(it), C.byref(rr)))
         return it.value, rr.value
+
+    # ---- discrete adjoint ----
+    def set_inlet(self, u_in=None):
+        """Inlet u per (j, k) of the inlet face, shape (ny, nz); None: the constant 1."""
+        a = None if u_in is None else np.ascontiguousarray(u_in, dtype=np.float64).reshape(-1)
+        if a is not None and a.size != self.cfg.ny * self.cfg.nz:
+            raise ValueError("inlet profile must have ny*nz values")
+        _check(self._L.cfdgb_set_inlet(self._h, _ptr(a)))
+
+    def forward(self, nsteps, first, last, ckpt_every):
+        """Run nsteps from the initial state; J = mean Cd over steps first..last."""
+        obj = Objective(nsteps, first, last, ckpt_every)
+        J = C.c_double()
+        _check(self._L.cfdgb_forward(self._h, C.byref(obj), C.byref(J)), allow=(ENOCONV,))
+        return J.value
+
+    def backward(self):
+        """(dJ/d inlet profile (ny, nz), dJ/d eta (padded)) for the last forward()."""
+        g_in = np.zeros((self.cfg.ny, self.cfg.nz))
+        g_eta = self.zeros()
+        _check(self._L.cfdgb_backward(self._h, _ptr(g_in), _ptr(g_eta)), allow=(ENOCONV,))
+        return g_in, g_eta
 
     # ---- instrumentation ----
     def set_kernel_timing(self, on: bool):

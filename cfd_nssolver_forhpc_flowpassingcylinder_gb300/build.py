@@ -22,8 +22,10 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 # no fused multiply-add contraction, IEEE division and square root.
 PER_FILE = {
     "step_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
+    # the adjoint re-derives the forward branch decisions with the same arithmetic
+    "adjoint.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
 }
-SOURCES = ["api.cu", "step_exact.cu", "step_fast.cu", "solver.cu"]
+SOURCES = ["api.cu", "step_exact.cu", "step_fast.cu", "solver.cu", "adjoint.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,401 @@
+// Discrete adjoint of the FP64 projection step (reverse mode, hand-written).
+//
+// Forward step n (reference order, src/RUN_CPU.cpp:257-436) on the state U^n (T0 after
+// the ghost fill):
+//   u*  = CD(U^n) on interior faces; T1's ghost and last-face values are copies of U^n
+//   b   = -(1/dt) div(u*)                       (n > 1)
+//   x   = A^+ b  (p^n on the interior)          (n > 1; p^1 = initial p)
+//   U~  = (1 - eta_f)(u* - dt grad p^n)          on the faces update_UandF writes
+//   Cd^n = (2 / (lz dt)) sum eta_f (u* - dt dp/dx) dV   (x faces)
+//   U^{n+1} = BC(U~; inlet)
+// The adjoint of each piece, in reverse: BC^T (phases z, y, x: the reverse of the forward
+// order), correction^T (with dCd/d and d/d eta), the Poisson solve (A is symmetric on a
+// uniform grid, and the Jacobi-scaled system has the same solution, so lambda_b =
+// A^+ lambda_x for both solvers), RHS^T, and CD^T, the transposed QUICK stencil with the
+// upwind branches of the forward state held fixed (the scheme is piecewise linear in the
+// transported field and bilinear in the face velocities).  CD^T scatters with FP64
+// atomics; every other kernel gathers.
+#include "cfdgb_internal.cuh"
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace cfdgb {
+
+#define ROWS(g) \
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < (g).ncell; row += (long long)gridDim.x * kBlock)
+
+// ---- BC^T: transpose of the velocity part of k_bc_x/y/z --------------------------------
+// A write dst = a + s * src (chains dst1 = dst2 = ... = a + s * src) has adjoint
+// lam[src] += s * sum(lam[dst]); lam[dst] = 0.  Within a phase a thread owns one line.
+__global__ void __launch_bounds__(kBlock) k_adj_bc_x(Geo g, BcTable t, double *lu, double *lv, double *lw,
+                                                     double *linlet) {
+  const int nyc = g.nyc, nzc = g.nzc, nx = g.nx;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nyc * nzc; q += gridDim.x * kBlock) {
+    const int j = q / nzc + 2, k = q % nzc + 2;
+    auto I = [&](int i) { return pidx(g, i, j, k); };
+    // face x+ (BC_1)
+    double s = lu[I(nx - 1)] + lu[I(nx - 2)] + lu[I(nx - 3)];
+    lu[I(nx - 1)] = lu[I(nx - 2)] = lu[I(nx - 3)] = 0.0;
+    lu[I(nx - 4)] += t.num[1][0] * s;
+    s = lv[I(nx - 1)] + lv[I(nx - 2)];
+    lv[I(nx - 1)] = lv[I(nx - 2)] = 0.0;
+    lv[I(nx - 3)] += (2.0 * t.num[1][1] - 1.0) * s;
+    s = lw[I(nx - 1)] + lw[I(nx - 2)];
+    lw[I(nx - 1)] = lw[I(nx - 2)] = 0.0;
+    lw[I(nx - 3)] += (2.0 * t.num[1][2] - 1.0) * s;
+    // face x- (BC_0): u ghosts = inlet + num * u[2]
+    s = lu[I(0)] + lu[I(1)];
+    lu[I(0)] = lu[I(1)] = 0.0;
+    if (linlet) linlet[q] += s;
+    lu[I(2)] += t.num[0][0] * s;
+    s = lv[I(0)] + lv[I(1)];
+    lv[I(0)] = lv[I(1)] = 0.0;
+    lv[I(2)] += (2.0 * t.num[0][1] - 1.0) * s;
+    s = lw[I(0)] + lw[I(1)];
+    lw[I(0)] = lw[I(1)] = 0.0;
+    lw[I(2)] += (2.0 * t.num[0][2] - 1.0) * s;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_adj_bc_y(Geo g, BcTable t, double *lu, double *lv, double *lw) {
+  const int nxc = g.nxc, nzc = g.nzc, ny = g.ny;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nzc; q += gridDim.x * kBlock) {
+    const int i = q / nzc + 2, k = q % nzc + 2;
+    auto J = [&](int j) { return pidx(g, i, j, k); };
+    // face y+ (BC_3)
+    double s = lv[J(ny - 1)] + lv[J(ny - 2)] + lv[J(ny - 3)];
+    lv[J(ny - 1)] = lv[J(ny - 2)] = lv[J(ny - 3)] = 0.0;
+    lv[J(ny - 4)] += t.num[3][1] * s;
+    s = lu[J(ny - 1)] + lu[J(ny - 2)];
+    lu[J(ny - 1)] = lu[J(ny - 2)] = 0.0;
+    lu[J(ny - 3)] += (2.0 * t.num[3][0] - 1.0) * s;
+    s = lw[J(ny - 1)] + lw[J(ny - 2)];
+    lw[J(ny - 1)] = lw[J(ny - 2)] = 0.0;
+    lw[J(ny - 3)] += (2.0 * t.num[3][2] - 1.0) * s;
+    // face y- (BC_2)
+    s = lu[J(0)] + lu[J(1)];
+    lu[J(0)] = lu[J(1)] = 0.0;
+    lu[J(2)] += (2.0 * t.num[2][0] - 1.0) * s;
+    s = lv[J(0)] + lv[J(1)];
+    lv[J(0)] = lv[J(1)] = 0.0;
+    lv[J(2)] += t.num[2][1] * s;
+    s = lw[J(0)] + lw[J(1)];
+    lw[J(0)] = lw[J(1)] = 0.0;
+    lw[J(2)] += (2.0 * t.num[2][2] - 1.0) * s;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_adj_bc_z(Geo g, BcTable t, double *lu, double *lv, double *lw) {
+  const int nxc = g.nxc, nyc = g.nyc, nz = g.nz;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nyc; q += gridDim.x * kBlock) {
+    const int i = q / nyc + 2, j = q % nyc + 2;
+    const long long b = pidx(g, i, j, 0);
+    // face z+ (BC_5)
+    double s = lw[b + nz - 1] + lw[b + nz - 2] + lw[b + nz - 3];
+    lw[b + nz - 1] = lw[b + nz - 2] = lw[b + nz - 3] = 0.0;
+    lw[b + nz - 4] += t.num[5][2] * s;
+    s = lu[b + nz - 1] + lu[b + nz - 2];
+    lu[b + nz - 1] = lu[b + nz - 2] = 0.0;
+    lu[b + nz - 3] += (2.0 * t.num[5][0] - 1.0) * s;
+    s = lv[b + nz - 1] + lv[b + nz - 2];
+    lv[b + nz - 1] = lv[b + nz - 2] = 0.0;
+    lv[b + nz - 3] += (2.0 * t.num[5][1] - 1.0) * s;
+    // face z- (BC_4)
+    s = lu[b + 0] + lu[b + 1];
+    lu[b + 0] = lu[b + 1] = 0.0;
+    lu[b + 2] += (2.0 * t.num[4][0] - 1.0) * s;
+    s = lv[b + 0] + lv[b + 1];
+    lv[b + 0] = lv[b + 1] = 0.0;
+    lv[b + 2] += (2.0 * t.num[4][1] - 1.0) * s;
+    s = lw[b + 0] + lw[b + 1];
+    lw[b + 0] = lw[b + 1] = 0.0;
+    lw[b + 2] += t.num[4][2] * s;
+  }
+}
+
+// ---- correction^T, per face: lambda of T2 = u* - dt grad p and of eta_f -------------------
+// cw: weight of Cd^n in the objective times 2 / (lz dt) (0 outside the averaging window)
+__global__ void __launch_bounds__(kBlock) k_adj_corr(Geo g, double dt, double cw, const double *__restrict__ eta,
+                                                     const double *__restrict__ p, const double *__restrict__ us,
+                                                     const double *__restrict__ vs, const double *__restrict__ ws,
+                                                     const double *__restrict__ lu, const double *__restrict__ lv,
+                                                     const double *__restrict__ lw, double *lus, double *lvs,
+                                                     double *lws, double *lex, double *ley, double *lez) {
+  ROWS(g) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const double ec = eta[c];
+    if (i < g.nx - 3) {
+      const long long cp = c + g.sx;
+      const double T2 = us[c] - dt * (p[cp] - p[c]) / g.Dxs[i];
+      const double e = ec + (eta[cp] - ec) * ((g.Dxs[i] * 0.5) / g.Dx[i]);
+      const double vol = g.Dx[i] * g.Dy[j] * g.Dz[k];
+      lus[c] = (1.0 - e) * lu[c] + cw * e * vol;
+      lex[c] = -T2 * lu[c] + cw * T2 * vol;
+    } else {
+      lus[c] = 0.0;
+      lex[c] = 0.0;
+    }
+    if (j < g.ny - 3) {
+      const long long cp = c + g.sy;
+      const double T2 = vs[c] - dt * (p[cp] - p[c]) / g.Dys[j];
+      const double e = ec + (eta[cp] - ec) * ((g.Dys[j] * 0.5) / g.Dy[j]);
+      lvs[c] = (1.0 - e) * lv[c];
+      ley[c] = -T2 * lv[c];
+    } else {
+      lvs[c] = 0.0;
+      ley[c] = 0.0;
+    }
+    if (k < g.nz - 3) {
+      const long long cp = c + 1;
+      const double T2 = ws[c] - dt * (p[cp] - p[c]) / g.Dzs[k];
+      const double e = ec + (eta[cp] - ec) * ((g.Dzs[k] * 0.5) / g.Dz[k]);
+      lws[c] = (1.0 - e) * lw[c];
+      lez[c] = -T2 * lw[c];
+    } else {
+      lws[c] = 0.0;
+      lez[c] = 0.0;
+    }
+  }
+}
+
+// per cell: lambda_p (compact) from the faces around it, and eta's share of the faces'
+// interpolated solid fractions (accumulated over steps); ghost faces hold zeros
+__global__ void __launch_bounds__(kBlock) k_adj_corr_gather(Geo g, double dt, const double *__restrict__ lus,
+                                                            const double *__restrict__ lvs,
+                                                            const double *__restrict__ lws,
+                                                            const double *__restrict__ lex,
+                                                            const double *__restrict__ ley,
+                                                            const double *__restrict__ lez, double *lx, double *leta,
+                                                            double *part, StepScal *ss) {
+  double acc[1] = {0.0};
+  ROWS(g) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const double l = dt * (lus[c] / g.Dxs[i] - lus[c - g.sx] / g.Dxs[i - 1] + lvs[c] / g.Dys[j] -
+                           lvs[c - g.sy] / g.Dys[j - 1] + lws[c] / g.Dzs[k] - lws[c - 1] / g.Dzs[k - 1]);
+    lx[row] = l;
+    acc[0] += l;
+    const double itx = (g.Dxs[i] * 0.5) / g.Dx[i], itx1 = (g.Dxs[i - 1] * 0.5) / g.Dx[i - 1];
+    const double ity = (g.Dys[j] * 0.5) / g.Dy[j], ity1 = (g.Dys[j - 1] * 0.5) / g.Dy[j - 1];
+    const double itz = (g.Dzs[k] * 0.5) / g.Dz[k], itz1 = (g.Dzs[k - 1] * 0.5) / g.Dz[k - 1];
+    leta[c] += (1.0 - itx) * lex[c] + itx1 * lex[c - g.sx] + (1.0 - ity) * ley[c] + ity1 * ley[c - g.sy] +
+               (1.0 - itz) * lez[c] + itz1 * lez[c - 1];
+  }
+  double out[1];
+  if (grid_sum<1>(acc, part, &ss->cnt[4], out) && threadIdx.x == 0) ss->fsum[0] = out[0];  // sum of lambda_x
+}
+
+// y -= mean (mean = sum / ncell taken from ss->fsum[0], written by the previous kernel)
+__global__ void __launch_bounds__(kBlock) k_sub_mean(Geo g, double *y, const StepScal *ss) {
+  const double m = ss->fsum[0] / (double)g.ncell;
+  ROWS(g) y[row] -= m;
+}
+__global__ void __launch_bounds__(kBlock) k_sum(Geo g, const double *__restrict__ y, double *part, StepScal *ss) {
+  double acc[1] = {0.0};
+  ROWS(g) acc[0] += y[row];
+  double out[1];
+  if (grid_sum<1>(acc, part, &ss->cnt[4], out) && threadIdx.x == 0) ss->fsum[0] = out[0];
+}
+
+// ---- RHS^T: b = -(1/dt) div u* ---------------------------------------------------------
+// Interior faces feed lambda_u*; the faces T1 copies from U^n (x: i = 1 and nx-3; y, z
+// alike) feed lambda_U^n directly.  Each face is owned by one thread.
+__global__ void __launch_bounds__(kBlock) k_adj_rhs(Geo g, double dt, const double *__restrict__ lb, double *lus,
+                                                    double *lvs, double *lws, double *lu, double *lv, double *lw) {
+  const double ddt = 1.0 / dt;
+  const long long nyz = (long long)g.nyc * g.nzc;
+  ROWS(g) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const double l = lb[row];
+    if (i < g.nx - 3) lus[c] += -ddt / g.Dx[i] * l + ddt / g.Dx[i + 1] * lb[row + nyz];
+    else lu[c] += -ddt / g.Dx[i] * l;
+    if (i == 2) lu[c - g.sx] += ddt / g.Dx[i] * l;
+    if (j < g.ny - 3) lvs[c] += -ddt / g.Dy[j] * l + ddt / g.Dy[j + 1] * lb[row + g.nzc];
+    else lv[c] += -ddt / g.Dy[j] * l;
+    if (j == 2) lv[c - g.sy] += ddt / g.Dy[j] * l;
+    if (k < g.nz - 3) lws[c] += -ddt / g.Dz[k] * l + ddt / g.Dz[k + 1] * lb[row + 1];
+    else lw[c] += -ddt / g.Dz[k] * l;
+    if (k == 2) lw[c - 1] += ddt / g.Dz[k] * l;
+  }
+}
+
+// ---- CD^T: transposed QUICK convection-diffusion ---------------------------------------
+// A face value of QuickUnitA/B (inc/source/Convection_Difussion.hpp:20-90) is, for the
+// branch the face velocity selects, a fixed combination of three transported values.
+struct Lin3 {
+  long long q[3];
+  double c[3];
+  double val;
+};
+
+__device__ __forceinline__ void lin_set(Lin3 &L, long long q0, double c0, long long q1, double c1, long long q2,
+                                        double c2, const double *phi) {
+  L.q[0] = q0; L.q[1] = q1; L.q[2] = q2;
+  L.c[0] = c0; L.c[1] = c1; L.c[2] = c2;
+  L.val = c0 * phi[q0] + c1 * phi[q1] + c2 * phi[q2];
+}
+
+// QuickUnitA (the component's own axis)
+__device__ __forceinline__ void qa_lin(double Up, double Un, long long pp, long long p, long long ic, long long n,
+                                       long long nn, const double *Di, const double *Ds, int I, const double *phi,
+                                       Lin3 &P, Lin3 &N) {
+  if (Up > 0.0) {
+    const double k1 = 0.125 * Di[I + 1] * Di[I + 1] / Ds[I], a = 1.0 / Di[I + 1], b = 1.0 / Di[I];
+    lin_set(P, p, 0.5 - k1 * a, ic, 0.5 + k1 * a + k1 * b, n, -k1 * b, phi);
+  } else {
+    const double k2 = 0.125 * Di[I + 1] * Di[I + 1] / Ds[I + 1], a2 = 1.0 / Di[I + 2], a1 = 1.0 / Di[I + 1];
+    lin_set(P, pp, -k2 * a2, p, 0.5 + k2 * a2 + k2 * a1, ic, 0.5 - k2 * a1, phi);
+  }
+  if (Un > 0.0) {
+    const double k3 = 0.125 * Di[I] * Di[I] / Ds[I - 1], a = 1.0 / Di[I], b = 1.0 / Di[I - 1];
+    lin_set(N, ic, 0.5 - k3 * a, n, 0.5 + k3 * a + k3 * b, nn, -k3 * b, phi);
+  } else {
+    const double k4 = 0.125 * Di[I] * Di[I] / Ds[I], a1 = 1.0 / Di[I + 1], a0 = 1.0 / Di[I];
+    lin_set(N, p, -k4 * a1, ic, 0.5 + k4 * a1 + k4 * a0, n, 0.5 - k4 * a0, phi);
+  }
+}
+
+// QuickUnitB (across)
+__device__ __forceinline__ void qb_lin(double Up, double Un, long long pp, long long p, long long ic, long long n,
+                                       long long nn, const double *Di, const double *Ds, int I, const double *phi,
+                                       Lin3 &P, Lin3 &N) {
+  if (Up > 0.0) {
+    const double k = 0.125 * Ds[I] * Ds[I] / Di[I], a = 1.0 / Ds[I], b = 1.0 / Ds[I - 1];
+    lin_set(P, p, 0.5 - k * a, ic, 0.5 + k * a + k * b, n, -k * b, phi);
+  } else {
+    const double k = 0.125 * Ds[I] * Ds[I] / Di[I + 1], a2 = 1.0 / Ds[I + 1], a1 = 1.0 / Ds[I];
+    lin_set(P, pp, -k * a2, p, 0.5 + k * a2 + k * a1, ic, 0.5 - k * a1, phi);
+  }
+  if (Un > 0.0) {
+    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I - 1], a = 1.0 / Ds[I - 1], b = 1.0 / Ds[I - 2];
+    lin_set(N, ic, 0.5 - k * a, n, 0.5 + k * a + k * b, nn, -k * b, phi);
+  } else {
+    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I], a1 = 1.0 / Ds[I], a0 = 1.0 / Ds[I - 1];
+    lin_set(N, p, -k * a1, ic, 0.5 + k * a1 + k * a0, n, 0.5 - k * a0, phi);
+  }
+}
+
+__device__ __forceinline__ void scatter(double *lam, const Lin3 &L, double w) {
+#pragma unroll
+  for (int t = 0; t < 3; ++t) atomicAdd(lam + L.q[t], w * L.c[t]);
+}
+
+// Adjoint of one component (own axis A) of ConvectionDifussion at face c:
+// u*_c = u_c - dt * sum_b conv_b + nu dt * sum_b diff_b.
+template <int A>
+__device__ __forceinline__ void adj_component(const Geo &g, double dt, double nu, const double *const *vel,
+                                              double *const *lam, long long c, const int (&I)[3], double L) {
+  const long long s[3] = {g.sx, g.sy, 1};
+  const double *D[3] = {g.Dx, g.Dy, g.Dz};
+  const double *S[3] = {g.Dxs, g.Dys, g.Dzs};
+  const double *phi = vel[A];
+  double *lphi = lam[A];
+  atomicAdd(lphi + c, L);  // u*_c = u_c + ...
+  const double gc = -dt * L, h = nu * dt * L;
+  const double IT = (S[A][I[A]] * 0.5) / D[A][I[A]];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const long long sb = s[b];
+    const int Ib = I[b];
+    const double *Db = D[b], *Sb = S[b];
+    // diffusion
+    double ap, an;
+    if (b == A) {
+      ap = 1.0 / (Db[Ib + 1] * Sb[Ib]);
+      an = 1.0 / (Db[Ib] * Sb[Ib]);
+    } else {
+      ap = 1.0 / (Sb[Ib] * Db[Ib]);
+      an = 1.0 / (Sb[Ib - 1] * Db[Ib]);
+    }
+    atomicAdd(lphi + c + sb, h * ap);
+    atomicAdd(lphi + c - sb, h * an);
+    atomicAdd(lphi + c, -h * (ap + an));
+    // convection
+    Lin3 P, N;
+    if (b == A) {
+      const double Up = 0.5 * (phi[c + sb] + phi[c]), Un = 0.5 * (phi[c - sb] + phi[c]);
+      qa_lin(Up, Un, c + 2 * sb, c + sb, c, c - sb, c - 2 * sb, Db, Sb, Ib, phi, P, N);
+      const double w = gc / Sb[Ib];  // (P^2 - N^2) / Ds
+      scatter(lphi, P, w * 2.0 * P.val);
+      scatter(lphi, N, -w * 2.0 * N.val);
+    } else {
+      const double *vb = vel[b];
+      double *lvb = lam[b];
+      const long long sA = s[A];
+      const double b0 = vb[c], bA = vb[c + sA], bm = vb[c - sb], bmA = vb[c - sb + sA];
+      const double Bp = b0 + (bA - b0) * IT, Bn = bm + (bmA - bm) * IT;
+      qb_lin(Bp, Bn, c + 2 * sb, c + sb, c, c - sb, c - 2 * sb, Db, Sb, Ib, phi, P, N);
+      const double w = gc / Db[Ib];  // (P Bp - N Bn) / D
+      scatter(lphi, P, w * Bp);
+      scatter(lphi, N, -w * Bn);
+      const double lBp = w * P.val, lBn = -w * N.val;
+      atomicAdd(lvb + c, (1.0 - IT) * lBp);
+      atomicAdd(lvb + c + sA, IT * lBp);
+      atomicAdd(lvb + c - sb, (1.0 - IT) * lBn);
+      atomicAdd(lvb + c - sb + sA, IT * lBn);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_adj_convdiff(Geo g, double dt, double nu, const double *u, const double *v,
+                                                         const double *w, const double *__restrict__ lus,
+                                                         const double *__restrict__ lvs,
+                                                         const double *__restrict__ lws, double *lu, double *lv,
+                                                         double *lw) {
+  const double *vel[3] = {u, v, w};
+  double *lam[3] = {lu, lv, lw};
+  ROWS(g) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const int I[3] = {i, j, k};
+    if (i < g.nx - 3 && lus[c] != 0.0) adj_component<0>(g, dt, nu, vel, lam, c, I, lus[c]);
+    if (j < g.ny - 3 && lvs[c] != 0.0) adj_component<1>(g, dt, nu, vel, lam, c, I, lvs[c]);
+    if (k < g.nz - 3 && lws[c] != 0.0) adj_component<2>(g, dt, nu, vel, lam, c, I, lws[c]);
+  }
+}
+
+// ---- launchers ----
+static int grid_for(long long n, int cap) {
+  long long b = (n + kBlock - 1) / kBlock;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+void launch_adj_bc(cudaStream_t s, const Geo &g, double *lu, double *lv, double *lw, double *linlet) {
+  const BcTable t = flowpassing_table();
+  // reverse of the forward phase order x, y, z
+  k_adj_bc_z<<<grid_for((long long)g.nxc * g.nyc, 1024), kBlock, 0, s>>>(g, t, lu, lv, lw);
+  k_adj_bc_y<<<grid_for((long long)g.nxc * g.nzc, 1024), kBlock, 0, s>>>(g, t, lu, lv, lw);
+  k_adj_bc_x<<<grid_for((long long)g.nyc * g.nzc, 1024), kBlock, 0, s>>>(g, t, lu, lv, lw, linlet);
+}
+
+void launch_adj_corr(cudaStream_t s, int nblk, const Geo &g, double dt, double cw, const double *eta, const double *p,
+                     const double *us, const double *vs, const double *ws, const double *lu, const double *lv,
+                     const double *lw, double *lus, double *lvs, double *lws, double *lex, double *ley, double *lez,
+                     double *lx, double *leta, double *part, StepScal *ss) {
+  k_adj_corr<<<nblk, kBlock, 0, s>>>(g, dt, cw, eta, p, us, vs, ws, lu, lv, lw, lus, lvs, lws, lex, ley, lez);
+  k_adj_corr_gather<<<nblk, kBlock, 0, s>>>(g, dt, lus, lvs, lws, lex, ley, lez, lx, leta, part, ss);
+}
+
+void launch_remove_mean(cudaStream_t s, int nblk, const Geo &g, double *y, double *part, StepScal *ss, bool sum_known) {
+  if (!sum_known) k_sum<<<nblk, kBlock, 0, s>>>(g, y, part, ss);
+  k_sub_mean<<<nblk, kBlock, 0, s>>>(g, y, ss);
+}
+
+void launch_adj_rhs(cudaStream_t s, int nblk, const Geo &g, double dt, const double *lb, double *lus, double *lvs,
+                    double *lws, double *lu, double *lv, double *lw) {
+  k_adj_rhs<<<nblk, kBlock, 0, s>>>(g, dt, lb, lus, lvs, lws, lu, lv, lw);
+}
+
+void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u, const double *v,
+                         const double *w, const double *lus, const double *lvs, const double *lws, double *lu,
+                         double *lv, double *lw) {
+  k_adj_convdiff<<<nblk, kBlock, 0, s>>>(g, dt, nu, u, v, w, lus, lvs, lws, lu, lv, lw);
+}
+
+}  // namespace cfdgb

@@ -57,12 +57,12 @@ uint64_t splitmix64(uint64_t &s) {
 
 // Kernels the instrumentation tells apart (cfdgb_kernel_stat).
 enum KId {
-  K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_AP32, K_S32, K_AS32, K_XR32, K_P32,
+  K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
-    "bicg_p64", "bicg_ap32", "bicg_s32", "bicg_as32", "bicg_xr32", "bicg_p32", "residual64", "inner_setup32",
+    "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "inner_setup32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction"};
 
 struct PendingEv {
@@ -90,6 +90,7 @@ struct cfdgb_ctx {
   double *b = nullptr, *x = nullptr, *px1 = nullptr, *px2 = nullptr, *r64 = nullptr;
   KrylovVecs<double> k64{};
   KrylovVecs<float> k32{};
+  float *p32[2] = {nullptr, nullptr}, *ap32[2] = {nullptr, nullptr};  // FP32 double buffers
   double *part = nullptr;
   SolverScal *sc = nullptr, *sc32 = nullptr;
   StepScal *ss = nullptr;
@@ -112,6 +113,22 @@ struct cfdgb_ctx {
   long long kn[K_COUNT] = {0};
   std::vector<cudaEvent_t> ev_free;
   std::vector<PendingEv> ev_pending;
+  // inlet u profile (nyc*nzc) replacing Dir[0][0]; NULL = the reference's constant 1
+  double *inlet = nullptr, *inlet_buf = nullptr;
+  // discrete adjoint: checkpoints (T0, p, warm start x, solver scalars, step counter)
+  // every ckpt_every steps, a recompute window of ckpt_every steps, adjoint fields
+  cfdgb_objective obj{};
+  bool fwd_done = false;
+  std::vector<double *> ck_f;  // 5 buffers per checkpoint: u, v, w, p (padded), x (compact)
+  std::vector<SolverScal> ck_sc;
+  std::vector<int> ck_loop;
+  std::vector<double *> win;  // 4 padded buffers per window step: u, v, w, p
+  double *lA[3] = {nullptr}, *lB[3] = {nullptr}, *lus[3] = {nullptr}, *le[3] = {nullptr};
+  double *leta = nullptr, *lx = nullptr, *linlet = nullptr;
+  KrylovVecs<double> ka{};
+  double *kapx[2] = {nullptr, nullptr};
+  SolverScal *sca = nullptr;
+  double J = 0.0;
 };
 
 namespace {
@@ -282,13 +299,15 @@ int validate(const cfdgb_config *c) {
 int capture_chunk(cfdgb_ctx *c, bool fp32) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   for (int m = 0; m < c->chunk_len; ++m) {
     if (fp32)
-      launch_bicg_iter<float>(c->stream, c->nblk, c->g, c->cfg.solver == CFDGB_BICGSTAB_JACOBI ? c->jac32 : c->spe32,
-                              c->k32, c->part, c->sc32);
+      for (int part = 0; part < 3; ++part)
+        launch_bicg32_part(c->stream, part, m & 1, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part,
+                           c->sc32);
     else
-      launch_bicg_iter<double>(c->stream, c->nblk, c->g, c->cfg.solver == CFDGB_BICGSTAB_JACOBI ? c->jac64 : c->spe64,
-                               c->k64, c->part, c->sc);
+      for (int part = 0; part < 5; ++part)
+        launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
   }
   CK(cudaStreamEndCapture(c->stream, &graph));
   cudaGraphExec_t exec;
@@ -322,21 +341,23 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   const long long max_chunks = (long long)c->cfg.maxit / c->chunk_len + 3;
   for (long long q = 0; q < max_chunks; ++q) {
     if (c->timing) {
-      for (int m = 0; m < c->chunk_len; ++m)
-        for (int part = 0; part < 5; ++part) {
-          if (fp32)
-            L(c, K_AP32 + part, 1, [&] {
-              launch_bicg_part<float>(c->stream, part, c->nblk, c->g, jac ? c->jac32 : c->spe32, c->k32, c->part, c->sc32);
+      for (int m = 0; m < c->chunk_len; ++m) {
+        if (fp32)
+          for (int part = 0; part < 3; ++part)
+            L(c, K_PAP32 + part, 1, [&] {
+              launch_bicg32_part(c->stream, part, m & 1, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32,
+                                 c->part, c->sc32);
             });
-          else
+        else
+          for (int part = 0; part < 5; ++part)
             L(c, K_AP64 + part, 1, [&] {
-              launch_bicg_part<double>(c->stream, part, c->nblk, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
+              launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
             });
-        }
+      }
     } else {
-      const int first = fp32 ? K_AP32 : K_AP64;
-      c->launches += 5LL * c->chunk_len;
-      for (int part = 0; part < 5; ++part) c->kn[first + part] += c->chunk_len;
+      const int first = fp32 ? K_PAP32 : K_AP64, nk = fp32 ? 3 : 5;
+      c->launches += (long long)nk * c->chunk_len;
+      for (int part = 0; part < nk; ++part) c->kn[first + part] += c->chunk_len;
       CK(cudaGraphLaunch(fp32 ? c->chunk32 : c->chunk64, c->stream));
     }
     CK(cudaMemcpyAsync(c->h_sc, dsc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
@@ -393,28 +414,54 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   // MIXED: FP64 defect correction around FP32 BiCGSTAB on the unit-scaled residual.
   // Each inner solve is asked for the reduction that finishes the job with a 5x margin,
   // but not below inner_tol (the FP32 floor).
+  // A correction that made the FP64 residual worse is taken back; when the sweeps stall
+  // (less than 2x per sweep) or an inner solve breaks down, the FP64 BiCGSTAB finishes
+  // from the current x, so the mode always ends at the FP64 tolerance.
   static const bool trace = std::getenv("CFDGB_TRACE") != nullptr;
+  double prev_rel = HUGE_VAL, applied = 0.0;
+  bool finish64 = false;
   for (int o = 0;; ++o) {
     L(c, K_RESID64, 1, [&] { launch_residual64(c->stream, c->nblk, c->g, st64, c->b, c->x, c->r64, c->part, c->ss, c->sc32, o == 0); });
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    const double rel = c->h_ss->relres;
+    const double rel = c->h_ss->relres, rnorm = c->h_ss->rnorm;
     *relres = rel;
     if (trace) std::fprintf(stderr, "[cfdgb] step %d outer %d relres %.3e\n", c->loop, o, rel);
-    if (!std::isfinite(rel)) { *status = CFDGB_ENAN; break; }
+    if (!std::isfinite(rel) && applied == 0.0) { *status = CFDGB_ENAN; break; }
     if (rel < c->cfg.tol) break;
-    if (o >= c->cfg.max_outer) { *status = CFDGB_ENOCONV; break; }
+    if (!std::isfinite(rel) || rel > 0.5 * prev_rel || o >= c->cfg.max_outer) {
+      if (!(rel <= prev_rel) && applied != 0.0)
+        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -applied); });
+      finish64 = true;
+      break;
+    }
     const double itol = std::min(0.5, std::max(c->cfg.inner_tol, 0.2 * c->cfg.tol / rel));
     TRY(set_solver_params(c, c->sc32, itol, c->cfg.maxit));
-    L(c, K_SETUP32, 1, [&] { launch_inner_setup32(c->stream, c->nblk, c->g, c->k32, c->r64, c->part, c->sc32); });
+    L(c, K_SETUP32, 1, [&] { launch_inner_setup32(c->stream, c->nblk, c->g, c->k32, c->p32, c->ap32, c->r64, c->part, c->sc32); });
     SolverScal r;
     TRY(run_chunks(c, true, &r));
     if (trace)
-      std::fprintf(stderr, "[cfdgb]   inner tol %.1e iters %d status %d relres %.3e\n", itol, r.iter, r.status, r.relres);
+      std::fprintf(stderr, "[cfdgb]   inner tol %.1e iters %d status %d relres %.3e best %.3e\n", itol, r.iter,
+                   r.status, r.relres, r.best);
     *iters += r.iter + 1;
     *outer = o + 1;
-    if (!std::isfinite(r.relres)) { *status = CFDGB_ENAN; break; }  // never apply a broken correction
-    L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, c->sc32); });
+    if (!std::isfinite(r.relres)) {  // never apply a broken correction
+      finish64 = true;
+      break;
+    }
+    applied = rnorm;
+    prev_rel = rel;
+    L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, applied); });
+  }
+  if (finish64) {
+    TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
+    L(c, K_SETUP64, 1, [&] { launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc); });
+    SolverScal r;
+    TRY(run_chunks(c, false, &r));
+    if (trace) std::fprintf(stderr, "[cfdgb]   FP64 finish iters %d status %d relres %.3e\n", r.iter, r.status, r.relres);
+    *iters += r.iter;
+    *relres = r.relres;
+    *status = r.status;
   }
   return 0;
 }
@@ -428,7 +475,7 @@ int apply_init_bc(cfdgb_ctx *c) {
   CK(cudaMemcpyAsync(c->us, c->u, bytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->vs, c->v, bytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->ws, c->w, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1);
+  launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet);
   CK(cudaMemsetAsync(c->x, 0, c->ncell * sizeof(double), c->stream));  // X_result = 0
   CK(cudaMemsetAsync(c->px1, 0, c->ncell * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->px2, 0, c->ncell * sizeof(double), c->stream));
@@ -482,7 +529,7 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->tol = 1e-8;
   c->maxit = 5000;
   c->omega = 1.7;
-  c->inner_tol = 1e-4;
+  c->inner_tol = 1e-3;
   c->max_outer = 20;
   c->check_every = 10;
   c->dfib = 1;
@@ -544,6 +591,14 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.ncell = c->ncell;
   g.Dx = c->metric; g.Dy = g.Dx + nx; g.Dz = g.Dy + ny;
   g.Dxs = g.Dz + nz; g.Dys = g.Dxs + nx; g.Dzs = g.Dys + ny;
+  // solver launch geometry: k along x (up to a warp), j along y, i strided over grid z
+  g.lbx = 1;
+  while (g.lbx < cfg->nz && g.lbx < 32) g.lbx *= 2;
+  g.lby = kBlock / g.lbx;
+  g.lgx = (cfg->nz + g.lbx - 1) / g.lbx;
+  g.lgy = (cfg->ny + g.lby - 1) / g.lby;
+  g.lgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.lgx * g.lgy)));
+  const int nblk3 = g.lgx * g.lgy * g.lgz;
   // fields and solver vectors
   double **pad[] = {&c->u, &c->v, &c->w, &c->us, &c->vs, &c->ws, &c->ui, &c->vi, &c->wi, &c->p, &c->eta};
   for (auto **q : pad)
@@ -552,18 +607,19 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   for (auto **q : cmp)
     if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   c->k64.x = c->x;
-  if (cfg->precision == CFDGB_FP64 && cfg->solver != CFDGB_RBSOR) {
+  if (cfg->solver != CFDGB_RBSOR) {  // MIXED keeps them for its FP64 finish
     double **kv[] = {&c->k64.r0, &c->k64.r1, &c->k64.p1, &c->k64.s, &c->k64.ap, &c->k64.as};
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
   if (cfg->precision == CFDGB_MIXED) {
     if ((rc = dalloc(c, &c->r64, c->ncell))) return bail(rc);
-    float **kv[] = {&c->k32.x, &c->k32.r0, &c->k32.r1, &c->k32.p1, &c->k32.s, &c->k32.ap, &c->k32.as};
+    float **kv[] = {&c->k32.x, &c->k32.r0, &c->k32.r1, &c->k32.s, &c->k32.as, &c->p32[0], &c->p32[1],
+                    &c->ap32[0], &c->ap32[1]};
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
-  if ((rc = dalloc(c, &c->part, 8 * (size_t)c->nblk))) return bail(rc);
+  if ((rc = dalloc(c, &c->part, 8 * (size_t)std::max(c->nblk, nblk3)))) return bail(rc);
   if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc32, 1)) || (rc = dalloc(c, &c->ss, 1))) return bail(rc);
   cudaMemset(c->sc, 0, sizeof(SolverScal));
   cudaMemset(c->sc32, 0, sizeof(SolverScal));
@@ -706,7 +762,7 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
                              c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part, c->ss);
     });
     // 4. ghost fill of T0 and p, copy into T1 (RUN_CPU.cpp:399-400)
-    L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1); });
+    L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet); });
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
     resolve_events(c);
@@ -865,7 +921,8 @@ int cfdgb_op_bicgstab(cfdgb_ctx *c, int solver, double tol, int maxit, const dou
   SolverScal r{};
   int rc = 0;
   for (long long q = 0; q < (long long)maxit / 8 + 3; ++q) {
-    for (int m = 0; m < 8; ++m) launch_bicg_iter<double>(c->stream, c->nblk, c->g, st, c->k64, c->part, c->sc);
+    for (int m = 0; m < 8; ++m)
+      for (int part = 0; part < 5; ++part) launch_bicg64_part(c->stream, part, c->g, st, c->k64, c->part, c->sc);
     CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
     if (c->h_sc->done) { r = *c->h_sc; break; }
@@ -914,6 +971,188 @@ int cfdgb_op_solid_fraction(cfdgb_ctx *c, double *eta) {
   launch_eta(c->stream, c->nblk, c->g, c->Xd, c->Yd, c->cfg.cx, c->cfg.cy, c->cfg.radius, c->op[6]);
   TRY(d2h(c, eta, c->op[6], c->npad));
   return sync(c);
+}
+
+// ---- discrete adjoint -------------------------------------------------------------------
+
+int cfdgb_set_inlet(cfdgb_ctx *c, const double *u_in) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!u_in) {
+    c->inlet = nullptr;
+    return 0;
+  }
+  const size_t n = (size_t)c->cfg.ny * c->cfg.nz;
+  if (!c->inlet_buf) TRY(dalloc(c, &c->inlet_buf, n));
+  c->inlet = c->inlet_buf;
+  TRY(h2d(c, c->inlet, u_in, n));
+  return sync(c);
+}
+
+namespace {
+
+int dd_copy(cfdgb_ctx *c, double *dst, const double *src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return 0;
+}
+
+// Adjoint Poisson solve A y = rhs with the unscaled operator, zero start, its own scalars
+// (no restarts: a fresh solver object each time).
+int adjoint_solve(cfdgb_ctx *c, const double *rhs, double tol, int *iters) {
+  CK(cudaMemsetAsync(c->sca, 0, sizeof(SolverScal), c->stream));
+  CK(cudaMemsetAsync(c->ka.x, 0, c->ncell * sizeof(double), c->stream));
+  TRY(set_solver_params(c, c->sca, tol, c->cfg.maxit));
+  launch_bicg_setup64(c->stream, c->nblk, c->g, c->spe64, c->ka, rhs, c->kapx[0], c->kapx[1], c->part, c->sca);
+  for (long long q = 0; q < (long long)c->cfg.maxit / 8 + 3; ++q) {
+    for (int m = 0; m < 8; ++m)
+      for (int part = 0; part < 5; ++part)
+        L(c, K_AP64 + part, 1, [&] { launch_bicg64_part(c->stream, part, c->g, c->spe64, c->ka, c->part, c->sca); });
+    CK(cudaMemcpyAsync(c->h_sc, c->sca, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    if (c->h_sc->done) {
+      *iters = c->h_sc->iter;
+      return c->h_sc->status;
+    }
+  }
+  return fail(CFDGB_ECUDA, "adjoint solver did not report completion");
+}
+
+}  // namespace
+
+int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
+  if (!c || !obj) return fail(CFDGB_EINVAL, "null argument");
+  if (c->cfg.precision != CFDGB_FP64 || c->cfg.solver == CFDGB_RBSOR)
+    return fail(CFDGB_EINVAL, "the adjoint needs an FP64 BiCGSTAB context");
+  if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
+    return fail(CFDGB_EINVAL, "bad objective window");
+  if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");
+  c->obj = *obj;
+  c->fwd_done = false;
+  const int K = obj->ckpt_every, nck = (obj->nsteps + K - 1) / K;
+  while ((int)c->ck_f.size() < 5 * nck) {
+    double *d = nullptr;
+    TRY(dalloc(c, &d, ((c->ck_f.size() % 5) == 4) ? c->ncell : c->npad));
+    c->ck_f.push_back(d);
+  }
+  c->ck_sc.assign(nck, SolverScal{});
+  c->ck_loop.assign(nck, 0);
+  double sum = 0.0;
+  for (int n = 1; n <= obj->nsteps; ++n) {
+    if ((n - 1) % K == 0) {
+      const int q = (n - 1) / K;
+      double **f = &c->ck_f[5 * q];
+      TRY(dd_copy(c, f[0], c->u, c->npad));
+      TRY(dd_copy(c, f[1], c->v, c->npad));
+      TRY(dd_copy(c, f[2], c->w, c->npad));
+      TRY(dd_copy(c, f[3], c->p, c->npad));
+      TRY(dd_copy(c, f[4], c->x, c->ncell));
+      CK(cudaMemcpyAsync(&c->ck_sc[q], c->sc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
+      c->ck_loop[q] = c->loop;
+    }
+    cfdgb_step_stats st{};
+    const int rc = cfdgb_step(c, 1, &st);
+    if (rc < 0 && rc != CFDGB_ENOCONV) return rc;
+    if (n >= obj->first && n <= obj->last) sum += st.cd;
+  }
+  TRY(sync(c));
+  c->J = sum / (obj->last - obj->first + 1);
+  c->fwd_done = true;
+  if (J) *J = c->J;
+  return 0;
+}
+
+int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!c->fwd_done) return fail(CFDGB_ESTATE, "cfdgb_forward must come first");
+  const cfdgb_objective &obj = c->obj;
+  const int K = obj.ckpt_every, nck = (obj.nsteps + K - 1) / K;
+  const size_t np = c->npad;
+  // buffers (allocated once per context, zeroed per call)
+  if (!c->leta) {
+    for (int a = 0; a < 3; ++a) {
+      TRY(dalloc(c, &c->lA[a], np)); TRY(dalloc(c, &c->lB[a], np));
+      TRY(dalloc(c, &c->lus[a], np)); TRY(dalloc(c, &c->le[a], np));
+    }
+    TRY(dalloc(c, &c->leta, np));
+    TRY(dalloc(c, &c->lx, c->ncell));
+    TRY(dalloc(c, &c->linlet, (size_t)c->cfg.ny * c->cfg.nz));
+    double **kv[] = {&c->ka.x, &c->ka.r0, &c->ka.r1, &c->ka.p1, &c->ka.s, &c->ka.ap, &c->ka.as, &c->kapx[0], &c->kapx[1]};
+    for (auto **q : kv) TRY(dalloc(c, q, c->ncell));
+    TRY(dalloc(c, &c->sca, 1));
+  }
+  while ((int)c->win.size() < 4 * K) {
+    double *d = nullptr;
+    TRY(dalloc(c, &d, np));
+    c->win.push_back(d);
+  }
+  for (int a = 0; a < 3; ++a) {
+    CK(cudaMemsetAsync(c->lA[a], 0, np * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(c->lus[a], 0, np * sizeof(double), c->stream));
+    CK(cudaMemsetAsync(c->le[a], 0, np * sizeof(double), c->stream));
+  }
+  CK(cudaMemsetAsync(c->leta, 0, np * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(c->linlet, 0, (size_t)c->cfg.ny * c->cfg.nz * sizeof(double), c->stream));
+  const double nu = 1.0 / c->cfg.Re, dt = c->cfg.dt;
+  const double cw_in = 2.0 / (c->cfg.lz * dt) / (double)(obj.last - obj.first + 1);
+  int worst = 0;
+  for (int q = nck - 1; q >= 0; --q) {
+    const int n0 = q * K + 1, n1 = std::min(n0 + K - 1, obj.nsteps);
+    // restore the checkpoint and recompute the window forward, keeping U^n and p^n
+    double **f = &c->ck_f[5 * q];
+    TRY(dd_copy(c, c->u, f[0], np));
+    TRY(dd_copy(c, c->v, f[1], np));
+    TRY(dd_copy(c, c->w, f[2], np));
+    TRY(dd_copy(c, c->p, f[3], np));
+    TRY(dd_copy(c, c->x, f[4], c->ncell));
+    CK(cudaMemcpyAsync(c->sc, &c->ck_sc[q], sizeof(SolverScal), cudaMemcpyHostToDevice, c->stream));
+    launch_bc(c->stream, c->g, c->u, c->v, c->w, nullptr, c->us, c->vs, c->ws, 0);  // T1's copies of T0
+    c->loop = c->ck_loop[q];
+    for (int n = n0; n <= n1; ++n) {
+      double **wv = &c->win[4 * (n - n0)];
+      TRY(dd_copy(c, wv[0], c->u, np));
+      TRY(dd_copy(c, wv[1], c->v, np));
+      TRY(dd_copy(c, wv[2], c->w, np));
+      cfdgb_step_stats st{};
+      const int rc = cfdgb_step(c, 1, &st);
+      if (rc < 0 && rc != CFDGB_ENOCONV) return rc;
+      TRY(dd_copy(c, wv[3], c->p, np));
+    }
+    // reverse sweep over the window
+    for (int n = n1; n >= n0; --n) {
+      double **wv = &c->win[4 * (n - n0)];
+      launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
+      // u* of step n (interior faces), from U^n
+      launch_convdiff_exact(c->stream, c->nblk, c->g, dt, nu, wv[0], wv[1], wv[2], c->us, c->vs, c->ws);
+      const double cw = (n >= obj.first && n <= obj.last) ? cw_in : 0.0;
+      launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, wv[3], c->us, c->vs, c->ws, c->lA[0], c->lA[1],
+                      c->lA[2], c->lus[0], c->lus[1], c->lus[2], c->le[0], c->le[1], c->le[2], c->lx, c->leta,
+                      c->part, c->ss);
+      for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(c->lB[a], 0, np * sizeof(double), c->stream));
+      if (n > 1) {
+        // lambda_b = A^+ lambda_x (both sides mean-free)
+        launch_remove_mean(c->stream, c->nblk, c->g, c->lx, c->part, c->ss, true);
+        int it = 0;
+        const int rc = adjoint_solve(c, c->lx, c->cfg.tol, &it);
+        if (rc < worst) worst = rc;
+        launch_remove_mean(c->stream, c->nblk, c->g, c->ka.x, c->part, c->ss, false);
+        launch_adj_rhs(c->stream, c->nblk, c->g, dt, c->ka.x, c->lus[0], c->lus[1], c->lus[2], c->lB[0], c->lB[1],
+                       c->lB[2]);
+      }
+      launch_adj_convdiff(c->stream, c->nblk, c->g, dt, nu, wv[0], wv[1], wv[2], c->lus[0], c->lus[1], c->lus[2],
+                          c->lB[0], c->lB[1], c->lB[2]);
+      for (int a = 0; a < 3; ++a) std::swap(c->lA[a], c->lB[a]);
+    }
+  }
+  // the ghost fill of the initial state (cfdgb_init_fields) also reads the inlet
+  launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
+  CK(cudaGetLastError());
+  if (dJ_dinlet) TRY(d2h(c, dJ_dinlet, c->linlet, (size_t)c->cfg.ny * c->cfg.nz));
+  if (dJ_deta) TRY(d2h(c, dJ_deta, c->leta, np));
+  TRY(sync(c));
+  // the fields now hold the first recompute window's end state: stepping on needs a new
+  // cfdgb_init_fields (cfdgb_backward may be called again: it restarts from checkpoints)
+  c->have_fields = false;
+  if (worst < 0) fail(worst, "an adjoint Poisson solve ended with status %d", worst);
+  return worst;
 }
 
 }  // extern "C"

@@ -26,6 +26,9 @@ struct Geo {
   long long sx, sy;     // padded strides: sx = ny*nz, sy = nz
   long long ncell;      // nxc*nyc*nzc
   const double *Dx, *Dy, *Dz, *Dxs, *Dys, *Dzs;  // metric arrays (padded lengths)
+  // 3-D launch geometry of the solver kernels: blocks of (lbx along k) x (lby along j)
+  // threads, grid (lgx, lgy) covering a (j, k) plane and lgz blocks striding over i
+  int lbx, lby, lgx, lgy, lgz;
 };
 
 // compact row -> padded (i,j,k)
@@ -85,6 +88,7 @@ __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &i
 struct SolverScal {
   double rho, alpha, omega, beta, norm0, relres, tol, restart_thr;
   double scale;              // MIXED: ||r|| of the outer residual the inner rhs is scaled by
+  double best;               // FP32 inner solve: smallest relative residual seen
   int iter, maxit, done, status, timestep, restart, pad0, pad1;
   unsigned cnt[8];           // last-block counters, one per kernel kind
 };
@@ -97,7 +101,19 @@ struct StepScal {
   unsigned cnt[8];
 };
 
-// ---- launch helpers implemented in the .cu files ----
-struct Ctx;
+// Dir/Num boundary table of inc/BoundaryCondition/FLOWpassing.hpp:6-40 as
+// dir[face][component], num[face][component]; faces 0..5 = x-, x+, y-, y+, z-, z+.
+// Face 0 is the inlet (u = 1, reflected v and w); every other face is zero-gradient.
+struct BcTable {
+  double dir[6][3], num[6][3];
+};
+inline BcTable flowpassing_table() {
+  BcTable t{};
+  for (int f = 0; f < 6; ++f)
+    for (int c = 0; c < 3; ++c) { t.dir[f][c] = 0.0; t.num[f][c] = 1.0; }
+  t.dir[0][0] = 1.0;
+  t.num[0][0] = t.num[0][1] = t.num[0][2] = 0.0;
+  return t;
+}
 
 }  // namespace cfdgb

@@ -17,8 +17,9 @@ void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, d
                             const double *p, const double *us, const double *vs, const double *ws, double *u3,
                             double *v3, double *w3, double *f, const double *ui, const double *vi,
                             const double *wi, double *part, StepScal *ss);
+// inlet: nyc*nzc inlet u values (NULL: the reference's constant Dir[0][0] = 1)
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
-               double *vs, double *ws, int do_main);
+               double *vs, double *ws, int do_main, const double *inlet = nullptr);
 void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
                 double R, double *eta);
 
@@ -36,14 +37,14 @@ struct KrylovVecs {
 void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st,
                          KrylovVecs<double> v, const double *b, double *px1, double *px2, double *part,
                          SolverScal *sc);
-// kernel `part` (0..4: ap, s, as, xr, p) of one iteration
-template <typename T>
-void launch_bicg_part(cudaStream_t s, int part, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v,
-                      double *part_buf, SolverScal *sc);
-// one iteration (five kernels, each a no-op once sc->done is set)
-template <typename T>
-void launch_bicg_iter(cudaStream_t s, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v,
-                      double *part, SolverScal *sc);
+// FP64 iteration, kernel `part` 0..4 (ap, s, as, xr, p); each a no-op once sc->done is set
+void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
+                        double *part_buf, SolverScal *sc);
+// FP32 iteration, kernel `part` 0..2 (p update + A p, s + A s, x and r1); p and ap are
+// double-buffered (p2[parity] holds the previous p, p2[parity^1] receives the new one)
+void launch_bicg32_part(cudaStream_t s, int part, int parity, const Geo &g, const Stencil<float> &st,
+                        KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
+                        SolverScal *sc);
 // after the loop: NaN/Inf recovery of bicgstabRe2.hpp:133-153 when the cap was hit
 void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
                            const double *px2, double *part, SolverScal *sc);
@@ -51,9 +52,23 @@ void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, co
 // MIXED defect correction pieces
 void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first);
-void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, KrylovVecs<float> v, const double *r64,
-                          double *part, SolverScal *sc);
-void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, const SolverScal *sc);
+void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, KrylovVecs<float> v, float *const p2[2],
+                          float *const ap2[2], const double *r64, double *part, SolverScal *sc);
+void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor);
+
+// adjoint.cu (discrete adjoint of the FP64 step)
+void launch_adj_bc(cudaStream_t s, const Geo &g, double *lu, double *lv, double *lw, double *linlet);
+void launch_adj_corr(cudaStream_t s, int nblk, const Geo &g, double dt, double cw, const double *eta, const double *p,
+                     const double *us, const double *vs, const double *ws, const double *lu, const double *lv,
+                     const double *lw, double *lus, double *lvs, double *lws, double *lex, double *ley, double *lez,
+                     double *lx, double *leta, double *part, StepScal *ss);
+// y -= mean(y); sum_known: the previous kernel left sum(y) in ss->fsum[0]
+void launch_remove_mean(cudaStream_t s, int nblk, const Geo &g, double *y, double *part, StepScal *ss, bool sum_known);
+void launch_adj_rhs(cudaStream_t s, int nblk, const Geo &g, double dt, const double *lb, double *lus, double *lvs,
+                    double *lws, double *lu, double *lv, double *lw);
+void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u, const double *v,
+                         const double *w, const double *lus, const double *lvs, const double *lws, double *lu,
+                         double *lv, double *lw);
 
 // red-black SOR on the same operator (FP64)
 void launch_rbsor_sweep(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,

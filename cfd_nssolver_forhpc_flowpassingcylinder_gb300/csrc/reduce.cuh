@@ -1,14 +1,19 @@
-// Deterministic two-stage FP64 reductions for grid-stride kernels with a fixed grid.
+// Deterministic two-stage FP64 reductions for kernels with a fixed grid (1-D or 3-D
+// blocks of kBlock threads).
 //
 // Stage 1: each block reduces its NV per-thread values (warp shuffles + shared memory)
-// and stores them to part[q * gridDim.x + blockIdx.x].  Stage 2: the last block to
-// finish (atomic ticket) sums the partials in a fixed order, so results do not depend
-// on block scheduling.  No block ever waits on another.
+// and stores them to part[q * nblocks + block].  Stage 2: the last block to finish (atomic
+// ticket) sums the partials in a fixed order, so results do not depend on block
+// scheduling.  No block ever waits on another.
 #pragma once
 
 #include "cfdgb_internal.cuh"
 
 namespace cfdgb {
+
+__device__ __forceinline__ int lin_tid() { return (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int lin_bid() { return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x; }
+__device__ __forceinline__ int nblocks() { return gridDim.x * gridDim.y * gridDim.z; }
 
 template <int NV>
 __device__ __forceinline__ void warp_sum(double (&v)[NV]) {
@@ -22,7 +27,8 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV]) {
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
   __shared__ double sh[NV][kBlock / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int t = lin_tid();
+  const int lane = t & 31, wid = t >> 5;
   warp_sum<NV>(v);
   __syncthreads();  // sh may still be read by a previous call
   if (lane == 0)
@@ -44,10 +50,10 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, unsigned
   __shared__ bool last;
   __shared__ double res[NV];
   block_sum<NV>(v);
-  const int G = gridDim.x;
-  if (threadIdx.x == 0) {
+  const int G = nblocks(), t = lin_tid();
+  if (t == 0) {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) part[q * G + blockIdx.x] = v[q];
+    for (int q = 0; q < NV; ++q) part[q * G + lin_bid()] = v[q];
     __threadfence();
     last = (atomicAdd(ticket, 1u) == (unsigned)(G - 1));
   }
@@ -58,11 +64,11 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, unsigned
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < G; b += kBlock) s += __ldcg(part + q * G + b);
+    for (int b = t; b < G; b += kBlock) s += __ldcg(part + q * G + b);
     w[q] = s;
   }
   block_sum<NV>(w);
-  if (threadIdx.x == 0) {
+  if (t == 0) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) res[q] = w[q];
     *ticket = 0u;

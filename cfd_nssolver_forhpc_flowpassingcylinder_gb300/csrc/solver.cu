@@ -1,29 +1,62 @@
 // Pressure Poisson solvers on the 7-point Neumann operator.
 //
 // BiCGSTAB follows bicgstabRe2::solve (inc/solver/bicgstabRe2.hpp:84-180) step for step:
-// warm start, relative-residual stop, rho restart, iteration cap and NaN recovery.  One
-// iteration is five grid-stride kernels; every global dot product is a deterministic
-// two-stage FP64 reduction (reduce.cuh) whose last block also computes the scalar
-// update (alpha, omega, convergence, beta, restart), so no host round trip is needed
-// inside an iteration.  Every kernel returns at once when sc->done is set, which lets
-// the host enqueue iterations in chunks (or a CUDA graph) and poll only between chunks.
+// warm start, relative-residual stop, rho restart, iteration cap and NaN recovery.  Every
+// global dot product is a deterministic two-stage FP64 reduction (reduce.cuh) whose last
+// block also makes the scalar decisions (alpha, omega, stop test, beta, restart), so no
+// host round trip happens inside an iteration.  Every kernel returns at once when
+// sc->done is set, which lets the host enqueue iterations in chunks (captured as CUDA
+// graphs) and poll only between chunks.
 //
-// Templated on the vector type: double for the FP64 path, float for the inner solve
-// of the mixed-precision defect correction (dots still accumulate in FP64).
+// Launch geometry: 3-D blocks (bx along k, by along j) with the grid's z dimension
+// striding over i, so each thread knows its (i, j, k) without a division.
+//
+// FP64 (the plain path, bound by the FP64 pipe): five kernels per iteration, no
+// recomputation.  FP32 (inner solve of the mixed path, bound by HBM): three kernels per
+// iteration; the p update is fused into the next SpMV and s into its SpMV by
+// recomputing them at the stencil points (L1-resident), 17 instead of 19 words per cell.
 #include "cfdgb_internal.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
 namespace cfdgb {
 
-#define GRID_STRIDE(row, n) \
-  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < (n); row += (long long)gridDim.x * kBlock)
+// (ic, jc, kc) of this thread and the loop over the i planes it owns.
+#define FOR_CELLS(g)                                               \
+  const int kc = blockIdx.x * blockDim.x + threadIdx.x;            \
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y;            \
+  const bool on_ = (kc < (g).nzc) && (jc < (g).nyc);               \
+  for (int ic = blockIdx.z; on_ && ic < (g).nxc; ic += gridDim.z)
+
+#define ROW(g) ((((long long)ic * (g).nyc + jc) * (g).nzc) + kc)
+
+__device__ __forceinline__ const int cls_of(const Geo &g, int ic, int jc, int kc) {
+  return axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc);
+}
+
+// y = (A f)(row) where f(q) is evaluated on demand at the stencil points
+template <typename T, class F>
+__device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, int ic, int jc, int kc,
+                                           long long row, F &&f, T &center) {
+  const long long nyz = (long long)g.nyc * g.nzc;
+  const T *c = st.c[cls_of(g, ic, jc, kc)];
+  T sum = T(0);
+  if (ic > 0) sum += c[0] * f(row - nyz);
+  if (jc > 0) sum += c[1] * f(row - g.nzc);
+  if (kc > 0) sum += c[2] * f(row - 1);
+  center = f(row);
+  sum += c[3] * center;
+  if (kc < g.nzc - 1) sum += c[4] * f(row + 1);
+  if (jc < g.nyc - 1) sum += c[5] * f(row + g.nzc);
+  if (ic < g.nxc - 1) sum += c[6] * f(row + nyz);
+  return sum;
+}
 
 template <typename T>
-__device__ __forceinline__ T spmv(const Geo &g, const Stencil<T> &st, const T *__restrict__ x, long long row) {
-  int ic, jc, kc;
-  row_cijk(row, g.nyc, g.nzc, ic, jc, kc);
-  return stencil_row<T>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
+__device__ __forceinline__ T spmv_at(const Geo &g, const Stencil<T> &st, const T *__restrict__ x, int ic, int jc,
+                                     int kc, long long row) {
+  T c;
+  return stencil_apply<T>(g, st, ic, jc, kc, row, [&](long long q) { return x[q]; }, c);
 }
 
 // ---- FP64 set-up: bicgstabRe2.hpp:86-106 ----
@@ -31,9 +64,10 @@ __global__ void __launch_bounds__(kBlock) k_bicg_setup64(Geo g, Stencil<double> 
                                                           const double *__restrict__ b, double *px1, double *px2,
                                                           double *part, SolverScal *sc) {
   double acc[2] = {0.0, 0.0};
-  GRID_STRIDE(row, g.ncell) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
     const double bb = b[row];
-    const double r = bb - spmv<double>(g, st, v.x, row);
+    const double r = bb - spmv_at<double>(g, st, v.x, ic, jc, kc, row);
     v.r0[row] = r;
     v.r1[row] = r;
     v.p1[row] = r;
@@ -43,7 +77,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_setup64(Geo g, Stencil<double> 
     acc[1] += r * r;
   }
   double out[2];
-  if (grid_sum<2>(acc, part, &sc->cnt[0], out) && threadIdx.x == 0) {
+  if (grid_sum<2>(acc, part, &sc->cnt[0], out) && lin_tid() == 0) {
     sc->timestep += 1;
     sc->norm0 = sqrt(out[0]);
     sc->rho = out[1];
@@ -55,109 +89,199 @@ __global__ void __launch_bounds__(kBlock) k_bicg_setup64(Geo g, Stencil<double> 
   }
 }
 
-// ---- one iteration ----
+// ---- FP64 iteration: five kernels ----
 // K1: ap = A p1, alpha = rho / <ap, r0>
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_bicg_ap(Geo g, Stencil<T> st, KrylovVecs<T> v, double *part,
-                                                     SolverScal *sc) {
+__global__ void __launch_bounds__(kBlock) k64_ap(Geo g, Stencil<double> st, KrylovVecs<double> v, double *part,
+                                                 SolverScal *sc) {
   if (sc->done) return;
-  typename AccFor<T>::type acc;
-  GRID_STRIDE(row, g.ncell) {
-    const T y = spmv<T>(g, st, v.p1, row);
+  double a[1] = {0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double y = spmv_at<double>(g, st, v.p1, ic, jc, kc, row);
     v.ap[row] = y;
-    acc.add(y * v.r0[row]);
+    a[0] += y * v.r0[row];
   }
-  double a[1] = {acc.get()}, out[1];
-  if (grid_sum<1>(a, part, &sc->cnt[1], out) && threadIdx.x == 0) sc->alpha = sc->rho / out[0];
+  double out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
 }
 
 // K2: s = r1 - alpha ap
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_bicg_s(Geo g, KrylovVecs<T> v, const SolverScal *sc) {
+__global__ void __launch_bounds__(kBlock) k64_s(Geo g, KrylovVecs<double> v, const SolverScal *sc) {
   if (sc->done) return;
-  const T a = (T)sc->alpha;
-  GRID_STRIDE(row, g.ncell) v.s[row] = v.r1[row] - a * v.ap[row];
+  const double a = sc->alpha;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.s[row] = v.r1[row] - a * v.ap[row];
+  }
 }
 
 // K3: as = A s, omega = <as, s> / <as, as>
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_bicg_as(Geo g, Stencil<T> st, KrylovVecs<T> v, double *part,
-                                                     SolverScal *sc) {
+__global__ void __launch_bounds__(kBlock) k64_as(Geo g, Stencil<double> st, KrylovVecs<double> v, double *part,
+                                                 SolverScal *sc) {
   if (sc->done) return;
-  typename AccFor<T>::type a0, a1;
-  GRID_STRIDE(row, g.ncell) {
-    const T y = spmv<T>(g, st, v.s, row);
+  double a[2] = {0.0, 0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double y = spmv_at<double>(g, st, v.s, ic, jc, kc, row);
     v.as[row] = y;
-    a0.add(y * v.s[row]);
-    a1.add(y * y);
+    a[0] += y * v.s[row];
+    a[1] += y * y;
   }
-  double a[2] = {a0.get(), a1.get()}, out[2];
-  if (grid_sum<2>(a, part, &sc->cnt[2], out) && threadIdx.x == 0) {
-    double w = out[0] / out[1];
-    // FP32 inner solve only: when s has vanished (<as,as> = 0) the half step already
-    // solved the system; omega = 0 makes K4 take x += alpha p1, r1 = s and stop, where
-    // the unguarded formula would give 0/0.  The FP64 path keeps the reference's formula.
-    if (sizeof(T) == 4 && !(out[1] > 0.0 && isfinite(w))) w = 0.0;
-    sc->omega = w;
+  double out[2];
+  if (grid_sum<2>(a, part, &sc->cnt[2], out) && lin_tid() == 0) sc->omega = out[0] / out[1];
+}
+
+// stop test, beta and restart decision of bicgstabRe2.hpp:128-176 (last block, thread 0);
+// n2 = ||r1||^2, rr = <r1, r0>
+template <bool FP32>
+__device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, double rr) {
+  const double relres = sqrt(n2) / sc->norm0;
+  sc->relres = relres;
+  if (FP32 && relres < sc->best) sc->best = relres;
+  if (relres < sc->tol) {  // :129
+    sc->done = 1;
+  } else if (FP32 && !isfinite(relres)) {  // FP32 inner solve broke down
+    sc->done = 1;
+    sc->status = CFDGB_ENAN;
+  } else if (FP32 && sc->iter > 16 && relres > 1e3 * sc->best) {
+    // FP32 inner solve diverging (rounding has destroyed the bi-orthogonality): stop;
+    // the FP64 outer residual decides what to keep
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+  } else if (sc->iter >= sc->maxit) {  // :133
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+  } else {  // :156-176
+    const double rho_old = sc->rho;
+    sc->rho = rr;
+    sc->beta = (sc->alpha / sc->omega) * (sc->rho / rho_old);
+    sc->restart = !(sc->timestep < 10 || fabs(rho_old) > sc->restart_thr);
+    if (FP32 && !(isfinite(sc->beta) && sc->omega != 0.0 && sc->rho != 0.0)) {
+      // Lanczos breakdown of the FP32 inner solve: restart from the current residual
+      // with a fresh shadow vector r0 = r1, so rho = <r1, r1>
+      sc->restart = 1;
+      sc->rho = n2;
+    }
+    sc->iter += 1;
   }
 }
 
-// K4: x += alpha p1 + omega s; r1 = s - omega as; stop test; beta and restart decision
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_bicg_xr(Geo g, KrylovVecs<T> v, double *part, SolverScal *sc) {
+// K4: x += alpha p1 + omega s; r1 = s - omega as; ||r1||^2, <r1, r0>
+__global__ void __launch_bounds__(kBlock) k64_xr(Geo g, KrylovVecs<double> v, double *part, SolverScal *sc) {
   if (sc->done) return;
-  const T a = (T)sc->alpha, w = (T)sc->omega;
-  typename AccFor<T>::type n2, rr;
-  GRID_STRIDE(row, g.ncell) {
-    const T s = v.s[row];
-    v.x[row] += a * v.p1[row] + w * s;
-    const T r1 = s - w * v.as[row];
+  const double a = sc->alpha, w = sc->omega;
+  double acc[2] = {0.0, 0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double s = v.s[row];
+    v.x[row] = fma(w, s, fma(a, v.p1[row], v.x[row]));  // two FP64 ops instead of three
+    const double r1 = fma(-w, v.as[row], s);
+    v.r1[row] = r1;
+    acc[0] += r1 * r1;
+    acc[1] += r1 * v.r0[row];
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<false>(sc, out[0], out[1]);
+}
+
+// K5: p1 = r1 + beta (p1 - omega ap), or restart r0 = p1 = r1
+__global__ void __launch_bounds__(kBlock) k64_p(Geo g, KrylovVecs<double> v, const SolverScal *sc) {
+  if (sc->done) return;
+  const double b = sc->beta, w = sc->omega;
+  const bool rst = sc->restart != 0;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double r1 = v.r1[row];
+    if (rst) {
+      v.r0[row] = r1;
+      v.p1[row] = r1;
+    } else {
+      v.p1[row] = r1 + b * (v.p1[row] - w * v.ap[row]);
+    }
+  }
+}
+
+// ---- FP32 iteration: three fused kernels; p and ap are double-buffered by parity ----
+struct Vec32 {
+  float *x, *r0, *r1, *s, *as, *p[2], *ap[2];
+};
+
+// p_new = r1 + beta (p_old - omega ap_old) (or r1 on restart, which also sets r0 = r1),
+// evaluated at the stencil points; ap_new = A p_new; alpha = rho / <ap_new, r0>
+__global__ void __launch_bounds__(kBlock) k32_pap(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+                                                  SolverScal *sc) {
+  if (sc->done) return;
+  const float b = (float)sc->beta, w = (float)sc->omega;
+  const bool rst = sc->restart != 0;
+  const float *__restrict__ po = v.p[parity];
+  const float *__restrict__ apo = v.ap[parity];
+  float *__restrict__ pn = v.p[parity ^ 1];
+  float *__restrict__ apn = v.ap[parity ^ 1];
+  const float *__restrict__ r1 = v.r1;
+  AccF acc;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    float pc;
+    const float y = rst ? stencil_apply<float>(g, st, ic, jc, kc, row, [&](long long q) { return r1[q]; }, pc)
+                        : stencil_apply<float>(g, st, ic, jc, kc, row,
+                                               [&](long long q) { return r1[q] + b * (po[q] - w * apo[q]); }, pc);
+    pn[row] = pc;
+    apn[row] = y;
+    float r0 = v.r0[row];
+    if (rst) {
+      r0 = r1[row];
+      v.r0[row] = r0;
+    }
+    acc.add(y * r0);
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+// s = r1 - alpha ap at the stencil points; as = A s; omega = <as, s> / <as, as>
+__global__ void __launch_bounds__(kBlock) k32_sas(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+                                                  SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha;
+  const float *__restrict__ ap = v.ap[parity ^ 1];
+  const float *__restrict__ r1 = v.r1;
+  AccF a0, a1;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    float sc_;
+    const float y = stencil_apply<float>(g, st, ic, jc, kc, row, [&](long long q) { return r1[q] - a * ap[q]; }, sc_);
+    v.s[row] = sc_;
+    v.as[row] = y;
+    a0.add(y * sc_);
+    a1.add(y * y);
+  }
+  double acc[2] = {a0.get(), a1.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    // s has vanished: the half step solved the system; omega = 0 makes the next kernel
+    // take x += alpha p, r1 = s and stop instead of forming 0/0
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;
+    sc->omega = wv;
+  }
+}
+
+// x += alpha p + omega s; r1 = s - omega as; stop test, beta, restart
+__global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, int parity, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha, w = (float)sc->omega;
+  const float *__restrict__ p = v.p[parity ^ 1];
+  AccF n2, rr;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const float s = v.s[row];
+    v.x[row] = fmaf(w, s, fmaf(a, p[row], v.x[row]));
+    const float r1 = fmaf(-w, v.as[row], s);
     v.r1[row] = r1;
     n2.add(r1 * r1);
     rr.add(r1 * v.r0[row]);
   }
   double acc[2] = {n2.get(), rr.get()}, out[2];
-  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && threadIdx.x == 0) {
-    const double relres = sqrt(out[0]) / sc->norm0;
-    sc->relres = relres;
-    if (relres < sc->tol) {  // :129
-      sc->done = 1;
-    } else if (sizeof(T) == 4 && !isfinite(relres)) {  // FP32 inner solve broke down
-      sc->done = 1;
-      sc->status = CFDGB_ENAN;
-    } else if (sc->iter >= sc->maxit) {  // :133
-      sc->done = 1;
-      sc->status = CFDGB_ENOCONV;
-    } else {  // :156-176
-      const double rho_old = sc->rho;
-      sc->rho = out[1];
-      sc->beta = (sc->alpha / sc->omega) * (sc->rho / rho_old);
-      sc->restart = !(sc->timestep < 10 || fabs(rho_old) > sc->restart_thr);
-      if (sizeof(T) == 4 && !(isfinite(sc->beta) && sc->omega != 0.0 && sc->rho != 0.0)) {
-        // FP32 inner solve: Lanczos breakdown, restart from the current residual with a
-        // fresh shadow vector r0 = r1, so rho = <r1, r1>
-        sc->restart = 1;
-        sc->rho = out[0];
-      }
-      sc->iter += 1;
-    }
-  }
-}
-
-// K5: p1 = r1 + beta (p1 - omega ap), or restart r0 = p1 = r1
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_bicg_p(Geo g, KrylovVecs<T> v, const SolverScal *sc) {
-  if (sc->done) return;
-  const T b = (T)sc->beta, w = (T)sc->omega;
-  if (sc->restart) {
-    GRID_STRIDE(row, g.ncell) {
-      const T r1 = v.r1[row];
-      v.r0[row] = r1;
-      v.p1[row] = r1;
-    }
-  } else {
-    GRID_STRIDE(row, g.ncell) v.p1[row] = v.r1[row] + b * (v.p1[row] - w * v.ap[row]);
-  }
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
 }
 
 // bicgstabRe2.hpp:133-153: at the cap, NaN/Inf entries come from the previous solution;
@@ -166,16 +290,20 @@ __global__ void __launch_bounds__(kBlock) k_nan_replace(Geo g, double *x, const 
                                                         SolverScal *sc) {
   if (sc->status != CFDGB_ENOCONV) return;
   double bad[1] = {0.0}, out[1];
-  GRID_STRIDE(row, g.ncell) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
     const double xv = x[row];
     if (isnan(xv) || isinf(xv)) { x[row] = px1[row]; bad[0] += 1.0; }
   }
-  if (grid_sum<1>(bad, part, &sc->cnt[4], out) && threadIdx.x == 0)
+  if (grid_sum<1>(bad, part, &sc->cnt[4], out) && lin_tid() == 0)
     sc->restart = out[0] > (double)g.ncell * 0.1 ? 2 : 0;
 }
 __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const double *px2, const SolverScal *sc) {
   if (sc->status != CFDGB_ENOCONV || sc->restart != 2) return;
-  GRID_STRIDE(row, g.ncell) x[row] = px2[row];
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    x[row] = px2[row];
+  }
 }
 
 // ---- mixed precision: FP64 outer residual, FP32 inner solve on the scaled residual ----
@@ -184,15 +312,16 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
                                                         const double *__restrict__ x, double *__restrict__ r64,
                                                         double *part, StepScal *ss, SolverScal *inner, int first) {
   double acc[2] = {0.0, 0.0};
-  GRID_STRIDE(row, g.ncell) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
     const double bb = b[row];
-    const double r = bb - spmv<double>(g, st, x, row);
+    const double r = bb - spmv_at<double>(g, st, x, ic, jc, kc, row);
     r64[row] = r;
     acc[0] += r * r;
     acc[1] += bb * bb;
   }
   double out[2];
-  if (grid_sum<2>(acc, part, &ss->cnt[1], out) && threadIdx.x == 0) {
+  if (grid_sum<2>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
     if (first) ss->bnorm = sqrt(out[1]);
     ss->rnorm = sqrt(out[0]);
     ss->relres = ss->rnorm / ss->bnorm;
@@ -200,37 +329,41 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
   }
 }
 
-// inner set-up: e = 0, r0 = r1 = p1 = r64 / ||r|| in FP32, rho = <r0, r0>, norm0 = ||r0||
-__global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, KrylovVecs<float> v, const double *__restrict__ r64,
-                                                           double *part, SolverScal *sc) {
+// inner set-up: e = 0, r0 = r1 = r64 / ||r|| in FP32, rho = <r0, r0>, norm0 = ||r0||;
+// restart = 1 makes the first k32_pap take p = r1 (the reference's p1 = r0)
+__global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Vec32 v, const double *__restrict__ r64, double *part,
+                                                           SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
   AccF acc;
-  GRID_STRIDE(row, g.ncell) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
     const float r = (float)(r64[row] * inv);
     v.x[row] = 0.0f;
     v.r0[row] = r;
     v.r1[row] = r;
-    v.p1[row] = r;
     acc.add(r * r);
   }
   double a[1] = {acc.get()}, out[1];
-  if (grid_sum<1>(a, part, &sc->cnt[0], out) && threadIdx.x == 0) {
+  if (grid_sum<1>(a, part, &sc->cnt[0], out) && lin_tid() == 0) {
     sc->timestep += 1;
     sc->norm0 = sqrt(out[0]);
     sc->rho = out[0];
     sc->iter = 0;
     sc->done = 0;
     sc->status = 0;
-    sc->restart = 0;
+    sc->restart = 1;
     sc->relres = 0.0;
+    sc->best = 1.0;
   }
 }
 
-// x += ||r|| e
+// x += factor e: factor = ||r|| applies an inner correction, -||r|| takes it back
 __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict__ x, const float *__restrict__ e,
-                                                       const SolverScal *sc) {
-  const double s = sc->scale;
-  GRID_STRIDE(row, g.ncell) x[row] += s * (double)e[row];
+                                                       double s) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    x[row] += s * (double)e[row];
+  }
 }
 
 // ---- red-black SOR (FP64) on the exact Neumann rows ----
@@ -239,11 +372,10 @@ __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict_
 __global__ void __launch_bounds__(kBlock) k_rbsor(Geo g, Stencil<double> st, const double *__restrict__ b,
                                                    double *__restrict__ x, double omega, int color) {
   const long long nyz = (long long)g.nyc * g.nzc;
-  GRID_STRIDE(row, g.ncell) {
-    int ic, jc, kc;
-    row_cijk(row, g.nyc, g.nzc, ic, jc, kc);
+  FOR_CELLS(g) {
     if (((ic + jc + kc) & 1) != color) continue;
-    const double *c = st.c[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)];
+    const long long row = ROW(g);
+    const double *c = st.c[cls_of(g, ic, jc, kc)];
     double off = 0.0;
     if (ic > 0) off += c[0] * x[row - nyz];
     if (jc > 0) off += c[1] * x[row - g.nzc];
@@ -259,12 +391,13 @@ __global__ void __launch_bounds__(kBlock) k_rbsor(Geo g, Stencil<double> st, con
 __global__ void __launch_bounds__(kBlock) k_residual_norm64(Geo g, Stencil<double> st, const double *__restrict__ b,
                                                              const double *__restrict__ x, double *part, StepScal *ss) {
   double acc[1] = {0.0};
-  GRID_STRIDE(row, g.ncell) {
-    const double r = b[row] - spmv<double>(g, st, x, row);
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double r = b[row] - spmv_at<double>(g, st, x, ic, jc, kc, row);
     acc[0] += r * r;
   }
   double out[1];
-  if (grid_sum<1>(acc, part, &ss->cnt[2], out) && threadIdx.x == 0) {
+  if (grid_sum<1>(acc, part, &ss->cnt[2], out) && lin_tid() == 0) {
     ss->rnorm = sqrt(out[0]);
     ss->relres = ss->rnorm / ss->bnorm;
   }
@@ -272,71 +405,79 @@ __global__ void __launch_bounds__(kBlock) k_residual_norm64(Geo g, Stencil<doubl
 
 __global__ void __launch_bounds__(kBlock) k_vec_norm64(Geo g, const double *__restrict__ b, double *part, StepScal *ss) {
   double acc[1] = {0.0};
-  GRID_STRIDE(row, g.ncell) acc[0] += b[row] * b[row];
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    acc[0] += b[row] * b[row];
+  }
   double out[1];
-  if (grid_sum<1>(acc, part, &ss->cnt[3], out) && threadIdx.x == 0) ss->bnorm = sqrt(out[0]);
+  if (grid_sum<1>(acc, part, &ss->cnt[3], out) && lin_tid() == 0) ss->bnorm = sqrt(out[0]);
 }
 
 // ---- launchers ----
-void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
-                         const double *b, double *px1, double *px2, double *part, SolverScal *sc) {
-  k_bicg_setup64<<<nblk, kBlock, 0, s>>>(g, st, v, b, px1, px2, part, sc);
+static inline dim3 cgrid(const Geo &g) { return dim3(g.lgx, g.lgy, g.lgz); }
+static inline dim3 cblock(const Geo &g) { return dim3(g.lbx, g.lby, 1); }
+static inline Vec32 v32(const KrylovVecs<float> &v, float *const p2[2], float *const ap2[2]) {
+  Vec32 o;
+  o.x = v.x; o.r0 = v.r0; o.r1 = v.r1; o.s = v.s; o.as = v.as;
+  o.p[0] = p2[0]; o.p[1] = p2[1]; o.ap[0] = ap2[0]; o.ap[1] = ap2[1];
+  return o;
 }
 
-template <typename T>
-void launch_bicg_part(cudaStream_t s, int part, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v,
-                      double *part_buf, SolverScal *sc) {
+void launch_bicg_setup64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
+                         const double *b, double *px1, double *px2, double *part, SolverScal *sc) {
+  k_bicg_setup64<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, b, px1, px2, part, sc);
+}
+
+void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
+                        double *part_buf, SolverScal *sc) {
   switch (part) {
-    case 0: k_bicg_ap<T><<<nblk, kBlock, 0, s>>>(g, st, v, part_buf, sc); break;
-    case 1: k_bicg_s<T><<<nblk, kBlock, 0, s>>>(g, v, sc); break;
-    case 2: k_bicg_as<T><<<nblk, kBlock, 0, s>>>(g, st, v, part_buf, sc); break;
-    case 3: k_bicg_xr<T><<<nblk, kBlock, 0, s>>>(g, v, part_buf, sc); break;
-    default: k_bicg_p<T><<<nblk, kBlock, 0, s>>>(g, v, sc); break;
+    case 0: k64_ap<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    case 1: k64_s<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+    case 2: k64_as<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    case 3: k64_xr<<<cgrid(g), cblock(g), 0, s>>>(g, v, part_buf, sc); break;
+    default: k64_p<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
   }
 }
-template void launch_bicg_part<double>(cudaStream_t, int, int, const Geo &, const Stencil<double> &,
-                                       KrylovVecs<double>, double *, SolverScal *);
-template void launch_bicg_part<float>(cudaStream_t, int, int, const Geo &, const Stencil<float> &,
-                                      KrylovVecs<float>, double *, SolverScal *);
 
-template <typename T>
-void launch_bicg_iter(cudaStream_t s, int nblk, const Geo &g, const Stencil<T> &st, KrylovVecs<T> v, double *part,
-                      SolverScal *sc) {
-  for (int q = 0; q < 5; ++q) launch_bicg_part<T>(s, q, nblk, g, st, v, part, sc);
+void launch_bicg32_part(cudaStream_t s, int part, int parity, const Geo &g, const Stencil<float> &st,
+                        KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
+                        SolverScal *sc) {
+  const Vec32 w = v32(v, p2, ap2);
+  switch (part) {
+    case 0: k32_pap<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
+    case 1: k32_sas<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
+    default: k32_xr<<<cgrid(g), cblock(g), 0, s>>>(g, w, parity, part_buf, sc); break;
+  }
 }
-template void launch_bicg_iter<double>(cudaStream_t, int, const Geo &, const Stencil<double> &, KrylovVecs<double>,
-                                       double *, SolverScal *);
-template void launch_bicg_iter<float>(cudaStream_t, int, const Geo &, const Stencil<float> &, KrylovVecs<float>,
-                                      double *, SolverScal *);
 
-void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1, const double *px2,
+void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const double *px1, const double *px2,
                            double *part, SolverScal *sc) {
-  k_nan_replace<<<nblk, kBlock, 0, s>>>(g, x, px1, part, sc);
-  k_nan_restore<<<nblk, kBlock, 0, s>>>(g, x, px2, sc);
+  k_nan_replace<<<cgrid(g), cblock(g), 0, s>>>(g, x, px1, part, sc);
+  k_nan_restore<<<cgrid(g), cblock(g), 0, s>>>(g, x, px2, sc);
 }
 
-void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b,
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first) {
-  k_residual64<<<nblk, kBlock, 0, s>>>(g, st, b, x, r64, part, ss, inner, first);
+  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, b, x, r64, part, ss, inner, first);
 }
-void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, KrylovVecs<float> v, const double *r64,
-                          double *part, SolverScal *sc) {
-  k_inner_setup32<<<nblk, kBlock, 0, s>>>(g, v, r64, part, sc);
+void launch_inner_setup32(cudaStream_t s, int, const Geo &g, KrylovVecs<float> v, float *const p2[2],
+                          float *const ap2[2], const double *r64, double *part, SolverScal *sc) {
+  k_inner_setup32<<<cgrid(g), cblock(g), 0, s>>>(g, v32(v, p2, ap2), r64, part, sc);
 }
-void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, const SolverScal *sc) {
-  k_correct64<<<nblk, kBlock, 0, s>>>(g, x, e, sc);
+void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor) {
+  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, factor);
 }
-void launch_rbsor_sweep(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
-                        double *x, double omega) {
-  k_rbsor<<<nblk, kBlock, 0, s>>>(g, st, b, x, omega, 0);
-  k_rbsor<<<nblk, kBlock, 0, s>>>(g, st, b, x, omega, 1);
+void launch_rbsor_sweep(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b, double *x,
+                        double omega) {
+  k_rbsor<<<cgrid(g), cblock(g), 0, s>>>(g, st, b, x, omega, 0);
+  k_rbsor<<<cgrid(g), cblock(g), 0, s>>>(g, st, b, x, omega, 1);
 }
-void launch_residual_norm64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+void launch_residual_norm64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b,
                             const double *x, double *part, StepScal *ss) {
-  k_residual_norm64<<<nblk, kBlock, 0, s>>>(g, st, b, x, part, ss);
+  k_residual_norm64<<<cgrid(g), cblock(g), 0, s>>>(g, st, b, x, part, ss);
 }
-void launch_vec_norm64(cudaStream_t s, int nblk, const Geo &g, const double *b, double *part, StepScal *ss) {
-  k_vec_norm64<<<nblk, kBlock, 0, s>>>(g, b, part, ss);
+void launch_vec_norm64(cudaStream_t s, int, const Geo &g, const double *b, double *part, StepScal *ss) {
+  k_vec_norm64<<<cgrid(g), cblock(g), 0, s>>>(g, b, part, ss);
 }
 
 }  // namespace cfdgb

@@ -245,20 +245,19 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
 // keep its one-thread order (x faces, then y, then z; each later phase reads cells the
 // earlier ones wrote), each fused with the matching part of BC_staggered_copy
 // (updateBC.hpp:6-108), whose cells no later phase touches.  bc: Dir/Num table
-// (FLOWpassing.hpp:6-40) as bc[face][comp] = {Dir, Num}.
+// (FLOWpassing.hpp:6-40, BcTable).  inlet: optional per-(j,k) inlet velocity taking the
+// place of Dir[0][0] (all 1.0 reproduces the reference).
 
-struct BcTable {
-  double dir[6][3], num[6][3];
-};
-
-__global__ void __launch_bounds__(kBlock) k_bc_x(Geo g, BcTable t, double *u, double *v, double *w, double *p,
-                                                 double *us, double *vs, double *ws, int do_main) {
+__global__ void __launch_bounds__(kBlock) k_bc_x(Geo g, BcTable t, const double *__restrict__ inlet, double *u,
+                                                 double *v, double *w, double *p, double *us, double *vs, double *ws,
+                                                 int do_main) {
   const int nyc = g.nyc, nzc = g.nzc, nx = g.nx;
   for (int q = blockIdx.x * kBlock + threadIdx.x; q < nyc * nzc; q += gridDim.x * kBlock) {
     const int j = q / nzc + 2, k = q % nzc + 2;
     auto I = [&](int i) { return pidx(g, i, j, k); };
     if (do_main) {
-      u[I(1)] = u[I(0)] = t.dir[0][0] + t.num[0][0] * u[I(2)];
+      const double din = inlet ? inlet[q] : t.dir[0][0];
+      u[I(1)] = u[I(0)] = din + t.num[0][0] * u[I(2)];
       v[I(1)] = v[I(0)] = t.dir[0][1] * 2. + (2.0 * t.num[0][1] - 1.0) * v[I(2)];
       w[I(1)] = w[I(0)] = t.dir[0][2] * 2. + (2.0 * t.num[0][2] - 1.0) * w[I(2)];
       u[I(nx - 1)] = u[I(nx - 2)] = u[I(nx - 3)] = t.dir[1][0] + t.num[1][0] * u[I(nx - 4)];
@@ -407,20 +406,11 @@ void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, d
                             const double *wi, double *part, StepScal *ss) {
   k_update_uf_exact<<<nblk, kBlock, 0, s>>>(g, dt, lz, eta, p, us, vs, ws, u3, v3, w3, f, ui, vi, wi, part, ss);
 }
-static BcTable flowpassing_table() {
-  // inc/BoundaryCondition/FLOWpassing.hpp:6-40
-  BcTable t{};
-  for (int f = 0; f < 6; ++f)
-    for (int c = 0; c < 3; ++c) { t.dir[f][c] = 0.0; t.num[f][c] = 1.0; }
-  t.dir[0][0] = 1.0;
-  t.num[0][0] = t.num[0][1] = t.num[0][2] = 0.0;
-  return t;
-}
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
-               double *vs, double *ws, int do_main) {
+               double *vs, double *ws, int do_main, const double *inlet) {
   const BcTable t = flowpassing_table();
   auto blocks = [](long long n) { return (int)((n + kBlock - 1) / kBlock < 1024 ? (n + kBlock - 1) / kBlock : 1024); };
-  k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
+  k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, inlet, u, v, w, p, us, vs, ws, do_main);
   k_bc_y<<<blocks((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
   k_bc_z<<<blocks((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
 }

@@ -110,6 +110,26 @@ int cfdgb_set_eta(cfdgb_ctx *ctx, const double *eta);
  * nsteps entries.  Returns the worst status over the steps. */
 int cfdgb_step(cfdgb_ctx *ctx, int nsteps, cfdgb_step_stats *stats);
 
+/* ---- discrete adjoint (no reference counterpart: the reference has no gradients) ----
+ * Objective J: drag coefficient averaged over steps first..last of an nsteps run that
+ * starts from the state cfdgb_init_fields set.  cfdgb_forward runs it (FP64 context, a
+ * BiCGSTAB solver), keeping a checkpoint (T0, p, solver warm start and scalars) every
+ * ckpt_every steps, and returns J.  cfdgb_backward sweeps the steps in reverse,
+ * recomputing each checkpoint window forward first, and returns dJ/d(inlet u profile)
+ * (ny*nz values, the inlet ghost value of BC_staggered_main's face 0 per (j,k)) and
+ * dJ/d(solid fraction eta) (padded field).  Memory: (5 + 4*ckpt_every) padded FP64 fields
+ * beyond the forward ones. */
+typedef struct cfdgb_objective {
+  int nsteps;      /* forward steps */
+  int first, last; /* drag averaged over these steps (1-based, inclusive) */
+  int ckpt_every;  /* checkpoint interval K */
+} cfdgb_objective;
+/* Inlet u per (j,k) of the inlet face (ny*nz, k fastest), replacing the reference's
+ * constant Dir[0][0] = 1 (FLOWpassing.hpp:6); NULL restores the constant. */
+int cfdgb_set_inlet(cfdgb_ctx *ctx, const double *u_in);
+int cfdgb_forward(cfdgb_ctx *ctx, const cfdgb_objective *obj, double *J);
+int cfdgb_backward(cfdgb_ctx *ctx, double *dJ_dinlet, double *dJ_deta);
+
 /* ---- instrumentation (no reference counterpart: the reference times phases with
  * std::chrono stopwatches, inc/profiling/STL_clock.hpp:8) ---- */
 /* Kernel timing: while enabled, every kernel the step driver launches is bracketed by a

@@ -210,12 +210,13 @@ static const double kNum[6][3] = {{0, 0, 0}, {1, 1, 1}, {1, 1, 1},
 
 /* inc/BoundaryCondition/Boundary_Condition.hpp:37-176 (BC_staggered_main), in the
  * order one thread executes it: faces 0..5 for u,v,w, then pressure. */
-void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p) {
+static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet) {
   const int nx = g->nx, ny = g->ny, nz = g->nz;
   double *vel[3] = {u, v, w};
   for (int j = GC; j < ny - GC; ++j)
     for (int k = GC; k < nz - GC; ++k) { /* BC_0 */
-      u[IC(g, 1, j, k)] = u[IC(g, 0, j, k)] = kDir[0][0] + kNum[0][0] * u[IC(g, 2, j, k)];
+      const double din = inlet ? inlet[(j - GC) * g->nzc + (k - GC)] : kDir[0][0];
+      u[IC(g, 1, j, k)] = u[IC(g, 0, j, k)] = din + kNum[0][0] * u[IC(g, 2, j, k)];
       v[IC(g, 1, j, k)] = v[IC(g, 0, j, k)] =
           kDir[0][1] * 2. + (2.0 * kNum[0][1] - 1.0) * v[IC(g, 2, j, k)];
       w[IC(g, 1, j, k)] = w[IC(g, 0, j, k)] =
@@ -281,6 +282,10 @@ void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p) {
       p[IC(g, i, j, 1)] = p[IC(g, i, j, 0)] = p[IC(g, i, j, 2)];
       p[IC(g, i, j, nz - 2)] = p[IC(g, i, j, nz - 1)] = p[IC(g, i, j, nz - 3)];
     }
+}
+
+void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p) {
+  bc_main_in(g, u, v, w, p, NULL);
 }
 
 /* inc/BoundaryCondition/updateBC.hpp:6-108 (BC_staggered_copy) */
@@ -676,6 +681,12 @@ double og_force_sum(const og_grid *g, const double *f, int dir) {
 int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
            double omega, double *u, double *v, double *w, double *p, double *eta,
            double *stats) {
+  return og_run_ex(g, steps, Re, dt, tol, solver, omega, u, v, w, p, eta, stats, NULL, NULL);
+}
+
+int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
+              double omega, double *u, double *v, double *w, double *p, double *eta,
+              double *stats, const double *eta_in, const double *inlet) {
   const long tot = og_padded(g), n = og_cells(g);
   const double nu = 1.0 / Re; /* 0_1_SimulationVariable.hpp:26-31 */
   double *us = dalloc(tot), *vs = dalloc(tot), *ws = dalloc(tot);
@@ -687,11 +698,15 @@ int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int so
   memcpy(us, u, sizeof(double) * tot); memcpy(u3, u, sizeof(double) * tot);
   memcpy(vs, v, sizeof(double) * tot); memcpy(v3, v, sizeof(double) * tot);
   memcpy(ws, w, sizeof(double) * tot); memcpy(w3, w, sizeof(double) * tot);
-  og_bc_main(g, u, v, w, p);
+  bc_main_in(g, u, v, w, p, inlet);
   og_bc_copy(g, u, v, w, us, vs, ws);
   if (solver == 0 || solver == 1) og_bicg_init(&bs, g, solver, tol);
-  memset(eta, 0, sizeof(double) * tot);
-  og_dfib_cylinder_z(g, eta);
+  if (eta_in) {
+    memcpy(eta, eta_in, sizeof(double) * tot);
+  } else {
+    memset(eta, 0, sizeof(double) * tot);
+    og_dfib_cylinder_z(g, eta);
+  }
   for (int s = 1; s <= steps; ++s) {
     og_convection_diffusion(g, dt, nu, u, v, w, us, vs, ws);
     int iters = 0;
@@ -709,7 +724,7 @@ int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int so
     memcpy(u, u3, sizeof(double) * tot); /* copyVel */
     memcpy(v, v3, sizeof(double) * tot);
     memcpy(w, w3, sizeof(double) * tot);
-    og_bc_main(g, u, v, w, p);
+    bc_main_in(g, u, v, w, p, inlet);
     og_bc_copy(g, u, v, w, us, vs, ws);
     if (stats) {
       stats[4 * (s - 1) + 0] = iters;

@@ -77,6 +77,12 @@ double og_force_sum(const og_grid *g, const double *f, int dir);
 int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
            double omega, double *u, double *v, double *w, double *p, double *eta,
            double *stats);
+/* og_run with the two parameters of the adjoint exposed: eta_in (padded solid fraction,
+ * NULL: DFIB_CylinderZ) and inlet (ny*nz inlet u per (j,k), NULL: the constant 1 of
+ * FLOWpassing.hpp:6). */
+int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
+              double omega, double *u, double *v, double *w, double *p, double *eta,
+              double *stats, const double *eta_in, const double *inlet);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,107 @@
+"""Discrete adjoint of the projection step (cfdgb_forward / cfdgb_backward) against
+central finite differences: of the CUDA forward step itself, and of the reference
+restatement on the CPU (the oracle, same parameters injected).
+
+Objective: drag averaged over steps 8..12 of a 12-step run on a 32x16x4 grid (checkpoint
+every 5 steps, so one window is partial), Poisson solved to 1e-12 so that the FD
+quotients (eps = 1e-6) resolve the derivative to ~1e-6 of its size."""
+import numpy as np
+import pytest
+
+import cfd_nssolver_forhpc_flowpassingcylinder_gb300 as cg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASE = dict(nx=32, ny=16, nz=4, lx=8.0, ly=4.0, lz=1.0, cx=2.0, cy=2.0, Re=100.0, dt=0.005)
+NSTEPS, FIRST, LAST, K = 12, 8, 12, 5
+TOL = 1e-12
+EPS = 1e-6
+
+
+def _J(s, inlet=None, eta=None):
+    s.init_fields()
+    s.set_inlet(inlet)
+    if eta is not None:
+        s.set_eta(eta)
+    return s.forward(NSTEPS, FIRST, LAST, K)
+
+
+@pytest.fixture(scope="module")
+def adj():
+    s = cg.Solver(tol=TOL, **CASE)
+    eta0 = s.get_eta()
+    J0 = _J(s, eta=eta0)
+    g_in, g_eta = s.backward()
+    yield s, eta0, J0, g_in, g_eta
+    s.close()
+
+
+def _fd(s, base_inlet, eta0, d_in=None, d_eta=None):
+    ip = None if d_in is None else base_inlet + EPS * d_in
+    im = None if d_in is None else base_inlet - EPS * d_in
+    ep = eta0 if d_eta is None else eta0 + EPS * d_eta
+    em = eta0 if d_eta is None else eta0 - EPS * d_eta
+    return (_J(s, ip, ep) - _J(s, im, em)) / (2 * EPS)
+
+
+def test_gradients_are_finite_and_nonzero(adj):
+    s, eta0, J0, g_in, g_eta = adj
+    assert np.isfinite(J0) and J0 > 0
+    assert np.all(np.isfinite(g_in)) and np.abs(g_in).max() > 0
+    assert np.all(np.isfinite(g_eta)) and np.abs(g_eta).max() > 0
+    # eta enters only through interior faces
+    assert np.abs(g_eta[:2]).max() == 0 and np.abs(g_eta[-2:]).max() == 0
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_inlet_gradient_matches_central_fd(adj, seed):
+    s, eta0, J0, g_in, g_eta = adj
+    d = np.random.default_rng(seed).standard_normal(g_in.shape)
+    fd = _fd(s, np.ones(g_in.shape), eta0, d_in=d)
+    ad = float(np.sum(g_in * d))
+    assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-9, (ad, fd)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_eta_gradient_matches_central_fd(adj, seed):
+    s, eta0, J0, g_in, g_eta = adj
+    band = (eta0 > 0) & (eta0 < 1)
+    band[:2] = band[-2:] = False
+    band[:, :2] = band[:, -2:] = False
+    band[:, :, :2] = band[:, :, -2:] = False
+    d = np.where(band, np.random.default_rng(100 + seed).standard_normal(eta0.shape), 0.0)
+    fd = _fd(s, None, eta0, d_eta=d)
+    ad = float(np.sum(g_eta * d))
+    assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-9, (ad, fd)
+
+
+def test_against_fd_of_the_cpu_reference_restatement(adj):
+    """The same objective computed by the oracle (reference restatement, CPU), finite-
+    differenced in one inlet and one eta direction, against the GPU adjoint."""
+    s, eta0, J0, g_in, g_eta = adj
+    g = O.Grid(CASE["nx"], CASE["ny"], CASE["nz"], CASE["lx"], CASE["ly"], CASE["lz"], CASE["cx"])
+
+    def J_cpu(inlet=None, eta=None):
+        r = O.run(g, NSTEPS, CASE["Re"], CASE["dt"], TOL, "spe", eta_in=eta, inlet=inlet)
+        return float(np.mean(r["cd"][FIRST - 1:LAST]))
+
+    assert abs(J_cpu() - J0) <= 1e-10 * abs(J0)
+    rng = np.random.default_rng(7)
+    d = rng.standard_normal(g_in.shape)
+    one = np.ones(g_in.shape)
+    fd = (J_cpu(inlet=one + EPS * d) - J_cpu(inlet=one - EPS * d)) / (2 * EPS)
+    assert abs(float(np.sum(g_in * d)) - fd) <= 1e-4 * abs(fd) + 1e-9
+    band = (eta0 > 0) & (eta0 < 1)
+    de = np.where(band, rng.standard_normal(eta0.shape), 0.0)
+    de[:2] = de[-2:] = 0
+    fd = (J_cpu(eta=eta0 + EPS * de) - J_cpu(eta=eta0 - EPS * de)) / (2 * EPS)
+    assert abs(float(np.sum(g_eta * de)) - fd) <= 1e-4 * abs(fd) + 1e-9
+
+
+def test_backward_is_repeatable(adj):
+    s, eta0, J0, g_in, g_eta = adj
+    _J(s, eta=eta0)
+    g_in2, g_eta2 = s.backward()
+    np.testing.assert_allclose(g_in2, g_in, rtol=1e-12, atol=1e-14 * np.abs(g_in).max())
+    np.testing.assert_allclose(g_eta2, g_eta, rtol=1e-12, atol=1e-14 * np.abs(g_eta).max())
