@@ -61,6 +61,33 @@ KERNEL_WORDS = {
 }
 
 
+# FP64 flops per interior cell and launch of the FP64 iteration kernels (an FMA counts 2):
+# SpMV 1 mul + 6 FMA, each dot 1 FMA, each axpy-like update 1 FMA per term
+KERNEL_FP64_FLOPS = {"bicg_ap64": 15, "bicg_s64": 2, "bicg_as64": 17, "bicg_xr64": 10, "bicg_p64": 4}
+
+
+def alu_peaks():
+    """FP64/FP32 FMA throughput of this GPU, measured by the package's cfdgb_fp_peak."""
+    exe = ROOT / "cfd_nssolver_forhpc_flowpassingcylinder_gb300" / "cfdgb_fp_peak"
+    try:
+        out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout
+        return json.loads(out.strip().splitlines()[-1])
+    except Exception as e:  # binary missing or no GPU
+        return {"error": str(e)}
+
+
+def alu_roofline(prof, cells, fp_peak):
+    ks = {k: v for k, v in prof.items() if k in KERNEL_FP64_FLOPS and v[1] > 0 and v[0] > 0}
+    if not ks or not fp_peak.get("fp64_tflops"):
+        return None
+    dom = max(ks, key=lambda k: ks[k][0])
+    ms, n = ks[dom]
+    achieved = KERNEL_FP64_FLOPS[dom] * cells / (ms / n / 1e3) / 1e12
+    return {"kernel": dom, "bound": "fp64", "achieved": round(achieved, 4), "peak": fp_peak["fp64_tflops"],
+            "unit": "TFLOP/s", "frac": round(achieved / fp_peak["fp64_tflops"], 4),
+            "peak_kind": "measured (cfdgb_fp_peak FMA chains)"}
+
+
 def peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -327,6 +354,7 @@ def main(argv=None):
     wl = args.workload
     traffic_file = ROOT / "profiles" / f"traffic_{wl}.json"
 
+    fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
         fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64")
     t64 = dist.max(fp64["ms"])
@@ -343,6 +371,7 @@ def main(argv=None):
                    "l2": "inputs ~1.5 GB > 129 MB L2, no flush"},
         "iters_per_step": iters64, "relres": max(r.relres for r in fp64["stats"]),
         "gpu_launches": fp64["launches"], "roofline": roof, "kernel_share": share,
+        "alu_roofline": alu_roofline(fp64["kernels"], cells, fp_peak), "fp_peaks": fp_peak,
         "clocks": clk.summary(),
     }
     if "mixed" in modes:

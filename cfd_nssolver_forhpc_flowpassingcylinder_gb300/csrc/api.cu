@@ -420,8 +420,11 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   static const bool trace = std::getenv("CFDGB_TRACE") != nullptr;
   double prev_rel = HUGE_VAL, applied = 0.0;
   bool finish64 = false;
+  const int jacf = jac ? 1 : 0;
   for (int o = 0;; ++o) {
-    L(c, K_RESID64, 1, [&] { launch_residual64(c->stream, c->nblk, c->g, st64, c->b, c->x, c->r64, c->part, c->ss, c->sc32, o == 0); });
+    L(c, K_RESID64, 1, [&] {
+      launch_residual64(c->stream, c->nblk, c->g, st64, jacf, c->b, c->x, c->r64, c->part, c->ss, c->sc32, o == 0);
+    });
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     const double rel = c->h_ss->relres, rnorm = c->h_ss->rnorm;
@@ -431,13 +434,16 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     if (rel < c->cfg.tol) break;
     if (!std::isfinite(rel) || rel > 0.5 * prev_rel || o >= c->cfg.max_outer) {
       if (!(rel <= prev_rel) && applied != 0.0)
-        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -applied); });
+        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -applied, c->ss); });
       finish64 = true;
       break;
     }
     const double itol = std::min(0.5, std::max(c->cfg.inner_tol, 0.2 * c->cfg.tol / rel));
     TRY(set_solver_params(c, c->sc32, itol, c->cfg.maxit));
-    L(c, K_SETUP32, 1, [&] { launch_inner_setup32(c->stream, c->nblk, c->g, c->k32, c->p32, c->ap32, c->r64, c->part, c->sc32); });
+    L(c, K_SETUP32, 1, [&] {
+      launch_inner_setup32(c->stream, c->nblk, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->part,
+                           c->sc32);
+    });
     SolverScal r;
     TRY(run_chunks(c, true, &r));
     if (trace)
@@ -451,7 +457,10 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     }
     applied = rnorm;
     prev_rel = rel;
-    L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, applied); });
+    L(c, K_CORRECT64, 2, [&] {
+      launch_sum32(c->stream, c->g, c->k32.x, c->part, c->ss);
+      launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, applied, c->ss);
+    });
   }
   if (finish64) {
     TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
@@ -529,7 +538,9 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->tol = 1e-8;
   c->maxit = 5000;
   c->omega = 1.7;
-  c->inner_tol = 1e-3;
+  // FP32 inner solves stay well above their noise floor kappa * eps32 (~1e-3 on a 512-cell
+  // axis): each sweep asks for two decades
+  c->inner_tol = 1e-2;
   c->max_outer = 20;
   c->check_every = 10;
   c->dfib = 1;
@@ -598,7 +609,18 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.lgx = (cfg->nz + g.lbx - 1) / g.lbx;
   g.lgy = (cfg->ny + g.lby - 1) / g.lby;
   g.lgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.lgx * g.lgy)));
-  const int nblk3 = g.lgx * g.lgy * g.lgz;
+  int nblk3 = g.lgx * g.lgy * g.lgz;
+  // vectorised FP32 kernels: quads of four k cells per thread when nz % 4 == 0
+  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32")) {
+    const int nq = cfg->nz / 4;
+    g.vbx = 1;
+    while (g.vbx < nq && g.vbx < 32) g.vbx *= 2;
+    g.vby = kBlock / g.vbx;
+    g.vgx = (nq + g.vbx - 1) / g.vbx;
+    g.vgy = (cfg->ny + g.vby - 1) / g.vby;
+    g.vgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.vgx * g.vgy)));
+    nblk3 = std::max(nblk3, g.vgx * g.vgy * g.vgz);
+  }
   // fields and solver vectors
   double **pad[] = {&c->u, &c->v, &c->w, &c->us, &c->vs, &c->ws, &c->ui, &c->vi, &c->wi, &c->p, &c->eta};
   for (auto **q : pad)

@@ -29,6 +29,9 @@ struct Geo {
   // 3-D launch geometry of the solver kernels: blocks of (lbx along k) x (lby along j)
   // threads, grid (lgx, lgy) covering a (j, k) plane and lgz blocks striding over i
   int lbx, lby, lgx, lgy, lgz;
+  // geometry of the vectorised FP32 kernels (four consecutive k cells per thread; used
+  // when nzc % 4 == 0, else vbx = 0): vbx quads along k, vby rows along j, vgz over i
+  int vbx, vby, vgx, vgy, vgz;
 };
 
 // compact row -> padded (i,j,k)
@@ -97,6 +100,8 @@ struct SolverScal {
 struct StepScal {
   double cd, cl, fsum[2];
   double bnorm, rnorm, relres;
+  double rsum;  // MIXED: sum of the raw residual (its component along the operator's null space)
+  double esum;  // MIXED: sum of the inner correction e
   int nan_flag, pad;
   unsigned cnt[8];
 };

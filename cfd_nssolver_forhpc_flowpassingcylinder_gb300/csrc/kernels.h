@@ -50,11 +50,15 @@ void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, co
                            const double *px2, double *part, SolverScal *sc);
 
 // MIXED defect correction pieces
-void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
+void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first);
-void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, KrylovVecs<float> v, float *const p2[2],
-                          float *const ap2[2], const double *r64, double *part, SolverScal *sc);
-void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor);
+void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, int jacobi,
+                          KrylovVecs<float> v, float *const p2[2], float *const ap2[2], const double *r64,
+                          const StepScal *ss, double *part, SolverScal *sc);
+void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss);
+// x += factor (e - mean e), the mean taken from the preceding launch_sum32
+void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor,
+                      const StepScal *ss);
 
 // adjoint.cu (discrete adjoint of the FP64 step)
 void launch_adj_bc(cudaStream_t s, const Geo &g, double *lu, double *lv, double *lw, double *linlet);

@@ -143,7 +143,7 @@ __device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, doub
   } else if (FP32 && !isfinite(relres)) {  // FP32 inner solve broke down
     sc->done = 1;
     sc->status = CFDGB_ENAN;
-  } else if (FP32 && sc->iter > 16 && relres > 1e3 * sc->best) {
+  } else if (FP32 && sc->iter > 16 && relres > 1e2 * sc->best) {
     // FP32 inner solve diverging (rounding has destroyed the bi-orthogonality): stop;
     // the FP64 outer residual decides what to keep
     sc->done = 1;
@@ -284,6 +284,157 @@ __global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, int parity, dou
   if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
 }
 
+// ---- FP32 iteration, vectorised: four consecutive k cells per thread (nzc % 4 == 0) ----
+// One float4 load per vector and stencil point instead of four scalar loads; the k
+// neighbours inside the quad come from registers.  Dot partials stay FP32 over the few
+// dozen quads a thread owns and are added into the FP64 block/grid reduction once.
+#define FOR_QUADS(g)                                               \
+  const int kc0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);     \
+  const int kc = kc0; /* ROW(g) of the quad's first cell */        \
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y;            \
+  const bool on_ = (kc0 < (g).nzc) && (jc < (g).nyc);              \
+  for (int ic = blockIdx.z; on_ && ic < (g).nxc; ic += gridDim.z)
+
+struct F4 {
+  float v[4];
+};
+__device__ __forceinline__ F4 ld4(const float *p) {
+  const float4 t = *reinterpret_cast<const float4 *>(p);
+  return F4{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ void st4(float *p, const F4 &a) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+}
+
+// y = A f on the quad starting at (ic, jc, kc0); f4(q) gives four values at row q, f1(q)
+// one value; the quad's own values are returned in ctr.
+template <class F4f, class F1f>
+__device__ __forceinline__ F4 quad_apply(const Geo &g, const Stencil<float> &st, int ic, int jc, int kc0, long long row,
+                                         F4f &&f4, F1f &&f1, F4 &ctr) {
+  const long long nyz = (long long)g.nyc * g.nzc;
+  ctr = f4(row);
+  const bool hx0 = ic > 0, hx1 = ic < g.nxc - 1, hy0 = jc > 0, hy1 = jc < g.nyc - 1;
+  const F4 xm = hx0 ? f4(row - nyz) : F4{}, xp = hx1 ? f4(row + nyz) : F4{};
+  const F4 ym = hy0 ? f4(row - g.nzc) : F4{}, yp = hy1 ? f4(row + g.nzc) : F4{};
+  const float zl = kc0 > 0 ? f1(row - 1) : 0.0f, zr = kc0 + 4 < g.nzc ? f1(row + 4) : 0.0f;
+  const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
+  F4 y;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int kc = kc0 + q;
+    const float *c = st.c[cxy + axis_class(kc, g.nzc)];
+    const float zm = q == 0 ? zl : ctr.v[q - 1], zp = q == 3 ? zr : ctr.v[q + 1];
+    float s = 0.0f;
+    if (hx0) s += c[0] * xm.v[q];
+    if (hy0) s += c[1] * ym.v[q];
+    if (kc > 0) s += c[2] * zm;
+    s += c[3] * ctr.v[q];
+    if (kc < g.nzc - 1) s += c[4] * zp;
+    if (hy1) s += c[5] * yp.v[q];
+    if (hx1) s += c[6] * xp.v[q];
+    y.v[q] = s;
+  }
+  return y;
+}
+
+__global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+                                                   SolverScal *sc) {
+  if (sc->done) return;
+  const float b = (float)sc->beta, w = (float)sc->omega;
+  const bool rst = sc->restart != 0;
+  const float *__restrict__ po = v.p[parity];
+  const float *__restrict__ apo = v.ap[parity];
+  float *__restrict__ pn = v.p[parity ^ 1];
+  float *__restrict__ apn = v.ap[parity ^ 1];
+  const float *__restrict__ r1 = v.r1;
+  float acc = 0.0f;
+  FOR_QUADS(g) {
+    const long long row = ROW(g);
+    F4 pc, y;
+    if (rst) {
+      y = quad_apply(g, st, ic, jc, kc0, row, [&](long long q) { return ld4(r1 + q); },
+                     [&](long long q) { return r1[q]; }, pc);
+      st4(v.r0 + row, pc);
+    } else {
+      auto f4 = [&](long long q) {
+        const F4 r = ld4(r1 + q), p = ld4(po + q), a = ld4(apo + q);
+        F4 o;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) o.v[t] = fmaf(b, fmaf(-w, a.v[t], p.v[t]), r.v[t]);
+        return o;
+      };
+      auto f1 = [&](long long q) { return fmaf(b, fmaf(-w, apo[q], po[q]), r1[q]); };
+      y = quad_apply(g, st, ic, jc, kc0, row, f4, f1, pc);
+    }
+    st4(pn + row, pc);
+    st4(apn + row, y);
+    const F4 r0 = rst ? pc : ld4(v.r0 + row);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], r0.v[t], acc);
+  }
+  double a[1] = {(double)acc}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+                                                   SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha;
+  const float *__restrict__ ap = v.ap[parity ^ 1];
+  const float *__restrict__ r1 = v.r1;
+  float a0 = 0.0f, a1 = 0.0f;
+  FOR_QUADS(g) {
+    const long long row = ROW(g);
+    F4 sc4;
+    const F4 y = quad_apply(
+        g, st, ic, jc, kc0, row,
+        [&](long long q) {
+          const F4 r = ld4(r1 + q), p = ld4(ap + q);
+          F4 o;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) o.v[t] = fmaf(-a, p.v[t], r.v[t]);
+          return o;
+        },
+        [&](long long q) { return fmaf(-a, ap[q], r1[q]); }, sc4);
+    st4(v.s + row, sc4);
+    st4(v.as + row, y);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      a0 = fmaf(y.v[t], sc4.v[t], a0);
+      a1 = fmaf(y.v[t], y.v[t], a1);
+    }
+  }
+  double acc[2] = {(double)a0, (double)a1}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;  // see k32_sas
+    sc->omega = wv;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, int parity, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha, w = (float)sc->omega;
+  const float *__restrict__ p = v.p[parity ^ 1];
+  float n2 = 0.0f, rr = 0.0f;
+  FOR_QUADS(g) {
+    const long long row = ROW(g);
+    const F4 s = ld4(v.s + row), as = ld4(v.as + row), pp = ld4(p + row), r0 = ld4(v.r0 + row);
+    F4 x = ld4(v.x + row), r1;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      x.v[t] = fmaf(w, s.v[t], fmaf(a, pp.v[t], x.v[t]));
+      r1.v[t] = fmaf(-w, as.v[t], s.v[t]);
+      n2 = fmaf(r1.v[t], r1.v[t], n2);
+      rr = fmaf(r1.v[t], r0.v[t], rr);
+    }
+    st4(v.x + row, x);
+    st4(v.r1 + row, r1);
+  }
+  double acc[2] = {(double)n2, (double)rr}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
+}
+
 // bicgstabRe2.hpp:133-153: at the cap, NaN/Inf entries come from the previous solution;
 // if more than 10 % were bad, the whole vector comes from the one before.
 __global__ void __launch_bounds__(kBlock) k_nan_replace(Geo g, double *x, const double *px1, double *part,
@@ -308,10 +459,12 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
 
 // ---- mixed precision: FP64 outer residual, FP32 inner solve on the scaled residual ----
 // r64 = b - A x (FP64); ||r||, and ||b|| on the first sweep; inner scale = ||r||.
-__global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st, const double *__restrict__ b,
-                                                        const double *__restrict__ x, double *__restrict__ r64,
-                                                        double *part, StepScal *ss, SolverScal *inner, int first) {
-  double acc[2] = {0.0, 0.0};
+// jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose unscaled residual is r / jp.
+__global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st, int jacobi,
+                                                        const double *__restrict__ b, const double *__restrict__ x,
+                                                        double *__restrict__ r64, double *part, StepScal *ss,
+                                                        SolverScal *inner, int first) {
+  double acc[3] = {0.0, 0.0, 0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const double bb = b[row];
@@ -319,25 +472,34 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
     r64[row] = r;
     acc[0] += r * r;
     acc[1] += bb * bb;
+    // the unscaled residual's sum: its component along the operator's null space
+    acc[2] += jacobi ? r / st.c[cls_of(g, ic, jc, kc)][7] : r;
   }
-  double out[2];
-  if (grid_sum<2>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
+  double out[3];
+  if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
     if (first) ss->bnorm = sqrt(out[1]);
     ss->rnorm = sqrt(out[0]);
     ss->relres = ss->rnorm / ss->bnorm;
+    ss->rsum = out[2];
     inner->scale = ss->rnorm;
   }
 }
 
-// inner set-up: e = 0, r0 = r1 = r64 / ||r|| in FP32, rho = <r0, r0>, norm0 = ||r0||;
-// restart = 1 makes the first k32_pap take p = r1 (the reference's p1 = r0)
-__global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Vec32 v, const double *__restrict__ r64, double *part,
-                                                           SolverScal *sc) {
+// inner set-up: e = 0, r0 = r1 = (r64 - its null-space part) / ||r|| in FP32, rho =
+// <r0, r0>, norm0 = ||r0||; restart = 1 makes the first k32_pap take p = r1 (the
+// reference's p1 = r0).  Removing the null-space part (the mean of the unscaled residual;
+// for the Jacobi rows its image jp * mean) keeps the FP32 system consistent, so its
+// solution cannot drift along the constant mode.
+__global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Stencil<double> st, int jacobi, Vec32 v,
+                                                           const double *__restrict__ r64, const StepScal *ss,
+                                                           double *part, SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
+  const double m = ss->rsum / (double)g.ncell;
   AccF acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    const float r = (float)(r64[row] * inv);
+    const double wgt = jacobi ? st.c[cls_of(g, ic, jc, kc)][7] : 1.0;
+    const float r = (float)((r64[row] - m * wgt) * inv);
     v.x[row] = 0.0f;
     v.r0[row] = r;
     v.r1[row] = r;
@@ -357,12 +519,25 @@ __global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Vec32 v, const 
   }
 }
 
-// x += factor e: factor = ||r|| applies an inner correction, -||r|| takes it back
-__global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict__ x, const float *__restrict__ e,
-                                                       double s) {
+// sum of the inner correction e (FP64)
+__global__ void __launch_bounds__(kBlock) k_sum32(Geo g, const float *__restrict__ e, double *part, StepScal *ss) {
+  double acc[1] = {0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    x[row] += s * (double)e[row];
+    acc[0] += (double)e[row];
+  }
+  double out[1];
+  if (grid_sum<1>(acc, part, &ss->cnt[5], out) && lin_tid() == 0) ss->esum = out[0];
+}
+
+// x += factor (e - mean e): factor = ||r|| applies an inner correction, -||r|| takes it
+// back; the mean (the constant mode, which the pressure leaves free) is dropped
+__global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict__ x, const float *__restrict__ e,
+                                                       double s, const StepScal *ss) {
+  const double m = ss->esum / (double)g.ncell;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    x[row] += s * ((double)e[row] - m);
   }
 }
 
@@ -443,6 +618,15 @@ void launch_bicg32_part(cudaStream_t s, int part, int parity, const Geo &g, cons
                         KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
                         SolverScal *sc) {
   const Vec32 w = v32(v, p2, ap2);
+  if (g.vbx > 0) {  // vectorised path
+    const dim3 vg(g.vgx, g.vgy, g.vgz), vb(g.vbx, g.vby, 1);
+    switch (part) {
+      case 0: k32v_pap<<<vg, vb, 0, s>>>(g, st, w, parity, part_buf, sc); break;
+      case 1: k32v_sas<<<vg, vb, 0, s>>>(g, st, w, parity, part_buf, sc); break;
+      default: k32v_xr<<<vg, vb, 0, s>>>(g, w, parity, part_buf, sc); break;
+    }
+    return;
+  }
   switch (part) {
     case 0: k32_pap<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
     case 1: k32_sas<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
@@ -456,16 +640,21 @@ void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const d
   k_nan_restore<<<cgrid(g), cblock(g), 0, s>>>(g, x, px2, sc);
 }
 
-void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b,
+void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first) {
-  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, b, x, r64, part, ss, inner, first);
+  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, first);
 }
-void launch_inner_setup32(cudaStream_t s, int, const Geo &g, KrylovVecs<float> v, float *const p2[2],
-                          float *const ap2[2], const double *r64, double *part, SolverScal *sc) {
-  k_inner_setup32<<<cgrid(g), cblock(g), 0, s>>>(g, v32(v, p2, ap2), r64, part, sc);
+void launch_inner_setup32(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi,
+                          KrylovVecs<float> v, float *const p2[2], float *const ap2[2], const double *r64,
+                          const StepScal *ss, double *part, SolverScal *sc) {
+  k_inner_setup32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, part, sc);
 }
-void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor) {
-  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, factor);
+void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss) {
+  k_sum32<<<cgrid(g), cblock(g), 0, s>>>(g, e, part, ss);
+}
+void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor,
+                      const StepScal *ss) {
+  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, factor, ss);
 }
 void launch_rbsor_sweep(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b, double *x,
                         double omega) {
