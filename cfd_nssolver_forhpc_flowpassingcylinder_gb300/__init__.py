@@ -75,6 +75,9 @@ EXPORTS = {
     "cfdgb_set_inlet": (C.c_int, [C.c_void_p, _dp]),
     "cfdgb_forward": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
     "cfdgb_backward": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "cfdgb_poisson_solve_static": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                             C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.POINTER(C.c_int), _dp]),
     "cfdgb_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "cfdgb_reset_counters": (C.c_int, [C.c_void_p]),
     "cfdgb_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
