@@ -35,13 +35,17 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
-    # configs[1]-shaped workload: plain FP64 on the GPU at scale
+    # plain FP64 on the GPU at scale (8.4M cells)
     "c2": dict(nx=512, ny=256, nz=64, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0, Re=200.0, dt=0.002),
     # the reference's CPU-runnable case
     "c1": dict(nx=96, ny=48, nz=4, lx=24.0, ly=12.0, lz=1.0, cx=6.0, cy=6.0, Re=100.0, dt=0.005),
     # mixed-precision scale case (67M cells)
     "c3": dict(nx=1024, ny=512, nz=128, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0, Re=300.0, dt=0.001),
+    # adjoint case (1M cells)
+    "c4": dict(nx=256, ny=128, nz=32, lx=24.0, ly=12.0, lz=2.0, cx=6.0, cy=6.0, Re=100.0, dt=0.004),
 }
+
+
 TOL = 1e-8
 FALLBACK_HBM_GBS = 6800.0
 
@@ -189,7 +193,7 @@ def _timed_steps(s, steps, dist, torch):
     return e0.elapsed_time(e1), stats
 
 
-def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True):
+def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True, keep_fields=False):
     cfg = dict(WORKLOADS[wl])
     with cg.Solver(solver=solver, precision=precision, tol=TOL, maxit=maxit, **cfg) as s:
         s.init_fields()
@@ -198,6 +202,8 @@ def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, 
         ms, stats = _timed_steps(s, steps, dist, torch)
         launches = s.launch_count()
         out = {"ms": ms, "stats": stats, "launches": launches, "cells": s.cells}
+        if keep_fields:
+            out["fields"] = s.get_fields()
         if profile:
             # live per-kernel durations: the same number of further steps with every
             # kernel bracketed by CUDA events on the library's stream
@@ -233,6 +239,47 @@ def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
         ms = e0.elapsed_time(e1)
         nbytes = 4 * int(host["u"].nbytes)
         return ms, nbytes, s.cells
+
+
+def adjoint_mode(cg, torch, dist, nsteps, ckpt):
+    """Forward run with checkpoints and the adjoint sweep (gradient of the drag averaged
+    over the last third of the window w.r.t. the inlet profile and eta) on the adjoint
+    case; returns both wall times (CUDA events on the library's stream) and their ratio."""
+    cfg = dict(WORKLOADS["c4"])
+    with cg.Solver(solver="jacobi", precision="fp64", tol=TOL, **cfg) as s:
+        stream = torch.cuda.ExternalStream(s.stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        s.init_fields()
+        first = nsteps - nsteps // 3 + 1
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        J = s.forward(nsteps, first, nsteps, ckpt)
+        ev[1].record(stream)
+        g_in, g_eta = s.backward()
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        tf, tb = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+        import numpy as np
+        return {"workload": "c4", "steps": nsteps, "objective_steps": [first, nsteps], "ckpt_every": ckpt,
+                "J": J, "forward_ms": tf, "backward_ms": tb, "adjoint_over_forward": tb / tf,
+                "forward_cell_steps_per_s": s.cells * nsteps / (tf / 1e3),
+                "grad_inlet_norm": float(np.linalg.norm(g_in)), "grad_eta_norm": float(np.linalg.norm(g_eta))}
+
+
+def field_errors(a, b):
+    """Relative L2 errors of run a against run b after the same steps: u, v, w against the
+    norm of b's whole velocity, p without its mean (the Neumann problem leaves it free),
+    drag as the largest relative difference over the timed steps."""
+    import numpy as np
+    fa, fb = a["fields"], b["fields"]
+    core = (slice(2, -2),) * 3
+    scale = float(np.sqrt(sum(np.linalg.norm(fb[k][core]) ** 2 for k in "uvw")))
+    out = {k: float(np.linalg.norm(fa[k][core] - fb[k][core]) / scale) for k in "uvw"}
+    pa, pb = fa["p"][core], fb["p"][core]
+    out["p"] = float(np.linalg.norm((pa - pa.mean()) - (pb - pb.mean())) / np.linalg.norm(pb - pb.mean()))
+    cda, cdb = np.array([r.cd for r in a["stats"]]), np.array([r.cd for r in b["stats"]])
+    out["cd"] = float(np.abs(cda - cdb).max() / np.abs(cdb).max())
+    return out
 
 
 def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file):
@@ -335,7 +382,9 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cfdgb", choices=["cfdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--modes", default="fp64,mixed,rbsor,e2e,cpu")
+    ap.add_argument("--modes", default="fp64,mixed,rbsor,e2e,adjoint,cpu")
+    ap.add_argument("--adj-steps", type=int, default=30)
+    ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
     ap.add_argument("--sor-steps", type=int, default=2)
     ap.add_argument("--sor-maxit", type=int, default=20000)
@@ -356,7 +405,7 @@ def main(argv=None):
 
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
-        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64")
+        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64", keep_fields="mixed" in modes)
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
     value = cells * args.steps * dist.world / (t64 / 1e3)
@@ -376,13 +425,14 @@ def main(argv=None):
     }
     if "mixed" in modes:
         try:
-            mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed")
+            mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", keep_fields=True)
             tm = dist.max(mx["ms"])
             r32, share32 = roofline(mx["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
             line["mixed"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
                              "iters_per_step": [r.iters for r in mx["stats"]],
                              "outer_per_step": [r.outer for r in mx["stats"]],
                              "relres": max(r.relres for r in mx["stats"]), "speedup_vs_fp64": t64 / tm,
+                             "error_vs_fp64": field_errors(mx, fp64),
                              "gpu_launches": mx["launches"], "roofline": r32, "kernel_share": share32}
         except cg.CfdgbError as e:
             line["mixed"] = {"value": None, "error": str(e)}
@@ -398,6 +448,11 @@ def main(argv=None):
         te = dist.max(ms)
         line["e2e"] = {"value": cells * args.steps * dist.world / (te / 1e3), "unit": "cell-steps/s",
                        "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    if "adjoint" in modes:
+        try:
+            line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt)
+        except cg.CfdgbError as e:
+            line["adjoint"] = {"value": None, "error": str(e)}
     if "cpu" in modes and dist.rank == 0:
         rec = reference_iteration_record(wl)
         try:

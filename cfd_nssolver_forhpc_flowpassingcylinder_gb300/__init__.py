@@ -17,6 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
+ABI_VERSION = 2  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR = 0, 1, 2
 FP64, MIXED = 0, 1
@@ -40,7 +41,7 @@ class Config(C.Structure):
                 ("solver", C.c_int), ("precision", C.c_int),
                 ("tol", C.c_double), ("maxit", C.c_int), ("omega", C.c_double),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
-                ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double)]
+                ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -109,7 +110,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
-    if L.cfdgb_abi_version() != 1:
+    if L.cfdgb_abi_version() != ABI_VERSION:
         raise ImportError("libcfdgb ABI version mismatch")
     if path is None:
         _lib = L

@@ -62,7 +62,7 @@ enum KId {
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
-    "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "inner_setup32",
+    "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction"};
 
 struct PendingEv {
@@ -303,8 +303,7 @@ int capture_chunk(cfdgb_ctx *c, bool fp32) {
   for (int m = 0; m < c->chunk_len; ++m) {
     if (fp32)
       for (int part = 0; part < 3; ++part)
-        launch_bicg32_part(c->stream, part, m & 1, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part,
-                           c->sc32);
+        launch_bicg32_part(c->stream, part, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part, c->sc32);
     else
       for (int part = 0; part < 5; ++part)
         launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
@@ -345,8 +344,8 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
         if (fp32)
           for (int part = 0; part < 3; ++part)
             L(c, K_PAP32 + part, 1, [&] {
-              launch_bicg32_part(c->stream, part, m & 1, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32,
-                                 c->part, c->sc32);
+              launch_bicg32_part(c->stream, part, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part,
+                                 c->sc32);
             });
         else
           for (int part = 0; part < 5; ++part)
@@ -363,6 +362,10 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
     CK(cudaMemcpyAsync(c->h_sc, dsc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     resolve_events(c);
+    static const int trace = std::getenv("CFDGB_TRACE") ? std::atoi(std::getenv("CFDGB_TRACE")) : 0;
+    if (trace >= 2)
+      std::fprintf(stderr, "[cfdgb]     %s it %d relres %.4e\n", fp32 ? "fp32" : "fp64", c->h_sc->iter,
+                   c->h_sc->relres);
     if (c->h_sc->done) {
       *out = *c->h_sc;
       return 0;
@@ -376,6 +379,8 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
   L(c, K_RHS, 1, [&] { launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, jac, c->jac64, c->b); });
+  if (c->cfg.project_rhs)
+    L(c, K_RHS, 2, [&] { launch_project_rhs(c->stream, c->g, st64, jac ? 1 : 0, c->b, c->part, c->ss); });
   *iters = 0;
   *outer = 0;
   *status = 0;
@@ -411,55 +416,89 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     *status = r.status;
     return 0;
   }
-  // MIXED: FP64 defect correction around FP32 BiCGSTAB on the unit-scaled residual.
-  // Each inner solve is asked for the reduction that finishes the job with a 5x margin,
-  // but not below inner_tol (the FP32 floor).
-  // A correction that made the FP64 residual worse is taken back; when the sweeps stall
-  // (less than 2x per sweep) or an inner solve breaks down, the FP64 BiCGSTAB finishes
-  // from the current x, so the mode always ends at the FP64 tolerance.
+  // MIXED: FP32 BiCGSTAB sweeps inside FP64 iterative refinement (defect correction).
+  // Each sweep starts afresh from the FP64 residual and stops once its own residual has
+  // dropped by inner_tol (or looks converged); the refinement adds its correction to the
+  // FP64 solution and recomputes the residual in FP64.  The FP64 residual is the
+  // convergence and divergence test: when a sweep's FP32 residual has drifted from it, or
+  // it runs away, the last correction is taken back if it raised the residual and the FP64
+  // BiCGSTAB finishes from the current solution, so the mode always ends at the FP64
+  // tolerance.
   static const bool trace = std::getenv("CFDGB_TRACE") != nullptr;
-  double prev_rel = HUGE_VAL, applied = 0.0;
-  bool finish64 = false;
   const int jacf = jac ? 1 : 0;
-  for (int o = 0;; ++o) {
+  auto residual = [&](int flags, double *rel) -> int {
     L(c, K_RESID64, 1, [&] {
-      launch_residual64(c->stream, c->nblk, c->g, st64, jacf, c->b, c->x, c->r64, c->part, c->ss, c->sc32, o == 0);
+      launch_residual64(c->stream, c->nblk, c->g, st64, jacf, c->b, c->x, c->r64, c->part, c->ss, c->sc32, flags);
     });
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    const double rel = c->h_ss->relres, rnorm = c->h_ss->rnorm;
-    *relres = rel;
-    if (trace) std::fprintf(stderr, "[cfdgb] step %d outer %d relres %.3e\n", c->loop, o, rel);
-    if (!std::isfinite(rel) && applied == 0.0) { *status = CFDGB_ENAN; break; }
-    if (rel < c->cfg.tol) break;
-    if (!std::isfinite(rel) || rel > 0.5 * prev_rel || o >= c->cfg.max_outer) {
-      if (!(rel <= prev_rel) && applied != 0.0)
-        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -applied, c->ss); });
-      finish64 = true;
-      break;
-    }
-    const double itol = std::min(0.5, std::max(c->cfg.inner_tol, 0.2 * c->cfg.tol / rel));
-    TRY(set_solver_params(c, c->sc32, itol, c->cfg.maxit));
-    L(c, K_SETUP32, 1, [&] {
-      launch_inner_setup32(c->stream, c->nblk, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->part,
-                           c->sc32);
-    });
+    *rel = c->h_ss->relres;
+    return 0;
+  };
+  double rel = 0.0;
+  TRY(residual(3, &rel));
+  const double scale = c->h_ss->rnorm;
+  *relres = rel;
+  if (trace) std::fprintf(stderr, "[cfdgb] step %d relres %.3e\n", c->loop, rel);
+  if (!std::isfinite(rel)) {
+    *status = CFDGB_ENAN;
+    return 0;
+  }
+  if (rel < c->cfg.tol) return 0;
+  TRY(set_solver_params(c, c->sc32, c->cfg.tol, c->cfg.maxit));
+  L(c, K_SETUP32, 1, [&] {
+    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->cfg.inner_tol, 1,
+                          c->part, c->sc32);
+  });
+  bool finish64 = false;
+  double best = rel;
+  for (int o = 0;; ++o) {
     SolverScal r;
     TRY(run_chunks(c, true, &r));
-    if (trace)
-      std::fprintf(stderr, "[cfdgb]   inner tol %.1e iters %d status %d relres %.3e best %.3e\n", itol, r.iter,
-                   r.status, r.relres, r.best);
-    *iters += r.iter + 1;
-    *outer = o + 1;
-    if (!std::isfinite(r.relres)) {  // never apply a broken correction
+    *iters = r.iter;
+    if (r.status == CFDGB_ENAN || (r.status == CFDGB_ENOCONV && r.iter < c->cfg.maxit)) {
+      // the FP32 iteration broke down or diverged: its correction is dropped
+      if (trace) std::fprintf(stderr, "[cfdgb]   FP32 stopped: status %d at %d\n", r.status, r.iter);
       finish64 = true;
       break;
     }
-    applied = rnorm;
-    prev_rel = rel;
     L(c, K_CORRECT64, 2, [&] {
       launch_sum32(c->stream, c->g, c->k32.x, c->part, c->ss);
-      launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, applied, c->ss);
+      launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, scale, c->ss);
+    });
+    double rn = 0.0;
+    TRY(residual(0, &rn));
+    *outer = o + 1;
+    if (trace)
+      std::fprintf(stderr, "[cfdgb]   refinement %d after %d FP32 iterations: relres %.3e (FP32 estimate %.3e)\n",
+                   o + 1, r.iter, rn, r.relres);
+    // the FP32 recursion must still track the true residual (BiCGSTAB's residual is not
+    // monotone, so a larger one alone is no failure); if it has drifted or the residual
+    // runs away, the correction is taken back when it made things worse
+    const bool drifted = !(std::fabs(rn - r.relres) <= 0.5 * rn);
+    if (!std::isfinite(rn) || drifted || rn > 1e3 * best) {
+      if (!(rn <= rel))
+        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -scale, c->ss); });
+      else
+        *relres = rn;
+      finish64 = true;
+      break;
+    }
+    rel = rn;
+    best = std::min(best, rn);
+    *relres = rn;
+    if (rn < c->cfg.tol) break;
+    if (r.status == CFDGB_ENOCONV) {  // iteration cap
+      *status = CFDGB_ENOCONV;
+      break;
+    }
+    if (o + 1 >= c->cfg.max_outer) {
+      finish64 = true;
+      break;
+    }
+    L(c, K_SETUP32, 1, [&] {
+      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->cfg.inner_tol, 0,
+                            c->part, c->sc32);
     });
   }
   if (finish64) {
@@ -538,10 +577,11 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->tol = 1e-8;
   c->maxit = 5000;
   c->omega = 1.7;
-  // FP32 inner solves stay well above their noise floor kappa * eps32 (~1e-3 on a 512-cell
-  // axis): each sweep asks for two decades
-  c->inner_tol = 1e-2;
-  c->max_outer = 20;
+  // an FP64 refinement whenever an FP32 sweep has cut its residual by 0.3: short sweeps
+  // stay clear of the FP32 stall (measured on the 512x256x64 workload: 0.3 and 0.1 need
+  // ~3000 FP32 iterations per solve without a fallback, 0.01 stalls)
+  c->inner_tol = 0.3;
+  c->max_outer = 400;
   c->check_every = 10;
   c->dfib = 1;
   c->seed = 0;
@@ -618,7 +658,11 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.vby = kBlock / g.vbx;
     g.vgx = (nq + g.vbx - 1) / g.vbx;
     g.vgy = (cfg->ny + g.vby - 1) / g.vby;
-    g.vgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.vgx * g.vgy)));
+    // the stencil kernels march along x through chunks of planes: a few resident blocks
+    // per SM, each with a long chunk (one extra plane read per chunk)
+    const char *bps = std::getenv("CFDGB_FP32_BLOCKS_PER_SM");
+    const int per_sm = bps ? std::max(1, std::atoi(bps)) : 4;
+    g.vgz = std::max(1, std::min(cfg->nx, c->nsm * per_sm / std::max(1, g.vgx * g.vgy)));
     nblk3 = std::max(nblk3, g.vgx * g.vgy * g.vgz);
   }
   // fields and solver vectors

@@ -90,11 +90,17 @@ __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &i
 // read by the next kernel in stream order.
 struct SolverScal {
   double rho, alpha, omega, beta, norm0, relres, tol, restart_thr;
-  double scale;              // MIXED: ||r|| of the outer residual the inner rhs is scaled by
-  double best;               // FP32 inner solve: smallest relative residual seen
-  int iter, maxit, done, status, timestep, restart, pad0, pad1;
+  double scale;              // MIXED: fixed scale of the FP32 residual (FP64 ||r|| at the start)
+  double best;               // FP32: smallest estimated relative residual seen
+  double rmax;               // MIXED: largest FP32 residual norm since the last refinement
+  double delta;              // MIXED: refine once ||r1|| < delta * rmax
+  int iter, maxit, done, status, timestep, restart;
+  int par;                   // FP32: p[par], ap[par] hold the previous iteration's vectors
+  int pad;
   unsigned cnt[8];           // last-block counters, one per kernel kind
 };
+// status of an FP32 solve that stopped for an FP64 refinement (never returned to callers)
+constexpr int kStatusRefine = 1;
 
 // Per-step scalars (drag, lift, outer residual of the mixed solve)
 struct StepScal {

@@ -4,6 +4,7 @@
 //
 //   cfdgb_run nx=96 ny=48 nz=4 lx=24 ly=12 lz=1 cx=6 cy=6 Re=100 dt=0.005 steps=200 \
 //             solver=bicgstab|jacobi|rbsor precision=fp64|mixed tol=1e-8 [out=Information]
+//             [amp=1e-3 seed=1234 project_rhs=1 inner_tol=0.3 max_outer=400 maxit=5000]
 //
 // Per step it prints the reference's lines ("[SPE (BICG)] iter:...", "[cD, cL] : ...")
 // and appends the drag/lift series to <out>/Time_cDcL.dat in the reference's Tecplot
@@ -36,8 +37,9 @@ int main(int argc, char **argv) {
   cfg.cx = num("cx", cfg.cx); cfg.cy = num("cy", cfg.ly / 2.0); cfg.radius = num("radius", cfg.radius);
   cfg.Re = num("Re", cfg.Re); cfg.dt = num("dt", cfg.dt); cfg.tol = num("tol", cfg.tol);
   cfg.maxit = (int)num("maxit", cfg.maxit); cfg.omega = num("omega", cfg.omega);
-  cfg.inner_tol = num("inner_tol", cfg.inner_tol);
+  cfg.inner_tol = num("inner_tol", cfg.inner_tol); cfg.max_outer = (int)num("max_outer", cfg.max_outer);
   cfg.amp = num("amp", 0.0); cfg.seed = (uint64_t)num("seed", 0.0);
+  cfg.project_rhs = (int)num("project_rhs", 0.0);
   const std::string solver = kv.count("solver") ? kv["solver"] : "bicgstab";
   cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI : solver == "rbsor" ? CFDGB_RBSOR : CFDGB_BICGSTAB;
   cfg.precision = (kv.count("precision") && kv["precision"] == "mixed") ? CFDGB_MIXED : CFDGB_FP64;

@@ -41,20 +41,20 @@ void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<d
 void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
                         double *part_buf, SolverScal *sc);
 // FP32 iteration, kernel `part` 0..2 (p update + A p, s + A s, x and r1); p and ap are
-// double-buffered (p2[parity] holds the previous p, p2[parity^1] receives the new one)
-void launch_bicg32_part(cudaStream_t s, int part, int parity, const Geo &g, const Stencil<float> &st,
-                        KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
-                        SolverScal *sc);
+// double-buffered: p2[sc->par] holds the previous p, p2[sc->par ^ 1] receives the new one
+void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, KrylovVecs<float> v,
+                        float *const p2[2], float *const ap2[2], double *part_buf, SolverScal *sc);
 // after the loop: NaN/Inf recovery of bicgstabRe2.hpp:133-153 when the cap was hit
 void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
                            const double *px2, double *part, SolverScal *sc);
 
-// MIXED defect correction pieces
+// MIXED refinement pieces: FP64 residual (flags: 1 = also ||b||, 2 = also the FP32 scale)
+// and the start of an FP32 sweep on it (first: also the solve's set-up)
 void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
-                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first);
-void launch_inner_setup32(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, int jacobi,
-                          KrylovVecs<float> v, float *const p2[2], float *const ap2[2], const double *r64,
-                          const StepScal *ss, double *part, SolverScal *sc);
+                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags);
+void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
+                           float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
+                           double delta, int first, double *part, SolverScal *sc);
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss);
 // x += factor (e - mean e), the mean taken from the preceding launch_sum32
 void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor,
@@ -73,6 +73,10 @@ void launch_adj_rhs(cudaStream_t s, int nblk, const Geo &g, double dt, const dou
 void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u, const double *v,
                          const double *w, const double *lus, const double *lvs, const double *lws, double *lu,
                          double *lv, double *lw);
+
+// b -= its null-space part (mean of the unscaled rhs; jp-weighted for the Jacobi rows)
+void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
+                        StepScal *ss);
 
 // red-black SOR on the same operator (FP64)
 void launch_rbsor_sweep(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,

@@ -52,6 +52,29 @@ __device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, i
   return sum;
 }
 
+// FP32 form of the same operator: every row sums to zero (Neumann rows: the diagonal is
+// minus the sum of the neighbour coefficients), so A f = sum_nb c_nb (f_nb - f_centre).
+// Differencing first makes A exactly singular on constants in FP32 and keeps the rounding
+// error proportional to the local differences rather than to |f|: on the smooth modes that
+// dominate late in a solve, the plain 7-term sum would lose ~eps32 * cond(A) (~1e-2 at
+// 512 cells per axis) and stall the iteration there.
+template <class F>
+__device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<float> &st, int ic, int jc, int kc,
+                                                    long long row, F &&f, float &center) {
+  const long long nyz = (long long)g.nyc * g.nzc;
+  const float *c = st.c[cls_of(g, ic, jc, kc)];
+  const float fc = f(row);
+  center = fc;
+  float sum = 0.0f;
+  if (ic > 0) sum = fmaf(c[0], f(row - nyz) - fc, sum);
+  if (jc > 0) sum = fmaf(c[1], f(row - g.nzc) - fc, sum);
+  if (kc > 0) sum = fmaf(c[2], f(row - 1) - fc, sum);
+  if (kc < g.nzc - 1) sum = fmaf(c[4], f(row + 1) - fc, sum);
+  if (jc < g.nyc - 1) sum = fmaf(c[5], f(row + g.nzc) - fc, sum);
+  if (ic < g.nxc - 1) sum = fmaf(c[6], f(row + nyz) - fc, sum);
+  return sum;
+}
+
 template <typename T>
 __device__ __forceinline__ T spmv_at(const Geo &g, const Stencil<T> &st, const T *__restrict__ x, int ic, int jc,
                                      int kc, long long row) {
@@ -137,17 +160,42 @@ template <bool FP32>
 __device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, double rr) {
   const double relres = sqrt(n2) / sc->norm0;
   sc->relres = relres;
-  if (FP32 && relres < sc->best) sc->best = relres;
+  if (FP32) {
+    // MIXED sweep: hand over to the FP64 refinement once the residual has dropped by
+    // delta below the sweep's largest one, or looks converged
+    const double rn = sqrt(n2);
+    if (relres < sc->best) sc->best = relres;
+    if (!isfinite(relres)) {
+      sc->done = 1;
+      sc->status = CFDGB_ENAN;
+    } else if (sc->iter > 16 && relres > 1e3 * sc->best) {
+      // runaway growth (BiCGSTAB's ordinary bumps stay far below this)
+      sc->done = 1;
+      sc->status = CFDGB_ENOCONV;
+    } else if (sc->iter >= sc->maxit) {
+      sc->done = 1;
+      sc->status = CFDGB_ENOCONV;
+      sc->iter += 1;
+    } else if (relres < sc->tol || rn < sc->delta * sc->rmax) {
+      sc->done = 1;
+      sc->status = kStatusRefine;
+      sc->iter += 1;
+    } else {
+      const double rho_old = sc->rho;
+      sc->rho = rr;
+      sc->beta = (sc->alpha / sc->omega) * (rr / rho_old);
+      sc->restart = 0;
+      if (!(isfinite(sc->beta) && sc->omega != 0.0 && rr != 0.0)) {  // Lanczos breakdown
+        sc->restart = 1;
+        sc->rho = n2;
+      }
+      sc->rmax = fmax(sc->rmax, rn);
+      sc->iter += 1;
+    }
+    return;
+  }
   if (relres < sc->tol) {  // :129
     sc->done = 1;
-  } else if (FP32 && !isfinite(relres)) {  // FP32 inner solve broke down
-    sc->done = 1;
-    sc->status = CFDGB_ENAN;
-  } else if (FP32 && sc->iter > 16 && relres > 1e2 * sc->best) {
-    // FP32 inner solve diverging (rounding has destroyed the bi-orthogonality): stop;
-    // the FP64 outer residual decides what to keep
-    sc->done = 1;
-    sc->status = CFDGB_ENOCONV;
   } else if (sc->iter >= sc->maxit) {  // :133
     sc->done = 1;
     sc->status = CFDGB_ENOCONV;
@@ -156,12 +204,6 @@ __device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, doub
     sc->rho = rr;
     sc->beta = (sc->alpha / sc->omega) * (sc->rho / rho_old);
     sc->restart = !(sc->timestep < 10 || fabs(rho_old) > sc->restart_thr);
-    if (FP32 && !(isfinite(sc->beta) && sc->omega != 0.0 && sc->rho != 0.0)) {
-      // Lanczos breakdown of the FP32 inner solve: restart from the current residual
-      // with a fresh shadow vector r0 = r1, so rho = <r1, r1>
-      sc->restart = 1;
-      sc->rho = n2;
-    }
     sc->iter += 1;
   }
 }
@@ -208,22 +250,23 @@ struct Vec32 {
 
 // p_new = r1 + beta (p_old - omega ap_old) (or r1 on restart, which also sets r0 = r1),
 // evaluated at the stencil points; ap_new = A p_new; alpha = rho / <ap_new, r0>
-__global__ void __launch_bounds__(kBlock) k32_pap(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+__global__ void __launch_bounds__(kBlock) k32_pap(Geo g, Stencil<float> st, Vec32 v, double *part,
                                                   SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float b = (float)sc->beta, w = (float)sc->omega;
   const bool rst = sc->restart != 0;
-  const float *__restrict__ po = v.p[parity];
-  const float *__restrict__ apo = v.ap[parity];
-  float *__restrict__ pn = v.p[parity ^ 1];
-  float *__restrict__ apn = v.ap[parity ^ 1];
+  const float *__restrict__ po = (parity ? v.p[1] : v.p[0]);
+  const float *__restrict__ apo = (parity ? v.ap[1] : v.ap[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  float *__restrict__ apn = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
   AccF acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     float pc;
-    const float y = rst ? stencil_apply<float>(g, st, ic, jc, kc, row, [&](long long q) { return r1[q]; }, pc)
-                        : stencil_apply<float>(g, st, ic, jc, kc, row,
+    const float y = rst ? stencil_apply_diff(g, st, ic, jc, kc, row, [&](long long q) { return r1[q]; }, pc)
+                        : stencil_apply_diff(g, st, ic, jc, kc, row,
                                                [&](long long q) { return r1[q] + b * (po[q] - w * apo[q]); }, pc);
     pn[row] = pc;
     apn[row] = y;
@@ -239,17 +282,18 @@ __global__ void __launch_bounds__(kBlock) k32_pap(Geo g, Stencil<float> st, Vec3
 }
 
 // s = r1 - alpha ap at the stencil points; as = A s; omega = <as, s> / <as, as>
-__global__ void __launch_bounds__(kBlock) k32_sas(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+__global__ void __launch_bounds__(kBlock) k32_sas(Geo g, Stencil<float> st, Vec32 v, double *part,
                                                   SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float a = (float)sc->alpha;
-  const float *__restrict__ ap = v.ap[parity ^ 1];
+  const float *__restrict__ ap = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
   AccF a0, a1;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     float sc_;
-    const float y = stencil_apply<float>(g, st, ic, jc, kc, row, [&](long long q) { return r1[q] - a * ap[q]; }, sc_);
+    const float y = stencil_apply_diff(g, st, ic, jc, kc, row, [&](long long q) { return r1[q] - a * ap[q]; }, sc_);
     v.s[row] = sc_;
     v.as[row] = y;
     a0.add(y * sc_);
@@ -266,10 +310,11 @@ __global__ void __launch_bounds__(kBlock) k32_sas(Geo g, Stencil<float> st, Vec3
 }
 
 // x += alpha p + omega s; r1 = s - omega as; stop test, beta, restart
-__global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, int parity, double *part, SolverScal *sc) {
+__global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, double *part, SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float a = (float)sc->alpha, w = (float)sc->omega;
-  const float *__restrict__ p = v.p[parity ^ 1];
+  const float *__restrict__ p = (parity ? v.p[0] : v.p[1]);
   AccF n2, rr;
   FOR_CELLS(g) {
     const long long row = ROW(g);
@@ -281,13 +326,17 @@ __global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, int parity, dou
     rr.add(r1 * v.r0[row]);
   }
   double acc[2] = {n2.get(), rr.get()}, out[2];
-  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) {
+    sc->par ^= 1;  // this iteration's p and ap become the previous ones
+    finish_iteration<true>(sc, out[0], out[1]);
+  }
 }
 
 // ---- FP32 iteration, vectorised: four consecutive k cells per thread (nzc % 4 == 0) ----
 // One float4 load per vector and stencil point instead of four scalar loads; the k
 // neighbours inside the quad come from registers.  Dot partials stay FP32 over the few
 // dozen quads a thread owns and are added into the FP64 block/grid reduction once.
+// k32v_xr is pointwise: a grid-stride loop over the planes.
 #define FOR_QUADS(g)                                               \
   const int kc0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);     \
   const int kc = kc0; /* ROW(g) of the quad's first cell */        \
@@ -306,104 +355,157 @@ __device__ __forceinline__ void st4(float *p, const F4 &a) {
   *reinterpret_cast<float4 *>(p) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
 }
 
-// y = A f on the quad starting at (ic, jc, kc0); f4(q) gives four values at row q, f1(q)
-// one value; the quad's own values are returned in ctr.
-template <class F4f, class F1f>
-__device__ __forceinline__ F4 quad_apply(const Geo &g, const Stencil<float> &st, int ic, int jc, int kc0, long long row,
-                                         F4f &&f4, F1f &&f1, F4 &ctr) {
+// The two stencil kernels march along x.  A thread owns one quad of one j row and walks a
+// chunk of consecutive i planes (the same chunk for the whole block, so every thread runs
+// the same trip count).  The values of planes i-1, i, i+1 stay in registers: per plane a
+// thread loads the next plane's quad (its first read from HBM) and the quads of rows j-1
+// and j+1 (L1 hits, loaded one plane earlier by their owners); the cells left and right
+// of the quad come from the neighbouring lanes by warp shuffle, from memory only at a
+// block's k edge.  f4(q) evaluates the stencil's argument at the quad of row q, f1(q) at
+// one cell; body(row, centre values, A-applied values) consumes the result.
+__device__ __forceinline__ void prefetch_l2(const float *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+template <class F4f, class F1f, class Pf, class Body>
+__device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &st, F4f &&f4, F1f &&f1, Pf &&pf,
+                                            Body &&body) {
+  const int kc0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y;
+  const bool on = kc0 < g.nzc && jc < g.nyc;
+  const int chunk = (g.nxc + gridDim.z - 1) / gridDim.z;
+  const int i0 = min(g.nxc, (int)blockIdx.z * chunk), i1 = min(g.nxc, i0 + chunk);
   const long long nyz = (long long)g.nyc * g.nzc;
-  ctr = f4(row);
-  const bool hx0 = ic > 0, hx1 = ic < g.nxc - 1, hy0 = jc > 0, hy1 = jc < g.nyc - 1;
-  const F4 xm = hx0 ? f4(row - nyz) : F4{}, xp = hx1 ? f4(row + nyz) : F4{};
-  const F4 ym = hy0 ? f4(row - g.nzc) : F4{}, yp = hy1 ? f4(row + g.nzc) : F4{};
-  const float zl = kc0 > 0 ? f1(row - 1) : 0.0f, zr = kc0 + 4 < g.nzc ? f1(row + 4) : 0.0f;
-  const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
-  F4 y;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int kc = kc0 + q;
-    const float *c = st.c[cxy + axis_class(kc, g.nzc)];
-    const float zm = q == 0 ? zl : ctr.v[q - 1], zp = q == 3 ? zr : ctr.v[q + 1];
-    float s = 0.0f;
-    if (hx0) s += c[0] * xm.v[q];
-    if (hy0) s += c[1] * ym.v[q];
-    if (kc > 0) s += c[2] * zm;
-    s += c[3] * ctr.v[q];
-    if (kc < g.nzc - 1) s += c[4] * zp;
-    if (hy1) s += c[5] * yp.v[q];
-    if (hx1) s += c[6] * xp.v[q];
-    y.v[q] = s;
+  const bool hy0 = jc > 0, hy1 = jc + 1 < g.nyc;
+  const bool kl = kc0 > 0, kr = kc0 + 4 < g.nzc;                       // cells left / right exist
+  const bool sl = threadIdx.x > 0, sr = threadIdx.x + 1 < blockDim.x;  // ... and are in this warp
+  long long row = ((long long)i0 * g.nyc + jc) * g.nzc + kc0;
+  F4 fm{}, fc{};
+  if (on && i0 < i1) {
+    if (i0 > 0) fm = f4(row - nyz);
+    fc = f4(row);
   }
-  return y;
+  for (int ic = i0; ic < i1; ++ic, row += nyz) {
+    F4 fp{}, ym{}, yp{};
+    if (on) {
+      if (ic + 2 < g.nxc && ic + 1 < i1) pf(row + 2 * nyz);  // the plane after next, into L2
+      if (ic + 1 < g.nxc) fp = f4(row + nyz);
+      if (hy0) ym = f4(row - g.nzc);
+      if (hy1) yp = f4(row + g.nzc);
+    }
+    const float l = __shfl_up_sync(0xffffffffu, fc.v[3], 1);
+    const float r = __shfl_down_sync(0xffffffffu, fc.v[0], 1);
+    const float zl = !kl ? 0.0f : (sl ? l : (on ? f1(row - 1) : 0.0f));
+    const float zr = !kr ? 0.0f : (sr ? r : (on ? f1(row + 4) : 0.0f));
+    // difference form (stencil_apply_diff); a missing neighbour has coefficient 0
+    const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
+    F4 y;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float *c = st.c[cxy + axis_class(kc0 + q, g.nzc)];
+      const float f0 = fc.v[q];
+      const float zm = q == 0 ? zl : fc.v[q - 1], zp = q == 3 ? zr : fc.v[q + 1];
+      float t = c[0] * (fm.v[q] - f0);
+      t = fmaf(c[1], ym.v[q] - f0, t);
+      t = fmaf(c[2], zm - f0, t);
+      t = fmaf(c[4], zp - f0, t);
+      t = fmaf(c[5], yp.v[q] - f0, t);
+      t = fmaf(c[6], fp.v[q] - f0, t);
+      y.v[q] = t;
+    }
+    if (on) body(row, fc, y);
+    fm = fc;
+    fc = fp;
+  }
 }
 
-__global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+// p_new = r1 + beta (p_old - omega ap_old) (restart: p_new = r0 = r1); ap_new = A p_new;
+// alpha = rho / <ap_new, r0>
+__global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec32 v, double *part,
                                                    SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float b = (float)sc->beta, w = (float)sc->omega;
   const bool rst = sc->restart != 0;
-  const float *__restrict__ po = v.p[parity];
-  const float *__restrict__ apo = v.ap[parity];
-  float *__restrict__ pn = v.p[parity ^ 1];
-  float *__restrict__ apn = v.ap[parity ^ 1];
+  const float *__restrict__ po = (parity ? v.p[1] : v.p[0]);
+  const float *__restrict__ apo = (parity ? v.ap[1] : v.ap[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  float *__restrict__ apn = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
+  float *__restrict__ r0 = v.r0;
   float acc = 0.0f;
-  FOR_QUADS(g) {
-    const long long row = ROW(g);
-    F4 pc, y;
-    if (rst) {
-      y = quad_apply(g, st, ic, jc, kc0, row, [&](long long q) { return ld4(r1 + q); },
-                     [&](long long q) { return r1[q]; }, pc);
-      st4(v.r0 + row, pc);
-    } else {
-      auto f4 = [&](long long q) {
-        const F4 r = ld4(r1 + q), p = ld4(po + q), a = ld4(apo + q);
-        F4 o;
+  if (rst) {
+    march_quads(
+        g, st, [&](long long q) { return ld4(r1 + q); }, [&](long long q) { return r1[q]; },
+        [&](long long q) { prefetch_l2(r1 + q); },
+        [&](long long row, const F4 &pc, const F4 &y) {
+          st4(pn + row, pc);
+          st4(apn + row, y);
+          st4(r0 + row, pc);
 #pragma unroll
-        for (int t = 0; t < 4; ++t) o.v[t] = fmaf(b, fmaf(-w, a.v[t], p.v[t]), r.v[t]);
-        return o;
-      };
-      auto f1 = [&](long long q) { return fmaf(b, fmaf(-w, apo[q], po[q]), r1[q]); };
-      y = quad_apply(g, st, ic, jc, kc0, row, f4, f1, pc);
-    }
-    st4(pn + row, pc);
-    st4(apn + row, y);
-    const F4 r0 = rst ? pc : ld4(v.r0 + row);
+          for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], pc.v[t], acc);
+        });
+  } else {
+    march_quads(
+        g, st,
+        [&](long long q) {
+          const F4 r = ld4(r1 + q), p = ld4(po + q), a = ld4(apo + q);
+          F4 o;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], r0.v[t], acc);
+          for (int t = 0; t < 4; ++t) o.v[t] = fmaf(b, fmaf(-w, a.v[t], p.v[t]), r.v[t]);
+          return o;
+        },
+        [&](long long q) { return fmaf(b, fmaf(-w, apo[q], po[q]), r1[q]); },
+        [&](long long q) {
+          prefetch_l2(r1 + q);
+          prefetch_l2(po + q);
+          prefetch_l2(apo + q);
+          prefetch_l2(r0 + q);
+        },
+        [&](long long row, const F4 &pc, const F4 &y) {
+          st4(pn + row, pc);
+          st4(apn + row, y);
+          const F4 z = ld4(r0 + row);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], z.v[t], acc);
+        });
   }
   double a[1] = {(double)acc}, out[1];
   if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
 }
 
-__global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec32 v, int parity, double *part,
+// s = r1 - alpha ap; as = A s; omega = <as, s> / <as, as>
+__global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec32 v, double *part,
                                                    SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float a = (float)sc->alpha;
-  const float *__restrict__ ap = v.ap[parity ^ 1];
+  const float *__restrict__ ap = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
+  float *__restrict__ sv = v.s;
+  float *__restrict__ asv = v.as;
   float a0 = 0.0f, a1 = 0.0f;
-  FOR_QUADS(g) {
-    const long long row = ROW(g);
-    F4 sc4;
-    const F4 y = quad_apply(
-        g, st, ic, jc, kc0, row,
-        [&](long long q) {
-          const F4 r = ld4(r1 + q), p = ld4(ap + q);
-          F4 o;
+  march_quads(
+      g, st,
+      [&](long long q) {
+        const F4 r = ld4(r1 + q), p = ld4(ap + q);
+        F4 o;
 #pragma unroll
-          for (int t = 0; t < 4; ++t) o.v[t] = fmaf(-a, p.v[t], r.v[t]);
-          return o;
-        },
-        [&](long long q) { return fmaf(-a, ap[q], r1[q]); }, sc4);
-    st4(v.s + row, sc4);
-    st4(v.as + row, y);
+        for (int t = 0; t < 4; ++t) o.v[t] = fmaf(-a, p.v[t], r.v[t]);
+        return o;
+      },
+      [&](long long q) { return fmaf(-a, ap[q], r1[q]); },
+      [&](long long q) {
+        prefetch_l2(r1 + q);
+        prefetch_l2(ap + q);
+      },
+      [&](long long row, const F4 &s4, const F4 &y) {
+        st4(sv + row, s4);
+        st4(asv + row, y);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      a0 = fmaf(y.v[t], sc4.v[t], a0);
-      a1 = fmaf(y.v[t], y.v[t], a1);
-    }
-  }
+        for (int t = 0; t < 4; ++t) {
+          a0 = fmaf(y.v[t], s4.v[t], a0);
+          a1 = fmaf(y.v[t], y.v[t], a1);
+        }
+      });
   double acc[2] = {(double)a0, (double)a1}, out[2];
   if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
     double wv = out[0] / out[1];
@@ -412,10 +514,11 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, int parity, double *part, SolverScal *sc) {
+__global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, SolverScal *sc) {
   if (sc->done) return;
+  const int parity = sc->par;
   const float a = (float)sc->alpha, w = (float)sc->omega;
-  const float *__restrict__ p = v.p[parity ^ 1];
+  const float *__restrict__ p = (parity ? v.p[0] : v.p[1]);
   float n2 = 0.0f, rr = 0.0f;
   FOR_QUADS(g) {
     const long long row = ROW(g);
@@ -432,7 +535,10 @@ __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, int parity, do
     st4(v.r1 + row, r1);
   }
   double acc[2] = {(double)n2, (double)rr}, out[2];
-  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) {
+    sc->par ^= 1;  // this iteration's p and ap become the previous ones
+    finish_iteration<true>(sc, out[0], out[1]);
+  }
 }
 
 // bicgstabRe2.hpp:133-153: at the cap, NaN/Inf entries come from the previous solution;
@@ -457,13 +563,21 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
   }
 }
 
-// ---- mixed precision: FP64 outer residual, FP32 inner solve on the scaled residual ----
-// r64 = b - A x (FP64); ||r||, and ||b|| on the first sweep; inner scale = ||r||.
+// ---- mixed precision: FP32 BiCGSTAB inside FP64 iterative refinement ----
+// Each sweep runs FP32 BiCGSTAB from a fresh start on r1 = (r64 - null-space part) / scale
+// (scale fixed for the whole solve) until its residual has dropped by delta; its
+// correction accumulates in the FP32 x.  The refinement adds scale * x to the FP64
+// solution and recomputes r64 = b - A x in FP64, which starts the next sweep.  Keeping the
+// Krylov space across refinements (reliable updates) was measured too: on the 512-cell
+// axis the FP32 iteration then loses bi-orthogonality near 1e-3 and stalls, while short
+// restarted sweeps converge to the FP64 tolerance.
+
+// r64 = b - A x (FP64); ||r||, ||b|| (flags & 1) and the scale (flags & 2).
 // jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose unscaled residual is r / jp.
 __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st, int jacobi,
                                                         const double *__restrict__ b, const double *__restrict__ x,
                                                         double *__restrict__ r64, double *part, StepScal *ss,
-                                                        SolverScal *inner, int first) {
+                                                        SolverScal *inner, int flags) {
   double acc[3] = {0.0, 0.0, 0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
@@ -477,29 +591,36 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
   }
   double out[3];
   if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
-    if (first) ss->bnorm = sqrt(out[1]);
+    if (flags & 1) ss->bnorm = sqrt(out[1]);
     ss->rnorm = sqrt(out[0]);
     ss->relres = ss->rnorm / ss->bnorm;
     ss->rsum = out[2];
-    inner->scale = ss->rnorm;
+    if (flags & 2) inner->scale = ss->rnorm;
   }
 }
 
-// inner set-up: e = 0, r0 = r1 = (r64 - its null-space part) / ||r|| in FP32, rho =
-// <r0, r0>, norm0 = ||r0||; restart = 1 makes the first k32_pap take p = r1 (the
-// reference's p1 = r0).  Removing the null-space part (the mean of the unscaled residual;
-// for the Jacobi rows its image jp * mean) keeps the FP32 system consistent, so its
-// solution cannot drift along the constant mode.
-__global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Stencil<double> st, int jacobi, Vec32 v,
-                                                           const double *__restrict__ r64, const StepScal *ss,
-                                                           double *part, SolverScal *sc) {
+// r64 minus its null-space part (the mean of the unscaled residual; for the Jacobi rows its
+// image jp * mean), scaled to FP32.  Removing it keeps the FP32 system consistent, so the
+// iteration cannot drift along the constant mode.
+__device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<double> &st, int jacobi,
+                                                 const double *__restrict__ r64, double m, double inv, int ic, int jc,
+                                                 int kc, long long row) {
+  const double wgt = jacobi ? st.c[cls_of(g, ic, jc, kc)][7] : 1.0;
+  return (float)((r64[row] - m * wgt) * inv);
+}
+
+// start of a sweep: x = 0, r0 = r1 = scaled residual, rho = <r1, r1>; restart = 1 makes the
+// first k32_pap take p = r1 (the reference's p1 = r0).  first: also the solve's set-up
+// (iteration count, delta, the FP32 estimate's normalisation).
+__global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double> st, int jacobi, Vec32 v,
+                                                            const double *__restrict__ r64, const StepScal *ss,
+                                                            double delta, int first, double *part, SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
   const double m = ss->rsum / (double)g.ncell;
   AccF acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    const double wgt = jacobi ? st.c[cls_of(g, ic, jc, kc)][7] : 1.0;
-    const float r = (float)((r64[row] - m * wgt) * inv);
+    const float r = scaled_residual(g, st, jacobi, r64, m, inv, ic, jc, kc, row);
     v.x[row] = 0.0f;
     v.r0[row] = r;
     v.r1[row] = r;
@@ -507,15 +628,20 @@ __global__ void __launch_bounds__(kBlock) k_inner_setup32(Geo g, Stencil<double>
   }
   double a[1] = {acc.get()}, out[1];
   if (grid_sum<1>(a, part, &sc->cnt[0], out) && lin_tid() == 0) {
-    sc->timestep += 1;
-    sc->norm0 = sqrt(out[0]);
+    if (first) {
+      sc->timestep += 1;
+      sc->norm0 = ss->bnorm * inv;  // relres = ||r1|| scale / ||b||
+      sc->delta = delta;
+      sc->best = ss->relres;
+      sc->iter = 0;
+    }
     sc->rho = out[0];
-    sc->iter = 0;
+    sc->rmax = sqrt(out[0]);
+    sc->relres = sqrt(out[0]) / sc->norm0;
     sc->done = 0;
     sc->status = 0;
     sc->restart = 1;
-    sc->relres = 0.0;
-    sc->best = 1.0;
+    sc->par = 0;
   }
 }
 
@@ -538,6 +664,29 @@ __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict_
   FOR_CELLS(g) {
     const long long row = ROW(g);
     x[row] += s * ((double)e[row] - m);
+  }
+}
+
+// ---- null-space projection of the right-hand side (project_rhs) ----
+// The Neumann operator annihilates constants, so b must sum to zero (unscaled rows) for
+// the system to have a solution.  rsum = sum of the unscaled b; b -= its mean, mapped
+// back through jp for the Jacobi rows.
+__global__ void __launch_bounds__(kBlock) k_rhs_sum(Geo g, Stencil<double> st, int jacobi,
+                                                     const double *__restrict__ b, double *part, StepScal *ss) {
+  double acc[1] = {0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    acc[0] += jacobi ? b[row] / st.c[cls_of(g, ic, jc, kc)][7] : b[row];
+  }
+  double out[1];
+  if (grid_sum<1>(acc, part, &ss->cnt[6], out) && lin_tid() == 0) ss->rsum = out[0];
+}
+__global__ void __launch_bounds__(kBlock) k_rhs_subtract(Geo g, Stencil<double> st, int jacobi,
+                                                          double *__restrict__ b, const StepScal *ss) {
+  const double m = ss->rsum / (double)g.ncell;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    b[row] -= jacobi ? m * st.c[cls_of(g, ic, jc, kc)][7] : m;
   }
 }
 
@@ -614,23 +763,23 @@ void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<do
   }
 }
 
-void launch_bicg32_part(cudaStream_t s, int part, int parity, const Geo &g, const Stencil<float> &st,
+void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st,
                         KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
                         SolverScal *sc) {
   const Vec32 w = v32(v, p2, ap2);
   if (g.vbx > 0) {  // vectorised path
     const dim3 vg(g.vgx, g.vgy, g.vgz), vb(g.vbx, g.vby, 1);
     switch (part) {
-      case 0: k32v_pap<<<vg, vb, 0, s>>>(g, st, w, parity, part_buf, sc); break;
-      case 1: k32v_sas<<<vg, vb, 0, s>>>(g, st, w, parity, part_buf, sc); break;
-      default: k32v_xr<<<vg, vb, 0, s>>>(g, w, parity, part_buf, sc); break;
+      case 0: k32v_pap<<<vg, vb, 0, s>>>(g, st, w, part_buf, sc); break;
+      case 1: k32v_sas<<<vg, vb, 0, s>>>(g, st, w, part_buf, sc); break;
+      default: k32v_xr<<<vg, vb, 0, s>>>(g, w, part_buf, sc); break;
     }
     return;
   }
   switch (part) {
-    case 0: k32_pap<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
-    case 1: k32_sas<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, parity, part_buf, sc); break;
-    default: k32_xr<<<cgrid(g), cblock(g), 0, s>>>(g, w, parity, part_buf, sc); break;
+    case 0: k32_pap<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, part_buf, sc); break;
+    case 1: k32_sas<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, part_buf, sc); break;
+    default: k32_xr<<<cgrid(g), cblock(g), 0, s>>>(g, w, part_buf, sc); break;
   }
 }
 
@@ -641,13 +790,13 @@ void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const d
 }
 
 void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
-                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int first) {
-  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, first);
+                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags) {
+  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
 }
-void launch_inner_setup32(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi,
-                          KrylovVecs<float> v, float *const p2[2], float *const ap2[2], const double *r64,
-                          const StepScal *ss, double *part, SolverScal *sc) {
-  k_inner_setup32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, part, sc);
+void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
+                           float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
+                           double delta, int first, double *part, SolverScal *sc) {
+  k_refine_start32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, delta, first, part, sc);
 }
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss) {
   k_sum32<<<cgrid(g), cblock(g), 0, s>>>(g, e, part, ss);
@@ -655,6 +804,11 @@ void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, St
 void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor,
                       const StepScal *ss) {
   k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, factor, ss);
+}
+void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
+                        StepScal *ss) {
+  k_rhs_sum<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, part, ss);
+  k_rhs_subtract<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, ss);
 }
 void launch_rbsor_sweep(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b, double *x,
                         double omega) {

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 1
+#define CFDGB_ABI_VERSION 2
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -43,8 +43,12 @@ typedef enum cfdgb_solver {
 
 typedef enum cfdgb_precision {
   CFDGB_FP64 = 0,  /* every kernel in FP64 */
-  CFDGB_MIXED = 1  /* FP32 stencil sweep and inner BiCGSTAB inside FP64 defect
-                      correction; FP64 outer residual, global dots and divergence */
+  CFDGB_MIXED = 1  /* FP32 stencil sweep and FP32 BiCGSTAB sweeps inside FP64 iterative
+                      refinement (defect correction): each sweep starts from the FP64
+                      residual and runs until its own residual has dropped by inner_tol;
+                      its correction is added to the FP64 solution and the residual is
+                      recomputed in FP64.  FP64 outer residual, global dots and
+                      divergence check */
 } cfdgb_precision;
 
 typedef struct cfdgb_config {
@@ -57,18 +61,22 @@ typedef struct cfdgb_config {
   double tol;                /* relative residual ||b-Ax||/||b|| (p_criteria) */
   int maxit;                 /* iteration cap (5000: bicgstabRe2.hpp:47) */
   double omega;              /* SOR relaxation */
-  double inner_tol;          /* MIXED: relative tolerance of each FP32 inner solve */
-  int max_outer;             /* MIXED: cap on defect-correction sweeps */
+  double inner_tol;          /* MIXED: residual reduction of each FP32 sweep (0.3) */
+  int max_outer;             /* MIXED: cap on FP64 refinements per solve */
   int check_every;           /* SOR: residual checked every this many sweeps */
   int dfib;                  /* 1: cylinder solid fraction on; 0: no immersed body */
   uint64_t seed;             /* perturbation seed (splitmix64), used when amp != 0 */
   double amp;                /* uniform(-amp, amp) added to interior u, v, w at init */
+  int project_rhs;           /* 1: remove the Poisson right-hand side's null-space part (its
+                                mean; jp-weighted for the Jacobi rows) before each solve, which
+                                makes the Neumann problem consistent for any inflow; 0: the
+                                reference, which solves b as it is (default) */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {
   int step;          /* 1-based step number (simu.loop) */
   int iters;         /* Poisson iterations (inner iterations summed for MIXED) */
-  int outer;         /* MIXED: defect-correction sweeps; 0 otherwise */
+  int outer;         /* MIXED: FP64 refinements (true-residual updates); 0 otherwise */
   int status;        /* cfdgb_status of this step's solve */
   double relres;     /* final relative residual of the solve (FP64) */
   double cd, cl;     /* drag and lift coefficients (CD_CL, virtualForceIntergrator.hpp:92) */

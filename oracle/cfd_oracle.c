@@ -681,12 +681,20 @@ double og_force_sum(const og_grid *g, const double *f, int dir) {
 int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
            double omega, double *u, double *v, double *w, double *p, double *eta,
            double *stats) {
-  return og_run_ex(g, steps, Re, dt, tol, solver, omega, u, v, w, p, eta, stats, NULL, NULL);
+  return og_run_ex(g, steps, Re, dt, tol, solver, omega, u, v, w, p, eta, stats, NULL, NULL, 0);
+}
+
+void og_project_rhs(const og_grid *g, const double *jp, double *b) {
+  const long n = og_cells(g);
+  double sum = 0.0;
+  for (long r = 0; r < n; ++r) sum += jp ? b[r] / jp[r] : b[r];
+  const double m = sum / (double)n;
+  for (long r = 0; r < n; ++r) b[r] -= jp ? m * jp[r] : m;
 }
 
 int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
               double omega, double *u, double *v, double *w, double *p, double *eta,
-              double *stats, const double *eta_in, const double *inlet) {
+              double *stats, const double *eta_in, const double *inlet, int project) {
   const long tot = og_padded(g), n = og_cells(g);
   const double nu = 1.0 / Re; /* 0_1_SimulationVariable.hpp:26-31 */
   double *us = dalloc(tot), *vs = dalloc(tot), *ws = dalloc(tot);
@@ -716,6 +724,7 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
         iters = og_sor(g, dt, omega, tol, 5000, us, vs, ws, p, &err);
       } else {
         og_rhs(g, dt, us, vs, ws, solver == 1 ? bs.jp : NULL, b);
+        if (project) og_project_rhs(g, solver == 1 ? bs.jp : NULL, b);
         iters = og_bicg_solve(&bs, b, x, &err);
         og_transform(g, x, p);
       }

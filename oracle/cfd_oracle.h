@@ -79,10 +79,15 @@ int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int so
            double *stats);
 /* og_run with the two parameters of the adjoint exposed: eta_in (padded solid fraction,
  * NULL: DFIB_CylinderZ) and inlet (ny*nz inlet u per (j,k), NULL: the constant 1 of
- * FLOWpassing.hpp:6). */
+ * FLOWpassing.hpp:6); project != 0 removes the right-hand side's null-space part before
+ * each BiCGSTAB solve (og_project_rhs; not in the reference). */
 int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int solver,
               double omega, double *u, double *v, double *w, double *p, double *eta,
-              double *stats, const double *eta_in, const double *inlet);
+              double *stats, const double *eta_in, const double *inlet, int project);
+/* b -= mean of the unscaled rhs (jp != NULL: b holds jp-scaled rows, b -= mean(b/jp) jp).
+ * Not in the reference: with a non-uniform inflow its Neumann problem has no solution and
+ * its BiCGSTAB diverges; this makes the system consistent. */
+void og_project_rhs(const og_grid *g, const double *jp, double *b);
 
 #ifdef __cplusplus
 }

@@ -84,7 +84,7 @@ def lib():
         L.og_force_sum.restype = C.c_double
         L.og_run.argtypes = [gp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                              C.c_double, _dp, _dp, _dp, _dp, _dp, C.c_void_p]
-        L.og_run_ex.argtypes = L.og_run.argtypes + [C.c_void_p, C.c_void_p]
+        L.og_run_ex.argtypes = L.og_run.argtypes + [C.c_void_p, C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -212,9 +212,10 @@ SOLVERS = {"spe": 0, "bicgstab": 0, "jacobi": 1, "csr": 1, "sor": 2}
 
 
 def run(g: Grid, steps, Re, dt, tol, solver="spe", omega=1.8, seed=0, amp=0.0, eta_in=None,
-        inlet=None):
+        inlet=None, project=False):
     """Whole run (src/RUN_CPU.cpp:257-436 order); returns dict of final fields + stats.
-    eta_in (padded) replaces the cylinder's solid fraction, inlet (ny, nz) the inlet u."""
+    eta_in (padded) replaces the cylinder's solid fraction, inlet (ny, nz) the inlet u;
+    project removes the Poisson rhs's mean before each BiCGSTAB solve (not in the reference)."""
     u = np.ones(g.shape)
     v = g.zeros()
     w = g.zeros()
@@ -228,6 +229,6 @@ def run(g: Grid, steps, Re, dt, tol, solver="spe", omega=1.8, seed=0, amp=0.0, e
     lib().og_run_ex(g.ptr, steps, Re, dt, tol, SOLVERS[solver], omega, u, v, w, p, eta,
                     stats.ctypes.data_as(C.c_void_p),
                     None if ein is None else ein.ctypes.data_as(C.c_void_p),
-                    None if inl is None else inl.ctypes.data_as(C.c_void_p))
+                    None if inl is None else inl.ctypes.data_as(C.c_void_p), int(bool(project)))
     return {"u": u, "v": v, "w": w, "p": p, "eta": eta, "iters": stats[:, 0].astype(int),
             "err": stats[:, 1], "cd": stats[:, 2], "cl": stats[:, 3]}

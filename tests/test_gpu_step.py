@@ -107,7 +107,7 @@ def test_deterministic():
 
 
 def test_mixed_precision_error_against_fp64():
-    """FP32 stencil + FP32 inner BiCGSTAB inside FP64 defect correction, resid 1e-8."""
+    """FP32 stencil + FP32 BiCGSTAB inside FP64 iterative refinement, resid 1e-8."""
     n = 60
     res = {}
     for prec in ("fp64", "mixed"):
@@ -124,6 +124,37 @@ def test_mixed_precision_error_against_fp64():
     errs["cd"] = float(np.abs(cdmx - cd64).max() / np.abs(cd64).max())
     print("mixed vs fp64 relative errors after", n, "steps:", errs)
     for k, e in errs.items():
+        assert e < 1e-4, (k, e)
+
+
+def test_projected_rhs_with_seeded_perturbation_matches_oracle():
+    """project_rhs on the seeded uniform(-1e-3, 1e-3) perturbation, which without it makes
+    the reference's Neumann problem inconsistent: FP64 GPU vs the oracle, both projected."""
+    g = O.Grid(96, 48, 4, 24.0, 12.0, 1.0, 6.0)
+    ref = O.run(g, 10, 100.0, 0.005, 1e-12, "spe", seed=1234, amp=1e-3, project=True)
+    assert np.all(ref["err"][1:] < 1e-12)
+    with _c1(tol=1e-12, seed=1234, amp=1e-3, project_rhs=1) as s:
+        s.init_fields()
+        st = s.step(10)
+        f = s.get_fields()
+    assert all(r.status == 0 and r.relres < 1e-12 for r in st[1:])
+    for k, e in vel_err(f, ref).items():
+        assert e <= 1e-9, (k, e)
+    assert rel_p(interior(f["p"]), interior(ref["p"])) <= 1e-9
+    np.testing.assert_allclose([r.cd for r in st], ref["cd"], rtol=1e-9)
+
+
+def test_mixed_precision_with_perturbation_and_projection():
+    """The seeded-perturbation case in MIXED precision: every solve ends below 1e-8 (FP64
+    residual) and the fields stay within 1e-4 of the FP64 run."""
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with _c1(precision=prec, tol=1e-8, seed=1234, amp=1e-3, project_rhs=1) as s:
+            s.init_fields()
+            st = s.step(20)
+            res[prec] = (s.get_fields(), st)
+    assert all(r.relres < 1e-8 and r.status == 0 for r in res["mixed"][1][1:])
+    for k, e in vel_err(res["mixed"][0], res["fp64"][0]).items():
         assert e < 1e-4, (k, e)
 
 
