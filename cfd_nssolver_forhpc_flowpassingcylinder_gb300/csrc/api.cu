@@ -366,6 +366,8 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
     if (trace >= 2)
       std::fprintf(stderr, "[cfdgb]     %s it %d relres %.4e\n", fp32 ? "fp32" : "fp64", c->h_sc->iter,
                    c->h_sc->relres);
+    if (fp32 && c->h_sc->fault)
+      return fail(CFDGB_ECUDA, "FP32 stencil pipeline: a bounded wait gave up (block stopped early)");
     if (c->h_sc->done) {
       *out = *c->h_sc;
       return 0;
@@ -663,7 +665,15 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     const char *bps = std::getenv("CFDGB_FP32_BLOCKS_PER_SM");
     const int per_sm = bps ? std::max(1, std::atoi(bps)) : 4;
     g.vgz = std::max(1, std::min(cfg->nx, c->nsm * per_sm / std::max(1, g.vgx * g.vgy)));
-    nblk3 = std::max(nblk3, g.vgx * g.vgy * g.vgz);
+    g.xgrid = c->nsm * fp32_pointwise_blocks_per_sm();
+    nblk3 = std::max(nblk3, std::max(g.vgx * g.vgy * g.vgz, g.xgrid));
+    int tbps = 0;
+    if (!std::getenv("CFDGB_NO_TMA") && fp32_stage_plan(cfg->nz, cfg->ny, &g.tj, &g.tsmem, &tbps)) {
+      g.tma = 1;
+      g.tgx = (cfg->ny + g.tj - 1) / g.tj;
+      g.tgy = std::max(1, std::min(cfg->nx, c->nsm * tbps / g.tgx));  // one wave of resident blocks
+      nblk3 = std::max(nblk3, g.tgx * g.tgy);
+    }
   }
   // fields and solver vectors
   double **pad[] = {&c->u, &c->v, &c->w, &c->us, &c->vs, &c->ws, &c->ui, &c->vi, &c->wi, &c->p, &c->eta};

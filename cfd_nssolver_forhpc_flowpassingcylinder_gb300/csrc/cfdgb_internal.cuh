@@ -32,6 +32,10 @@ struct Geo {
   // geometry of the vectorised FP32 kernels (four consecutive k cells per thread; used
   // when nzc % 4 == 0, else vbx = 0): vbx quads along k, vby rows along j, vgz over i
   int vbx, vby, vgx, vgy, vgz;
+  int xgrid;  // blocks of the flat pointwise FP32 kernel (every SM filled)
+  // bulk-copy (TMA) pipeline of the FP32 stencil kernels (nzc % 4 == 0, nzc <= 1024):
+  // blocks of tj rows x all k, tgx row tiles x tgy chunks of planes, dynamic shared memory
+  int tma, tj, tgx, tgy, tsmem;
 };
 
 // compact row -> padded (i,j,k)
@@ -96,7 +100,7 @@ struct SolverScal {
   double delta;              // MIXED: refine once ||r1|| < delta * rmax
   int iter, maxit, done, status, timestep, restart;
   int par;                   // FP32: p[par], ap[par] hold the previous iteration's vectors
-  int pad;
+  int fault;                 // FP32: a pipeline wait of a stencil kernel gave up (never expected)
   unsigned cnt[8];           // last-block counters, one per kernel kind
 };
 // status of an FP32 solve that stopped for an FP64 refinement (never returned to callers)

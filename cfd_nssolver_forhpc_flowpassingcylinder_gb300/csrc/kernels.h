@@ -44,6 +44,11 @@ void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<do
 // double-buffered: p2[sc->par] holds the previous p, p2[sc->par ^ 1] receives the new one
 void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, KrylovVecs<float> v,
                         float *const p2[2], float *const ap2[2], double *part_buf, SolverScal *sc);
+// resident blocks per SM of the pointwise FP32 kernel (sizes Geo::xgrid)
+int fp32_pointwise_blocks_per_sm();
+// bulk-copy pipeline of the FP32 stencil kernels: rows per block, dynamic shared memory,
+// resident blocks per SM; returns 0 when the grid does not fit it
+int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm);
 // after the loop: NaN/Inf recovery of bicgstabRe2.hpp:133-153 when the cap was hit
 void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
                            const double *px2, double *part, SolverScal *sc);

@@ -91,6 +91,22 @@ struct AccF {
   }
   __device__ __forceinline__ double get() const { return d + (double)f; }
 };
+// Compensated FP32 dot product (Ogita, Rump and Oishi's Dot2: the error-free product by
+// FMA and Knuth's TwoSum): as accurate as a dot product in twice the working precision,
+// at a few FP32 operations per term.
+struct Dot2F {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = a * b;
+    const float pe = fmaf(a, b, -p);  // a*b - p exactly
+    const float s = hi + p;
+    const float bp = s - hi;
+    const float se = (hi - (s - bp)) + (p - bp);  // hi + p - s exactly
+    hi = s;
+    lo += pe + se;
+  }
+  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
 struct AccD {
   double d = 0.0;
   __device__ __forceinline__ void add(double x) { d += x; }

@@ -30,7 +30,7 @@ namespace cfdgb {
 
 #define ROW(g) ((((long long)ic * (g).nyc + jc) * (g).nzc) + kc)
 
-__device__ __forceinline__ const int cls_of(const Geo &g, int ic, int jc, int kc) {
+__device__ __forceinline__ int cls_of(const Geo &g, int ic, int jc, int kc) {
   return axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc);
 }
 
@@ -362,12 +362,10 @@ __device__ __forceinline__ void st4(float *p, const F4 &a) {
 // and j+1 (L1 hits, loaded one plane earlier by their owners); the cells left and right
 // of the quad come from the neighbouring lanes by warp shuffle, from memory only at a
 // block's k edge.  f4(q) evaluates the stencil's argument at the quad of row q, f1(q) at
-// one cell; body(row, centre values, A-applied values) consumes the result.
-__device__ __forceinline__ void prefetch_l2(const float *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-
-template <class F4f, class F1f, class Pf, class Body>
-__device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &st, F4f &&f4, F1f &&f1, Pf &&pf,
-                                            Body &&body) {
+// one cell; body(row, centre values, A-applied values) consumes the result.  (A shared-
+// memory tile for the j neighbours, one barrier per plane, measured slower.)
+template <class F4f, class F1f, class Body>
+__device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &st, F4f &&f4, F1f &&f1, Body &&body) {
   const int kc0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int jc = blockIdx.y * blockDim.y + threadIdx.y;
   const bool on = kc0 < g.nzc && jc < g.nyc;
@@ -386,7 +384,6 @@ __device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &
   for (int ic = i0; ic < i1; ++ic, row += nyz) {
     F4 fp{}, ym{}, yp{};
     if (on) {
-      if (ic + 2 < g.nxc && ic + 1 < i1) pf(row + 2 * nyz);  // the plane after next, into L2
       if (ic + 1 < g.nxc) fp = f4(row + nyz);
       if (hy0) ym = f4(row - g.nzc);
       if (hy1) yp = f4(row + g.nzc);
@@ -431,17 +428,16 @@ __global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec
   float *__restrict__ apn = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
   float *__restrict__ r0 = v.r0;
-  float acc = 0.0f;
+  Dot2F acc;
   if (rst) {
     march_quads(
         g, st, [&](long long q) { return ld4(r1 + q); }, [&](long long q) { return r1[q]; },
-        [&](long long q) { prefetch_l2(r1 + q); },
         [&](long long row, const F4 &pc, const F4 &y) {
           st4(pn + row, pc);
           st4(apn + row, y);
           st4(r0 + row, pc);
 #pragma unroll
-          for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], pc.v[t], acc);
+          for (int t = 0; t < 4; ++t) acc.add(y.v[t], pc.v[t]);
         });
   } else {
     march_quads(
@@ -454,21 +450,15 @@ __global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec
           return o;
         },
         [&](long long q) { return fmaf(b, fmaf(-w, apo[q], po[q]), r1[q]); },
-        [&](long long q) {
-          prefetch_l2(r1 + q);
-          prefetch_l2(po + q);
-          prefetch_l2(apo + q);
-          prefetch_l2(r0 + q);
-        },
         [&](long long row, const F4 &pc, const F4 &y) {
           st4(pn + row, pc);
           st4(apn + row, y);
           const F4 z = ld4(r0 + row);
 #pragma unroll
-          for (int t = 0; t < 4; ++t) acc = fmaf(y.v[t], z.v[t], acc);
+          for (int t = 0; t < 4; ++t) acc.add(y.v[t], z.v[t]);
         });
   }
-  double a[1] = {(double)acc}, out[1];
+  double a[1] = {acc.get()}, out[1];
   if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
 }
 
@@ -482,7 +472,7 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
   const float *__restrict__ r1 = v.r1;
   float *__restrict__ sv = v.s;
   float *__restrict__ asv = v.as;
-  float a0 = 0.0f, a1 = 0.0f;
+  Dot2F a0, a1;
   march_quads(
       g, st,
       [&](long long q) {
@@ -493,20 +483,16 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
         return o;
       },
       [&](long long q) { return fmaf(-a, ap[q], r1[q]); },
-      [&](long long q) {
-        prefetch_l2(r1 + q);
-        prefetch_l2(ap + q);
-      },
       [&](long long row, const F4 &s4, const F4 &y) {
         st4(sv + row, s4);
         st4(asv + row, y);
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
-          a0 = fmaf(y.v[t], s4.v[t], a0);
-          a1 = fmaf(y.v[t], y.v[t], a1);
+          a0.add(y.v[t], s4.v[t]);
+          a1.add(y.v[t], y.v[t]);
         }
       });
-  double acc[2] = {(double)a0, (double)a1}, out[2];
+  double acc[2] = {a0.get(), a1.get()}, out[2];
   if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
     double wv = out[0] / out[1];
     if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;  // see k32_sas
@@ -514,31 +500,377 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
   }
 }
 
+// ---- FP32 stencil kernels on a bulk-copy (TMA) pipeline ----
+// A block owns tj rows (all k) of the compact vectors and a chunk of consecutive i planes.
+// Thread 0 streams each plane's rows jt-1 .. jt+tj (the halo rows included: one contiguous
+// range per vector, since rows of a plane are contiguous) into one of kStages shared-memory
+// stages with cp.async.bulk, signalling an mbarrier; every thread evaluates the stencil's
+// argument from the stage, keeps its own quad's values of planes i-1, i, i+1 in registers
+// and takes the j +- 1 values from the stage, the k +- 1 values by warp shuffle.  A stage is
+// refilled once all warps have released it (a second mbarrier), one plane after its last
+// use, so loads run up to kStages - 2 planes ahead of the computation.  Every wait is
+// bounded: a wait that gives up sets sc->fault, the block stops, waits (bounded) for its
+// own copies in flight and still joins the reduction.
+constexpr int kStages = 4;
+constexpr long long kWaitCycles = 1LL << 32;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// wait for the phase with the given parity to complete; false if it did not within kWaitCycles
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_load(float *dst, const float *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// The vectors a stage holds: na with halo rows (the stencil's argument is built from them)
+// and optionally one with the block's own rows only.
+struct StageSrc {
+  const float *a[3];
+  int na;
+  const float *own;
+};
+
+__host__ __device__ inline long long stage_floats(int tj, int nz, int na, bool own) {
+  return (long long)na * (tj + 2) * nz + (own ? (long long)tj * nz : 0);
+}
+
+// fval(arrays of a stage, stage row, first cell) -> the argument's four values of a quad;
+// f1(arrays, stage row, cell) -> one value; body(row, centre values, A-applied values,
+// own-rows vector of the stage at this thread's row or nullptr)
+template <class Fv, class F1, class Body>
+__device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st, const StageSrc &src, SolverScal *sc,
+                                          Fv &&fval, F1 &&f1, Body &&body) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ int bad;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *empty = full + kStages;
+  float *stage0 = reinterpret_cast<float *>(smem + 128);
+  const int nz = g.nzc, nq = nz / 4, tj = g.tj;
+  const long long SA = (long long)(tj + 2) * nz, SS = stage_floats(tj, nz, src.na, src.own != nullptr);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int tq = tid % nq, ty = tid / nq;
+  const int jt = blockIdx.x * tj, jc = jt + ty, kc0 = 4 * tq;
+  const bool on = ty < tj && jc < g.nyc;
+  const int chunk = (g.nxc + gridDim.y - 1) / gridDim.y;
+  const int i0 = min(g.nxc, (int)blockIdx.y * chunk), i1 = min(g.nxc, i0 + chunk);
+  if (i0 >= i1) return;  // uniform per block
+  const int lo = max(i0 - 1, 0), hi = min(i1, g.nxc - 1), khi = hi - lo;  // staged planes lo..hi
+  const int jlo = max(jt - 1, 0), jhi = min(jt + tj, g.nyc - 1), ohi = min(jt + tj, g.nyc) - 1;
+  const uint32_t hbytes = (uint32_t)((jhi - jlo + 1) * nz * 4), obytes = (uint32_t)((ohi - jt + 1) * nz * 4);
+  const uint32_t txb = src.na * hbytes + (src.own ? obytes : 0u);
+  const long long nyz = (long long)g.nyc * nz;
+  int issued = -1;  // thread 0: highest plane index issued
+  auto issue = [&](int k) {
+    const int s = k % kStages;
+    float *dst = stage0 + s * SS;
+    const long long plane = (long long)(lo + k) * nyz;
+    mbar_expect_tx(&full[s], txb);
+    for (int a = 0; a < src.na; ++a)
+      bulk_load(dst + a * SA + (long long)(jlo - (jt - 1)) * nz, src.a[a] + plane + (long long)jlo * nz, hbytes,
+                &full[s]);
+    if (src.own) bulk_load(dst + src.na * SA, src.own + plane + (long long)jt * nz, obytes, &full[s]);
+    issued = k;
+  };
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kBlock / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    bad = 0;
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int k = 0; k <= min(khi, kStages - 1); ++k) issue(k);
+  auto fail = [&]() {
+    *(volatile int *)&bad = 1;
+    atomicExch(&sc->fault, 1);
+  };
+  auto wait_full = [&](int k) {
+    if (mbar_wait(&full[k % kStages], (k / kStages) & 1)) return true;
+    fail();
+    return false;
+  };
+  auto arrays = [&](int k) { return stage0 + (k % kStages) * SS; };
+  auto release = [&](int k) {
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[k % kStages]);
+  };
+  auto refill = [&](int k) {  // thread 0: plane k was released by every warp -> load plane k + kStages
+    if (tid != 0 || k < 0 || k + kStages > khi) return;
+    if (!mbar_wait(&empty[k % kStages], (k / kStages) & 1)) {
+      fail();
+      return;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    issue(k + kStages);
+  };
+  const int own = ty + 1;  // this thread's stage row
+  int kc = i0 - lo;        // stage index of the centre plane
+  int waited = -1;         // highest plane this thread waited for
+  bool ok = wait_full(0);
+  waited = 0;
+  F4 fm{}, fc{};
+  if (ok && kc == 1) {
+    ok = wait_full(1);
+    waited = 1;
+  }
+  if (ok) {
+    if (kc == 1) {
+      if (on) fm = fval(arrays(0), own, kc0);
+      release(0);
+    }
+    if (on) fc = fval(arrays(kc), own, kc0);
+  }
+  long long row = ((long long)i0 * g.nyc + jc) * nz + kc0;
+  for (int ic = i0; ok && ic < i1; ++ic, ++kc, row += nyz) {
+    if (*(volatile int *)&bad) {
+      ok = false;
+      break;
+    }
+    F4 fp{}, ym{}, yp{};
+    if (ic + 1 < g.nxc) {
+      if (!wait_full(kc + 1)) {
+        ok = false;
+        break;
+      }
+      waited = kc + 1;
+      if (on) fp = fval(arrays(kc + 1), own, kc0);
+    }
+    const float *arr = arrays(kc);
+    if (on) {
+      if (jc > 0) ym = fval(arr, own - 1, kc0);
+      if (jc + 1 < g.nyc) yp = fval(arr, own + 1, kc0);
+    }
+    const float l = __shfl_up_sync(0xffffffffu, fc.v[3], 1);
+    const float r = __shfl_down_sync(0xffffffffu, fc.v[0], 1);
+    const float zl = tq == 0 ? 0.0f : (lane > 0 ? l : (on ? f1(arr, own, kc0 - 1) : 0.0f));
+    const float zr = tq == nq - 1 ? 0.0f : (lane < 31 ? r : (on ? f1(arr, own, kc0 + 4) : 0.0f));
+    const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
+    F4 y;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float *c = st.c[cxy + axis_class(kc0 + q, nz)];
+      const float f0 = fc.v[q];
+      const float zm = q == 0 ? zl : fc.v[q - 1], zp = q == 3 ? zr : fc.v[q + 1];
+      float t = c[0] * (fm.v[q] - f0);
+      t = fmaf(c[1], ym.v[q] - f0, t);
+      t = fmaf(c[2], zm - f0, t);
+      t = fmaf(c[4], zp - f0, t);
+      t = fmaf(c[5], yp.v[q] - f0, t);
+      t = fmaf(c[6], fp.v[q] - f0, t);
+      y.v[q] = t;
+    }
+    if (on) body(row, fc, y, src.own ? arr + src.na * SA + (long long)ty * nz + kc0 : nullptr);
+    release(kc);
+    refill(kc - 1);
+    fm = fc;
+    fc = fp;
+  }
+  if (!ok && tid == 0)  // stopped early: let this block's copies land before it exits
+    for (int k = waited + 1; k <= issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1);
+}
+
+__device__ __forceinline__ F4 lds4(const float *p) {
+  const float4 t = *reinterpret_cast<const float4 *>(p);
+  return F4{{t.x, t.y, t.z, t.w}};
+}
+
+__global__ void __launch_bounds__(kBlock) k32t_pap(Geo g, Stencil<float> st, Vec32 v, double *part,
+                                                   SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float b = (float)sc->beta, w = (float)sc->omega;
+  const bool rst = sc->restart != 0;
+  const float *po = (parity ? v.p[1] : v.p[0]);
+  const float *apo = (parity ? v.ap[1] : v.ap[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  float *__restrict__ apn = (parity ? v.ap[0] : v.ap[1]);
+  float *__restrict__ r0 = v.r0;
+  const long long SA = (long long)(g.tj + 2) * g.nzc;
+  const int nz = g.nzc;
+  Dot2F acc;
+  if (rst) {
+    const StageSrc src{{v.r1, nullptr, nullptr}, 1, nullptr};
+    tma_march(
+        g, st, src, sc, [&](const float *a, int r, int k) { return lds4(a + r * nz + k); },
+        [&](const float *a, int r, int k) { return a[r * nz + k]; },
+        [&](long long row, const F4 &pc, const F4 &y, const float *) {
+          st4(pn + row, pc);
+          st4(apn + row, y);
+          st4(r0 + row, pc);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) acc.add(y.v[t], pc.v[t]);
+        });
+  } else {
+    const StageSrc src{{v.r1, po, apo}, 3, r0};
+    auto f4 = [&](const float *a, int r, int k) {
+      const int o = r * nz + k;
+      const F4 rr = lds4(a + o), pp = lds4(a + SA + o), aa = lds4(a + 2 * SA + o);
+      F4 f;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) f.v[t] = fmaf(b, fmaf(-w, aa.v[t], pp.v[t]), rr.v[t]);
+      return f;
+    };
+    tma_march(
+        g, st, src, sc, f4,
+        [&](const float *a, int r, int k) {
+          const int o = r * nz + k;
+          return fmaf(b, fmaf(-w, a[2 * SA + o], a[SA + o]), a[o]);
+        },
+        [&](long long row, const F4 &pc, const F4 &y, const float *z0) {
+          st4(pn + row, pc);
+          st4(apn + row, y);
+          const F4 z = lds4(z0);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) acc.add(y.v[t], z.v[t]);
+        });
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k32t_sas(Geo g, Stencil<float> st, Vec32 v, double *part,
+                                                   SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float al = (float)sc->alpha;
+  const float *ap = (parity ? v.ap[0] : v.ap[1]);
+  float *__restrict__ sv = v.s;
+  float *__restrict__ asv = v.as;
+  const long long SA = (long long)(g.tj + 2) * g.nzc;
+  const int nz = g.nzc;
+  Dot2F a0, a1;
+  const StageSrc src{{v.r1, ap, nullptr}, 2, nullptr};
+  tma_march(
+      g, st, src, sc,
+      [&](const float *a, int r, int k) {
+        const int o = r * nz + k;
+        const F4 rr = lds4(a + o), pp = lds4(a + SA + o);
+        F4 f;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) f.v[t] = fmaf(-al, pp.v[t], rr.v[t]);
+        return f;
+      },
+      [&](const float *a, int r, int k) { return fmaf(-al, a[SA + r * nz + k], a[r * nz + k]); },
+      [&](long long row, const F4 &s4, const F4 &y, const float *) {
+        st4(sv + row, s4);
+        st4(asv + row, y);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          a0.add(y.v[t], s4.v[t]);
+          a1.add(y.v[t], y.v[t]);
+        }
+      });
+  double acc[2] = {a0.get(), a1.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;  // see k32_sas
+    sc->omega = wv;
+  }
+}
+
+// Shared memory of the bulk-copy kernels (the larger pap variant) and their residency;
+// 0 when the grid does not fit the scheme (nz % 4 != 0 or more than 256 quads per row).
+int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm) {
+  if (nzc % 4 != 0 || nzc / 4 > kBlock) return 0;
+  const int t = kBlock / (nzc / 4);
+  const long long bytes = 128 + kStages * stage_floats(t, nzc, 3, true) * 4;
+  if (bytes > 227 * 1024) return 0;
+  *tj = t;
+  *smem_bytes = (int)bytes;
+  if (cudaFuncSetAttribute(k32t_pap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k32t_sas, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32t_pap, kBlock, (size_t)bytes) != cudaSuccess || n < 1)
+    return 0;
+  *blocks_per_sm = n;
+  (void)nyc;
+  return 1;
+}
+
+// x += alpha p + omega s; r1 = s - omega as; ||r1||^2, <r1, r0>.  Pointwise, so a flat
+// grid-stride loop over quads with a grid sized to fill every SM (g.xgrid blocks), two
+// quads per trip so that ten 16-byte loads are in flight per thread.
 __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, SolverScal *sc) {
   if (sc->done) return;
   const int parity = sc->par;
   const float a = (float)sc->alpha, w = (float)sc->omega;
   const float *__restrict__ p = (parity ? v.p[0] : v.p[1]);
-  float n2 = 0.0f, rr = 0.0f;
-  FOR_QUADS(g) {
-    const long long row = ROW(g);
-    const F4 s = ld4(v.s + row), as = ld4(v.as + row), pp = ld4(p + row), r0 = ld4(v.r0 + row);
-    F4 x = ld4(v.x + row), r1;
+  const float *__restrict__ sv = v.s;
+  const float *__restrict__ asv = v.as;
+  const float *__restrict__ r0v = v.r0;
+  float *__restrict__ xv = v.x;
+  float *__restrict__ r1v = v.r1;
+  Dot2F n2, rr;
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < nq; q0 += 2 * stride) {
+    const long long q1 = q0 + stride;
+    const bool two = q1 < nq;
+    F4 s[2], as[2], pp[2], r0[2], x[2];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      x.v[t] = fmaf(w, s.v[t], fmaf(a, pp.v[t], x.v[t]));
-      r1.v[t] = fmaf(-w, as.v[t], s.v[t]);
-      n2 = fmaf(r1.v[t], r1.v[t], n2);
-      rr = fmaf(r1.v[t], r0.v[t], rr);
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 && !two) break;
+      const long long row = 4 * (u ? q1 : q0);
+      s[u] = ld4(sv + row);
+      as[u] = ld4(asv + row);
+      pp[u] = ld4(p + row);
+      r0[u] = ld4(r0v + row);
+      x[u] = ld4(xv + row);
     }
-    st4(v.x + row, x);
-    st4(v.r1 + row, r1);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (u == 1 && !two) break;
+      const long long row = 4 * (u ? q1 : q0);
+      F4 r1;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        x[u].v[t] = fmaf(w, s[u].v[t], fmaf(a, pp[u].v[t], x[u].v[t]));
+        r1.v[t] = fmaf(-w, as[u].v[t], s[u].v[t]);
+        n2.add(r1.v[t], r1.v[t]);
+        rr.add(r1.v[t], r0[u].v[t]);
+      }
+      st4(xv + row, x[u]);
+      st4(r1v + row, r1);
+    }
   }
-  double acc[2] = {(double)n2, (double)rr}, out[2];
+  double acc[2] = {n2.get(), rr.get()}, out[2];
   if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) {
     sc->par ^= 1;  // this iteration's p and ap become the previous ones
     finish_iteration<true>(sc, out[0], out[1]);
   }
+}
+
+int fp32_pointwise_blocks_per_sm() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32v_xr, kBlock, 0) != cudaSuccess) n = 4;
+  return n > 0 ? n : 1;
 }
 
 // bicgstabRe2.hpp:133-153: at the cap, NaN/Inf entries come from the previous solution;
@@ -569,8 +901,9 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
 // correction accumulates in the FP32 x.  The refinement adds scale * x to the FP64
 // solution and recomputes r64 = b - A x in FP64, which starts the next sweep.  Keeping the
 // Krylov space across refinements (reliable updates) was measured too: on the 512-cell
-// axis the FP32 iteration then loses bi-orthogonality near 1e-3 and stalls, while short
-// restarted sweeps converge to the FP64 tolerance.
+// axis the FP32 iteration then breaks down near 1e-3 (with compensated dot products as
+// well: the FP32 vectors and stencil are the limit), while short restarted sweeps
+// converge to the FP64 tolerance.
 
 // r64 = b - A x (FP64); ||r||, ||b|| (flags & 1) and the scale (flags & 2).
 // jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose unscaled residual is r / jp.
@@ -617,18 +950,19 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
                                                             double delta, int first, double *part, SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
   const double m = ss->rsum / (double)g.ncell;
-  AccF acc;
+  Dot2F acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const float r = scaled_residual(g, st, jacobi, r64, m, inv, ic, jc, kc, row);
     v.x[row] = 0.0f;
     v.r0[row] = r;
     v.r1[row] = r;
-    acc.add(r * r);
+    acc.add(r, r);
   }
   double a[1] = {acc.get()}, out[1];
   if (grid_sum<1>(a, part, &sc->cnt[0], out) && lin_tid() == 0) {
     if (first) {
+      sc->fault = 0;
       sc->timestep += 1;
       sc->norm0 = ss->bnorm * inv;  // relres = ||r1|| scale / ||b||
       sc->delta = delta;
@@ -767,12 +1101,20 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
                         KrylovVecs<float> v, float *const p2[2], float *const ap2[2], double *part_buf,
                         SolverScal *sc) {
   const Vec32 w = v32(v, p2, ap2);
+  if (g.tma && part < 2) {  // stencil kernels on the bulk-copy pipeline
+    const dim3 tg(g.tgx, g.tgy, 1);
+    if (part == 0)
+      k32t_pap<<<tg, kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+    else
+      k32t_sas<<<tg, kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+    return;
+  }
   if (g.vbx > 0) {  // vectorised path
     const dim3 vg(g.vgx, g.vgy, g.vgz), vb(g.vbx, g.vby, 1);
     switch (part) {
       case 0: k32v_pap<<<vg, vb, 0, s>>>(g, st, w, part_buf, sc); break;
       case 1: k32v_sas<<<vg, vb, 0, s>>>(g, st, w, part_buf, sc); break;
-      default: k32v_xr<<<vg, vb, 0, s>>>(g, w, part_buf, sc); break;
+      default: k32v_xr<<<g.xgrid, kBlock, 0, s>>>(g, w, part_buf, sc); break;
     }
     return;
   }
