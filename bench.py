@@ -62,12 +62,19 @@ KERNEL_WORDS = {
     "bicg_pap32": 6,   # read r1, p, ap, r0; write p', ap'
     "bicg_sas32": 4,   # read r1, ap; write s, as
     "bicg_xr32": 7,    # read x, p, s, as, r0; write x, r1
+    # CG (the reference's cg.hpp method): FP64 three kernels, 11 words; FP32 sweeps two, 10
+    "cg_q64": 2,       # read p; write q
+    "cg_xr64": 6,      # read x, p, r, q; write x, r
+    "cg_p64": 3,       # read r, p; write p
+    "cg_pq32": 4,      # read r, p; write p', q
+    "cg_xr32": 6,      # read x, p, r, q; write x, r
 }
 
 
 # FP64 flops per interior cell and launch of the FP64 iteration kernels (an FMA counts 2):
 # SpMV 1 mul + 6 FMA, each dot 1 FMA, each axpy-like update 1 FMA per term
-KERNEL_FP64_FLOPS = {"bicg_ap64": 15, "bicg_s64": 2, "bicg_as64": 17, "bicg_xr64": 10, "bicg_p64": 4}
+KERNEL_FP64_FLOPS = {"bicg_ap64": 15, "bicg_s64": 2, "bicg_as64": 17, "bicg_xr64": 10, "bicg_p64": 4,
+                     "cg_q64": 15, "cg_xr64": 6, "cg_p64": 2}
 
 
 def alu_peaks():
@@ -382,7 +389,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cfdgb", choices=["cfdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--modes", default="fp64,mixed,rbsor,e2e,adjoint,cpu")
+    ap.add_argument("--modes", default="fp64,mixed,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
@@ -405,7 +412,8 @@ def main(argv=None):
 
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
-        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64", keep_fields="mixed" in modes)
+        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64",
+                        keep_fields=bool(modes & {"mixed", "cg", "mixed_cg"}))
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
     value = cells * args.steps * dist.world / (t64 / 1e3)
@@ -436,6 +444,23 @@ def main(argv=None):
                              "gpu_launches": mx["launches"], "roofline": r32, "kernel_share": share32}
         except cg.CfdgbError as e:
             line["mixed"] = {"value": None, "error": str(e)}
+    for key, solver, prec in (("cg", "cg", "fp64"), ("mixed_cg", "cg", "mixed")):
+        if key not in modes:
+            continue
+        try:
+            rm = run_mode(cg, torch, dist, wl, args.steps, args.warmup, solver, prec, keep_fields=True)
+            tm = dist.max(rm["ms"])
+            rf, shr = roofline(rm["kernels"], cells, 4 if prec == "mixed" else 8, "32" if prec == "mixed" else "64",
+                               hbm_peak, peak_kind, traffic_file)
+            line[key] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
+                         "solver": "cg (SPE operator)", "precision": prec,
+                         "iters_per_step": [r.iters for r in rm["stats"]],
+                         "outer_per_step": [r.outer for r in rm["stats"]],
+                         "relres": max(r.relres for r in rm["stats"]), "speedup_vs_fp64": t64 / tm,
+                         "error_vs_fp64": field_errors(rm, fp64), "gpu_launches": rm["launches"],
+                         "roofline": rf, "kernel_share": shr}
+        except cg.CfdgbError as e:
+            line[key] = {"value": None, "error": str(e)}
     if "rbsor" in modes:
         sr = run_mode(cg, torch, dist, wl, args.sor_steps, args.warmup, "rbsor", "fp64", maxit=args.sor_maxit,
                       profile=False)

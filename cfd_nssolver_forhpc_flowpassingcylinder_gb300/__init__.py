@@ -19,10 +19,10 @@ LIB_PATH = PKG / "libcfdgb.so"
 
 ABI_VERSION = 2  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
-BICGSTAB, BICGSTAB_JACOBI, RBSOR = 0, 1, 2
+BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 SOLVERS = {"bicgstab": BICGSTAB, "spe": BICGSTAB, "jacobi": BICGSTAB_JACOBI, "csr": BICGSTAB_JACOBI,
-           "rbsor": RBSOR, "sor": RBSOR}
+           "rbsor": RBSOR, "sor": RBSOR, "cg": CG}
 PRECISIONS = {"fp64": FP64, "mixed": MIXED}
 
 

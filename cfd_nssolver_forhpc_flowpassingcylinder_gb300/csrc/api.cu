@@ -58,12 +58,14 @@ uint64_t splitmix64(uint64_t &s) {
 // Kernels the instrumentation tells apart (cfdgb_kernel_stat).
 enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
-  K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA, K_COUNT
+  K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
+  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
-    "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction"};
+    "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
+    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32"};
 
 struct PendingEv {
   int id;
@@ -283,31 +285,47 @@ int validate(const cfdgb_config *c) {
   if (cells > 4.0e9) return fail(CFDGB_EINVAL, "padded grid above 4e9 cells");
   if (!(c->lx > 0 && c->ly > 0 && c->lz > 0)) return fail(CFDGB_EINVAL, "domain lengths must be positive");
   if (!(c->Re > 0) || !(c->dt > 0)) return fail(CFDGB_EINVAL, "Re and dt must be positive");
-  if (c->solver < 0 || c->solver > 2) return fail(CFDGB_EINVAL, "unknown solver %d", c->solver);
+  if (c->solver < 0 || c->solver > 3) return fail(CFDGB_EINVAL, "unknown solver %d", c->solver);
   if (c->precision < 0 || c->precision > 1) return fail(CFDGB_EINVAL, "unknown precision %d", c->precision);
   if (!(c->tol > 0)) return fail(CFDGB_EINVAL, "tol must be positive");
   if (c->maxit < 1) return fail(CFDGB_EINVAL, "maxit must be >= 1");
   if (c->solver == CFDGB_RBSOR && !(c->omega > 0 && c->omega < 2)) return fail(CFDGB_EINVAL, "omega outside (0,2)");
   if (c->precision == CFDGB_MIXED && c->solver == CFDGB_RBSOR)
-    return fail(CFDGB_EINVAL, "MIXED precision is implemented for the BiCGSTAB solvers");
+    return fail(CFDGB_EINVAL, "MIXED precision is implemented for the Krylov solvers");
   if (c->precision == CFDGB_MIXED && !(c->inner_tol > 0 && c->inner_tol < 1))
     return fail(CFDGB_EINVAL, "inner_tol outside (0,1)");
   if (c->dfib && !(c->radius > 0)) return fail(CFDGB_EINVAL, "radius must be positive");
   return 0;
 }
 
+// The kernels of one Krylov iteration: BiCGSTAB 5 (FP64) / 3 (FP32), CG 3 / 2.
+int iter_kernels(const cfdgb_ctx *c, bool fp32) {
+  if (c->cfg.solver == CFDGB_CG) return fp32 ? 2 : 3;
+  return fp32 ? 3 : 5;
+}
+int iter_kid(const cfdgb_ctx *c, bool fp32, int part) {
+  if (c->cfg.solver == CFDGB_CG) return (fp32 ? K_CGPQ32 : K_CGQ64) + part;
+  return (fp32 ? K_PAP32 : K_AP64) + part;
+}
+void launch_iter_kernel(cfdgb_ctx *c, bool fp32, int part) {
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  if (c->cfg.solver == CFDGB_CG) {
+    if (fp32)
+      launch_cg32_part(c->stream, part, c->g, c->spe32, c->k32, c->p32, c->ap32, c->part, c->sc32);
+    else
+      launch_cg64_part(c->stream, part, c->g, c->spe64, c->k64, c->part, c->sc);
+  } else if (fp32) {
+    launch_bicg32_part(c->stream, part, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part, c->sc32);
+  } else {
+    launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
+  }
+}
+
 int capture_chunk(cfdgb_ctx *c, bool fp32) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
-  for (int m = 0; m < c->chunk_len; ++m) {
-    if (fp32)
-      for (int part = 0; part < 3; ++part)
-        launch_bicg32_part(c->stream, part, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part, c->sc32);
-    else
-      for (int part = 0; part < 5; ++part)
-        launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
-  }
+  for (int m = 0; m < c->chunk_len; ++m)
+    for (int part = 0; part < iter_kernels(c, fp32); ++part) launch_iter_kernel(c, fp32, part);
   CK(cudaStreamEndCapture(c->stream, &graph));
   cudaGraphExec_t exec;
   cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
@@ -335,28 +353,17 @@ int set_solver_params(cfdgb_ctx *c, SolverScal *dsc, double tol, int maxit) {
 // are launched one by one between event pairs instead.
 int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   SolverScal *dsc = fp32 ? c->sc32 : c->sc;
-  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   if (!c->timing && !(fp32 ? c->chunk32 : c->chunk64)) TRY(capture_chunk(c, fp32));
   const long long max_chunks = (long long)c->cfg.maxit / c->chunk_len + 3;
+  const int nk = iter_kernels(c, fp32);
   for (long long q = 0; q < max_chunks; ++q) {
     if (c->timing) {
-      for (int m = 0; m < c->chunk_len; ++m) {
-        if (fp32)
-          for (int part = 0; part < 3; ++part)
-            L(c, K_PAP32 + part, 1, [&] {
-              launch_bicg32_part(c->stream, part, c->g, jac ? c->jac32 : c->spe32, c->k32, c->p32, c->ap32, c->part,
-                                 c->sc32);
-            });
-        else
-          for (int part = 0; part < 5; ++part)
-            L(c, K_AP64 + part, 1, [&] {
-              launch_bicg64_part(c->stream, part, c->g, jac ? c->jac64 : c->spe64, c->k64, c->part, c->sc);
-            });
-      }
+      for (int m = 0; m < c->chunk_len; ++m)
+        for (int part = 0; part < nk; ++part)
+          L(c, iter_kid(c, fp32, part), 1, [&] { launch_iter_kernel(c, fp32, part); });
     } else {
-      const int first = fp32 ? K_PAP32 : K_AP64, nk = fp32 ? 3 : 5;
       c->launches += (long long)nk * c->chunk_len;
-      for (int part = 0; part < nk; ++part) c->kn[first + part] += c->chunk_len;
+      for (int part = 0; part < nk; ++part) c->kn[iter_kid(c, fp32, part)] += c->chunk_len;
       CK(cudaGraphLaunch(fp32 ? c->chunk32 : c->chunk64, c->stream));
     }
     CK(cudaMemcpyAsync(c->h_sc, dsc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
@@ -374,6 +381,14 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
     }
   }
   return fail(CFDGB_ECUDA, "solver did not report completion");
+}
+
+// FP64 Krylov set-up on the current b and warm start x
+void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
+  if (c->cfg.solver == CFDGB_CG)
+    launch_cg_setup64(c->stream, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc);
+  else
+    launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc);
 }
 
 // createBMatrix + solve + (caller) transform, on the current u*.  Fills iters/relres.
@@ -408,7 +423,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   }
   if (c->cfg.precision == CFDGB_FP64) {
     TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
-    L(c, K_SETUP64, 1, [&] { launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc); });
+    L(c, K_SETUP64, 1, [&] { launch_setup64(c, st64); });
     SolverScal r;
     TRY(run_chunks(c, false, &r));
     if (r.status == CFDGB_ENOCONV)
@@ -505,7 +520,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   }
   if (finish64) {
     TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
-    L(c, K_SETUP64, 1, [&] { launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc); });
+    L(c, K_SETUP64, 1, [&] { launch_setup64(c, st64); });
     SolverScal r;
     TRY(run_chunks(c, false, &r));
     if (trace) std::fprintf(stderr, "[cfdgb]   FP64 finish iters %d status %d relres %.3e\n", r.iter, r.status, r.relres);

@@ -49,6 +49,15 @@ int fp32_pointwise_blocks_per_sm();
 // bulk-copy pipeline of the FP32 stencil kernels: rows per block, dynamic shared memory,
 // resident blocks per SM; returns 0 when the grid does not fit it
 int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm);
+// CG on the SPE operator (inc/solver/cg.hpp): set-up r = b - A x, p = r; FP64 iteration
+// kernels 0..2 (q = A p, x and r, p update); FP32 sweep kernels 0..1 (p update + A p,
+// x and r), p double-buffered like the BiCGSTAB sweeps, q in ap2[0]
+void launch_cg_setup64(cudaStream_t s, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v, const double *b,
+                       double *px1, double *px2, double *part, SolverScal *sc);
+void launch_cg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
+                      double *part_buf, SolverScal *sc);
+void launch_cg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, KrylovVecs<float> v,
+                      float *const p2[2], float *const ap2[2], double *part_buf, SolverScal *sc);
 // after the loop: NaN/Inf recovery of bicgstabRe2.hpp:133-153 when the cap was hit
 void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
                            const double *px2, double *part, SolverScal *sc);

@@ -107,6 +107,13 @@ struct Dot2F {
   }
   __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
+// Plain FP32 running sum of products for the vectorised kernels: a thread covers a few
+// dozen quads, and the sum over threads is FP64 (grid_sum).
+struct SumF {
+  float f = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) { f = fmaf(a, b, f); }
+  __device__ __forceinline__ double get() const { return (double)f; }
+};
 struct AccD {
   double d = 0.0;
   __device__ __forceinline__ void add(double x) { d += x; }

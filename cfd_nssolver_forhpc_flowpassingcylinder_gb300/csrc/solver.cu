@@ -394,10 +394,12 @@ __device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &
     const float zr = !kr ? 0.0f : (sr ? r : (on ? f1(row + 4) : 0.0f));
     // difference form (stencil_apply_diff); a missing neighbour has coefficient 0
     const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
+    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 ? 0 : 1)],
+                *clast = st.c[cxy + (kc0 + 4 == g.nzc ? 2 : 1)];
     F4 y;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const float *c = st.c[cxy + axis_class(kc0 + q, g.nzc)];
+      const float *c = q == 0 ? cfirst : (q == 3 ? clast : cmid);
       const float f0 = fc.v[q];
       const float zm = q == 0 ? zl : fc.v[q - 1], zp = q == 3 ? zr : fc.v[q + 1];
       float t = c[0] * (fm.v[q] - f0);
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(kBlock) k32v_pap(Geo g, Stencil<float> st, Vec
   float *__restrict__ apn = (parity ? v.ap[0] : v.ap[1]);
   const float *__restrict__ r1 = v.r1;
   float *__restrict__ r0 = v.r0;
-  Dot2F acc;
+  SumF acc;
   if (rst) {
     march_quads(
         g, st, [&](long long q) { return ld4(r1 + q); }, [&](long long q) { return r1[q]; },
@@ -472,7 +474,7 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
   const float *__restrict__ r1 = v.r1;
   float *__restrict__ sv = v.s;
   float *__restrict__ asv = v.as;
-  Dot2F a0, a1;
+  SumF a0, a1;
   march_quads(
       g, st,
       [&](long long q) {
@@ -672,10 +674,12 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     const float zl = tq == 0 ? 0.0f : (lane > 0 ? l : (on ? f1(arr, own, kc0 - 1) : 0.0f));
     const float zr = tq == nq - 1 ? 0.0f : (lane < 31 ? r : (on ? f1(arr, own, kc0 + 4) : 0.0f));
     const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
+    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 ? 0 : 1)],
+                *clast = st.c[cxy + (kc0 + 4 == nz ? 2 : 1)];
     F4 y;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const float *c = st.c[cxy + axis_class(kc0 + q, nz)];
+      const float *c = q == 0 ? cfirst : (q == 3 ? clast : cmid);
       const float f0 = fc.v[q];
       const float zm = q == 0 ? zl : fc.v[q - 1], zp = q == 3 ? zr : fc.v[q + 1];
       float t = c[0] * (fm.v[q] - f0);
@@ -714,7 +718,7 @@ __global__ void __launch_bounds__(kBlock) k32t_pap(Geo g, Stencil<float> st, Vec
   float *__restrict__ r0 = v.r0;
   const long long SA = (long long)(g.tj + 2) * g.nzc;
   const int nz = g.nzc;
-  Dot2F acc;
+  SumF acc;
   if (rst) {
     const StageSrc src{{v.r1, nullptr, nullptr}, 1, nullptr};
     tma_march(
@@ -765,7 +769,7 @@ __global__ void __launch_bounds__(kBlock) k32t_sas(Geo g, Stencil<float> st, Vec
   float *__restrict__ asv = v.as;
   const long long SA = (long long)(g.tj + 2) * g.nzc;
   const int nz = g.nzc;
-  Dot2F a0, a1;
+  SumF a0, a1;
   const StageSrc src{{v.r1, ap, nullptr}, 2, nullptr};
   tma_march(
       g, st, src, sc,
@@ -797,6 +801,8 @@ __global__ void __launch_bounds__(kBlock) k32t_sas(Geo g, Stencil<float> st, Vec
 
 // Shared memory of the bulk-copy kernels (the larger pap variant) and their residency;
 // 0 when the grid does not fit the scheme (nz % 4 != 0 or more than 256 quads per row).
+__global__ void k32cgt_pq(Geo g, Stencil<float> st, Vec32 v, double *part, SolverScal *sc);
+
 int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm) {
   if (nzc % 4 != 0 || nzc / 4 > kBlock) return 0;
   const int t = kBlock / (nzc / 4);
@@ -805,7 +811,8 @@ int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_
   *tj = t;
   *smem_bytes = (int)bytes;
   if (cudaFuncSetAttribute(k32t_pap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
-      cudaFuncSetAttribute(k32t_sas, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      cudaFuncSetAttribute(k32t_sas, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k32cgt_pq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
     return 0;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32t_pap, kBlock, (size_t)bytes) != cudaSuccess || n < 1)
@@ -816,8 +823,7 @@ int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_
 }
 
 // x += alpha p + omega s; r1 = s - omega as; ||r1||^2, <r1, r0>.  Pointwise, so a flat
-// grid-stride loop over quads with a grid sized to fill every SM (g.xgrid blocks), two
-// quads per trip so that ten 16-byte loads are in flight per thread.
+// grid-stride loop over quads with a grid sized to fill every SM (g.xgrid blocks).
 __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, SolverScal *sc) {
   if (sc->done) return;
   const int parity = sc->par;
@@ -828,37 +834,21 @@ __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, 
   const float *__restrict__ r0v = v.r0;
   float *__restrict__ xv = v.x;
   float *__restrict__ r1v = v.r1;
-  Dot2F n2, rr;
+  SumF n2, rr;
   const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
-  for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < nq; q0 += 2 * stride) {
-    const long long q1 = q0 + stride;
-    const bool two = q1 < nq;
-    F4 s[2], as[2], pp[2], r0[2], x[2];
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const long long row = 4 * q;
+    const F4 s = ld4(sv + row), as = ld4(asv + row), pp = ld4(p + row), r0 = ld4(r0v + row);
+    F4 x = ld4(xv + row), r1;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (u == 1 && !two) break;
-      const long long row = 4 * (u ? q1 : q0);
-      s[u] = ld4(sv + row);
-      as[u] = ld4(asv + row);
-      pp[u] = ld4(p + row);
-      r0[u] = ld4(r0v + row);
-      x[u] = ld4(xv + row);
+    for (int t = 0; t < 4; ++t) {
+      x.v[t] = fmaf(w, s.v[t], fmaf(a, pp.v[t], x.v[t]));
+      r1.v[t] = fmaf(-w, as.v[t], s.v[t]);
+      n2.add(r1.v[t], r1.v[t]);
+      rr.add(r1.v[t], r0.v[t]);
     }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (u == 1 && !two) break;
-      const long long row = 4 * (u ? q1 : q0);
-      F4 r1;
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        x[u].v[t] = fmaf(w, s[u].v[t], fmaf(a, pp[u].v[t], x[u].v[t]));
-        r1.v[t] = fmaf(-w, as[u].v[t], s[u].v[t]);
-        n2.add(r1.v[t], r1.v[t]);
-        rr.add(r1.v[t], r0[u].v[t]);
-      }
-      st4(xv + row, x[u]);
-      st4(r1v + row, r1);
-    }
+    st4(xv + row, x);
+    st4(r1v + row, r1);
   }
   double acc[2] = {n2.get(), rr.get()}, out[2];
   if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) {
@@ -871,6 +861,268 @@ int fp32_pointwise_blocks_per_sm() {
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32v_xr, kBlock, 0) != cudaSuccess) n = 4;
   return n > 0 ? n : 1;
+}
+
+// ---- conjugate gradients on the SPE operator ----
+// The reference's other Krylov solver, inc/solver/cg.hpp (selected by P_SOLVER_CG_ELL):
+// unpreconditioned CG, x += alpha p, r -= alpha q, beta = <r, r>_new / <r, r>_old.  (That
+// header does not compile as published; the method it spells out is followed, with
+// bicgstabRe2's stop test ||r|| / ||b|| < tol and iteration cap.)  Three FP64 kernels per
+// iteration; the FP32 sweeps of the MIXED mode fuse the p update into the SpMV (two
+// kernels, 10 words per cell).
+__device__ __forceinline__ void finish_cg64(SolverScal *sc, double n2) {
+  const double relres = sqrt(n2) / sc->norm0;
+  sc->relres = relres;
+  if (relres < sc->tol) {
+    sc->done = 1;
+  } else if (!isfinite(relres)) {
+    sc->done = 1;
+    sc->status = CFDGB_ENAN;
+  } else if (sc->iter >= sc->maxit) {
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+  } else {
+    sc->beta = n2 / sc->rho;
+    sc->rho = n2;
+    sc->iter += 1;
+  }
+}
+
+// r = b - A x, p = r; history px2 <- px1 <- x (the NaN recovery of the BiCGSTAB path)
+__global__ void __launch_bounds__(kBlock) k64cg_setup(Geo g, Stencil<double> st, KrylovVecs<double> v,
+                                                       const double *__restrict__ b, double *px1, double *px2,
+                                                       double *part, SolverScal *sc) {
+  double acc[2] = {0.0, 0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double bb = b[row];
+    const double r = bb - spmv_at<double>(g, st, v.x, ic, jc, kc, row);
+    v.r1[row] = r;
+    v.p1[row] = r;
+    px2[row] = px1[row];
+    px1[row] = v.x[row];
+    acc[0] += bb * bb;
+    acc[1] += r * r;
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[0], out) && lin_tid() == 0) {
+    sc->timestep += 1;
+    sc->norm0 = sqrt(out[0]);
+    sc->rho = out[1];
+    sc->iter = 0;
+    sc->status = 0;
+    sc->relres = sqrt(out[1]) / sc->norm0;
+    sc->done = (sc->relres < sc->tol) ? 1 : 0;
+  }
+}
+// q = A p, alpha = rho / <p, q>
+__global__ void __launch_bounds__(kBlock) k64cg_q(Geo g, Stencil<double> st, KrylovVecs<double> v, double *part,
+                                                   SolverScal *sc) {
+  if (sc->done) return;
+  double a[1] = {0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double q = spmv_at<double>(g, st, v.p1, ic, jc, kc, row);
+    v.ap[row] = q;
+    a[0] += q * v.p1[row];
+  }
+  double out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+// x += alpha p, r -= alpha q, ||r||^2: stop test and beta
+__global__ void __launch_bounds__(kBlock) k64cg_xr(Geo g, KrylovVecs<double> v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const double al = sc->alpha;
+  double a[1] = {0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.x[row] = fma(al, v.p1[row], v.x[row]);
+    const double r = fma(-al, v.ap[row], v.r1[row]);
+    v.r1[row] = r;
+    a[0] += r * r;
+  }
+  double out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[3], out) && lin_tid() == 0) finish_cg64(sc, out[0]);
+}
+// p = r + beta p
+__global__ void __launch_bounds__(kBlock) k64cg_p(Geo g, KrylovVecs<double> v, const SolverScal *sc) {
+  if (sc->done) return;
+  const double be = sc->beta;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.p1[row] = fma(be, v.p1[row], v.r1[row]);
+  }
+}
+
+// FP32 sweep (MIXED): hand over to the FP64 refinement like the BiCGSTAB sweeps
+__device__ __forceinline__ void finish_cg32(SolverScal *sc, double n2) {
+  const double relres = sqrt(n2) / sc->norm0, rn = sqrt(n2);
+  sc->relres = relres;
+  if (relres < sc->best) sc->best = relres;
+  if (!isfinite(relres)) {
+    sc->done = 1;
+    sc->status = CFDGB_ENAN;
+  } else if (sc->iter > 16 && relres > 1e3 * sc->best) {
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+  } else if (sc->iter >= sc->maxit) {
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+    sc->iter += 1;
+  } else if (relres < sc->tol || rn < sc->delta * sc->rmax) {
+    sc->done = 1;
+    sc->status = kStatusRefine;
+    sc->iter += 1;
+  } else {
+    sc->beta = n2 / sc->rho;
+    sc->rho = n2;
+    sc->restart = 0;
+    if (!isfinite(sc->beta)) {
+      sc->restart = 1;
+      sc->rho = n2;
+    }
+    sc->rmax = fmax(sc->rmax, rn);
+    sc->iter += 1;
+  }
+}
+
+// p_new = r + beta p_old (restart: r) at the stencil points; q = A p_new; alpha = rho / <p_new, q>
+__global__ void __launch_bounds__(kBlock) k32cgt_pq(Geo g, Stencil<float> st, Vec32 v, double *part,
+                                                     SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float be = (float)sc->beta;
+  const bool rst = sc->restart != 0;
+  const float *po = (parity ? v.p[1] : v.p[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  float *__restrict__ q = v.ap[0];
+  const long long SA = (long long)(g.tj + 2) * g.nzc;
+  const int nz = g.nzc;
+  SumF acc;
+  auto body = [&](long long row, const F4 &pc, const F4 &y, const float *) {
+    st4(pn + row, pc);
+    st4(q + row, y);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc.add(y.v[t], pc.v[t]);
+  };
+  if (rst) {
+    const StageSrc src{{v.r1, nullptr, nullptr}, 1, nullptr};
+    tma_march(
+        g, st, src, sc, [&](const float *a, int r, int k) { return lds4(a + r * nz + k); },
+        [&](const float *a, int r, int k) { return a[r * nz + k]; }, body);
+  } else {
+    const StageSrc src{{v.r1, po, nullptr}, 2, nullptr};
+    tma_march(
+        g, st, src, sc,
+        [&](const float *a, int r, int k) {
+          const int o = r * nz + k;
+          const F4 rr = lds4(a + o), pp = lds4(a + SA + o);
+          F4 f;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) f.v[t] = fmaf(be, pp.v[t], rr.v[t]);
+          return f;
+        },
+        [&](const float *a, int r, int k) { return fmaf(be, a[SA + r * nz + k], a[r * nz + k]); }, body);
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+__global__ void __launch_bounds__(kBlock) k32cgv_pq(Geo g, Stencil<float> st, Vec32 v, double *part,
+                                                     SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float be = (float)sc->beta;
+  const bool rst = sc->restart != 0;
+  const float *__restrict__ po = (parity ? v.p[1] : v.p[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  float *__restrict__ q = v.ap[0];
+  const float *__restrict__ r1 = v.r1;
+  SumF acc;
+  auto body = [&](long long row, const F4 &pc, const F4 &y) {
+    st4(pn + row, pc);
+    st4(q + row, y);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc.add(y.v[t], pc.v[t]);
+  };
+  if (rst) {
+    march_quads(
+        g, st, [&](long long k) { return ld4(r1 + k); }, [&](long long k) { return r1[k]; }, body);
+  } else {
+    march_quads(
+        g, st,
+        [&](long long k) {
+          const F4 rr = ld4(r1 + k), pp = ld4(po + k);
+          F4 f;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) f.v[t] = fmaf(be, pp.v[t], rr.v[t]);
+          return f;
+        },
+        [&](long long k) { return fmaf(be, po[k], r1[k]); }, body);
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+__global__ void __launch_bounds__(kBlock) k32cg_pq(Geo g, Stencil<float> st, Vec32 v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float be = (float)sc->beta;
+  const bool rst = sc->restart != 0;
+  const float *__restrict__ po = (parity ? v.p[1] : v.p[0]);
+  float *__restrict__ pn = (parity ? v.p[0] : v.p[1]);
+  const float *__restrict__ r1 = v.r1;
+  AccF acc;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    float pc;
+    const float y = rst ? stencil_apply_diff(g, st, ic, jc, kc, row, [&](long long k) { return r1[k]; }, pc)
+                        : stencil_apply_diff(g, st, ic, jc, kc, row,
+                                             [&](long long k) { return fmaf(be, po[k], r1[k]); }, pc);
+    pn[row] = pc;
+    v.ap[0][row] = y;
+    acc.add(y * pc);
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+// x += alpha p_new; r -= alpha q; ||r||^2: refinement test and beta (flat: any cell count)
+__global__ void __launch_bounds__(kBlock) k32cg_xr(Geo g, Vec32 v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const int parity = sc->par;
+  const float al = (float)sc->alpha;
+  const float *__restrict__ p = (parity ? v.p[0] : v.p[1]);
+  const float *__restrict__ q = v.ap[0];
+  float *__restrict__ xv = v.x;
+  float *__restrict__ r1v = v.r1;
+  SumF n2;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g.ncell % 4 == 0) {
+    for (long long k = t0; k < g.ncell / 4; k += stride) {
+      const long long row = 4 * k;
+      const F4 pp = ld4(p + row), qq = ld4(q + row);
+      F4 x = ld4(xv + row), r = ld4(r1v + row);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        x.v[t] = fmaf(al, pp.v[t], x.v[t]);
+        r.v[t] = fmaf(-al, qq.v[t], r.v[t]);
+        n2.add(r.v[t], r.v[t]);
+      }
+      st4(xv + row, x);
+      st4(r1v + row, r);
+    }
+  } else {
+    for (long long row = t0; row < g.ncell; row += stride) {
+      xv[row] = fmaf(al, p[row], xv[row]);
+      const float r = fmaf(-al, q[row], r1v[row]);
+      r1v[row] = r;
+      n2.add(r, r);
+    }
+  }
+  double acc[1] = {n2.get()}, out[1];
+  if (grid_sum<1>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) {
+    sc->par ^= 1;
+    finish_cg32(sc, out[0]);
+  }
 }
 
 // bicgstabRe2.hpp:133-153: at the cap, NaN/Inf entries come from the previous solution;
@@ -1125,6 +1377,32 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
   }
 }
 
+void launch_cg_setup64(cudaStream_t s, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v, const double *b,
+                       double *px1, double *px2, double *part, SolverScal *sc) {
+  k64cg_setup<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, b, px1, px2, part, sc);
+}
+void launch_cg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
+                      double *part_buf, SolverScal *sc) {
+  switch (part) {
+    case 0: k64cg_q<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    case 1: k64cg_xr<<<cgrid(g), cblock(g), 0, s>>>(g, v, part_buf, sc); break;
+    default: k64cg_p<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+  }
+}
+void launch_cg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, KrylovVecs<float> v,
+                      float *const p2[2], float *const ap2[2], double *part_buf, SolverScal *sc) {
+  const Vec32 w = v32(v, p2, ap2);
+  if (part == 1) {
+    const int grid = g.xgrid > 0 ? g.xgrid : g.lgx * g.lgy * g.lgz;
+    k32cg_xr<<<grid, kBlock, 0, s>>>(g, w, part_buf, sc);
+  } else if (g.tma) {
+    k32cgt_pq<<<dim3(g.tgx, g.tgy, 1), kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+  } else if (g.vbx > 0) {
+    k32cgv_pq<<<dim3(g.vgx, g.vgy, g.vgz), dim3(g.vbx, g.vby, 1), 0, s>>>(g, st, w, part_buf, sc);
+  } else {
+    k32cg_pq<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, part_buf, sc);
+  }
+}
 void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const double *px1, const double *px2,
                            double *part, SolverScal *sc) {
   k_nan_replace<<<cgrid(g), cblock(g), 0, s>>>(g, x, px1, part, sc);

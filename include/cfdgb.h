@@ -38,7 +38,9 @@ typedef enum cfdgb_status {
 typedef enum cfdgb_solver {
   CFDGB_BICGSTAB = 0,        /* SPE operator, unscaled (P_SOLVER_BICG_SPE, the default) */
   CFDGB_BICGSTAB_JACOBI = 1, /* rows and rhs scaled by 1/diag (P_SOLVER_BICG_CSR) */
-  CFDGB_RBSOR = 2            /* red-black SOR on the same Neumann operator */
+  CFDGB_RBSOR = 2,           /* red-black SOR on the same Neumann operator */
+  CFDGB_CG = 3               /* conjugate gradients on the SPE operator (inc/solver/cg.hpp,
+                                P_SOLVER_CG_ELL; the operator is symmetric on a uniform grid) */
 } cfdgb_solver;
 
 typedef enum cfdgb_precision {

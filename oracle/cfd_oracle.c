@@ -684,6 +684,44 @@ int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int so
   return og_run_ex(g, steps, Re, dt, tol, solver, omega, u, v, w, p, eta, stats, NULL, NULL, 0);
 }
 
+int og_cg_solve(const og_grid *g, const double *val7, const double *rhs, double *x, double tol, int maxit,
+                double *relres) {
+  const long n = og_cells(g);
+  double *r = dalloc(n), *p = dalloc(n), *q = dalloc(n);
+  og_spe_multiply(g, val7, x, q);
+  double bb = 0.0, rr = 0.0;
+  for (long i = 0; i < n; ++i) {
+    r[i] = rhs[i] - q[i];
+    p[i] = r[i];
+    bb += rhs[i] * rhs[i];
+    rr += r[i] * r[i];
+  }
+  const double norm0 = sqrt(bb);
+  double rel = sqrt(rr) / norm0;
+  int it = 0;
+  while (rel >= tol && it < maxit) {
+    og_spe_multiply(g, val7, p, q);
+    double pq = 0.0;
+    for (long i = 0; i < n; ++i) pq += p[i] * q[i];
+    const double a = rr / pq;
+    double rn = 0.0;
+    for (long i = 0; i < n; ++i) {
+      x[i] += a * p[i];
+      r[i] -= a * q[i];
+      rn += r[i] * r[i];
+    }
+    ++it;
+    rel = sqrt(rn) / norm0;
+    if (rel < tol) break;
+    const double be = rn / rr;
+    rr = rn;
+    for (long i = 0; i < n; ++i) p[i] = r[i] + be * p[i];
+  }
+  free(r); free(p); free(q);
+  if (relres) *relres = rel;
+  return it;
+}
+
 void og_project_rhs(const og_grid *g, const double *jp, double *b) {
   const long n = og_cells(g);
   double sum = 0.0;
@@ -709,6 +747,8 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
   bc_main_in(g, u, v, w, p, inlet);
   og_bc_copy(g, u, v, w, us, vs, ws);
   if (solver == 0 || solver == 1) og_bicg_init(&bs, g, solver, tol);
+  double *val7 = solver == 3 ? dalloc(7 * n) : NULL;
+  if (val7) og_spe_setup(g, val7);
   if (eta_in) {
     memcpy(eta, eta_in, sizeof(double) * tot);
   } else {
@@ -722,6 +762,11 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
     if (s > 1) { /* RUN_CPU.cpp:287/:303: no pressure solve at the first step */
       if (solver == 2) {
         iters = og_sor(g, dt, omega, tol, 5000, us, vs, ws, p, &err);
+      } else if (solver == 3) {
+        og_rhs(g, dt, us, vs, ws, NULL, b);
+        if (project) og_project_rhs(g, NULL, b);
+        iters = og_cg_solve(g, val7, b, x, tol, 5000, &err);
+        og_transform(g, x, p);
       } else {
         og_rhs(g, dt, us, vs, ws, solver == 1 ? bs.jp : NULL, b);
         if (project) og_project_rhs(g, solver == 1 ? bs.jp : NULL, b);
@@ -743,6 +788,7 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
     }
   }
   if (solver == 0 || solver == 1) og_bicg_free(&bs);
+  free(val7);
   free(us); free(vs); free(ws); free(u3); free(v3); free(w3); free(f); free(b); free(x);
   return rc;
 }

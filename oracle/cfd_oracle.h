@@ -60,6 +60,13 @@ int og_bicg_init(og_bicg *s, const og_grid *g, int kind, double tol);
 void og_bicg_free(og_bicg *s);
 int og_bicg_solve(og_bicg *s, const double *rhs, double *x, double *relres);
 
+/* Conjugate gradients on the SPE operator, the method of inc/solver/cg.hpp (which does
+ * not compile as published): r = b - A x, p = r; alpha = <r,r>/<p,Ap>; x += alpha p;
+ * r -= alpha Ap; stop on ||r||/||b|| < tol (bicgstabRe2's test) or maxit; beta = <r,r>
+ * new/old; p = r + beta p.  Warm start from x.  Returns the iterations. */
+int og_cg_solve(const og_grid *g, const double *val7, const double *rhs, double *x, double tol, int maxit,
+                double *relres);
+
 int og_sor(const og_grid *g, double dt, double omega, double tol, int itmax,
            const double *us, const double *vs, const double *ws, double *p, double *err);
 void og_transform(const og_grid *g, const double *x, double *p);
@@ -70,7 +77,7 @@ void og_dfib_cylinder_z(const og_grid *g, double *eta);
 double og_force_sum(const og_grid *g, const double *f, int dir);
 
 /* Whole run in the order of src/RUN_CPU.cpp:257-436.  solver: 0 SPE-BiCGSTAB,
- * 1 CSR(Jacobi)-BiCGSTAB, 2 lexicographic SOR.  Fields in/out are padded; stats gets
+ * 1 CSR(Jacobi)-BiCGSTAB, 2 lexicographic SOR, 3 SPE-CG (og_cg_solve).  Fields in/out are padded; stats gets
  * 4 doubles per step (iters, err, cd, cl).  u,v,w,p on entry: the initial state before
  * the first ghost fill (uniform u=1 plus any perturbation); on exit: T0 and p after the
  * last step. */

@@ -208,7 +208,7 @@ def perturb(g, u, v, w, seed, amp):
     lib().og_perturb(g.ptr, u, v, w, seed, amp)
 
 
-SOLVERS = {"spe": 0, "bicgstab": 0, "jacobi": 1, "csr": 1, "sor": 2}
+SOLVERS = {"spe": 0, "bicgstab": 0, "jacobi": 1, "csr": 1, "sor": 2, "cg": 3}
 
 
 def run(g: Grid, steps, Re, dt, tol, solver="spe", omega=1.8, seed=0, amp=0.0, eta_in=None,

@@ -158,6 +158,41 @@ def test_mixed_precision_with_perturbation_and_projection():
         assert e < 1e-4, (k, e)
 
 
+def test_cg_fp64_matches_oracle_cg():
+    """CG on the SPE operator (the reference's cg.hpp method) against the oracle's CG, both
+    to 1e-13: same fields to 1e-10, iteration counts within 10 %, and the same solution as
+    the BiCGSTAB run of the reference."""
+    g = O.Grid(96, 48, 4, 24.0, 12.0, 1.0, 6.0)
+    ref = O.run(g, 12, 100.0, 0.005, 1e-13, "cg")
+    bic = O.run(g, 12, 100.0, 0.005, 1e-13, "spe")
+    with _c1(solver="cg", tol=1e-13) as s:
+        s.init_fields()
+        st = s.step(12)
+        f = s.get_fields()
+    assert all(r.status == 0 and r.relres < 1e-13 for r in st[1:])
+    for other in (ref, bic):
+        for k, e in vel_err(f, other).items():
+            assert e <= 1e-10, (k, e)
+        assert rel_p(interior(f["p"]), interior(other["p"])) <= 1e-10
+    its = np.array([r.iters for r in st[1:]])
+    assert np.all(np.abs(its - ref["iters"][1:]) <= 0.1 * ref["iters"][1:]), (its, ref["iters"])
+
+
+def test_mixed_cg_error_against_fp64():
+    """FP32 CG sweeps inside FP64 refinement: every solve ends below 1e-8 in the FP64
+    residual, fields within 1e-4 of the FP64 BiCGSTAB run."""
+    res = {}
+    for solver, prec in (("bicgstab", "fp64"), ("cg", "mixed")):
+        with _c1(solver=solver, precision=prec, tol=1e-8, seed=1234, amp=1e-3, project_rhs=1) as s:
+            s.init_fields()
+            st = s.step(20)
+            res[prec] = (s.get_fields(), st)
+    assert all(r.relres < 1e-8 and r.status == 0 for r in res["mixed"][1][1:])
+    assert all(r.outer >= 1 for r in res["mixed"][1][1:])
+    for k, e in vel_err(res["mixed"][0], res["fp64"][0]).items():
+        assert e < 1e-4, (k, e)
+
+
 def test_rbsor_converges_to_the_same_pressure():
     with _c1(tol=1e-10) as a, _c1(solver="rbsor", tol=1e-10, omega=1.7, maxit=200000) as b:
         a.init_fields()

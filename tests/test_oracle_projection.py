@@ -31,3 +31,15 @@ def test_projection_leaves_a_consistent_problem_unchanged():
     np.testing.assert_allclose(b["cd"], a["cd"], rtol=1e-9)
     for k in ("u", "v", "w"):
         assert np.abs(b[k] - a[k]).max() <= 1e-9 * np.abs(a["u"]).max()
+
+
+def test_cg_restatement_converges_to_the_bicgstab_solution():
+    """The CG restatement (inc/solver/cg.hpp's method) reaches the same fields as the
+    reference's BiCGSTAB at a tight tolerance."""
+    g = O.Grid(*GRID)
+    a = O.run(g, 4, 100.0, 0.005, 1e-13, "spe")
+    b = O.run(g, 4, 100.0, 0.005, 1e-13, "cg")
+    assert np.all(b["err"][1:] < 1e-13) and np.all(b["iters"][1:] > 0)
+    np.testing.assert_allclose(b["cd"], a["cd"], rtol=1e-11)
+    for k in ("u", "v", "w"):
+        assert np.abs(b[k] - a[k]).max() <= 1e-11 * np.abs(a["u"]).max()
