@@ -193,7 +193,7 @@ def _timed_steps(s, steps, dist, torch):
     dist.barrier()
     torch.cuda.synchronize()
     e0.record(stream)
-    stats = s.step(steps)
+    stats = s.step(steps, allow_noconv=True)  # a capped solve is reported in its status
     e1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()

@@ -292,8 +292,8 @@ int validate(const cfdgb_config *c) {
   if (c->solver == CFDGB_RBSOR && !(c->omega > 0 && c->omega < 2)) return fail(CFDGB_EINVAL, "omega outside (0,2)");
   if (c->precision == CFDGB_MIXED && c->solver == CFDGB_RBSOR)
     return fail(CFDGB_EINVAL, "MIXED precision is implemented for the Krylov solvers");
-  if (c->precision == CFDGB_MIXED && !(c->inner_tol > 0 && c->inner_tol < 1))
-    return fail(CFDGB_EINVAL, "inner_tol outside (0,1)");
+  if (c->precision == CFDGB_MIXED && !(c->inner_tol >= 0 && c->inner_tol < 1))
+    return fail(CFDGB_EINVAL, "inner_tol outside [0,1)");
   if (c->dfib && !(c->radius > 0)) return fail(CFDGB_EINVAL, "radius must be positive");
   return 0;
 }
@@ -383,6 +383,15 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   return fail(CFDGB_ECUDA, "solver did not report completion");
 }
 
+// Residual reduction of one FP32 sweep (cfg.inner_tol, or 0 for the solver's own, measured
+// on the 512x256x64 workload): BiCGSTAB in FP32 breaks down near a 1e-3 reduction, so its
+// sweeps stay short (0.3: ~3000 FP32 iterations per solve, no fallback; 0.01 stalls); CG
+// has no such breakdown and gains from long sweeps (1e-3: ~2400 iterations, 0.3: ~4000).
+double sweep_reduction(const cfdgb_ctx *c) {
+  if (c->cfg.inner_tol > 0.0) return c->cfg.inner_tol;
+  return c->cfg.solver == CFDGB_CG ? 1e-3 : 0.3;
+}
+
 // FP64 Krylov set-up on the current b and warm start x
 void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
   if (c->cfg.solver == CFDGB_CG)
@@ -464,7 +473,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   if (rel < c->cfg.tol) return 0;
   TRY(set_solver_params(c, c->sc32, c->cfg.tol, c->cfg.maxit));
   L(c, K_SETUP32, 1, [&] {
-    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->cfg.inner_tol, 1,
+    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), 1,
                           c->part, c->sc32);
   });
   bool finish64 = false;
@@ -514,7 +523,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
       break;
     }
     L(c, K_SETUP32, 1, [&] {
-      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, c->cfg.inner_tol, 0,
+      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), 0,
                             c->part, c->sc32);
     });
   }
@@ -594,10 +603,7 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->tol = 1e-8;
   c->maxit = 5000;
   c->omega = 1.7;
-  // an FP64 refinement whenever an FP32 sweep has cut its residual by 0.3: short sweeps
-  // stay clear of the FP32 stall (measured on the 512x256x64 workload: 0.3 and 0.1 need
-  // ~3000 FP32 iterations per solve without a fallback, 0.01 stalls)
-  c->inner_tol = 0.3;
+  c->inner_tol = 0.0;  // each solver's own sweep reduction (sweep_reduction)
   c->max_outer = 400;
   c->check_every = 10;
   c->dfib = 1;

@@ -3,8 +3,8 @@
 // instead of compile-time constants:
 //
 //   cfdgb_run nx=96 ny=48 nz=4 lx=24 ly=12 lz=1 cx=6 cy=6 Re=100 dt=0.005 steps=200 \
-//             solver=bicgstab|jacobi|rbsor precision=fp64|mixed tol=1e-8 [out=Information]
-//             [amp=1e-3 seed=1234 project_rhs=1 inner_tol=0.3 max_outer=400 maxit=5000]
+//             solver=bicgstab|jacobi|rbsor|cg precision=fp64|mixed tol=1e-8 [out=Information]
+//             [solver=cg amp=1e-3 seed=1234 project_rhs=1 inner_tol=0 max_outer=400 maxit=5000]
 //
 // Per step it prints the reference's lines ("[SPE (BICG)] iter:...", "[cD, cL] : ...")
 // and appends the drag/lift series to <out>/Time_cDcL.dat in the reference's Tecplot
@@ -41,7 +41,10 @@ int main(int argc, char **argv) {
   cfg.amp = num("amp", 0.0); cfg.seed = (uint64_t)num("seed", 0.0);
   cfg.project_rhs = (int)num("project_rhs", 0.0);
   const std::string solver = kv.count("solver") ? kv["solver"] : "bicgstab";
-  cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI : solver == "rbsor" ? CFDGB_RBSOR : CFDGB_BICGSTAB;
+  cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI
+               : solver == "rbsor"  ? CFDGB_RBSOR
+               : solver == "cg"     ? CFDGB_CG
+                                    : CFDGB_BICGSTAB;
   cfg.precision = (kv.count("precision") && kv["precision"] == "mixed") ? CFDGB_MIXED : CFDGB_FP64;
   const int steps = (int)num("steps", 200);
   const std::string out = kv.count("out") ? kv["out"] : "Information";
@@ -56,7 +59,7 @@ int main(int argc, char **argv) {
     mkdir(out.c_str(), 0755);
     FILE *f = std::fopen((out + "/Time_cDcL.dat").c_str(), "w");
     if (f) std::fprintf(f, "TITLE     = \"\"\nVARIABLES = \"simulation time\",\"C<sub>D</sub>\",\"C<sub>L</sub>\"\nZONE T=\"%s\"",
-                        solver == "rbsor" ? "SOR" : (solver == "jacobi" ? "CSR (BICG)" : "SPE (BICG)"));
+                        solver == "rbsor" ? "SOR" : solver == "jacobi" ? "CSR (BICG)" : solver == "cg" ? "ELL (CG)" : "SPE (BICG)");
     double time = 0.0;
     int worst = 0;
     for (int s = 0; s < steps; ++s) {

@@ -857,9 +857,14 @@ __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, 
   }
 }
 
+__global__ void k32cg_xr(Geo g, Vec32 v, double *part, SolverScal *sc);
+
 int fp32_pointwise_blocks_per_sm() {
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32v_xr, kBlock, 0) != cudaSuccess) n = 4;
+  // the grid serves both pointwise kernels (BiCGSTAB and CG sweeps): the smaller residency
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k32v_xr, kBlock, 0) != cudaSuccess) a = 4;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k32cg_xr, kBlock, 0) != cudaSuccess) b = 4;
+  const int n = a < b ? a : b;
   return n > 0 ? n : 1;
 }
 
