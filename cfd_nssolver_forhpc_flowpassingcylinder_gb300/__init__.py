@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 2  # CFDGB_ABI_VERSION
+ABI_VERSION = 3  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -51,7 +51,7 @@ class Objective(C.Structure):
 
 class StepStats(C.Structure):
     _fields_ = [("step", C.c_int), ("iters", C.c_int), ("outer", C.c_int), ("status", C.c_int),
-                ("relres", C.c_double), ("cd", C.c_double), ("cl", C.c_double)]
+                ("relres", C.c_double), ("cd", C.c_double), ("cl", C.c_double), ("cfl", C.c_double)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -93,6 +93,9 @@ EXPORTS = {
                                     C.POINTER(C.c_int), _dp]),
     "cfdgb_op_update_uf": (C.c_int, [C.c_void_p] + [_dp] * 11),
     "cfdgb_op_solid_fraction": (C.c_int, [C.c_void_p, _dp]),
+    "cfdgb_op_cfl": (C.c_int, [C.c_void_p] + [_dp] * 4),
+    "cfdgb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
+    "cfdgb_write_plot3d": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_double]),
 }
 
 
@@ -152,6 +155,7 @@ class StepResult:
     relres: float
     cd: float
     cl: float
+    cfl: float = 0.0
 
 
 class Solver:
@@ -218,7 +222,7 @@ class Solver:
         st = (StepStats * max(n, 1))()
         rc = self._L.cfdgb_step(self._h, n, st)
         _check(rc, allow=(ENOCONV,) if allow_noconv else ())
-        return [StepResult(s.step, s.iters, s.outer, s.status, s.relres, s.cd, s.cl) for s in st[:n]]
+        return [StepResult(s.step, s.iters, s.outer, s.status, s.relres, s.cd, s.cl, s.cfl) for s in st[:n]]
 
     def pressure_solve(self):
         it, rr = C.c_int(), C.c_double()
@@ -306,6 +310,22 @@ class Solver:
         e = self.zeros()
         _check(self._L.cfdgb_op_solid_fraction(self._h, _ptr(e)))
         return e
+
+    def cfl(self, us, vs, ws):
+        """get_Cfl on padded u*: [cfl, U_max x3, U_min x3]."""
+        out = np.zeros(7)
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (us, vs, ws)]
+        _check(self._L.cfdgb_op_cfl(self._h, *[_ptr(x) for x in a], _ptr(out)))
+        return out
+
+    def set_dt(self, dt):
+        _check(self._L.cfdgb_set_dt(self._h, float(dt)))
+        self.cfg.dt = float(dt)
+
+    def write_plot3d(self, xpath=None, qpath=None, time=0.0):
+        """The reference's Plot3D grid (.x) and solution (.q) files of the current state."""
+        enc = lambda p: None if p is None else str(p).encode()
+        _check(self._L.cfdgb_write_plot3d(self._h, enc(xpath), enc(qpath), float(time)))
 
 
 def perturbation(shape, seed, amp):

@@ -59,13 +59,13 @@ uint64_t splitmix64(uint64_t &s) {
 enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
-  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_COUNT
+  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
-    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32"};
+    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl"};
 
 struct PendingEv {
   int id;
@@ -104,6 +104,8 @@ struct cfdgb_ctx {
   int chunk_len = 16;
   // scratch for the per-function entry points (allocated on first use)
   double *op[10] = {nullptr};
+  // Plot3D staging: five float32 arrays on the device and a pinned host copy
+  float *p3d = nullptr, *h_p3d = nullptr;
   double *opc[3] = {nullptr};
   std::vector<void *> allocs;
   int loop = 0;  // steps taken since the last init_fields
@@ -741,6 +743,7 @@ int cfdgb_destroy(cfdgb_ctx *c) {
   if (c->chunk64) cudaGraphExecDestroy(c->chunk64);
   if (c->chunk32) cudaGraphExecDestroy(c->chunk32);
   for (void *q : c->allocs) cudaFree(q);
+  if (c->h_p3d) cudaFreeHost(c->h_p3d);
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->h_ss) cudaFreeHost(c->h_ss);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -846,6 +849,8 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
       else
         launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.dt, nu, c->u, c->v, c->w, c->us, c->vs, c->ws);
     });
+    // CFL diagnostic on u* (get_Cfl, RUN_CPU.cpp:274)
+    L(c, K_CFL, 1, [&] { launch_cfl(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, c->part, c->ss); });
     // 2. pressure, not at the first step (RUN_CPU.cpp:303)
     int iters = 0, outer = 0, status = 0;
     double relres = 0.0;
@@ -873,6 +878,7 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
       st.relres = relres;
       st.cd = c->h_ss->cd;
       st.cl = c->h_ss->cl;
+      st.cfl = c->h_ss->cfl[0];
     }
     if (status < worst) worst = status;
   }
@@ -1068,6 +1074,71 @@ int cfdgb_op_solid_fraction(cfdgb_ctx *c, double *eta) {
   launch_eta(c->stream, c->nblk, c->g, c->Xd, c->Yd, c->cfg.cx, c->cfg.cy, c->cfg.radius, c->op[6]);
   TRY(d2h(c, eta, c->op[6], c->npad));
   return sync(c);
+}
+
+int cfdgb_op_cfl(cfdgb_ctx *c, const double *us, const double *vs, const double *ws, double *out7) {
+  if (!c || !us || !vs || !ws || !out7) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  TRY(h2d(c, c->op[0], us, c->npad));
+  TRY(h2d(c, c->op[1], vs, c->npad));
+  TRY(h2d(c, c->op[2], ws, c->npad));
+  launch_cfl(c->stream, c->nblk, c->g, c->cfg.dt, c->op[0], c->op[1], c->op[2], c->part, c->ss);
+  CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
+  TRY(sync(c));
+  for (int q = 0; q < 7; ++q) out7[q] = c->h_ss->cfl[q];
+  return 0;
+}
+
+int cfdgb_set_dt(cfdgb_ctx *c, double dt) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(CFDGB_EINVAL, "dt must be positive");
+  c->cfg.dt = dt;  // read at every launch of the step kernels; nothing captured depends on it
+  return 0;
+}
+
+int cfdgb_write_plot3d(cfdgb_ctx *c, const char *xpath, const char *qpath, double time) {
+  if (!c) return fail(CFDGB_EINVAL, "null context");
+  const int hdr[4] = {1, c->cfg.nx, c->cfg.ny, c->cfg.nz};
+  if (xpath) {  // xfileWrite.hpp:14-47: cell centres, k-j-i order (structureGrid.hpp:219)
+    FILE *f = std::fopen(xpath, "wb");
+    if (!f) return fail(CFDGB_EINVAL, "cannot write %s", xpath);
+    std::fwrite(hdr, sizeof(int), 4, f);
+    const std::vector<double> *N[3] = {&c->X, &c->Y, &c->Z};
+    const int n[3] = {c->cfg.nx, c->cfg.ny, c->cfg.nz};
+    std::vector<float> line;
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < n[2]; ++k)
+        for (int j = 0; j < n[1]; ++j) {
+          line.clear();
+          for (int i = 0; i < n[0]; ++i) {
+            const int q = a == 0 ? i : (a == 1 ? j : k);
+            line.push_back((float)(((*N[a])[q + 2] + (*N[a])[q + 3]) / 2.0));
+          }
+          std::fwrite(line.data(), sizeof(float), line.size(), f);
+        }
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) return fail(CFDGB_EINVAL, "write of %s failed", xpath);
+  }
+  if (qpath) {  // qfile.hpp:6-105: the current T0, p and eta, packed on the device
+    if (!c->have_fields) return fail(CFDGB_ESTATE, "no fields yet");
+    const size_t n = (size_t)c->ncell;
+    if (!c->p3d) {
+      TRY(dalloc(c, &c->p3d, 5 * n));
+      CK(cudaMallocHost(&c->h_p3d, 5 * n * sizeof(float)));
+    }
+    launch_plot3d_pack(c->stream, c->nblk, c->g, c->p, c->u, c->v, c->w, c->eta, c->p3d);
+    CK(cudaMemcpyAsync(c->h_p3d, c->p3d, 5 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    TRY(sync(c));
+    FILE *f = std::fopen(qpath, "wb");
+    if (!f) return fail(CFDGB_EINVAL, "cannot write %s", qpath);
+    const float head[4] = {0.0f, 0.0f, (float)c->cfg.Re, (float)time};  // mach, alpha, Re, time
+    std::fwrite(hdr, sizeof(int), 4, f);
+    std::fwrite(head, sizeof(float), 4, f);
+    const size_t wrote = std::fwrite(c->h_p3d, sizeof(float), 5 * n, f);
+    const bool ok = std::fclose(f) == 0 && wrote == 5 * n;
+    if (!ok) return fail(CFDGB_EINVAL, "write of %s failed", qpath);
+  }
+  return 0;
 }
 
 // ---- discrete adjoint -------------------------------------------------------------------

@@ -112,6 +112,7 @@ struct StepScal {
   double bnorm, rnorm, relres;
   double rsum;  // MIXED: sum of the raw residual (its component along the operator's null space)
   double esum;  // MIXED: sum of the inner correction e
+  double cfl[7];  // get_Cfl on u*: cfl, U_max[3], U_min[3]
   int nan_flag, pad;
   unsigned cnt[8];
 };

@@ -5,6 +5,8 @@
 //   cfdgb_run nx=96 ny=48 nz=4 lx=24 ly=12 lz=1 cx=6 cy=6 Re=100 dt=0.005 steps=200 \
 //             solver=bicgstab|jacobi|rbsor|cg precision=fp64|mixed tol=1e-8 [out=Information]
 //             [solver=cg amp=1e-3 seed=1234 project_rhs=1 inner_tol=0 max_outer=400 maxit=5000]
+//             [p3d=N: Plot3D grid file <out>/P3D.x and a solution file <out>/P3D<nn>.q
+//              every N steps, byte-compatible with the reference's writers]
 //
 // Per step it prints the reference's lines ("[SPE (BICG)] iter:...", "[cD, cL] : ...")
 // and appends the drag/lift series to <out>/Time_cDcL.dat in the reference's Tecplot
@@ -47,6 +49,7 @@ int main(int argc, char **argv) {
                                     : CFDGB_BICGSTAB;
   cfg.precision = (kv.count("precision") && kv["precision"] == "mixed") ? CFDGB_MIXED : CFDGB_FP64;
   const int steps = (int)num("steps", 200);
+  const int p3d = (int)num("p3d", 0);  // Plot3D solution file every p3d steps (0: none)
   const std::string out = kv.count("out") ? kv["out"] : "Information";
   try {
     cfdgb::Context ctx(cfg);
@@ -62,6 +65,7 @@ int main(int argc, char **argv) {
                         solver == "rbsor" ? "SOR" : solver == "jacobi" ? "CSR (BICG)" : solver == "cg" ? "ELL (CG)" : "SPE (BICG)");
     double time = 0.0;
     int worst = 0;
+    if (p3d > 0) cfdgb::check(cfdgb_write_plot3d(ctx.handle(), (out + "/P3D.x").c_str(), nullptr, 0.0));
     for (int s = 0; s < steps; ++s) {
       cfdgb_step_stats st{};
       const int rc = cfdgb_step(ctx.handle(), 1, &st);
@@ -70,6 +74,11 @@ int main(int argc, char **argv) {
       std::printf("[%s] iter:%d, error %g\n[cD, cL] : %g, %g\n", solver.c_str(), st.iters, st.relres, st.cd, st.cl);
       if (f) std::fprintf(f, "\n%.17g %.17g %.17g", time, st.cd, st.cl);
       time += cfg.dt;
+      if (p3d > 0 && (s + 1) % p3d == 0) {  // qfile.hpp: P3D<nn>.q, nn the file counter
+        char name[64];
+        std::snprintf(name, sizeof(name), "/P3D%02d.q", (s + 1) / p3d);
+        cfdgb::check(cfdgb_write_plot3d(ctx.handle(), nullptr, (out + name).c_str(), time));
+      }
     }
     if (f) std::fclose(f);
     return worst == CFDGB_OK ? 0 : 3;

@@ -13,6 +13,12 @@ void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const d
 void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
                        double *y);
 void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p);
+// get_Cfl on u* into ss->cfl (cfl, U_max[3], U_min[3])
+void launch_cfl(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
+                const double *ws, double *part, StepScal *ss);
+// Plot3D solution arrays p, u, v, w, eta (float32, k-j-i order) into out[5 * ncell]
+void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p, const double *u, const double *v,
+                        const double *w, const double *eta, float *out);
 void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
                             const double *p, const double *us, const double *vs, const double *ws, double *u3,
                             double *v3, double *w3, double *f, const double *ui, const double *vi,

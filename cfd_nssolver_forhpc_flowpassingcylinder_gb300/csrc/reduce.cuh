@@ -79,6 +79,52 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, unsigned
   return true;
 }
 
+// Grid-wide maxima of NV values per thread, with the same last-block pattern as grid_sum
+// (minima: pass the negated values).  Maxima are exact, so the result does not depend on
+// the order either.
+template <int NV>
+__device__ __forceinline__ bool grid_max(double (&v)[NV], double *part, unsigned *ticket, double (&out)[NV]) {
+  __shared__ double sh[NV][kBlock / 32];
+  __shared__ bool last;
+  __shared__ double res[NV];
+  const int t = lin_tid(), lane = t & 31, wid = t >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[q] = fmax(v[q], __shfl_down_sync(0xffffffffu, v[q], off));
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q][wid] = v[q];
+  __syncthreads();
+  const int G = nblocks();
+  if (t == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double m = sh[q][0];
+      for (int w = 1; w < kBlock / 32; ++w) m = fmax(m, sh[q][w]);
+      part[q * G + lin_bid()] = m;
+    }
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == (unsigned)(G - 1));
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  if (t == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double m = __ldcg(part + q * G);
+      for (int b = 1; b < G; ++b) m = fmax(m, __ldcg(part + q * G + b));
+      res[q] = m;
+    }
+    *ticket = 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q] = res[q];
+  return true;
+}
+
 // FP32 products summed in short FP32 runs, each run added into an FP64 accumulator:
 // global sums stay FP64 while the per-element work stays FP32.
 struct AccF {

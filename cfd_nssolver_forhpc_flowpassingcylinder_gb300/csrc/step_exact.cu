@@ -166,6 +166,66 @@ __global__ void __launch_bounds__(kBlock) k_spmv_exact(Geo g, Stencil<double> st
   }
 }
 
+// inc/analyses/cfl.hpp:3-78 (get_Cfl) on u*: per cell c = u/Dxs + v/Dys + w/Dzs, each term
+// left out on the last face of its own axis (the loops' "-d"), added in that order; the
+// maximum of c times dt, and the extremes of each component over its faces.  ss->cfl.
+__global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *__restrict__ us,
+                                                 const double *__restrict__ vs, const double *__restrict__ ws,
+                                                 double *part, StepScal *ss) {
+  double m[7] = {-1e300, -1e10, -1e10, -1e10, -1e10, -1e10, -1e10};  // c, U_max, -U_min
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    double c = 0.0;
+    if (i < g.nx - 3) {
+      c += us[ic] / g.Dxs[i];
+      m[1] = fmax(m[1], us[ic]);
+      m[4] = fmax(m[4], -us[ic]);
+    }
+    if (j < g.ny - 3) {
+      c += vs[ic] / g.Dys[j];
+      m[2] = fmax(m[2], vs[ic]);
+      m[5] = fmax(m[5], -vs[ic]);
+    }
+    if (k < g.nz - 3) {
+      c += ws[ic] / g.Dzs[k];
+      m[3] = fmax(m[3], ws[ic]);
+      m[6] = fmax(m[6], -ws[ic]);
+    }
+    m[0] = fmax(m[0], c);
+  }
+  double out[7];
+  if (grid_max<7>(m, part, &ss->cnt[7], out) && lin_tid() == 0) {
+    ss->cfl[0] = out[0] * dt;
+    for (int a = 0; a < 3; ++a) {
+      ss->cfl[1 + a] = out[1 + a];
+      ss->cfl[4 + a] = -out[4 + a];
+    }
+  }
+}
+
+// Plot3D solution arrays (inc/io/Plot3D/qfile.hpp:62-103) in k-j-i order, i fastest, as
+// float32: p, the cell-centred u, v, w (face means, rounded once) and eta
+__global__ void __launch_bounds__(kBlock) k_plot3d_pack(Geo g, const double *__restrict__ p,
+                                                         const double *__restrict__ u, const double *__restrict__ v,
+                                                         const double *__restrict__ w, const double *__restrict__ eta,
+                                                         float *__restrict__ out) {
+  const long long n = g.ncell;
+  for (long long o = blockIdx.x * (long long)kBlock + threadIdx.x; o < n; o += (long long)gridDim.x * kBlock) {
+    const int ic = (int)(o % g.nxc);
+    const long long r = o / g.nxc;
+    const int jc = (int)(r % g.nyc), kc = (int)(r / g.nyc);
+    const long long c = pidx(g, ic + 2, jc + 2, kc + 2);
+    out[o] = (float)p[c];
+    out[n + o] = (float)(0.5 * (u[c - g.sx] + u[c]));
+    out[2 * n + o] = (float)(0.5 * (v[c - g.sy] + v[c]));
+    out[3 * n + o] = (float)(0.5 * (w[c - 1] + w[c]));
+    out[4 * n + o] = (float)eta[c];
+  }
+}
+
 // inc/pressure/Transform.hpp:8-20
 __global__ void __launch_bounds__(kBlock) k_transform(Geo g, const double *__restrict__ x, double *__restrict__ p) {
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
@@ -396,6 +456,14 @@ void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const d
 void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
                        double *y) {
   k_spmv_exact<<<nblk, kBlock, 0, s>>>(g, st, x, y);
+}
+void launch_cfl(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
+                const double *ws, double *part, StepScal *ss) {
+  k_cfl<<<nblk, kBlock, 0, s>>>(g, dt, us, vs, ws, part, ss);
+}
+void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p, const double *u, const double *v,
+                        const double *w, const double *eta, float *out) {
+  k_plot3d_pack<<<nblk, kBlock, 0, s>>>(g, p, u, v, w, eta, out);
 }
 void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p) {
   k_transform<<<nblk, kBlock, 0, s>>>(g, x, p);

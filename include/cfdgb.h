@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 2
+#define CFDGB_ABI_VERSION 3
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -83,6 +83,7 @@ typedef struct cfdgb_step_stats {
   int status;        /* cfdgb_status of this step's solve */
   double relres;     /* final relative residual of the solve (FP64) */
   double cd, cl;     /* drag and lift coefficients (CD_CL, virtualForceIntergrator.hpp:92) */
+  double cfl;        /* CFL number of u* (get_Cfl, inc/analyses/cfl.hpp:3, src/RUN_CPU.cpp:274) */
 } cfdgb_step_stats;
 
 /* Library identity and last error text (thread-local). */
@@ -202,6 +203,21 @@ int cfdgb_op_update_uf(cfdgb_ctx *ctx, const double *eta, const double *p, const
                        double *w3, double *f, double *cd, double *cl);
 /* DFIB_CylinderZ (inc/dfib/setEta.hpp:136): solid fraction of the context's cylinder. */
 int cfdgb_op_solid_fraction(cfdgb_ctx *ctx, double *eta);
+/* get_Cfl (inc/analyses/cfl.hpp:3) on padded u*, v*, w*: out7 = {cfl (max over cells of
+ * u/Dxs + v/Dys + w/Dzs, times dt), U_max[3], U_min[3]}. */
+int cfdgb_op_cfl(cfdgb_ctx *ctx, const double *us, const double *vs, const double *ws, double *out7);
+
+/* ---- time step and output ---- */
+/* New dt for the following steps (simu.dt; the adaptive step of timestepper,
+ * inc/0_1_SimulationVariable.hpp:172, which the reference leaves switched off at
+ * src/RUN_CPU.cpp:275, is the caller's choice: each step reports its CFL number). */
+int cfdgb_set_dt(cfdgb_ctx *ctx, double dt);
+/* Plot3D files of the current state, byte-compatible with the reference's writers:
+ * xpath (may be NULL) the grid file of OutputPlot3D_Xfile (inc/io/Plot3D/xfileWrite.hpp:6),
+ * qpath (may be NULL) the solution file of OutputPLOT3D_Qfile (inc/io/Plot3D/qfile.hpp:6):
+ * header (1 block, nx, ny, nz; mach 0, alpha 0, Re, time) and float32 p, cell-centred
+ * u, v, w and eta in k-j-i order.  The arrays are packed on the GPU and copied out once. */
+int cfdgb_write_plot3d(cfdgb_ctx *ctx, const char *xpath, const char *qpath, double time);
 /* Pressure solve on the current u* of the context (createBMatrix + solve +
  * Pressure_transform_X_result, src/RUN_CPU.cpp:310-320) with the configured solver. */
 int cfdgb_pressure_solve(cfdgb_ctx *ctx, int *iters, double *relres);

@@ -10,6 +10,7 @@
 
 #include <math.h>
 #include <stdlib.h>
+#include <stdio.h>
 #include <string.h>
 
 #define IC(g, i, j, k) (((long)(i) * (g)->ny + (j)) * (g)->nz + (k))
@@ -682,6 +683,87 @@ int og_run(const og_grid *g, int steps, double Re, double dt, double tol, int so
            double omega, double *u, double *v, double *w, double *p, double *eta,
            double *stats) {
   return og_run_ex(g, steps, Re, dt, tol, solver, omega, u, v, w, p, eta, stats, NULL, NULL, 0);
+}
+
+void og_cfl(const og_grid *g, double dt, const double *us, const double *vs, const double *ws,
+            double *out7) {
+  const long n = og_cells(g);
+  double *c = dalloc(n);
+  double umax[3] = {-1e10, -1e10, -1e10}, umin[3] = {1e10, 1e10, 1e10};
+  const double *f[3] = {us, vs, ws};
+  const double *Ds[3] = {g->Dxs, g->Dys, g->Dzs};
+  /* cfl.hpp:20-63: one loop per component over the interior, the last face of its axis
+   * excluded, in the reference's i-j-k order */
+  for (int a = 0; a < 3; ++a)
+    for (int i = GC; i < g->nx - GC - (a == 0); ++i)
+      for (int j = GC; j < g->ny - GC - (a == 1); ++j)
+        for (int k = GC; k < g->nz - GC - (a == 2); ++k) {
+          const long ic = IC(g, i, j, k);
+          const long r = ((long)(i - GC) * g->nyc + (j - GC)) * g->nzc + (k - GC);
+          const int d = a == 0 ? i : (a == 1 ? j : k);
+          c[r] += f[a][ic] / Ds[a][d];
+          if (f[a][ic] > umax[a]) umax[a] = f[a][ic];
+          if (f[a][ic] < umin[a]) umin[a] = f[a][ic];
+        }
+  double m = c[0];
+  for (long r = 1; r < n; ++r)
+    if (c[r] > m) m = c[r];
+  out7[0] = m * dt; /* cfl.hpp:67-68 */
+  for (int a = 0; a < 3; ++a) {
+    out7[1 + a] = umax[a];
+    out7[4 + a] = umin[a];
+  }
+  free(c);
+}
+
+static void put_header(FILE *f, const og_grid *g) {
+  const int h[4] = {1, g->nxc, g->nyc, g->nzc};
+  fwrite(h, sizeof(int), 4, f);
+}
+
+int og_plot3d_x(const og_grid *g, const char *path) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  put_header(f, g);
+  /* xfileWrite.hpp:14-47: cell centres Xc[i] = (X[i+gC] + X[i+gC+1]) / 2 (structureGrid.hpp:219) */
+  const double *N[3] = {g->X, g->Y, g->Z};
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < g->nzc; ++k)
+      for (int j = 0; j < g->nyc; ++j)
+        for (int i = 0; i < g->nxc; ++i) {
+          const int q = a == 0 ? i : (a == 1 ? j : k);
+          const float v = (float)((N[a][q + GC] + N[a][q + GC + 1]) / 2.0);
+          fwrite(&v, sizeof(float), 1, f);
+        }
+  fclose(f);
+  return 0;
+}
+
+int og_plot3d_q(const og_grid *g, const double *p, const double *u, const double *v, const double *w,
+                const double *eta, double Re, double time, const char *path) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  put_header(f, g);
+  const float hdr[4] = {0.0f, 0.0f, (float)Re, (float)time};  /* qfile.hpp:22-25 */
+  fwrite(hdr, sizeof(float), 4, f);
+  const long sx = (long)g->ny * g->nz, sy = g->nz;
+  for (int a = 0; a < 5; ++a)
+    for (int k = GC; k < g->nzc + GC; ++k)
+      for (int j = GC; j < g->nyc + GC; ++j)
+        for (int i = GC; i < g->nxc + GC; ++i) {
+          const long ic = IC(g, i, j, k);
+          float o;
+          switch (a) {
+            case 0: o = (float)p[ic]; break;
+            case 1: o = (float)(0.5 * (u[ic - sx] + u[ic])); break;
+            case 2: o = (float)(0.5 * (v[ic - sy] + v[ic])); break;
+            case 3: o = (float)(0.5 * (w[ic - 1] + w[ic])); break;
+            default: o = (float)eta[ic]; break;
+          }
+          fwrite(&o, sizeof(float), 1, f);
+        }
+  fclose(f);
+  return 0;
 }
 
 int og_cg_solve(const og_grid *g, const double *val7, const double *rhs, double *x, double tol, int maxit,

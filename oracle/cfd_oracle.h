@@ -76,6 +76,18 @@ void og_update_uf(const og_grid *g, double dt, const double *eta, const double *
 void og_dfib_cylinder_z(const og_grid *g, double *eta);
 double og_force_sum(const og_grid *g, const double *f, int dir);
 
+/* get_Cfl (inc/analyses/cfl.hpp:3) on u*: per cell c = u/Dxs + v/Dys + w/Dzs (each face
+ * term left out on the last face of its axis), out = {max(c)*dt, U_max[3], U_min[3]}. */
+void og_cfl(const og_grid *g, double dt, const double *us, const double *vs, const double *ws,
+            double *out7);
+/* Plot3D files of the reference (inc/io/Plot3D/xfileWrite.hpp, qfile.hpp): int header,
+ * then float32 arrays in k-j-i order (i fastest).  x: cell-centre X, Y, Z.  q: mach 0,
+ * alpha 0, Re, time, then p, the cell-centred u, v, w (mean of the two faces) and eta.
+ * Return 0, or -1 if the file cannot be written. */
+int og_plot3d_x(const og_grid *g, const char *path);
+int og_plot3d_q(const og_grid *g, const double *p, const double *u, const double *v, const double *w,
+                const double *eta, double Re, double time, const char *path);
+
 /* Whole run in the order of src/RUN_CPU.cpp:257-436.  solver: 0 SPE-BiCGSTAB,
  * 1 CSR(Jacobi)-BiCGSTAB, 2 lexicographic SOR, 3 SPE-CG (og_cg_solve).  Fields in/out are padded; stats gets
  * 4 doubles per step (iters, err, cd, cl).  u,v,w,p on entry: the initial state before

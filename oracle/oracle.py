@@ -184,6 +184,27 @@ class BiCGSTAB:
             pass
 
 
+def cfl(g, dt, us, vs, ws):
+    """get_Cfl (cfl.hpp:3): [cfl, U_max x3, U_min x3]."""
+    out = np.zeros(7)
+    L = lib()
+    L.og_cfl.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.og_cfl(g.ptr, dt, _c(us).ctypes.data_as(C.c_void_p), _c(vs).ctypes.data_as(C.c_void_p),
+             _c(ws).ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def plot3d(g, p, u, v, w, eta, Re, time, qpath, xpath):
+    """The reference's Plot3D .q and .x files (qfile.hpp, xfileWrite.hpp)."""
+    L = lib()
+    L.og_plot3d_x.argtypes = [C.c_void_p, C.c_char_p]
+    L.og_plot3d_q.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [C.c_double, C.c_double, C.c_char_p]
+    arrs = [_c(a) for a in (p, u, v, w, eta)]
+    if L.og_plot3d_x(g.ptr, str(xpath).encode()) or L.og_plot3d_q(
+            g.ptr, *[a.ctypes.data_as(C.c_void_p) for a in arrs], Re, time, str(qpath).encode()):
+        raise OSError("plot3d write failed")
+
+
 def sor(g, dt, omega, tol, itmax, us, vs, ws, p):
     err = C.c_double()
     it = lib().og_sor(g.ptr, dt, omega, tol, itmax, _c(us), _c(vs), _c(ws), p, C.byref(err))

@@ -65,6 +65,13 @@ double sym_uniform(uint64_t &s) {
   return 2.0 * r - 1.0;
 }
 
+void copy_bytes(const std::string &from, const std::string &to) {
+  std::ifstream in(from, std::ios::binary);
+  std::ofstream o(to, std::ios::binary);
+  if (!in || !o) { std::fprintf(stderr, "copy %s -> %s failed\n", from.c_str(), to.c_str()); std::exit(3); }
+  o << in.rdbuf();
+}
+
 void dump(const std::string &dir, const std::string &name, const std::vector<double> &a) {
   std::string p = dir + "/" + name + ".f64";
   FILE *f = std::fopen(p.c_str(), "wb");
@@ -299,6 +306,25 @@ int unit_mode(int argc, char **argv) {
     dump(out, "sor_p", P.p);
     std::vector<double> ie{(double)simu.iters, simu.error};
     dump(out, "sor_it", ie);
+  }
+  // 10. CFL diagnostic on u* (get_Cfl, src/RUN_CPU.cpp:274): cfl, U_max[3], U_min[3]
+  {
+    simu.cfl_max = 0.0;
+    get_Cfl(T1, Lo, gA, simu);
+    std::vector<double> c{simu.cfl_max,  simu.U_max[0], simu.U_max[1], simu.U_max[2],
+                          simu.U_min[0], simu.U_min[1], simu.U_min[2]};
+    dump(out, "cfl", c);
+  }
+  // 11. Plot3D grid and solution files (OutputPlot3D_Xfile, OutputPLOT3D_Qfile of T3, p,
+  // eta at time 0), written by the reference into ./mx_out; it also wants ../mx_out
+  {
+    mkdir("../mx_out", 0755);
+    mkdir("mx_out", 0755);
+    OutputPlot3D_Xfile(simu, gA);
+    simu.currentFile = 0;
+    OutputPLOT3D_Qfile(Dfib, simu, t1, T3, Lo, gA);
+    copy_bytes("mx_out/P3D.x", out + "/p3d_x.bin");
+    copy_bytes("mx_out/P3D00.q", out + "/p3d_q.bin");
   }
   return 0;
 }

@@ -8,7 +8,8 @@ order.  Needs the reference tree (this container), not a GPU.
 
 Fixtures written next to this file:
   unit_<grid>.npz   every hot-path function once on seeded random fields
-                    (inputs and outputs, padded layout)
+                    (inputs and outputs, padded layout), the CFL diagnostic and the
+                    bytes of the reference's Plot3D .x and .q files
   run_<case>.npz    whole runs of the 96x48x4 flow-past-cylinder case (reference BCs,
                     Re 100, dt 0.005): interior of the final u, v, w, p and the per-step
                     iterations, residual, Cd and Cl.
@@ -54,6 +55,8 @@ def _load_dir(d: Path) -> dict:
     out = {}
     for f in sorted(d.glob("*.f64")):
         out[f.stem] = np.fromfile(f, dtype="<f8")
+    for f in sorted(d.glob("*.bin")):  # files the reference writes itself (Plot3D)
+        out[f.stem] = np.fromfile(f, dtype=np.uint8)
     return out
 
 
@@ -61,8 +64,11 @@ def make_unit(name, spec):
     nxc, nyc, nzc, lx, ly, lz, cx = spec
     exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity")
     with tempfile.TemporaryDirectory() as td:
+        # the reference's Plot3D writers use ./mx_out and ../mx_out: run one level down
+        wd = Path(td) / "run"
+        wd.mkdir()
         subprocess.run([str(exe), "unit", str(UNIT_SEED), repr(UNIT_RE), repr(UNIT_DT), td],
-                       check=True, env=_env(), stdout=subprocess.DEVNULL, cwd=td)
+                       check=True, env=_env(), stdout=subprocess.DEVNULL, cwd=wd)
         arrs = _load_dir(Path(td))
     meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, UNIT_RE, UNIT_DT, UNIT_SEED], dtype=np.float64)
     np.savez_compressed(HERE / f"unit_{name}.npz", meta=meta, **arrs)

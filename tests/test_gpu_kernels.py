@@ -111,3 +111,23 @@ def test_fp32_operator_matches_fp64(unit):
     z, s, P = unit
     y64 = O.spe_multiply(O.Grid(*(int(v) for v in z["meta"][:3]), *z["meta"][3:7]), z["in_x"])
     np.testing.assert_array_equal(s.spmv(z["in_x"]), y64)
+
+
+def test_cfl_bit_exact(unit):
+    """get_Cfl (cfl.hpp:3) on u*: CFL number (divisions in the reference's order, exact
+    maxima) and velocity extremes, against the reference's own values."""
+    z, s, P = unit
+    np.testing.assert_array_equal(s.cfl(P["in_us"], P["in_vs"], P["in_ws"]), z["cfl"])
+
+
+def test_plot3d_files_byte_identical(unit, tmp_path):
+    """The reference's Plot3D .x and .q files of a state (T3, p, eta at time 0), byte for
+    byte; the solution arrays are packed on the GPU."""
+    z, s, P = unit
+    s.init_fields()
+    s.set_fields(u=P["in_u3"], v=P["in_v3"], w=P["in_w3"], p=P["in_p"])
+    s.set_eta(P["in_eta"])
+    q, x = tmp_path / "P3D00.q", tmp_path / "P3D.x"
+    s.write_plot3d(x, q, 0.0)
+    np.testing.assert_array_equal(np.fromfile(x, dtype=np.uint8), z["p3d_x"])
+    np.testing.assert_array_equal(np.fromfile(q, dtype=np.uint8), z["p3d_q"])

@@ -193,6 +193,22 @@ def test_mixed_cg_error_against_fp64():
         assert e < 1e-4, (k, e)
 
 
+def test_set_dt_and_step_cfl():
+    """cfdgb_set_dt takes effect at the next step (same fields as a context created with
+    that dt), and each step reports the CFL number of its u* (get_Cfl)."""
+    with _c1(dt=0.01) as a, _c1(dt=0.005) as b:
+        a.set_dt(0.005)
+        a.init_fields()
+        b.init_fields()
+        sa, sb = a.step(4), b.step(4)
+        fa, fb = a.get_fields(), b.get_fields()
+    for k in "uvwp":
+        np.testing.assert_array_equal(fa[k], fb[k])
+    assert [r.cfl for r in sa] == [r.cfl for r in sb]
+    # u = 1 on 96x48x4 over [0,24]: u*/dx*dt = 0.005 * 4 = 0.02 at step 1, plus v, w terms
+    assert all(0.0 < r.cfl < 1.0 for r in sa) and abs(sa[0].cfl - 0.02) < 1e-3
+
+
 def test_rbsor_converges_to_the_same_pressure():
     with _c1(tol=1e-10) as a, _c1(solver="rbsor", tol=1e-10, omega=1.7, maxit=200000) as b:
         a.init_fields()

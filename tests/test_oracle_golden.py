@@ -115,3 +115,22 @@ def test_whole_run_bit_exact(case, golden):
     np.testing.assert_array_equal(r["cl"], z["cl"])
     for k in ("u", "v", "w", "p"):
         np.testing.assert_array_equal(r[k][2:-2, 2:-2, 2:-2], z[k])
+
+
+def test_cfl_bit_exact(unit):
+    """get_Cfl (cfl.hpp:3) on u*: the CFL number and the velocity extremes."""
+    z, g, P = unit
+    dt = z["meta"][8]
+    out = O.cfl(g, dt, P["in_us"], P["in_vs"], P["in_ws"])
+    np.testing.assert_array_equal(out, z["cfl"])
+
+
+def test_plot3d_files_byte_identical(unit, tmp_path):
+    """The reference's Plot3D grid (.x) and solution (.q) files, byte for byte: T3, p and
+    eta of the unit fields at time 0."""
+    z, g, P = unit
+    Re = z["meta"][7]
+    q, x = tmp_path / "P3D00.q", tmp_path / "P3D.x"
+    O.plot3d(g, P["in_p"], P["in_u3"], P["in_v3"], P["in_w3"], P["in_eta"], Re, 0.0, q, x)
+    np.testing.assert_array_equal(np.fromfile(x, dtype=np.uint8), z["p3d_x"])
+    np.testing.assert_array_equal(np.fromfile(q, dtype=np.uint8), z["p3d_q"])
