@@ -17,13 +17,15 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 3  # CFDGB_ABI_VERSION
+ABI_VERSION = 4  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 SOLVERS = {"bicgstab": BICGSTAB, "spe": BICGSTAB, "jacobi": BICGSTAB_JACOBI, "csr": BICGSTAB_JACOBI,
            "rbsor": RBSOR, "sor": RBSOR, "cg": CG}
 PRECISIONS = {"fp64": FP64, "mixed": MIXED}
+GRID_UNIFORM, GRID_SML = 0, 1
+GRIDS = {"uniform": GRID_UNIFORM, "sml": GRID_SML}
 
 
 class CfdgbError(RuntimeError):
@@ -41,7 +43,8 @@ class Config(C.Structure):
                 ("solver", C.c_int), ("precision", C.c_int),
                 ("tol", C.c_double), ("maxit", C.c_int), ("omega", C.c_double),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
-                ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int)]
+                ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
+                ("grid", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -142,6 +145,8 @@ def default_config(**kw) -> Config:
             v = SOLVERS[v]
         if k == "precision" and isinstance(v, str):
             v = PRECISIONS[v]
+        if k == "grid" and isinstance(v, str):
+            v = GRIDS[v]
         setattr(cfg, k, v)
     return cfg
 

@@ -199,6 +199,37 @@ struct Coef {
   double zm(int k) const { return 1.0 / c->Dz[k + 2] / c->Dzs[k + 1]; }
 };
 
+// init_nonuniform_SML's axis (structureGrid.hpp:250-310, unit_SML): three uniform parts,
+// ns fine cells over lsml shifted by off cells, then init_gC_dx (:433-487): ghost nodes by
+// linear extrapolation, widths and centre spacings, ghost widths from the nearest interior
+void sml_axis(std::vector<double> &a, std::vector<double> &D, std::vector<double> &Ds, double lsml, int ns, int off,
+              double l, int n) {
+  const int gc = 2, ncal = n - 2 * gc;
+  a[gc] = 0.0;
+  if (ns != 0) {
+    const double dS = lsml / ns, d = (l - lsml) / (ncal - ns);
+    int nl0 = (ncal - ns) / 2, ns0 = nl0 + ns;
+    const int nl1 = ns0 + nl0;
+    nl0 += off;
+    ns0 += off;
+    for (int i = 0; i < nl0; i++) a[i + gc + 1] = a[i + gc] + d;
+    for (int i = nl0; i < ns0; ++i) a[i + gc + 1] = a[i + gc] + dS;
+    for (int i = ns0; i < nl1; i++) a[i + gc + 1] = a[i + gc] + d;
+  } else {
+    for (int i = gc; i < n - gc; i++) a[i + 1] = a[i] + l / ncal;
+  }
+  a[1] = 2 * a[2] - a[3];
+  a[0] = 2 * a[1] - a[2];
+  a[n - 1] = 2 * a[n - 2] - a[n - 3];
+  a[n] = 2 * a[n - 1] - a[n - 2];
+  for (int i = gc; i < n - gc - 1; ++i) Ds[i] = (a[i + 2] - a[i]) / 2.0;
+  for (int i = gc; i < n - gc - 1; ++i) D[i] = (a[i + 1] - a[i]);
+  D[0] = D[1] = D[2];
+  Ds[0] = Ds[1] = Ds[2];
+  D[n - 1] = D[n - 2] = D[n - 3] = a[n - 2] - a[n - 3];
+  Ds[n - 1] = Ds[n - 2] = Ds[n - 3] = Ds[n - 4];
+}
+
 // 27 boundary classes: a representative compact index per class along each axis.
 int class_rep(int cls, int n) { return cls == 0 ? 0 : (cls == 2 ? n - 1 : 1); }
 
@@ -251,6 +282,8 @@ void build_stencils(cfdgb_ctx *c) {
           c->jac32.c[cls][e] = (float)q[e];
         }
       }
+  c->spe64.jac = c->spe32.jac = 0;
+  c->jac64.jac = c->jac32.jac = 1;
 }
 
 // FP32 per-axis tables for step_fast.cu (rows: 1/D, 1/Ds, interpolation factor, QUICK
@@ -297,6 +330,17 @@ int validate(const cfdgb_config *c) {
   if (c->precision == CFDGB_MIXED && !(c->inner_tol >= 0 && c->inner_tol < 1))
     return fail(CFDGB_EINVAL, "inner_tol outside [0,1)");
   if (c->dfib && !(c->radius > 0)) return fail(CFDGB_EINVAL, "radius must be positive");
+  if (c->grid < 0 || c->grid > 1) return fail(CFDGB_EINVAL, "unknown grid %d", c->grid);
+  if (c->grid == CFDGB_GRID_SML) {
+    // unit_SML's own conditions (structureGrid.hpp:269,283): 100 fine cells in x (shifted 4
+    // cells) and in y, an even number of coarse ones on both sides
+    if (c->nx % 2 || c->nx <= 108 || c->ny % 2 || c->ny <= 100)
+      return fail(CFDGB_EINVAL, "the SML grid needs nx even > 108 and ny even > 100");
+    if (c->precision != CFDGB_FP64 || (c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI))
+      return fail(CFDGB_EINVAL, "the SML grid is implemented for the FP64 BiCGSTAB solvers");
+    if (c->project_rhs)
+      return fail(CFDGB_EINVAL, "project_rhs removes the mean, not the stretched operator's null-space part");
+  }
   return 0;
 }
 
@@ -640,6 +684,11 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   axis(c->X, c->Dx, c->Dxs, nx, cfg->lx);
   axis(c->Y, c->Dy, c->Dys, ny, cfg->ly);
   axis(c->Z, c->Dz, c->Dzs, nz, cfg->lz);
+  if (cfg->grid == CFDGB_GRID_SML) {  // init_nonuniform_SML, structureGrid.hpp:312-329
+    sml_axis(c->X, c->Dx, c->Dxs, 0.3 * cfg->lx, 100, -4, cfg->lx, nx);
+    sml_axis(c->Y, c->Dy, c->Dys, 0.3 * cfg->ly, 100, 0, cfg->ly, ny);
+    sml_axis(c->Z, c->Dz, c->Dzs, 0.5 * cfg->lz, 0, 0, cfg->lz, nz);
+  }
   c->npad = (long long)nx * ny * nz;
   c->ncell = (long long)cfg->nx * cfg->ny * cfg->nz;
   build_stencils(c);
@@ -667,6 +716,41 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.ncell = c->ncell;
   g.Dx = c->metric; g.Dy = g.Dx + nx; g.Dz = g.Dy + ny;
   g.Dxs = g.Dz + nz; g.Dys = g.Dxs + nx; g.Dzs = g.Dys + ny;
+  if (cfg->grid == CFDGB_GRID_SML) {
+    // per-axis operator factors and the Jacobi scale of every row (createPressureMatrixCSR)
+    const Coef C{c};
+    std::vector<double> fac;
+    for (int q = 0; q < cfg->nx; ++q) fac.push_back(C.xm(q));
+    for (int q = 0; q < cfg->nx; ++q) fac.push_back(C.xp(q));
+    for (int q = 0; q < cfg->ny; ++q) fac.push_back(C.ym(q));
+    for (int q = 0; q < cfg->ny; ++q) fac.push_back(C.yp(q));
+    for (int q = 0; q < cfg->nz; ++q) fac.push_back(C.zm(q));
+    for (int q = 0; q < cfg->nz; ++q) fac.push_back(C.zp(q));
+    std::vector<double> jp((size_t)c->ncell);
+    for (int i = 0; i < cfg->nx; ++i)
+      for (int j = 0; j < cfg->ny; ++j)
+        for (int k = 0; k < cfg->nz; ++k) {
+          double aa = 0.0, bb = 0.0, cc = 0.0;
+          if (i == 0) aa = -C.xm(i);
+          if (i == cfg->nx - 1) aa = -C.xp(i);
+          if (j == 0) bb = -C.ym(j);
+          if (j == cfg->ny - 1) bb = -C.yp(j);
+          if (k == 0) cc = -C.zm(k);
+          if (k == cfg->nz - 1) cc = -C.zp(k);
+          const double dj = C.xm(i) + C.ym(j) + C.zm(k) + C.xp(i) + C.yp(j) + C.zp(k) + aa + bb + cc;
+          jp[((size_t)i * cfg->ny + j) * cfg->nz + k] = 1.0 / dj;
+        }
+    double *dfac = nullptr, *djp = nullptr;
+    if ((rc = dalloc(c, &dfac, fac.size())) || (rc = dalloc(c, &djp, jp.size()))) return bail(rc);
+    if (cudaMemcpy(dfac, fac.data(), fac.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(djp, jp.data(), jp.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(fail(CFDGB_ECUDA, "stretched-grid factor upload"));
+    g.nonuni = 1;
+    g.fxm = dfac; g.fxp = g.fxm + cfg->nx;
+    g.fym = g.fxp + cfg->nx; g.fyp = g.fym + cfg->ny;
+    g.fzm = g.fyp + cfg->ny; g.fzp = g.fzm + cfg->nz;
+    g.jpv = djp;
+  }
   // solver launch geometry: k along x (up to a warp), j along y, i strided over grid z
   g.lbx = 1;
   while (g.lbx < cfg->nz && g.lbx < 32) g.lbx *= 2;
@@ -1190,6 +1274,8 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
   if (!c || !obj) return fail(CFDGB_EINVAL, "null argument");
   if (c->cfg.precision != CFDGB_FP64 || c->cfg.solver == CFDGB_RBSOR)
     return fail(CFDGB_EINVAL, "the adjoint needs an FP64 BiCGSTAB context");
+  if (c->g.nonuni)  // its transposed solve relies on the symmetric uniform-grid operator
+    return fail(CFDGB_EINVAL, "the adjoint is implemented on the uniform grid");
   if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
     return fail(CFDGB_EINVAL, "bad objective window");
   if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");

@@ -36,6 +36,11 @@ struct Geo {
   // bulk-copy (TMA) pipeline of the FP32 stencil kernels (nzc % 4 == 0, nzc <= 1024):
   // blocks of tj rows x all k, tgx row tiles x tgy chunks of planes, dynamic shared memory
   int tma, tj, tgx, tgy, tsmem;
+  // stretched grid (the reference's non_uniform-SML): the operator rows come from per-axis
+  // factors 1/(D Ds) (fxm[i] = 1/Dx[i+2]/Dxs[i+1], fxp[i] = 1/Dx[i+2]/Dxs[i+2], compact
+  // index; SPE_sparseMatrix.hpp:52-58) and jpv, the Jacobi scale of every row
+  int nonuni;
+  const double *fxm, *fxp, *fym, *fyp, *fzm, *fzp, *jpv;
 };
 
 // compact row -> padded (i,j,k)
@@ -60,9 +65,50 @@ __device__ __forceinline__ long long pidx(const Geo &g, int i, int j, int k) {
 template <typename T>
 struct Stencil {
   T c[27][8];
+  int jac;  // 1: the rows are scaled by jp (CSR / Jacobi)
 };
 
 __device__ __forceinline__ int axis_class(int a, int n) { return a == 0 ? 0 : (a == n - 1 ? 2 : 1); }
+
+// Coefficients of row (ic, jc, kc) on a stretched grid, computed from the per-axis factors
+// with the reference's arithmetic: SPE_sparseMatrix.hpp:66-85 (c[1] the j-1 neighbour with
+// the j+1 factor and c[5] the reverse, as there) or, scaled, the CSR rows of
+// structureGrid.hpp:583-645 (not swapped); c[7] = jp (CSR) or 1/diag (SPE).
+__device__ __forceinline__ void nonuni_row(const Geo &g, int jac, int ic, int jc, int kc, long long row,
+                                           double (&c)[8]) {
+  const double xm = g.fxm[ic], xp = g.fxp[ic], ym = g.fym[jc], yp = g.fyp[jc], zm = g.fzm[kc], zp = g.fzp[kc];
+  const bool i0 = ic == 0, i1 = ic == g.nxc - 1, j0 = jc == 0, j1 = jc == g.nyc - 1, k0 = kc == 0,
+             k1 = kc == g.nzc - 1;
+  if (!jac) {
+    double ijk = xm + ym + zm + xp + yp + zp;
+    if (i0) ijk -= xm;
+    if (i1) ijk -= xp;
+    if (j0) ijk -= ym;
+    if (j1) ijk -= yp;
+    if (k0) ijk -= zm;
+    if (k1) ijk -= zp;
+    c[0] = i0 ? 0.0 : -xm;
+    c[1] = j0 ? 0.0 : -yp;
+    c[2] = k0 ? 0.0 : -zm;
+    c[3] = ijk;
+    c[4] = k1 ? 0.0 : -zp;
+    c[5] = j1 ? 0.0 : -ym;
+    c[6] = i1 ? 0.0 : -xp;
+    c[7] = 1.0 / ijk;
+    return;
+  }
+  const double aa = i0 ? -xm : (i1 ? -xp : 0.0), bb = j0 ? -ym : (j1 ? -yp : 0.0), cc = k0 ? -zm : (k1 ? -zp : 0.0);
+  const double dj = xm + ym + zm + xp + yp + zp + aa + bb + cc;
+  const double jp = g.jpv[row];
+  c[0] = i0 ? 0.0 : -xm * jp;
+  c[1] = j0 ? 0.0 : -ym * jp;
+  c[2] = k0 ? 0.0 : -zm * jp;
+  c[3] = dj * jp;
+  c[4] = k1 ? 0.0 : -zp * jp;
+  c[5] = j1 ? 0.0 : -yp * jp;
+  c[6] = i1 ? 0.0 : -xp * jp;
+  c[7] = jp;
+}
 
 // y = (A x)[row] for compact row with compact coordinates (ic,jc,kc); bounds on the
 // coordinates, terms accumulated in SPE column order.
@@ -80,6 +126,30 @@ __device__ __forceinline__ T stencil_row(const Stencil<T> &st, const T *__restri
   if (jc < nyc - 1) sum += c[5] * x[row + nzc];
   if (ic < nxc - 1) sum += c[6] * x[row + nyz];
   return sum;
+}
+
+// the same on any grid (the class table on a uniform one)
+__device__ __forceinline__ double stencil_row_g(const Geo &g, const Stencil<double> &st, const double *__restrict__ x,
+                                                long long row, int ic, int jc, int kc) {
+  if (!g.nonuni) return stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
+  double c[8];
+  nonuni_row(g, st.jac, ic, jc, kc, row, c);
+  const long long nyz = (long long)g.nyc * g.nzc;
+  double sum = 0.0;
+  if (ic > 0) sum += c[0] * x[row - nyz];
+  if (jc > 0) sum += c[1] * x[row - g.nzc];
+  if (kc > 0) sum += c[2] * x[row - 1];
+  sum += c[3] * x[row];
+  if (kc < g.nzc - 1) sum += c[4] * x[row + 1];
+  if (jc < g.nyc - 1) sum += c[5] * x[row + g.nzc];
+  if (ic < g.nxc - 1) sum += c[6] * x[row + nyz];
+  return sum;
+}
+// jp of a row (the Jacobi scale): class table or the stretched grid's per-row vector
+__device__ __forceinline__ double row_jp(const Geo &g, const Stencil<double> &st, int ic, int jc, int kc,
+                                         long long row) {
+  if (g.nonuni) return g.jpv[row];
+  return st.c[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)][7];
 }
 
 __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &ic, int &jc, int &kc) {

@@ -39,7 +39,14 @@ template <typename T, class F>
 __device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, int ic, int jc, int kc,
                                            long long row, F &&f, T &center) {
   const long long nyz = (long long)g.nyc * g.nzc;
+  T cs[8];
   const T *c = st.c[cls_of(g, ic, jc, kc)];
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (g.nonuni) {  // stretched grid (FP64 solvers only)
+      nonuni_row(g, st.jac, ic, jc, kc, row, cs);
+      c = cs;
+    }
+  }
   T sum = T(0);
   if (ic > 0) sum += c[0] * f(row - nyz);
   if (jc > 0) sum += c[1] * f(row - g.nzc);
@@ -1177,7 +1184,7 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
     acc[0] += r * r;
     acc[1] += bb * bb;
     // the unscaled residual's sum: its component along the operator's null space
-    acc[2] += jacobi ? r / st.c[cls_of(g, ic, jc, kc)][7] : r;
+    acc[2] += jacobi ? r / row_jp(g, st, ic, jc, kc, row) : r;
   }
   double out[3];
   if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
@@ -1195,7 +1202,7 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
 __device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<double> &st, int jacobi,
                                                  const double *__restrict__ r64, double m, double inv, int ic, int jc,
                                                  int kc, long long row) {
-  const double wgt = jacobi ? st.c[cls_of(g, ic, jc, kc)][7] : 1.0;
+  const double wgt = jacobi ? row_jp(g, st, ic, jc, kc, row) : 1.0;
   return (float)((r64[row] - m * wgt) * inv);
 }
 
@@ -1267,7 +1274,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs_sum(Geo g, Stencil<double> st, i
   double acc[1] = {0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    acc[0] += jacobi ? b[row] / st.c[cls_of(g, ic, jc, kc)][7] : b[row];
+    acc[0] += jacobi ? b[row] / row_jp(g, st, ic, jc, kc, row) : b[row];
   }
   double out[1];
   if (grid_sum<1>(acc, part, &ss->cnt[6], out) && lin_tid() == 0) ss->rsum = out[0];
@@ -1277,7 +1284,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs_subtract(Geo g, Stencil<double> 
   const double m = ss->rsum / (double)g.ncell;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    b[row] -= jacobi ? m * st.c[cls_of(g, ic, jc, kc)][7] : m;
+    b[row] -= jacobi ? m * row_jp(g, st, ic, jc, kc, row) : m;
   }
 }
 

@@ -147,8 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt, const do
     const double div = (us[ic] - us[ic - g.sx]) / g.Dx[i] + (vs[ic] - vs[ic - g.sy]) / g.Dy[j] +
                        (ws[ic] - ws[ic - 1]) / g.Dz[k];
     if (jacobi) {
-      const int cls = axis_class(i - 2, g.nxc) * 9 + axis_class(j - 2, g.nyc) * 3 + axis_class(k - 2, g.nzc);
-      b[row] = -st.c[cls][7] * ddt * div;
+      b[row] = -row_jp(g, st, i - 2, j - 2, k - 2, row) * ddt * div;
     } else {
       b[row] = -ddt * div;
     }
@@ -162,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_exact(Geo g, Stencil<double> st
        row += (long long)gridDim.x * kBlock) {
     int ic, jc, kc;
     row_cijk(row, g.nyc, g.nzc, ic, jc, kc);
-    y[row] = stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
+    y[row] = stencil_row_g(g, st, x, row, ic, jc, kc);
   }
 }
 

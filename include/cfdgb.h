@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 3
+#define CFDGB_ABI_VERSION 4
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -53,9 +53,17 @@ typedef enum cfdgb_precision {
                       divergence check */
 } cfdgb_precision;
 
+typedef enum cfdgb_grid {
+  CFDGB_GRID_UNIFORM = 0,  /* init_uniform (inc/grid/structureGrid.hpp:336) */
+  CFDGB_GRID_SML = 1       /* the reference's default stretched grid, "non_uniform-SML"
+                              (structureGrid.hpp:250-329): 100 fine cells over 30 % of x
+                              (shifted 4 cells upstream) and of y, coarse cells outside, z
+                              uniform; FP64 BiCGSTAB solvers; nx even > 108, ny even > 100 */
+} cfdgb_grid;
+
 typedef struct cfdgb_config {
   int nx, ny, nz;            /* interior cells (nxCal, nyCal, nzCal) */
-  double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; uniform spacing */
+  double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; spacing per cfdgb_config.grid */
   double cx, cy, radius;     /* cylinder axis along z (DFIB_CylinderZ, setEta.hpp:136) */
   double Re, dt;             /* nu = 1/Re (0_1_SimulationVariable.hpp:26) */
   int solver;                /* cfdgb_solver */
@@ -74,6 +82,7 @@ typedef struct cfdgb_config {
                                 mean; jp-weighted for the Jacobi rows) before each solve, which
                                 makes the Neumann problem consistent for any inflow; 0: the
                                 reference, which solves b as it is (default) */
+  int grid;                  /* a cfdgb_grid value; default uniform */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {

@@ -93,19 +93,24 @@ def stage_sources(force: bool = False) -> Path:
     return SRC
 
 
-def binary_name(nx: int, ny: int, nz: int, flavour: str) -> Path:
-    return BIN / f"ref_{nx}x{ny}x{nz}_{flavour}"
+GRIDDERS = {"uniform": "uniform", "sml": "non_uniform-SML"}  # structureGrid.hpp:19-20
+
+
+def binary_name(nx: int, ny: int, nz: int, flavour: str, gridder: str = "uniform") -> Path:
+    tag = "" if gridder == "uniform" else f"_{gridder}"
+    return BIN / f"ref_{nx}x{ny}x{nz}{tag}_{flavour}"
 
 
 def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
-          flavour: str = "parity", force: bool = False) -> Path:
-    """Compile the harness for one grid; returns the binary path."""
+          flavour: str = "parity", force: bool = False, gridder: str = "uniform") -> Path:
+    """Compile the harness for one grid; returns the binary path.  gridder: "uniform" or
+    "sml" (the reference's own default, non_uniform-SML)."""
     src = stage_sources()
     BIN.mkdir(parents=True, exist_ok=True)
-    exe = binary_name(nx, ny, nz, flavour)
+    exe = binary_name(nx, ny, nz, flavour, gridder)
     # the domain is part of the name only through a sidecar, so check it too
     sidecar = exe.with_suffix(".cfg")
-    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r}\n"
+    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r} {gridder}\n"
     harness = HERE / "ref_harness.cpp"
     if (exe.exists() and not force and sidecar.exists() and sidecar.read_text() == cfg
             and exe.stat().st_mtime >= harness.stat().st_mtime):
@@ -118,7 +123,7 @@ def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
         raise ValueError(flavour)
     defs = [f"-DORACLE_NX={nx}", f"-DORACLE_NY={ny}", f"-DORACLE_NZ={nz}",
             f"-DORACLE_LX={lx!r}", f"-DORACLE_LY={ly!r}", f"-DORACLE_LZ={lz!r}",
-            f"-DORACLE_CX={cx!r}", '-DORACLE_GRIDDER="uniform"']
+            f"-DORACLE_CX={cx!r}", f'-DORACLE_GRIDDER="{GRIDDERS[gridder]}"']
     cmd = (["g++", "-std=c++17", "-w"] + flags + defs +
            ["-I", str(src / "inc"), str(harness), "-o", str(exe)])
     r = subprocess.run(cmd, capture_output=True, text=True)

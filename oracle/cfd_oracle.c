@@ -47,6 +47,61 @@ int og_grid_init_uniform(og_grid *g, int nxc, int nyc, int nzc, double lx, doubl
   return 0;
 }
 
+/* inc/grid/structureGrid.hpp:250-310 (unit_SML): nodes a[gC..] of one axis of n padded
+ * cells, three uniform parts (coarse d, fine dS = lSml/nS, coarse d), the fine part
+ * shifted by off cells; nS = 0 is the plain uniform axis. */
+static int unit_sml(double *a, double lsml, int ns, int off, double l, int n) {
+  const int ncal = n - 2 * GC;
+  const double dS = lsml / ns, d = (l - lsml) / (ncal - ns);
+  a[GC] = 0.0;
+  if (ns != 0) {
+    if ((n - ns) % 2 != 0) return -1;
+    int nl0 = (ncal - ns) / 2;
+    int ns0 = nl0 + ns;
+    const int nl1 = ns0 + nl0;
+    nl0 += off;
+    ns0 += off;
+    if (nl0 <= 0) return -1;
+    for (int i = 0; i < nl0; i++) a[i + GC + 1] = a[i + GC] + d;
+    for (int i = nl0; i < ns0; ++i) a[i + GC + 1] = a[i + GC] + dS;
+    for (int i = ns0; i < nl1; i++) a[i + GC + 1] = a[i + GC] + d;
+  } else {
+    for (int i = GC; i < n - GC; i++) a[i + 1] = a[i] + l / ncal;
+  }
+  return 0;
+}
+
+/* structureGrid.hpp:433-487 (init_gC_dx): ghost nodes by linear extrapolation, widths
+ * and centre spacings, ghost widths copied from the nearest interior ones */
+static void init_gc_dx(double *X, double *Dx, double *Dxs, int nx) {
+  X[1] = 2 * X[2] - X[3];
+  X[0] = 2 * X[1] - X[2];
+  X[nx - 1] = 2 * X[nx - 2] - X[nx - 3];
+  X[nx] = 2 * X[nx - 1] - X[nx - 2];
+  for (int i = GC; i < nx - GC - 1; ++i) Dxs[i] = (X[i + 2] - X[i]) / 2.0;
+  for (int i = GC; i < nx - GC - 1; ++i) Dx[i] = (X[i + 1] - X[i]);
+  Dx[0] = Dx[1] = Dx[2];
+  Dxs[0] = Dxs[1] = Dxs[2];
+  Dx[nx - 1] = Dx[nx - 2] = Dx[nx - 3] = X[nx - 2] - X[nx - 3];
+  Dxs[nx - 1] = Dxs[nx - 2] = Dxs[nx - 3] = Dxs[nx - 4];
+}
+
+/* structureGrid.hpp:312-329 (init_nonuniform_SML, the reference's default gridder):
+ * 30 % of x and y resolved by 100 fine cells (x shifted 4 cells upstream), z uniform */
+int og_grid_init_sml(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly, double lz, double cx,
+                     double cy, double radius) {
+  if (og_grid_init_uniform(g, nxc, nyc, nzc, lx, ly, lz, cx, cy, radius)) return -1;
+  if (unit_sml(g->X, 0.3 * lx, 100, -4, lx, g->nx) || unit_sml(g->Y, 0.3 * ly, 100, 0, ly, g->ny) ||
+      unit_sml(g->Z, 0.5 * lz, 0, 0, lz, g->nz)) {
+    og_grid_free(g);
+    return -1;
+  }
+  init_gc_dx(g->X, g->Dx, g->Dxs, g->nx);
+  init_gc_dx(g->Y, g->Dy, g->Dys, g->ny);
+  init_gc_dx(g->Z, g->Dz, g->Dzs, g->nz);
+  return 0;
+}
+
 void og_grid_free(og_grid *g) {
   free(g->X); free(g->Y); free(g->Z);
   free(g->Dx); free(g->Dy); free(g->Dz);

@@ -28,6 +28,10 @@ typedef struct og_grid {
 
 int og_grid_init_uniform(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly,
                          double lz, double cx, double cy, double radius);
+/* The reference's default stretched "non_uniform-SML" grid (structureGrid.hpp:250-329,
+ * 433-487); needs nxc even and > 108, nyc even and > 100.  Returns -1 otherwise. */
+int og_grid_init_sml(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly, double lz, double cx,
+                     double cy, double radius);
 void og_grid_free(og_grid *g);
 long og_padded(const og_grid *g);
 long og_cells(const og_grid *g);

@@ -61,6 +61,7 @@ def lib():
         L = C.CDLL(str(build()))
         gp = C.POINTER(_Grid)
         L.og_grid_init_uniform.argtypes = [gp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 6
+        L.og_grid_init_sml.argtypes = [gp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 6
         L.og_grid_free.argtypes = [gp]
         L.og_perturb.argtypes = [gp, _dp, _dp, _dp, C.c_uint64, C.c_double]
         L.og_convection_diffusion.argtypes = [gp, C.c_double, C.c_double] + [_dp] * 6
@@ -92,10 +93,12 @@ def lib():
 class Grid:
     """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
 
-    def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5):
+    def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform"):
+        """gridder: "uniform" (init_uniform) or "sml" (the reference's default stretched
+        non_uniform-SML grid)."""
         self._g = _Grid()
-        rc = lib().og_grid_init_uniform(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx,
-                                        ly / 2.0, radius)
+        init = {"uniform": lib().og_grid_init_uniform, "sml": lib().og_grid_init_sml}[gridder]
+        rc = init(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx, ly / 2.0, radius)
         if rc != 0:
             raise ValueError("grid too small")
         self.shape = (nxc + 4, nyc + 4, nzc + 4)

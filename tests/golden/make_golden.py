@@ -11,8 +11,8 @@ Fixtures written next to this file:
                     (inputs and outputs, padded layout), the CFL diagnostic and the
                     bytes of the reference's Plot3D .x and .q files
   run_<case>.npz    whole runs of the 96x48x4 flow-past-cylinder case (reference BCs,
-                    Re 100, dt 0.005): interior of the final u, v, w, p and the per-step
-                    iterations, residual, Cd and Cl.
+                    Re 100, dt 0.005) and of the stretched SML grid: interior of the final
+                    u, v, w, p and the per-step iterations, residual, Cd and Cl.
 """
 from __future__ import annotations
 
@@ -40,6 +40,17 @@ RUNS = {
     "c1_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8),
     "c1_csr_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "csr", 1.8),
     "c1_sor_tol1e-3_4": (4, 100.0, 0.005, 1e-3, "sor", 1.8),
+}
+# the reference's default stretched grid (non_uniform-SML) at the smallest sizes its
+# unit_SML accepts (100 fine cells per x/y axis), on its default domain 17 x 12 x 3 with
+# the cylinder at (6.5, 6); tol 1e-3, the tolerance the reference's default case runs at
+# (with its zero-gradient boundaries the stretched Neumann problem is not consistent, and
+# its own BiCGSTAB hits the cap from step 3 at 1e-6 and tighter)
+SML = (120, 110, 4, 17.0, 12.0, 3.0, 6.5)
+SML_RUNS = {
+    # name: (steps, Re, dt, tol, solver, omega, fields stored)
+    "sml_spe_tol1e-3_10": (10, 100.0, 0.005, 1e-3, "spe", 1.8, ("u", "v", "w", "p")),
+    "sml_csr_tol1e-3_10": (10, 100.0, 0.005, 1e-3, "csr", 1.8, ("p",)),
 }
 UNIT_SEED = 7
 UNIT_RE, UNIT_DT = 100.0, 0.005
@@ -74,17 +85,17 @@ def make_unit(name, spec):
     np.savez_compressed(HERE / f"unit_{name}.npz", meta=meta, **arrs)
 
 
-def make_run(name, spec):
-    nxc, nyc, nzc, lx, ly, lz, cx = C1
+def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p")):
+    nxc, nyc, nzc, lx, ly, lz, cx = grid
     steps, Re, dt, tol, solver, omega = spec
-    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity")
+    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", gridder=gridder)
     with tempfile.TemporaryDirectory() as td:
         subprocess.run([str(exe), "run", str(steps), repr(Re), repr(dt), repr(tol), solver,
                         repr(omega), "0", "0", td], check=True, env=_env(),
                        stdout=subprocess.DEVNULL, cwd=td)
         shape = (nxc + 4, nyc + 4, nzc + 4)
         fields = {k: np.fromfile(Path(td) / f"{k}.f64").reshape(shape)[2:-2, 2:-2, 2:-2].copy()
-                  for k in ("u", "v", "w", "p")}
+                  for k in keep}
         stats = np.loadtxt(Path(td) / "stats.txt")
     meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, steps, Re, dt, tol, omega], dtype=np.float64)
     np.savez_compressed(HERE / f"run_{name}.npz", meta=meta, solver=np.array(solver),
@@ -98,6 +109,9 @@ def main():
         print("unit", n)
     for n, s in RUNS.items():
         make_run(n, s)
+        print("run", n)
+    for n, s in SML_RUNS.items():
+        make_run(n, s[:6], grid=SML, gridder="sml", keep=s[6])
         print("run", n)
 
 

@@ -42,7 +42,7 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 3
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 4
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
@@ -77,3 +77,16 @@ def test_perturbation_generator_matches_oracle():
     np.testing.assert_array_equal(u, 1.0 + du)
     np.testing.assert_array_equal(v, dv)
     np.testing.assert_array_equal(w, dw)
+
+
+@pytest.mark.parametrize("kw", [dict(nx=96, ny=110), dict(nx=121, ny=110), dict(nx=120, ny=100),
+                                dict(precision="mixed"), dict(solver="cg"), dict(solver="rbsor"),
+                                dict(project_rhs=1)])
+def test_stretched_grid_limits_rejected(lib, kw):
+    """The SML grid needs unit_SML's sizes and runs the FP64 BiCGSTAB solvers only."""
+    base = dict(nx=120, ny=110, nz=4, lx=17.0, ly=12.0, lz=3.0, cx=6.5, cy=6.0, grid="sml")
+    base.update(kw)
+    cfg = cg.default_config(**base)
+    h = C.c_void_p()
+    assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
+    assert h.value is None

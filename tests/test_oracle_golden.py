@@ -134,3 +134,21 @@ def test_plot3d_files_byte_identical(unit, tmp_path):
     O.plot3d(g, P["in_p"], P["in_u3"], P["in_v3"], P["in_w3"], P["in_eta"], Re, 0.0, q, x)
     np.testing.assert_array_equal(np.fromfile(x, dtype=np.uint8), z["p3d_x"])
     np.testing.assert_array_equal(np.fromfile(q, dtype=np.uint8), z["p3d_q"])
+
+
+@pytest.mark.parametrize("case", ["sml_spe_tol1e-3_10", "sml_csr_tol1e-3_10"])
+def test_stretched_grid_run_bit_exact(case, golden):
+    """The reference's default stretched grid (non_uniform-SML): the restated grid generator
+    and the whole step on it, SPE and CSR-Jacobi, against the reference's own runs."""
+    z = golden(f"run_{case}.npz")
+    m = z["meta"]
+    nxc, nyc, nzc = (int(x) for x in m[:3])
+    g = O.Grid(nxc, nyc, nzc, m[3], m[4], m[5], m[6], gridder="sml")
+    steps, Re, dt, tol, omega = int(m[7]), m[8], m[9], m[10], m[11]
+    r = O.run(g, steps, Re, dt, tol, str(z["solver"]), omega)
+    np.testing.assert_array_equal(r["iters"], z["iters"])
+    np.testing.assert_array_equal(r["cd"], z["cd"])
+    np.testing.assert_array_equal(r["cl"], z["cl"])
+    for k in ("u", "v", "w", "p"):
+        if k in z:
+            np.testing.assert_array_equal(r[k][2:-2, 2:-2, 2:-2], z[k])
