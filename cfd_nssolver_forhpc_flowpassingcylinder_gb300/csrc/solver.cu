@@ -39,14 +39,23 @@ template <typename T, class F>
 __device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, int ic, int jc, int kc,
                                            long long row, F &&f, T &center) {
   const long long nyz = (long long)g.nyc * g.nzc;
-  T cs[8];
-  const T *c = st.c[cls_of(g, ic, jc, kc)];
   if constexpr (sizeof(T) == sizeof(double)) {
-    if (g.nonuni) {  // stretched grid (FP64 solvers only)
+    if (g.nonuni) {  // stretched grid (FP64 solvers only): coefficients in registers
+      double cs[8];
       nonuni_row(g, st.jac, ic, jc, kc, row, cs);
-      c = cs;
+      T sum = T(0);
+      if (ic > 0) sum += cs[0] * f(row - nyz);
+      if (jc > 0) sum += cs[1] * f(row - g.nzc);
+      if (kc > 0) sum += cs[2] * f(row - 1);
+      center = f(row);
+      sum += cs[3] * center;
+      if (kc < g.nzc - 1) sum += cs[4] * f(row + 1);
+      if (jc < g.nyc - 1) sum += cs[5] * f(row + g.nzc);
+      if (ic < g.nxc - 1) sum += cs[6] * f(row + nyz);
+      return sum;
     }
   }
+  const T *c = st.c[cls_of(g, ic, jc, kc)];
   T sum = T(0);
   if (ic > 0) sum += c[0] * f(row - nyz);
   if (jc > 0) sum += c[1] * f(row - g.nzc);
