@@ -821,6 +821,48 @@ int og_plot3d_q(const og_grid *g, const double *p, const double *u, const double
   return 0;
 }
 
+int og_plot3d_read(const og_grid *g, const char *path, double head[5], double *p, double *u, double *v, double *w,
+                   double *eta) {
+  /* QfileRead (inc/io/Plot3D/qfileRead.hpp:6-106): the header, five float32 arrays in
+   * k-j-i order; p and eta go to the interior cells as they are, u, v, w back to faces as
+   * the float sum of the two cells beside the face, halved in double (:87-97), the last
+   * face of each axis taking its cell's value.  Everything else stays 0. */
+  FILE *f = fopen(path, "rb");
+  if (!f) return -1;
+  int ih[4];
+  float fh[4];
+  const long n = og_cells(g);
+  float *q = (float *)malloc(sizeof(float) * 5 * (size_t)n);
+  int ok = q && fread(ih, sizeof(int), 4, f) == 4 && fread(fh, sizeof(float), 4, f) == 4 &&
+           ih[1] == g->nxc && ih[2] == g->nyc && ih[3] == g->nzc;
+  if (ok) ok = fread(q, sizeof(float), 5 * (size_t)n, f) == 5 * (size_t)n;
+  fclose(f);
+  if (!ok) {
+    free(q);
+    return -1;
+  }
+  head[0] = ih[0];
+  for (int a = 0; a < 4; ++a) head[1 + a] = fh[a];
+  const long np = og_padded(g);
+  double *o[5] = {p, u, v, w, eta};
+  for (int a = 0; a < 5; ++a) memset(o[a], 0, sizeof(double) * (size_t)np);
+  /* file index of compact (i, j, k) and its neighbours along each axis */
+#define QF(a, i, j, k) q[(long)(a) * n + (i) + (long)g->nxc * ((j) + (long)g->nyc * (k))]
+  for (int k = 0; k < g->nzc; ++k)
+    for (int j = 0; j < g->nyc; ++j)
+      for (int i = 0; i < g->nxc; ++i) {
+        const long c = IC(g, i + GC, j + GC, k + GC);
+        p[c] = QF(0, i, j, k);
+        eta[c] = QF(4, i, j, k);
+        u[c] = i == g->nxc - 1 ? (double)QF(1, i, j, k) : (float)(QF(1, i, j, k) + QF(1, i + 1, j, k)) / 2.0;
+        v[c] = j == g->nyc - 1 ? (double)QF(2, i, j, k) : (float)(QF(2, i, j, k) + QF(2, i, j + 1, k)) / 2.0;
+        w[c] = k == g->nzc - 1 ? (double)QF(3, i, j, k) : (float)(QF(3, i, j, k) + QF(3, i, j, k + 1)) / 2.0;
+      }
+#undef QF
+  free(q);
+  return 0;
+}
+
 int og_cg_solve(const og_grid *g, const double *val7, const double *rhs, double *x, double tol, int maxit,
                 double *relres) {
   const long n = og_cells(g);

@@ -91,6 +91,11 @@ void og_cfl(const og_grid *g, double dt, const double *us, const double *vs, con
 int og_plot3d_x(const og_grid *g, const char *path);
 int og_plot3d_q(const og_grid *g, const double *p, const double *u, const double *v, const double *w,
                 const double *eta, double Re, double time, const char *path);
+/* QfileRead (inc/io/Plot3D/qfileRead.hpp:6): head = {blocks, mach, alpha, Re, time}; the
+ * padded p, u, v, w, eta it rebuilds from the cell-centred file (zero outside the interior).
+ * Return 0, or -1 if the file cannot be read or its sizes are not this grid's. */
+int og_plot3d_read(const og_grid *g, const char *path, double head[5], double *p, double *u, double *v, double *w,
+                   double *eta);
 
 /* Whole run in the order of src/RUN_CPU.cpp:257-436.  solver: 0 SPE-BiCGSTAB,
  * 1 CSR(Jacobi)-BiCGSTAB, 2 lexicographic SOR, 3 SPE-CG (og_cg_solve).  Fields in/out are padded; stats gets

@@ -208,6 +208,19 @@ def plot3d(g, p, u, v, w, eta, Re, time, qpath, xpath):
         raise OSError("plot3d write failed")
 
 
+def plot3d_read(g, qpath):
+    """QfileRead (qfileRead.hpp:6): (head = [blocks, mach, alpha, Re, time], p, u, v, w, eta)
+    as padded arrays rebuilt from the cell-centred .q file."""
+    L = lib()
+    L.og_plot3d_read.argtypes = [C.c_void_p, C.c_char_p] + [C.c_void_p] * 6
+    head = np.zeros(5)
+    out = [g.zeros() for _ in range(5)]
+    if L.og_plot3d_read(g.ptr, str(qpath).encode(), head.ctypes.data_as(C.c_void_p),
+                        *[a.ctypes.data_as(C.c_void_p) for a in out]):
+        raise OSError(f"cannot read {qpath} as a Plot3D solution of this grid")
+    return (head, *out)
+
+
 def sor(g, dt, omega, tol, itmax, us, vs, ws, p):
     err = C.c_double()
     it = lib().og_sor(g.ptr, dt, omega, tol, itmax, _c(us), _c(vs), _c(ws), p, C.byref(err))

@@ -326,6 +326,17 @@ int unit_mode(int argc, char **argv) {
     copy_bytes("mx_out/P3D.x", out + "/p3d_x.bin");
     copy_bytes("mx_out/P3D00.q", out + "/p3d_q.bin");
   }
+  // 12. the same .q file read back by QfileRead (the restart reader, its use commented out
+  // at src/RUN_CPU.cpp:88-99): header and the padded p, u, v, w, eta it rebuilds
+  {
+    auto [nb, mach, alpha, reyn, time, rp, ru, rv, rw, reta] = QfileRead(gA, "mx_out/P3D00.q");
+    dump(out, "p3d_read_head", std::vector<double>{(double)nb, mach, alpha, reyn, time});
+    dump(out, "p3d_read_p", rp);
+    dump(out, "p3d_read_u", ru);
+    dump(out, "p3d_read_v", rv);
+    dump(out, "p3d_read_w", rw);
+    dump(out, "p3d_read_eta", reta);
+  }
   return 0;
 }
 

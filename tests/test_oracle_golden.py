@@ -136,6 +136,27 @@ def test_plot3d_files_byte_identical(unit, tmp_path):
     np.testing.assert_array_equal(np.fromfile(q, dtype=np.uint8), z["p3d_q"])
 
 
+def test_plot3d_read_bit_exact(unit, tmp_path):
+    """QfileRead (qfileRead.hpp:6) of the reference's own .q file: header and the padded
+    p, u, v, w, eta it rebuilds from the cell-centred values."""
+    z, g, P = unit
+    q = tmp_path / "P3D00.q"
+    z["p3d_q"].tofile(q)
+    head, *fields = O.plot3d_read(g, q)
+    np.testing.assert_array_equal(head, z["p3d_read_head"])
+    for name, f in zip(("p", "u", "v", "w", "eta"), fields):
+        np.testing.assert_array_equal(f, P["p3d_read_" + name])
+
+
+def test_plot3d_read_rejects_another_grid(unit, tmp_path):
+    z, g, P = unit
+    q = tmp_path / "P3D00.q"
+    z["p3d_q"].tofile(q)
+    other = O.Grid(g.shape[0] - 3, g.shape[1] - 4, g.shape[2] - 4, 1.0, 1.0, 1.0, 0.5)
+    with pytest.raises(OSError):
+        O.plot3d_read(other, q)
+
+
 @pytest.mark.parametrize("case", ["sml_spe_tol1e-3_10", "sml_csr_tol1e-3_10"])
 def test_stretched_grid_run_bit_exact(case, golden):
     """The reference's default stretched grid (non_uniform-SML): the restated grid generator
