@@ -304,10 +304,16 @@ def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file)
         t = json.loads(traffic_file.read_text())
         traffic = t.get(dom, {}).get("bytes_per_launch")
     share = {k: round(v[0] / total, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0]) if v[0] > 0}
+    # every iteration kernel of this precision: average launch and algorithmic GB/s
+    each = {}
+    for k, (kms, kn) in sorted(ks.items(), key=lambda kv: -kv[1][0]):
+        us = kms / kn * 1e3
+        gbs = KERNEL_WORDS[k] * word_bytes * cells / (us * 1e-6) / 1e9
+        each[k] = {"avg_launch_us": round(us, 2), "achieved": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
     r = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
          "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(per_launch_s * 1e6, 2),
-         "peak_kind": peak_kind}
+         "peak_kind": peak_kind, "per_kernel": each}
     return r, share
 
 

@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 4  # CFDGB_ABI_VERSION
+ABI_VERSION = 5  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -26,6 +26,8 @@ SOLVERS = {"bicgstab": BICGSTAB, "spe": BICGSTAB, "jacobi": BICGSTAB_JACOBI, "cs
 PRECISIONS = {"fp64": FP64, "mixed": MIXED}
 GRID_UNIFORM, GRID_SML = 0, 1
 GRIDS = {"uniform": GRID_UNIFORM, "sml": GRID_SML}
+QUICK, LUD, UD = 0, 1, 2
+SCHEMES = {"quick": QUICK, "lud": LUD, "ud": UD}
 
 
 class CfdgbError(RuntimeError):
@@ -44,7 +46,7 @@ class Config(C.Structure):
                 ("tol", C.c_double), ("maxit", C.c_int), ("omega", C.c_double),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
-                ("grid", C.c_int)]
+                ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -97,8 +99,11 @@ EXPORTS = {
     "cfdgb_op_update_uf": (C.c_int, [C.c_void_p] + [_dp] * 11),
     "cfdgb_op_solid_fraction": (C.c_int, [C.c_void_p, _dp]),
     "cfdgb_op_cfl": (C.c_int, [C.c_void_p] + [_dp] * 4),
+    "cfdgb_op_smagorinsky": (C.c_int, [C.c_void_p] + [_dp] * 4),
     "cfdgb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
     "cfdgb_write_plot3d": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_double]),
+    "cfdgb_read_plot3d": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
+    "cfdgb_op_plot3d_read": (C.c_int, [C.c_void_p, C.c_void_p] + [_dp] * 5),
 }
 
 
@@ -147,6 +152,10 @@ def default_config(**kw) -> Config:
             v = PRECISIONS[v]
         if k == "grid" and isinstance(v, str):
             v = GRIDS[v]
+        if k == "scheme" and isinstance(v, str):
+            v = SCHEMES[v]
+        if k == "les":
+            v = int(bool(v))
         setattr(cfg, k, v)
     return cfg
 
@@ -281,6 +290,13 @@ class Solver:
     def convection_diffusion(self, u, v, w, us, vs, ws):
         _check(self._L.cfdgb_op_convection_diffusion(self._h, *map(_ptr, (u, v, w, us, vs, ws))))
 
+    def smagorinsky(self, u, v, w):
+        """SmagorinskyModel: the compact eddy viscosity of padded u, v, w."""
+        nut = np.zeros(self.cells)
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, w)]
+        _check(self._L.cfdgb_op_smagorinsky(self._h, *[_ptr(x) for x in a], _ptr(nut)))
+        return nut
+
     def bc_main(self, u, v, w, p):
         _check(self._L.cfdgb_op_bc_main(self._h, *map(_ptr, (u, v, w, p))))
 
@@ -331,6 +347,21 @@ class Solver:
         """The reference's Plot3D grid (.x) and solution (.q) files of the current state."""
         enc = lambda p: None if p is None else str(p).encode()
         _check(self._L.cfdgb_write_plot3d(self._h, enc(xpath), enc(qpath), float(time)))
+
+    def read_plot3d(self, qpath):
+        """Restart from a Plot3D solution file of this grid (QfileRead): it becomes the state,
+        as init_fields would set it.  Returns the header [blocks, mach, alpha, Re, time]."""
+        head = np.zeros(5)
+        _check(self._L.cfdgb_read_plot3d(self._h, str(qpath).encode(), _ptr(head)))
+        return head
+
+    def plot3d_read_arrays(self, q):
+        """QfileRead's padded p, u, v, w, eta from the float32 arrays of a .q file (after its
+        header)."""
+        q = np.ascontiguousarray(q, dtype=np.float32)
+        out = [self.zeros() for _ in range(5)]
+        _check(self._L.cfdgb_op_plot3d_read(self._h, q.ctypes.data_as(C.c_void_p), *map(_ptr, out)))
+        return out
 
 
 def perturbation(shape, seed, amp):

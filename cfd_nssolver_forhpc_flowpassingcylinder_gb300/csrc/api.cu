@@ -59,13 +59,13 @@ uint64_t splitmix64(uint64_t &s) {
 enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
-  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_COUNT
+  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_LES, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
-    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl"};
+    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl", "smagorinsky"};
 
 struct PendingEv {
   int id;
@@ -106,6 +106,8 @@ struct cfdgb_ctx {
   double *op[10] = {nullptr};
   // Plot3D staging: five float32 arrays on the device and a pinned host copy
   float *p3d = nullptr, *h_p3d = nullptr;
+  // Smagorinsky model: (CS delta)^2 per compact row and the eddy viscosity of T0
+  double *les_l2 = nullptr, *nut = nullptr;
   double *opc[3] = {nullptr};
   std::vector<void *> allocs;
   int loop = 0;  // steps taken since the last init_fields
@@ -331,6 +333,8 @@ int validate(const cfdgb_config *c) {
     return fail(CFDGB_EINVAL, "inner_tol outside [0,1)");
   if (c->dfib && !(c->radius > 0)) return fail(CFDGB_EINVAL, "radius must be positive");
   if (c->grid < 0 || c->grid > 1) return fail(CFDGB_EINVAL, "unknown grid %d", c->grid);
+  if (c->scheme < CFDGB_QUICK || c->scheme > CFDGB_UD) return fail(CFDGB_EINVAL, "unknown scheme %d", c->scheme);
+  if (c->les != 0 && c->les != 1) return fail(CFDGB_EINVAL, "les must be 0 or 1");
   if (c->grid == CFDGB_GRID_SML) {
     // unit_SML's own conditions (structureGrid.hpp:269,283): 100 fine cells in x (shifted 4
     // cells) and in y, an even number of coarse ones on both sides
@@ -429,14 +433,22 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   return fail(CFDGB_ECUDA, "solver did not report completion");
 }
 
-// Residual reduction of one FP32 sweep (cfg.inner_tol, or 0 for the solver's own, measured
-// on the 512x256x64 workload): BiCGSTAB in FP32 breaks down near a 1e-3 reduction, so its
-// sweeps stay short (0.3: ~3000 FP32 iterations per solve, no fallback; 0.01 stalls); CG
-// has no such breakdown and gains from long sweeps (1e-3: ~2400 iterations, 0.3: ~4000).
+// Residual reduction of one FP32 sweep against its start (cfg.inner_tol, or 0 for the
+// solver's own, measured on the 512x256x64 and 1024x512x128 workloads): BiCGSTAB in FP32
+// loses track of its residual a few decades into one Krylov run, so its sweeps stay short
+// (0.3); CG has no such breakdown and gains from long sweeps (1e-3: ~2400 iterations per
+// solve on 512x256x64, 0.3: ~4000).
 double sweep_reduction(const cfdgb_ctx *c) {
   if (c->cfg.inner_tol > 0.0) return c->cfg.inner_tol;
   return c->cfg.solver == CFDGB_CG ? 1e-3 : 0.3;
 }
+
+// A BiCGSTAB sweep also ends once its residual is this fraction of its largest one: its
+// residual can rise far above the sweep's start before it falls, and the FP32 recursion
+// cannot follow it down much more than two decades below such a peak (the kept iterate
+// bounds what the sweep gives back).  0.3 ended sweeps right after every bump and cost
+// ~15 % on 512x256x64; the two were even on 1024x512x128.
+double sweep_peak(const cfdgb_ctx *) { return 1e-2; }
 
 // FP64 Krylov set-up on the current b and warm start x
 void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
@@ -519,7 +531,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   if (rel < c->cfg.tol) return 0;
   TRY(set_solver_params(c, c->sc32, c->cfg.tol, c->cfg.maxit));
   L(c, K_SETUP32, 1, [&] {
-    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), 1,
+    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), sweep_peak(c), 1,
                           c->part, c->sc32);
   });
   bool finish64 = false;
@@ -528,29 +540,41 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     SolverScal r;
     TRY(run_chunks(c, true, &r));
     *iters = r.iter;
-    if (r.status == CFDGB_ENAN || (r.status == CFDGB_ENOCONV && r.iter < c->cfg.maxit)) {
-      // the FP32 iteration broke down or diverged: its correction is dropped
+    // the sweep's correction: its last iterate, or (BiCGSTAB) the best one it kept when the
+    // last is worse, as after a residual peak or a breakdown; CG keeps none.  A kept iterate
+    // counts only beyond the sweep's start (its residual at least halved): a zero correction
+    // would start the next sweep from the same residual, and that sweep would repeat this one
+    const bool broke = r.status == CFDGB_ENAN || (r.status == CFDGB_ENOCONV && r.iter < c->cfg.maxit);
+    const bool bicg = c->cfg.solver != CFDGB_CG;
+    const bool kept = bicg && r.snap_rel < r.rel0;
+    const bool last = !kept || (!broke && r.relres <= r.snap_rel);
+    const float *e = last ? c->k32.x : c->k32.xb;
+    const double est = last ? r.relres : r.snap_rel;
+    if (broke && !kept) {
+      // the FP32 iteration broke down or diverged before it kept any progress
       if (trace) std::fprintf(stderr, "[cfdgb]   FP32 stopped: status %d at %d\n", r.status, r.iter);
       finish64 = true;
       break;
     }
     L(c, K_CORRECT64, 2, [&] {
-      launch_sum32(c->stream, c->g, c->k32.x, c->part, c->ss);
-      launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, scale, c->ss);
+      launch_sum32(c->stream, c->g, e, c->part, c->ss);
+      launch_correct64(c->stream, c->nblk, c->g, c->x, e, scale, c->ss);
     });
     double rn = 0.0;
     TRY(residual(0, &rn));
     *outer = o + 1;
     if (trace)
-      std::fprintf(stderr, "[cfdgb]   refinement %d after %d FP32 iterations: relres %.3e (FP32 estimate %.3e)\n",
-                   o + 1, r.iter, rn, r.relres);
+      std::fprintf(stderr, "[cfdgb]   refinement %d after %d FP32 iterations: relres %.3e (FP32 estimate %.3e%s)\n",
+                   o + 1, r.iter, rn, est, last ? "" : ", kept iterate");
     // the FP32 recursion must still track the true residual (BiCGSTAB's residual is not
-    // monotone, so a larger one alone is no failure); if it has drifted or the residual
-    // runs away, the correction is taken back when it made things worse
-    const bool drifted = !(std::fabs(rn - r.relres) <= 0.5 * rn);
-    if (!std::isfinite(rn) || drifted || rn > 1e3 * best) {
+    // monotone, so a larger one alone is no failure).  A sweep whose estimate has drifted
+    // still counts when the true residual at least halved (a long CG sweep on a fine grid
+    // ends a little short of its FP32 estimate); otherwise, or when the residual runs away,
+    // the correction is taken back when it made things worse and FP64 finishes
+    const bool drifted = !(std::fabs(rn - est) <= 0.5 * rn);
+    if (!std::isfinite(rn) || (drifted && !(rn <= 0.5 * rel)) || rn > 1e3 * best) {
       if (!(rn <= rel))
-        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, c->k32.x, -scale, c->ss); });
+        L(c, K_CORRECT64, 1, [&] { launch_correct64(c->stream, c->nblk, c->g, c->x, e, -scale, c->ss); });
       else
         *relres = rn;
       finish64 = true;
@@ -560,7 +584,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     best = std::min(best, rn);
     *relres = rn;
     if (rn < c->cfg.tol) break;
-    if (r.status == CFDGB_ENOCONV) {  // iteration cap
+    if (r.status == CFDGB_ENOCONV && !broke) {  // iteration cap
       *status = CFDGB_ENOCONV;
       break;
     }
@@ -569,7 +593,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
       break;
     }
     L(c, K_SETUP32, 1, [&] {
-      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), 0,
+      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), sweep_peak(c), 0,
                             c->part, c->sc32);
     });
   }
@@ -605,6 +629,50 @@ int apply_init_bc(cfdgb_ctx *c) {
   c->loop = 0;
   c->have_fields = true;
   return 0;
+}
+
+// Plot3D staging: five float32 arrays on the device and their pinned host copy
+int ensure_p3d(cfdgb_ctx *c) {
+  if (c->p3d) return 0;
+  const size_t n = (size_t)c->ncell;
+  TRY(dalloc(c, &c->p3d, 5 * n));
+  CK(cudaMallocHost(&c->h_p3d, 5 * n * sizeof(float)));
+  return 0;
+}
+
+// Smagorinsky model: the length scale (CS delta)^2, delta = pow(Dx Dy Dz, 1/3) as
+// SmagorinskyModel.hpp:74-76 computes it, per compact row (on the host, with the same pow),
+// and the eddy viscosity buffer
+int ensure_les(cfdgb_ctx *c) {
+  if (c->nut) return 0;
+  const int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+  std::vector<double> l2((size_t)c->ncell);
+  const double CS = 0.18;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        const double delta = std::pow(c->Dx[i + 2] * c->Dy[j + 2] * c->Dz[k + 2], 1.0 / 3.0);
+        const double l = CS * delta;
+        l2[((size_t)i * ny + j) * nz + k] = l * l;
+      }
+  TRY(dalloc(c, &c->les_l2, l2.size()));
+  TRY(dalloc(c, &c->nut, l2.size()));
+  CK(cudaMemcpy(c->les_l2, l2.data(), l2.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// u* of the step: Smagorinsky first when on; the FP32 stencil sweep for MIXED QUICK
+void convdiff(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *us, double *vs, double *ws) {
+  const double nu = 1.0 / c->cfg.Re;  // 0_1_SimulationVariable.hpp:26-31
+  if (c->cfg.les)
+    L(c, K_LES, 1, [&] { launch_smagorinsky(c->stream, c->nblk, c->g, c->les_l2, u, v, w, c->nut); });
+  L(c, K_CONVDIFF, 1, [&] {
+    if (c->cfg.precision == CFDGB_MIXED && c->cfg.scheme == CFDGB_QUICK && !c->cfg.les)
+      launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, u, v, w, us, vs, ws);
+    else
+      launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.scheme, c->cfg.dt, nu, c->cfg.les ? c->nut : nullptr,
+                            u, v, w, us, vs, ws);
+  });
 }
 
 int ensure_op_buffers(cfdgb_ctx *c) {
@@ -774,12 +842,13 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.vgz = std::max(1, std::min(cfg->nx, c->nsm * per_sm / std::max(1, g.vgx * g.vgy)));
     g.xgrid = c->nsm * fp32_pointwise_blocks_per_sm();
     nblk3 = std::max(nblk3, std::max(g.vgx * g.vgy * g.vgz, g.xgrid));
-    int tbps = 0;
-    if (!std::getenv("CFDGB_NO_TMA") && fp32_stage_plan(cfg->nz, cfg->ny, &g.tj, &g.tsmem, &tbps)) {
+    int tbps = 0, tbps2 = 0;
+    if (!std::getenv("CFDGB_NO_TMA") && fp32_stage_plan(cfg->nz, &g.tj, &g.tsmem, &tbps, &g.tsmem2, &tbps2)) {
       g.tma = 1;
       g.tgx = (cfg->ny + g.tj - 1) / g.tj;
       g.tgy = std::max(1, std::min(cfg->nx, c->nsm * tbps / g.tgx));  // one wave of resident blocks
-      nblk3 = std::max(nblk3, g.tgx * g.tgy);
+      g.tgy2 = std::max(1, std::min(cfg->nx, c->nsm * tbps2 / g.tgx));
+      nblk3 = std::max(nblk3, g.tgx * std::max(g.tgy, g.tgy2));
     }
   }
   // fields and solver vectors
@@ -798,7 +867,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   if (cfg->precision == CFDGB_MIXED) {
     if ((rc = dalloc(c, &c->r64, c->ncell))) return bail(rc);
     float **kv[] = {&c->k32.x, &c->k32.r0, &c->k32.r1, &c->k32.s, &c->k32.as, &c->p32[0], &c->p32[1],
-                    &c->ap32[0], &c->ap32[1]};
+                    &c->ap32[0], &c->ap32[1], &c->k32.xb};
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
@@ -815,6 +884,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   if (cfg->dfib) launch_eta(c->stream, c->nblk, c->g, c->Xd, c->Yd, cfg->cx, cfg->cy, cfg->radius, c->eta);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return bail(fail(CFDGB_ECUDA, "set-up kernels: %s", cudaGetErrorString(cudaGetLastError())));
+  if (cfg->les && (rc = ensure_les(c))) return bail(rc);
   *out = c;
   return 0;
 }
@@ -927,12 +997,7 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
   for (int s = 0; s < nsteps; ++s) {
     const int loop = ++c->loop;
     // 1. u* (RUN_CPU.cpp:268)
-    L(c, K_CONVDIFF, 1, [&] {
-      if (c->cfg.precision == CFDGB_MIXED)
-        launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, c->u, c->v, c->w, c->us, c->vs, c->ws);
-      else
-        launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.dt, nu, c->u, c->v, c->w, c->us, c->vs, c->ws);
-    });
+    convdiff(c, c->u, c->v, c->w, c->us, c->vs, c->ws);
     // CFL diagnostic on u* (get_Cfl, RUN_CPU.cpp:274)
     L(c, K_CFL, 1, [&] { launch_cfl(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, c->part, c->ss); });
     // 2. pressure, not at the first step (RUN_CPU.cpp:303)
@@ -1027,11 +1092,20 @@ int cfdgb_op_convection_diffusion(cfdgb_ctx *c, const double *u, const double *v
   double **o = c->op;
   TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n));
   TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
-  if (c->cfg.precision == CFDGB_MIXED)
-    launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, 1.0 / c->cfg.Re, o[0], o[1], o[2], o[3], o[4], o[5]);
-  else
-    launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.dt, 1.0 / c->cfg.Re, o[0], o[1], o[2], o[3], o[4], o[5]);
+  convdiff(c, o[0], o[1], o[2], o[3], o[4], o[5]);
   TRY(d2h(c, us, o[3], n)); TRY(d2h(c, vs, o[4], n)); TRY(d2h(c, ws, o[5], n));
+  return sync(c);
+}
+
+int cfdgb_op_smagorinsky(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *nut) {
+  if (!c || !u || !v || !w || !nut) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  TRY(ensure_les(c));
+  const size_t n = c->npad;
+  double **o = c->op;
+  TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n));
+  launch_smagorinsky(c->stream, c->nblk, c->g, c->les_l2, o[0], o[1], o[2], c->nut);
+  TRY(d2h(c, nut, c->nut, (size_t)c->ncell));
   return sync(c);
 }
 
@@ -1206,10 +1280,7 @@ int cfdgb_write_plot3d(cfdgb_ctx *c, const char *xpath, const char *qpath, doubl
   if (qpath) {  // qfile.hpp:6-105: the current T0, p and eta, packed on the device
     if (!c->have_fields) return fail(CFDGB_ESTATE, "no fields yet");
     const size_t n = (size_t)c->ncell;
-    if (!c->p3d) {
-      TRY(dalloc(c, &c->p3d, 5 * n));
-      CK(cudaMallocHost(&c->h_p3d, 5 * n * sizeof(float)));
-    }
+    TRY(ensure_p3d(c));
     launch_plot3d_pack(c->stream, c->nblk, c->g, c->p, c->u, c->v, c->w, c->eta, c->p3d);
     CK(cudaMemcpyAsync(c->h_p3d, c->p3d, 5 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
@@ -1223,6 +1294,52 @@ int cfdgb_write_plot3d(cfdgb_ctx *c, const char *xpath, const char *qpath, doubl
     if (!ok) return fail(CFDGB_EINVAL, "write of %s failed", qpath);
   }
   return 0;
+}
+
+int cfdgb_op_plot3d_read(cfdgb_ctx *c, const float *q, double *p, double *u, double *v, double *w, double *eta) {
+  if (!c || !q || !p || !u || !v || !w || !eta) return fail(CFDGB_EINVAL, "null argument");
+  TRY(ensure_op_buffers(c));
+  TRY(ensure_p3d(c));
+  const size_t n = (size_t)c->ncell;
+  std::memcpy(c->h_p3d, q, 5 * n * sizeof(float));
+  CK(cudaMemcpyAsync(c->p3d, c->h_p3d, 5 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  for (int a = 0; a < 5; ++a) CK(cudaMemsetAsync(c->op[a], 0, c->npad * sizeof(double), c->stream));
+  launch_plot3d_unpack(c->stream, c->nblk, c->g, c->p3d, c->op[0], c->op[1], c->op[2], c->op[3], c->op[4]);
+  double *out[5] = {p, u, v, w, eta};
+  for (int a = 0; a < 5; ++a) TRY(d2h(c, out[a], c->op[a], c->npad));
+  return sync(c);
+}
+
+int cfdgb_read_plot3d(cfdgb_ctx *c, const char *qpath, double *head) {
+  if (!c || !qpath) return fail(CFDGB_EINVAL, "null argument");
+  const size_t n = (size_t)c->ncell;
+  FILE *f = std::fopen(qpath, "rb");
+  if (!f) return fail(CFDGB_EINVAL, "cannot open %s", qpath);
+  int ih[4] = {0, 0, 0, 0};
+  float fh[4] = {0, 0, 0, 0};
+  const bool hok = std::fread(ih, sizeof(int), 4, f) == 4 && std::fread(fh, sizeof(float), 4, f) == 4;
+  if (!hok || ih[1] != c->cfg.nx || ih[2] != c->cfg.ny || ih[3] != c->cfg.nz) {
+    std::fclose(f);
+    return fail(CFDGB_EINVAL, "%s is not a Plot3D solution of a %dx%dx%d grid", qpath, c->cfg.nx, c->cfg.ny,
+                c->cfg.nz);
+  }
+  if (int rc = ensure_p3d(c)) {
+    std::fclose(f);
+    return rc;
+  }
+  const size_t got = std::fread(c->h_p3d, sizeof(float), 5 * n, f);
+  std::fclose(f);
+  if (got != 5 * n) return fail(CFDGB_EINVAL, "%s is truncated", qpath);
+  if (head) {
+    head[0] = ih[0];
+    for (int a = 0; a < 4; ++a) head[1 + a] = fh[a];
+  }
+  CK(cudaMemcpyAsync(c->p3d, c->h_p3d, 5 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  double *st[4] = {c->p, c->u, c->v, c->w};
+  for (auto *a : st) CK(cudaMemsetAsync(a, 0, c->npad * sizeof(double), c->stream));
+  launch_plot3d_unpack(c->stream, c->nblk, c->g, c->p3d, c->p, c->u, c->v, c->w, nullptr);
+  TRY(apply_init_bc(c));  // the loaded state starts a run, as cfdgb_init_fields does
+  return sync(c);
 }
 
 // ---- discrete adjoint -------------------------------------------------------------------
@@ -1276,6 +1393,8 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
     return fail(CFDGB_EINVAL, "the adjoint needs an FP64 BiCGSTAB context");
   if (c->g.nonuni)  // its transposed solve relies on the symmetric uniform-grid operator
     return fail(CFDGB_EINVAL, "the adjoint is implemented on the uniform grid");
+  if (c->cfg.scheme != CFDGB_QUICK || c->cfg.les)  // its transposed stencil is QUICK's
+    return fail(CFDGB_EINVAL, "the adjoint is implemented for QUICK without the Smagorinsky model");
   if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
     return fail(CFDGB_EINVAL, "bad objective window");
   if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");
@@ -1375,7 +1494,8 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
       double **wv = &c->win[4 * (n - n0)];
       launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
       // u* of step n (interior faces), from U^n
-      launch_convdiff_exact(c->stream, c->nblk, c->g, dt, nu, wv[0], wv[1], wv[2], c->us, c->vs, c->ws);
+      launch_convdiff_exact(c->stream, c->nblk, c->g, CFDGB_QUICK, dt, nu, nullptr, wv[0], wv[1], wv[2], c->us, c->vs,
+                            c->ws);
       const double cw = (n >= obj.first && n <= obj.last) ? cw_in : 0.0;
       launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, wv[3], c->us, c->vs, c->ws, c->lA[0], c->lA[1],
                       c->lA[2], c->lus[0], c->lus[1], c->lus[2], c->le[0], c->le[1], c->le[2], c->lx, c->leta,

@@ -34,8 +34,9 @@ struct Geo {
   int vbx, vby, vgx, vgy, vgz;
   int xgrid;  // blocks of the flat pointwise FP32 kernel (every SM filled)
   // bulk-copy (TMA) pipeline of the FP32 stencil kernels (nzc % 4 == 0, nzc <= 1024):
-  // blocks of tj rows x all k, tgx row tiles x tgy chunks of planes, dynamic shared memory
-  int tma, tj, tgx, tgy, tsmem;
+  // blocks of tj rows x all k, tgx row tiles x tgy chunks of planes, dynamic shared memory;
+  // tgy2, tsmem2: the same for the kernels that stage two vectors (sas, CG pq)
+  int tma, tj, tgx, tgy, tsmem, tgy2, tsmem2;
   // stretched grid (the reference's non_uniform-SML): the operator rows come from per-axis
   // factors 1/(D Ds) (fxm[i] = 1/Dx[i+2]/Dxs[i+1], fxp[i] = 1/Dx[i+2]/Dxs[i+2], compact
   // index; SPE_sparseMatrix.hpp:52-58) and jpv, the Jacobi scale of every row
@@ -167,7 +168,12 @@ struct SolverScal {
   double scale;              // MIXED: fixed scale of the FP32 residual (FP64 ||r|| at the start)
   double best;               // FP32: smallest estimated relative residual seen
   double rmax;               // MIXED: largest FP32 residual norm since the last refinement
-  double delta;              // MIXED: refine once ||r1|| < delta * rmax
+  double rstart;             // MIXED: FP32 residual norm at the start of the sweep
+  double delta;              // MIXED: refine once ||r1|| < delta * rstart (CG: delta * rmax)
+  double peak;               // MIXED BiCGSTAB: or once ||r1|| < peak * rmax
+  double rel0;               // MIXED: relres at the start of the sweep
+  double snap_rel;           // MIXED BiCGSTAB: relres of the best iterate kept so far
+  int snap;                  // MIXED BiCGSTAB: 1 = the current iterate is the new one to keep
   int iter, maxit, done, status, timestep, restart;
   int par;                   // FP32: p[par], ap[par] hold the previous iteration's vectors
   int fault;                 // FP32: a pipeline wait of a stencil kernel gave up (never expected)

@@ -7,6 +7,11 @@
 //             [solver=cg amp=1e-3 seed=1234 project_rhs=1 inner_tol=0 max_outer=400 maxit=5000]
 //             [p3d=N: Plot3D grid file <out>/P3D.x and a solution file <out>/P3D<nn>.q
 //              every N steps, byte-compatible with the reference's writers]
+//             [scheme=quick|lud|ud: the convection switch (inc/0_General.hpp:114-118);
+//              les=1: the Smagorinsky model (TERBULENCE_SMAGORINSKY)]
+//             [restart=<file.q>: start from a Plot3D solution file of this grid (QfileRead,
+//              the restart the reference leaves commented out at src/RUN_CPU.cpp:88-99);
+//              the simulated time continues from the file's header]
 //
 // Per step it prints the reference's lines ("[SPE (BICG)] iter:...", "[cD, cL] : ...")
 // and appends the drag/lift series to <out>/Time_cDcL.dat in the reference's Tecplot
@@ -42,6 +47,9 @@ int main(int argc, char **argv) {
   cfg.inner_tol = num("inner_tol", cfg.inner_tol); cfg.max_outer = (int)num("max_outer", cfg.max_outer);
   cfg.amp = num("amp", 0.0); cfg.seed = (uint64_t)num("seed", 0.0);
   cfg.project_rhs = (int)num("project_rhs", 0.0);
+  const std::string scheme = kv.count("scheme") ? kv["scheme"] : "quick";
+  cfg.scheme = scheme == "lud" ? CFDGB_LUD : scheme == "ud" ? CFDGB_UD : CFDGB_QUICK;
+  cfg.les = (int)num("les", 0.0);
   const std::string solver = kv.count("solver") ? kv["solver"] : "bicgstab";
   cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI
                : solver == "rbsor"  ? CFDGB_RBSOR
@@ -59,11 +67,16 @@ int main(int argc, char **argv) {
     ctx.resize(t1);
     std::fill(T0.u.begin(), T0.u.end(), 1.0);  // iniU(1, 0, 0), RUN_CPU.cpp:66-76
     cfdgb::check(cfdgb_init_fields(ctx.handle(), nullptr, nullptr, nullptr, nullptr));
+    double time = 0.0;
+    if (kv.count("restart")) {  // head: blocks, mach, alpha, Re, time
+      double head[5];
+      cfdgb::check(cfdgb_read_plot3d(ctx.handle(), kv["restart"].c_str(), head));
+      time = head[4];
+    }
     mkdir(out.c_str(), 0755);
     FILE *f = std::fopen((out + "/Time_cDcL.dat").c_str(), "w");
     if (f) std::fprintf(f, "TITLE     = \"\"\nVARIABLES = \"simulation time\",\"C<sub>D</sub>\",\"C<sub>L</sub>\"\nZONE T=\"%s\"",
                         solver == "rbsor" ? "SOR" : solver == "jacobi" ? "CSR (BICG)" : solver == "cg" ? "ELL (CG)" : "SPE (BICG)");
-    double time = 0.0;
     int worst = 0;
     if (p3d > 0) cfdgb::check(cfdgb_write_plot3d(ctx.handle(), (out + "/P3D.x").c_str(), nullptr, 0.0));
     for (int s = 0; s < steps; ++s) {

@@ -6,8 +6,13 @@
 namespace cfdgb {
 
 // step_exact.cu (bit-exact FP64, reference operation order)
-void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u,
-                           const double *v, const double *w, double *us, double *vs, double *ws);
+// scheme: a cfdgb_scheme value; nut (compact, may be null): eddy viscosity added to nu
+void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu,
+                           const double *nut, const double *u, const double *v, const double *w, double *us,
+                           double *vs, double *ws);
+// SmagorinskyModel on u, v, w into compact nut; l2 = (CS delta)^2 per compact row
+void launch_smagorinsky(cudaStream_t s, int nblk, const Geo &g, const double *l2, const double *u, const double *v,
+                        const double *w, double *nut);
 void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
                       const double *ws, int jacobi, const Stencil<double> &st, double *b);
 void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
@@ -19,6 +24,10 @@ void launch_cfl(cudaStream_t s, int nblk, const Geo &g, double dt, const double 
 // Plot3D solution arrays p, u, v, w, eta (float32, k-j-i order) into out[5 * ncell]
 void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p, const double *u, const double *v,
                         const double *w, const double *eta, float *out);
+// QfileRead: in[5 * ncell] (p, u, v, w, eta cell-centred, i fastest, as in a .q file) to
+// the interior of padded p, u, v, w (faces) and eta (may be null)
+void launch_plot3d_unpack(cudaStream_t s, int nblk, const Geo &g, const float *in, double *p, double *u, double *v,
+                          double *w, double *eta);
 void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
                             const double *p, const double *us, const double *vs, const double *ws, double *u3,
                             double *v3, double *w3, double *f, const double *ui, const double *vi,
@@ -37,6 +46,7 @@ void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *ta
 template <typename T>
 struct KrylovVecs {
   T *x, *r0, *r1, *p1, *s, *ap, *as;
+  T *xb;  // FP32 BiCGSTAB sweep: the best iterate kept so far (unused elsewhere)
 };
 
 // FP64 BiCGSTAB (bicgstabRe2) set-up: r0 = b - A x, r1 = p1 = r0, history px2 <- px1 <- x
@@ -52,9 +62,10 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
                         float *const p2[2], float *const ap2[2], double *part_buf, SolverScal *sc);
 // resident blocks per SM of the pointwise FP32 kernel (sizes Geo::xgrid)
 int fp32_pointwise_blocks_per_sm();
-// bulk-copy pipeline of the FP32 stencil kernels: rows per block, dynamic shared memory,
-// resident blocks per SM; returns 0 when the grid does not fit it
-int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm);
+// bulk-copy pipeline of the FP32 stencil kernels: rows per block, dynamic shared memory and
+// resident blocks per SM of the pap kernel and (smem2, blocks2) of the two-vector kernels;
+// returns 0 when the grid does not fit it
+int fp32_stage_plan(int nzc, int *tj, int *smem_bytes, int *blocks_per_sm, int *smem2_bytes, int *blocks2_per_sm);
 // CG on the SPE operator (inc/solver/cg.hpp): set-up r = b - A x, p = r; FP64 iteration
 // kernels 0..2 (q = A p, x and r, p update); FP32 sweep kernels 0..1 (p update + A p,
 // x and r), p double-buffered like the BiCGSTAB sweeps, q in ap2[0]
@@ -74,7 +85,7 @@ void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<dou
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags);
 void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
                            float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
-                           double delta, int first, double *part, SolverScal *sc);
+                           double delta, double peak, int first, double *part, SolverScal *sc);
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss);
 // x += factor (e - mean e), the mean taken from the preceding launch_sum32
 void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor,

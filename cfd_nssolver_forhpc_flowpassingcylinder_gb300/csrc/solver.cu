@@ -177,10 +177,17 @@ __device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, doub
   const double relres = sqrt(n2) / sc->norm0;
   sc->relres = relres;
   if (FP32) {
-    // MIXED sweep: hand over to the FP64 refinement once the residual has dropped by
-    // delta below the sweep's largest one, or looks converged
+    // MIXED sweep: hand over to the FP64 refinement once the residual has dropped by delta
+    // below the sweep's start, or by peak below the sweep's largest one (BiCGSTAB's
+    // residual can rise far above its start before it falls, and an FP32 recursion cannot
+    // follow it down many decades below such a peak), or looks converged
     const double rn = sqrt(n2);
     if (relres < sc->best) sc->best = relres;
+    // keep this iterate (the next x update copies it) once its residual has halved since
+    // the last one kept: a few copies per sweep, and the sweep's correction is never worse
+    // than that kept iterate, whatever the residual does afterwards
+    sc->snap = relres <= 0.5 * sc->snap_rel;
+    if (sc->snap) sc->snap_rel = relres;
     if (!isfinite(relres)) {
       sc->done = 1;
       sc->status = CFDGB_ENAN;
@@ -192,7 +199,7 @@ __device__ __forceinline__ void finish_iteration(SolverScal *sc, double n2, doub
       sc->done = 1;
       sc->status = CFDGB_ENOCONV;
       sc->iter += 1;
-    } else if (relres < sc->tol || rn < sc->delta * sc->rmax) {
+    } else if (relres < sc->tol || rn < sc->delta * sc->rstart || rn < sc->peak * sc->rmax) {
       sc->done = 1;
       sc->status = kStatusRefine;
       sc->iter += 1;
@@ -262,6 +269,7 @@ __global__ void __launch_bounds__(kBlock) k64_p(Geo g, KrylovVecs<double> v, con
 // ---- FP32 iteration: three fused kernels; p and ap are double-buffered by parity ----
 struct Vec32 {
   float *x, *r0, *r1, *s, *as, *p[2], *ap[2];
+  float *xb;  // best iterate of the BiCGSTAB sweep (xr kernels keep it)
 };
 
 // p_new = r1 + beta (p_old - omega ap_old) (or r1 on restart, which also sets r0 = r1),
@@ -331,11 +339,14 @@ __global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, double *part, S
   const int parity = sc->par;
   const float a = (float)sc->alpha, w = (float)sc->omega;
   const float *__restrict__ p = (parity ? v.p[0] : v.p[1]);
+  const bool keep = sc->snap != 0;  // the current x is the iterate to keep
   AccF n2, rr;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const float s = v.s[row];
-    v.x[row] = fmaf(w, s, fmaf(a, p[row], v.x[row]));
+    const float x = v.x[row];
+    if (keep) v.xb[row] = x;
+    v.x[row] = fmaf(w, s, fmaf(a, p[row], x));
     const float r1 = fmaf(-w, v.as[row], s);
     v.r1[row] = r1;
     n2.add(r1 * r1);
@@ -815,26 +826,32 @@ __global__ void __launch_bounds__(kBlock) k32t_sas(Geo g, Stencil<float> st, Vec
   }
 }
 
-// Shared memory of the bulk-copy kernels (the larger pap variant) and their residency;
-// 0 when the grid does not fit the scheme (nz % 4 != 0 or more than 256 quads per row).
+// Shared memory of the bulk-copy kernels and their residency.  The pap kernel stages three
+// vectors with halo rows and one without; the two-vector kernels (sas, CG pq) stage two, so
+// they get their own, smaller size and more resident blocks.  0 when the grid does not fit
+// the scheme (nz % 4 != 0 or more than 256 quads per row).
 __global__ void k32cgt_pq(Geo g, Stencil<float> st, Vec32 v, double *part, SolverScal *sc);
 
-int fp32_stage_plan(int nzc, int nyc, int *tj, int *smem_bytes, int *blocks_per_sm) {
+int fp32_stage_plan(int nzc, int *tj, int *smem_bytes, int *blocks_per_sm, int *smem2_bytes, int *blocks2_per_sm) {
   if (nzc % 4 != 0 || nzc / 4 > kBlock) return 0;
   const int t = kBlock / (nzc / 4);
   const long long bytes = 128 + kStages * stage_floats(t, nzc, 3, true) * 4;
+  const long long bytes2 = 128 + kStages * stage_floats(t, nzc, 2, false) * 4;
   if (bytes > 227 * 1024) return 0;
   *tj = t;
   *smem_bytes = (int)bytes;
+  *smem2_bytes = (int)bytes2;
   if (cudaFuncSetAttribute(k32t_pap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
-      cudaFuncSetAttribute(k32t_sas, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess ||
-      cudaFuncSetAttribute(k32cgt_pq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      cudaFuncSetAttribute(k32t_sas, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes2) != cudaSuccess ||
+      cudaFuncSetAttribute(k32cgt_pq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes2) != cudaSuccess)
     return 0;
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32t_pap, kBlock, (size_t)bytes) != cudaSuccess || n < 1)
+  int n = 0, n2 = 0, n3 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32t_pap, kBlock, (size_t)bytes) != cudaSuccess || n < 1 ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k32t_sas, kBlock, (size_t)bytes2) != cudaSuccess || n2 < 1 ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k32cgt_pq, kBlock, (size_t)bytes2) != cudaSuccess || n3 < 1)
     return 0;
   *blocks_per_sm = n;
-  (void)nyc;
+  *blocks2_per_sm = n2 < n3 ? n2 : n3;
   return 1;
 }
 
@@ -850,12 +867,15 @@ __global__ void __launch_bounds__(kBlock) k32v_xr(Geo g, Vec32 v, double *part, 
   const float *__restrict__ r0v = v.r0;
   float *__restrict__ xv = v.x;
   float *__restrict__ r1v = v.r1;
+  float *__restrict__ xb = v.xb;
+  const bool keep = sc->snap != 0;  // the current x is the iterate to keep
   SumF n2, rr;
   const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
     const long long row = 4 * q;
     const F4 s = ld4(sv + row), as = ld4(asv + row), pp = ld4(p + row), r0 = ld4(r0v + row);
     F4 x = ld4(xv + row), r1;
+    if (keep) st4(xb + row, x);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       x.v[t] = fmaf(w, s.v[t], fmaf(a, pp.v[t], x.v[t]));
@@ -1216,11 +1236,13 @@ __device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<dou
 }
 
 // start of a sweep: x = 0, r0 = r1 = scaled residual, rho = <r1, r1>; restart = 1 makes the
-// first k32_pap take p = r1 (the reference's p1 = r0).  first: also the solve's set-up
-// (iteration count, delta, the FP32 estimate's normalisation).
+// first k32_pap take p = r1 (the reference's p1 = r0); delta, peak: this sweep's residual
+// reductions (against its start and its largest residual).  first: also the solve's set-up
+// (iteration count, the FP32 estimate's normalisation).
 __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double> st, int jacobi, Vec32 v,
                                                             const double *__restrict__ r64, const StepScal *ss,
-                                                            double delta, int first, double *part, SolverScal *sc) {
+                                                            double delta, double peak, int first, double *part,
+                                                            SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
   const double m = ss->rsum / (double)g.ncell;
   Dot2F acc;
@@ -1238,13 +1260,18 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
       sc->fault = 0;
       sc->timestep += 1;
       sc->norm0 = ss->bnorm * inv;  // relres = ||r1|| scale / ||b||
-      sc->delta = delta;
       sc->best = ss->relres;
       sc->iter = 0;
     }
+    sc->delta = delta;
+    sc->peak = peak;
     sc->rho = out[0];
     sc->rmax = sqrt(out[0]);
+    sc->rstart = sc->rmax;
     sc->relres = sqrt(out[0]) / sc->norm0;
+    sc->rel0 = sc->relres;
+    sc->snap_rel = sc->relres;  // x = 0, kept by the first x update
+    sc->snap = 1;
     sc->done = 0;
     sc->status = 0;
     sc->restart = 1;
@@ -1351,6 +1378,7 @@ static inline Vec32 v32(const KrylovVecs<float> &v, float *const p2[2], float *c
   Vec32 o;
   o.x = v.x; o.r0 = v.r0; o.r1 = v.r1; o.s = v.s; o.as = v.as;
   o.p[0] = p2[0]; o.p[1] = p2[1]; o.ap[0] = ap2[0]; o.ap[1] = ap2[1];
+  o.xb = v.xb;
   return o;
 }
 
@@ -1375,11 +1403,10 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
                         SolverScal *sc) {
   const Vec32 w = v32(v, p2, ap2);
   if (g.tma && part < 2) {  // stencil kernels on the bulk-copy pipeline
-    const dim3 tg(g.tgx, g.tgy, 1);
     if (part == 0)
-      k32t_pap<<<tg, kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+      k32t_pap<<<dim3(g.tgx, g.tgy, 1), kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
     else
-      k32t_sas<<<tg, kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+      k32t_sas<<<dim3(g.tgx, g.tgy2, 1), kBlock, g.tsmem2, s>>>(g, st, w, part_buf, sc);
     return;
   }
   if (g.vbx > 0) {  // vectorised path
@@ -1417,7 +1444,7 @@ void launch_cg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<floa
     const int grid = g.xgrid > 0 ? g.xgrid : g.lgx * g.lgy * g.lgz;
     k32cg_xr<<<grid, kBlock, 0, s>>>(g, w, part_buf, sc);
   } else if (g.tma) {
-    k32cgt_pq<<<dim3(g.tgx, g.tgy, 1), kBlock, g.tsmem, s>>>(g, st, w, part_buf, sc);
+    k32cgt_pq<<<dim3(g.tgx, g.tgy2, 1), kBlock, g.tsmem2, s>>>(g, st, w, part_buf, sc);
   } else if (g.vbx > 0) {
     k32cgv_pq<<<dim3(g.vgx, g.vgy, g.vgz), dim3(g.vbx, g.vby, 1), 0, s>>>(g, st, w, part_buf, sc);
   } else {
@@ -1436,8 +1463,9 @@ void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> 
 }
 void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
                            float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
-                           double delta, int first, double *part, SolverScal *sc) {
-  k_refine_start32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, delta, first, part, sc);
+                           double delta, double peak, int first, double *part, SolverScal *sc) {
+  k_refine_start32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, delta, peak, first, part,
+                                                   sc);
 }
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss) {
   k_sum32<<<cgrid(g), cblock(g), 0, s>>>(g, e, part, ss);

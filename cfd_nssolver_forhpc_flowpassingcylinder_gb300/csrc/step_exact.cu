@@ -47,9 +47,73 @@ __device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long
     N = 0.5 * (fn + fc) - 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I] * ((fp - fc) / Ds[I] - (fc - fn) / Ds[I - 1]);
 }
 
-// inc/source/Convection_Difussion.hpp:174-450: explicit Euler QUICK convection + central
-// diffusion; the last face along a component's own axis is a boundary face and skipped.
-__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, double nu,
+// inc/source/Convection_Difussion.hpp:96-147 (LudUnitA; LudUnitB has the same body)
+__device__ __forceinline__ void lud(double Up, double Un, long long pp, long long p, long long ic, long long n,
+                                    long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
+                                    int I, const double *__restrict__ phi, double &P, double &N) {
+  const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  if (Up > 0.0)
+    P = (fc + 0.5 * Ds[I] * (fc - fn) / Di[I]);
+  else
+    P = (fp + 0.5 * Ds[I + 1] * (fp - phi[pp]) / Di[I + 1]);
+  if (Un > 0.0)
+    N = (fn + 0.5 * Ds[I - 1] * (fn - phi[nn]) / Di[I - 1]);
+  else
+    N = (fc + 0.5 * Ds[I] * (fc - fp) / Di[I + 1]);
+}
+
+// face values of one axis under the convection switch (inc/0_General.hpp:114-118): QUICK,
+// LUD or UD (UdUnit, :150-168); OWN: the component's own axis (the "A" units)
+template <int S, bool OWN>
+__device__ __forceinline__ void face(double Up, double Un, long long pp, long long p, long long ic, long long n,
+                                     long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
+                                     int I, const double *__restrict__ phi, double &P, double &N) {
+  if (S == CFDGB_LUD) {
+    lud(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+  } else if (S == CFDGB_UD) {
+    P = Up > 0.0 ? phi[ic] : phi[p];
+    N = Un > 0.0 ? phi[n] : phi[ic];
+  } else if (OWN) {
+    quick_a(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+  } else {
+    quick_b(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+  }
+}
+
+// inc/source/SmagorinskyModel.hpp:30-79 with GradientGauss (:6-26), CS = 0.18: eddy
+// viscosity of T0 per cell, nut[row] = l2[row] sqrt|2 ux^2 + vy^2 + wz^2 + (uy + vx)^2 +
+// (uz + wx)^2 + (vz + wy)^2| with the reference's central differences (u over Dxs, Dy, Dz;
+// v over Dx, Dys, Dz; w over Dx, Dy, Dzs; the sum as the reference writes it).  l2 =
+// (CS cbrt(Dx Dy Dz))^2 per cell, computed once on the host with the same pow.
+__global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__restrict__ l2,
+                                                        const double *__restrict__ u, const double *__restrict__ v,
+                                                        const double *__restrict__ w, double *__restrict__ nut) {
+  const long long sx = g.sx, sy = g.sy;
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const double ux = 0.5 / g.Dxs[i] * (u[c - sx] - u[c + sx]), uy = 0.5 / g.Dy[j] * (u[c - sy] - u[c + sy]),
+                 uz = 0.5 / g.Dz[k] * (u[c - 1] - u[c + 1]);
+    const double vx = 0.5 / g.Dx[i] * (v[c - sx] - v[c + sx]), vy = 0.5 / g.Dys[j] * (v[c - sy] - v[c + sy]),
+                 vz = 0.5 / g.Dz[k] * (v[c - 1] - v[c + 1]);
+    const double wx = 0.5 / g.Dx[i] * (w[c - sx] - w[c + sx]), wy = 0.5 / g.Dy[j] * (w[c - sy] - w[c + sy]),
+                 wz = 0.5 / g.Dzs[k] * (w[c - 1] - w[c + 1]);
+    const double a = uy + vx, b = uz + wx, e = vz + wy;
+    const double temp = fabs(2.0 * (ux * ux) + vy * vy + wz * wz + a * a + b * b + e * e);
+    nut[row] = l2[row] * sqrt(temp);
+  }
+}
+
+// inc/source/Convection_Difussion.hpp:174-450: explicit Euler convection (QUICK, LUD or UD)
+// + central diffusion; the last face along a component's own axis is a boundary face and
+// skipped.
+// S: the convection scheme; nut (compact, may be null): the Smagorinsky eddy viscosity
+// added to nu per cell (Convection_Difussion.hpp:251-256).
+template <int S>
+__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, double nu0,
+                                                           const double *__restrict__ nut,
                                                            const double *__restrict__ u,
                                                            const double *__restrict__ v,
                                                            const double *__restrict__ w,
@@ -63,6 +127,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
+    const double nu = nut ? nu0 + nut[row] : nu0;
     const long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz, zp = ic + sz;
     if (i < g.nx - 3) {  // u
       const double IT = (Dxs[i] * 0.5) / Dx[i];
@@ -74,9 +139,9 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
       double uPx, uNx, uPy, uNy, uPz, uNz;
-      quick_a(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, u, uPx, uNx);
-      quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, u, uPy, uNy);
-      quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, u, uPz, uNz);
+      face<S, true>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, u, uPx, uNx);
+      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, u, uPy, uNy);
+      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, u, uPz, uNz);
       const double convection = -dt * ((uPx * uPx - uNx * uNx) / Dxs[i] + (uPy * Vp - uNy * Vn) / Dy[j] +
                                        (uPz * Wp - uNz * Wn) / Dz[k]);
       const double difussion =
@@ -96,9 +161,9 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
       double vPx, vNx, vPy, vNy, vPz, vNz;
-      quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, v, vPx, vNx);
-      quick_a(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, v, vPy, vNy);
-      quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, v, vPz, vNz);
+      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, v, vPx, vNx);
+      face<S, true>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, v, vPy, vNy);
+      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, v, vPz, vNz);
       const double convection = -dt * ((Up * vPx - Un * vNx) / Dx[i] + (vPy * vPy - vNy * vNy) / Dys[j] +
                                        (Wp * vPz - Wn * vNz) / Dz[k]);
       const double difussion =
@@ -118,9 +183,9 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
       const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
       double wPx, wNx, wPy, wNy, wPz, wNz;
-      quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, w, wPx, wNx);
-      quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, w, wPy, wNy);
-      quick_a(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, w, wPz, wNz);
+      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, w, wPx, wNx);
+      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, w, wPy, wNy);
+      face<S, true>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, w, wPz, wNz);
       const double convection = -dt * ((Up * wPx - Un * wNx) / Dx[i] + (Vp * wPy - Vn * wNy) / Dy[j] +
                                        (wPz * wPz - wNz * wNz) / Dzs[k]);
       const double difussion =
@@ -222,6 +287,29 @@ __global__ void __launch_bounds__(kBlock) k_plot3d_pack(Geo g, const double *__r
     out[2 * n + o] = (float)(0.5 * (v[c - g.sy] + v[c]));
     out[3 * n + o] = (float)(0.5 * (w[c - 1] + w[c]));
     out[4 * n + o] = (float)eta[c];
+  }
+}
+
+// QfileRead (inc/io/Plot3D/qfileRead.hpp:66-97): the five cell-centred float32 arrays of a
+// .q file (p, u, v, w, eta; i fastest) back to padded fields.  p and eta are copied; u, v, w
+// go to faces as the float sum of the cells on both sides, halved in double, and the last
+// face of each axis takes its own cell's value.  Interior cells only; eta may be null.
+__global__ void __launch_bounds__(kBlock) k_plot3d_unpack(Geo g, const float *__restrict__ in,
+                                                           double *__restrict__ p, double *__restrict__ u,
+                                                           double *__restrict__ v, double *__restrict__ w,
+                                                           double *__restrict__ eta) {
+  const long long n = g.ncell, sj = g.nxc, sk = (long long)g.nxc * g.nyc;
+  const float *U = in + n, *V = in + 2 * n, *W = in + 3 * n;
+  for (long long o = blockIdx.x * (long long)kBlock + threadIdx.x; o < n; o += (long long)gridDim.x * kBlock) {
+    const int ic = (int)(o % g.nxc);
+    const long long r = o / g.nxc;
+    const int jc = (int)(r % g.nyc), kc = (int)(r / g.nyc);
+    const long long c = pidx(g, ic + 2, jc + 2, kc + 2);
+    p[c] = (double)in[o];
+    u[c] = ic == g.nxc - 1 ? (double)U[o] : (double)__fadd_rn(U[o], U[o + 1]) / 2.0;
+    v[c] = jc == g.nyc - 1 ? (double)V[o] : (double)__fadd_rn(V[o], V[o + sj]) / 2.0;
+    w[c] = kc == g.nzc - 1 ? (double)W[o] : (double)__fadd_rn(W[o], W[o + sk]) / 2.0;
+    if (eta) eta[c] = (double)in[4 * n + o];
   }
 }
 
@@ -444,9 +532,19 @@ __global__ void __launch_bounds__(kBlock) k_eta_extrude(Geo g, double *__restric
 }
 
 // ---- launchers ----
-void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u,
-                           const double *v, const double *w, double *us, double *vs, double *ws) {
-  k_convdiff_exact<<<nblk, kBlock, 0, s>>>(g, dt, nu, u, v, w, us, vs, ws);
+void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu,
+                           const double *nut, const double *u, const double *v, const double *w, double *us,
+                           double *vs, double *ws) {
+  if (scheme == CFDGB_LUD)
+    k_convdiff_exact<CFDGB_LUD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+  else if (scheme == CFDGB_UD)
+    k_convdiff_exact<CFDGB_UD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+  else
+    k_convdiff_exact<CFDGB_QUICK><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+}
+void launch_smagorinsky(cudaStream_t s, int nblk, const Geo &g, const double *l2, const double *u, const double *v,
+                        const double *w, double *nut) {
+  k_smagorinsky<<<nblk, kBlock, 0, s>>>(g, l2, u, v, w, nut);
 }
 void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
                       const double *ws, int jacobi, const Stencil<double> &st, double *b) {
@@ -463,6 +561,10 @@ void launch_cfl(cudaStream_t s, int nblk, const Geo &g, double dt, const double 
 void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p, const double *u, const double *v,
                         const double *w, const double *eta, float *out) {
   k_plot3d_pack<<<nblk, kBlock, 0, s>>>(g, p, u, v, w, eta, out);
+}
+void launch_plot3d_unpack(cudaStream_t s, int nblk, const Geo &g, const float *in, double *p, double *u, double *v,
+                          double *w, double *eta) {
+  k_plot3d_unpack<<<nblk, kBlock, 0, s>>>(g, in, p, u, v, w, eta);
 }
 void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p) {
   k_transform<<<nblk, kBlock, 0, s>>>(g, x, p);

@@ -1,6 +1,6 @@
 /* cfdgb -- GB300-native (sm_103a) projection time step for incompressible flow past a
- * circular cylinder on a staggered MAC grid: QUICK convection-diffusion, direct-forcing
- * immersed boundary (DFIB), pressure Poisson solve and velocity correction.
+ * circular cylinder on a staggered MAC grid: convection-diffusion (QUICK by default),
+ * direct-forcing immersed boundary (DFIB), pressure Poisson solve and velocity correction.
  *
  * Drop-in for the projection step of jimmy3769tw/CFD_NSsolver_forHPC_flowPassingCylinder.
  * Each entry point names the reference interface it replaces (paths relative to that
@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 4
+#define CFDGB_ABI_VERSION 5
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -61,6 +61,13 @@ typedef enum cfdgb_grid {
                               uniform; FP64 BiCGSTAB solvers; nx even > 108, ny even > 100 */
 } cfdgb_grid;
 
+/* The reference's compile-time convection switch (inc/0_General.hpp:114-118). */
+typedef enum cfdgb_scheme {
+  CFDGB_QUICK = 0,  /* QuickUnitA/B (Convection_Difussion.hpp:20-90), the default */
+  CFDGB_LUD = 1,    /* linear upwind, LudUnitA/B (:96-147) */
+  CFDGB_UD = 2      /* first-order upwind, UdUnit (:150-168) */
+} cfdgb_scheme;
+
 typedef struct cfdgb_config {
   int nx, ny, nz;            /* interior cells (nxCal, nyCal, nzCal) */
   double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; spacing per cfdgb_config.grid */
@@ -83,6 +90,12 @@ typedef struct cfdgb_config {
                                 makes the Neumann problem consistent for any inflow; 0: the
                                 reference, which solves b as it is (default) */
   int grid;                  /* a cfdgb_grid value; default uniform */
+  int scheme;                /* a cfdgb_scheme value; default QUICK.  MIXED precision runs its
+                                FP32 stencil sweep for QUICK only; the other schemes use the
+                                FP64 kernel there */
+  int les;                   /* 1: Smagorinsky eddy viscosity (TERBULENCE_SMAGORINSKY,
+                                inc/source/SmagorinskyModel.hpp:30, CS = 0.18) added to nu,
+                                from T0 before each convection-diffusion; 0: off (default) */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {
@@ -184,10 +197,15 @@ int cfdgb_kernel_stat(cfdgb_ctx *ctx, int idx, const char **name, double *total_
 /* ---- per-function entry points on host buffers (one kernel each; for drop-in use of a
  * single reference function and for parity tests) ---- */
 
-/* ConvectionDifussion (inc/source/Convection_Difussion.hpp:174): reads u,v,w, writes
+/* ConvectionDifussion (inc/source/Convection_Difussion.hpp:174) with the context's scheme
+ * (and, les = 1, the eddy viscosity of u,v,w as the step computes it): reads u,v,w, writes
  * the interior faces of us,vs,ws (other entries of us,vs,ws are left as passed in). */
 int cfdgb_op_convection_diffusion(cfdgb_ctx *ctx, const double *u, const double *v,
                                   const double *w, double *us, double *vs, double *ws);
+/* SmagorinskyModel (inc/source/SmagorinskyModel.hpp:30): the eddy viscosity (Viseff) of
+ * padded u,v,w, into the compact array nut (nx*ny*nz). */
+int cfdgb_op_smagorinsky(cfdgb_ctx *ctx, const double *u, const double *v, const double *w,
+                         double *nut);
 /* BC_staggered_main (inc/BoundaryCondition/Boundary_Condition.hpp:37), in place. */
 int cfdgb_op_bc_main(cfdgb_ctx *ctx, double *u, double *v, double *w, double *p);
 /* BC_staggered_copy (inc/BoundaryCondition/updateBC.hpp:6): ghosts of u,v,w into us,vs,ws. */
@@ -227,6 +245,17 @@ int cfdgb_set_dt(cfdgb_ctx *ctx, double dt);
  * header (1 block, nx, ny, nz; mach 0, alpha 0, Re, time) and float32 p, cell-centred
  * u, v, w and eta in k-j-i order.  The arrays are packed on the GPU and copied out once. */
 int cfdgb_write_plot3d(cfdgb_ctx *ctx, const char *xpath, const char *qpath, double time);
+/* QfileRead (inc/io/Plot3D/qfileRead.hpp:6) and the restart it feeds (src/RUN_CPU.cpp:88-99,
+ * commented out in the reference): the solution file at qpath, which must be of this
+ * context's grid, becomes the state as cfdgb_init_fields would set it from p, u, v, w.  Faces
+ * get the float sum of the two cell-centred values beside them, halved; the last face of
+ * each axis its cell's value.  The context's eta is kept.  head (5 doubles, may be NULL):
+ * blocks, mach, alpha, Re, time of the file's header. */
+int cfdgb_read_plot3d(cfdgb_ctx *ctx, const char *qpath, double *head);
+/* QfileRead's arrays alone: q holds the 5 * nx*ny*nz float32 values of a .q file after its
+ * header; p, u, v, w, eta get the padded fields it returns (zero outside the interior). */
+int cfdgb_op_plot3d_read(cfdgb_ctx *ctx, const float *q, double *p, double *u, double *v,
+                         double *w, double *eta);
 /* Pressure solve on the current u* of the context (createBMatrix + solve +
  * Pressure_transform_X_result, src/RUN_CPU.cpp:310-320) with the configured solver. */
 int cfdgb_pressure_solve(cfdgb_ctx *ctx, int *iters, double *relres);

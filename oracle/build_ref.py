@@ -12,7 +12,11 @@ its own compile.  This recipe
 2. rewrites exactly five literals so they read from ``-D`` macros instead:
    ``inc/grid/structureGrid.hpp:20`` (Gridder), ``:28`` (lx, ly, lz),
    ``:38-40`` (nxCal, nyCal, nzCal) and ``inc/dfib/setEta.hpp:145`` (center_x);
-   every other line is the reference's own,
+   puts the convection switch ``#define CONVECTION_DIFUSSION_QUICK``
+   (``inc/0_General.hpp:114``) under ``#ifndef ORACLE_SCHEME_SET`` so that a build can
+   name LUD or UD; and corrects the one misspelt token (``auot``) that keeps the
+   Smagorinsky model (``inc/source/SmagorinskyModel.hpp:61``) from compiling, for the
+   builds that switch it on.  Every other line is the reference's own,
 3. compiles ``oracle/ref_harness.cpp`` (our driver, which calls the reference's own
    functions in the order of ``src/RUN_CPU.cpp:257-436``) once per grid into
    ``oracle/_ref/bin/ref_<nx>x<ny>x<nz>_<tag>``.
@@ -60,13 +64,24 @@ PATCHES = [
     ("inc/dfib/setEta.hpp",
      "double  center_x    = 6.5, ",
      "double  center_x    = ORACLE_CX, "),
+    # the convection switch: QUICK unless the build names another scheme
+    ("inc/0_General.hpp",
+     "\n#define CONVECTION_DIFUSSION_QUICK\n",
+     "\n#ifndef ORACLE_SCHEME_SET\n#define CONVECTION_DIFUSSION_QUICK\n#endif\n"),
+    # the Smagorinsky model does not compile as published (a misspelt `auto`); this one
+    # token is the whole fix, and it only matters to builds with TERBULENCE_SMAGORINSKY
+    ("inc/source/SmagorinskyModel.hpp",
+     "const auot icelCal",
+     "const auto icelCal"),
 ]
+# the staged copy is redone whenever the patch list changes
+PATCH_SIGNATURE = repr(PATCHES)
 
 
 def stage_sources(force: bool = False) -> Path:
     """Copy + patch the reference headers into oracle/_ref/src (idempotent)."""
     stamp = SRC / ".patched"
-    if stamp.exists() and not force:
+    if stamp.exists() and not force and stamp.read_text() == PATCH_SIGNATURE:
         return SRC
     if not (REF_ROOT / "inc").is_dir():
         if stamp.exists():
@@ -89,28 +104,37 @@ def stage_sources(force: bool = False) -> Path:
         if n != 1:
             raise RuntimeError(f"patch anchor found {n} times in {rel}: {old!r}")
         f.write_text(text.replace(old, new))
-    stamp.write_text("patched\n")
+    stamp.write_text(PATCH_SIGNATURE)
     return SRC
 
 
 GRIDDERS = {"uniform": "uniform", "sml": "non_uniform-SML"}  # structureGrid.hpp:19-20
 
 
-def binary_name(nx: int, ny: int, nz: int, flavour: str, gridder: str = "uniform") -> Path:
+SCHEMES = {"quick": "CONVECTION_DIFUSSION_QUICK", "lud": "CONVECTION_DIFUSSION_LUD",
+           "ud": "CONVECTION_DIFUSSION_UD"}  # 0_General.hpp:114-118
+
+
+def binary_name(nx: int, ny: int, nz: int, flavour: str, gridder: str = "uniform", scheme: str = "quick",
+                les: bool = False) -> Path:
     tag = "" if gridder == "uniform" else f"_{gridder}"
+    tag += "" if scheme == "quick" else f"_{scheme}"
+    tag += "_les" if les else ""
     return BIN / f"ref_{nx}x{ny}x{nz}{tag}_{flavour}"
 
 
 def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
-          flavour: str = "parity", force: bool = False, gridder: str = "uniform") -> Path:
+          flavour: str = "parity", force: bool = False, gridder: str = "uniform", scheme: str = "quick",
+          les: bool = False) -> Path:
     """Compile the harness for one grid; returns the binary path.  gridder: "uniform" or
-    "sml" (the reference's own default, non_uniform-SML)."""
+    "sml" (the reference's own default, non_uniform-SML); scheme: "quick", "lud" or "ud"
+    (the convection switch); les: TERBULENCE_SMAGORINSKY."""
     src = stage_sources()
     BIN.mkdir(parents=True, exist_ok=True)
-    exe = binary_name(nx, ny, nz, flavour, gridder)
+    exe = binary_name(nx, ny, nz, flavour, gridder, scheme, les)
     # the domain is part of the name only through a sidecar, so check it too
     sidecar = exe.with_suffix(".cfg")
-    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r} {gridder}\n"
+    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r} {gridder} {scheme} {int(les)}\n"
     harness = HERE / "ref_harness.cpp"
     if (exe.exists() and not force and sidecar.exists() and sidecar.read_text() == cfg
             and exe.stat().st_mtime >= harness.stat().st_mtime):
@@ -124,6 +148,10 @@ def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
     defs = [f"-DORACLE_NX={nx}", f"-DORACLE_NY={ny}", f"-DORACLE_NZ={nz}",
             f"-DORACLE_LX={lx!r}", f"-DORACLE_LY={ly!r}", f"-DORACLE_LZ={lz!r}",
             f"-DORACLE_CX={cx!r}", f'-DORACLE_GRIDDER="{GRIDDERS[gridder]}"']
+    if scheme != "quick":
+        defs += ["-DORACLE_SCHEME_SET", f"-D{SCHEMES[scheme]}"]
+    if les:
+        defs += ["-DTERBULENCE_SMAGORINSKY"]
     cmd = (["g++", "-std=c++17", "-w"] + flags + defs +
            ["-I", str(src / "inc"), str(harness), "-o", str(exe)])
     r = subprocess.run(cmd, capture_output=True, text=True)

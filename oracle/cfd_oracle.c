@@ -165,11 +165,83 @@ static void quick_b(double Up, double Un, long pp, long p, long ic, long n, long
              ((phi[p] - phi[ic]) / Ds[I] - (phi[ic] - phi[n]) / Ds[I - 1]);
 }
 
-/* inc/source/Convection_Difussion.hpp:174-450 (ConvectionDifussion, QUICK, 1st order) */
+/* inc/source/Convection_Difussion.hpp:96-147 (LudUnitA; LudUnitB has the same body):
+ * linear upwind, the upwind cell extrapolated half a spacing */
+static void lud(double Up, double Un, long pp, long p, long ic, long n, long nn, const double *Di,
+                const double *Ds, int I, const double *phi, double *P, double *N) {
+  if (Up > 0.0)
+    *P = (phi[ic] + 0.5 * Ds[I] * (phi[ic] - phi[n]) / Di[I]);
+  else
+    *P = (phi[p] + 0.5 * Ds[I + 1] * (phi[p] - phi[pp]) / Di[I + 1]);
+  if (Un > 0.0)
+    *N = (phi[n] + 0.5 * Ds[I - 1] * (phi[n] - phi[nn]) / Di[I - 1]);
+  else
+    *N = (phi[ic] + 0.5 * Ds[I] * (phi[ic] - phi[p]) / Di[I + 1]);
+}
+
+/* inc/source/Convection_Difussion.hpp:150-168 (UdUnit): first-order upwind */
+static void ud(double Up, double Un, long p, long ic, long n, const double *phi, double *P, double *N) {
+  *P = Up > 0.0 ? phi[ic] : phi[p];
+  *N = Un > 0.0 ? phi[n] : phi[ic];
+}
+
+/* the face values of one axis under the compile-time scheme switch of
+ * inc/0_General.hpp:114-118; own: the axis is the component's own (the "A" units) */
+static void face(int scheme, int own, double Up, double Un, long pp, long p, long ic, long n, long nn,
+                 const double *Di, const double *Ds, int I, const double *phi, double *P, double *N) {
+  if (scheme == OG_SCHEME_LUD)
+    lud(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+  else if (scheme == OG_SCHEME_UD)
+    ud(Up, Un, p, ic, n, phi, P, N);
+  else if (own)
+    quick_a(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+  else
+    quick_b(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+}
+
+/* inc/source/SmagorinskyModel.hpp:30-79 (SmagorinskyModel, CS = 0.18) with GradientGauss
+ * (:6-26): nut[icelCal] = (CS delta)^2 sqrt|S| of T0, central differences of u (metrics
+ * Dxs, Dy, Dz), v (Dx, Dys, Dz) and w (Dx, Dy, Dzs) at the cell, delta = the cube root of
+ * the cell volume.  The reference's sum is kept as written: the factor 2 multiplies
+ * du/dx^2 alone, and its gradients carry the opposite sign (they are only squared). */
+void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *nut) {
+  const double CS = 0.18;
+  const long sx = (long)g->ny * g->nz, sy = g->nz;
+  const double *M[3][3] = {{g->Dxs, g->Dy, g->Dz}, {g->Dx, g->Dys, g->Dz}, {g->Dx, g->Dy, g->Dzs}};
+  const double *F[3] = {u, v, w};
+  for (int i = GC; i < g->nx - GC; ++i)
+    for (int j = GC; j < g->ny - GC; ++j)
+      for (int k = GC; k < g->nz - GC; ++k) {
+        const long c = IC(g, i, j, k);
+        double d[3][3]; /* d[field][axis] */
+        for (int f = 0; f < 3; ++f) {
+          d[f][0] = 0.5 / M[f][0][i] * (F[f][c - sx] - F[f][c + sx]);
+          d[f][1] = 0.5 / M[f][1][j] * (F[f][c - sy] - F[f][c + sy]);
+          d[f][2] = 0.5 / M[f][2][k] * (F[f][c - 1] - F[f][c + 1]);
+        }
+        const double a = d[0][1] + d[1][0], b = d[0][2] + d[2][0], e = d[1][2] + d[2][1];
+        const double temp = fabs(2.0 * (d[0][0] * d[0][0]) + d[1][1] * d[1][1] + d[2][2] * d[2][2] + a * a +
+                                 b * b + e * e);
+        const double delta = pow(g->Dx[i] * g->Dy[j] * g->Dz[k], 1.0 / 3.0);
+        const double l = CS * delta;
+        nut[((long)(i - GC) * g->nyc + (j - GC)) * g->nzc + (k - GC)] = (l * l) * sqrt(temp);
+      }
+}
+
+/* inc/source/Convection_Difussion.hpp:174-450 (ConvectionDifussion, 1st order in time) */
 void og_convection_diffusion(const og_grid *g, double dt, double nu, const double *u,
                              const double *v, const double *w, double *us, double *vs,
                              double *ws) {
+  og_convection_diffusion_ex(g, dt, nu, NULL, u, v, w, us, vs, ws);
+}
+
+/* the same with the scheme of g->scheme and, nut != NULL, the eddy viscosity of the
+ * Smagorinsky model added to nu per cell (Convection_Difussion.hpp:251-256) */
+void og_convection_diffusion_ex(const og_grid *g, double dt, double nu0, const double *nut, const double *u,
+                                const double *v, const double *w, double *us, double *vs, double *ws) {
   const long sx = (long)g->ny * g->nz, sy = g->nz, sz = 1;
+  const int sc = g->scheme;
+#define NU_AT(i, j, k) (nut ? nu0 + nut[((long)((i) - GC) * g->nyc + ((j) - GC)) * g->nzc + ((k) - GC)] : nu0)
   const int nx = g->nx, ny = g->ny, nz = g->nz;
   /* u: last x face (i = nx-3) is a boundary face (:198-204) */
   for (int i = GC; i < nx - GC - 1; ++i)
@@ -186,12 +258,13 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
         const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
         const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
         double uPx, uNx, uPy, uNy, uPz, uNz;
-        quick_a(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, u, &uPx, &uNx);
-        quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, u, &uPy, &uNy);
-        quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, u, &uPz, &uNz);
+        face(sc, 1, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, u, &uPx, &uNx);
+        face(sc, 0, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, u, &uPy, &uNy);
+        face(sc, 0, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, u, &uPz, &uNz);
         const double convection = -dt * ((uPx * uPx - uNx * uNx) / g->Dxs[i] +
                                          (uPy * Vp - uNy * Vn) / g->Dy[j] +
                                          (uPz * Wp - uNz * Wn) / g->Dz[k]);
+        const double nu = NU_AT(i, j, k);
         const double difussion =
             nu * dt *
             (((u[xp] - u[ic]) / g->Dx[i + 1] - (u[ic] - u[xm]) / g->Dx[i]) / g->Dxs[i] +
@@ -214,12 +287,13 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
         const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
         const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
         double vPx, vNx, vPy, vNy, vPz, vNz;
-        quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, v, &vPx, &vNx);
-        quick_a(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, v, &vPy, &vNy);
-        quick_b(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, v, &vPz, &vNz);
+        face(sc, 0, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, v, &vPx, &vNx);
+        face(sc, 1, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, v, &vPy, &vNy);
+        face(sc, 0, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, v, &vPz, &vNz);
         const double convection = -dt * ((Up * vPx - Un * vNx) / g->Dx[i] +
                                          (vPy * vPy - vNy * vNy) / g->Dys[j] +
                                          (Wp * vPz - Wn * vNz) / g->Dz[k]);
+        const double nu = NU_AT(i, j, k);
         const double difussion =
             nu * dt *
             (((v[xp] - v[ic]) / g->Dxs[i] - (v[ic] - v[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
@@ -242,12 +316,13 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
         const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
         const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
         double wPx, wNx, wPy, wNy, wPz, wNz;
-        quick_b(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, w, &wPx, &wNx);
-        quick_b(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, w, &wPy, &wNy);
-        quick_a(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, w, &wPz, &wNz);
+        face(sc, 0, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, g->Dx, g->Dxs, i, w, &wPx, &wNx);
+        face(sc, 0, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, g->Dy, g->Dys, j, w, &wPy, &wNy);
+        face(sc, 1, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, g->Dz, g->Dzs, k, w, &wPz, &wNz);
         const double convection = -dt * ((Up * wPx - Un * wNx) / g->Dx[i] +
                                          (Vp * wPy - Vn * wNy) / g->Dy[j] +
                                          (wPz * wPz - wNz * wNz) / g->Dzs[k]);
+        const double nu = NU_AT(i, j, k);
         const double difussion =
             nu * dt *
             (((w[xp] - w[ic]) / g->Dxs[i] - (w[ic] - w[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
@@ -255,6 +330,7 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
              ((w[zp] - w[ic]) / g->Dz[k + 1] - (w[ic] - w[zm]) / g->Dz[k]) / g->Dzs[k]);
         ws[ic] = w[ic] + convection + difussion;
       }
+#undef NU_AT
 }
 
 /* Dir/Num table of inc/BoundaryCondition/FLOWpassing.hpp:6-40: face 0 inlet u=1 with
@@ -934,8 +1010,10 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
     memset(eta, 0, sizeof(double) * tot);
     og_dfib_cylinder_z(g, eta);
   }
+  double *nut = g->les ? dalloc(n) : NULL;
   for (int s = 1; s <= steps; ++s) {
-    og_convection_diffusion(g, dt, nu, u, v, w, us, vs, ws);
+    if (nut) og_smagorinsky(g, u, v, w, nut); /* RUN_CPU.cpp:261-263, on T0 */
+    og_convection_diffusion_ex(g, dt, nu, nut, u, v, w, us, vs, ws);
     int iters = 0;
     double err = 0.0;
     if (s > 1) { /* RUN_CPU.cpp:287/:303: no pressure solve at the first step */
@@ -968,6 +1046,7 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
   }
   if (solver == 0 || solver == 1) og_bicg_free(&bs);
   free(val7);
+  free(nut);
   free(us); free(vs); free(ws); free(u3); free(v3); free(w3); free(f); free(b); free(x);
   return rc;
 }

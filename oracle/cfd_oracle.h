@@ -24,7 +24,12 @@ typedef struct og_grid {
   double *X, *Y, *Z;           /* node coordinates, nx+1 / ny+1 / nz+1 */
   double *Dx, *Dy, *Dz;        /* cell widths, nx / ny / nz */
   double *Dxs, *Dys, *Dzs;     /* centre spacings */
+  int scheme;                  /* convection scheme: OG_SCHEME_* (0 after init: QUICK) */
+  int les;                     /* != 0: Smagorinsky eddy viscosity in og_run_ex */
 } og_grid;
+
+/* the reference's compile-time convection switch, inc/0_General.hpp:114-118 */
+enum { OG_SCHEME_QUICK = 0, OG_SCHEME_LUD = 1, OG_SCHEME_UD = 2 };
 
 int og_grid_init_uniform(og_grid *g, int nxc, int nyc, int nzc, double lx, double ly,
                          double lz, double cx, double cy, double radius);
@@ -40,6 +45,11 @@ void og_perturb(const og_grid *g, double *u, double *v, double *w, uint64_t seed
 void og_convection_diffusion(const og_grid *g, double dt, double nu, const double *u,
                              const double *v, const double *w, double *us, double *vs,
                              double *ws);
+/* with g->scheme and, nut != NULL (compact, og_smagorinsky), nu + nut per cell */
+void og_convection_diffusion_ex(const og_grid *g, double dt, double nu, const double *nut, const double *u,
+                                const double *v, const double *w, double *us, double *vs, double *ws);
+/* SmagorinskyModel (inc/source/SmagorinskyModel.hpp:30): compact eddy viscosity of T0 */
+void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *nut);
 void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p);
 void og_bc_copy(const og_grid *g, const double *u, const double *v, const double *w,
                 double *us, double *vs, double *ws);

@@ -40,7 +40,12 @@ class _Grid(C.Structure):
                 ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
                 ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)] + [
         (n, C.POINTER(C.c_double)) for n in
-        ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")]
+        ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")] + [
+        ("scheme", C.c_int), ("les", C.c_int)]
+
+
+# the reference's compile-time convection switch (0_General.hpp:114-118)
+SCHEMES = {"quick": 0, "lud": 1, "ud": 2}
 
 
 class _Bicg(C.Structure):
@@ -93,14 +98,18 @@ def lib():
 class Grid:
     """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
 
-    def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform"):
+    def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform", scheme="quick",
+                 les=False):
         """gridder: "uniform" (init_uniform) or "sml" (the reference's default stretched
-        non_uniform-SML grid)."""
+        non_uniform-SML grid); scheme: "quick", "lud" or "ud" (the convection switch);
+        les: the Smagorinsky eddy viscosity in run()."""
         self._g = _Grid()
         init = {"uniform": lib().og_grid_init_uniform, "sml": lib().og_grid_init_sml}[gridder]
         rc = init(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx, ly / 2.0, radius)
         if rc != 0:
             raise ValueError("grid too small")
+        self._g.scheme = SCHEMES[scheme]
+        self._g.les = 1 if les else 0
         self.shape = (nxc + 4, nyc + 4, nzc + 4)
         self.cells = nxc * nyc * nzc
 
@@ -128,8 +137,21 @@ def _c(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def convection_diffusion(g: Grid, dt, nu, u, v, w, us, vs, ws):
-    lib().og_convection_diffusion(g.ptr, dt, nu, _c(u), _c(v), _c(w), us, vs, ws)
+def convection_diffusion(g: Grid, dt, nu, u, v, w, us, vs, ws, nut=None):
+    """ConvectionDifussion with the grid's scheme; nut (compact): the eddy viscosity."""
+    L = lib()
+    L.og_convection_diffusion_ex.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p] + [_dp] * 6
+    L.og_convection_diffusion_ex(g.ptr, dt, nu, None if nut is None else _c(nut).ctypes.data_as(C.c_void_p),
+                                 _c(u), _c(v), _c(w), us, vs, ws)
+
+
+def smagorinsky(g: Grid, u, v, w):
+    """SmagorinskyModel (SmagorinskyModel.hpp:30): compact eddy viscosity of u, v, w."""
+    L = lib()
+    L.og_smagorinsky.argtypes = [C.c_void_p] + [_dp] * 4
+    nut = np.zeros(g.cells)
+    L.og_smagorinsky(g.ptr, _c(u), _c(v), _c(w), nut)
+    return nut
 
 
 def bc_main(g, u, v, w, p):

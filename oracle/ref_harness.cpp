@@ -19,6 +19,9 @@
 //
 // "unit" calls each hot-path function once on seeded random fields of this grid and
 // dumps inputs and outputs (golden vectors for the per-function parity tests).
+// Built with the convection switch set to LUD or UD, or with TERBULENCE_SMAGORINSKY (the
+// reference's Smagorinsky model, called before ConvectionDifussion as at
+// src/RUN_CPU.cpp:261-263), both modes use those instead.
 // Standard headers first, so that the access override below reaches only the
 // reference's own classes: it lets the bounded CPU-baseline sample set bicgstabRe2's
 // private iteration cap (iters_max_, bicgstabRe2.hpp:47); no arithmetic changes.
@@ -160,6 +163,9 @@ int run_mode(int argc, char **argv) {
   for (int s = 1; s <= steps; ++s) {
     const auto t0 = clk::now();
     simu.loop = s;
+#ifdef TERBULENCE_SMAGORINSKY
+    SmagorinskyModel(ShareM, simu, T0, t1, Lo, gA);  // src/RUN_CPU.cpp:261-263
+#endif
     ConvectionDifussion(simu, T0, T1, Lo, gA);
     simu.iters = 0; simu.error = 0.0;
     auto ts0 = clk::now(), ts1 = ts0;
@@ -236,6 +242,10 @@ int unit_mode(int argc, char **argv) {
   // 1. convection-diffusion T0 -> copy of T1
   {
     velocity C = T1;
+#ifdef TERBULENCE_SMAGORINSKY
+    SmagorinskyModel(ShareM, simu, T0, t1, Lo, gA);  // eddy viscosity of T0 (compact)
+    dump(out, "les_nut", T0.Viseff);
+#endif
     ConvectionDifussion(simu, T0, C, Lo, gA);
     dump(out, "cd_u", C.u); dump(out, "cd_v", C.v); dump(out, "cd_w", C.w);
   }

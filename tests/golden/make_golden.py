@@ -8,11 +8,16 @@ order.  Needs the reference tree (this container), not a GPU.
 
 Fixtures written next to this file:
   unit_<grid>.npz   every hot-path function once on seeded random fields
-                    (inputs and outputs, padded layout), the CFL diagnostic and the
-                    bytes of the reference's Plot3D .x and .q files
+                    (inputs and outputs, padded layout), the CFL diagnostic, the
+                    bytes of the reference's Plot3D .x and .q files and what its
+                    reader (QfileRead) makes of the .q file
+  unit_<grid>_variants.npz
+                    ConvectionDifussion of the same fields with the LUD scheme and with
+                    the Smagorinsky model (its eddy viscosity too)
   run_<case>.npz    whole runs of the 96x48x4 flow-past-cylinder case (reference BCs,
-                    Re 100, dt 0.005) and of the stretched SML grid: interior of the final
-                    u, v, w, p and the per-step iterations, residual, Cd and Cl.
+                    Re 100, dt 0.005; also with LUD and with the Smagorinsky model) and of
+                    the stretched SML grid: interior of the final u, v, w, p and the
+                    per-step iterations, residual, Cd and Cl.
 """
 from __future__ import annotations
 
@@ -85,10 +90,47 @@ def make_unit(name, spec):
     np.savez_compressed(HERE / f"unit_{name}.npz", meta=meta, **arrs)
 
 
-def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p")):
+# builds of the reference with its other convection scheme (LUD) and with its Smagorinsky
+# model switched on; UD does not compile as published (the uniform-grid variant's UdUnit
+# calls, Convection_Difussion.uniformGrid.hpp:143-144, match no overload)
+VARIANTS = {"lud": dict(scheme="lud"), "les": dict(les=True)}
+
+
+def make_unit_variants(name, spec):
+    """unit_<grid>_variants.npz: ConvectionDifussion of the same seeded fields under LUD
+    (cd_lud_*) and with the Smagorinsky eddy viscosity (les_nut, cd_les_*)."""
+    nxc, nyc, nzc, lx, ly, lz, cx = spec
+    base = np.load(HERE / f"unit_{name}.npz")
+    out = {}
+    for tag, kw in VARIANTS.items():
+        exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", **kw)
+        with tempfile.TemporaryDirectory() as td:
+            wd = Path(td) / "run"
+            wd.mkdir()
+            subprocess.run([str(exe), "unit", str(UNIT_SEED), repr(UNIT_RE), repr(UNIT_DT), td],
+                           check=True, env=_env(), stdout=subprocess.DEVNULL, cwd=wd)
+            arrs = _load_dir(Path(td))
+        for k in ("in_u", "in_v", "in_w"):  # the same seeded inputs as the QUICK fixture
+            assert np.array_equal(arrs[k], base[k]), k
+        for c in ("u", "v", "w"):
+            out[f"cd_{tag}_{c}"] = arrs[f"cd_{c}"]
+        if "les_nut" in arrs:
+            out["les_nut"] = arrs["les_nut"]
+    np.savez_compressed(HERE / f"unit_{name}_variants.npz", **out)
+
+
+# whole runs of the 96x48x4 case with LUD and with the Smagorinsky model
+VARIANT_RUNS = {
+    # name: (steps, Re, dt, tol, solver, omega, scheme, les)
+    "c1_lud_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8, "lud", False),
+    "c1_les_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8, "quick", True),
+}
+
+
+def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p"), scheme="quick", les=False):
     nxc, nyc, nzc, lx, ly, lz, cx = grid
     steps, Re, dt, tol, solver, omega = spec
-    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", gridder=gridder)
+    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", gridder=gridder, scheme=scheme, les=les)
     with tempfile.TemporaryDirectory() as td:
         subprocess.run([str(exe), "run", str(steps), repr(Re), repr(dt), repr(tol), solver,
                         repr(omega), "0", "0", td], check=True, env=_env(),
@@ -99,6 +141,7 @@ def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p")):
         stats = np.loadtxt(Path(td) / "stats.txt")
     meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, steps, Re, dt, tol, omega], dtype=np.float64)
     np.savez_compressed(HERE / f"run_{name}.npz", meta=meta, solver=np.array(solver),
+                        scheme=np.array(scheme), les=np.array(int(les)),
                         iters=stats[:, 2].astype(np.int64), err=stats[:, 3], cd=stats[:, 4],
                         cl=stats[:, 5], **fields)
 
@@ -106,12 +149,16 @@ def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p")):
 def main():
     for n, s in UNIT_GRIDS.items():
         make_unit(n, s)
+        make_unit_variants(n, s)
         print("unit", n)
     for n, s in RUNS.items():
         make_run(n, s)
         print("run", n)
     for n, s in SML_RUNS.items():
         make_run(n, s[:6], grid=SML, gridder="sml", keep=s[6])
+        print("run", n)
+    for n, s in VARIANT_RUNS.items():
+        make_run(n, s[:6], scheme=s[6], les=s[7])
         print("run", n)
 
 

@@ -42,11 +42,13 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 4
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 5
+    assert cfg.scheme == cg.QUICK and cfg.les == 0
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
-                                         ("precision", 3), ("tol", 0.0), ("maxit", 0)])
+                                         ("precision", 3), ("tol", 0.0), ("maxit", 0), ("scheme", 3),
+                                         ("scheme", -1), ("les", 2)])
 def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     cfg = cg.default_config()
     setattr(cfg, field, value)

@@ -39,6 +39,41 @@ def test_convection_diffusion_bit_exact(unit):
     np.testing.assert_array_equal(ws, P["cd_w"])
 
 
+@pytest.mark.parametrize("name", UNITS)
+def test_lud_ud_and_smagorinsky_kernels(name):
+    """ConvectionDifussion with LUD (bit-exact against the reference built with it), the
+    Smagorinsky eddy viscosity and the conv-diff using it (against the reference built
+    with TERBULENCE_SMAGORINSKY; its length scale pow(Dx Dy Dz, 1/3) comes from the host's
+    libm, which may round one ulp apart between machines, hence 1e-15 there), and UD
+    (against the oracle: no reference build compiles it)."""
+    from conftest import load_golden
+    z = load_golden(name)
+    zv = load_golden(name.replace(".npz", "_variants.npz"))
+    meta = z["meta"]
+    nxc, nyc, nzc = (int(x) for x in meta[:3])
+    shape = (nxc + 4, nyc + 4, nzc + 4)
+    P = {k: z[k].reshape(shape) for k in ("in_u", "in_v", "in_w", "in_us", "in_vs", "in_ws")}
+
+    def cd(s):
+        out = [P[k].copy() for k in ("in_us", "in_vs", "in_ws")]
+        s.convection_diffusion(P["in_u"], P["in_v"], P["in_w"], *out)
+        return out
+
+    with _solver_for(meta, scheme="lud") as s:
+        for a, c in zip(cd(s), "uvw"):
+            np.testing.assert_array_equal(a.ravel(), zv["cd_lud_" + c])
+    with _solver_for(meta, les=True) as s:
+        np.testing.assert_allclose(s.smagorinsky(P["in_u"], P["in_v"], P["in_w"]), zv["les_nut"], rtol=1e-15)
+        for a, c in zip(cd(s), "uvw"):
+            np.testing.assert_allclose(a.ravel(), zv["cd_les_" + c], rtol=1e-15)
+    g = O.Grid(nxc, nyc, nzc, *meta[3:7], scheme="ud")
+    ref = [P[k].copy() for k in ("in_us", "in_vs", "in_ws")]
+    O.convection_diffusion(g, meta[8], 1.0 / meta[7], P["in_u"], P["in_v"], P["in_w"], *ref)
+    with _solver_for(meta, scheme="ud") as s:
+        for a, b in zip(cd(s), ref):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_bc_main_and_copy_bit_exact(unit):
     z, s, P = unit
     u, v, w, p = (P[k].copy() for k in ("in_u", "in_v", "in_w", "in_p"))
@@ -131,3 +166,32 @@ def test_plot3d_files_byte_identical(unit, tmp_path):
     s.write_plot3d(x, q, 0.0)
     np.testing.assert_array_equal(np.fromfile(x, dtype=np.uint8), z["p3d_x"])
     np.testing.assert_array_equal(np.fromfile(q, dtype=np.uint8), z["p3d_q"])
+
+
+def test_plot3d_read_arrays_bit_exact(unit):
+    """QfileRead's padded p, u, v, w, eta rebuilt on the GPU from the reference's own .q
+    file: bit-exact against what the reference's reader returned."""
+    z, s, P = unit
+    q = z["p3d_q"][32:].view("<f4")  # after the 4 int + 4 float header
+    for name, f in zip(("p", "u", "v", "w", "eta"), s.plot3d_read_arrays(q)):
+        np.testing.assert_array_equal(f, P["p3d_read_" + name])
+
+
+def test_plot3d_restart_sets_the_state(unit, tmp_path):
+    """cfdgb_read_plot3d: the file's fields become the state, with the ghost fill a run
+    starts with (BC_staggered_main on the reader's arrays), and the header comes back."""
+    z, s, P = unit
+    q = tmp_path / "P3D00.q"
+    z["p3d_q"].tofile(q)
+    head = s.read_plot3d(q)
+    np.testing.assert_array_equal(head, z["p3d_read_head"])
+    g = O.Grid(*(int(x) for x in z["meta"][:3]), *z["meta"][3:7])
+    ref = {k: P["p3d_read_" + k].copy() for k in "uvwp"}
+    O.bc_main(g, ref["u"], ref["v"], ref["w"], ref["p"])
+    got = s.get_fields()
+    for k in "uvwp":
+        np.testing.assert_array_equal(got[k], ref[k])
+    bad = tmp_path / "short.q"
+    z["p3d_q"][:100].tofile(bad)
+    with pytest.raises(RuntimeError):
+        s.read_plot3d(bad)

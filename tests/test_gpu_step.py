@@ -63,6 +63,53 @@ def test_fp64_step_matches_reference_tight(case, solver, golden):
     np.testing.assert_allclose(cd, z["cd"], rtol=1e-10)
 
 
+@pytest.mark.parametrize("case,kw", [("c1_lud_spe_tol1e-13_20", dict(scheme="lud")),
+                                     ("c1_les_spe_tol1e-13_20", dict(les=True))])
+def test_scheme_and_smagorinsky_runs_match_reference(case, kw, golden):
+    """20 steps with the reference's LUD scheme and with its Smagorinsky model, against the
+    reference built with those switched on: the same 1e-10 bar as the QUICK runs."""
+    z = golden(f"run_{case}.npz")
+    steps, tol = int(z["meta"][7]), z["meta"][10]
+    with _c1(tol=tol, **kw) as s:
+        s.init_fields()
+        st = s.step(steps)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * steps
+    zf = {k: np.pad(z[k], 2) for k in "uvw"}
+    for k, e in vel_err(f, zf).items():
+        assert e <= 1e-10, (k, e)
+    assert rel_p(interior(f["p"]), z["p"]) <= 1e-10
+    np.testing.assert_allclose([r.cd for r in st], z["cd"], rtol=1e-10)
+
+
+def test_upwind_run_matches_oracle():
+    """UD: no reference build compiles it (its uniform-grid variant's calls match no
+    overload), so the oracle's restatement run is the checker, at the same bar."""
+    g = O.Grid(96, 48, 4, 24.0, 12.0, 1.0, 6.0, scheme="ud")
+    r = O.run(g, 10, 100.0, 0.005, 1e-13, "spe")
+    with _c1(tol=1e-13, scheme="ud") as s:
+        s.init_fields()
+        st = s.step(10)
+        f = s.get_fields()
+    for k, e in vel_err(f, r).items():
+        assert e <= 1e-10, (k, e)
+    np.testing.assert_allclose([x.cd for x in st], r["cd"], rtol=1e-10)
+
+
+def test_mixed_precision_with_les_and_lud_reaches_the_fp64_tolerance():
+    """MIXED with the Smagorinsky model or LUD: u* comes from the FP64 kernel, the solve
+    from FP32 sweeps in FP64 refinement; every solve ends below 1e-8."""
+    for kw in (dict(les=True), dict(scheme="lud")):
+        with _c1(precision="mixed", **kw) as a, _c1(**kw) as b:
+            a.init_fields()
+            b.init_fields()
+            sa, sb = a.step(6), b.step(6)
+            fa, fb = a.get_fields(), b.get_fields()
+        assert all(r.relres < 1e-8 for r in sa[1:]), [r.relres for r in sa]
+        for k, e in vel_err(fa, fb).items():
+            assert e <= 1e-6, (kw, k, e)
+
+
 def test_fp64_reference_case_200_steps(golden):
     """The reference's config-1 run (tol 1e-8, 200 steps): Cd(t=0.995) = 1.74226."""
     z = golden("run_c1_spe_tol1e-8_200.npz")

@@ -35,6 +35,48 @@ def test_convection_diffusion_bit_exact(unit):
     np.testing.assert_array_equal(ws, P["cd_w"])
 
 
+@pytest.mark.parametrize("name", UNITS)
+def test_lud_and_smagorinsky_bit_exact(name, golden):
+    """The reference's other convection scheme (LUD) and its Smagorinsky model, from builds
+    of the reference with those switched on: eddy viscosity and ConvectionDifussion."""
+    z = golden(name)
+    zv = golden(name.replace(".npz", "_variants.npz"))
+    meta = z["meta"]
+    Re, dt = meta[7], meta[8]
+    args = (int(meta[0]), int(meta[1]), int(meta[2]), *meta[3:7])
+    g = O.Grid(*args, scheme="lud")
+    P = {k: z[k].reshape(g.shape) for k in ("in_u", "in_v", "in_w", "in_us", "in_vs", "in_ws")}
+    us, vs, ws = P["in_us"].copy(), P["in_vs"].copy(), P["in_ws"].copy()
+    O.convection_diffusion(g, dt, 1.0 / Re, P["in_u"], P["in_v"], P["in_w"], us, vs, ws)
+    for a, c in ((us, "u"), (vs, "v"), (ws, "w")):
+        np.testing.assert_array_equal(a.ravel(), zv["cd_lud_" + c])
+    g = O.Grid(*args, les=True)
+    nut = O.smagorinsky(g, P["in_u"], P["in_v"], P["in_w"])
+    np.testing.assert_array_equal(nut, zv["les_nut"])
+    us, vs, ws = P["in_us"].copy(), P["in_vs"].copy(), P["in_ws"].copy()
+    O.convection_diffusion(g, dt, 1.0 / Re, P["in_u"], P["in_v"], P["in_w"], us, vs, ws, nut=nut)
+    for a, c in ((us, "u"), (vs, "v"), (ws, "w")):
+        np.testing.assert_array_equal(a.ravel(), zv["cd_les_" + c])
+
+
+def test_upwind_scheme_is_the_upwind_cell():
+    """UD (UdUnit, Convection_Difussion.hpp:150): no reference build compiles it, so its
+    restatement is checked by its definition: every face value is the upwind cell's, so a
+    flow along +x with v = w = 0 and nu = 0 gives u* - u = -dt (u_i^2 - u_{i-1}^2)/dx."""
+    g = O.Grid(12, 8, 6, 3.0, 2.0, 1.5, 1.5, scheme="ud")
+    rng = np.random.default_rng(3)
+    u = 1.0 + 0.1 * rng.random(g.shape)
+    v = np.zeros(g.shape)
+    w = np.zeros(g.shape)
+    us, vs, ws = u.copy(), v.copy(), w.copy()
+    dt = 0.01
+    O.convection_diffusion(g, dt, 0.0, u, v, w, us, vs, ws)
+    dx = 3.0 / 12
+    i, j, k = 5, 4, 3
+    upwind = u[i, j, k] - dt * (u[i, j, k] ** 2 - u[i - 1, j, k] ** 2) / dx
+    assert us[i, j, k] == pytest.approx(upwind, rel=1e-14)
+
+
 def test_bc_main_and_copy_bit_exact(unit):
     z, g, P = unit
     u, v, w, p = (P[k].copy() for k in ("in_u", "in_v", "in_w", "in_p"))
@@ -103,11 +145,16 @@ def test_sor_bit_exact(unit):
 
 
 @pytest.mark.parametrize("case", ["c1_spe_tol1e-13_20", "c1_csr_tol1e-13_20",
-                                  "c1_sor_tol1e-3_4", "c1_spe_tol1e-8_200"])
+                                  "c1_sor_tol1e-3_4", "c1_spe_tol1e-8_200",
+                                  "c1_lud_spe_tol1e-13_20", "c1_les_spe_tol1e-13_20"])
 def test_whole_run_bit_exact(case, golden):
     z = golden(f"run_{case}.npz")
     m = z["meta"]
-    g = _grid(m)
+    nxc, nyc, nzc = (int(x) for x in m[:3])
+    extra = {}
+    if "scheme" in z:  # runs of the reference built with LUD or its Smagorinsky model
+        extra = dict(scheme=str(z["scheme"]), les=bool(z["les"]))
+    g = O.Grid(nxc, nyc, nzc, *m[3:7], **extra)
     steps, Re, dt, tol, omega = int(m[7]), m[8], m[9], m[10], m[11]
     r = O.run(g, steps, Re, dt, tol, str(z["solver"]), omega)
     np.testing.assert_array_equal(r["iters"], z["iters"])
