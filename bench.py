@@ -350,6 +350,17 @@ def reference_iteration_record(wl):
     return None
 
 
+def reference_window_iters(rec, warmup, steps):
+    """The reference's recorded iteration counts on the timed steps warmup+1 .. warmup+steps
+    (1-based; the record's index 0 is step 1), and how many of those steps lie beyond the
+    record (filled with the mean over its solve steps)."""
+    its = rec["iters"]
+    solves = its[1:]
+    mean = sum(solves) / len(solves)
+    want = [its[i] if i < len(its) else mean for i in range(warmup, warmup + steps)]
+    return want, sum(1 for i in range(warmup, warmup + steps) if i >= len(its))
+
+
 def main_reference(args):
     """--impl reference: the reference's own CPU implementation, host cores."""
     world, rank, _ = _dist()
@@ -358,12 +369,7 @@ def main_reference(args):
     rec = reference_iteration_record(args.workload)
     threads = os.cpu_count() or 1
     steps = args.warmup + args.steps
-    if rec is None:
-        iters = None
-    else:
-        its = rec["iters"]
-        mean = sum(its) / len(its)
-        iters = [its[i] if i < len(its) else mean for i in range(args.warmup + 1, steps + 1)][-args.steps:]
+    iters = None if rec is None else reference_window_iters(rec, args.warmup, args.steps)[0]
     if iters is None:
         print(json.dumps({"impl": "reference", "unavailable": "no recorded reference iteration counts"}))
         return 0
@@ -385,7 +391,7 @@ METRIC = "cell-steps/s @resid 1e-8 (FP64 Jacobi-BiCGSTAB projection step)"
 SAMPLE_DOC = ("reference OpenMP build (-O3 -fopenmp -march=native) on the same grid, steps 1-3 with its "
               "BiCGSTAB capped at {cap} iterations: {t_iter:.4f} s per iteration, {t_other:.3f} s per step "
               "outside the solve; cell-steps/s at the iteration counts the reference itself needs to reach "
-              "1e-8 on these steps (recorded from full reference runs, tests/golden/reference_iters_<wl>.json)")
+              "1e-8 on the timed steps (recorded from a full reference run, tests/golden/reference_iters_<wl>.json)")
 
 
 def main(argv=None):
@@ -489,9 +495,7 @@ def main(argv=None):
         try:
             if rec is None:
                 raise RuntimeError("no recorded reference iteration counts")
-            its = rec["iters"]
-            mean = sum(its) / len(its)
-            want = [its[i] if i < len(its) else mean for i in range(args.warmup + 1, args.warmup + args.steps + 1)]
+            want = reference_window_iters(rec, args.warmup, args.steps)[0]
             threads = os.cpu_count() or 1
             cb = cpu_reference_sample(wl, 3, args.cap, threads, want)
             line["cpu_baseline"] = {"value": cb["value"], "unit": "cell-steps/s", "cores": threads,

@@ -436,11 +436,12 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
 // Residual reduction of one FP32 sweep against its start (cfg.inner_tol, or 0 for the
 // solver's own, measured on the 512x256x64 and 1024x512x128 workloads): BiCGSTAB in FP32
 // loses track of its residual a few decades into one Krylov run, so its sweeps stay short
-// (0.3); CG has no such breakdown and gains from long sweeps (1e-3: ~2400 iterations per
-// solve on 512x256x64, 0.3: ~4000).
+// (0.3); CG has no such breakdown and gains from long sweeps (iterations per solve on
+// 512x256x64: 0.3 ~4000, 1e-3 ~2400 in 3 refinements, 3e-4 ~2250 in 3; on 1024x512x128
+// 3e-4 saves the fourth refinement that 1e-3 needs, and 1e-4 restarts no less often).
 double sweep_reduction(const cfdgb_ctx *c) {
   if (c->cfg.inner_tol > 0.0) return c->cfg.inner_tol;
-  return c->cfg.solver == CFDGB_CG ? 1e-3 : 0.3;
+  return c->cfg.solver == CFDGB_CG ? 3e-4 : 0.3;
 }
 
 // A BiCGSTAB sweep also ends once its residual is this fraction of its largest one: its

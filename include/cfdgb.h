@@ -79,7 +79,7 @@ typedef struct cfdgb_config {
   int maxit;                 /* iteration cap (5000: bicgstabRe2.hpp:47) */
   double omega;              /* SOR relaxation */
   double inner_tol;          /* MIXED: residual reduction of each FP32 sweep; 0 (default):
-                                0.3 for the BiCGSTAB solvers, 1e-3 for CG */
+                                0.3 for the BiCGSTAB solvers, 3e-4 for CG */
   int max_outer;             /* MIXED: cap on FP64 refinements per solve */
   int check_every;           /* SOR: residual checked every this many sweeps */
   int dfib;                  /* 1: cylinder solid fraction on; 0: no immersed body */
