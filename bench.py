@@ -273,6 +273,51 @@ def adjoint_mode(cg, torch, dist, nsteps, ckpt):
                 "grad_inlet_norm": float(np.linalg.norm(g_in)), "grad_eta_norm": float(np.linalg.norm(g_eta))}
 
 
+def adjoint_fd_mode(cg, nsteps, ckpt, ndir, eps=1e-6, tol=1e-12):
+    """The adjoint gradients on the adjoint case against central finite differences of the
+    forward step: ndir seeded directions (seeds 1..ndir) for the inlet profile and as many
+    for eta (restricted to the DFIB band, 0 < eta < 1, interior cells), drag averaged over
+    the last third of nsteps steps, Poisson solved to tol with its right-hand side's mean
+    removed (with the reference's zero-gradient boundaries a perturbed inflow or body makes
+    the unprojected Neumann problem inconsistent).  Returns the relative errors."""
+    import numpy as np
+    cfg = dict(WORKLOADS["c4"])
+    first = nsteps - nsteps // 3 + 1
+    with cg.Solver(tol=tol, project_rhs=1, **cfg) as s:
+        eta0 = s.get_eta()
+
+        def J(inlet=None, eta=eta0):
+            s.set_inlet(inlet)
+            s.set_eta(eta)
+            s.init_fields()
+            return s.forward(nsteps, first, nsteps, ckpt)
+
+        J0 = J()
+        g_in, g_eta = s.backward()
+        one = np.ones(g_in.shape)
+        band = (eta0 > 0) & (eta0 < 1)
+        for a in range(3):
+            sl = [slice(None)] * 3
+            sl[a] = slice(0, 2)
+            band[tuple(sl)] = False
+            sl[a] = slice(-2, None)
+            band[tuple(sl)] = False
+        err_in, err_eta = [], []
+        for seed in range(1, ndir + 1):
+            rng = np.random.default_rng(seed)
+            d = rng.standard_normal(g_in.shape)
+            fd = (J(one + eps * d) - J(one - eps * d)) / (2 * eps)
+            err_in.append(abs(float(np.sum(g_in * d)) - fd) / abs(fd))
+            de = np.where(band, rng.standard_normal(eta0.shape), 0.0)
+            fd = (J(eta=eta0 + eps * de) - J(eta=eta0 - eps * de)) / (2 * eps)
+            err_eta.append(abs(float(np.sum(g_eta * de)) - fd) / abs(fd))
+        s.set_inlet(None)
+        s.set_eta(eta0)
+    return {"workload": "c4", "steps": nsteps, "objective_steps": [first, nsteps], "ckpt_every": ckpt,
+            "tol": tol, "eps": eps, "directions": ndir, "J": J0,
+            "inlet_rel_err": err_in, "eta_rel_err": err_eta, "max_rel_err": max(err_in + err_eta)}
+
+
 def field_errors(a, b):
     """Relative L2 errors of run a against run b after the same steps: u, v, w against the
     norm of b's whole velocity, p without its mean (the Neumann problem leaves it free),
@@ -404,6 +449,8 @@ def main(argv=None):
     ap.add_argument("--modes", default="fp64,mixed,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
+    ap.add_argument("--fd-steps", type=int, default=21, help="adjoint_fd mode: steps of each forward run")
+    ap.add_argument("--fd-dirs", type=int, default=16, help="adjoint_fd mode: directions per gradient")
     ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
     ap.add_argument("--sor-steps", type=int, default=2)
     ap.add_argument("--sor-maxit", type=int, default=20000)
@@ -490,6 +537,11 @@ def main(argv=None):
             line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt)
         except cg.CfdgbError as e:
             line["adjoint"] = {"value": None, "error": str(e)}
+    if "adjoint_fd" in modes:  # not in the default modes: ~4 * fd_dirs forward runs
+        try:
+            line["adjoint_fd"] = adjoint_fd_mode(cg, args.fd_steps, args.adj_ckpt, args.fd_dirs)
+        except cg.CfdgbError as e:
+            line["adjoint_fd"] = {"value": None, "error": str(e)}
     if "cpu" in modes and dist.rank == 0:
         rec = reference_iteration_record(wl)
         try:

@@ -293,3 +293,23 @@ def test_nan_input_is_detected():
         assert e.value.status in (cg.ENAN, cg.ENOCONV)
         s.init_fields()
         assert s.step(2)[1].status == 0
+
+
+@pytest.mark.parametrize("env", [{}, {"CFDGB_NO_TMA": "1"}, {"CFDGB_SCALAR_FP32": "1"}],
+                         ids=["bulk-copy", "vectorised", "scalar"])
+@pytest.mark.parametrize("solver", ["bicgstab", "cg"])
+def test_every_fp32_kernel_family_reaches_the_fp64_solution(env, solver, monkeypatch):
+    """The three FP32 sweep kernel families (bulk-copy pipeline, vectorised marching,
+    scalar; chosen at cfdgb_create) and a grid whose nz is no multiple of 4 (scalar by
+    shape): MIXED reaches the FP64 tolerance and the FP64 run's fields."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    for case in (dict(), dict(nx=48, ny=24, nz=6, lx=12.0, ly=6.0, lz=1.5, cx=3.0, cy=3.0)):
+        with _c1(solver=solver, precision="mixed", **case) as a, _c1(solver=solver, **case) as b:
+            a.init_fields()
+            b.init_fields()
+            sa, sb = a.step(5), b.step(5)
+            fa, fb = a.get_fields(), b.get_fields()
+        assert all(r.relres < 1e-8 for r in sa[1:]), [r.relres for r in sa]
+        for k, e in vel_err(fa, fb).items():
+            assert e <= 1e-6, (env, case, k, e)
