@@ -43,6 +43,8 @@ WORKLOADS = {
     "c3": dict(nx=1024, ny=512, nz=128, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0, Re=300.0, dt=0.001),
     # adjoint case (1M cells)
     "c4": dict(nx=256, ny=128, nz=32, lx=24.0, ly=12.0, lz=2.0, cx=6.0, cy=6.0, Re=100.0, dt=0.004),
+    # combined stress case (113M cells)
+    "c5": dict(nx=1536, ny=768, nz=96, lx=48.0, ly=24.0, lz=3.0, cx=12.0, cy=12.0, Re=300.0, dt=0.001),
 }
 
 
@@ -208,7 +210,9 @@ def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, 
         s.reset_counters()
         ms, stats = _timed_steps(s, steps, dist, torch)
         launches = s.launch_count()
-        out = {"ms": ms, "stats": stats, "launches": launches, "cells": s.cells}
+        free, total = torch.cuda.mem_get_info()
+        out = {"ms": ms, "stats": stats, "launches": launches, "cells": s.cells,
+               "device_mem_gb": round((total - free) / 1e9, 2)}
         if keep_fields:
             out["fields"] = s.get_fields()
         if profile:
@@ -248,11 +252,11 @@ def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
         return ms, nbytes, s.cells
 
 
-def adjoint_mode(cg, torch, dist, nsteps, ckpt):
+def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4"):
     """Forward run with checkpoints and the adjoint sweep (gradient of the drag averaged
     over the last third of the window w.r.t. the inlet profile and eta) on the adjoint
     case; returns both wall times (CUDA events on the library's stream) and their ratio."""
-    cfg = dict(WORKLOADS["c4"])
+    cfg = dict(WORKLOADS[wl])
     with cg.Solver(solver="jacobi", precision="fp64", tol=TOL, **cfg) as s:
         stream = torch.cuda.ExternalStream(s.stream)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -266,8 +270,9 @@ def adjoint_mode(cg, torch, dist, nsteps, ckpt):
         ev[2].record(stream)
         torch.cuda.synchronize()
         tf, tb = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+        free, total = torch.cuda.mem_get_info()
         import numpy as np
-        return {"workload": "c4", "steps": nsteps, "objective_steps": [first, nsteps], "ckpt_every": ckpt,
+        return {"workload": wl, "device_mem_gb": round((total - free) / 1e9, 2), "steps": nsteps, "objective_steps": [first, nsteps], "ckpt_every": ckpt,
                 "J": J, "forward_ms": tf, "backward_ms": tb, "adjoint_over_forward": tb / tf,
                 "forward_cell_steps_per_s": s.cells * nsteps / (tf / 1e3),
                 "grad_inlet_norm": float(np.linalg.norm(g_in)), "grad_eta_norm": float(np.linalg.norm(g_eta))}
@@ -449,6 +454,9 @@ def main(argv=None):
     ap.add_argument("--modes", default="fp64,mixed,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
+    ap.add_argument("--adj-workload", default="c4", choices=sorted(WORKLOADS))
+    ap.add_argument("--maxit", type=int, default=5000,
+                    help="Krylov iteration cap per solve (the reference's 5000; MIXED: FP32 iterations)")
     ap.add_argument("--fd-steps", type=int, default=21, help="adjoint_fd mode: steps of each forward run")
     ap.add_argument("--fd-dirs", type=int, default=16, help="adjoint_fd mode: directions per gradient")
     ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
@@ -471,7 +479,7 @@ def main(argv=None):
 
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
-        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64",
+        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64", maxit=args.maxit,
                         keep_fields=bool(modes & {"mixed", "cg", "mixed_cg"}))
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
@@ -482,17 +490,18 @@ def main(argv=None):
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t64 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state u=1, v=w=0)",
-        "config": {"workload": wl, **WORKLOADS[wl], "solver": "jacobi_bicgstab", "tol": TOL,
+        "config": {"workload": wl, **WORKLOADS[wl], "solver": "jacobi_bicgstab", "tol": TOL, "maxit": args.maxit,
                    "bc": "reference (FLOWpassing table)", "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs ~1.5 GB > 129 MB L2, no flush"},
         "iters_per_step": iters64, "relres": max(r.relres for r in fp64["stats"]),
         "gpu_launches": fp64["launches"], "roofline": roof, "kernel_share": share,
         "alu_roofline": alu_roofline(fp64["kernels"], cells, fp_peak), "fp_peaks": fp_peak,
-        "clocks": clk.summary(),
+        "clocks": clk.summary(), "device_mem_gb": fp64["device_mem_gb"],
     }
     if "mixed" in modes:
         try:
-            mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", keep_fields=True)
+            mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", maxit=args.maxit,
+                          keep_fields=True)
             tm = dist.max(mx["ms"])
             r32, share32 = roofline(mx["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
             line["mixed"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
@@ -500,14 +509,16 @@ def main(argv=None):
                              "outer_per_step": [r.outer for r in mx["stats"]],
                              "relres": max(r.relres for r in mx["stats"]), "speedup_vs_fp64": t64 / tm,
                              "error_vs_fp64": field_errors(mx, fp64),
-                             "gpu_launches": mx["launches"], "roofline": r32, "kernel_share": share32}
+                             "gpu_launches": mx["launches"], "device_mem_gb": mx["device_mem_gb"],
+                             "roofline": r32, "kernel_share": share32}
         except cg.CfdgbError as e:
             line["mixed"] = {"value": None, "error": str(e)}
     for key, solver, prec in (("cg", "cg", "fp64"), ("mixed_cg", "cg", "mixed")):
         if key not in modes:
             continue
         try:
-            rm = run_mode(cg, torch, dist, wl, args.steps, args.warmup, solver, prec, keep_fields=True)
+            rm = run_mode(cg, torch, dist, wl, args.steps, args.warmup, solver, prec, maxit=args.maxit,
+                          keep_fields=True)
             tm = dist.max(rm["ms"])
             rf, shr = roofline(rm["kernels"], cells, 4 if prec == "mixed" else 8, "32" if prec == "mixed" else "64",
                                hbm_peak, peak_kind, traffic_file)
@@ -517,7 +528,7 @@ def main(argv=None):
                          "outer_per_step": [r.outer for r in rm["stats"]],
                          "relres": max(r.relres for r in rm["stats"]), "speedup_vs_fp64": t64 / tm,
                          "error_vs_fp64": field_errors(rm, fp64), "gpu_launches": rm["launches"],
-                         "roofline": rf, "kernel_share": shr}
+                         "device_mem_gb": rm["device_mem_gb"], "roofline": rf, "kernel_share": shr}
         except cg.CfdgbError as e:
             line[key] = {"value": None, "error": str(e)}
     if "rbsor" in modes:
@@ -534,7 +545,7 @@ def main(argv=None):
                        "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
     if "adjoint" in modes:
         try:
-            line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt)
+            line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt, args.adj_workload)
         except cg.CfdgbError as e:
             line["adjoint"] = {"value": None, "error": str(e)}
     if "adjoint_fd" in modes:  # not in the default modes: ~4 * fd_dirs forward runs

@@ -76,7 +76,9 @@ typedef struct cfdgb_config {
   int solver;                /* cfdgb_solver */
   int precision;             /* cfdgb_precision */
   double tol;                /* relative residual ||b-Ax||/||b|| (p_criteria) */
-  int maxit;                 /* iteration cap (5000: bicgstabRe2.hpp:47) */
+  int maxit;                 /* iteration cap per solve (5000: bicgstabRe2.hpp:47); MIXED caps
+                                its FP32 iterations over all sweeps at maxit, and an FP64
+                                finish, when one runs, at maxit again */
   double omega;              /* SOR relaxation */
   double inner_tol;          /* MIXED: residual reduction of each FP32 sweep; 0 (default):
                                 0.3 for the BiCGSTAB solvers, 3e-4 for CG */
