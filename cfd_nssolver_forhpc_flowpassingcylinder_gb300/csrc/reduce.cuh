@@ -23,12 +23,14 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV]) {
     for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
 }
 
-// Reduce v over the block; the result is valid in thread 0 only.
+// Reduce v over the block (whole warps, at most 32 of them); the result is valid in
+// thread 0 only.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
-  __shared__ double sh[NV][kBlock / 32];
+  __shared__ double sh[NV][32];
   const int t = lin_tid();
   const int lane = t & 31, wid = t >> 5;
+  const int nw = (int)(blockDim.x * blockDim.y * blockDim.z) >> 5;
   warp_sum<NV>(v);
   __syncthreads();  // sh may still be read by a previous call
   if (lane == 0)
@@ -37,7 +39,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
   __syncthreads();
   if (wid == 0) {
 #pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = lane < kBlock / 32 ? sh[q][lane] : 0.0;
+    for (int q = 0; q < NV; ++q) v[q] = lane < nw ? sh[q][lane] : 0.0;
     warp_sum<NV>(v);
   }
 }
@@ -61,10 +63,11 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, unsigned
   if (!last) return false;
   __threadfence();
   double w[NV];
+  const int nt = (int)(blockDim.x * blockDim.y * blockDim.z);
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     double s = 0.0;
-    for (int b = t; b < G; b += kBlock) s += __ldcg(part + q * G + b);
+    for (int b = t; b < G; b += nt) s += __ldcg(part + q * G + b);
     w[q] = s;
   }
   block_sum<NV>(w);
