@@ -7,7 +7,7 @@ and writes reference_iters_<workload>.json beside this file: iterations per step
 reference's own per-step wall times.  bench.py evaluates the reference's CPU throughput
 at these counts from a bounded timing sample (one full C2 step takes ~5 min on 4 cores).
 
-    python tests/golden/make_reference_iters.py --workload c2 --steps 8 --threads 4
+    python tests/golden/make_reference_iters.py --workload c2 --steps 13 --threads 6
     python tests/golden/make_reference_iters.py --workload c2 --from-stats <run dir>/stats.txt
 """
 from __future__ import annotations
