@@ -252,7 +252,7 @@ def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
         return ms, nbytes, s.cells
 
 
-def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4"):
+def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4", first=0):
     """Forward run with checkpoints and the adjoint sweep (gradient of the drag averaged
     over the last third of the window w.r.t. the inlet profile and eta) on the adjoint
     case; returns both wall times (CUDA events on the library's stream) and their ratio."""
@@ -261,7 +261,7 @@ def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4"):
         stream = torch.cuda.ExternalStream(s.stream)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         s.init_fields()
-        first = nsteps - nsteps // 3 + 1
+        first = first or nsteps - nsteps // 3 + 1
         torch.cuda.synchronize()
         ev[0].record(stream)
         J = s.forward(nsteps, first, nsteps, ckpt)
@@ -455,6 +455,8 @@ def main(argv=None):
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--adj-workload", default="c4", choices=sorted(WORKLOADS))
+    ap.add_argument("--adj-first", type=int, default=0,
+                    help="first step of the drag average (0: the last third of --adj-steps)")
     ap.add_argument("--maxit", type=int, default=5000,
                     help="Krylov iteration cap per solve (the reference's 5000; MIXED: FP32 iterations)")
     ap.add_argument("--fd-steps", type=int, default=21, help="adjoint_fd mode: steps of each forward run")
@@ -545,7 +547,8 @@ def main(argv=None):
                        "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
     if "adjoint" in modes:
         try:
-            line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt, args.adj_workload)
+            line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt, args.adj_workload,
+                                           args.adj_first)
         except cg.CfdgbError as e:
             line["adjoint"] = {"value": None, "error": str(e)}
     if "adjoint_fd" in modes:  # not in the default modes: ~4 * fd_dirs forward runs

@@ -28,6 +28,8 @@ GRID_UNIFORM, GRID_SML = 0, 1
 GRIDS = {"uniform": GRID_UNIFORM, "sml": GRID_SML}
 QUICK, LUD, UD = 0, 1, 2
 SCHEMES = {"quick": QUICK, "lud": LUD, "ud": UD}
+WALLS_ZERO_GRADIENT, WALLS_FREE_SLIP = 0, 1
+WALLS = {"zero_gradient": WALLS_ZERO_GRADIENT, "free_slip": WALLS_FREE_SLIP}
 
 
 class CfdgbError(RuntimeError):
@@ -46,7 +48,7 @@ class Config(C.Structure):
                 ("tol", C.c_double), ("maxit", C.c_int), ("omega", C.c_double),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
-                ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int)]
+                ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -154,6 +156,8 @@ def default_config(**kw) -> Config:
             v = GRIDS[v]
         if k == "scheme" and isinstance(v, str):
             v = SCHEMES[v]
+        if k == "walls" and isinstance(v, str):
+            v = WALLS[v]
         if k == "les":
             v = int(bool(v))
         setattr(cfg, k, v)

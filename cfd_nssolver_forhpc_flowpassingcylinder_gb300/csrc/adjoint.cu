@@ -367,7 +367,7 @@ static int grid_for(long long n, int cap) {
 }
 
 void launch_adj_bc(cudaStream_t s, const Geo &g, double *lu, double *lv, double *lw, double *linlet) {
-  const BcTable t = flowpassing_table();
+  const BcTable t = flowpassing_table(g.walls);
   // reverse of the forward phase order x, y, z
   k_adj_bc_z<<<grid_for((long long)g.nxc * g.nyc, 1024), kBlock, 0, s>>>(g, t, lu, lv, lw);
   k_adj_bc_y<<<grid_for((long long)g.nxc * g.nzc, 1024), kBlock, 0, s>>>(g, t, lu, lv, lw);

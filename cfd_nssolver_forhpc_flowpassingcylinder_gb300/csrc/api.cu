@@ -335,6 +335,8 @@ int validate(const cfdgb_config *c) {
   if (c->grid < 0 || c->grid > 1) return fail(CFDGB_EINVAL, "unknown grid %d", c->grid);
   if (c->scheme < CFDGB_QUICK || c->scheme > CFDGB_UD) return fail(CFDGB_EINVAL, "unknown scheme %d", c->scheme);
   if (c->les != 0 && c->les != 1) return fail(CFDGB_EINVAL, "les must be 0 or 1");
+  if (c->walls != CFDGB_WALLS_ZERO_GRADIENT && c->walls != CFDGB_WALLS_FREE_SLIP)
+    return fail(CFDGB_EINVAL, "unknown walls %d", c->walls);
   if (c->grid == CFDGB_GRID_SML) {
     // unit_SML's own conditions (structureGrid.hpp:269,283): 100 fine cells in x (shifted 4
     // cells) and in y, an even number of coarse ones on both sides
@@ -780,6 +782,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   cudaMemcpy(c->tab32, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
   Geo &g = c->g;
   g.nxc = cfg->nx; g.nyc = cfg->ny; g.nzc = cfg->nz;
+  g.walls = cfg->walls;
   g.nx = nx; g.ny = ny; g.nz = nz;
   g.sx = (long long)ny * nz; g.sy = nz;
   g.ncell = c->ncell;

@@ -42,6 +42,7 @@ struct Geo {
   // index; SPE_sparseMatrix.hpp:52-58) and jpv, the Jacobi scale of every row
   int nonuni;
   const double *fxm, *fxp, *fym, *fyp, *fzm, *fzp, *jpv;
+  int walls;  // a cfdgb_walls value (the boundary table's y-wall rows)
 };
 
 // compact row -> padded (i,j,k)
@@ -195,16 +196,18 @@ struct StepScal {
 
 // Dir/Num boundary table of inc/BoundaryCondition/FLOWpassing.hpp:6-40 as
 // dir[face][component], num[face][component]; faces 0..5 = x-, x+, y-, y+, z-, z+.
-// Face 0 is the inlet (u = 1, reflected v and w); every other face is zero-gradient.
+// Face 0 is the inlet (u = 1, reflected v and w); every other face is zero-gradient, or,
+// with free-slip walls (the rows left commented out at :14-21), v = 0 on faces 2 and 3.
 struct BcTable {
   double dir[6][3], num[6][3];
 };
-inline BcTable flowpassing_table() {
+inline BcTable flowpassing_table(int walls) {
   BcTable t{};
   for (int f = 0; f < 6; ++f)
     for (int c = 0; c < 3; ++c) { t.dir[f][c] = 0.0; t.num[f][c] = 1.0; }
   t.dir[0][0] = 1.0;
   t.num[0][0] = t.num[0][1] = t.num[0][2] = 0.0;
+  if (walls == CFDGB_WALLS_FREE_SLIP) t.num[2][1] = t.num[3][1] = 0.0;
   return t;
 }
 

@@ -577,7 +577,7 @@ void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, d
 }
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
                double *vs, double *ws, int do_main, const double *inlet) {
-  const BcTable t = flowpassing_table();
+  const BcTable t = flowpassing_table(g.walls);
   auto blocks = [](long long n) { return (int)((n + kBlock - 1) / kBlock < 1024 ? (n + kBlock - 1) / kBlock : 1024); };
   k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, inlet, u, v, w, p, us, vs, ws, do_main);
   k_bc_y<<<blocks((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);

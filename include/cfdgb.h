@@ -61,6 +61,13 @@ typedef enum cfdgb_grid {
                               uniform; FP64 BiCGSTAB solvers; nx even > 108, ny even > 100 */
 } cfdgb_grid;
 
+/* The y-wall rows of the reference's boundary table (inc/BoundaryCondition/FLOWpassing.hpp). */
+typedef enum cfdgb_walls {
+  CFDGB_WALLS_ZERO_GRADIENT = 0,  /* the active rows (:23-29): u, v, w zero-gradient (default) */
+  CFDGB_WALLS_FREE_SLIP = 1       /* the rows left commented out there (:14-21): v = 0 on the
+                                     walls, u and w zero-gradient */
+} cfdgb_walls;
+
 /* The reference's compile-time convection switch (inc/0_General.hpp:114-118). */
 typedef enum cfdgb_scheme {
   CFDGB_QUICK = 0,  /* QuickUnitA/B (Convection_Difussion.hpp:20-90), the default */
@@ -98,6 +105,7 @@ typedef struct cfdgb_config {
   int les;                   /* 1: Smagorinsky eddy viscosity (TERBULENCE_SMAGORINSKY,
                                 inc/source/SmagorinskyModel.hpp:30, CS = 0.18) added to nu,
                                 from T0 before each convection-diffusion; 0: off (default) */
+  int walls;                 /* a cfdgb_walls value; default zero-gradient */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {

@@ -14,7 +14,10 @@ its own compile.  This recipe
    ``:38-40`` (nxCal, nyCal, nzCal) and ``inc/dfib/setEta.hpp:145`` (center_x);
    puts the convection switch ``#define CONVECTION_DIFUSSION_QUICK``
    (``inc/0_General.hpp:114``) under ``#ifndef ORACLE_SCHEME_SET`` so that a build can
-   name LUD or UD; and corrects the one misspelt token (``auot``) that keeps the
+   name LUD or UD; turns the v entries of the y-wall rows of the boundary table
+   (``inc/BoundaryCondition/FLOWpassing.hpp:25,29``) into a macro, so that a build can
+   take the free-slip rows the reference leaves commented out (``:14-21``); and corrects
+   the one misspelt token (``auot``) that keeps the
    Smagorinsky model (``inc/source/SmagorinskyModel.hpp:61``) from compiling, for the
    builds that switch it on.  Every other line is the reference's own,
 3. compiles ``oracle/ref_harness.cpp`` (our driver, which calls the reference's own
@@ -68,6 +71,14 @@ PATCHES = [
     ("inc/0_General.hpp",
      "\n#define CONVECTION_DIFUSSION_QUICK\n",
      "\n#ifndef ORACLE_SCHEME_SET\n#define CONVECTION_DIFUSSION_QUICK\n#endif\n"),
+    # the y-wall rows of the boundary table: v zero-gradient (active) or, for the builds
+    # with the free-slip rows the reference leaves commented out, Dirichlet 0
+    ("inc/BoundaryCondition/FLOWpassing.hpp",
+     "Dir[2][1] = 0.;/* 2 */Num[2][1] = 1.;",
+     "Dir[2][1] = 0.;/* 2 */Num[2][1] = ORACLE_WALL_NUM_V;"),
+    ("inc/BoundaryCondition/FLOWpassing.hpp",
+     "Dir[3][1] = 0.;/* 3 */Num[3][1] = 1.;",
+     "Dir[3][1] = 0.;/* 3 */Num[3][1] = ORACLE_WALL_NUM_V;"),
     # the Smagorinsky model does not compile as published (a misspelt `auto`); this one
     # token is the whole fix, and it only matters to builds with TERBULENCE_SMAGORINSKY
     ("inc/source/SmagorinskyModel.hpp",
@@ -116,25 +127,27 @@ SCHEMES = {"quick": "CONVECTION_DIFUSSION_QUICK", "lud": "CONVECTION_DIFUSSION_L
 
 
 def binary_name(nx: int, ny: int, nz: int, flavour: str, gridder: str = "uniform", scheme: str = "quick",
-                les: bool = False) -> Path:
+                les: bool = False, walls: str = "zero_gradient") -> Path:
     tag = "" if gridder == "uniform" else f"_{gridder}"
     tag += "" if scheme == "quick" else f"_{scheme}"
     tag += "_les" if les else ""
+    tag += "" if walls == "zero_gradient" else "_freeslip"
     return BIN / f"ref_{nx}x{ny}x{nz}{tag}_{flavour}"
 
 
 def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
           flavour: str = "parity", force: bool = False, gridder: str = "uniform", scheme: str = "quick",
-          les: bool = False) -> Path:
+          les: bool = False, walls: str = "zero_gradient") -> Path:
     """Compile the harness for one grid; returns the binary path.  gridder: "uniform" or
     "sml" (the reference's own default, non_uniform-SML); scheme: "quick", "lud" or "ud"
-    (the convection switch); les: TERBULENCE_SMAGORINSKY."""
+    (the convection switch); les: TERBULENCE_SMAGORINSKY; walls: "zero_gradient" (the
+    active boundary rows) or "free_slip" (the rows left commented out)."""
     src = stage_sources()
     BIN.mkdir(parents=True, exist_ok=True)
-    exe = binary_name(nx, ny, nz, flavour, gridder, scheme, les)
+    exe = binary_name(nx, ny, nz, flavour, gridder, scheme, les, walls)
     # the domain is part of the name only through a sidecar, so check it too
     sidecar = exe.with_suffix(".cfg")
-    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r} {gridder} {scheme} {int(les)}\n"
+    cfg = f"{nx} {ny} {nz} {lx!r} {ly!r} {lz!r} {cx!r} {gridder} {scheme} {int(les)} {walls}\n"
     harness = HERE / "ref_harness.cpp"
     if (exe.exists() and not force and sidecar.exists() and sidecar.read_text() == cfg
             and exe.stat().st_mtime >= harness.stat().st_mtime):
@@ -152,6 +165,7 @@ def build(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float, cx: float,
         defs += ["-DORACLE_SCHEME_SET", f"-D{SCHEMES[scheme]}"]
     if les:
         defs += ["-DTERBULENCE_SMAGORINSKY"]
+    defs += [f"-DORACLE_WALL_NUM_V={'0.' if walls == 'free_slip' else '1.'}"]
     cmd = (["g++", "-std=c++17", "-w"] + flags + defs +
            ["-I", str(src / "inc"), str(harness), "-o", str(exe)])
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -340,62 +340,70 @@ static const double kDir[6][3] = {{1, 0, 0}, {0, 0, 0}, {0, 0, 0},
 static const double kNum[6][3] = {{0, 0, 0}, {1, 1, 1}, {1, 1, 1},
                                   {1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
 
+/* the Num rows with the grid's choice of y walls (free slip: v Dirichlet 0 on faces 2, 3) */
+static void num_table(const og_grid *g, double N[6][3]) {
+  memcpy(N, kNum, sizeof(kNum));
+  if (g->walls == OG_WALLS_FREE_SLIP) N[2][1] = N[3][1] = 0.0;
+}
+
 /* inc/BoundaryCondition/Boundary_Condition.hpp:37-176 (BC_staggered_main), in the
  * order one thread executes it: faces 0..5 for u,v,w, then pressure. */
 static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet) {
+  double kN[6][3];
+  num_table(g, kN);
   const int nx = g->nx, ny = g->ny, nz = g->nz;
   double *vel[3] = {u, v, w};
   for (int j = GC; j < ny - GC; ++j)
     for (int k = GC; k < nz - GC; ++k) { /* BC_0 */
       const double din = inlet ? inlet[(j - GC) * g->nzc + (k - GC)] : kDir[0][0];
-      u[IC(g, 1, j, k)] = u[IC(g, 0, j, k)] = din + kNum[0][0] * u[IC(g, 2, j, k)];
+      u[IC(g, 1, j, k)] = u[IC(g, 0, j, k)] = din + kN[0][0] * u[IC(g, 2, j, k)];
       v[IC(g, 1, j, k)] = v[IC(g, 0, j, k)] =
-          kDir[0][1] * 2. + (2.0 * kNum[0][1] - 1.0) * v[IC(g, 2, j, k)];
+          kDir[0][1] * 2. + (2.0 * kN[0][1] - 1.0) * v[IC(g, 2, j, k)];
       w[IC(g, 1, j, k)] = w[IC(g, 0, j, k)] =
-          kDir[0][2] * 2. + (2.0 * kNum[0][2] - 1.0) * w[IC(g, 2, j, k)];
+          kDir[0][2] * 2. + (2.0 * kN[0][2] - 1.0) * w[IC(g, 2, j, k)];
     }
   for (int j = GC; j < ny - GC; ++j)
     for (int k = GC; k < nz - GC; ++k) { /* BC_1 */
       u[IC(g, nx - 1, j, k)] = u[IC(g, nx - 2, j, k)] = u[IC(g, nx - 3, j, k)] =
-          kDir[1][0] + kNum[1][0] * u[IC(g, nx - 4, j, k)];
+          kDir[1][0] + kN[1][0] * u[IC(g, nx - 4, j, k)];
       v[IC(g, nx - 1, j, k)] = v[IC(g, nx - 2, j, k)] =
-          kDir[1][1] * 2. + (2.0 * kNum[1][1] - 1.0) * v[IC(g, nx - 3, j, k)];
+          kDir[1][1] * 2. + (2.0 * kN[1][1] - 1.0) * v[IC(g, nx - 3, j, k)];
       w[IC(g, nx - 1, j, k)] = w[IC(g, nx - 2, j, k)] =
-          kDir[1][2] * 2. + (2.0 * kNum[1][2] - 1.0) * w[IC(g, nx - 3, j, k)];
+          kDir[1][2] * 2. + (2.0 * kN[1][2] - 1.0) * w[IC(g, nx - 3, j, k)];
     }
   for (int i = GC; i < nx - GC; ++i)
     for (int k = GC; k < nz - GC; ++k) { /* BC_2 */
       u[IC(g, i, 1, k)] = u[IC(g, i, 0, k)] =
-          kDir[2][0] * 2. + (2.0 * kNum[2][0] - 1.0) * u[IC(g, i, 2, k)];
-      v[IC(g, i, 1, k)] = v[IC(g, i, 0, k)] = kDir[2][1] + kNum[2][1] * v[IC(g, i, 2, k)];
+          kDir[2][0] * 2. + (2.0 * kN[2][0] - 1.0) * u[IC(g, i, 2, k)];
+      v[IC(g, i, 1, k)] = v[IC(g, i, 0, k)] = kDir[2][1] + kN[2][1] * v[IC(g, i, 2, k)];
       w[IC(g, i, 1, k)] = w[IC(g, i, 0, k)] =
-          kDir[2][2] * 2. + (2.0 * kNum[2][2] - 1.0) * w[IC(g, i, 2, k)];
+          kDir[2][2] * 2. + (2.0 * kN[2][2] - 1.0) * w[IC(g, i, 2, k)];
     }
   for (int i = GC; i < nx - GC; ++i)
     for (int k = GC; k < nz - GC; ++k) { /* BC_3 */
       v[IC(g, i, ny - 1, k)] = v[IC(g, i, ny - 2, k)] = v[IC(g, i, ny - 3, k)] =
-          kDir[3][1] + kNum[3][1] * v[IC(g, i, ny - 4, k)];
+          kDir[3][1] + kN[3][1] * v[IC(g, i, ny - 4, k)];
       u[IC(g, i, ny - 1, k)] = u[IC(g, i, ny - 2, k)] =
-          kDir[3][0] * 2. + (2.0 * kNum[3][0] - 1.0) * u[IC(g, i, ny - 3, k)];
+          kDir[3][0] * 2. + (2.0 * kN[3][0] - 1.0) * u[IC(g, i, ny - 3, k)];
       w[IC(g, i, ny - 1, k)] = w[IC(g, i, ny - 2, k)] =
-          kDir[3][2] * 2. + (2.0 * kNum[3][2] - 1.0) * w[IC(g, i, ny - 3, k)];
+          kDir[3][2] * 2. + (2.0 * kN[3][2] - 1.0) * w[IC(g, i, ny - 3, k)];
     }
   for (int i = GC; i < nx - GC; ++i)
     for (int j = GC; j < ny - GC; ++j) { /* BC_4 */
       u[IC(g, i, j, 1)] = u[IC(g, i, j, 0)] =
-          kDir[4][0] * 2. + (2.0 * kNum[4][0] - 1.0) * u[IC(g, i, j, 2)];
+          kDir[4][0] * 2. + (2.0 * kN[4][0] - 1.0) * u[IC(g, i, j, 2)];
       v[IC(g, i, j, 1)] = v[IC(g, i, j, 0)] =
-          kDir[4][1] * 2. + (2.0 * kNum[4][1] - 1.0) * v[IC(g, i, j, 2)];
-      w[IC(g, i, j, 1)] = w[IC(g, i, j, 0)] = kDir[4][2] + kNum[4][2] * w[IC(g, i, j, 2)];
+          kDir[4][1] * 2. + (2.0 * kN[4][1] - 1.0) * v[IC(g, i, j, 2)];
+      w[IC(g, i, j, 1)] = w[IC(g, i, j, 0)] = kDir[4][2] + kN[4][2] * w[IC(g, i, j, 2)];
     }
   for (int i = GC; i < nx - GC; ++i)
     for (int j = GC; j < ny - GC; ++j) { /* BC_5 */
       w[IC(g, i, j, nz - 1)] = w[IC(g, i, j, nz - 2)] = w[IC(g, i, j, nz - 3)] =
-          kDir[5][2] + kNum[5][2] * w[IC(g, i, j, nz - 4)];
+          kDir[5][2] + kN[5][2] * w[IC(g, i, j, nz - 4)];
       u[IC(g, i, j, nz - 1)] = u[IC(g, i, j, nz - 2)] =
-          kDir[5][0] * 2. + (2.0 * kNum[5][0] - 1.0) * u[IC(g, i, j, nz - 3)];
+          kDir[5][0] * 2. + (2.0 * kN[5][0] - 1.0) * u[IC(g, i, j, nz - 3)];
       v[IC(g, i, j, nz - 1)] = v[IC(g, i, j, nz - 2)] =
-          kDir[5][1] * 2. + (2.0 * kNum[5][1] - 1.0) * v[IC(g, i, j, nz - 3)];
+          kDir[5][1] * 2. + (2.0 * kN[5][1] - 1.0) * v[IC(g, i, j, nz - 3)];
     }
   (void)vel;
   /* pressure: homogeneous Neumann, :148-172 */

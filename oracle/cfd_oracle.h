@@ -26,7 +26,12 @@ typedef struct og_grid {
   double *Dxs, *Dys, *Dzs;     /* centre spacings */
   int scheme;                  /* convection scheme: OG_SCHEME_* (0 after init: QUICK) */
   int les;                     /* != 0: Smagorinsky eddy viscosity in og_run_ex */
+  int walls;                   /* y walls: OG_WALLS_* (0 after init: zero-gradient) */
 } og_grid;
+
+/* the y-wall rows of the Dir/Num table (inc/BoundaryCondition/FLOWpassing.hpp): the active
+ * zero-gradient rows (:23-29) or the free-slip rows left commented out there (:14-21) */
+enum { OG_WALLS_ZERO_GRADIENT = 0, OG_WALLS_FREE_SLIP = 1 };
 
 /* the reference's compile-time convection switch, inc/0_General.hpp:114-118 */
 enum { OG_SCHEME_QUICK = 0, OG_SCHEME_LUD = 1, OG_SCHEME_UD = 2 };

@@ -41,11 +41,13 @@ class _Grid(C.Structure):
                 ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)] + [
         (n, C.POINTER(C.c_double)) for n in
         ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")] + [
-        ("scheme", C.c_int), ("les", C.c_int)]
+        ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int)]
 
 
 # the reference's compile-time convection switch (0_General.hpp:114-118)
 SCHEMES = {"quick": 0, "lud": 1, "ud": 2}
+# the y-wall rows of its boundary table (FLOWpassing.hpp: active, and the commented-out ones)
+WALLS = {"zero_gradient": 0, "free_slip": 1}
 
 
 class _Bicg(C.Structure):
@@ -99,10 +101,10 @@ class Grid:
     """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
 
     def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform", scheme="quick",
-                 les=False):
+                 les=False, walls="zero_gradient"):
         """gridder: "uniform" (init_uniform) or "sml" (the reference's default stretched
         non_uniform-SML grid); scheme: "quick", "lud" or "ud" (the convection switch);
-        les: the Smagorinsky eddy viscosity in run()."""
+        les: the Smagorinsky eddy viscosity in run(); walls: the y walls' boundary rows."""
         self._g = _Grid()
         init = {"uniform": lib().og_grid_init_uniform, "sml": lib().og_grid_init_sml}[gridder]
         rc = init(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx, ly / 2.0, radius)
@@ -110,6 +112,7 @@ class Grid:
             raise ValueError("grid too small")
         self._g.scheme = SCHEMES[scheme]
         self._g.les = 1 if les else 0
+        self._g.walls = WALLS[walls]
         self.shape = (nxc + 4, nyc + 4, nzc + 4)
         self.cells = nxc * nyc * nzc
 

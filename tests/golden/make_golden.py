@@ -13,9 +13,11 @@ Fixtures written next to this file:
                     reader (QfileRead) makes of the .q file
   unit_<grid>_variants.npz
                     ConvectionDifussion of the same fields with the LUD scheme and with
-                    the Smagorinsky model (its eddy viscosity too)
+                    the Smagorinsky model (its eddy viscosity too); the ghost fill and copy
+                    with the free-slip wall rows of the boundary table
   run_<case>.npz    whole runs of the 96x48x4 flow-past-cylinder case (reference BCs,
-                    Re 100, dt 0.005; also with LUD and with the Smagorinsky model) and of
+                    Re 100, dt 0.005; also with LUD, with the Smagorinsky model and with
+                    free-slip walls) and of
                     the stretched SML grid: interior of the final u, v, w, p and the
                     per-step iterations, residual, Cd and Cl.
 """
@@ -93,7 +95,7 @@ def make_unit(name, spec):
 # builds of the reference with its other convection scheme (LUD) and with its Smagorinsky
 # model switched on; UD does not compile as published (the uniform-grid variant's UdUnit
 # calls, Convection_Difussion.uniformGrid.hpp:143-144, match no overload)
-VARIANTS = {"lud": dict(scheme="lud"), "les": dict(les=True)}
+VARIANTS = {"lud": dict(scheme="lud"), "les": dict(les=True), "freeslip": dict(walls="free_slip")}
 
 
 def make_unit_variants(name, spec):
@@ -112,6 +114,10 @@ def make_unit_variants(name, spec):
             arrs = _load_dir(Path(td))
         for k in ("in_u", "in_v", "in_w"):  # the same seeded inputs as the QUICK fixture
             assert np.array_equal(arrs[k], base[k]), k
+        if tag == "freeslip":  # the boundary rows change the ghost fill only
+            for k in ("bc_u", "bc_v", "bc_w", "bc_p", "bcc_u", "bcc_v", "bcc_w"):
+                out[f"{tag}_{k}"] = arrs[k]
+            continue
         for c in ("u", "v", "w"):
             out[f"cd_{tag}_{c}"] = arrs[f"cd_{c}"]
         if "les_nut" in arrs:
@@ -124,13 +130,16 @@ VARIANT_RUNS = {
     # name: (steps, Re, dt, tol, solver, omega, scheme, les)
     "c1_lud_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8, "lud", False),
     "c1_les_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8, "quick", True),
+    "c1_freeslip_spe_tol1e-13_20": (20, 100.0, 0.005, 1e-13, "spe", 1.8, "quick", False, "free_slip"),
 }
 
 
-def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p"), scheme="quick", les=False):
+def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p"), scheme="quick", les=False,
+             walls="zero_gradient"):
     nxc, nyc, nzc, lx, ly, lz, cx = grid
     steps, Re, dt, tol, solver, omega = spec
-    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", gridder=gridder, scheme=scheme, les=les)
+    exe = build_ref.build(nxc, nyc, nzc, lx, ly, lz, cx, "parity", gridder=gridder, scheme=scheme, les=les,
+                          walls=walls)
     with tempfile.TemporaryDirectory() as td:
         subprocess.run([str(exe), "run", str(steps), repr(Re), repr(dt), repr(tol), solver,
                         repr(omega), "0", "0", td], check=True, env=_env(),
@@ -141,7 +150,7 @@ def make_run(name, spec, grid=C1, gridder="uniform", keep=("u", "v", "w", "p"), 
         stats = np.loadtxt(Path(td) / "stats.txt")
     meta = np.array([nxc, nyc, nzc, lx, ly, lz, cx, steps, Re, dt, tol, omega], dtype=np.float64)
     np.savez_compressed(HERE / f"run_{name}.npz", meta=meta, solver=np.array(solver),
-                        scheme=np.array(scheme), les=np.array(int(les)),
+                        scheme=np.array(scheme), les=np.array(int(les)), walls=np.array(walls),
                         iters=stats[:, 2].astype(np.int64), err=stats[:, 3], cd=stats[:, 4],
                         cl=stats[:, 5], **fields)
 
@@ -158,7 +167,7 @@ def main():
         make_run(n, s[:6], grid=SML, gridder="sml", keep=s[6])
         print("run", n)
     for n, s in VARIANT_RUNS.items():
-        make_run(n, s[:6], scheme=s[6], les=s[7])
+        make_run(n, s[:6], scheme=s[6], les=s[7], walls=s[8] if len(s) > 8 else "zero_gradient")
         print("run", n)
 
 

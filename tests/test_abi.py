@@ -43,12 +43,12 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
     assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 5
-    assert cfg.scheme == cg.QUICK and cfg.les == 0
+    assert cfg.scheme == cg.QUICK and cfg.les == 0 and cfg.walls == cg.WALLS_ZERO_GRADIENT
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
                                          ("precision", 3), ("tol", 0.0), ("maxit", 0), ("scheme", 3),
-                                         ("scheme", -1), ("les", 2)])
+                                         ("scheme", -1), ("les", 2), ("walls", 2)])
 def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     cfg = cg.default_config()
     setattr(cfg, field, value)

@@ -116,3 +116,24 @@ def test_backward_is_repeatable(adj):
     g_in2, g_eta2 = s.backward()
     np.testing.assert_allclose(g_in2, g_in, rtol=1e-7, atol=1e-9 * np.abs(g_in).max())
     np.testing.assert_allclose(g_eta2, g_eta, rtol=1e-7, atol=1e-9 * np.abs(g_eta).max())
+
+
+def test_free_slip_walls_gradients_match_central_fd():
+    """With the free-slip wall rows of the boundary table the adjoint's transposed ghost
+    fill takes the same table: one inlet and one eta direction against central FD."""
+    s = cg.Solver(tol=TOL, project_rhs=PROJECT, walls="free_slip", **CASE)
+    try:
+        eta0 = s.get_eta()
+        _J(s, eta=eta0)
+        g_in, g_eta = s.backward()
+        rng = np.random.default_rng(11)
+        d = rng.standard_normal(g_in.shape)
+        fd = _fd(s, np.ones(g_in.shape), eta0, d_in=d)
+        assert abs(float(np.sum(g_in * d)) - fd) <= 1e-4 * abs(fd) + 1e-9
+        band = (eta0 > 0) & (eta0 < 1)
+        band[:2] = band[-2:] = False
+        de = np.where(band, rng.standard_normal(eta0.shape), 0.0)
+        fd = _fd(s, None, eta0, d_eta=de)
+        assert abs(float(np.sum(g_eta * de)) - fd) <= 1e-4 * abs(fd) + 1e-9
+    finally:
+        s.close()

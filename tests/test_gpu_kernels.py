@@ -74,6 +74,26 @@ def test_lud_ud_and_smagorinsky_kernels(name):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("name", UNITS)
+def test_free_slip_walls_bit_exact(name):
+    """The free-slip y-wall rows of the boundary table (FLOWpassing.hpp:14-21): ghost fill
+    and copy bit-exact against the reference built with them."""
+    from conftest import load_golden
+    z = load_golden(name)
+    zv = load_golden(name.replace(".npz", "_variants.npz"))
+    meta = z["meta"]
+    with _solver_for(meta, walls="free_slip") as s:
+        P = {k: z[k].reshape(s.shape).copy() for k in ("in_u", "in_v", "in_w", "in_p", "in_us", "in_vs", "in_ws")}
+        u, v, w, p = P["in_u"], P["in_v"], P["in_w"], P["in_p"]
+        s.bc_main(u, v, w, p)
+        for a, k in ((u, "bc_u"), (v, "bc_v"), (w, "bc_w"), (p, "bc_p")):
+            np.testing.assert_array_equal(a.ravel(), zv["freeslip_" + k])
+        us, vs, ws = P["in_us"], P["in_vs"], P["in_ws"]
+        s.bc_copy(u, v, w, us, vs, ws)
+        for a, k in ((us, "bcc_u"), (vs, "bcc_v"), (ws, "bcc_w")):
+            np.testing.assert_array_equal(a.ravel(), zv["freeslip_" + k])
+
+
 def test_bc_main_and_copy_bit_exact(unit):
     z, s, P = unit
     u, v, w, p = (P[k].copy() for k in ("in_u", "in_v", "in_w", "in_p"))

@@ -64,10 +64,12 @@ def test_fp64_step_matches_reference_tight(case, solver, golden):
 
 
 @pytest.mark.parametrize("case,kw", [("c1_lud_spe_tol1e-13_20", dict(scheme="lud")),
-                                     ("c1_les_spe_tol1e-13_20", dict(les=True))])
+                                     ("c1_les_spe_tol1e-13_20", dict(les=True)),
+                                     ("c1_freeslip_spe_tol1e-13_20", dict(walls="free_slip"))])
 def test_scheme_and_smagorinsky_runs_match_reference(case, kw, golden):
-    """20 steps with the reference's LUD scheme and with its Smagorinsky model, against the
-    reference built with those switched on: the same 1e-10 bar as the QUICK runs."""
+    """20 steps with the reference's LUD scheme, with its Smagorinsky model and with its
+    free-slip wall rows, against the reference built with each: the same 1e-10 bar as the
+    QUICK runs."""
     z = golden(f"run_{case}.npz")
     steps, tol = int(z["meta"][7]), z["meta"][10]
     with _c1(tol=tol, **kw) as s:

@@ -59,6 +59,25 @@ def test_lud_and_smagorinsky_bit_exact(name, golden):
         np.testing.assert_array_equal(a.ravel(), zv["cd_les_" + c])
 
 
+@pytest.mark.parametrize("name", UNITS)
+def test_free_slip_walls_bit_exact(name, golden):
+    """The free-slip rows of the boundary table (FLOWpassing.hpp:14-21, commented out in the
+    reference; a build of the reference with them): BC_staggered_main and the copy."""
+    z = golden(name)
+    zv = golden(name.replace(".npz", "_variants.npz"))
+    meta = z["meta"]
+    g = O.Grid(int(meta[0]), int(meta[1]), int(meta[2]), *meta[3:7], walls="free_slip")
+    P = {k: z[k].reshape(g.shape).copy() for k in ("in_u", "in_v", "in_w", "in_p", "in_us", "in_vs", "in_ws")}
+    u, v, w, p = P["in_u"], P["in_v"], P["in_w"], P["in_p"]
+    O.bc_main(g, u, v, w, p)
+    for a, k in ((u, "bc_u"), (v, "bc_v"), (w, "bc_w"), (p, "bc_p")):
+        np.testing.assert_array_equal(a.ravel(), zv["freeslip_" + k])
+    us, vs, ws = P["in_us"], P["in_vs"], P["in_ws"]
+    O.bc_copy(g, u, v, w, us, vs, ws)
+    for a, k in ((us, "bcc_u"), (vs, "bcc_v"), (ws, "bcc_w")):
+        np.testing.assert_array_equal(a.ravel(), zv["freeslip_" + k])
+
+
 def test_upwind_scheme_is_the_upwind_cell():
     """UD (UdUnit, Convection_Difussion.hpp:150): no reference build compiles it, so its
     restatement is checked by its definition: every face value is the upwind cell's, so a
@@ -146,14 +165,17 @@ def test_sor_bit_exact(unit):
 
 @pytest.mark.parametrize("case", ["c1_spe_tol1e-13_20", "c1_csr_tol1e-13_20",
                                   "c1_sor_tol1e-3_4", "c1_spe_tol1e-8_200",
-                                  "c1_lud_spe_tol1e-13_20", "c1_les_spe_tol1e-13_20"])
+                                  "c1_lud_spe_tol1e-13_20", "c1_les_spe_tol1e-13_20",
+                                  "c1_freeslip_spe_tol1e-13_20"])
 def test_whole_run_bit_exact(case, golden):
     z = golden(f"run_{case}.npz")
     m = z["meta"]
     nxc, nyc, nzc = (int(x) for x in m[:3])
     extra = {}
-    if "scheme" in z:  # runs of the reference built with LUD or its Smagorinsky model
+    if "scheme" in z:  # runs of the reference built with LUD, its Smagorinsky model or free slip
         extra = dict(scheme=str(z["scheme"]), les=bool(z["les"]))
+        if "walls" in z:
+            extra["walls"] = str(z["walls"])
     g = O.Grid(nxc, nyc, nzc, *m[3:7], **extra)
     steps, Re, dt, tol, omega = int(m[7]), m[8], m[9], m[10], m[11]
     r = O.run(g, steps, Re, dt, tol, str(z["solver"]), omega)
