@@ -25,10 +25,20 @@
 //     (inc/dfib/setEta.hpp:136)
 //   CD_CL(simu, Lo, Dfib, gA)                               returned by update_UandF_omp / runSeqOmp stats
 //     (inc/dfib/virtualForceIntergrator.hpp:92)
+//   SmagorinskyModel(ShareM, simu, TX, t1, Lo, gridA)       cfdgb::SmagorinskyModel(ctx, TX)
+//     (inc/source/SmagorinskyModel.hpp:30)
+//   get_Cfl(T1, Lo, gA, simu)                               cfdgb::get_Cfl(ctx, T1)
+//     (inc/analyses/cfl.hpp:3)
+//   OutputPLOT3D_Qfile / OutputPlot3D_Xfile                 cfdgb::OutputPLOT3D_Qfile / OutputPlot3D_Xfile
+//     (inc/io/Plot3D/qfile.hpp:6, xfileWrite.hpp:6)         (files of the context's current state)
+//   QfileRead(gA, filename)                                 cfdgb::QfileRead(ctx, filename)
+//     (inc/io/Plot3D/qfileRead.hpp:6)
 #pragma once
 
+#include <cstdio>
 #include <initializer_list>
 #include <stdexcept>
+#include <tuple>
 #include <string>
 #include <utility>
 #include <vector>
@@ -39,6 +49,7 @@ namespace cfdgb {
 
 struct velocity {  // inc/0_0_PhisicalVaribal.hpp:5
   std::vector<double> u, v, w;
+  std::vector<double> Viseff;  // Smagorinsky eddy viscosity per compact cell (:11)
 };
 struct pressure {  // :75
   std::vector<double> p;
@@ -162,6 +173,53 @@ inline bool update_UandF_omp(Context &c, DfibArray &Dfib, const pressure &t1, co
 inline void DFIB_CylinderZ(Context &c, DfibArray &Dfib) {
   Dfib.eta.resize(c.iceltot());
   check(cfdgb_op_solid_fraction(c.handle(), Dfib.eta.data()));
+}
+
+// TX.Viseff = the Smagorinsky eddy viscosity of TX (the context need not have les on).
+inline void SmagorinskyModel(Context &c, velocity &TX) {
+  for (auto *a : {&TX.u, &TX.v, &TX.w}) need(c, *a, c.iceltot(), "TX");
+  TX.Viseff.resize(c.iceltotCal());
+  check(cfdgb_op_smagorinsky(c.handle(), TX.u.data(), TX.v.data(), TX.w.data(), TX.Viseff.data()));
+}
+
+// get_Cfl's outputs (simu.cfl_max, U_max, U_min) for u* = T1.
+struct Cfl {
+  double cfl_max, U_max[3], U_min[3];
+};
+inline Cfl get_Cfl(Context &c, const velocity &T1) {
+  for (auto *a : {&T1.u, &T1.v, &T1.w}) need(c, *a, c.iceltot(), "T1");
+  double o[7];
+  check(cfdgb_op_cfl(c.handle(), T1.u.data(), T1.v.data(), T1.w.data(), o));
+  return {o[0], {o[1], o[2], o[3]}, {o[4], o[5], o[6]}};
+}
+
+// The reference's Plot3D writers, for the context's current state.
+inline void OutputPLOT3D_Qfile(Context &c, double time, const std::string &path) {
+  check(cfdgb_write_plot3d(c.handle(), nullptr, path.c_str(), time));
+}
+inline void OutputPlot3D_Xfile(Context &c, const std::string &path) {
+  check(cfdgb_write_plot3d(c.handle(), path.c_str(), nullptr, 0.0));
+}
+
+// QfileRead: (Nblock, mach, alpha, reyn, time, p, u, v, w, eta), the fields padded as the
+// reference returns them (zero outside the interior).  Throws if the file is not a Plot3D
+// solution of the context's grid.
+inline auto QfileRead(Context &c, const std::string &path) {
+  const auto &g = c.config();
+  const size_t n = c.iceltotCal();
+  std::FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) throw std::invalid_argument("cfdgb: cannot open " + path);
+  int ih[4] = {0, 0, 0, 0};
+  float fh[4] = {0, 0, 0, 0};
+  std::vector<float> q(5 * n);
+  const bool ok = std::fread(ih, sizeof(int), 4, f) == 4 && std::fread(fh, sizeof(float), 4, f) == 4 &&
+                  ih[1] == g.nx && ih[2] == g.ny && ih[3] == g.nz && std::fread(q.data(), sizeof(float), 5 * n, f) == 5 * n;
+  std::fclose(f);
+  if (!ok) throw std::invalid_argument("cfdgb: " + path + " is not a Plot3D solution of this grid");
+  std::vector<double> p(c.iceltot()), u(c.iceltot()), v(c.iceltot()), w(c.iceltot()), eta(c.iceltot());
+  check(cfdgb_op_plot3d_read(c.handle(), q.data(), p.data(), u.data(), v.data(), w.data(), eta.data()));
+  return std::make_tuple(ih[0], fh[0], fh[1], fh[2], fh[3], std::move(p), std::move(u), std::move(v), std::move(w),
+                         std::move(eta));
 }
 
 // The time loop of runSeqOmp (src/RUN_CPU.cpp:257-436) on the device: T0/t1 in as the
