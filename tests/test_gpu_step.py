@@ -315,3 +315,29 @@ def test_every_fp32_kernel_family_reaches_the_fp64_solution(env, solver, monkeyp
         assert all(r.relres < 1e-8 for r in sa[1:]), [r.relres for r in sa]
         for k, e in vel_err(fa, fb).items():
             assert e <= 1e-6, (env, case, k, e)
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 3), (5, 4, 3), (7, 5, 9), (12, 6, 13)])
+def test_small_and_ragged_grids(shape):
+    """The smallest grid the ABI accepts and ragged ones (nz odd, no multiple of 4): three
+    FP64 steps against the oracle, and CG and both MIXED solvers to the FP64 tolerance.
+    The body fills much of these domains, and with the reference's zero-gradient outflow
+    their Neumann problems are inconsistent (the reference's own BiCGSTAB runs to its cap,
+    and on 7x5x9 diverges), so both sides project the right-hand side."""
+    nx, ny, nz = shape
+    dom = dict(nx=nx, ny=ny, nz=nz, lx=float(nx), ly=float(ny), lz=float(nz), cx=nx / 2.0, cy=ny / 2.0, radius=0.75,
+               project_rhs=1)
+    g = O.Grid(nx, ny, nz, float(nx), float(ny), float(nz), nx / 2.0, radius=0.75)
+    ref = O.run(g, 3, 100.0, 0.005, 1e-12, "spe", project=True)
+    with _c1(tol=1e-12, **dom) as s:
+        s.init_fields()
+        st = s.step(3)
+        f = s.get_fields()
+    np.testing.assert_allclose([r.cd for r in st], ref["cd"], rtol=1e-9, atol=1e-12)
+    for k, e in vel_err(f, ref).items():
+        assert e <= 1e-10, (shape, k, e)
+    for solver, prec in (("cg", "fp64"), ("bicgstab", "mixed"), ("cg", "mixed")):
+        with _c1(solver=solver, precision=prec, tol=1e-8, **dom) as s:
+            s.init_fields()
+            st = s.step(3)
+        assert all(r.status == 0 and r.relres < 1e-8 for r in st[1:]), (shape, solver, prec, st)
