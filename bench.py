@@ -45,7 +45,40 @@ WORKLOADS = {
     "c4": dict(nx=256, ny=128, nz=32, lx=24.0, ly=12.0, lz=2.0, cx=6.0, cy=6.0, Re=100.0, dt=0.004),
     # combined stress case (113M cells)
     "c5": dict(nx=1536, ny=768, nz=96, lx=48.0, ly=24.0, lz=3.0, cx=12.0, cy=12.0, Re=300.0, dt=0.001),
+    # the reference's own default case (src/CFD_MX.cpp:23-27, structureGrid.hpp:20-40,
+    # setEta.hpp:145, 0_1_SimulationVariable.hpp:61): its stretched SML grid of 190x210x40,
+    # SPE BiCGSTAB to its default 1e-3
+    "ref": dict(nx=190, ny=210, nz=40, lx=17.0, ly=12.0, lz=3.0, cx=6.5, cy=6.0, Re=40.0, dt=0.002, grid="sml",
+                solver="bicgstab", tol=1e-3),
 }
+
+
+def workload(wl):
+    """(Solver keyword arguments of the case, the solver of its FP64 run, its tolerance)."""
+    cfg = dict(WORKLOADS[wl])
+    return cfg, cfg.pop("solver", "jacobi"), cfg.pop("tol", TOL)
+
+
+def l2_note(wl):
+    """The state a step reads (11 padded FP64 fields, ~10 compact FP64 vectors) against L2."""
+    cfg, _, _ = workload(wl)
+    pad = (cfg["nx"] + 4) * (cfg["ny"] + 4) * (cfg["nz"] + 4)
+    gb = (11 * pad + 10 * cfg["nx"] * cfg["ny"] * cfg["nz"]) * 8 / 1e9
+    return f"state ~{gb:.2g} GB > 129 MB L2 each step, no flush"
+
+
+def config_of(wl):
+    cfg, solver, tol = workload(wl)
+    return {"workload": wl, **cfg, "solver": {"jacobi": "jacobi_bicgstab", "bicgstab": "spe_bicgstab"}[solver],
+            "tol": tol}
+
+
+def metric(wl):
+    _, solver, tol = workload(wl)
+    if (solver, tol) == ("jacobi", TOL):
+        return METRIC
+    name = {"jacobi": "Jacobi-BiCGSTAB", "bicgstab": "SPE-BiCGSTAB"}[solver]
+    return f"cell-steps/s @resid {tol:g} (FP64 {name} projection step)"
 
 
 TOL = 1e-8
@@ -204,8 +237,9 @@ def _timed_steps(s, steps, dist, torch):
 
 
 def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True, keep_fields=False):
-    cfg = dict(WORKLOADS[wl])
-    with cg.Solver(solver=solver, precision=precision, tol=TOL, maxit=maxit, **cfg) as s:
+    """solver None: the case's own FP64 solver; the case's tolerance throughout."""
+    cfg, wsolver, tol = workload(wl)
+    with cg.Solver(solver=solver or wsolver, precision=precision, tol=tol, maxit=maxit, **cfg) as s:
         s.init_fields()
         s.step(warmup, allow_noconv=True)
         s.reset_counters()
@@ -230,8 +264,8 @@ def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, 
 def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
     """The public API with HOST buffers: per step, H2D of u,v,w,p from pinned memory,
     one step, D2H of u,v,w,p; all on the library's stream inside the events."""
-    cfg = dict(WORKLOADS[wl])
-    with cg.Solver(solver=solver, precision=precision, tol=TOL, **cfg) as s:
+    cfg, wsolver, tol = workload(wl)
+    with cg.Solver(solver=solver or wsolver, precision=precision, tol=tol, **cfg) as s:
         s.init_fields()
         s.step(warmup)
         host = {k: torch.empty(s.shape, dtype=torch.float64, pin_memory=True).numpy() for k in "uvwp"}
@@ -368,18 +402,26 @@ def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file)
     return r, share
 
 
+def reference_build(wl, flavour="native"):
+    """The reference's own build for a case and the harness's name of its solver."""
+    from oracle import build_ref
+    cfg, solver, tol = workload(wl)
+    exe = build_ref.build(cfg["nx"], cfg["ny"], cfg["nz"], cfg["lx"], cfg["ly"], cfg["lz"], cfg["cx"], flavour,
+                          gridder=cfg.get("grid", "uniform"))
+    return exe, {"jacobi": "csr", "bicgstab": "spe"}[solver], tol
+
+
 def cpu_reference_sample(wl, steps, cap, threads, iters_per_step):
     """Run the reference's own build (oracle/_ref) for `steps` steps with its BiCGSTAB
     capped at `cap` iterations; derive its time per iteration and per non-solve step
-    part, and from those its cell-steps/s at the iteration counts a full solve to 1e-8
-    needs (iters_per_step: list, one per step)."""
-    from oracle import build_ref
+    part, and from those its cell-steps/s at the iteration counts a full solve to the
+    case's tolerance needs (iters_per_step: list, one per step)."""
     cfg = WORKLOADS[wl]
-    exe = build_ref.build(cfg["nx"], cfg["ny"], cfg["nz"], cfg["lx"], cfg["ly"], cfg["lz"], cfg["cx"], "native")
+    exe, hsolver, tol = reference_build(wl)
     with tempfile.TemporaryDirectory() as td:
         env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="close", OMP_PLACES="cores")
         t0 = time.perf_counter()
-        subprocess.run([str(exe), "run", str(steps), repr(cfg["Re"]), repr(cfg["dt"]), repr(TOL), "csr", "1.7",
+        subprocess.run([str(exe), "run", str(steps), repr(cfg["Re"]), repr(cfg["dt"]), repr(tol), hsolver, "1.7",
                         "0", "0", td, str(cap)], check=True, env=env, cwd=td, stdout=subprocess.DEVNULL,
                        stderr=subprocess.DEVNULL)
         wall = time.perf_counter() - t0
@@ -425,12 +467,11 @@ def main_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "no recorded reference iteration counts"}))
         return 0
     r = cpu_reference_sample(args.workload, min(steps, 3), args.cap, threads, iters)
-    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "cell-steps/s",
+    line = {"impl": "reference", "metric": metric(args.workload), "value": r["value"], "unit": "cell-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * r["cells"] / r["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state)",
-            "config": {"workload": args.workload, **WORKLOADS[args.workload], "solver": "jacobi_bicgstab",
-                       "tol": TOL},
+            "config": config_of(args.workload),
             "cpu_baseline": {"value": r["value"], "unit": "cell-steps/s", "cores": threads, "kind": "reference",
                              "sample": SAMPLE_DOC.format(cap=args.cap, t_iter=r["t_iter_s"], t_other=r["t_other_s"])},
             "e2e": {"value": r["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -482,7 +523,7 @@ def main(argv=None):
 
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
-        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64", maxit=args.maxit,
+        fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64", maxit=args.maxit,
                         keep_fields=bool(modes & {"mixed", "cg", "mixed_cg"}))
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
@@ -490,12 +531,12 @@ def main(argv=None):
     roof, share = roofline(fp64["kernels"], cells, 8, "64", hbm_peak, peak_kind, traffic_file)
     iters64 = [r.iters for r in fp64["stats"]]
     line = {
-        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": dist.world, "steps": args.steps,
+        "metric": metric(wl), "value": value, "unit": "cell-steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t64 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state u=1, v=w=0)",
-        "config": {"workload": wl, **WORKLOADS[wl], "solver": "jacobi_bicgstab", "tol": TOL, "maxit": args.maxit,
+        "config": {**config_of(wl), "maxit": args.maxit,
                    "bc": "reference (FLOWpassing table)", "parallelism": f"replicas x{dist.world}",
-                   "l2": "inputs ~1.5 GB > 129 MB L2, no flush"},
+                   "l2": l2_note(wl)},
         "iters_per_step": iters64, "relres": max(r.relres for r in fp64["stats"]),
         "gpu_launches": fp64["launches"], "roofline": roof, "kernel_share": share,
         "alu_roofline": alu_roofline(fp64["kernels"], cells, fp_peak), "fp_peaks": fp_peak,
@@ -542,7 +583,7 @@ def main(argv=None):
                          "omega": 1.7, "sweeps_per_step": [r.iters for r in sr["stats"]],
                          "relres": [r.relres for r in sr["stats"]], "status": [r.status for r in sr["stats"]]}
     if "e2e" in modes:
-        ms, nbytes, _ = e2e_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "fp64")
+        ms, nbytes, _ = e2e_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64")
         te = dist.max(ms)
         line["e2e"] = {"value": cells * args.steps * dist.world / (te / 1e3), "unit": "cell-steps/s",
                        "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
