@@ -822,10 +822,19 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.fym = g.fxp + cfg->nx; g.fyp = g.fym + cfg->ny;
     g.fzm = g.fyp + cfg->ny; g.fzp = g.fzm + cfg->nz;
     g.jpv = djp;
+    double *rows = nullptr;
+    if ((rc = dalloc(c, &rows, 14 * (size_t)c->ncell))) return bail(rc);
+    g.cof[0] = rows;
+    g.cof[1] = rows + 7 * c->ncell;
   }
-  // solver launch geometry: k along x (up to a warp), j along y, i strided over grid z
+  // solver launch geometry: k along x (up to a warp), j along y, i strided over grid z.
+  // From 8 k cells up, the width among 8, 16, 32 that leaves the fewest idle lanes at
+  // the end of a k line (40 cells: 8 wide, where 32 would idle 24 of every 64 lanes)
   g.lbx = 1;
   while (g.lbx < cfg->nz && g.lbx < 32) g.lbx *= 2;
+  auto idle = [](int n, int w) { return (n + w - 1) / w * w - n; };
+  for (int w = 16; w >= 8 && cfg->nz >= 8; w /= 2)
+    if (idle(cfg->nz, w) < idle(cfg->nz, g.lbx)) g.lbx = w;
   g.lby = kBlock / g.lbx;
   g.lgx = (cfg->nz + g.lbx - 1) / g.lbx;
   g.lgy = (cfg->ny + g.lby - 1) / g.lby;
@@ -854,6 +863,11 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
       g.tgy2 = std::max(1, std::min(cfg->nx, c->nsm * tbps2 / g.tgx));
       nblk3 = std::max(nblk3, g.tgx * std::max(g.tgy, g.tgy2));
     }
+  }
+  if (g.nonuni) {  // the stored rows, from the same per-axis factors and jpv
+    launch_build_rows(c->stream, g, 0, const_cast<double *>(g.cof[0]));
+    launch_build_rows(c->stream, g, 1, const_cast<double *>(g.cof[1]));
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(fail(CFDGB_ECUDA, "stretched-grid rows"));
   }
   // fields and solver vectors
   double **pad[] = {&c->u, &c->v, &c->w, &c->us, &c->vs, &c->ws, &c->ui, &c->vi, &c->wi, &c->p, &c->eta};

@@ -42,6 +42,10 @@ struct Geo {
   // index; SPE_sparseMatrix.hpp:52-58) and jpv, the Jacobi scale of every row
   int nonuni;
   const double *fxm, *fxp, *fym, *fyp, *fzm, *fzp, *jpv;
+  // the same rows stored once per context, [7][ncell] (column q of row r at q*ncell + r),
+  // cof[0] the SPE rows and cof[1] the Jacobi-scaled CSR rows: built by nonuni_row, so the
+  // solver kernels read the bits they would otherwise recompute at every application
+  const double *cof[2];
   int walls;  // a cfdgb_walls value (the boundary table's y-wall rows)
 };
 
@@ -134,17 +138,16 @@ __device__ __forceinline__ T stencil_row(const Stencil<T> &st, const T *__restri
 __device__ __forceinline__ double stencil_row_g(const Geo &g, const Stencil<double> &st, const double *__restrict__ x,
                                                 long long row, int ic, int jc, int kc) {
   if (!g.nonuni) return stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
-  double c[8];
-  nonuni_row(g, st.jac, ic, jc, kc, row, c);
-  const long long nyz = (long long)g.nyc * g.nzc;
+  const double *__restrict__ c = g.cof[st.jac] + row;
+  const long long n = g.ncell, nyz = (long long)g.nyc * g.nzc;
   double sum = 0.0;
   if (ic > 0) sum += c[0] * x[row - nyz];
-  if (jc > 0) sum += c[1] * x[row - g.nzc];
-  if (kc > 0) sum += c[2] * x[row - 1];
-  sum += c[3] * x[row];
-  if (kc < g.nzc - 1) sum += c[4] * x[row + 1];
-  if (jc < g.nyc - 1) sum += c[5] * x[row + g.nzc];
-  if (ic < g.nxc - 1) sum += c[6] * x[row + nyz];
+  if (jc > 0) sum += c[n] * x[row - g.nzc];
+  if (kc > 0) sum += c[2 * n] * x[row - 1];
+  sum += c[3 * n] * x[row];
+  if (kc < g.nzc - 1) sum += c[4 * n] * x[row + 1];
+  if (jc < g.nyc - 1) sum += c[5 * n] * x[row + g.nzc];
+  if (ic < g.nxc - 1) sum += c[6 * n] * x[row + nyz];
   return sum;
 }
 // jp of a row (the Jacobi scale): class table or the stretched grid's per-row vector

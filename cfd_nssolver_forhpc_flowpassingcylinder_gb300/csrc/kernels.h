@@ -49,6 +49,8 @@ struct KrylovVecs {
   T *xb;  // FP32 BiCGSTAB sweep: the best iterate kept so far (unused elsewhere)
 };
 
+// stretched grid: store the SPE (jac 0) or Jacobi-scaled CSR (jac 1) rows into out[7][ncell]
+void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out);
 // FP64 BiCGSTAB (bicgstabRe2) set-up: r0 = b - A x, r1 = p1 = r0, history px2 <- px1 <- x
 void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st,
                          KrylovVecs<double> v, const double *b, double *px1, double *px2, double *part,

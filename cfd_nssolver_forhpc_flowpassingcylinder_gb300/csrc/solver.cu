@@ -40,18 +40,18 @@ __device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, i
                                            long long row, F &&f, T &center) {
   const long long nyz = (long long)g.nyc * g.nzc;
   if constexpr (sizeof(T) == sizeof(double)) {
-    if (g.nonuni) {  // stretched grid (FP64 solvers only): coefficients in registers
-      double cs[8];
-      nonuni_row(g, st.jac, ic, jc, kc, row, cs);
+    if (g.nonuni) {  // stretched grid (FP64 solvers only): the rows stored per context
+      const double *__restrict__ cs = g.cof[st.jac] + row;
+      const long long n = g.ncell;
       T sum = T(0);
       if (ic > 0) sum += cs[0] * f(row - nyz);
-      if (jc > 0) sum += cs[1] * f(row - g.nzc);
-      if (kc > 0) sum += cs[2] * f(row - 1);
+      if (jc > 0) sum += cs[n] * f(row - g.nzc);
+      if (kc > 0) sum += cs[2 * n] * f(row - 1);
       center = f(row);
-      sum += cs[3] * center;
-      if (kc < g.nzc - 1) sum += cs[4] * f(row + 1);
-      if (jc < g.nyc - 1) sum += cs[5] * f(row + g.nzc);
-      if (ic < g.nxc - 1) sum += cs[6] * f(row + nyz);
+      sum += cs[3 * n] * center;
+      if (kc < g.nzc - 1) sum += cs[4 * n] * f(row + 1);
+      if (jc < g.nyc - 1) sum += cs[5 * n] * f(row + g.nzc);
+      if (ic < g.nxc - 1) sum += cs[6 * n] * f(row + nyz);
       return sum;
     }
   }
@@ -1380,6 +1380,21 @@ static inline Vec32 v32(const KrylovVecs<float> &v, float *const p2[2], float *c
   o.p[0] = p2[0]; o.p[1] = p2[1]; o.ap[0] = ap2[0]; o.ap[1] = ap2[1];
   o.xb = v.xb;
   return o;
+}
+
+// the stretched grid's rows, [7][ncell]: every column of nonuni_row, zeros included
+__global__ void __launch_bounds__(kBlock) k_build_rows(Geo g, int jac, double *__restrict__ out) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    double c[8];
+    nonuni_row(g, jac, ic, jc, kc, row, c);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) out[q * g.ncell + row] = c[q];
+  }
+}
+
+void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out) {
+  k_build_rows<<<cgrid(g), cblock(g), 0, s>>>(g, jac, out);
 }
 
 void launch_bicg_setup64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
