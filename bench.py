@@ -97,6 +97,13 @@ KERNEL_WORDS = {
     "bicg_pap32": 6,   # read r1, p, ap, r0; write p', ap'
     "bicg_sas32": 4,   # read r1, ap; write s, as
     "bicg_xr32": 7,    # read x, p, s, as, r0; write x, r1
+    # FP32 iteration right-preconditioned by the multigrid V-cycle: five kernels, 21 words
+    # per cell beside the two V-cycles (~17 words each over all levels, timed as mg_vcycle)
+    "bicgp_p32": 4,    # read r1, p, v; write p
+    "bicgp_v32": 3,    # read ph, r0; write v
+    "bicgp_s32": 3,    # read r1, v; write s
+    "bicgp_t32": 3,    # read sh, s; write t
+    "bicgp_xr32": 8,   # read x, ph, sh, s, t, r0; write x, r1
     # CG (the reference's cg.hpp method): FP64 three kernels, 11 words; FP32 sweeps two, 10
     "cg_q64": 2,       # read p; write q
     "cg_xr64": 6,      # read x, p, r, q; write x, r
@@ -236,10 +243,12 @@ def _timed_steps(s, steps, dist, torch):
     return e0.elapsed_time(e1), stats
 
 
-def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True, keep_fields=False):
+def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True, keep_fields=False,
+             precond="none"):
     """solver None: the case's own FP64 solver; the case's tolerance throughout."""
     cfg, wsolver, tol = workload(wl)
-    with cg.Solver(solver=solver or wsolver, precision=precision, tol=tol, maxit=maxit, **cfg) as s:
+    with cg.Solver(solver=solver or wsolver, precision=precision, tol=tol, maxit=maxit, precond=precond,
+                   **cfg) as s:
         s.init_fields()
         s.step(warmup, allow_noconv=True)
         s.reset_counters()
@@ -493,7 +502,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cfdgb", choices=["cfdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--modes", default="fp64,mixed,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
+    ap.add_argument("--modes", default="fp64,mixed,mixed_mg,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--adj-workload", default="c4", choices=sorted(WORKLOADS))
@@ -524,7 +533,7 @@ def main(argv=None):
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
         fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64", maxit=args.maxit,
-                        keep_fields=bool(modes & {"mixed", "cg", "mixed_cg"}))
+                        keep_fields=bool(modes & {"mixed", "mixed_mg", "cg", "mixed_cg"}))
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
     value = cells * args.steps * dist.world / (t64 / 1e3)
@@ -557,6 +566,21 @@ def main(argv=None):
                              "roofline": r32, "kernel_share": share32}
         except cg.CfdgbError as e:
             line["mixed"] = {"value": None, "error": str(e)}
+    if "mixed_mg" in modes:
+        try:
+            mg = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", maxit=args.maxit,
+                          keep_fields=True, precond="multigrid")
+            tm = dist.max(mg["ms"])
+            rg, shg = roofline(mg["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
+            line["mixed_mg"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
+                                "solver": "jacobi bicgstab, FP32 sweeps right-preconditioned by a multigrid V-cycle",
+                                "iters_per_step": [r.iters for r in mg["stats"]],
+                                "outer_per_step": [r.outer for r in mg["stats"]],
+                                "relres": max(r.relres for r in mg["stats"]), "speedup_vs_fp64": t64 / tm,
+                                "error_vs_fp64": field_errors(mg, fp64), "gpu_launches": mg["launches"],
+                                "device_mem_gb": mg["device_mem_gb"], "roofline": rg, "kernel_share": shg}
+        except cg.CfdgbError as e:
+            line["mixed_mg"] = {"value": None, "error": str(e)}
     for key, solver, prec in (("cg", "cg", "fp64"), ("mixed_cg", "cg", "mixed")):
         if key not in modes:
             continue

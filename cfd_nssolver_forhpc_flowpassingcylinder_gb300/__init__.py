@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 5  # CFDGB_ABI_VERSION
+ABI_VERSION = 6  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -30,6 +30,8 @@ QUICK, LUD, UD = 0, 1, 2
 SCHEMES = {"quick": QUICK, "lud": LUD, "ud": UD}
 WALLS_ZERO_GRADIENT, WALLS_FREE_SLIP = 0, 1
 WALLS = {"zero_gradient": WALLS_ZERO_GRADIENT, "free_slip": WALLS_FREE_SLIP}
+PRECOND_NONE, PRECOND_MULTIGRID = 0, 1
+PRECONDS = {"none": PRECOND_NONE, "multigrid": PRECOND_MULTIGRID}
 
 
 class CfdgbError(RuntimeError):
@@ -48,7 +50,8 @@ class Config(C.Structure):
                 ("tol", C.c_double), ("maxit", C.c_int), ("omega", C.c_double),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
-                ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int)]
+                ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int),
+                ("precond", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -158,6 +161,8 @@ def default_config(**kw) -> Config:
             v = SCHEMES[v]
         if k == "walls" and isinstance(v, str):
             v = WALLS[v]
+        if k == "precond" and isinstance(v, str):
+            v = PRECONDS[v]
         if k == "les":
             v = int(bool(v))
         setattr(cfg, k, v)

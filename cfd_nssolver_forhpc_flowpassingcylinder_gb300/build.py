@@ -25,7 +25,7 @@ PER_FILE = {
     # the adjoint re-derives the forward branch decisions with the same arithmetic
     "adjoint.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
 }
-SOURCES = ["api.cu", "step_exact.cu", "step_fast.cu", "solver.cu", "adjoint.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "step_exact.cu", "step_fast.cu", "solver.cu", "multigrid.cu", "adjoint.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -59,13 +59,15 @@ uint64_t splitmix64(uint64_t &s) {
 enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
-  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_LES, K_COUNT
+  K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_LES,
+  K_PP32, K_MG, K_PV32, K_PS32, K_PT32, K_PXR32, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
-    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl", "smagorinsky"};
+    "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl", "smagorinsky",
+    "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32"};
 
 struct PendingEv {
   int id;
@@ -93,6 +95,11 @@ struct cfdgb_ctx {
   KrylovVecs<double> k64{};
   KrylovVecs<float> k32{};
   float *p32[2] = {nullptr, nullptr}, *ap32[2] = {nullptr, nullptr};  // FP32 double buffers
+  // multigrid preconditioner of the FP32 BiCGSTAB sweeps: levels and the two
+  // preconditioned vectors M p, M s
+  bool use_mg = false;
+  MgPlan mg{};
+  float *ph32 = nullptr, *sh32 = nullptr;
   double *part = nullptr;
   SolverScal *sc = nullptr, *sc32 = nullptr;
   StepScal *ss = nullptr;
@@ -337,6 +344,17 @@ int validate(const cfdgb_config *c) {
   if (c->les != 0 && c->les != 1) return fail(CFDGB_EINVAL, "les must be 0 or 1");
   if (c->walls != CFDGB_WALLS_ZERO_GRADIENT && c->walls != CFDGB_WALLS_FREE_SLIP)
     return fail(CFDGB_EINVAL, "unknown walls %d", c->walls);
+  if (c->precond != CFDGB_PRECOND_NONE && c->precond != CFDGB_PRECOND_MULTIGRID)
+    return fail(CFDGB_EINVAL, "unknown precond %d", c->precond);
+  if (c->precond == CFDGB_PRECOND_MULTIGRID) {
+    if (c->precision != CFDGB_MIXED || (c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI) ||
+        c->grid != CFDGB_GRID_UNIFORM)
+      return fail(CFDGB_EINVAL, "the multigrid preconditioner is for the MIXED BiCGSTAB solvers on a uniform grid");
+    MgPlan mg;
+    if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, &mg))
+      return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
+                  c->ny, c->nz, kMgSharedCells);
+  }
   if (c->grid == CFDGB_GRID_SML) {
     // unit_SML's own conditions (structureGrid.hpp:269,283): 100 fine cells in x (shifted 4
     // cells) and in y, an even number of coarse ones on both sides
@@ -351,16 +369,41 @@ int validate(const cfdgb_config *c) {
 }
 
 // The kernels of one Krylov iteration: BiCGSTAB 5 (FP64) / 3 (FP32), CG 3 / 2.
+// The multigrid-preconditioned FP32 iteration: p, M p, v = A M p, s, M s, t = A M s, x/r
+constexpr int kPrecParts = 7;
+const int kPrecKid[kPrecParts] = {K_PP32, K_MG, K_PV32, K_PS32, K_MG, K_PT32, K_PXR32};
+
 int iter_kernels(const cfdgb_ctx *c, bool fp32) {
+  if (fp32 && c->use_mg) return kPrecParts;
   if (c->cfg.solver == CFDGB_CG) return fp32 ? 2 : 3;
   return fp32 ? 3 : 5;
 }
 int iter_kid(const cfdgb_ctx *c, bool fp32, int part) {
+  if (fp32 && c->use_mg) return kPrecKid[part];
   if (c->cfg.solver == CFDGB_CG) return (fp32 ? K_CGPQ32 : K_CGQ64) + part;
   return (fp32 ? K_PAP32 : K_AP64) + part;
 }
+// kernels one part launches (a V-cycle is many)
+int iter_part_launches(const cfdgb_ctx *c, bool fp32, int part) {
+  return iter_kid(c, fp32, part) == K_MG ? mg_vcycle_launches(c->mg) : 1;
+}
+// iterations per captured chunk: the preconditioned iteration is long and needs few
+int chunk_iters(const cfdgb_ctx *c, bool fp32) { return fp32 && c->use_mg ? 2 : c->chunk_len; }
 void launch_iter_kernel(cfdgb_ctx *c, bool fp32, int part) {
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  if (fp32 && c->use_mg) {
+    PrecVecs v{c->k32.x, c->k32.r0, c->k32.r1, c->p32[0], c->ap32[0], c->k32.s, c->k32.as, c->ph32, c->sh32,
+               c->k32.xb};
+    const int jf = jac ? 1 : 0;
+    switch (part) {
+      case 1: launch_mg_vcycle(c->stream, c->mg, jf, v.p, v.ph, c->sc32); break;
+      case 4: launch_mg_vcycle(c->stream, c->mg, jf, v.s, v.sh, c->sc32); break;
+      default:
+        launch_bicgp32_part(c->stream, part == 0 ? 0 : part == 2 ? 1 : part == 3 ? 2 : part == 5 ? 3 : 4, c->g,
+                            jac ? c->jac32 : c->spe32, v, c->part, c->sc32);
+    }
+    return;
+  }
   if (c->cfg.solver == CFDGB_CG) {
     if (fp32)
       launch_cg32_part(c->stream, part, c->g, c->spe32, c->k32, c->p32, c->ap32, c->part, c->sc32);
@@ -376,7 +419,7 @@ void launch_iter_kernel(cfdgb_ctx *c, bool fp32, int part) {
 int capture_chunk(cfdgb_ctx *c, bool fp32) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  for (int m = 0; m < c->chunk_len; ++m)
+  for (int m = 0; m < chunk_iters(c, fp32); ++m)
     for (int part = 0; part < iter_kernels(c, fp32); ++part) launch_iter_kernel(c, fp32, part);
   CK(cudaStreamEndCapture(c->stream, &graph));
   cudaGraphExec_t exec;
@@ -406,16 +449,20 @@ int set_solver_params(cfdgb_ctx *c, SolverScal *dsc, double tol, int maxit) {
 int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   SolverScal *dsc = fp32 ? c->sc32 : c->sc;
   if (!c->timing && !(fp32 ? c->chunk32 : c->chunk64)) TRY(capture_chunk(c, fp32));
-  const long long max_chunks = (long long)c->cfg.maxit / c->chunk_len + 3;
+  const int len = chunk_iters(c, fp32);
+  const long long max_chunks = (long long)c->cfg.maxit / len + 3;
   const int nk = iter_kernels(c, fp32);
   for (long long q = 0; q < max_chunks; ++q) {
     if (c->timing) {
-      for (int m = 0; m < c->chunk_len; ++m)
+      for (int m = 0; m < len; ++m)
         for (int part = 0; part < nk; ++part)
-          L(c, iter_kid(c, fp32, part), 1, [&] { launch_iter_kernel(c, fp32, part); });
+          L(c, iter_kid(c, fp32, part), iter_part_launches(c, fp32, part), [&] { launch_iter_kernel(c, fp32, part); });
     } else {
-      c->launches += (long long)nk * c->chunk_len;
-      for (int part = 0; part < nk; ++part) c->kn[iter_kid(c, fp32, part)] += c->chunk_len;
+      for (int part = 0; part < nk; ++part) {
+        const int n = iter_part_launches(c, fp32, part);
+        c->launches += (long long)n * len;
+        c->kn[iter_kid(c, fp32, part)] += (long long)n * len;
+      }
       CK(cudaGraphLaunch(fp32 ? c->chunk32 : c->chunk64, c->stream));
     }
     CK(cudaMemcpyAsync(c->h_sc, dsc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
@@ -441,8 +488,11 @@ int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
 // (0.3); CG has no such breakdown and gains from long sweeps (iterations per solve on
 // 512x256x64: 0.3 ~4000, 1e-3 ~2400 in 3 refinements, 3e-4 ~2250 in 3; on 1024x512x128
 // 3e-4 saves the fourth refinement that 1e-3 needs, and 1e-4 restarts no less often).
+// The multigrid-preconditioned sweep converges in a few dozen iterations, far too few for
+// the FP32 recursion to drift, and runs 1e-3 deep.
 double sweep_reduction(const cfdgb_ctx *c) {
   if (c->cfg.inner_tol > 0.0) return c->cfg.inner_tol;
+  if (c->use_mg) return 1e-3;
   return c->cfg.solver == CFDGB_CG ? 3e-4 : 0.3;
 }
 
@@ -888,6 +938,16 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
                     &c->ap32[0], &c->ap32[1], &c->k32.xb};
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
+  }
+  if (cfg->precond == CFDGB_PRECOND_MULTIGRID) {  // levels >= 1 and the vectors M p, M s
+    mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm, &c->mg);
+    if ((rc = dalloc(c, &c->ph32, c->ncell)) || (rc = dalloc(c, &c->sh32, c->ncell))) return bail(rc);
+    for (int l = 1; l < c->mg.nlev; ++l) {
+      MgLevel &L = c->mg.lev[l];
+      const size_t n = (size_t)L.nx * L.ny * L.nz;
+      if ((rc = dalloc(c, &L.x, n)) || (rc = dalloc(c, &L.b, n))) return bail(rc);
+    }
+    c->use_mg = true;
   }
   if ((rc = dalloc(c, &c->part, 8 * (size_t)std::max(c->nblk, nblk3)))) return bail(rc);
   if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc32, 1)) || (rc = dalloc(c, &c->ss, 1))) return bail(rc);

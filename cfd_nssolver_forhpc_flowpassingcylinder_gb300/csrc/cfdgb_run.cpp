@@ -9,7 +9,9 @@
 //              every N steps, byte-compatible with the reference's writers]
 //             [scheme=quick|lud|ud: the convection switch (inc/0_General.hpp:114-118);
 //              les=1: the Smagorinsky model (TERBULENCE_SMAGORINSKY);
-//              walls=free_slip: the free-slip y-wall rows of the boundary table]
+//              walls=free_slip: the free-slip y-wall rows of the boundary table;
+//              precond=multigrid: the FP32 multigrid V-cycle preconditioning the MIXED
+//              BiCGSTAB sweeps]
 //             [restart=<file.q>: start from a Plot3D solution file of this grid (QfileRead,
 //              the restart the reference leaves commented out at src/RUN_CPU.cpp:88-99);
 //              the simulated time continues from the file's header]
@@ -52,6 +54,7 @@ int main(int argc, char **argv) {
   cfg.scheme = scheme == "lud" ? CFDGB_LUD : scheme == "ud" ? CFDGB_UD : CFDGB_QUICK;
   cfg.les = (int)num("les", 0.0);
   cfg.walls = (kv.count("walls") && kv["walls"] == "free_slip") ? CFDGB_WALLS_FREE_SLIP : CFDGB_WALLS_ZERO_GRADIENT;
+  cfg.precond = (kv.count("precond") && kv["precond"] == "multigrid") ? CFDGB_PRECOND_MULTIGRID : CFDGB_PRECOND_NONE;
   const std::string solver = kv.count("solver") ? kv["solver"] : "bicgstab";
   cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI
                : solver == "rbsor"  ? CFDGB_RBSOR

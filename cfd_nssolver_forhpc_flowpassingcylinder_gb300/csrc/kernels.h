@@ -111,6 +111,47 @@ void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, doub
 void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
                         StepScal *ss);
 
+// ---- multigrid.cu: geometric multigrid V-cycle, the preconditioner of the FP32 sweep ----
+// Level 0 is the Poisson grid; each coarser level halves every even extent (cell-centred
+// agglomeration of two cells per halved axis) until at most kMgCoarseCells cells remain
+// or no extent is even.  Operator on every level: the unscaled 7-point Neumann Laplacian
+// of that level's spacing (1/h^2 per axis), the uniform-grid SPE rows rediscretised.
+constexpr int kMgMaxLevels = 16;
+constexpr int kMgCoarseCells = 64;      // coarsening stops at or below this many cells
+constexpr int kMgSharedCells = 4096;    // largest coarsest level solved in one block
+struct MgLevel {
+  int nx, ny, nz;          // cells
+  float wx, wy, wz;        // 1/h^2 per axis
+  int fx, fy, fz;          // cells of this level per cell of the next one, per axis (1, 2)
+  float *x, *b;            // correction and right-hand side (levels >= 1)
+  int bx, by, gx, gy, gz;  // launch geometry: bx along k, by along j, gz planes strided over i
+};
+struct MgPlan {
+  int nlev;
+  int coarse_sweeps;  // red-black sweeps of the coarsest solve
+  MgLevel lev[kMgMaxLevels];
+};
+// levels of an nx x ny x nz grid with spacing hx, hy, hz (arrays left null); false when
+// the grid has a single level too large for the one-block coarsest solve
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, MgPlan *mg);
+// kernels one V-cycle launches
+int mg_vcycle_launches(const MgPlan &mg);
+// x0 = M b0, one V(1,1) cycle: red-black Gauss-Seidel smoothing from a zero start,
+// averaging restriction, cell-centred trilinear prolongation, a one-block red-black solve
+// on the coarsest level.  jacobi: b0 holds Jacobi-scaled rows (jp = 1/diag), so M applies
+// to diag * b0.  Every kernel returns at once when sc->done is set.
+void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float *b0, float *x0, const SolverScal *sc);
+
+// FP32 BiCGSTAB with a right preconditioner M (the V-cycle), kernel `part` 0..4:
+// 0 p = r1 + beta (p - omega v) (or r1 on restart, r0 = r1); 1 v = A ph, alpha;
+// 2 s = r1 - alpha v; 3 t = A sh, omega; 4 x += alpha ph + omega sh, r1 = s - omega t,
+// stop test and beta.  ph = M p and sh = M s come from the V-cycles between them.
+struct PrecVecs {
+  float *x, *r0, *r1, *p, *v, *s, *t, *ph, *sh, *xb;
+};
+void launch_bicgp32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, PrecVecs v,
+                         double *part_buf, SolverScal *sc);
+
 // red-black SOR on the same operator (FP64)
 void launch_rbsor_sweep(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *b,
                         double *x, double omega);

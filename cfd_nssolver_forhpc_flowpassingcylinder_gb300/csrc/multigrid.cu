@@ -1,0 +1,234 @@
+// Geometric multigrid V-cycle in FP32: the preconditioner of the FP32 BiCGSTAB sweep
+// inside the FP64 refinement (the reference has no multigrid; its Poisson operator on a
+// uniform grid is the 7-point Neumann Laplacian of SPE_sparseMatrix.hpp:42-85, which every
+// level here rediscretises at its own spacing).
+//
+// Cell-centred hierarchy: a coarse cell is the union of 2 cells along each halved axis.
+// Restriction averages the fine residual over a coarse cell's children; prolongation is
+// the cell-centred trilinear interpolation (weights 3/4 and 1/4 per halved axis, the
+// parent's value standing in for a neighbour beyond a Neumann wall); the smoother is
+// red-black Gauss-Seidel, one sweep before and one after the coarse correction; the
+// coarsest level (at most kMgSharedCells cells) is solved by red-black sweeps in the
+// shared memory of one block.  The V-cycle is a fixed linear map, as a right
+// preconditioner of BiCGSTAB requires.  Every kernel is pointwise or a stencil over one
+// level and reads sc->done first, so a captured chunk of iterations idles once the sweep
+// has stopped.
+#include <algorithm>
+
+#include "cfdgb_internal.cuh"
+#include "kernels.h"
+
+namespace cfdgb {
+
+#define FOR_LEVEL(L)                                   \
+  const int k = blockIdx.x * blockDim.x + threadIdx.x; \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y; \
+  const bool on_ = (k < (L).nz) && (j < (L).ny);       \
+  for (int i = blockIdx.z; on_ && i < (L).nx; i += gridDim.z)
+
+__device__ __forceinline__ long long lrow(const MgLevel &L, int i, int j, int k) {
+  return ((long long)i * L.ny + j) * L.nz + k;
+}
+
+// diagonal of a Neumann row: the weights of the neighbours that exist
+__device__ __forceinline__ float ldiag(const MgLevel &L, int i, int j, int k) {
+  return L.wx * (float)((i > 0) + (i < L.nx - 1)) + L.wy * (float)((j > 0) + (j < L.ny - 1)) +
+         L.wz * (float)((k > 0) + (k < L.nz - 1));
+}
+
+// weighted sum of the neighbours' values (minus the off-diagonal part of the row)
+__device__ __forceinline__ float lnb(const MgLevel &L, const float *x, int i, int j, int k, long long r) {
+  const long long sx = (long long)L.ny * L.nz;
+  float a = 0.f, b = 0.f, c = 0.f;
+  if (i > 0) a += x[r - sx];
+  if (i < L.nx - 1) a += x[r + sx];
+  if (j > 0) b += x[r - L.nz];
+  if (j < L.ny - 1) b += x[r + L.nz];
+  if (k > 0) c += x[r - 1];
+  if (k < L.nz - 1) c += x[r + 1];
+  return L.wx * a + L.wy * b + L.wz * c;
+}
+
+// One colour of a red-black Gauss-Seidel sweep (colour = (i + j + k) & 1).  zero: x starts
+// at zero, so the cells of this colour take b / diag and the others are set to zero.
+// bscale: b holds Jacobi-scaled rows (b / diag), which are unscaled first.
+__global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, int colour, int zero, int bscale,
+                                                      const float *__restrict__ b, float *x, const SolverScal *sc) {
+  if (sc->done) return;
+  FOR_LEVEL(L) {
+    const long long r = lrow(L, i, j, k);
+    if (((i + j + k) & 1) != colour) {
+      if (zero) x[r] = 0.f;
+      continue;
+    }
+    const float d = ldiag(L, i, j, k);
+    float bb = b[r];
+    if (bscale) bb *= d;
+    const float num = zero ? bb : bb + lnb(L, x, i, j, k, r);
+    x[r] = d > 0.f ? num / d : 0.f;
+  }
+}
+
+// bc = average over each coarse cell's children of the fine residual b - A x
+__global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel Cl, int bscale, const float *__restrict__ bf,
+                                                        const float *__restrict__ xf, float *__restrict__ bc,
+                                                        const SolverScal *sc) {
+  if (sc->done) return;
+  const float inv = 1.0f / (float)(F.fx * F.fy * F.fz);
+  FOR_LEVEL(Cl) {
+    float sum = 0.f;
+    for (int a = 0; a < F.fx; ++a)
+      for (int e = 0; e < F.fy; ++e)
+        for (int c = 0; c < F.fz; ++c) {
+          const int fi = i * F.fx + a, fj = j * F.fy + e, fk = k * F.fz + c;
+          const long long r = lrow(F, fi, fj, fk);
+          const float d = ldiag(F, fi, fj, fk);
+          float bb = bf[r];
+          if (bscale) bb *= d;
+          sum += bb - d * xf[r] + lnb(F, xf, fi, fj, fk, r);
+        }
+    bc[lrow(Cl, i, j, k)] = sum * inv;
+  }
+}
+
+// the two coarse cells a fine cell interpolates from along one axis, and their weights
+__device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], float (&w)[2]) {
+  if (f == 1) {
+    c[0] = c[1] = i;
+    w[0] = 1.f;
+    w[1] = 0.f;
+    return;
+  }
+  const int p = i >> 1;
+  int q = p + ((i & 1) ? 1 : -1);
+  if (q < 0 || q >= n) q = p;  // beyond a wall: the parent's value (zero normal gradient)
+  c[0] = p;
+  c[1] = q;
+  w[0] = 0.75f;
+  w[1] = 0.25f;
+}
+
+// xf += P xc
+__global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel Cl, const float *__restrict__ xc,
+                                                       float *__restrict__ xf, const SolverScal *sc) {
+  if (sc->done) return;
+  FOR_LEVEL(F) {
+    int ci[2], cj[2], ck[2];
+    float wi[2], wj[2], wk[2];
+    axis_taps(i, F.fx, Cl.nx, ci, wi);
+    axis_taps(j, F.fy, Cl.ny, cj, wj);
+    axis_taps(k, F.fz, Cl.nz, ck, wk);
+    float v = 0.f;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const float w = wi[a] * wj[e] * wk[c];
+          if (w != 0.f) v += w * xc[lrow(Cl, ci[a], cj[e], ck[c])];
+        }
+    xf[lrow(F, i, j, k)] += v;
+  }
+}
+
+// coarsest level: x = 0, then `sweeps` red-black sweeps in shared memory, one block
+__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, int sweeps, int bscale, const float *__restrict__ b,
+                                                    float *__restrict__ x, const SolverScal *sc) {
+  if (sc->done) return;
+  extern __shared__ float sm[];
+  const int n = L.nx * L.ny * L.nz;
+  float *xs = sm, *bs = sm + n;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int k = q % L.nz, t = q / L.nz, j = t % L.ny, i = t / L.ny;
+    float bb = b[q];
+    if (bscale) bb *= ldiag(L, i, j, k);
+    bs[q] = bb;
+    xs[q] = 0.f;
+  }
+  __syncthreads();
+  for (int s = 0; s < sweeps; ++s)
+    for (int colour = 0; colour < 2; ++colour) {
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int k = q % L.nz, t = q / L.nz, j = t % L.ny, i = t / L.ny;
+        if (((i + j + k) & 1) != colour) continue;
+        const float d = ldiag(L, i, j, k);
+        xs[q] = d > 0.f ? (bs[q] + lnb(L, xs, i, j, k, q)) / d : 0.f;
+      }
+      __syncthreads();
+    }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) x[q] = xs[q];
+}
+
+static void level_geometry(MgLevel &L, int nsm) {
+  L.bx = 1;
+  while (L.bx < L.nz && L.bx < 32) L.bx *= 2;
+  L.by = kBlock / L.bx;
+  L.gx = (L.nz + L.bx - 1) / L.bx;
+  L.gy = (L.ny + L.by - 1) / L.by;
+  L.gz = std::max(1, std::min(L.nx, nsm * 8 / std::max(1, L.gx * L.gy)));
+}
+
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, MgPlan *mg) {
+  *mg = MgPlan{};
+  int l = 0;
+  for (;;) {
+    MgLevel &L = mg->lev[l];
+    L.nx = nx;
+    L.ny = ny;
+    L.nz = nz;
+    L.wx = (float)(1.0 / (hx * hx));
+    L.wy = (float)(1.0 / (hy * hy));
+    L.wz = (float)(1.0 / (hz * hz));
+    level_geometry(L, nsm);
+    const long long cells = (long long)nx * ny * nz;
+    const int fx = nx % 2 == 0 ? 2 : 1, fy = ny % 2 == 0 ? 2 : 1, fz = nz % 2 == 0 ? 2 : 1;
+    if (cells <= kMgCoarseCells || fx * fy * fz == 1 || l + 1 == kMgMaxLevels) {
+      L.fx = L.fy = L.fz = 1;
+      break;
+    }
+    L.fx = fx;
+    L.fy = fy;
+    L.fz = fz;
+    nx /= fx;
+    ny /= fy;
+    nz /= fz;
+    hx *= fx;
+    hy *= fy;
+    hz *= fz;
+    ++l;
+  }
+  mg->nlev = l + 1;
+  const MgLevel &C = mg->lev[l];
+  mg->coarse_sweeps = std::min(256, 16 + 2 * std::max(C.nx, std::max(C.ny, C.nz)));
+  return (long long)C.nx * C.ny * C.nz <= kMgSharedCells;
+}
+
+int mg_vcycle_launches(const MgPlan &mg) { return 6 * (mg.nlev - 1) + 1; }
+
+void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float *b0, float *x0, const SolverScal *sc) {
+  const int n = mg.nlev;
+  auto B = [&](int l) -> const float * { return l == 0 ? b0 : mg.lev[l].b; };
+  auto X = [&](int l) -> float * { return l == 0 ? x0 : mg.lev[l].x; };
+  auto grid = [&](int l) { return dim3(mg.lev[l].gx, mg.lev[l].gy, mg.lev[l].gz); };
+  auto block = [&](int l) { return dim3(mg.lev[l].bx, mg.lev[l].by, 1); };
+  auto smooth = [&](int l, int colour, int zero) {
+    k_mg_smooth<<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+  };
+  for (int l = 0; l + 1 < n; ++l) {
+    smooth(l, 0, 1);
+    smooth(l, 1, 0);
+    k_mg_restrict<<<grid(l + 1), block(l + 1), 0, s>>>(mg.lev[l], mg.lev[l + 1], l == 0 ? jacobi : 0, B(l), X(l),
+                                                         mg.lev[l + 1].b, sc);
+  }
+  const MgLevel &C = mg.lev[n - 1];
+  const size_t smem = 2 * sizeof(float) * (size_t)C.nx * C.ny * C.nz;
+  k_mg_coarse<<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
+  for (int l = n - 2; l >= 0; --l) {
+    k_mg_prolong<<<grid(l), block(l), 0, s>>>(mg.lev[l], mg.lev[l + 1], X(l + 1), X(l), sc);
+    smooth(l, 1, 0);
+    smooth(l, 0, 0);
+  }
+}
+
+}  // namespace cfdgb

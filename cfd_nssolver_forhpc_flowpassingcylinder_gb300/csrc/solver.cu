@@ -359,6 +359,96 @@ __global__ void __launch_bounds__(kBlock) k32_xr(Geo g, Vec32 v, double *part, S
   }
 }
 
+// ---- FP32 BiCGSTAB with a right preconditioner (the multigrid V-cycle, multigrid.cu) ----
+// The iteration of bicgstabRe2 on A M y = r with x = M y: p and s are preconditioned
+// (ph = M p, sh = M s) before each operator application and the update of x, while r, s,
+// and the stop test stay on the unpreconditioned residual.  Same device scalars and
+// decisions as the plain FP32 sweep (finish_iteration<true>), counters 1-3 as there.
+
+// p = r1 + beta (p - omega v), or p = r0 = r1 on restart
+__global__ void __launch_bounds__(kBlock) k32p_p(Geo g, PrecVecs v, const SolverScal *sc) {
+  if (sc->done) return;
+  const float b = (float)sc->beta, w = (float)sc->omega;
+  const bool rst = sc->restart != 0;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const float r1 = v.r1[row];
+    if (rst) {
+      v.r0[row] = r1;
+      v.p[row] = r1;
+    } else {
+      v.p[row] = r1 + b * (v.p[row] - w * v.v[row]);
+    }
+  }
+}
+
+// v = A ph, alpha = rho / <v, r0>
+__global__ void __launch_bounds__(kBlock) k32p_v(Geo g, Stencil<float> st, PrecVecs v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float *__restrict__ ph = v.ph;
+  AccF acc;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    float c;
+    const float y = stencil_apply_diff(g, st, ic, jc, kc, row, [&](long long q) { return ph[q]; }, c);
+    v.v[row] = y;
+    acc.add(y * v.r0[row]);
+  }
+  double a[1] = {acc.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+// s = r1 - alpha v
+__global__ void __launch_bounds__(kBlock) k32p_s(Geo g, PrecVecs v, const SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.s[row] = fmaf(-a, v.v[row], v.r1[row]);
+  }
+}
+
+// t = A sh, omega = <t, s> / <t, t> (0 when t vanishes, as in k32_sas)
+__global__ void __launch_bounds__(kBlock) k32p_t(Geo g, Stencil<float> st, PrecVecs v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float *__restrict__ sh = v.sh;
+  AccF a0, a1;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    float c;
+    const float y = stencil_apply_diff(g, st, ic, jc, kc, row, [&](long long q) { return sh[q]; }, c);
+    v.t[row] = y;
+    a0.add(y * v.s[row]);
+    a1.add(y * y);
+  }
+  double acc[2] = {a0.get(), a1.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;
+    sc->omega = wv;
+  }
+}
+
+// x += alpha ph + omega sh; r1 = s - omega t; stop test, beta, restart
+__global__ void __launch_bounds__(kBlock) k32p_xr(Geo g, PrecVecs v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha, w = (float)sc->omega;
+  const bool keep = sc->snap != 0;
+  AccF n2, rr;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const float x = v.x[row];
+    if (keep) v.xb[row] = x;
+    v.x[row] = fmaf(w, v.sh[row], fmaf(a, v.ph[row], x));
+    const float r1 = fmaf(-w, v.t[row], v.s[row]);
+    v.r1[row] = r1;
+    n2.add(r1 * r1);
+    rr.add(r1 * v.r0[row]);
+  }
+  double acc[2] = {n2.get(), rr.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
+}
+
 // ---- FP32 iteration, vectorised: four consecutive k cells per thread (nzc % 4 == 0) ----
 // One float4 load per vector and stencil point instead of four scalar loads; the k
 // neighbours inside the quad come from registers.  Dot partials stay FP32 over the few
@@ -1437,6 +1527,17 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
     case 0: k32_pap<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, part_buf, sc); break;
     case 1: k32_sas<<<cgrid(g), cblock(g), 0, s>>>(g, st, w, part_buf, sc); break;
     default: k32_xr<<<cgrid(g), cblock(g), 0, s>>>(g, w, part_buf, sc); break;
+  }
+}
+
+void launch_bicgp32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, PrecVecs v,
+                         double *part_buf, SolverScal *sc) {
+  switch (part) {
+    case 0: k32p_p<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+    case 1: k32p_v<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    case 2: k32p_s<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+    case 3: k32p_t<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    default: k32p_xr<<<cgrid(g), cblock(g), 0, s>>>(g, v, part_buf, sc); break;
   }
 }
 

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 5
+#define CFDGB_ABI_VERSION 6
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -75,6 +75,18 @@ typedef enum cfdgb_scheme {
   CFDGB_UD = 2      /* first-order upwind, UdUnit (:150-168) */
 } cfdgb_scheme;
 
+/* Preconditioner of the FP32 BiCGSTAB sweeps of the MIXED precision mode (the reference
+   has none; its FP64 BiCGSTAB stays unpreconditioned in every mode). */
+typedef enum cfdgb_precond {
+  CFDGB_PRECOND_NONE = 0,      /* the plain sweep (default) */
+  CFDGB_PRECOND_MULTIGRID = 1  /* one FP32 geometric multigrid V-cycle per application (right
+                                  preconditioning): red-black Gauss-Seidel smoothing, cell-
+                                  centred transfers, the uniform-grid Laplacian rediscretised
+                                  per level.  MIXED, BICGSTAB or BICGSTAB_JACOBI, uniform grid;
+                                  the grid must coarsen (by halving its even extents) to at
+                                  most 4096 cells */
+} cfdgb_precond;
+
 typedef struct cfdgb_config {
   int nx, ny, nz;            /* interior cells (nxCal, nyCal, nzCal) */
   double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; spacing per cfdgb_config.grid */
@@ -106,6 +118,8 @@ typedef struct cfdgb_config {
                                 inc/source/SmagorinskyModel.hpp:30, CS = 0.18) added to nu,
                                 from T0 before each convection-diffusion; 0: off (default) */
   int walls;                 /* a cfdgb_walls value; default zero-gradient */
+  int precond;               /* a cfdgb_precond value: the preconditioner of the MIXED
+                                BiCGSTAB sweeps; default none (the reference's iteration) */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {

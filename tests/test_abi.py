@@ -42,7 +42,7 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 5
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 6
     assert cfg.scheme == cg.QUICK and cfg.les == 0 and cfg.walls == cg.WALLS_ZERO_GRADIENT
 
 
