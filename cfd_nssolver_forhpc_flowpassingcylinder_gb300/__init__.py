@@ -70,6 +70,7 @@ _lib = None
 EXPORTS = {
     # name: (restype, argtypes)
     "cfdgb_abi_version": (C.c_int, []),
+    "cfdgb_check_division": (C.c_int, [C.c_longlong, C.c_uint64, C.c_double, C.POINTER(C.c_ulonglong)]),
     "cfdgb_last_error": (C.c_char_p, []),
     "cfdgb_config_default": (C.c_int, [C.POINTER(Config)]),
     "cfdgb_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
@@ -145,6 +146,14 @@ def _ptr(a):
     if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
         raise TypeError("expected a C-contiguous float64 array")
     return a.ctypes.data_as(_dp)
+
+
+def check_division(n: int, seed: int, b: float) -> int:
+    """cfdgb_check_division: results of the step kernels' reciprocal division that differ
+    from IEEE division over n seeded dividends for divisor b (0 expected)."""
+    out = C.c_ulonglong(0)
+    _check(load_library().cfdgb_check_division(n, seed, b, C.byref(out)))
+    return int(out.value)
 
 
 def default_config(**kw) -> Config:

@@ -838,6 +838,21 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.ncell = c->ncell;
   g.Dx = c->metric; g.Dy = g.Dx + nx; g.Dz = g.Dy + ny;
   g.Dxs = g.Dz + nz; g.Dys = g.Dxs + nx; g.Dzs = g.Dys + ny;
+  {  // reciprocals of the metrics and the DFIB face factors, one IEEE division each
+    std::vector<double> rm;
+    for (auto *v : {&c->Dx, &c->Dy, &c->Dz, &c->Dxs, &c->Dys, &c->Dzs})
+      for (double d : *v) rm.push_back(1.0 / d);
+    const std::vector<double> *DD[3] = {&c->Dx, &c->Dy, &c->Dz}, *DS[3] = {&c->Dxs, &c->Dys, &c->Dzs};
+    for (int a = 0; a < 3; ++a)
+      for (size_t q = 0; q < DD[a]->size(); ++q) rm.push_back(((*DS[a])[q] * 0.5) / (*DD[a])[q]);
+    double *drm = nullptr;
+    if ((rc = dalloc(c, &drm, rm.size()))) return bail(rc);
+    if (cudaMemcpy(drm, rm.data(), rm.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(fail(CFDGB_ECUDA, "metric reciprocal upload"));
+    g.rDx = drm; g.rDy = g.rDx + nx; g.rDz = g.rDy + ny;
+    g.rDxs = g.rDz + nz; g.rDys = g.rDxs + nx; g.rDzs = g.rDys + ny;
+    g.hfx = g.rDzs + nz; g.hfy = g.hfx + nx; g.hfz = g.hfy + ny;
+  }
   if (cfg->grid == CFDGB_GRID_SML) {
     // per-axis operator factors and the Jacobi scale of every row (createPressureMatrixCSR)
     const Coef C{c};

@@ -47,7 +47,22 @@ struct Geo {
   // solver kernels read the bits they would otherwise recompute at every application
   const double *cof[2];
   int walls;  // a cfdgb_walls value (the boundary table's y-wall rows)
+  // per-index reciprocals RN(1/D), RN(1/Ds) of the metrics (padded lengths) for div_by, and
+  // the DFIB face-fraction factors (Ds * 0.5) / D of updateUandF.hpp, each one IEEE division
+  const double *rDx, *rDy, *rDz, *rDxs, *rDys, *rDzs, *hfx, *hfy, *hfz;
 };
+
+// a / b correctly rounded, given y = RN(1/b): q = RN(a y) lies within an ulp of a / b, so
+// the remainder a - b q is exact in one FMA and RN(q + (a - b q) y) = RN(a / b) (Markstein's
+// theorem: P. Markstein, IBM J. Res. Develop. 34(1), 1990; J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, the chapter on division by FMA).  It holds while a / b and the
+// intermediates are normal numbers; a = +-0 returns the zero of IEEE division's sign.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  const double q = __dmul_rn(a, y);
+  const double r = fma(-q, b, a);
+  const double q1 = fma(r, y, q);
+  return a == 0.0 ? q : q1;
+}
 
 // compact row -> padded (i,j,k)
 __device__ __forceinline__ void row_ijk(const Geo &g, long long row, int &i, int &j, int &k) {

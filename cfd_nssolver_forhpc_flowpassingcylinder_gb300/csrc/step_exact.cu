@@ -5,6 +5,8 @@
 // the results are bit-identical to the reference (checked against its golden vectors).
 // One thread per interior cell (grid-stride over compact rows, k fastest, so a warp
 // reads contiguous k runs of each padded array).
+#include <cmath>
+
 #include "cfdgb_internal.cuh"
 #include "reduce.cuh"
 #include "kernels.h"
@@ -14,52 +16,55 @@ namespace cfdgb {
 // inc/source/Convection_Difussion.hpp:20-51 (QuickUnitA)
 __device__ __forceinline__ void quick_a(double Up, double Un, long long pp, long long p, long long ic,
                                         long long n, long long nn, const double *__restrict__ Di,
-                                        const double *__restrict__ Ds, int I,
+                                        const double *__restrict__ Ds, const double *__restrict__ rDi,
+                                        const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
   if (Up > 0.0)
-    P = 0.5 * (fc + fp) - 0.125 * Di[I + 1] * Di[I + 1] / Ds[I] * ((fp - fc) / Di[I + 1] - (fc - fn) / Di[I]);
+    P = 0.5 * (fc + fp) - div_by(0.125 * Di[I + 1] * Di[I + 1], Ds[I], rDs[I]) * (div_by((fp - fc), Di[I + 1], rDi[I + 1]) - div_by((fc - fn), Di[I], rDi[I]));
   else
     P = 0.5 * (fc + fp) -
-        0.125 * Di[I + 1] * Di[I + 1] / Ds[I + 1] * ((phi[pp] - fp) / Di[I + 2] - (fp - fc) / Di[I + 1]);
+        div_by(0.125 * Di[I + 1] * Di[I + 1], Ds[I + 1], rDs[I + 1]) * (div_by((phi[pp] - fp), Di[I + 2], rDi[I + 2]) - div_by((fp - fc), Di[I + 1], rDi[I + 1]));
   if (Un > 0.0)
     N = 0.5 * (fn + fc) -
-        0.125 * Di[I] * Di[I] / Ds[I - 1] * ((fc - fn) / Di[I] - (fn - phi[nn]) / Di[I - 1]);
+        div_by(0.125 * Di[I] * Di[I], Ds[I - 1], rDs[I - 1]) * (div_by((fc - fn), Di[I], rDi[I]) - div_by((fn - phi[nn]), Di[I - 1], rDi[I - 1]));
   else
-    N = 0.5 * (fn + fc) - 0.125 * Di[I] * Di[I] / Ds[I] * ((fp - fc) / Di[I + 1] - (fc - fn) / Di[I]);
+    N = 0.5 * (fn + fc) - div_by(0.125 * Di[I] * Di[I], Ds[I], rDs[I]) * (div_by((fp - fc), Di[I + 1], rDi[I + 1]) - div_by((fc - fn), Di[I], rDi[I]));
 }
 
 // inc/source/Convection_Difussion.hpp:55-90 (QuickUnitB)
 __device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long long p, long long ic,
                                         long long n, long long nn, const double *__restrict__ Di,
-                                        const double *__restrict__ Ds, int I,
+                                        const double *__restrict__ Ds, const double *__restrict__ rDi,
+                                        const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
   if (Up > 0.0)
-    P = 0.5 * (fc + fp) - 0.125 * Ds[I] * Ds[I] / Di[I] * ((fp - fc) / Ds[I] - (fc - fn) / Ds[I - 1]);
+    P = 0.5 * (fc + fp) - div_by(0.125 * Ds[I] * Ds[I], Di[I], rDi[I]) * (div_by((fp - fc), Ds[I], rDs[I]) - div_by((fc - fn), Ds[I - 1], rDs[I - 1]));
   else
     P = 0.5 * (fc + fp) -
-        0.125 * Ds[I] * Ds[I] / Di[I + 1] * ((phi[pp] - fp) / Ds[I + 1] - (fp - fc) / Ds[I]);
+        div_by(0.125 * Ds[I] * Ds[I], Di[I + 1], rDi[I + 1]) * (div_by((phi[pp] - fp), Ds[I + 1], rDs[I + 1]) - div_by((fp - fc), Ds[I], rDs[I]));
   if (Un > 0.0)
     N = 0.5 * (fn + fc) -
-        0.125 * Ds[I - 1] * Ds[I - 1] / Di[I - 1] * ((fc - fn) / Ds[I - 1] - (fn - phi[nn]) / Ds[I - 2]);
+        div_by(0.125 * Ds[I - 1] * Ds[I - 1], Di[I - 1], rDi[I - 1]) * (div_by((fc - fn), Ds[I - 1], rDs[I - 1]) - div_by((fn - phi[nn]), Ds[I - 2], rDs[I - 2]));
   else
-    N = 0.5 * (fn + fc) - 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I] * ((fp - fc) / Ds[I] - (fc - fn) / Ds[I - 1]);
+    N = 0.5 * (fn + fc) - div_by(0.125 * Ds[I - 1] * Ds[I - 1], Di[I], rDi[I]) * (div_by((fp - fc), Ds[I], rDs[I]) - div_by((fc - fn), Ds[I - 1], rDs[I - 1]));
 }
 
 // inc/source/Convection_Difussion.hpp:96-147 (LudUnitA; LudUnitB has the same body)
 __device__ __forceinline__ void lud(double Up, double Un, long long pp, long long p, long long ic, long long n,
                                     long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
-                                    int I, const double *__restrict__ phi, double &P, double &N) {
+                                    const double *__restrict__ rDi, const double *__restrict__ rDs, int I,
+                                    const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
   if (Up > 0.0)
-    P = (fc + 0.5 * Ds[I] * (fc - fn) / Di[I]);
+    P = (fc + div_by(0.5 * Ds[I] * (fc - fn), Di[I], rDi[I]));
   else
-    P = (fp + 0.5 * Ds[I + 1] * (fp - phi[pp]) / Di[I + 1]);
+    P = (fp + div_by(0.5 * Ds[I + 1] * (fp - phi[pp]), Di[I + 1], rDi[I + 1]));
   if (Un > 0.0)
-    N = (fn + 0.5 * Ds[I - 1] * (fn - phi[nn]) / Di[I - 1]);
+    N = (fn + div_by(0.5 * Ds[I - 1] * (fn - phi[nn]), Di[I - 1], rDi[I - 1]));
   else
-    N = (fc + 0.5 * Ds[I] * (fc - fp) / Di[I + 1]);
+    N = (fc + div_by(0.5 * Ds[I] * (fc - fp), Di[I + 1], rDi[I + 1]));
 }
 
 // face values of one axis under the convection switch (inc/0_General.hpp:114-118): QUICK,
@@ -67,16 +72,17 @@ __device__ __forceinline__ void lud(double Up, double Un, long long pp, long lon
 template <int S, bool OWN>
 __device__ __forceinline__ void face(double Up, double Un, long long pp, long long p, long long ic, long long n,
                                      long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
-                                     int I, const double *__restrict__ phi, double &P, double &N) {
+                                     const double *__restrict__ rDi, const double *__restrict__ rDs, int I,
+                                     const double *__restrict__ phi, double &P, double &N) {
   if (S == CFDGB_LUD) {
-    lud(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+    lud(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   } else if (S == CFDGB_UD) {
     P = Up > 0.0 ? phi[ic] : phi[p];
     N = Un > 0.0 ? phi[n] : phi[ic];
   } else if (OWN) {
-    quick_a(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+    quick_a(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   } else {
-    quick_b(Up, Un, pp, p, ic, n, nn, Di, Ds, I, phi, P, N);
+    quick_b(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   }
 }
 
@@ -94,12 +100,12 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
-    const double ux = 0.5 / g.Dxs[i] * (u[c - sx] - u[c + sx]), uy = 0.5 / g.Dy[j] * (u[c - sy] - u[c + sy]),
-                 uz = 0.5 / g.Dz[k] * (u[c - 1] - u[c + 1]);
-    const double vx = 0.5 / g.Dx[i] * (v[c - sx] - v[c + sx]), vy = 0.5 / g.Dys[j] * (v[c - sy] - v[c + sy]),
-                 vz = 0.5 / g.Dz[k] * (v[c - 1] - v[c + 1]);
-    const double wx = 0.5 / g.Dx[i] * (w[c - sx] - w[c + sx]), wy = 0.5 / g.Dy[j] * (w[c - sy] - w[c + sy]),
-                 wz = 0.5 / g.Dzs[k] * (w[c - 1] - w[c + 1]);
+    const double ux = div_by(0.5, g.Dxs[i], g.rDxs[i]) * (u[c - sx] - u[c + sx]), uy = div_by(0.5, g.Dy[j], g.rDy[j]) * (u[c - sy] - u[c + sy]),
+                 uz = div_by(0.5, g.Dz[k], g.rDz[k]) * (u[c - 1] - u[c + 1]);
+    const double vx = div_by(0.5, g.Dx[i], g.rDx[i]) * (v[c - sx] - v[c + sx]), vy = div_by(0.5, g.Dys[j], g.rDys[j]) * (v[c - sy] - v[c + sy]),
+                 vz = div_by(0.5, g.Dz[k], g.rDz[k]) * (v[c - 1] - v[c + 1]);
+    const double wx = div_by(0.5, g.Dx[i], g.rDx[i]) * (w[c - sx] - w[c + sx]), wy = div_by(0.5, g.Dy[j], g.rDy[j]) * (w[c - sy] - w[c + sy]),
+                 wz = div_by(0.5, g.Dzs[k], g.rDzs[k]) * (w[c - 1] - w[c + 1]);
     const double a = uy + vx, b = uz + wx, e = vz + wy;
     const double temp = fabs(2.0 * (ux * ux) + vy * vy + wz * wz + a * a + b * b + e * e);
     nut[row] = l2[row] * sqrt(temp);
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
                                                            double *__restrict__ ws) {
   const long long sx = g.sx, sy = g.sy, sz = 1;
   const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
+  const double *rDx = g.rDx, *rDy = g.rDy, *rDz = g.rDz, *rDxs = g.rDxs, *rDys = g.rDys, *rDzs = g.rDzs;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
@@ -130,7 +137,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
     const double nu = nut ? nu0 + nut[row] : nu0;
     const long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz, zp = ic + sz;
     if (i < g.nx - 3) {  // u
-      const double IT = (Dxs[i] * 0.5) / Dx[i];
+      const double IT = div_by((Dxs[i] * 0.5), Dx[i], rDx[i]);
       const double uc = u[ic], uxp = u[xp], uxm = u[xm];
       const double Up = 0.5 * (uxp + uc);
       const double Un = 0.5 * (uxm + uc);
@@ -139,20 +146,20 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
       double uPx, uNx, uPy, uNy, uPz, uNz;
-      face<S, true>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, u, uPx, uNx);
-      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, u, uPy, uNy);
-      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, u, uPz, uNz);
-      const double convection = -dt * ((uPx * uPx - uNx * uNx) / Dxs[i] + (uPy * Vp - uNy * Vn) / Dy[j] +
-                                       (uPz * Wp - uNz * Wn) / Dz[k]);
+      face<S, true>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, u, uPx, uNx);
+      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, u, uPy, uNy);
+      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, u, uPz, uNz);
+      const double convection = -dt * (div_by((uPx * uPx - uNx * uNx), Dxs[i], rDxs[i]) + div_by((uPy * Vp - uNy * Vn), Dy[j], rDy[j]) +
+                                       div_by((uPz * Wp - uNz * Wn), Dz[k], rDz[k]));
       const double difussion =
           nu * dt *
-          (((uxp - uc) / Dx[i + 1] - (uc - uxm) / Dx[i]) / Dxs[i] +
-           ((u[yp] - uc) / Dys[j] - (uc - u[ym]) / Dys[j - 1]) / Dy[j] +
-           ((u[zp] - uc) / Dzs[k] - (uc - u[zm]) / Dzs[k - 1]) / Dz[k]);
+          (div_by((div_by((uxp - uc), Dx[i + 1], rDx[i + 1]) - div_by((uc - uxm), Dx[i], rDx[i])), Dxs[i], rDxs[i]) +
+           div_by((div_by((u[yp] - uc), Dys[j], rDys[j]) - div_by((uc - u[ym]), Dys[j - 1], rDys[j - 1])), Dy[j], rDy[j]) +
+           div_by((div_by((u[zp] - uc), Dzs[k], rDzs[k]) - div_by((uc - u[zm]), Dzs[k - 1], rDzs[k - 1])), Dz[k], rDz[k]));
       us[ic] = uc + convection + difussion;
     }
     if (j < g.ny - 3) {  // v
-      const double IT = (Dys[j] * 0.5) / Dy[j];
+      const double IT = div_by((Dys[j] * 0.5), Dy[j], rDy[j]);
       const double vc = v[ic], vyp = v[yp], vym = v[ym];
       const double Vp = 0.5 * (vyp + vc);
       const double Vn = 0.5 * (vym + vc);
@@ -161,20 +168,20 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
       double vPx, vNx, vPy, vNy, vPz, vNz;
-      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, v, vPx, vNx);
-      face<S, true>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, v, vPy, vNy);
-      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, v, vPz, vNz);
-      const double convection = -dt * ((Up * vPx - Un * vNx) / Dx[i] + (vPy * vPy - vNy * vNy) / Dys[j] +
-                                       (Wp * vPz - Wn * vNz) / Dz[k]);
+      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, v, vPx, vNx);
+      face<S, true>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, v, vPy, vNy);
+      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, v, vPz, vNz);
+      const double convection = -dt * (div_by((Up * vPx - Un * vNx), Dx[i], rDx[i]) + div_by((vPy * vPy - vNy * vNy), Dys[j], rDys[j]) +
+                                       div_by((Wp * vPz - Wn * vNz), Dz[k], rDz[k]));
       const double difussion =
           nu * dt *
-          (((v[xp] - vc) / Dxs[i] - (vc - v[xm]) / Dxs[i - 1]) / Dx[i] +
-           ((vyp - vc) / Dy[j + 1] - (vc - vym) / Dy[j]) / Dys[j] +
-           ((v[zp] - vc) / Dzs[k] - (vc - v[zm]) / Dzs[k - 1]) / Dz[k]);
+          (div_by((div_by((v[xp] - vc), Dxs[i], rDxs[i]) - div_by((vc - v[xm]), Dxs[i - 1], rDxs[i - 1])), Dx[i], rDx[i]) +
+           div_by((div_by((vyp - vc), Dy[j + 1], rDy[j + 1]) - div_by((vc - vym), Dy[j], rDy[j])), Dys[j], rDys[j]) +
+           div_by((div_by((v[zp] - vc), Dzs[k], rDzs[k]) - div_by((vc - v[zm]), Dzs[k - 1], rDzs[k - 1])), Dz[k], rDz[k]));
       vs[ic] = vc + convection + difussion;
     }
     if (k < g.nz - 3) {  // w
-      const double IT = (Dzs[k] * 0.5) / Dz[k];
+      const double IT = div_by((Dzs[k] * 0.5), Dz[k], rDz[k]);
       const double wc = w[ic], wzp = w[zp], wzm = w[zm];
       const double Wp = 0.5 * (wzp + wc);
       const double Wn = 0.5 * (wzm + wc);
@@ -183,16 +190,16 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
       const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
       double wPx, wNx, wPy, wNy, wPz, wNz;
-      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, i, w, wPx, wNx);
-      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, j, w, wPy, wNy);
-      face<S, true>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, k, w, wPz, wNz);
-      const double convection = -dt * ((Up * wPx - Un * wNx) / Dx[i] + (Vp * wPy - Vn * wNy) / Dy[j] +
-                                       (wPz * wPz - wNz * wNz) / Dzs[k]);
+      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, w, wPx, wNx);
+      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, w, wPy, wNy);
+      face<S, true>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, w, wPz, wNz);
+      const double convection = -dt * (div_by((Up * wPx - Un * wNx), Dx[i], rDx[i]) + div_by((Vp * wPy - Vn * wNy), Dy[j], rDy[j]) +
+                                       div_by((wPz * wPz - wNz * wNz), Dzs[k], rDzs[k]));
       const double difussion =
           nu * dt *
-          (((w[xp] - wc) / Dxs[i] - (wc - w[xm]) / Dxs[i - 1]) / Dx[i] +
-           ((w[yp] - wc) / Dys[j] - (wc - w[ym]) / Dys[j - 1]) / Dy[j] +
-           ((wzp - wc) / Dz[k + 1] - (wc - wzm) / Dz[k]) / Dzs[k]);
+          (div_by((div_by((w[xp] - wc), Dxs[i], rDxs[i]) - div_by((wc - w[xm]), Dxs[i - 1], rDxs[i - 1])), Dx[i], rDx[i]) +
+           div_by((div_by((w[yp] - wc), Dys[j], rDys[j]) - div_by((wc - w[ym]), Dys[j - 1], rDys[j - 1])), Dy[j], rDy[j]) +
+           div_by((div_by((wzp - wc), Dz[k + 1], rDz[k + 1]) - div_by((wc - wzm), Dz[k], rDz[k])), Dzs[k], rDzs[k]));
       ws[ic] = wc + convection + difussion;
     }
   }
@@ -209,8 +216,9 @@ __global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt, const do
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
-    const double div = (us[ic] - us[ic - g.sx]) / g.Dx[i] + (vs[ic] - vs[ic - g.sy]) / g.Dy[j] +
-                       (ws[ic] - ws[ic - 1]) / g.Dz[k];
+    const double div = div_by(us[ic] - us[ic - g.sx], g.Dx[i], g.rDx[i]) +
+                       div_by(vs[ic] - vs[ic - g.sy], g.Dy[j], g.rDy[j]) +
+                       div_by(ws[ic] - ws[ic - 1], g.Dz[k], g.rDz[k]);
     if (jacobi) {
       b[row] = -row_jp(g, st, i - 2, j - 2, k - 2, row) * ddt * div;
     } else {
@@ -244,17 +252,17 @@ __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *
     const long long ic = pidx(g, i, j, k);
     double c = 0.0;
     if (i < g.nx - 3) {
-      c += us[ic] / g.Dxs[i];
+      c += div_by(us[ic], g.Dxs[i], g.rDxs[i]);
       m[1] = fmax(m[1], us[ic]);
       m[4] = fmax(m[4], -us[ic]);
     }
     if (j < g.ny - 3) {
-      c += vs[ic] / g.Dys[j];
+      c += div_by(vs[ic], g.Dys[j], g.rDys[j]);
       m[2] = fmax(m[2], vs[ic]);
       m[5] = fmax(m[5], -vs[ic]);
     }
     if (k < g.nz - 3) {
-      c += ws[ic] / g.Dzs[k];
+      c += div_by(ws[ic], g.Dzs[k], g.rDzs[k]);
       m[3] = fmax(m[3], ws[ic]);
       m[6] = fmax(m[6], -ws[ic]);
     }
@@ -335,6 +343,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     double *part, StepScal *ss) {
   const long long tot = (long long)g.nx * g.ny * g.nz;
   const double uS = 0.0, vS = 0.0, wS = 0.0;
+  const double rdt = 1.0 / dt;
   double acc[2] = {0.0, 0.0};
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
@@ -345,10 +354,10 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     const double ec = eta[ic];
     if (i < g.nx - 3) {
       const long long icP = ic + g.sx;
-      const double T2u = us[ic] - dt * (p[icP] - p[ic]) / g.Dxs[i];
-      const double e = ec + (eta[icP] - ec) * ((g.Dxs[i] * 0.5) / g.Dx[i]);
+      const double T2u = us[ic] - div_by(dt * (p[icP] - p[ic]), g.Dxs[i], g.rDxs[i]);
+      const double e = ec + (eta[icP] - ec) * g.hfx[i];
       const double nu3 = ec * uS + (1.0 - e) * T2u;
-      const double fx = (nu3 - T2u) / dt;
+      const double fx = div_by(nu3 - T2u, dt, rdt);
       u3[ic] = nu3;
       if (f) f[ic] = fx;
       acc[0] += fx * vol;
@@ -357,10 +366,10 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     }
     if (j < g.ny - 3) {
       const long long icP = ic + g.sy;
-      const double T2v = vs[ic] - dt * (p[icP] - p[ic]) / g.Dys[j];
-      const double e = ec + (eta[icP] - ec) * ((g.Dys[j] * 0.5) / g.Dy[j]);
+      const double T2v = vs[ic] - div_by(dt * (p[icP] - p[ic]), g.Dys[j], g.rDys[j]);
+      const double e = ec + (eta[icP] - ec) * g.hfy[j];
       const double nv3 = ec * vS + (1.0 - e) * T2v;
-      const double fy = (nv3 - T2v) / dt;
+      const double fy = div_by(nv3 - T2v, dt, rdt);
       v3[ic] = nv3;
       if (f) f[ic + tot] = fy;
       acc[1] += fy * vol;
@@ -369,11 +378,11 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     }
     if (k < g.nz - 3) {
       const long long icP = ic + 1;
-      const double T2w = ws[ic] - dt * (p[icP] - p[ic]) / g.Dzs[k];
-      const double e = ec + (eta[icP] - ec) * ((g.Dzs[k] * 0.5) / g.Dz[k]);
+      const double T2w = ws[ic] - div_by(dt * (p[icP] - p[ic]), g.Dzs[k], g.rDzs[k]);
+      const double e = ec + (eta[icP] - ec) * g.hfz[k];
       const double nw3 = ec * wS + (1.0 - e) * T2w;
       w3[ic] = nw3;
-      if (f) f[ic + 2 * tot] = (nw3 - T2w) / dt;
+      if (f) f[ic + 2 * tot] = div_by(nw3 - T2w, dt, rdt);
     } else if (wi) {
       w3[ic] = wi[ic];
     }
@@ -590,3 +599,43 @@ void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const d
 }
 
 }  // namespace cfdgb
+
+// ---- self-check of div_by against IEEE division (this file is built with -prec-div=true) ----
+namespace cfdgb {
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void __launch_bounds__(kBlock) k_check_div(long long n, unsigned long long seed, double b, double y,
+                                                      unsigned long long *bad) {
+  unsigned long long miss = 0;
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock) {
+    const unsigned long long h1 = mix64(seed ^ (unsigned long long)q), h2 = mix64(h1);
+    double a;
+    if (q % 1000 == 0) {
+      a = (q % 2000 == 0) ? 0.0 : -0.0;
+    } else if (q % 10 == 0) {
+      a = b * (double)(long long)(h2 % 1000000);  // exact quotients
+    } else {
+      const double m = 1.0 + (double)(h1 >> 12) * 0x1.0p-52;  // [1, 2), 52 random bits
+      a = scalbn(m, (int)(h2 % 81) - 40) * ((h2 >> 40) & 1 ? -1.0 : 1.0);
+    }
+    if (__double_as_longlong(a / b) != __double_as_longlong(div_by(a, b, y))) ++miss;
+  }
+  if (miss) atomicAdd(bad, miss);
+}
+}  // namespace cfdgb
+
+extern "C" int cfdgb_check_division(long long n, uint64_t seed, double b, unsigned long long *mismatches) {
+  using namespace cfdgb;
+  if (!mismatches || n < 0 || !(b != 0.0) || !std::isfinite(b)) return CFDGB_EINVAL;
+  unsigned long long *d = nullptr;
+  if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return CFDGB_ECUDA;
+  cudaMemset(d, 0, sizeof(*d));
+  k_check_div<<<1216, kBlock>>>(n, seed, b, 1.0 / b, d);
+  const cudaError_t e = cudaMemcpy(mismatches, d, sizeof(*d), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? CFDGB_OK : CFDGB_ECUDA;
+}

@@ -284,6 +284,13 @@ int cfdgb_op_plot3d_read(cfdgb_ctx *ctx, const float *q, double *p, double *u, d
  * Pressure_transform_X_result, src/RUN_CPU.cpp:310-320) with the configured solver. */
 int cfdgb_pressure_solve(cfdgb_ctx *ctx, int *iters, double *relres);
 
+/* ---- self-check ---- */
+/* The step kernels divide by a metric or dt through its reciprocal (Markstein's FMA
+ * correction, correctly rounded like IEEE division).  On the current GPU: n seeded dividends
+ * (random sign, significand and exponent in [2^-40, 2^40], a tenth of them exact multiples
+ * of b, and zeros) divided by b both ways; *mismatches counts results whose bits differ. */
+int cfdgb_check_division(long long n, uint64_t seed, double b, unsigned long long *mismatches);
+
 #ifdef __cplusplus
 }
 #endif
