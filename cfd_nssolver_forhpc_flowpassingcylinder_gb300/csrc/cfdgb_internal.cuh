@@ -64,8 +64,17 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   return a == 0.0 ? q : q1;
 }
 
-// compact row -> padded (i,j,k)
+// compact row -> padded (i,j,k).  Grids below 2^31 cells divide in 32 bits: a 64-bit
+// division is a long software sequence on the GPU, twice per cell in every grid-stride kernel.
 __device__ __forceinline__ void row_ijk(const Geo &g, long long row, int &i, int &j, int &k) {
+  if (g.ncell < (1LL << 31)) {
+    const unsigned r = (unsigned)row, nz = (unsigned)g.nzc, nyz = (unsigned)g.nyc * nz;
+    const unsigned ic = r / nyz, rem = r - ic * nyz, jc = rem / nz;
+    i = (int)ic + 2;
+    j = (int)jc + 2;
+    k = (int)(rem - jc * nz) + 2;
+    return;
+  }
   const long long nyz = (long long)g.nyc * g.nzc;
   const int ic = (int)(row / nyz);
   const long long rem = row - (long long)ic * nyz;
@@ -173,6 +182,14 @@ __device__ __forceinline__ double row_jp(const Geo &g, const Stencil<double> &st
 }
 
 __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &ic, int &jc, int &kc) {
+  if (row < (1LL << 31) && (long long)nyc * nzc < (1LL << 31)) {  // 32-bit division, as row_ijk
+    const unsigned r = (unsigned)row, nz = (unsigned)nzc, nyz = (unsigned)nyc * nz;
+    const unsigned a = r / nyz, rem = r - a * nyz, b = rem / nz;
+    ic = (int)a;
+    jc = (int)b;
+    kc = (int)(rem - b * nz);
+    return;
+  }
   const long long nyz = (long long)nyc * nzc;
   ic = (int)(row / nyz);
   const long long rem = row - (long long)ic * nyz;
