@@ -501,7 +501,9 @@ double sweep_reduction(const cfdgb_ctx *c) {
 // cannot follow it down much more than two decades below such a peak (the kept iterate
 // bounds what the sweep gives back).  0.3 ended sweeps right after every bump and cost
 // ~15 % on 512x256x64; the two were even on 1024x512x128.
-double sweep_peak(const cfdgb_ctx *) { return 1e-2; }
+// The multigrid-preconditioned sweep has no such bumps (its residual falls ~30x an
+// iteration): the rule stays off there and only the reduction ends it (0 never fires).
+double sweep_peak(const cfdgb_ctx *c) { return c->use_mg ? 0.0 : 1e-2; }
 
 // FP64 Krylov set-up on the current b and warm start x
 void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
