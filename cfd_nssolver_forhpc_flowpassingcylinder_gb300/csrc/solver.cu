@@ -619,6 +619,114 @@ __global__ void __launch_bounds__(kBlock) k32v_sas(Geo g, Stencil<float> st, Vec
   }
 }
 
+// ---- the preconditioned FP32 iteration on quads (nzc % 4 == 0): the operator kernels march
+// along x as k32v_sas does, the pointwise ones stride over float4 quads as k32v_xr does ----
+__global__ void __launch_bounds__(kBlock) k32pv_p(Geo g, PrecVecs v, const SolverScal *sc) {
+  if (sc->done) return;
+  const float b = (float)sc->beta, w = (float)sc->omega;
+  const bool rst = sc->restart != 0;
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const long long row = 4 * q;
+    const F4 r1 = ld4(v.r1 + row);
+    if (rst) {
+      st4(v.r0 + row, r1);
+      st4(v.p + row, r1);
+      continue;
+    }
+    const F4 pp = ld4(v.p + row), vv = ld4(v.v + row);
+    F4 o;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) o.v[t] = r1.v[t] + b * (pp.v[t] - w * vv.v[t]);
+    st4(v.p + row, o);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k32pv_v(Geo g, Stencil<float> st, PrecVecs v, double *part,
+                                                  SolverScal *sc) {
+  if (sc->done) return;
+  const float *__restrict__ ph = v.ph;
+  const float *__restrict__ r0 = v.r0;
+  float *__restrict__ vv = v.v;
+  SumF a0;
+  march_quads(
+      g, st, [&](long long q) { return ld4(ph + q); }, [&](long long q) { return ph[q]; },
+      [&](long long row, const F4 &, const F4 &y) {
+        st4(vv + row, y);
+        const F4 r = ld4(r0 + row);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) a0.add(y.v[t], r.v[t]);
+      });
+  double a[1] = {a0.get()}, out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k32pv_s(Geo g, PrecVecs v, const SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha;
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const long long row = 4 * q;
+    const F4 r1 = ld4(v.r1 + row), vv = ld4(v.v + row);
+    F4 o;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) o.v[t] = fmaf(-a, vv.v[t], r1.v[t]);
+    st4(v.s + row, o);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k32pv_t(Geo g, Stencil<float> st, PrecVecs v, double *part,
+                                                  SolverScal *sc) {
+  if (sc->done) return;
+  const float *__restrict__ sh = v.sh;
+  const float *__restrict__ sv = v.s;
+  float *__restrict__ tv = v.t;
+  SumF a0, a1;
+  march_quads(
+      g, st, [&](long long q) { return ld4(sh + q); }, [&](long long q) { return sh[q]; },
+      [&](long long row, const F4 &, const F4 &y) {
+        st4(tv + row, y);
+        const F4 s4 = ld4(sv + row);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          a0.add(y.v[t], s4.v[t]);
+          a1.add(y.v[t], y.v[t]);
+        }
+      });
+  double acc[2] = {a0.get(), a1.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;
+    sc->omega = wv;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k32pv_xr(Geo g, PrecVecs v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const float a = (float)sc->alpha, w = (float)sc->omega;
+  const bool keep = sc->snap != 0;
+  SumF n2, rr;
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const long long row = 4 * q;
+    const F4 ph = ld4(v.ph + row), sh = ld4(v.sh + row), s = ld4(v.s + row), t4 = ld4(v.t + row),
+             r0 = ld4(v.r0 + row);
+    F4 x = ld4(v.x + row), r1;
+    if (keep) st4(v.xb + row, x);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      x.v[t] = fmaf(w, sh.v[t], fmaf(a, ph.v[t], x.v[t]));
+      r1.v[t] = fmaf(-w, t4.v[t], s.v[t]);
+      n2.add(r1.v[t], r1.v[t]);
+      rr.add(r1.v[t], r0.v[t]);
+    }
+    st4(v.x + row, x);
+    st4(v.r1 + row, r1);
+  }
+  double acc[2] = {n2.get(), rr.get()}, out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
+}
+
 // ---- FP32 stencil kernels on a bulk-copy (TMA) pipeline ----
 // A block owns tj rows (all k) of the compact vectors and a chunk of consecutive i planes.
 // Thread 0 streams each plane's rows jt-1 .. jt+tj (the halo rows included: one contiguous
@@ -1532,6 +1640,17 @@ void launch_bicg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<fl
 
 void launch_bicgp32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, PrecVecs v,
                          double *part_buf, SolverScal *sc) {
+  if (g.vbx > 0) {  // quads
+    const dim3 vg(g.vgx, g.vgy, g.vgz), vb(g.vbx, g.vby, 1);
+    switch (part) {
+      case 0: k32pv_p<<<g.xgrid, kBlock, 0, s>>>(g, v, sc); break;
+      case 1: k32pv_v<<<vg, vb, 0, s>>>(g, st, v, part_buf, sc); break;
+      case 2: k32pv_s<<<g.xgrid, kBlock, 0, s>>>(g, v, sc); break;
+      case 3: k32pv_t<<<vg, vb, 0, s>>>(g, st, v, part_buf, sc); break;
+      default: k32pv_xr<<<g.xgrid, kBlock, 0, s>>>(g, v, part_buf, sc); break;
+    }
+    return;
+  }
   switch (part) {
     case 0: k32p_p<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
     case 1: k32p_v<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;

@@ -42,6 +42,23 @@ def test_multigrid_sweeps_reach_the_fp64_solution(solver, case):
         assert e <= 1e-6, (solver, case, k, e)
 
 
+@pytest.mark.parametrize("env", [{}, {"CFDGB_SCALAR_FP32": "1"}], ids=["quads", "scalar"])
+def test_multigrid_quad_and_scalar_kernels_agree(env, monkeypatch):
+    """The preconditioned iteration's quad kernels (nz a multiple of 4) and its scalar ones
+    (any nz; forced here) on the same grid: both reach the FP64 run's fields."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    dom = CASES["128x64x16"]
+    with cg.Solver(precision="mixed", precond="multigrid", **dom) as a, cg.Solver(**dom) as b:
+        a.init_fields()
+        b.init_fields()
+        sa, sb = a.step(4), b.step(4)
+        fa, fb = a.get_fields(), b.get_fields()
+    assert all(r.status == 0 and r.relres < 1e-8 for r in sa[1:])
+    for k, e in vel_err(fa, fb).items():
+        assert e <= 1e-6, (env, k, e)
+
+
 def test_multigrid_with_perturbation_and_projection():
     """The seeded-perturbation case over 20 steps."""
     res = {}
