@@ -351,7 +351,7 @@ int validate(const cfdgb_config *c) {
         c->grid != CFDGB_GRID_UNIFORM)
       return fail(CFDGB_EINVAL, "the multigrid preconditioner is for the MIXED BiCGSTAB solvers on a uniform grid");
     MgPlan mg;
-    if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, &mg))
+    if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, false, &mg))
       return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
                   c->ny, c->nz, kMgSharedCells);
   }
@@ -957,7 +957,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
   if (cfg->precond == CFDGB_PRECOND_MULTIGRID) {  // levels >= 1 and the vectors M p, M s
-    mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm, &c->mg);
+    mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm,
+            !std::getenv("CFDGB_SCALAR_FP32"), &c->mg);
     if ((rc = dalloc(c, &c->ph32, c->ncell)) || (rc = dalloc(c, &c->sh32, c->ncell))) return bail(rc);
     for (int l = 1; l < c->mg.nlev; ++l) {
       MgLevel &L = c->mg.lev[l];

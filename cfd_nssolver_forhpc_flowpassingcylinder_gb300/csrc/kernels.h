@@ -125,6 +125,7 @@ struct MgLevel {
   int fx, fy, fz;          // cells of this level per cell of the next one, per axis (1, 2)
   float *x, *b;            // correction and right-hand side (levels >= 1)
   int bx, by, gx, gy, gz;  // launch geometry: bx along k, by along j, gz planes strided over i
+  int qgrid;               // blocks of the quad smoother (nz % 4 == 0), 0: the scalar one
 };
 struct MgPlan {
   int nlev;
@@ -133,7 +134,7 @@ struct MgPlan {
 };
 // levels of an nx x ny x nz grid with spacing hx, hy, hz (arrays left null); false when
 // the grid has a single level too large for the one-block coarsest solve
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, MgPlan *mg);
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlan *mg);
 // kernels one V-cycle launches
 int mg_vcycle_launches(const MgPlan &mg);
 // x0 = M b0, one V(1,1) cycle: red-black Gauss-Seidel smoothing from a zero start,

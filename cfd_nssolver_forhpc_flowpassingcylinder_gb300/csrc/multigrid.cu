@@ -69,6 +69,67 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, int colour, int
   }
 }
 
+// The same colour pass on quads of four consecutive k cells (nz % 4 == 0): a thread updates
+// the two cells of the colour in its quad and stores the whole quad, the other two
+// unchanged (no thread writes them in this pass, so rewriting them races with nothing).
+// Neighbour sums in the order of lnb.
+__global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, int zero, int bscale,
+                                                       const float *__restrict__ b, float *x, const SolverScal *sc) {
+  if (sc->done) return;
+  const unsigned nq = (unsigned)L.nz >> 2, nquads = (unsigned)L.nx * L.ny * nq;
+  const long long sx = (long long)L.ny * L.nz;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nquads; q += gridDim.x * blockDim.x) {
+    const unsigned t = q / nq, kq = q - t * nq, j = t % (unsigned)L.ny, i = t / (unsigned)L.ny;
+    const int k0 = (int)(4 * kq);
+    const long long r = lrow(L, (int)i, (int)j, k0);
+    const int t0 = ((int)i + (int)j + k0 + colour) & 1;  // first cell of the colour in the quad
+    const float4 bq = *reinterpret_cast<const float4 *>(b + r);
+    const float bv[4] = {bq.x, bq.y, bq.z, bq.w};
+    float o[4];
+    if (zero) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if ((c & 1) != t0) {
+          o[c] = 0.f;
+          continue;
+        }
+        const float d = ldiag(L, (int)i, (int)j, k0 + c);
+        const float bb = bscale ? bv[c] * d : bv[c];
+        o[c] = d > 0.f ? bb / d : 0.f;
+      }
+    } else {
+      const float4 xq = *reinterpret_cast<const float4 *>(x + r);
+      const float xv[4] = {xq.x, xq.y, xq.z, xq.w};
+      const bool im = i > 0, ip = (int)i < L.nx - 1, jm = j > 0, jp = (int)j < L.ny - 1;
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 xm = im ? *reinterpret_cast<const float4 *>(x + r - sx) : z4;
+      const float4 xp = ip ? *reinterpret_cast<const float4 *>(x + r + sx) : z4;
+      const float4 ym = jm ? *reinterpret_cast<const float4 *>(x + r - L.nz) : z4;
+      const float4 yp = jp ? *reinterpret_cast<const float4 *>(x + r + L.nz) : z4;
+      const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+      const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
+      const float kl = k0 > 0 ? x[r - 1] : 0.f, kr = k0 + 4 < L.nz ? x[r + 4] : 0.f;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        o[c] = xv[c];
+        if ((c & 1) != t0) continue;
+        const int k = k0 + c;
+        float a = 0.f, e = 0.f, f = 0.f;
+        if (im) a += xmv[c];
+        if (ip) a += xpv[c];
+        if (jm) e += ymv[c];
+        if (jp) e += ypv[c];
+        if (k > 0) f += c == 0 ? kl : xv[c - 1];
+        if (k < L.nz - 1) f += c == 3 ? kr : xv[c + 1];
+        const float d = ldiag(L, (int)i, (int)j, k);
+        const float bb = bscale ? bv[c] * d : bv[c];
+        o[c] = d > 0.f ? (bb + (L.wx * a + L.wy * e + L.wz * f)) / d : 0.f;
+      }
+    }
+    *reinterpret_cast<float4 *>(x + r) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 // bc = average over each coarse cell's children of the fine residual b - A x
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel Cl, int bscale, const float *__restrict__ bf,
                                                         const float *__restrict__ xf, float *__restrict__ bc,
@@ -160,16 +221,18 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, int sweeps, int b
   for (int q = threadIdx.x; q < n; q += blockDim.x) x[q] = xs[q];
 }
 
-static void level_geometry(MgLevel &L, int nsm) {
+static void level_geometry(MgLevel &L, int nsm, bool quads) {
   L.bx = 1;
   while (L.bx < L.nz && L.bx < 32) L.bx *= 2;
   L.by = kBlock / L.bx;
   L.gx = (L.nz + L.bx - 1) / L.bx;
   L.gy = (L.ny + L.by - 1) / L.by;
   L.gz = std::max(1, std::min(L.nx, nsm * 8 / std::max(1, L.gx * L.gy)));
+  const long long nquads = (long long)L.nx * L.ny * (L.nz / 4);
+  L.qgrid = quads && L.nz % 4 == 0 ? (int)std::max(1LL, std::min((nquads + kBlock - 1) / kBlock, 8LL * nsm)) : 0;
 }
 
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, MgPlan *mg) {
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlan *mg) {
   *mg = MgPlan{};
   int l = 0;
   for (;;) {
@@ -180,7 +243,7 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, M
     L.wx = (float)(1.0 / (hx * hx));
     L.wy = (float)(1.0 / (hy * hy));
     L.wz = (float)(1.0 / (hz * hz));
-    level_geometry(L, nsm);
+    level_geometry(L, nsm, quads);
     const long long cells = (long long)nx * ny * nz;
     const int fx = nx % 2 == 0 ? 2 : 1, fy = ny % 2 == 0 ? 2 : 1, fz = nz % 2 == 0 ? 2 : 1;
     if (cells <= kMgCoarseCells || fx * fy * fz == 1 || l + 1 == kMgMaxLevels) {
@@ -213,7 +276,10 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float 
   auto grid = [&](int l) { return dim3(mg.lev[l].gx, mg.lev[l].gy, mg.lev[l].gz); };
   auto block = [&](int l) { return dim3(mg.lev[l].bx, mg.lev[l].by, 1); };
   auto smooth = [&](int l, int colour, int zero) {
-    k_mg_smooth<<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+    if (mg.lev[l].qgrid > 0)
+      k_mg_smooth4<<<mg.lev[l].qgrid, kBlock, 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+    else
+      k_mg_smooth<<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
   };
   for (int l = 0; l + 1 < n; ++l) {
     smooth(l, 0, 1);
