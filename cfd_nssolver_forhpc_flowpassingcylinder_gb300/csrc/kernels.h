@@ -130,6 +130,7 @@ struct MgLevel {
 struct MgPlan {
   int nlev;
   int coarse_sweeps;  // red-black sweeps of the coarsest solve
+  int tail;           // levels tail..nlev-1 run in one block's shared memory (tail >= 1); nlev: none
   MgLevel lev[kMgMaxLevels];
 };
 // levels of an nx x ny x nz grid with spacing hx, hy, hz (arrays left null); false when

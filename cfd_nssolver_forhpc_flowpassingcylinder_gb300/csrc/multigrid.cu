@@ -221,6 +221,119 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, int sweeps, int b
   for (int q = threadIdx.x; q < n; q += blockDim.x) x[q] = xs[q];
 }
 
+// ---- the small levels in one block: levels t..nlev-1 together hold at most kMgTailCells
+// cells, x and b of each in shared memory; the same smoothing, transfers and coarsest solve
+// as the per-level kernels (same arithmetic, same order), a barrier between phases where
+// the per-level path has a launch ----
+constexpr int kMgTailCells = 6144;  // 2 arrays of floats: 48 KB of shared memory
+
+__device__ __forceinline__ void cell_ijk(const MgLevel &L, int q, int &i, int &j, int &k) {
+  k = q % L.nz;
+  const int t = q / L.nz;
+  j = t % L.ny;
+  i = t / L.ny;
+}
+
+__device__ void blk_smooth(const MgLevel &L, int colour, int zero, const float *b, float *x) {
+  const int n = L.nx * L.ny * L.nz;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    int i, j, k;
+    cell_ijk(L, q, i, j, k);
+    if (((i + j + k) & 1) != colour) {
+      if (zero) x[q] = 0.f;
+      continue;
+    }
+    const float d = ldiag(L, i, j, k);
+    const float num = zero ? b[q] : b[q] + lnb(L, x, i, j, k, q);
+    x[q] = d > 0.f ? num / d : 0.f;
+  }
+  __syncthreads();
+}
+
+__device__ void blk_restrict(const MgLevel &F, const MgLevel &Cl, const float *bf, const float *xf, float *bc) {
+  const float inv = 1.0f / (float)(F.fx * F.fy * F.fz);
+  const int n = Cl.nx * Cl.ny * Cl.nz;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    int i, j, k;
+    cell_ijk(Cl, q, i, j, k);
+    float sum = 0.f;
+    for (int a = 0; a < F.fx; ++a)
+      for (int e = 0; e < F.fy; ++e)
+        for (int c = 0; c < F.fz; ++c) {
+          const int fi = i * F.fx + a, fj = j * F.fy + e, fk = k * F.fz + c;
+          const long long r = lrow(F, fi, fj, fk);
+          const float d = ldiag(F, fi, fj, fk);
+          sum += bf[r] - d * xf[r] + lnb(F, xf, fi, fj, fk, r);
+        }
+    bc[q] = sum * inv;
+  }
+  __syncthreads();
+}
+
+__device__ void blk_prolong(const MgLevel &F, const MgLevel &Cl, const float *xc, float *xf) {
+  const int n = F.nx * F.ny * F.nz;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    int i, j, k;
+    cell_ijk(F, q, i, j, k);
+    int ci[2], cj[2], ck[2];
+    float wi[2], wj[2], wk[2];
+    axis_taps(i, F.fx, Cl.nx, ci, wi);
+    axis_taps(j, F.fy, Cl.ny, cj, wj);
+    axis_taps(k, F.fz, Cl.nz, ck, wk);
+    float v = 0.f;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const float w = wi[a] * wj[e] * wk[c];
+          if (w != 0.f) v += w * xc[lrow(Cl, ci[a], cj[e], ck[c])];
+        }
+    xf[q] += v;
+  }
+  __syncthreads();
+}
+
+// x_t = V-cycle of levels t..nlev-1 on b_t (both in global memory, level t >= 1)
+__global__ void __launch_bounds__(1024) k_mg_tail(MgPlan mg, int t, const SolverScal *sc) {
+  if (sc->done) return;
+  extern __shared__ float sm[];
+  const int n = mg.nlev;
+  float *xs[kMgMaxLevels], *bs[kMgMaxLevels];
+  int off = 0;
+  for (int l = t; l < n; ++l) {
+    const int c = mg.lev[l].nx * mg.lev[l].ny * mg.lev[l].nz;
+    xs[l] = sm + off;
+    bs[l] = sm + off + c;
+    off += 2 * c;
+  }
+  const int nt = mg.lev[t].nx * mg.lev[t].ny * mg.lev[t].nz;
+  for (int q = threadIdx.x; q < nt; q += blockDim.x) bs[t][q] = mg.lev[t].b[q];
+  __syncthreads();
+  for (int l = t; l + 1 < n; ++l) {
+    blk_smooth(mg.lev[l], 0, 1, bs[l], xs[l]);
+    blk_smooth(mg.lev[l], 1, 0, bs[l], xs[l]);
+    blk_restrict(mg.lev[l], mg.lev[l + 1], bs[l], xs[l], bs[l + 1]);
+  }
+  {  // coarsest: x = 0, then red-black sweeps (k_mg_coarse)
+    const MgLevel &C = mg.lev[n - 1];
+    const int nc = C.nx * C.ny * C.nz;
+    for (int q = threadIdx.x; q < nc; q += blockDim.x) xs[n - 1][q] = 0.f;
+    __syncthreads();
+    for (int s = 0; s < mg.coarse_sweeps; ++s) {
+      blk_smooth(C, 0, 0, bs[n - 1], xs[n - 1]);
+      blk_smooth(C, 1, 0, bs[n - 1], xs[n - 1]);
+    }
+  }
+  for (int l = n - 2; l >= t; --l) {
+    blk_prolong(mg.lev[l], mg.lev[l + 1], xs[l + 1], xs[l]);
+    blk_smooth(mg.lev[l], 1, 0, bs[l], xs[l]);
+    blk_smooth(mg.lev[l], 0, 0, bs[l], xs[l]);
+  }
+  for (int q = threadIdx.x; q < nt; q += blockDim.x) mg.lev[t].x[q] = xs[t][q];
+}
+
 static void level_geometry(MgLevel &L, int nsm, bool quads) {
   L.bx = 1;
   while (L.bx < L.nz && L.bx < 32) L.bx *= 2;
@@ -262,12 +375,24 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
     ++l;
   }
   mg->nlev = l + 1;
+  // first level of the one-block tail: the smallest t >= 1 whose levels t..nlev-1 fit
+  mg->tail = mg->nlev;  // none
+  long long tail_cells = 0;
+  for (int t = mg->nlev - 1; t >= 1; --t) {
+    tail_cells += (long long)mg->lev[t].nx * mg->lev[t].ny * mg->lev[t].nz;
+    if (tail_cells > kMgTailCells) break;
+    mg->tail = t;
+  }
   const MgLevel &C = mg->lev[l];
   mg->coarse_sweeps = std::min(256, 16 + 2 * std::max(C.nx, std::max(C.ny, C.nz)));
   return (long long)C.nx * C.ny * C.nz <= kMgSharedCells;
 }
 
-int mg_vcycle_launches(const MgPlan &mg) { return 6 * (mg.nlev - 1) + 1; }
+// per level above the tail (or the coarsest): 2 smooths + restrict, prolong + 2 smooths;
+// then one tail (or coarsest) kernel
+int mg_vcycle_launches(const MgPlan &mg) {
+  return mg.tail < mg.nlev ? 6 * mg.tail + 1 : 6 * (mg.nlev - 1) + 1;
+}
 
 void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float *b0, float *x0, const SolverScal *sc) {
   const int n = mg.nlev;
@@ -281,16 +406,28 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float 
     else
       k_mg_smooth<<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
   };
-  for (int l = 0; l + 1 < n; ++l) {
+  const int m = std::min(mg.tail, n);  // levels m..n-1 run in one block (m < n), or none
+  for (int l = 0; l + 1 < m; ++l) {
     smooth(l, 0, 1);
     smooth(l, 1, 0);
     k_mg_restrict<<<grid(l + 1), block(l + 1), 0, s>>>(mg.lev[l], mg.lev[l + 1], l == 0 ? jacobi : 0, B(l), X(l),
                                                          mg.lev[l + 1].b, sc);
   }
-  const MgLevel &C = mg.lev[n - 1];
-  const size_t smem = 2 * sizeof(float) * (size_t)C.nx * C.ny * C.nz;
-  k_mg_coarse<<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
-  for (int l = n - 2; l >= 0; --l) {
+  if (m < n) {
+    // levels m-1 -> m: smooth and restrict as above, then the tail
+    smooth(m - 1, 0, 1);
+    smooth(m - 1, 1, 0);
+    k_mg_restrict<<<grid(m), block(m), 0, s>>>(mg.lev[m - 1], mg.lev[m], m == 1 ? jacobi : 0, B(m - 1), X(m - 1),
+                                                 mg.lev[m].b, sc);
+    size_t cells = 0;
+    for (int l = m; l < n; ++l) cells += (size_t)mg.lev[l].nx * mg.lev[l].ny * mg.lev[l].nz;
+    k_mg_tail<<<1, 1024, 2 * sizeof(float) * cells, s>>>(mg, m, sc);
+  } else {
+    const MgLevel &C = mg.lev[n - 1];
+    const size_t smem = 2 * sizeof(float) * (size_t)C.nx * C.ny * C.nz;
+    k_mg_coarse<<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
+  }
+  for (int l = (m < n ? m : n - 1) - 1; l >= 0; --l) {
     k_mg_prolong<<<grid(l), block(l), 0, s>>>(mg.lev[l], mg.lev[l + 1], X(l + 1), X(l), sc);
     smooth(l, 1, 0);
     smooth(l, 0, 0);
