@@ -20,16 +20,18 @@ __device__ __forceinline__ void quick_a(double Up, double Un, long long pp, long
                                         const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
+  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q]); };  // a / Ds[q]
   if (Up > 0.0)
-    P = 0.5 * (fc + fp) - div_by(0.125 * Di[I + 1] * Di[I + 1], Ds[I], rDs[I]) * (div_by((fp - fc), Di[I + 1], rDi[I + 1]) - div_by((fc - fn), Di[I], rDi[I]));
+    P = 0.5 * (fc + fp) - os(0.125 * Di[I + 1] * Di[I + 1], I) * (oi(fp - fc, I + 1) - oi(fc - fn, I));
   else
     P = 0.5 * (fc + fp) -
-        div_by(0.125 * Di[I + 1] * Di[I + 1], Ds[I + 1], rDs[I + 1]) * (div_by((phi[pp] - fp), Di[I + 2], rDi[I + 2]) - div_by((fp - fc), Di[I + 1], rDi[I + 1]));
+        os(0.125 * Di[I + 1] * Di[I + 1], I + 1) * (oi(phi[pp] - fp, I + 2) - oi(fp - fc, I + 1));
   if (Un > 0.0)
     N = 0.5 * (fn + fc) -
-        div_by(0.125 * Di[I] * Di[I], Ds[I - 1], rDs[I - 1]) * (div_by((fc - fn), Di[I], rDi[I]) - div_by((fn - phi[nn]), Di[I - 1], rDi[I - 1]));
+        os(0.125 * Di[I] * Di[I], I - 1) * (oi(fc - fn, I) - oi(fn - phi[nn], I - 1));
   else
-    N = 0.5 * (fn + fc) - div_by(0.125 * Di[I] * Di[I], Ds[I], rDs[I]) * (div_by((fp - fc), Di[I + 1], rDi[I + 1]) - div_by((fc - fn), Di[I], rDi[I]));
+    N = 0.5 * (fn + fc) - os(0.125 * Di[I] * Di[I], I) * (oi(fp - fc, I + 1) - oi(fc - fn, I));
 }
 
 // inc/source/Convection_Difussion.hpp:55-90 (QuickUnitB)
@@ -39,16 +41,18 @@ __device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long
                                         const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
+  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q]); };  // a / Ds[q]
   if (Up > 0.0)
-    P = 0.5 * (fc + fp) - div_by(0.125 * Ds[I] * Ds[I], Di[I], rDi[I]) * (div_by((fp - fc), Ds[I], rDs[I]) - div_by((fc - fn), Ds[I - 1], rDs[I - 1]));
+    P = 0.5 * (fc + fp) - oi(0.125 * Ds[I] * Ds[I], I) * (os(fp - fc, I) - os(fc - fn, I - 1));
   else
     P = 0.5 * (fc + fp) -
-        div_by(0.125 * Ds[I] * Ds[I], Di[I + 1], rDi[I + 1]) * (div_by((phi[pp] - fp), Ds[I + 1], rDs[I + 1]) - div_by((fp - fc), Ds[I], rDs[I]));
+        oi(0.125 * Ds[I] * Ds[I], I + 1) * (os(phi[pp] - fp, I + 1) - os(fp - fc, I));
   if (Un > 0.0)
     N = 0.5 * (fn + fc) -
-        div_by(0.125 * Ds[I - 1] * Ds[I - 1], Di[I - 1], rDi[I - 1]) * (div_by((fc - fn), Ds[I - 1], rDs[I - 1]) - div_by((fn - phi[nn]), Ds[I - 2], rDs[I - 2]));
+        oi(0.125 * Ds[I - 1] * Ds[I - 1], I - 1) * (os(fc - fn, I - 1) - os(fn - phi[nn], I - 2));
   else
-    N = 0.5 * (fn + fc) - div_by(0.125 * Ds[I - 1] * Ds[I - 1], Di[I], rDi[I]) * (div_by((fp - fc), Ds[I], rDs[I]) - div_by((fc - fn), Ds[I - 1], rDs[I - 1]));
+    N = 0.5 * (fn + fc) - oi(0.125 * Ds[I - 1] * Ds[I - 1], I) * (os(fp - fc, I) - os(fc - fn, I - 1));
 }
 
 // inc/source/Convection_Difussion.hpp:96-147 (LudUnitA; LudUnitB has the same body)
@@ -57,14 +61,15 @@ __device__ __forceinline__ void lud(double Up, double Un, long long pp, long lon
                                     const double *__restrict__ rDi, const double *__restrict__ rDs, int I,
                                     const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
   if (Up > 0.0)
-    P = (fc + div_by(0.5 * Ds[I] * (fc - fn), Di[I], rDi[I]));
+    P = (fc + oi(0.5 * Ds[I] * (fc - fn), I));
   else
-    P = (fp + div_by(0.5 * Ds[I + 1] * (fp - phi[pp]), Di[I + 1], rDi[I + 1]));
+    P = (fp + oi(0.5 * Ds[I + 1] * (fp - phi[pp]), I + 1));
   if (Un > 0.0)
-    N = (fn + div_by(0.5 * Ds[I - 1] * (fn - phi[nn]), Di[I - 1], rDi[I - 1]));
+    N = (fn + oi(0.5 * Ds[I - 1] * (fn - phi[nn]), I - 1));
   else
-    N = (fc + div_by(0.5 * Ds[I] * (fc - fp), Di[I + 1], rDi[I + 1]));
+    N = (fc + oi(0.5 * Ds[I] * (fc - fp), I + 1));
 }
 
 // face values of one axis under the convection switch (inc/0_General.hpp:114-118): QUICK,
@@ -100,12 +105,16 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
-    const double ux = div_by(0.5, g.Dxs[i], g.rDxs[i]) * (u[c - sx] - u[c + sx]), uy = div_by(0.5, g.Dy[j], g.rDy[j]) * (u[c - sy] - u[c + sy]),
-                 uz = div_by(0.5, g.Dz[k], g.rDz[k]) * (u[c - 1] - u[c + 1]);
-    const double vx = div_by(0.5, g.Dx[i], g.rDx[i]) * (v[c - sx] - v[c + sx]), vy = div_by(0.5, g.Dys[j], g.rDys[j]) * (v[c - sy] - v[c + sy]),
-                 vz = div_by(0.5, g.Dz[k], g.rDz[k]) * (v[c - 1] - v[c + 1]);
-    const double wx = div_by(0.5, g.Dx[i], g.rDx[i]) * (w[c - sx] - w[c + sx]), wy = div_by(0.5, g.Dy[j], g.rDy[j]) * (w[c - sy] - w[c + sy]),
-                 wz = div_by(0.5, g.Dzs[k], g.rDzs[k]) * (w[c - 1] - w[c + 1]);
+    auto h = [&](double d, double r) { return div_by(0.5, d, r); };  // 0.5 / d
+    const double ux = h(g.Dxs[i], g.rDxs[i]) * (u[c - sx] - u[c + sx]);
+    const double uy = h(g.Dy[j], g.rDy[j]) * (u[c - sy] - u[c + sy]);
+    const double uz = h(g.Dz[k], g.rDz[k]) * (u[c - 1] - u[c + 1]);
+    const double vx = h(g.Dx[i], g.rDx[i]) * (v[c - sx] - v[c + sx]);
+    const double vy = h(g.Dys[j], g.rDys[j]) * (v[c - sy] - v[c + sy]);
+    const double vz = h(g.Dz[k], g.rDz[k]) * (v[c - 1] - v[c + 1]);
+    const double wx = h(g.Dx[i], g.rDx[i]) * (w[c - sx] - w[c + sx]);
+    const double wy = h(g.Dy[j], g.rDy[j]) * (w[c - sy] - w[c + sy]);
+    const double wz = h(g.Dzs[k], g.rDzs[k]) * (w[c - 1] - w[c + 1]);
     const double a = uy + vx, b = uz + wx, e = vz + wy;
     const double temp = fabs(2.0 * (ux * ux) + vy * vy + wz * wz + a * a + b * b + e * e);
     nut[row] = l2[row] * sqrt(temp);
@@ -129,6 +138,13 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
   const long long sx = g.sx, sy = g.sy, sz = 1;
   const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
   const double *rDx = g.rDx, *rDy = g.rDy, *rDz = g.rDz, *rDxs = g.rDxs, *rDys = g.rDys, *rDzs = g.rDzs;
+  // a / D[q] of each metric array (div_by with the array's reciprocals)
+  auto ox = [&](double a, int q) { return div_by(a, Dx[q], rDx[q]); };
+  auto oy = [&](double a, int q) { return div_by(a, Dy[q], rDy[q]); };
+  auto oz = [&](double a, int q) { return div_by(a, Dz[q], rDz[q]); };
+  auto oxs = [&](double a, int q) { return div_by(a, Dxs[q], rDxs[q]); };
+  auto oys = [&](double a, int q) { return div_by(a, Dys[q], rDys[q]); };
+  auto ozs = [&](double a, int q) { return div_by(a, Dzs[q], rDzs[q]); };
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
@@ -137,7 +153,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
     const double nu = nut ? nu0 + nut[row] : nu0;
     const long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz, zp = ic + sz;
     if (i < g.nx - 3) {  // u
-      const double IT = div_by((Dxs[i] * 0.5), Dx[i], rDx[i]);
+      const double IT = ox(Dxs[i] * 0.5, i);
       const double uc = u[ic], uxp = u[xp], uxm = u[xm];
       const double Up = 0.5 * (uxp + uc);
       const double Un = 0.5 * (uxm + uc);
@@ -149,17 +165,17 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       face<S, true>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, u, uPx, uNx);
       face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, u, uPy, uNy);
       face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, u, uPz, uNz);
-      const double convection = -dt * (div_by((uPx * uPx - uNx * uNx), Dxs[i], rDxs[i]) + div_by((uPy * Vp - uNy * Vn), Dy[j], rDy[j]) +
-                                       div_by((uPz * Wp - uNz * Wn), Dz[k], rDz[k]));
+      const double convection = -dt * (oxs(uPx * uPx - uNx * uNx, i) + oy(uPy * Vp - uNy * Vn, j) +
+                                       oz(uPz * Wp - uNz * Wn, k));
       const double difussion =
           nu * dt *
-          (div_by((div_by((uxp - uc), Dx[i + 1], rDx[i + 1]) - div_by((uc - uxm), Dx[i], rDx[i])), Dxs[i], rDxs[i]) +
-           div_by((div_by((u[yp] - uc), Dys[j], rDys[j]) - div_by((uc - u[ym]), Dys[j - 1], rDys[j - 1])), Dy[j], rDy[j]) +
-           div_by((div_by((u[zp] - uc), Dzs[k], rDzs[k]) - div_by((uc - u[zm]), Dzs[k - 1], rDzs[k - 1])), Dz[k], rDz[k]));
+          (oxs(ox(uxp - uc, i + 1) - ox(uc - uxm, i), i) +
+           oy(oys(u[yp] - uc, j) - oys(uc - u[ym], j - 1), j) +
+           oz(ozs(u[zp] - uc, k) - ozs(uc - u[zm], k - 1), k));
       us[ic] = uc + convection + difussion;
     }
     if (j < g.ny - 3) {  // v
-      const double IT = div_by((Dys[j] * 0.5), Dy[j], rDy[j]);
+      const double IT = oy(Dys[j] * 0.5, j);
       const double vc = v[ic], vyp = v[yp], vym = v[ym];
       const double Vp = 0.5 * (vyp + vc);
       const double Vn = 0.5 * (vym + vc);
@@ -171,17 +187,17 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, v, vPx, vNx);
       face<S, true>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, v, vPy, vNy);
       face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, v, vPz, vNz);
-      const double convection = -dt * (div_by((Up * vPx - Un * vNx), Dx[i], rDx[i]) + div_by((vPy * vPy - vNy * vNy), Dys[j], rDys[j]) +
-                                       div_by((Wp * vPz - Wn * vNz), Dz[k], rDz[k]));
+      const double convection = -dt * (ox(Up * vPx - Un * vNx, i) + oys(vPy * vPy - vNy * vNy, j) +
+                                       oz(Wp * vPz - Wn * vNz, k));
       const double difussion =
           nu * dt *
-          (div_by((div_by((v[xp] - vc), Dxs[i], rDxs[i]) - div_by((vc - v[xm]), Dxs[i - 1], rDxs[i - 1])), Dx[i], rDx[i]) +
-           div_by((div_by((vyp - vc), Dy[j + 1], rDy[j + 1]) - div_by((vc - vym), Dy[j], rDy[j])), Dys[j], rDys[j]) +
-           div_by((div_by((v[zp] - vc), Dzs[k], rDzs[k]) - div_by((vc - v[zm]), Dzs[k - 1], rDzs[k - 1])), Dz[k], rDz[k]));
+          (ox(oxs(v[xp] - vc, i) - oxs(vc - v[xm], i - 1), i) +
+           oys(oy(vyp - vc, j + 1) - oy(vc - vym, j), j) +
+           oz(ozs(v[zp] - vc, k) - ozs(vc - v[zm], k - 1), k));
       vs[ic] = vc + convection + difussion;
     }
     if (k < g.nz - 3) {  // w
-      const double IT = div_by((Dzs[k] * 0.5), Dz[k], rDz[k]);
+      const double IT = oz(Dzs[k] * 0.5, k);
       const double wc = w[ic], wzp = w[zp], wzm = w[zm];
       const double Wp = 0.5 * (wzp + wc);
       const double Wn = 0.5 * (wzm + wc);
@@ -193,13 +209,13 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
       face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, w, wPx, wNx);
       face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, w, wPy, wNy);
       face<S, true>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, w, wPz, wNz);
-      const double convection = -dt * (div_by((Up * wPx - Un * wNx), Dx[i], rDx[i]) + div_by((Vp * wPy - Vn * wNy), Dy[j], rDy[j]) +
-                                       div_by((wPz * wPz - wNz * wNz), Dzs[k], rDzs[k]));
+      const double convection = -dt * (ox(Up * wPx - Un * wNx, i) + oy(Vp * wPy - Vn * wNy, j) +
+                                       ozs(wPz * wPz - wNz * wNz, k));
       const double difussion =
           nu * dt *
-          (div_by((div_by((w[xp] - wc), Dxs[i], rDxs[i]) - div_by((wc - w[xm]), Dxs[i - 1], rDxs[i - 1])), Dx[i], rDx[i]) +
-           div_by((div_by((w[yp] - wc), Dys[j], rDys[j]) - div_by((wc - w[ym]), Dys[j - 1], rDys[j - 1])), Dy[j], rDy[j]) +
-           div_by((div_by((wzp - wc), Dz[k + 1], rDz[k + 1]) - div_by((wc - wzm), Dz[k], rDz[k])), Dzs[k], rDzs[k]));
+          (ox(oxs(w[xp] - wc, i) - oxs(wc - w[xm], i - 1), i) +
+           oy(oys(w[yp] - wc, j) - oys(wc - w[ym], j - 1), j) +
+           ozs(oz(wzp - wc, k + 1) - oz(wc - wzm, k), k));
       ws[ic] = wc + convection + difussion;
     }
   }
