@@ -119,10 +119,23 @@ KERNEL_FP64_FLOPS = {"bicg_ap64": 15, "bicg_s64": 2, "bicg_as64": 17, "bicg_xr64
                      "cg_q64": 15, "cg_xr64": 6, "cg_p64": 2}
 
 
+FP_PEAK_SRC = ROOT / "bench_fp_peak.cu"
+FP_PEAK_EXE = ROOT / "bench_fp_peak"
+
+
+def build_fp_peak(force=False):
+    """Compile the FMA throughput probe beside this script (sm_103a); returns its path."""
+    if force or not FP_PEAK_EXE.exists() or FP_PEAK_EXE.stat().st_mtime < FP_PEAK_SRC.stat().st_mtime:
+        from cfd_nssolver_forhpc_flowpassingcylinder_gb300.build import nvcc
+        subprocess.run([nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", str(FP_PEAK_SRC), "-o",
+                        str(FP_PEAK_EXE)], check=True, capture_output=True)
+    return FP_PEAK_EXE
+
+
 def alu_peaks():
-    """FP64/FP32 FMA throughput of this GPU, measured by the package's cfdgb_fp_peak."""
-    exe = ROOT / "cfd_nssolver_forhpc_flowpassingcylinder_gb300" / "cfdgb_fp_peak"
+    """FP64/FP32 FMA throughput of this GPU, measured by the probe bench_fp_peak.cu."""
     try:
+        exe = build_fp_peak()
         out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout
         return json.loads(out.strip().splitlines()[-1])
     except Exception as e:  # binary missing or no GPU
@@ -138,7 +151,7 @@ def alu_roofline(prof, cells, fp_peak):
     achieved = KERNEL_FP64_FLOPS[dom] * cells / (ms / n / 1e3) / 1e12
     return {"kernel": dom, "bound": "fp64", "achieved": round(achieved, 4), "peak": fp_peak["fp64_tflops"],
             "unit": "TFLOP/s", "frac": round(achieved / fp_peak["fp64_tflops"], 4),
-            "peak_kind": "measured (cfdgb_fp_peak FMA chains)"}
+            "peak_kind": "measured (bench_fp_peak FMA chains)"}
 
 
 def peaks():
@@ -454,13 +467,50 @@ def reference_iteration_record(wl):
 
 def reference_window_iters(rec, warmup, steps):
     """The reference's recorded iteration counts on the timed steps warmup+1 .. warmup+steps
-    (1-based; the record's index 0 is step 1), and how many of those steps lie beyond the
-    record (filled with the mean over its solve steps)."""
+    (1-based; the record's index 0 is step 1).  Nothing is imputed: a window that reaches
+    beyond the record raises ValueError, naming how many timed steps it lacks."""
     its = rec["iters"]
-    solves = its[1:]
-    mean = sum(solves) / len(solves)
-    want = [its[i] if i < len(its) else mean for i in range(warmup, warmup + steps)]
-    return want, sum(1 for i in range(warmup, warmup + steps) if i >= len(its))
+    missing = warmup + steps - len(its)
+    if missing > 0:
+        raise ValueError(f"the recorded reference run ends at step {len(its)}; the timed window "
+                         f"(steps {warmup + 1}-{warmup + steps}) lacks {missing} recorded steps")
+    return [its[i] for i in range(warmup, warmup + steps)]
+
+
+def window_record(rec, warmup, steps, cap, sampled_steps):
+    """What the reference arm's number rests on: the recorded steps it is scored on, how
+    many were imputed (always 0: a short record makes the arm unavailable), the steps the
+    timing sample ran and its iteration cap."""
+    return {"recorded_steps": [warmup + 1, warmup + steps], "record_length": len(rec["iters"]),
+            "record_threads": rec.get("threads"), "record_host": rec.get("host"), "imputed_steps": 0,
+            "sampled_steps": [1, sampled_steps], "cap": cap}
+
+
+def bench_config(wl, maxit, world):
+    """The config both arms print: the workload, its solver, tolerance and cap, the boundary
+    set, the replica count and the L2 note."""
+    return {**config_of(wl), "maxit": maxit, "bc": "reference (FLOWpassing table)",
+            "parallelism": f"replicas x{world}", "l2": l2_note(wl)}
+
+
+def reference_baseline(wl, warmup, steps, cap, cap1):
+    """The reference's CPU throughput on the timed window: all host cores and one thread,
+    each from a bounded timing sample (3 steps, BiCGSTAB capped) scored on the iteration
+    counts of the recorded full reference run.  Raises when there is no record or it does
+    not cover the window."""
+    rec = reference_iteration_record(wl)
+    if rec is None:
+        raise ValueError(f"no recorded reference iteration counts for workload {wl}")
+    want = reference_window_iters(rec, warmup, steps)
+    threads = os.cpu_count() or 1
+    cb = cpu_reference_sample(wl, 3, cap, threads, want)
+    c1 = cpu_reference_sample(wl, 3, cap1, 1, want)
+    out = {"value": cb["value"], "unit": "cell-steps/s", "cores": threads, "kind": "reference",
+           "sample": SAMPLE_DOC.format(cap=cap, t_iter=cb["t_iter_s"], t_other=cb["t_other_s"]),
+           "window": window_record(rec, warmup, steps, cap, 3),
+           "single_thread": {"value": c1["value"], "unit": "cell-steps/s", "cores": 1, "cap": cap1,
+                             "t_iter_s": c1["t_iter_s"], "t_other_s": c1["t_other_s"]}}
+    return out
 
 
 def main_reference(args):
@@ -468,31 +518,50 @@ def main_reference(args):
     world, rank, _ = _dist()
     if rank != 0:
         return 0
-    rec = reference_iteration_record(args.workload)
-    threads = os.cpu_count() or 1
-    steps = args.warmup + args.steps
-    iters = None if rec is None else reference_window_iters(rec, args.warmup, args.steps)[0]
-    if iters is None:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded reference iteration counts"}))
+    try:
+        cb = reference_baseline(args.workload, args.warmup, args.steps, args.cap, args.cap1)
+    except (ValueError, FileNotFoundError, subprocess.CalledProcessError) as e:
+        print(json.dumps({"impl": "reference", "unavailable": str(e)}))
         return 0
-    r = cpu_reference_sample(args.workload, min(steps, 3), args.cap, threads, iters)
-    line = {"impl": "reference", "metric": metric(args.workload), "value": r["value"], "unit": "cell-steps/s",
+    line = {"impl": "reference", "metric": metric(args.workload), "value": cb["value"], "unit": "cell-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * r["cells"] / r["value"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state)",
-            "config": config_of(args.workload),
-            "cpu_baseline": {"value": r["value"], "unit": "cell-steps/s", "cores": threads, "kind": "reference",
-                             "sample": SAMPLE_DOC.format(cap=args.cap, t_iter=r["t_iter_s"], t_other=r["t_other_s"])},
-            "e2e": {"value": r["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "ms_per_step": 1e3 * cells_of(args.workload) / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (reference initial state u=1, v=w=0)",
+            "config": bench_config(args.workload, args.maxit, args.gpus),
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def cells_of(wl):
+    cfg = WORKLOADS[wl]
+    return cfg["nx"] * cfg["ny"] * cfg["nz"]
+
+
+def solve_record(stats, tol):
+    """Per-step solve outcome of a timed window: iterations, final relative residual and
+    status of every step, the solves that hit the iteration cap and the solves that ended
+    at or above the tolerance (step 1 of a run has no solve and is not counted)."""
+    solves = [r for r in stats if r.step > 1]
+    return {"step": [r.step for r in stats], "iters": [r.iters for r in stats],
+            "relres": [r.relres for r in stats], "status": [r.status for r in stats],
+            "capped_solves": sum(1 for r in solves if r.status == -3),
+            "unconverged_solves": sum(1 for r in solves if not (r.relres < tol))}
+
+
+def solve_counts(stats, tol):
+    r = solve_record(stats, tol)
+    return {"capped_solves": r["capped_solves"], "unconverged_solves": r["unconverged_solves"]}
 
 
 METRIC = "cell-steps/s @resid 1e-8 (FP64 Jacobi-BiCGSTAB projection step)"
 SAMPLE_DOC = ("reference OpenMP build (-O3 -fopenmp -march=native) on the same grid, steps 1-3 with its "
               "BiCGSTAB capped at {cap} iterations: {t_iter:.4f} s per iteration, {t_other:.3f} s per step "
-              "outside the solve; cell-steps/s at the iteration counts the reference itself needs to reach "
-              "1e-8 on the timed steps (recorded from a full reference run, tests/golden/reference_iters_<wl>.json)")
+              "outside the solve; cell-steps/s at the iteration counts the reference itself needed to reach "
+              "the tolerance on exactly the timed steps, recorded from a full reference run "
+              "(tests/golden/reference_iters_<workload>.json; none imputed)")
 
 
 def main(argv=None):
@@ -513,6 +582,8 @@ def main(argv=None):
     ap.add_argument("--fd-steps", type=int, default=21, help="adjoint_fd mode: steps of each forward run")
     ap.add_argument("--fd-dirs", type=int, default=16, help="adjoint_fd mode: directions per gradient")
     ap.add_argument("--cap", type=int, default=10, help="reference BiCGSTAB iteration cap of the CPU sample")
+    ap.add_argument("--cap1", type=int, default=4,
+                    help="reference BiCGSTAB iteration cap of the single-thread CPU sample")
     ap.add_argument("--sor-steps", type=int, default=2)
     ap.add_argument("--sor-maxit", type=int, default=20000)
     args = ap.parse_args(argv)
@@ -539,18 +610,23 @@ def main(argv=None):
     value = cells * args.steps * dist.world / (t64 / 1e3)
     roof, share = roofline(fp64["kernels"], cells, 8, "64", hbm_peak, peak_kind, traffic_file)
     iters64 = [r.iters for r in fp64["stats"]]
+    _, _, tol = workload(wl)
+    rec64 = solve_record(fp64["stats"], tol)
     line = {
         "metric": metric(wl), "value": value, "unit": "cell-steps/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t64 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial state u=1, v=w=0)",
-        "config": {**config_of(wl), "maxit": args.maxit,
-                   "bc": "reference (FLOWpassing table)", "parallelism": f"replicas x{dist.world}",
-                   "l2": l2_note(wl)},
+        "config": bench_config(wl, args.maxit, dist.world),
         "iters_per_step": iters64, "relres": max(r.relres for r in fp64["stats"]),
+        "solves": rec64,
         "gpu_launches": fp64["launches"], "roofline": roof, "kernel_share": share,
         "alu_roofline": alu_roofline(fp64["kernels"], cells, fp_peak), "fp_peaks": fp_peak,
         "clocks": clk.summary(), "device_mem_gb": fp64["device_mem_gb"],
     }
+    if rec64["unconverged_solves"]:
+        # the metric names the tolerance: say plainly that some timed solves missed it
+        line["failure"] = (f"{rec64['unconverged_solves']} of {args.steps} timed solves ended at or above "
+                           f"relres {tol:g} ({rec64['capped_solves']} at the {args.maxit}-iteration cap)")
     if "mixed" in modes:
         try:
             mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", maxit=args.maxit,
@@ -560,7 +636,7 @@ def main(argv=None):
             line["mixed"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
                              "iters_per_step": [r.iters for r in mx["stats"]],
                              "outer_per_step": [r.outer for r in mx["stats"]],
-                             "relres": max(r.relres for r in mx["stats"]), "speedup_vs_fp64": t64 / tm,
+                             "relres": max(r.relres for r in mx["stats"]), **solve_counts(mx["stats"], tol), "speedup_vs_fp64": t64 / tm,
                              "error_vs_fp64": field_errors(mx, fp64),
                              "gpu_launches": mx["launches"], "device_mem_gb": mx["device_mem_gb"],
                              "roofline": r32, "kernel_share": share32}
@@ -576,7 +652,7 @@ def main(argv=None):
                                 "solver": "jacobi bicgstab, FP32 sweeps right-preconditioned by a multigrid V-cycle",
                                 "iters_per_step": [r.iters for r in mg["stats"]],
                                 "outer_per_step": [r.outer for r in mg["stats"]],
-                                "relres": max(r.relres for r in mg["stats"]), "speedup_vs_fp64": t64 / tm,
+                                "relres": max(r.relres for r in mg["stats"]), **solve_counts(mg["stats"], tol), "speedup_vs_fp64": t64 / tm,
                                 "error_vs_fp64": field_errors(mg, fp64), "gpu_launches": mg["launches"],
                                 "device_mem_gb": mg["device_mem_gb"], "roofline": rg, "kernel_share": shg}
         except cg.CfdgbError as e:
@@ -594,7 +670,7 @@ def main(argv=None):
                          "solver": "cg (SPE operator)", "precision": prec,
                          "iters_per_step": [r.iters for r in rm["stats"]],
                          "outer_per_step": [r.outer for r in rm["stats"]],
-                         "relres": max(r.relres for r in rm["stats"]), "speedup_vs_fp64": t64 / tm,
+                         "relres": max(r.relres for r in rm["stats"]), **solve_counts(rm["stats"], tol), "speedup_vs_fp64": t64 / tm,
                          "error_vs_fp64": field_errors(rm, fp64), "gpu_launches": rm["launches"],
                          "device_mem_gb": rm["device_mem_gb"], "roofline": rf, "kernel_share": shr}
         except cg.CfdgbError as e:
@@ -623,17 +699,8 @@ def main(argv=None):
         except cg.CfdgbError as e:
             line["adjoint_fd"] = {"value": None, "error": str(e)}
     if "cpu" in modes and dist.rank == 0:
-        rec = reference_iteration_record(wl)
         try:
-            if rec is None:
-                raise RuntimeError("no recorded reference iteration counts")
-            want = reference_window_iters(rec, args.warmup, args.steps)[0]
-            threads = os.cpu_count() or 1
-            cb = cpu_reference_sample(wl, 3, args.cap, threads, want)
-            line["cpu_baseline"] = {"value": cb["value"], "unit": "cell-steps/s", "cores": threads,
-                                    "kind": "reference",
-                                    "sample": SAMPLE_DOC.format(cap=args.cap, t_iter=cb["t_iter_s"],
-                                                                t_other=cb["t_other_s"])}
+            line["cpu_baseline"] = reference_baseline(wl, args.warmup, args.steps, args.cap, args.cap1)
         except Exception as e:  # reference binary or record unavailable on this host
             line["cpu_baseline"] = {"value": None, "unit": "cell-steps/s", "cores": os.cpu_count(),
                                     "kind": "reference", "sample": f"unavailable: {e}"}

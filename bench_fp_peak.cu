@@ -1,4 +1,4 @@
-// cfdgb_fp_peak: measures the FP64 and FP32 fused multiply-add throughput of the current
+// bench_fp_peak: measures the FP64 and FP32 fused multiply-add throughput of the current
 // GPU (the ALU roof of the FP64 solver kernels).  Eight independent FMA chains per thread,
 // 8 blocks of 256 threads per SM, timed with CUDA events after a warm-up launch.
 // Prints one JSON object: {"fp64_tflops": ..., "fp32_tflops": ..., "sms": ..., "name": ...}.

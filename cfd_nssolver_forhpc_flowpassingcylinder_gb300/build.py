@@ -73,12 +73,6 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr[-4000:])
         os.replace(tmp, LIB)
-    peak = PKG / "cfdgb_fp_peak"
-    peak_src = CSRC / "fp_peak.cu"
-    if force or _stale(peak, [peak_src]):
-        r = subprocess.run([nvcc(), *ARCH, "-O3", str(peak_src), "-o", str(peak)], capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("cfdgb_fp_peak build failed:\n" + r.stderr[-4000:])
     cli = PKG / "cfdgb_run"
     cli_src = CSRC / "cfdgb_run.cpp"
     if force or _stale(cli, [cli_src, LIB, ROOT / "include" / "cfdgb.hpp"]):

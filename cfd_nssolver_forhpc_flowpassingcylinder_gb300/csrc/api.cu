@@ -894,14 +894,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.cof[0] = rows;
     g.cof[1] = rows + 7 * c->ncell;
   }
-  // solver launch geometry: k along x (up to a warp), j along y, i strided over grid z.
-  // From 8 k cells up, the width among 8, 16, 32 that leaves the fewest idle lanes at
-  // the end of a k line (40 cells: 8 wide, where 32 would idle 24 of every 64 lanes)
-  g.lbx = 1;
-  while (g.lbx < cfg->nz && g.lbx < 32) g.lbx *= 2;
-  auto idle = [](int n, int w) { return (n + w - 1) / w * w - n; };
-  for (int w = 16; w >= 8 && cfg->nz >= 8; w /= 2)
-    if (idle(cfg->nz, w) < idle(cfg->nz, g.lbx)) g.lbx = w;
+  // solver launch geometry: k along x (k_block_width), j along y, i strided over grid z
+  g.lbx = k_block_width(cfg->nz);
   g.lby = kBlock / g.lbx;
   g.lgx = (cfg->nz + g.lbx - 1) / g.lbx;
   g.lgy = (cfg->ny + g.lby - 1) / g.lby;

@@ -52,6 +52,20 @@ struct Geo {
   const double *rDx, *rDy, *rDz, *rDxs, *rDys, *rDzs, *hfx, *hfy, *hfz;
 };
 
+// Width along k of the 3-D solver blocks (host side; the context driver and the
+// allocation-free solve share it, so both launch the same shape and reduce in the same
+// order): the next power of two up to a warp, then, from 8 k cells up, the width among
+// 8, 16 and 32 that leaves the fewest idle lanes at the end of a k line (40 cells: 8 wide,
+// where 32 would idle 24 of every 64 lanes).
+inline int k_block_width(int nz) {
+  int w = 1;
+  while (w < nz && w < 32) w *= 2;
+  auto idle = [](int n, int b) { return (n + b - 1) / b * b - n; };
+  for (int c = 16; c >= 8 && nz >= 8; c /= 2)
+    if (idle(nz, c) < idle(nz, w)) w = c;
+  return w;
+}
+
 // a / b correctly rounded, given y = RN(1/b): q = RN(a y) lies within an ulp of a / b, so
 // the remainder a - b q is exact in one FMA and RN(q + (a - b q) y) = RN(a / b) (Markstein's
 // theorem: P. Markstein, IBM J. Res. Develop. 34(1), 1990; J.-M. Muller et al., Handbook of

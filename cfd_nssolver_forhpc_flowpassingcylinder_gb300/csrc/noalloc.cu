@@ -1,25 +1,28 @@
 // cfdgb_poisson_solve_static: the BiCGSTAB pressure solve for callers that cannot
 // allocate device memory.
 //
-// Who needs it: code that runs while a CUDA stream is being captured into a graph
-// (cudaMalloc is not permitted during capture), callers inside a host framework that owns
-// all device memory through its own pool and forbids raw allocations, and real-time or
-// long-running services that must not allocate after start-up.  Such a caller passes its
-// own device buffers for the right-hand side and the solution; every work vector, block
-// partial and solver scalar lives in one file-scope static device array, so the call makes
-// no cudaMalloc/cudaFree and no allocating library call.
+// Who needs it: callers inside a host framework that owns all device memory through its
+// own pool and forbids raw allocations, and real-time or long-running services that must
+// not allocate after start-up.  Such a caller passes its own device buffers for the
+// right-hand side and the solution; every work vector, block partial and solver scalar
+// lives in one file-scope static device array, so the call makes no cudaMalloc/cudaFree
+// and no allocating library call.
 //
 // Limits and sharing:
-//   - at most kStaticMaxCells unknowns (64^3); larger grids are rejected with CFDGB_EINVAL;
-//   - the array is reserved on every GPU that loads the library, until the process exits
-//     (about 16.3 MB);
+//   - at most kStaticMaxCells unknowns (2^18, e.g. 64^3); larger grids are rejected with
+//     CFDGB_EINVAL;
+//   - the array is reserved on every GPU that loads the library, until the process exits:
+//     8 work vectors of 2 MiB, 256 KiB of block partials and 256 B of solver scalars,
+//     17,039,616 bytes (about 17.0 MB, kScratchBytes);
 //   - all calls share it and it keeps the last call's contents: each call clears the
 //     solver scalars and reduction tickets it relies on before it starts, but two calls
 //     whose work overlaps on the GPU (different streams or threads at the same time) race
 //     on it and must not be issued;
+//   - the call polls the solver's convergence from the host every 8 iterations (a
+//     device-to-host copy and a wait on `stream`), so `stream` must not be capturing into a
+//     CUDA graph: a capturing stream is rejected with CFDGB_EINVAL before any work;
 //   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, cached); make that first call before any
-//     stream capture begins.
+//     cudaGetSymbolAddress (once per device, cached).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,11 +39,12 @@ using namespace cfdgb;
 
 constexpr long long kStaticMaxCells = 1LL << 18;  // 262,144 unknowns, e.g. 64 x 64 x 64
 constexpr int kStaticMaxBlocks = 4096;            // reduction partials per vector
-constexpr int kStaticVectors = 9;                 // x-history x2, r0 r1 p1 s ap as + spare
+constexpr int kStaticVectors = 8;                 // x-history x2, r0 r1 p1 s ap as
 constexpr size_t kVecBytes = kStaticMaxCells * sizeof(double);
 constexpr size_t kPartBytes = 8 * kStaticMaxBlocks * sizeof(double);
 constexpr size_t kScalBytes = (sizeof(SolverScal) + 255) / 256 * 256;
 constexpr size_t kScratchBytes = kStaticVectors * kVecBytes + kPartBytes + kScalBytes;
+static_assert(kScalBytes == 256 && kScratchBytes == 17039616, "the documented size of the static array");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
@@ -124,20 +128,24 @@ extern "C" int cfdgb_poisson_solve_static(int nx, int ny, int nz, double dx, dou
   const long long n = (long long)nx * ny * nz;
   if (n > kStaticMaxCells) return CFDGB_EINVAL;  // the static work array holds 2^18 unknowns
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the convergence polls wait on the stream: a stream that is being captured cannot run them
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return CFDGB_ECUDA;
+  if (cap != cudaStreamCaptureStatusNone) return CFDGB_EINVAL;
   unsigned char *base = nullptr;
   if (scratch_address(&base) != cudaSuccess) return CFDGB_ECUDA;
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return CFDGB_ECUDA;
-  // geometry: the same launch shape the context driver uses
+  // geometry: the launch shape of the context driver's solver kernels (k_block_width and
+  // the same grid), so the reductions sum in the same order
   Geo g{};
   g.nxc = nx; g.nyc = ny; g.nzc = nz;
   g.nx = nx + 4; g.ny = ny + 4; g.nz = nz + 4;
   g.sx = (long long)g.ny * g.nz; g.sy = g.nz;
   g.ncell = n;
-  g.lbx = 1;
-  while (g.lbx < nz && g.lbx < 32) g.lbx *= 2;
+  g.lbx = k_block_width(nz);
   g.lby = kBlock / g.lbx;
   g.lgx = (nz + g.lbx - 1) / g.lbx;
   g.lgy = (ny + g.lby - 1) / g.lby;

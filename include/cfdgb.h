@@ -190,17 +190,19 @@ int cfdgb_backward(cfdgb_ctx *ctx, double *dJ_dinlet, double *dJ_deta);
 
 /* ---- allocation-free Poisson solve (no counterpart in the reference) ----
  * The BiCGSTAB solve of cfdgb_op_bicgstab (SPE operator, or the Jacobi-scaled rows for
- * CFDGB_BICGSTAB_JACOBI) for callers that cannot allocate device memory: code running
- * while a stream is being captured into a CUDA graph, hosts whose framework owns all
- * device memory, services that must not allocate after start-up.  Grid: nx*ny*nz interior
- * cells with uniform spacing dx, dy, dz.  d_rhs and d_x (warm start in, solution out) are
- * the caller's DEVICE arrays of nx*ny*nz doubles; the work is enqueued on `stream` (a
- * cudaStream_t; NULL = the legacy default stream) and the call returns after it finished.
- * No cudaMalloc/cudaFree or allocating library call is made: all work vectors live in a
- * static device array reserved on every GPU that loads the library (about 16.3 MB) and
- * shared by all calls, so at most 2^18 = 262,144 unknowns (larger grids: CFDGB_EINVAL),
- * and calls whose work overlaps on the GPU race.  The first call on a device looks up the
- * array's address; make it before any stream capture starts. */
+ * CFDGB_BICGSTAB_JACOBI) for callers that cannot allocate device memory: hosts whose
+ * framework owns all device memory through its own pool, and services that must not
+ * allocate after start-up.  Grid: nx*ny*nz interior cells with uniform spacing dx, dy, dz.
+ * d_rhs and d_x (warm start in, solution out) are the caller's DEVICE arrays of nx*ny*nz
+ * doubles; the work is enqueued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and the call returns after it finished.  No cudaMalloc/cudaFree or allocating
+ * library call is made: all work vectors live in a static device array reserved on every
+ * GPU that loads the library (17,039,616 bytes, about 17.0 MB: 8 vectors of 2 MiB, block
+ * partials and scalars) and shared by all calls, so at most 2^18 = 262,144 unknowns (larger
+ * grids: CFDGB_EINVAL), and calls whose work overlaps on the GPU race.  The call polls the
+ * solver's convergence from the host, waiting on `stream` every 8 iterations, so a stream
+ * that is capturing into a CUDA graph is rejected (CFDGB_EINVAL).  The first call on a
+ * device looks up the array's device address. */
 int cfdgb_poisson_solve_static(int nx, int ny, int nz, double dx, double dy, double dz, int solver, double tol,
                                int maxit, const double *d_rhs, double *d_x, void *stream, int *iters,
                                double *relres);

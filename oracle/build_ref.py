@@ -45,7 +45,17 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("CFD_REFERENCE_ROOT", "/root/reference"))
+# The reference tree this recipe reads: --reference-root, else CFD_REFERENCE_ROOT, else the
+# location where this build's container mounts it (read-only).  Nothing but this recipe and
+# the fixture scripts beside the goldens reads it; the GPU host uses the staged copy.
+DEFAULT_REF_ROOT = "/root/reference"
+REF_ROOT = Path(os.environ.get("CFD_REFERENCE_ROOT", DEFAULT_REF_ROOT))
+
+
+def set_reference_root(path) -> None:
+    """Read the reference tree from `path` instead (the --reference-root option)."""
+    global REF_ROOT
+    REF_ROOT = Path(path)
 OUT = HERE / "_ref"
 SRC = OUT / "src"
 BIN = OUT / "bin"
@@ -186,7 +196,11 @@ def main(argv=None):
     ap.add_argument("--cx", type=float, default=6.0)
     ap.add_argument("--flavour", default="parity", choices=["parity", "native"])
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--reference-root", default=None,
+                    help="the reference project's root (default: $CFD_REFERENCE_ROOT or " + DEFAULT_REF_ROOT + ")")
     a = ap.parse_args(argv)
+    if a.reference_root:
+        set_reference_root(a.reference_root)
     exe = build(*a.grid, *a.domain, a.cx, flavour=a.flavour, force=a.force)
     print(exe)
 

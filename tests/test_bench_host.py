@@ -1,18 +1,45 @@
 """Host-side logic of bench.py that needs no GPU: which recorded reference iteration counts
 the CPU arm is scored on."""
+import json
+
+import pytest
+
 import bench
 
 
 def test_reference_window_takes_the_timed_steps():
     rec = {"iters": [0, 10, 20, 30, 40, 50]}  # steps 1..6; step 1 has no solve
-    want, beyond = bench.reference_window_iters(rec, warmup=3, steps=2)
-    assert want == [30, 40] and beyond == 0  # steps 4 and 5
+    assert bench.reference_window_iters(rec, warmup=3, steps=2) == [30, 40]  # steps 4 and 5
+    assert bench.reference_window_iters(rec, warmup=3, steps=3) == [30, 40, 50]
 
 
-def test_reference_window_beyond_the_record_uses_the_solve_mean():
+def test_reference_window_beyond_the_record_is_refused():
+    """Nothing is imputed: a timed window past the recorded run makes the arm unavailable."""
     rec = {"iters": [0, 10, 20, 30]}
-    want, beyond = bench.reference_window_iters(rec, warmup=2, steps=4)
-    assert want[:2] == [20, 30] and want[2:] == [20.0, 20.0] and beyond == 2
+    with pytest.raises(ValueError, match="lacks 2 recorded steps"):
+        bench.reference_window_iters(rec, warmup=2, steps=4)
+
+
+def test_reference_arm_unavailable_when_the_record_is_short(capsys, monkeypatch):
+    monkeypatch.setattr(bench, "reference_iteration_record", lambda wl: {"iters": [0, 1, 2]})
+    assert bench.main(["--impl", "reference", "--steps", "20", "--warmup", "5"]) == 0
+    line = json.loads(capsys.readouterr().out)
+    assert line["impl"] == "reference" and "lacks 22 recorded steps" in line["unavailable"]
+
+
+def test_both_arms_print_the_same_config():
+    a = bench.bench_config("c2", 5000, 1)
+    assert a == bench.bench_config("c2", 5000, 1)
+    assert {"workload", "nx", "solver", "tol", "maxit", "bc", "parallelism", "l2"} <= set(a)
+
+
+def test_solve_record_counts_capped_and_unconverged_solves():
+    from types import SimpleNamespace as S
+    st = [S(step=1, iters=0, relres=0.0, status=0), S(step=2, iters=900, relres=5e-9, status=0),
+          S(step=3, iters=5000, relres=3e-8, status=-3), S(step=4, iters=1200, relres=1e-8, status=0)]
+    r = bench.solve_record(st, 1e-8)
+    assert r["capped_solves"] == 1 and r["unconverged_solves"] == 2
+    assert r["iters"] == [0, 900, 5000, 1200] and r["status"] == [0, 0, -3, 0]
 
 
 def _replica(rank, port, q):
