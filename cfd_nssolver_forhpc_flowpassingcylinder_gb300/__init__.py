@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 6  # CFDGB_ABI_VERSION
+ABI_VERSION = 7  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -32,6 +32,8 @@ WALLS_ZERO_GRADIENT, WALLS_FREE_SLIP = 0, 1
 WALLS = {"zero_gradient": WALLS_ZERO_GRADIENT, "free_slip": WALLS_FREE_SLIP}
 PRECOND_NONE, PRECOND_MULTIGRID = 0, 1
 PRECONDS = {"none": PRECOND_NONE, "multigrid": PRECOND_MULTIGRID}
+DT_FIXED, DT_REFERENCE, DT_CFL = 0, 1, 2
+DT_MODES = {"fixed": DT_FIXED, "reference": DT_REFERENCE, "cfl": DT_CFL}
 
 
 class CfdgbError(RuntimeError):
@@ -51,7 +53,7 @@ class Config(C.Structure):
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
                 ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int),
-                ("precond", C.c_int)]
+                ("precond", C.c_int), ("dt_mode", C.c_int), ("cfl_target", C.c_double), ("dt_max", C.c_double)]
 
 
 class Objective(C.Structure):
@@ -61,7 +63,8 @@ class Objective(C.Structure):
 
 class StepStats(C.Structure):
     _fields_ = [("step", C.c_int), ("iters", C.c_int), ("outer", C.c_int), ("status", C.c_int),
-                ("relres", C.c_double), ("cd", C.c_double), ("cl", C.c_double), ("cfl", C.c_double)]
+                ("relres", C.c_double), ("cd", C.c_double), ("cl", C.c_double), ("cfl", C.c_double),
+                ("dt", C.c_double), ("time", C.c_double)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -172,6 +175,8 @@ def default_config(**kw) -> Config:
             v = WALLS[v]
         if k == "precond" and isinstance(v, str):
             v = PRECONDS[v]
+        if k == "dt_mode" and isinstance(v, str):
+            v = DT_MODES[v]
         if k == "les":
             v = int(bool(v))
         setattr(cfg, k, v)
@@ -188,6 +193,8 @@ class StepResult:
     cd: float
     cl: float
     cfl: float = 0.0
+    dt: float = 0.0
+    time: float = 0.0
 
 
 class Solver:
@@ -254,7 +261,8 @@ class Solver:
         st = (StepStats * max(n, 1))()
         rc = self._L.cfdgb_step(self._h, n, st)
         _check(rc, allow=(ENOCONV,) if allow_noconv else ())
-        return [StepResult(s.step, s.iters, s.outer, s.status, s.relres, s.cd, s.cl, s.cfl) for s in st[:n]]
+        return [StepResult(s.step, s.iters, s.outer, s.status, s.relres, s.cd, s.cl, s.cfl, s.dt, s.time)
+                for s in st[:n]]
 
     def pressure_solve(self):
         it, rr = C.c_int(), C.c_double()

@@ -60,14 +60,14 @@ enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
   K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_LES,
-  K_PP32, K_MG, K_PV32, K_PS32, K_PT32, K_PXR32, K_COUNT
+  K_PP32, K_MG, K_PV32, K_PS32, K_PT32, K_PXR32, K_MIRROR, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
     "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl", "smagorinsky",
-    "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32"};
+    "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32", "mirror32"};
 
 struct PendingEv {
   int id;
@@ -100,6 +100,8 @@ struct cfdgb_ctx {
   bool use_mg = false;
   MgPlan mg{};
   float *ph32 = nullptr, *sh32 = nullptr;
+  // MIXED QUICK: FP32 copies of the padded u, v, w that the FP32 stencil sweep reads
+  float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;
   double *part = nullptr;
   SolverScal *sc = nullptr, *sc32 = nullptr;
   StepScal *ss = nullptr;
@@ -286,6 +288,8 @@ void build_stencils(cfdgb_ctx *c) {
         q[6] = i != nx - 1 ? -C.xp(i) * jp : 0.0;
         q[7] = jp;
         s[7] = 1.0 / ijk;
+        c->spe64.dg[cls] = c->jac64.dg[cls] = ijk;
+        c->spe32.dg[cls] = c->jac32.dg[cls] = (float)ijk;
         for (int e = 0; e < 8; ++e) {
           c->spe32.c[cls][e] = (float)s[e];
           c->jac32.c[cls][e] = (float)q[e];
@@ -355,6 +359,9 @@ int validate(const cfdgb_config *c) {
       return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
                   c->ny, c->nz, kMgSharedCells);
   }
+  if (c->dt_mode < CFDGB_DT_FIXED || c->dt_mode > CFDGB_DT_CFL) return fail(CFDGB_EINVAL, "unknown dt_mode %d", c->dt_mode);
+  if (c->dt_mode == CFDGB_DT_CFL && !(c->cfl_target > 0 && c->dt_max >= 0))
+    return fail(CFDGB_EINVAL, "CFDGB_DT_CFL needs cfl_target > 0 and dt_max >= 0");
   if (c->grid == CFDGB_GRID_SML) {
     // unit_SML's own conditions (structureGrid.hpp:269,283): 100 fine cells in x (shifted 4
     // cells) and in y, an even number of coarse ones on both sides
@@ -445,11 +452,12 @@ int set_solver_params(cfdgb_ctx *c, SolverScal *dsc, double tol, int maxit) {
 
 // Iterate chunks until the device says done.  Returns the scalars in *out.  Each chunk
 // is a captured graph of chunk_len iterations; with kernel timing on, the same kernels
-// are launched one by one between event pairs instead.
+// are launched one by one between event pairs instead, one iteration per poll, so that no
+// launch after the stop (which returns at once) enters the per-kernel averages.
 int run_chunks(cfdgb_ctx *c, bool fp32, SolverScal *out) {
   SolverScal *dsc = fp32 ? c->sc32 : c->sc;
   if (!c->timing && !(fp32 ? c->chunk32 : c->chunk64)) TRY(capture_chunk(c, fp32));
-  const int len = chunk_iters(c, fp32);
+  const int len = c->timing ? 1 : chunk_iters(c, fp32);
   const long long max_chunks = (long long)c->cfg.maxit / len + 3;
   const int nk = iter_kernels(c, fp32);
   for (long long q = 0; q < max_chunks; ++q) {
@@ -517,7 +525,9 @@ void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
 int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *status) {
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
-  L(c, K_RHS, 1, [&] { launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, jac, c->jac64, c->b); });
+  L(c, K_RHS, 1, [&] {
+    launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, c->us, c->vs, c->ws, jac, c->jac64, c->b);
+  });
   if (c->cfg.project_rhs)
     L(c, K_RHS, 2, [&] { launch_project_rhs(c->stream, c->g, st64, jac ? 1 : 0, c->b, c->part, c->ss); });
   *iters = 0;
@@ -665,6 +675,23 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   return 0;
 }
 
+// time-step scalars at init: dt as configured, time 0, running extremes at get_Cfl's
+// starting values (U_max = -1e10, U_min = 1e10, cfl.hpp:12-13)
+int reset_time(cfdgb_ctx *c) {
+  double h[9];
+  h[0] = c->cfg.dt;
+  h[1] = c->cfg.dt;
+  h[2] = 0.0;
+  for (int q = 0; q < 6; ++q) h[3 + q] = -1e10;
+  static_assert(offsetof(StepScal, dt_next) == offsetof(StepScal, dt) + 8 &&
+                    offsetof(StepScal, time) == offsetof(StepScal, dt) + 16 &&
+                    offsetof(StepScal, urun) == offsetof(StepScal, dt) + 24,
+                "StepScal time-step fields are contiguous");
+  CK(cudaMemcpyAsync(&c->ss->dt, h, 9 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));  // h is reused by the next call
+  return 0;
+}
+
 int apply_init_bc(cfdgb_ctx *c) {
   // src/RUN_CPU.cpp:104-109: T1 = T3 = T0, then the first ghost fill and copy
   const size_t bytes = c->npad * sizeof(double);
@@ -680,6 +707,7 @@ int apply_init_bc(cfdgb_ctx *c) {
   CK(cudaMemsetAsync(c->px2, 0, c->ncell * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->sc, 0, sizeof(SolverScal), c->stream));
   CK(cudaMemsetAsync(c->sc32, 0, sizeof(SolverScal), c->stream));
+  TRY(reset_time(c));
   CK(cudaGetLastError());
   c->loop = 0;
   c->have_fields = true;
@@ -716,18 +744,49 @@ int ensure_les(cfdgb_ctx *c) {
   return 0;
 }
 
-// u* of the step: Smagorinsky first when on; the FP32 stencil sweep for MIXED QUICK
-void convdiff(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *us, double *vs, double *ws) {
+// The step kernels' time-step control: in a time step dt comes from the step scalars (so an
+// adaptive rule needs no host round trip) and the CFL reduction keeps the running extremes
+// and the next dt; a single call uses the configured dt and only reports the CFL number.
+StepCtl step_ctl(const cfdgb_ctx *c, bool in_step) {
+  StepCtl sc{};
+  sc.dtp = in_step ? &c->ss->dt : nullptr;
+  sc.ss = c->ss;
+  sc.part = c->part;
+  sc.in_step = in_step ? 1 : 0;
+  sc.dt_mode = c->cfg.dt_mode;
+  sc.Re = c->cfg.Re;
+  sc.cfl_target = c->cfg.cfl_target;
+  sc.dt_max = c->cfg.dt_max > 0.0 ? c->cfg.dt_max : c->cfg.dt;
+  return sc;
+}
+// step_end mode of the velocity correction (launch_update_uf_exact)
+int step_mode(const cfdgb_ctx *c) { return c->cfg.dt_mode == CFDGB_DT_FIXED ? 1 : 2; }
+
+bool fast_convdiff(const cfdgb_ctx *c) {
+  return c->cfg.precision == CFDGB_MIXED && c->cfg.scheme == CFDGB_QUICK && !c->cfg.les;
+}
+
+// u* of the step, with the CFL number of u* (get_Cfl, src/RUN_CPU.cpp:274) from the same
+// kernel: Smagorinsky first when on; the FP32 stencil sweep for MIXED QUICK, on FP32
+// copies of u, v, w made first
+void convdiff(cfdgb_ctx *c, const double *u, const double *v, const double *w, double *us, double *vs, double *ws,
+              bool in_step) {
   const double nu = 1.0 / c->cfg.Re;  // 0_1_SimulationVariable.hpp:26-31
+  const StepCtl sc = step_ctl(c, in_step);
   if (c->cfg.les)
     L(c, K_LES, 1, [&] { launch_smagorinsky(c->stream, c->nblk, c->g, c->les_l2, u, v, w, c->nut); });
-  L(c, K_CONVDIFF, 1, [&] {
-    if (c->cfg.precision == CFDGB_MIXED && c->cfg.scheme == CFDGB_QUICK && !c->cfg.les)
-      launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, u, v, w, us, vs, ws);
-    else
+  if (fast_convdiff(c)) {
+    L(c, K_MIRROR, 1, [&] { launch_mirror32(c->stream, c->g, u, v, w, c->u32, c->v32, c->w32); });
+    L(c, K_CONVDIFF, 1, [&] {
+      launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, u, v, w, c->u32, c->v32, c->w32, us, vs,
+                          ws, sc);
+    });
+  } else {
+    L(c, K_CONVDIFF, 1, [&] {
       launch_convdiff_exact(c->stream, c->nblk, c->g, c->cfg.scheme, c->cfg.dt, nu, c->cfg.les ? c->nut : nullptr,
-                            u, v, w, us, vs, ws);
-  });
+                            u, v, w, us, vs, ws, sc);
+    });
+  }
 }
 
 int ensure_op_buffers(cfdgb_ctx *c) {
@@ -778,6 +837,9 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->dfib = 1;
   c->seed = 0;
   c->amp = 0.0;
+  c->dt_mode = CFDGB_DT_FIXED;
+  c->cfl_target = 0.5;
+  c->dt_max = 0.0;  // 0: the configured dt
   return 0;
 }
 
@@ -950,6 +1012,10 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
+  if (cfg->precision == CFDGB_MIXED && cfg->scheme == CFDGB_QUICK && !cfg->les) {  // FP32 copies of u, v, w
+    if ((rc = dalloc(c, &c->u32, c->npad)) || (rc = dalloc(c, &c->v32, c->npad)) || (rc = dalloc(c, &c->w32, c->npad)))
+      return bail(rc);
+  }
   if (cfg->precond == CFDGB_PRECOND_MULTIGRID) {  // levels >= 1 and the vectors M p, M s
     mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm,
             !std::getenv("CFDGB_SCALAR_FP32"), &c->mg);
@@ -1086,10 +1152,9 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
   int worst = 0;
   for (int s = 0; s < nsteps; ++s) {
     const int loop = ++c->loop;
-    // 1. u* (RUN_CPU.cpp:268)
-    convdiff(c, c->u, c->v, c->w, c->us, c->vs, c->ws);
-    // CFL diagnostic on u* (get_Cfl, RUN_CPU.cpp:274)
-    L(c, K_CFL, 1, [&] { launch_cfl(c->stream, c->nblk, c->g, c->cfg.dt, c->us, c->vs, c->ws, c->part, c->ss); });
+    // 1. u* (RUN_CPU.cpp:268) and, from the same kernel, the CFL diagnostic on u* (get_Cfl,
+    // RUN_CPU.cpp:274) with the next dt of an adaptive rule (timestepper, :275)
+    convdiff(c, c->u, c->v, c->w, c->us, c->vs, c->ws, true);
     // 2. pressure, not at the first step (RUN_CPU.cpp:303)
     int iters = 0, outer = 0, status = 0;
     double relres = 0.0;
@@ -1099,8 +1164,13 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
     }
     // 3. correction + DFIB + drag, written straight into T0 (copyVel, RUN_CPU.cpp:369-391)
     L(c, K_UPDATE, 1, [&] {
-      launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->cfg.lz, c->eta, c->p, c->us, c->vs, c->ws, c->u,
-                             c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part, c->ss);
+      if (c->cfg.precision == CFDGB_MIXED)
+        launch_update_uf_fast(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta, c->p,
+                              c->us, c->vs, c->ws, c->u, c->v, c->w, c->ui, c->vi, c->wi, c->part, c->ss);
+      else
+        launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta,
+                               c->p, c->us, c->vs, c->ws, c->u, c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part,
+                               c->ss);
     });
     // 4. ghost fill of T0 and p, copy into T1 (RUN_CPU.cpp:399-400)
     L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet); });
@@ -1118,6 +1188,8 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
       st.cd = c->h_ss->cd;
       st.cl = c->h_ss->cl;
       st.cfl = c->h_ss->cfl[0];
+      st.dt = c->h_ss->dt_step;
+      st.time = c->h_ss->time;
     }
     if (status < worst) worst = status;
   }
@@ -1182,7 +1254,7 @@ int cfdgb_op_convection_diffusion(cfdgb_ctx *c, const double *u, const double *v
   double **o = c->op;
   TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n));
   TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
-  convdiff(c, o[0], o[1], o[2], o[3], o[4], o[5]);
+  convdiff(c, o[0], o[1], o[2], o[3], o[4], o[5], false);
   TRY(d2h(c, us, o[3], n)); TRY(d2h(c, vs, o[4], n)); TRY(d2h(c, ws, o[5], n));
   return sync(c);
 }
@@ -1229,7 +1301,7 @@ int cfdgb_op_rhs(cfdgb_ctx *c, int jacobi, const double *us, const double *vs, c
   const size_t n = c->npad;
   double **o = c->op;
   TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
-  launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, o[3], o[4], o[5], jacobi != 0, c->jac64, c->opc[0]);
+  launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, nullptr, o[3], o[4], o[5], jacobi != 0, c->jac64, c->opc[0]);
   TRY(d2h(c, b, c->opc[0], c->ncell));
   return sync(c);
 }
@@ -1304,8 +1376,8 @@ int cfdgb_op_update_uf(cfdgb_ctx *c, const double *eta, const double *p, const d
   TRY(h2d(c, o[3], us, n)); TRY(h2d(c, o[4], vs, n)); TRY(h2d(c, o[5], ws, n));
   TRY(h2d(c, o[1], u3, n)); TRY(h2d(c, o[2], v3, n)); TRY(h2d(c, o[8], w3, n));
   if (f) TRY(h2d(c, o[7], f, 3 * n));
-  launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, c->cfg.lz, o[6], o[0], o[3], o[4], o[5], o[1], o[2],
-                         o[8], f ? o[7] : nullptr, nullptr, nullptr, nullptr, c->part, c->ss);
+  launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, nullptr, 0, c->cfg.lz, o[6], o[0], o[3], o[4], o[5],
+                         o[1], o[2], o[8], f ? o[7] : nullptr, nullptr, nullptr, nullptr, c->part, c->ss);
   TRY(d2h(c, u3, o[1], n)); TRY(d2h(c, v3, o[2], n)); TRY(d2h(c, w3, o[8], n));
   if (f) TRY(d2h(c, f, o[7], 3 * n));
   CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
@@ -1340,8 +1412,11 @@ int cfdgb_op_cfl(cfdgb_ctx *c, const double *us, const double *vs, const double 
 int cfdgb_set_dt(cfdgb_ctx *c, double dt) {
   if (!c) return fail(CFDGB_EINVAL, "null context");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(CFDGB_EINVAL, "dt must be positive");
-  c->cfg.dt = dt;  // read at every launch of the step kernels; nothing captured depends on it
-  return 0;
+  c->cfg.dt = dt;
+  // the step kernels read dt from the step scalars
+  const double h[2] = {dt, dt};
+  CK(cudaMemcpyAsync(&c->ss->dt, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  return sync(c);
 }
 
 int cfdgb_write_plot3d(cfdgb_ctx *c, const char *xpath, const char *qpath, double time) {
@@ -1485,6 +1560,8 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
     return fail(CFDGB_EINVAL, "the adjoint is implemented on the uniform grid");
   if (c->cfg.scheme != CFDGB_QUICK || c->cfg.les)  // its transposed stencil is QUICK's
     return fail(CFDGB_EINVAL, "the adjoint is implemented for QUICK without the Smagorinsky model");
+  if (c->cfg.dt_mode != CFDGB_DT_FIXED)  // its reverse sweep replays the steps at one dt
+    return fail(CFDGB_EINVAL, "the adjoint needs a fixed dt (CFDGB_DT_FIXED)");
   if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
     return fail(CFDGB_EINVAL, "bad objective window");
   if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");
@@ -1585,7 +1662,7 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
       launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
       // u* of step n (interior faces), from U^n
       launch_convdiff_exact(c->stream, c->nblk, c->g, CFDGB_QUICK, dt, nu, nullptr, wv[0], wv[1], wv[2], c->us, c->vs,
-                            c->ws);
+                            c->ws, StepCtl{});
       const double cw = (n >= obj.first && n <= obj.last) ? cw_in : 0.0;
       launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, wv[3], c->us, c->vs, c->ws, c->lA[0], c->lA[1],
                       c->lA[2], c->lus[0], c->lus[1], c->lus[2], c->le[0], c->le[1], c->le[2], c->lx, c->leta,

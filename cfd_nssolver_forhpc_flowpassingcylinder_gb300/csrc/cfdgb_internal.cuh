@@ -109,7 +109,8 @@ __device__ __forceinline__ long long pidx(const Geo &g, int i, int j, int k) {
 template <typename T>
 struct Stencil {
   T c[27][8];
-  int jac;  // 1: the rows are scaled by jp (CSR / Jacobi)
+  T dg[27];  // the unscaled diagonal of each class (1/jp up to rounding)
+  int jac;   // 1: the rows are scaled by jp (CSR / Jacobi)
 };
 
 __device__ __forceinline__ int axis_class(int a, int n) { return a == 0 ? 0 : (a == n - 1 ? 2 : 1); }
@@ -195,6 +196,14 @@ __device__ __forceinline__ double row_jp(const Geo &g, const Stencil<double> &st
   return st.c[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)][7];
 }
 
+// the unscaled diagonal of a row (class table, or column 3 of the stored SPE rows): maps a
+// Jacobi-scaled residual back to the unscaled one by a multiplication (r / jp ~ r * diag)
+__device__ __forceinline__ double row_diag(const Geo &g, const Stencil<double> &st, int ic, int jc, int kc,
+                                           long long row) {
+  if (g.nonuni) return g.cof[0][3 * g.ncell + row];
+  return st.dg[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)];
+}
+
 __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &ic, int &jc, int &kc) {
   if (row < (1LL << 31) && (long long)nyc * nzc < (1LL << 31)) {  // 32-bit division, as row_ijk
     const unsigned r = (unsigned)row, nz = (unsigned)nzc, nyz = (unsigned)nyc * nz;
@@ -239,8 +248,27 @@ struct StepScal {
   double rsum;  // MIXED: sum of the raw residual (its component along the operator's null space)
   double esum;  // MIXED: sum of the inner correction e
   double cfl[7];  // get_Cfl on u*: cfl, U_max[3], U_min[3]
+  // time step: dt of the current step (read by the step kernels), the next step's dt (set
+  // with the CFL reduction), the simulated time at the end of the last step, and the
+  // running extremes U_max[3], -U_min[3] since init (the reference's simu.U_max / U_min
+  // keep their values from step to step: cfl.hpp:12-13 resizes, it does not reset)
+  double dt, dt_next, time;
+  double urun[6];
+  double dt_step;  // dt of the last step (set with time at its end)
   int nan_flag, pad;
   unsigned cnt[8];
+};
+
+// What the step kernels need beside their fields: where dt lives (device memory, so an
+// adaptive step needs no host round trip), where the CFL reduction goes and how the next
+// dt is chosen (cfdgb_dt_mode: fixed, the reference's timestepper, or a CFL target).
+struct StepCtl {
+  const double *dtp;  // current dt on the device; null: the kernel's dt argument
+  StepScal *ss;       // CFL extremes, dt_next, running extremes
+  double *part;       // block partials of the CFL reduction
+  int in_step;        // 1: a time step (running extremes and dt_next are kept); 0: a single call
+  int dt_mode;        // a cfdgb_dt_mode value
+  double Re, cfl_target, dt_max;
 };
 
 // Dir/Num boundary table of inc/BoundaryCondition/FLOWpassing.hpp:6-40 as

@@ -6,15 +6,17 @@
 namespace cfdgb {
 
 // step_exact.cu (bit-exact FP64, reference operation order)
-// scheme: a cfdgb_scheme value; nut (compact, may be null): eddy viscosity added to nu
+// scheme: a cfdgb_scheme value; nut (compact, may be null): eddy viscosity added to nu.
+// Fused CFL reduction into sc.ss (none when sc.ss is null); dt from sc.dtp when set.
 void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu,
                            const double *nut, const double *u, const double *v, const double *w, double *us,
-                           double *vs, double *ws);
+                           double *vs, double *ws, const StepCtl &sc);
 // SmagorinskyModel on u, v, w into compact nut; l2 = (CS delta)^2 per compact row
 void launch_smagorinsky(cudaStream_t s, int nblk, const Geo &g, const double *l2, const double *u, const double *v,
                         const double *w, double *nut);
-void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
-                      const double *ws, int jacobi, const Stencil<double> &st, double *b);
+// dtp: dt on the device (null: dt)
+void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, const double *us,
+                      const double *vs, const double *ws, int jacobi, const Stencil<double> &st, double *b);
 void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
                        double *y);
 void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p);
@@ -28,10 +30,18 @@ void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p,
 // the interior of padded p, u, v, w (faces) and eta (may be null)
 void launch_plot3d_unpack(cudaStream_t s, int nblk, const Geo &g, const float *in, double *p, double *u, double *v,
                           double *w, double *eta);
-void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
-                            const double *p, const double *us, const double *vs, const double *ws, double *u3,
-                            double *v3, double *w3, double *f, const double *ui, const double *vi,
-                            const double *wi, double *part, StepScal *ss);
+// dtp: dt on the device (null: dt); step_mode: 0 a single call, 1 a time step (time += dt),
+// 2 a time step with an adaptive dt (then dt = dt_next)
+void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, int step_mode,
+                            double lz, const double *eta, const double *p, const double *us, const double *vs,
+                            const double *ws, double *u3, double *v3, double *w3, double *f, const double *ui,
+                            const double *vi, const double *wi, double *part, StepScal *ss);
+// MIXED: the same correction with reciprocal multiplications (not the reference's rounding)
+// and the DFIB arithmetic only where eta is non-zero on either side of a face
+void launch_update_uf_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, int step_mode,
+                           double lz, const double *eta, const double *p, const double *us, const double *vs,
+                           const double *ws, double *u3, double *v3, double *w3, const double *ui, const double *vi,
+                           const double *wi, double *part, StepScal *ss);
 // inlet: nyc*nzc inlet u values (NULL: the reference's constant Dir[0][0] = 1)
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
                double *vs, double *ws, int do_main, const double *inlet = nullptr);
@@ -39,8 +49,14 @@ void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const d
                 double R, double *eta);
 
 // step_fast.cu (MIXED: FP32 arithmetic on the FP64 state)
+// u32, v32, w32: FP32 copies of the padded u, v, w (launch_mirror32), which the stencil
+// reads; u, v, w (FP64) give u* = u + increment.  Fused CFL reduction into sc.ss.
 void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
-                         const double *u, const double *v, const double *w, double *us, double *vs, double *ws);
+                         const double *u, const double *v, const double *w, const float *u32, const float *v32,
+                         const float *w32, double *us, double *vs, double *ws, const StepCtl &sc);
+// padded FP32 copies of u, v, w (rounded to nearest)
+void launch_mirror32(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w, float *u32,
+                     float *v32, float *w32);
 
 // solver.cu
 template <typename T>

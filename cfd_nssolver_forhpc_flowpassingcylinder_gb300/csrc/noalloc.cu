@@ -96,6 +96,7 @@ void uniform_stencils(int nx, int ny, int nz, double dx, double dy, double dz, S
         s[5] = j != ny - 1 ? -cy : 0.0;
         s[6] = i != nx - 1 ? -cx : 0.0;
         s[7] = 1.0 / ijk;
+        spe.dg[cls] = jac.dg[cls] = ijk;
         double aa = 0.0, bb = 0.0, cc = 0.0;
         if (i == 0) aa = -cx;
         if (i == nx - 1) aa = -cx;

@@ -113,11 +113,26 @@ __device__ __forceinline__ bool grid_max(double (&v)[NV], double *part, unsigned
   __syncthreads();
   if (!last) return false;
   __threadfence();
+  // the partials, strided over the block's threads, then over its warps (every thread of
+  // the block takes part: a one-thread loop over the partials held the grid for a long tail)
+  const int nt = (int)(blockDim.x * blockDim.y * blockDim.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double m = -INFINITY;
+    for (int b = t; b < G; b += nt) m = fmax(m, __ldcg(part + q * G + b));
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    v[q] = m;
+  }
+  __syncthreads();  // sh is reused below
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q][wid] = v[q];
+  __syncthreads();
   if (t == 0) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
-      double m = __ldcg(part + q * G);
-      for (int b = 1; b < G; ++b) m = fmax(m, __ldcg(part + q * G + b));
+      double m = sh[q][0];
+      for (int w = 1; w < nt / 32; ++w) m = fmax(m, sh[q][w]);
       res[q] = m;
     }
     *ticket = 0u;

@@ -1411,7 +1411,7 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
     acc[0] += r * r;
     acc[1] += bb * bb;
     // the unscaled residual's sum: its component along the operator's null space
-    acc[2] += jacobi ? r / row_jp(g, st, ic, jc, kc, row) : r;
+    acc[2] += jacobi ? r * row_diag(g, st, ic, jc, kc, row) : r;
   }
   double out[3];
   if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
@@ -1508,7 +1508,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs_sum(Geo g, Stencil<double> st, i
   double acc[1] = {0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    acc[0] += jacobi ? b[row] / row_jp(g, st, ic, jc, kc, row) : b[row];
+    acc[0] += jacobi ? b[row] * row_diag(g, st, ic, jc, kc, row) : b[row];
   }
   double out[1];
   if (grid_sum<1>(acc, part, &ss->cnt[6], out) && lin_tid() == 0) ss->rsum = out[0];

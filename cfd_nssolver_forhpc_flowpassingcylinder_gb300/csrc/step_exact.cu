@@ -9,6 +9,7 @@
 
 #include "cfdgb_internal.cuh"
 #include "reduce.cuh"
+#include "stepctl.cuh"
 #include "kernels.h"
 
 namespace cfdgb {
@@ -126,15 +127,22 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
 // skipped.
 // S: the convection scheme; nut (compact, may be null): the Smagorinsky eddy viscosity
 // added to nu per cell (Convection_Difussion.hpp:251-256).
+// Fused with get_Cfl (inc/analyses/cfl.hpp:3-78, called on u* right after this function,
+// src/RUN_CPU.cpp:274): each thread takes u*, v*, w* of its cell from registers, with the
+// reference's division and order (c = u/Dxs + v/Dys + w/Dzs, a term left out on the last
+// face of its axis), so the CFL number and extremes are those of get_Cfl bit for bit; the
+// maxima are exact in any order.  The last block also sets the next dt (StepCtl).
 template <int S>
-__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, double nu0,
+__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt_arg, double nu0,
                                                            const double *__restrict__ nut,
                                                            const double *__restrict__ u,
                                                            const double *__restrict__ v,
                                                            const double *__restrict__ w,
                                                            double *__restrict__ us,
                                                            double *__restrict__ vs,
-                                                           double *__restrict__ ws) {
+                                                           double *__restrict__ ws, StepCtl sc) {
+  const double dt = step_dt(sc, dt_arg);
+  CflAcc cfl;
   const long long sx = g.sx, sy = g.sy, sz = 1;
   const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
   const double *rDx = g.rDx, *rDy = g.rDy, *rDz = g.rDz, *rDxs = g.rDxs, *rDys = g.rDys, *rDzs = g.rDzs;
@@ -152,6 +160,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
     const long long ic = pidx(g, i, j, k);
     const double nu = nut ? nu0 + nut[row] : nu0;
     const long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz, zp = ic + sz;
+    double ccfl = 0.0;
     if (i < g.nx - 3) {  // u
       const double IT = ox(Dxs[i] * 0.5, i);
       const double uc = u[ic], uxp = u[xp], uxm = u[xm];
@@ -172,7 +181,10 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
           (oxs(ox(uxp - uc, i + 1) - ox(uc - uxm, i), i) +
            oy(oys(u[yp] - uc, j) - oys(uc - u[ym], j - 1), j) +
            oz(ozs(u[zp] - uc, k) - ozs(uc - u[zm], k - 1), k));
-      us[ic] = uc + convection + difussion;
+      const double r = uc + convection + difussion;
+      us[ic] = r;
+      ccfl += oxs(r, i);
+      cfl.comp(0, r);
     }
     if (j < g.ny - 3) {  // v
       const double IT = oy(Dys[j] * 0.5, j);
@@ -194,7 +206,10 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
           (ox(oxs(v[xp] - vc, i) - oxs(vc - v[xm], i - 1), i) +
            oys(oy(vyp - vc, j + 1) - oy(vc - vym, j), j) +
            oz(ozs(v[zp] - vc, k) - ozs(vc - v[zm], k - 1), k));
-      vs[ic] = vc + convection + difussion;
+      const double r = vc + convection + difussion;
+      vs[ic] = r;
+      ccfl += oys(r, j);
+      cfl.comp(1, r);
     }
     if (k < g.nz - 3) {  // w
       const double IT = oz(Dzs[k] * 0.5, k);
@@ -216,17 +231,23 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt, dou
           (ox(oxs(w[xp] - wc, i) - oxs(wc - w[xm], i - 1), i) +
            oy(oys(w[yp] - wc, j) - oys(wc - w[ym], j - 1), j) +
            ozs(oz(wzp - wc, k + 1) - oz(wc - wzm, k), k));
-      ws[ic] = wc + convection + difussion;
+      const double r = wc + convection + difussion;
+      ws[ic] = r;
+      ccfl += ozs(r, k);
+      cfl.comp(2, r);
     }
+    cfl.cell(ccfl);
   }
+  if (sc.ss) cfl_finish(cfl, dt, sc);
 }
 
 // inc/matrix/b_matrix.hpp:35-98: b = -(jp)(1/dt) div(u*), one-sided differences
-__global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt, const double *__restrict__ us,
+__global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt_arg, const double *dtp,
+                                                      const double *__restrict__ us,
                                                       const double *__restrict__ vs,
                                                       const double *__restrict__ ws, int jacobi,
                                                       Stencil<double> st, double *__restrict__ b) {
-  const double ddt = 1.0 / dt;
+  const double ddt = 1.0 / (dtp ? *dtp : dt_arg);
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
@@ -257,10 +278,11 @@ __global__ void __launch_bounds__(kBlock) k_spmv_exact(Geo g, Stencil<double> st
 // inc/analyses/cfl.hpp:3-78 (get_Cfl) on u*: per cell c = u/Dxs + v/Dys + w/Dzs, each term
 // left out on the last face of its own axis (the loops' "-d"), added in that order; the
 // maximum of c times dt, and the extremes of each component over its faces.  ss->cfl.
+// (The time step computes the same inside k_convdiff_exact; this is the single call.)
 __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *__restrict__ us,
                                                  const double *__restrict__ vs, const double *__restrict__ ws,
-                                                 double *part, StepScal *ss) {
-  double m[7] = {-1e300, -1e10, -1e10, -1e10, -1e10, -1e10, -1e10};  // c, U_max, -U_min
+                                                 StepCtl sc) {
+  CflAcc cfl;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
@@ -269,29 +291,19 @@ __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *
     double c = 0.0;
     if (i < g.nx - 3) {
       c += div_by(us[ic], g.Dxs[i], g.rDxs[i]);
-      m[1] = fmax(m[1], us[ic]);
-      m[4] = fmax(m[4], -us[ic]);
+      cfl.comp(0, us[ic]);
     }
     if (j < g.ny - 3) {
       c += div_by(vs[ic], g.Dys[j], g.rDys[j]);
-      m[2] = fmax(m[2], vs[ic]);
-      m[5] = fmax(m[5], -vs[ic]);
+      cfl.comp(1, vs[ic]);
     }
     if (k < g.nz - 3) {
       c += div_by(ws[ic], g.Dzs[k], g.rDzs[k]);
-      m[3] = fmax(m[3], ws[ic]);
-      m[6] = fmax(m[6], -ws[ic]);
+      cfl.comp(2, ws[ic]);
     }
-    m[0] = fmax(m[0], c);
+    cfl.cell(c);
   }
-  double out[7];
-  if (grid_max<7>(m, part, &ss->cnt[7], out) && lin_tid() == 0) {
-    ss->cfl[0] = out[0] * dt;
-    for (int a = 0; a < 3; ++a) {
-      ss->cfl[1 + a] = out[1 + a];
-      ss->cfl[4 + a] = -out[4 + a];
-    }
-  }
+  cfl_finish(cfl, dt, sc);
 }
 
 // Plot3D solution arrays (inc/io/Plot3D/qfile.hpp:62-103) in k-j-i order, i fastest, as
@@ -352,11 +364,12 @@ __global__ void __launch_bounds__(kBlock) k_transform(Geo g, const double *__res
 // the part of copyVel (inc/source/copyVel.hpp:4) that matters: the faces update_UandF
 // never writes keep the initial values (ui, vi, wi) they hold in the reference's T3.
 __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
-    Geo g, double dt, double lz, const double *__restrict__ eta, const double *__restrict__ p,
-    const double *__restrict__ us, const double *__restrict__ vs, const double *__restrict__ ws,
-    double *__restrict__ u3, double *__restrict__ v3, double *__restrict__ w3, double *__restrict__ f,
-    const double *__restrict__ ui, const double *__restrict__ vi, const double *__restrict__ wi,
-    double *part, StepScal *ss) {
+    Geo g, double dt_arg, const double *dtp, int in_step /* step_end mode */, double lz, const double *__restrict__ eta,
+    const double *__restrict__ p, const double *__restrict__ us, const double *__restrict__ vs,
+    const double *__restrict__ ws, double *__restrict__ u3, double *__restrict__ v3, double *__restrict__ w3,
+    double *__restrict__ f, const double *__restrict__ ui, const double *__restrict__ vi,
+    const double *__restrict__ wi, double *part, StepScal *ss) {
+  const double dt = dtp ? *dtp : dt_arg;
   const long long tot = (long long)g.nx * g.ny * g.nz;
   const double uS = 0.0, vS = 0.0, wS = 0.0;
   const double rdt = 1.0 / dt;
@@ -410,6 +423,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     ss->cd = -2.0 * out[0] / lz;  // CD_CL, virtualForceIntergrator.hpp:309-314
     ss->cl = -2.0 * out[1] / lz;
     ss->nan_flag = !(isfinite(out[0]) && isfinite(out[1]));
+    step_end(ss, dt, in_step);
   }
 }
 
@@ -559,21 +573,21 @@ __global__ void __launch_bounds__(kBlock) k_eta_extrude(Geo g, double *__restric
 // ---- launchers ----
 void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu,
                            const double *nut, const double *u, const double *v, const double *w, double *us,
-                           double *vs, double *ws) {
+                           double *vs, double *ws, const StepCtl &sc) {
   if (scheme == CFDGB_LUD)
-    k_convdiff_exact<CFDGB_LUD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+    k_convdiff_exact<CFDGB_LUD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
   else if (scheme == CFDGB_UD)
-    k_convdiff_exact<CFDGB_UD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+    k_convdiff_exact<CFDGB_UD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
   else
-    k_convdiff_exact<CFDGB_QUICK><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws);
+    k_convdiff_exact<CFDGB_QUICK><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
 }
 void launch_smagorinsky(cudaStream_t s, int nblk, const Geo &g, const double *l2, const double *u, const double *v,
                         const double *w, double *nut) {
   k_smagorinsky<<<nblk, kBlock, 0, s>>>(g, l2, u, v, w, nut);
 }
-void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
-                      const double *ws, int jacobi, const Stencil<double> &st, double *b) {
-  k_rhs_exact<<<nblk, kBlock, 0, s>>>(g, dt, us, vs, ws, jacobi, st, b);
+void launch_rhs_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, const double *us,
+                      const double *vs, const double *ws, int jacobi, const Stencil<double> &st, double *b) {
+  k_rhs_exact<<<nblk, kBlock, 0, s>>>(g, dt, dtp, us, vs, ws, jacobi, st, b);
 }
 void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, const double *x,
                        double *y) {
@@ -581,7 +595,10 @@ void launch_spmv_exact(cudaStream_t s, int nblk, const Geo &g, const Stencil<dou
 }
 void launch_cfl(cudaStream_t s, int nblk, const Geo &g, double dt, const double *us, const double *vs,
                 const double *ws, double *part, StepScal *ss) {
-  k_cfl<<<nblk, kBlock, 0, s>>>(g, dt, us, vs, ws, part, ss);
+  StepCtl sc{};
+  sc.ss = ss;
+  sc.part = part;
+  k_cfl<<<nblk, kBlock, 0, s>>>(g, dt, us, vs, ws, sc);
 }
 void launch_plot3d_pack(cudaStream_t s, int nblk, const Geo &g, const double *p, const double *u, const double *v,
                         const double *w, const double *eta, float *out) {
@@ -594,11 +611,12 @@ void launch_plot3d_unpack(cudaStream_t s, int nblk, const Geo &g, const float *i
 void launch_transform(cudaStream_t s, int nblk, const Geo &g, const double *x, double *p) {
   k_transform<<<nblk, kBlock, 0, s>>>(g, x, p);
 }
-void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, double lz, const double *eta,
-                            const double *p, const double *us, const double *vs, const double *ws, double *u3,
-                            double *v3, double *w3, double *f, const double *ui, const double *vi,
-                            const double *wi, double *part, StepScal *ss) {
-  k_update_uf_exact<<<nblk, kBlock, 0, s>>>(g, dt, lz, eta, p, us, vs, ws, u3, v3, w3, f, ui, vi, wi, part, ss);
+void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, int step_mode,
+                            double lz, const double *eta, const double *p, const double *us, const double *vs,
+                            const double *ws, double *u3, double *v3, double *w3, double *f, const double *ui,
+                            const double *vi, const double *wi, double *part, StepScal *ss) {
+  k_update_uf_exact<<<nblk, kBlock, 0, s>>>(g, dt, dtp, step_mode, lz, eta, p, us, vs, ws, u3, v3, w3, f, ui, vi,
+                                            wi, part, ss);
 }
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
                double *vs, double *ws, int do_main, const double *inlet) {

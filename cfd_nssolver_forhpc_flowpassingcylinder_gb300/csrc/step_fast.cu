@@ -1,11 +1,57 @@
-// MIXED precision stencil sweep: QUICK convection-diffusion (the same discretisation as
-// inc/source/Convection_Difussion.hpp:174) computed in FP32 on the FP64 state.  All
-// divisions by the metric arrays are replaced by per-axis FP32 coefficient tables, so
-// the per-cell work is FP32 FMAs; only the final u* = u + increment is FP64.
+// MIXED precision step kernels.
+//
+// Stencil sweep: QUICK convection-diffusion (the same discretisation as
+// inc/source/Convection_Difussion.hpp:174) computed in FP32 on FP32 copies of the FP64
+// state.  All divisions by the metric arrays are replaced by per-axis FP32 coefficient
+// tables, so the per-cell work is FP32 FMAs; only the final u* = u + increment is FP64.
+// On this GPU the FP64 pipe runs at about 1/70 of the FP32 rate and also executes the
+// FP64 <-> FP32 conversions, so the state is converted once per step (launch_mirror32,
+// integer rounding) instead of once per neighbour read, and the increment is widened by
+// integer operations (exact).
+// Velocity correction: update_UandF with reciprocal multiplications and the DFIB
+// arithmetic only on faces that touch the body.
+#include <algorithm>
+
 #include "cfdgb_internal.cuh"
+#include "reduce.cuh"
+#include "stepctl.cuh"
 #include "kernels.h"
 
 namespace cfdgb {
+
+// double -> float, rounded to nearest (ties to even), by integer operations.  Results
+// below the normal FP32 range flush to a signed zero, above it to infinity; NaN stays NaN.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long a = b & 0x7fffffffffffffffULL;
+  if ((a >> 52) == 0x7ffULL) return __uint_as_float(sign | 0x7f800000u | ((a << 12) ? 0x400000u : 0u));
+  const unsigned long long r = a + 0x0fffffffULL + ((a >> 29) & 1ULL);  // drop 29 bits: nearest, even
+  const int e = (int)(r >> 52) - 896;                                     // FP32 exponent field
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((r >> 29) & 0x7fffffULL));
+}
+
+// float -> double, exact, by integer operations (FP32 subnormals, never met here, read as zero)
+__device__ __forceinline__ double f2d_int(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+  const unsigned eh = e == 0xffu ? 0x7ffu : e + 896u;
+  return __hiloint2double((int)((b & 0x80000000u) | (eh << 20) | ((b >> 3) & 0xfffffu)), (int)(b << 29));
+}
+
+__global__ void __launch_bounds__(kBlock) k_mirror32(long long n, const double *__restrict__ u,
+                                                     const double *__restrict__ v, const double *__restrict__ w,
+                                                     float *__restrict__ u32, float *__restrict__ v32,
+                                                     float *__restrict__ w32) {
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock) {
+    u32[q] = d2f_int(u[q]);
+    v32[q] = d2f_int(v[q]);
+    w32[q] = d2f_int(w[q]);
+  }
+}
 
 // Per-axis table rows (each of length L = tab_len): see host_tables_f32 in api.cu.
 enum TabRow { T_ID = 0, T_IDS, T_IT, T_AP1, T_AP2, T_AN1, T_AN2, T_BP1, T_BP2, T_BN1, T_BN2, T_NROW };
@@ -40,13 +86,14 @@ __device__ __forceinline__ void qb(float Up, float Un, float pp, float p, float 
                                   : tb(tab, L, ax, T_BN2, I) * ((p - c) * iS0 - (c - n) * iSm1));
 }
 
-// One staggered component whose own axis is A.  vel[0..2] = u, v, w.
+// The FP32 increment of one staggered component whose own axis is A.  vel[0..2] = the FP32
+// copies of u, v, w.
 template <int A>
-__device__ __forceinline__ double component(const Geo &g, const FastArgs &fa, const float *__restrict__ tab,
-                                            const double *__restrict__ const *vel, long long ic, const int (&I)[3]) {
+__device__ __forceinline__ float component(const Geo &g, const FastArgs &fa, const float *__restrict__ tab,
+                                           const float *__restrict__ const *vel, long long ic, const int (&I)[3]) {
   const long long s[3] = {g.sx, g.sy, 1};
-  const double *phi = vel[A];
-  auto ld = [&](long long q) { return (float)__ldg(phi + q); };
+  const float *phi = vel[A];
+  auto ld = [&](long long q) { return __ldg(phi + q); };
   const float c = ld(ic);
   float conv = 0.0f, diff = 0.0f;
   const float IT = tb(tab, fa.L, A, T_IT, I[A]);
@@ -64,9 +111,9 @@ __device__ __forceinline__ double component(const Geo &g, const FastArgs &fa, co
               tb(tab, fa.L, b, T_IDS, Ib);
     } else {
       // velocity normal to the b-faces of this control volume, interpolated along A
-      const double *vb = vel[b];
-      const float b0 = (float)__ldg(vb + ic), bA = (float)__ldg(vb + ic + s[A]);
-      const float bm = (float)__ldg(vb + ic - sb), bmA = (float)__ldg(vb + ic - sb + s[A]);
+      const float *vb = vel[b];
+      const float b0 = __ldg(vb + ic), bA = __ldg(vb + ic + s[A]);
+      const float bm = __ldg(vb + ic - sb), bmA = __ldg(vb + ic - sb + s[A]);
       const float Bp = b0 + (bA - b0) * IT, Bn = bm + (bmA - bm) * IT;
       qb(Bp, Bn, pp, p, c, n, nn, tab, fa.L, b, Ib, P, N);
       conv += (P * Bp - N * Bn) * tb(tab, fa.L, b, T_ID, Ib);
@@ -74,33 +121,161 @@ __device__ __forceinline__ double component(const Geo &g, const FastArgs &fa, co
               tb(tab, fa.L, b, T_ID, Ib);
     }
   }
-  return (double)(fa.nu * fa.dt * diff - fa.dt * conv);
+  return fa.nu * fa.dt * diff - fa.dt * conv;
 }
 
-__global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, const float *__restrict__ tab,
+// FP32 CFL state of one thread: the sum u*/Dxs + v*/Dys + w*/Dzs per cell from the FP32
+// u* (u32 + increment) and the FP32 reciprocals; the extremes of each component
+struct CflAccF {
+  float m[7] = {-3e38f, -1e10f, -1e10f, -1e10f, -1e10f, -1e10f, -1e10f};
+  __device__ __forceinline__ void comp(int a, float x) {
+    m[1 + a] = fmaxf(m[1 + a], x);
+    m[4 + a] = fmaxf(m[4 + a], -x);
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, double dt_arg, const float *__restrict__ tab,
                                                          const double *__restrict__ u, const double *__restrict__ v,
-                                                         const double *__restrict__ w, double *__restrict__ us,
-                                                         double *__restrict__ vs, double *__restrict__ ws) {
-  const double *vel[3] = {u, v, w};
+                                                         const double *__restrict__ w, const float *__restrict__ u32,
+                                                         const float *__restrict__ v32, const float *__restrict__ w32,
+                                                         double *__restrict__ us, double *__restrict__ vs,
+                                                         double *__restrict__ ws, StepCtl sc) {
+  const double dt = step_dt(sc, dt_arg);
+  fa.dt = (float)dt;
+  const float *vel[3] = {u32, v32, w32};
+  CflAccF cfl;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
     const int I[3] = {i, j, k};
-    if (i < g.nx - 3) us[ic] = u[ic] + component<0>(g, fa, tab, vel, ic, I);
-    if (j < g.ny - 3) vs[ic] = v[ic] + component<1>(g, fa, tab, vel, ic, I);
-    if (k < g.nz - 3) ws[ic] = w[ic] + component<2>(g, fa, tab, vel, ic, I);
+    float c = 0.0f;
+    if (i < g.nx - 3) {
+      const float d = component<0>(g, fa, tab, vel, ic, I);
+      us[ic] = u[ic] + f2d_int(d);
+      const float r = u32[ic] + d;
+      c += r * tb(tab, fa.L, 0, T_IDS, i);
+      cfl.comp(0, r);
+    }
+    if (j < g.ny - 3) {
+      const float d = component<1>(g, fa, tab, vel, ic, I);
+      vs[ic] = v[ic] + f2d_int(d);
+      const float r = v32[ic] + d;
+      c += r * tb(tab, fa.L, 1, T_IDS, j);
+      cfl.comp(1, r);
+    }
+    if (k < g.nz - 3) {
+      const float d = component<2>(g, fa, tab, vel, ic, I);
+      ws[ic] = w[ic] + f2d_int(d);
+      const float r = w32[ic] + d;
+      c += r * tb(tab, fa.L, 2, T_IDS, k);
+      cfl.comp(2, r);
+    }
+    cfl.m[0] = fmaxf(cfl.m[0], c);
+  }
+  if (sc.ss) {
+    CflAcc acc;
+    for (int q = 0; q < 7; ++q) acc.m[q] = (double)cfl.m[q];
+    cfl_finish(acc, dt, sc);
+  }
+}
+
+// update_UandF (inc/dfib/updateUandF.hpp:90-180, solid velocity 0) for the MIXED mode:
+// T2 = u* - (dt / Ds) (p+ - p) with the reciprocal metric, and the DFIB fraction, velocity
+// and force only on faces where eta is non-zero on either side (elsewhere u = T2 and the
+// force is zero); drag and lift summed as the exact kernel does.
+__global__ void __launch_bounds__(kBlock) k_update_uf_fast(
+    Geo g, double dt_arg, const double *dtp, int step_mode, double lz, const double *__restrict__ eta,
+    const double *__restrict__ p, const double *__restrict__ us, const double *__restrict__ vs,
+    const double *__restrict__ ws, double *__restrict__ u3, double *__restrict__ v3, double *__restrict__ w3,
+    const double *__restrict__ ui, const double *__restrict__ vi, const double *__restrict__ wi, double *part,
+    StepScal *ss) {
+  const double dt = dtp ? *dtp : dt_arg;
+  const double rdt = 1.0 / dt;
+  auto nonzero = [](double e) { return (__double_as_longlong(e) << 1) != 0; };  // +-0 is zero
+  double acc[2] = {0.0, 0.0};
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    const double ec = eta[ic];
+    const bool bc = nonzero(ec);
+    if (i < g.nx - 3) {
+      const long long icP = ic + g.sx;
+      const double T2 = fma(-(dt * g.rDxs[i]), p[icP] - p[ic], us[ic]);
+      const double en = eta[icP];
+      double n3 = T2;
+      if (bc || nonzero(en)) {
+        const double e = fma(en - ec, g.hfx[i], ec);
+        n3 = (1.0 - e) * T2;
+        acc[0] += (n3 - T2) * rdt * (g.Dx[i] * g.Dy[j] * g.Dz[k]);
+      }
+      u3[ic] = n3;
+    } else if (ui) {
+      u3[ic] = ui[ic];
+    }
+    if (j < g.ny - 3) {
+      const long long icP = ic + g.sy;
+      const double T2 = fma(-(dt * g.rDys[j]), p[icP] - p[ic], vs[ic]);
+      const double en = eta[icP];
+      double n3 = T2;
+      if (bc || nonzero(en)) {
+        const double e = fma(en - ec, g.hfy[j], ec);
+        n3 = (1.0 - e) * T2;
+        acc[1] += (n3 - T2) * rdt * (g.Dx[i] * g.Dy[j] * g.Dz[k]);
+      }
+      v3[ic] = n3;
+    } else if (vi) {
+      v3[ic] = vi[ic];
+    }
+    if (k < g.nz - 3) {
+      const long long icP = ic + 1;
+      const double T2 = fma(-(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
+      const double en = eta[icP];
+      w3[ic] = (bc || nonzero(en)) ? (1.0 - fma(en - ec, g.hfz[k], ec)) * T2 : T2;
+    } else if (wi) {
+      w3[ic] = wi[ic];
+    }
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &ss->cnt[0], out) && threadIdx.x == 0) {
+    ss->fsum[0] = out[0];
+    ss->fsum[1] = out[1];
+    ss->cd = -2.0 * out[0] / lz;  // CD_CL, virtualForceIntergrator.hpp:309-314
+    ss->cl = -2.0 * out[1] / lz;
+    ss->nan_flag = !(isfinite(out[0]) && isfinite(out[1]));
+    step_end(ss, dt, step_mode);
   }
 }
 
 void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
-                         const double *u, const double *v, const double *w, double *us, double *vs, double *ws) {
+                         const double *u, const double *v, const double *w, const float *u32, const float *v32,
+                         const float *w32, double *us, double *vs, double *ws, const StepCtl &sc) {
   FastArgs fa;
   fa.L = (g.nx > g.ny ? (g.nx > g.nz ? g.nx : g.nz) : (g.ny > g.nz ? g.ny : g.nz)) + 1;
   fa.dt = (float)dt;
   fa.nu = (float)nu;
-  k_convdiff_f32<<<nblk, kBlock, 0, s>>>(g, fa, tab, u, v, w, us, vs, ws);
+  k_convdiff_f32<<<nblk, kBlock, 0, s>>>(g, fa, dt, tab, u, v, w, u32, v32, w32, us, vs, ws, sc);
+}
+
+void launch_mirror32(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w, float *u32,
+                     float *v32, float *w32) {
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long blocks = std::min<long long>((n + kBlock - 1) / kBlock, (long long)nsm * 8);
+  k_mirror32<<<(int)blocks, kBlock, 0, s>>>(n, u, v, w, u32, v32, w32);
+}
+
+void launch_update_uf_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, int step_mode,
+                           double lz, const double *eta, const double *p, const double *us, const double *vs,
+                           const double *ws, double *u3, double *v3, double *w3, const double *ui, const double *vi,
+                           const double *wi, double *part, StepScal *ss) {
+  k_update_uf_fast<<<nblk, kBlock, 0, s>>>(g, dt, dtp, step_mode, lz, eta, p, us, vs, ws, u3, v3, w3, ui, vi, wi,
+                                           part, ss);
 }
 
 }  // namespace cfdgb

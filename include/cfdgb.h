@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 6
+#define CFDGB_ABI_VERSION 7
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -87,6 +87,23 @@ typedef enum cfdgb_precond {
                                   most 4096 cells */
 } cfdgb_precond;
 
+/* How dt changes from step to step.  The reference keeps dt fixed: its adaptive
+   timestepper (inc/0_1_SimulationVariable.hpp:172-185) is commented out at
+   src/RUN_CPU.cpp:275.  Both adaptive rules run on the device, in the reduction that the
+   convection-diffusion kernel makes over u* for the CFL number; the new dt takes effect
+   at the next step (finishloop, 0_1_SimulationVariable.hpp:139-155). */
+typedef enum cfdgb_dt_mode {
+  CFDGB_DT_FIXED = 0,      /* dt as set by cfdgb_config.dt and cfdgb_set_dt (default) */
+  CFDGB_DT_REFERENCE = 1,  /* timestepper as written: dt_next = the least of 0.05 / (Re U_max^2)
+                              and 0.15 * 0.5 * Re U_min^2 over the three components, at least
+                              1e-12, with U_max, U_min the extremes of u*, v*, w* since init
+                              (get_Cfl keeps them from step to step, cfl.hpp:12-13).  A component
+                              whose minimum is zero, such as w in a flow without z motion, drives
+                              dt to that 1e-12 floor */
+  CFDGB_DT_CFL = 2         /* dt_next = cfl_target / max over cells of (u/Dxs + v/Dys + w/Dzs),
+                              the get_Cfl number divided by dt, and at most dt_max */
+} cfdgb_dt_mode;
+
 typedef struct cfdgb_config {
   int nx, ny, nz;            /* interior cells (nxCal, nyCal, nzCal) */
   double lx, ly, lz;         /* domain [0,lx]x[0,ly]x[0,lz]; spacing per cfdgb_config.grid */
@@ -120,6 +137,9 @@ typedef struct cfdgb_config {
   int walls;                 /* a cfdgb_walls value; default zero-gradient */
   int precond;               /* a cfdgb_precond value: the preconditioner of the MIXED
                                 BiCGSTAB sweeps; default none (the reference's iteration) */
+  int dt_mode;               /* a cfdgb_dt_mode value; default fixed */
+  double cfl_target;         /* CFDGB_DT_CFL: the CFL number each step aims at (default 0.5) */
+  double dt_max;             /* CFDGB_DT_CFL: upper bound of dt (default: cfdgb_config.dt) */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {
@@ -130,6 +150,8 @@ typedef struct cfdgb_step_stats {
   double relres;     /* final relative residual of the solve (FP64) */
   double cd, cl;     /* drag and lift coefficients (CD_CL, virtualForceIntergrator.hpp:92) */
   double cfl;        /* CFL number of u* (get_Cfl, inc/analyses/cfl.hpp:3, src/RUN_CPU.cpp:274) */
+  double dt;         /* dt of this step */
+  double time;       /* simulated time at the end of this step (simu.time after finishloop) */
 } cfdgb_step_stats;
 
 /* Library identity and last error text (thread-local). */
@@ -261,9 +283,8 @@ int cfdgb_op_solid_fraction(cfdgb_ctx *ctx, double *eta);
 int cfdgb_op_cfl(cfdgb_ctx *ctx, const double *us, const double *vs, const double *ws, double *out7);
 
 /* ---- time step and output ---- */
-/* New dt for the following steps (simu.dt; the adaptive step of timestepper,
- * inc/0_1_SimulationVariable.hpp:172, which the reference leaves switched off at
- * src/RUN_CPU.cpp:275, is the caller's choice: each step reports its CFL number). */
+/* New dt for the following steps (simu.dt).  With an adaptive cfdgb_dt_mode the next
+ * step's own rule takes over again after that step. */
 int cfdgb_set_dt(cfdgb_ctx *ctx, double dt);
 /* Plot3D files of the current state, byte-compatible with the reference's writers:
  * xpath (may be NULL) the grid file of OutputPlot3D_Xfile (inc/io/Plot3D/xfileWrite.hpp:6),

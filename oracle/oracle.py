@@ -222,6 +222,20 @@ def cfl(g, dt, us, vs, ws):
     return out
 
 
+def timestepper(Re, U_max, U_min, dt_min=1e-12, cfl_factor=0.05, grid_fo_factor=0.15):
+    """simpulationVariable::timestepper (inc/0_1_SimulationVariable.hpp:172-185) with its
+    factors (:270-272): dt_next from the velocity extremes get_Cfl keeps, each product in
+    the reference's left-to-right order, std::min as (b < a ? b : a)."""
+    d = 1e10
+    for x in U_max:
+        lim = cfl_factor / (Re * x * x) if Re * x * x != 0.0 else float("inf")
+        d = lim if lim < d else d
+    for x in U_min:
+        lim = grid_fo_factor * 0.5 * Re * x * x
+        d = lim if lim < d else d
+    return dt_min if d < dt_min else d
+
+
 def plot3d(g, p, u, v, w, eta, Re, time, qpath, xpath):
     """The reference's Plot3D .q and .x files (qfile.hpp, xfileWrite.hpp)."""
     L = lib()

@@ -42,13 +42,15 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 6
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 7
     assert cfg.scheme == cg.QUICK and cfg.les == 0 and cfg.walls == cg.WALLS_ZERO_GRADIENT
+    assert cfg.dt_mode == cg.DT_FIXED and cfg.cfl_target == 0.5 and cfg.dt_max == 0.0
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
                                          ("precision", 3), ("tol", 0.0), ("maxit", 0), ("scheme", 3),
-                                         ("scheme", -1), ("les", 2), ("walls", 2)])
+                                         ("scheme", -1), ("les", 2), ("walls", 2), ("dt_mode", 3),
+                                         ("dt_mode", -1)])
 def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     cfg = cg.default_config()
     setattr(cfg, field, value)
@@ -57,6 +59,19 @@ def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     assert rc == cg.EINVAL
     assert h.value is None
     assert lib.cfdgb_last_error()
+
+
+def test_cfl_timestep_needs_a_positive_target(lib):
+    cfg = cg.default_config(dt_mode="cfl", cfl_target=0.0)
+    h = C.c_void_p()
+    assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
+
+
+def test_timestepper_restatement():
+    """The oracle's timestepper (0_1_SimulationVariable.hpp:172-185): the CFL limit of each
+    component's maximum, the grid-Fourier limit of its minimum, the 1e-12 floor."""
+    assert O.timestepper(100.0, [1.0, 0.5, 0.0], [0.5, -0.5, -0.3]) == min(0.05 / 100.0, 0.075 * 100 * 0.09)
+    assert O.timestepper(100.0, [1.0, 0.5, 0.0], [0.5, -0.5, 0.0]) == 1e-12
 
 
 def test_mixed_sor_combination_rejected(lib):
