@@ -110,6 +110,8 @@ KERNEL_WORDS = {
     "cg_p64": 3,       # read r, p; write p
     "cg_pq32": 4,      # read r, p; write p', q
     "cg_xr32": 6,      # read x, p, r, q; write x, r
+    # the same preconditioned iteration in FP64 (fp64_mg)
+    "bicgp_p64": 4, "bicgp_v64": 3, "bicgp_s64": 3, "bicgp_t64": 3, "bicgp_xr64": 8,
 }
 
 
@@ -117,6 +119,7 @@ KERNEL_WORDS = {
 # SpMV 1 mul + 6 FMA, each dot 1 FMA, each axpy-like update 1 FMA per term
 KERNEL_FP64_FLOPS = {"bicg_ap64": 15, "bicg_s64": 2, "bicg_as64": 17, "bicg_xr64": 10, "bicg_p64": 4,
                      "cg_q64": 15, "cg_xr64": 6, "cg_p64": 2}
+
 
 
 FP_PEAK_SRC = ROOT / "bench_fp_peak.cu"
@@ -257,11 +260,11 @@ def _timed_steps(s, steps, dist, torch):
 
 
 def run_mode(cg, torch, dist, wl, steps, warmup, solver, precision, maxit=5000, profile=True, keep_fields=False,
-             precond="none"):
+             precond="none", **extra):
     """solver None: the case's own FP64 solver; the case's tolerance throughout."""
     cfg, wsolver, tol = workload(wl)
     with cg.Solver(solver=solver or wsolver, precision=precision, tol=tol, maxit=maxit, precond=precond,
-                   **cfg) as s:
+                   **cfg, **extra) as s:
         s.init_fields()
         s.step(warmup, allow_noconv=True)
         s.reset_counters()
@@ -424,6 +427,115 @@ def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file)
     return r, share
 
 
+# the modes beside the FP64 value: (solver, precision, preconditioner, what it is).  Each
+# MIXED mode has an FP64 counterpart with the same solver (PRECISION_PAIR), so that its
+# speed-up over that one isolates the precision; against `value` it also includes the
+# change of solver.
+MODES = {
+    "cg": ("cg", "fp64", "none", "cg (SPE operator), FP64"),
+    "fp64_mg": ("jacobi", "fp64", "multigrid",
+                "jacobi bicgstab right-preconditioned by an FP64 multigrid V-cycle, FP64"),
+    "mixed": ("jacobi", "mixed", "none", "jacobi bicgstab, FP32 sweeps in FP64 refinement"),
+    "mixed_cg": ("cg", "mixed", "none", "cg (SPE operator), FP32 sweeps in FP64 refinement"),
+    "mixed_mg": ("jacobi", "mixed", "multigrid",
+                 "jacobi bicgstab, FP32 sweeps right-preconditioned by an FP32 multigrid V-cycle, in FP64 refinement"),
+}
+PRECISION_PAIR = {"mixed": "fp64", "mixed_cg": "cg", "mixed_mg": "fp64_mg"}
+
+
+def measure_mode(cg, torch, dist, wl, key, steps, warmup, maxit, fp64, t64, hbm_peak, peak_kind, traffic_file,
+                 keep_fields=True, profile=True):
+    """One mode of MODES on the workload: its timed window, solve record, errors against the
+    FP64 run (when fp64 holds its fields) and per-kernel roofline."""
+    solver, prec, precond, what = MODES[key]
+    _, _, tol = workload(wl)
+    rm = run_mode(cg, torch, dist, wl, steps, warmup, solver, prec, maxit=maxit, keep_fields=keep_fields,
+                  precond=precond, profile=profile)
+    tm = dist.max(rm["ms"])
+    cells = rm["cells"]
+    out = {"value": cells * steps * dist.world / (tm / 1e3), "ms_per_step": tm / steps, "solver": what,
+           "precision": prec, "iters_per_step": [r.iters for r in rm["stats"]],
+           "outer_per_step": [r.outer for r in rm["stats"]], "relres": max(r.relres for r in rm["stats"]),
+           **solve_counts(rm["stats"], tol), "speedup_vs_fp64": t64 / tm if t64 else None,
+           "gpu_launches": rm["launches"], "device_mem_gb": rm["device_mem_gb"]}
+    if fp64 is not None and "fields" in fp64 and "fields" in rm:
+        out["error_vs_fp64"] = field_errors(rm, fp64)
+    if profile:
+        word, suffix = (4, "32") if prec == "mixed" else (8, "64")
+        out["roofline"], out["kernel_share"] = roofline(rm["kernels"], cells, word, suffix, hbm_peak, peak_kind,
+                                                        traffic_file)
+    rm.pop("fields", None)
+    return out, rm
+
+
+def precision_speedups(line, t64, steps):
+    """Each MIXED mode against the FP64 mode with the same solver (precision alone)."""
+    out = {}
+    for m, ref in PRECISION_PAIR.items():
+        a = line.get(m) or {}
+        b = {"ms_per_step": t64 / steps} if ref == "fp64" else (line.get(ref) or {})
+        if a.get("ms_per_step") and b.get("ms_per_step"):
+            out[m] = {"against": ref, "speedup": b["ms_per_step"] / a["ms_per_step"]}
+            a["speedup_vs_fp64_same_solver"] = out[m]["speedup"]
+    return out
+
+
+def subline(cg, torch, dist, wl, steps, warmup, maxit, hbm_peak, peak_kind):
+    """A short measurement of a second workload (the 1024x512x128 case the mixed-precision
+    target is quoted on): every solver and precision pair, per-step time, iterations and,
+    for the MIXED modes, the sweep kernels' fraction of the HBM bandwidth.  The FP64 modes
+    are timed without the per-kernel pass (their kernels are the FP64 pipe's)."""
+    traffic_file = ROOT / "profiles" / f"traffic_{wl}.json"
+    base = run_mode(cg, torch, dist, wl, steps, warmup, None, "fp64", maxit=maxit, profile=False)
+    t64 = dist.max(base["ms"])
+    _, _, tol = workload(wl)
+    out = {"workload": wl, "config": bench_config(wl, maxit, dist.world), "steps": steps, "warmup": warmup,
+           "fp64": {"value": base["cells"] * steps * dist.world / (t64 / 1e3), "ms_per_step": t64 / steps,
+                    "iters_per_step": [r.iters for r in base["stats"]], **solve_counts(base["stats"], tol)}}
+    for key in ("cg", "fp64_mg", "mixed_cg", "mixed_mg"):
+        prof = MODES[key][1] == "mixed"
+        out[key], _ = measure_mode(cg, torch, dist, wl, key, steps, warmup, maxit, None, t64, hbm_peak, peak_kind,
+                                   traffic_file, keep_fields=False, profile=prof)
+        r = out[key].pop("roofline", None)
+        if r:
+            out[key]["hbm_frac"] = {k: v["frac"] for k, v in r["per_kernel"].items()}
+        out[key].pop("kernel_share", None)
+    out["precision_speedup"] = precision_speedups(out, t64, steps)
+    return out
+
+
+def sor_legs(cg, torch, dist, wl, args, cells, tol):
+    """Red-black SOR twice: at the optimal relaxation of the grid (omega = 0 picks it: Young's
+    2 / (1 + sqrt(1 - mu^2)), mu the Jacobi spectral radius), timed to the tolerance, and at
+    omega = 1.7, capped at --sor-maxit sweeps, with the sweeps the Jacobi spectral radius
+    predicts it would need (its value is that of an unconverged solve, so it reports none)."""
+    import math
+    c = WORKLOADS[wl]
+    h = [c["lx"] / c["nx"], c["ly"] / c["ny"], c["lz"] / c["nz"]]
+    w = [1 / x ** 2 for x in h]
+    low = min(wa * (1 - math.cos(math.pi / n)) for wa, n in zip(w, (c["nx"], c["ny"], c["nz"])) if n > 1)
+    mu = 1 - low / sum(w)
+    opt = 2 / (1 + math.sqrt(1 - mu * mu))
+    so = run_mode(cg, torch, dist, wl, args.sor_steps, args.warmup, "rbsor", "fp64", maxit=args.sor_maxit,
+                  profile=False, omega=0.0)
+    ts = dist.max(so["ms"])
+    out = {"value": cells * args.sor_steps * dist.world / (ts / 1e3), "ms_per_step": ts / args.sor_steps,
+           "steps": args.sor_steps, "omega": opt, "sweeps_per_step": [r.iters for r in so["stats"]],
+           "relres": [r.relres for r in so["stats"]], "status": [r.status for r in so["stats"]],
+           **solve_counts(so["stats"], tol)}
+    s17 = run_mode(cg, torch, dist, wl, 1, args.warmup, "rbsor", "fp64", maxit=args.sor_maxit, profile=False,
+                   omega=1.7)
+    # red-black SOR at omega below the optimum: rate from the largest root of
+    # lambda - omega mu sqrt(lambda) + omega - 1 = 0 (Young), sweeps = ln(tol) / ln(rate)
+    om = 1.7
+    sq = (om * mu + math.sqrt(max(0.0, om * om * mu * mu - 4 * (om - 1)))) / 2
+    out["omega_1_7"] = {"value": None, "omega": om, "sweeps_cap": args.sor_maxit,
+                        "relres": [r.relres for r in s17["stats"]], "status": [r.status for r in s17["stats"]],
+                        "predicted_sweeps_to_tol": round(math.log(tol) / math.log(sq * sq)),
+                        "note": "unreachable at omega 1.7 within the cap; the leg above uses the optimal omega"}
+    return out
+
+
 def reference_build(wl, flavour="native"):
     """The reference's own build for a case and the harness's name of its solver."""
     from oracle import build_ref
@@ -571,7 +683,9 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cfdgb", choices=["cfdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--modes", default="fp64,mixed,mixed_mg,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
+    ap.add_argument("--modes", default="fp64,mixed,fp64_mg,mixed_mg,cg,mixed_cg,rbsor,e2e,adjoint,cpu")
+    ap.add_argument("--c3-steps", type=int, default=2,
+                    help="timed steps of the 1024x512x128 sub-line (0: none)")
     ap.add_argument("--adj-steps", type=int, default=30)
     ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--adj-workload", default="c4", choices=sorted(WORKLOADS))
@@ -604,7 +718,7 @@ def main(argv=None):
     fp_peak = alu_peaks()
     with Clocks(dist.local) as clk:
         fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64", maxit=args.maxit,
-                        keep_fields=bool(modes & {"mixed", "mixed_mg", "cg", "mixed_cg"}))
+                        keep_fields=bool(modes & set(MODES)))
     t64 = dist.max(fp64["ms"])
     cells = fp64["cells"]
     value = cells * args.steps * dist.world / (t64 / 1e3)
@@ -627,61 +741,21 @@ def main(argv=None):
         # the metric names the tolerance: say plainly that some timed solves missed it
         line["failure"] = (f"{rec64['unconverged_solves']} of {args.steps} timed solves ended at or above "
                            f"relres {tol:g} ({rec64['capped_solves']} at the {args.maxit}-iteration cap)")
-    if "mixed" in modes:
+    results = {"fp64": fp64}
+    for key in [m for m in MODES if m in modes]:
         try:
-            mx = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", maxit=args.maxit,
-                          keep_fields=True)
-            tm = dist.max(mx["ms"])
-            r32, share32 = roofline(mx["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
-            line["mixed"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
-                             "iters_per_step": [r.iters for r in mx["stats"]],
-                             "outer_per_step": [r.outer for r in mx["stats"]],
-                             "relres": max(r.relres for r in mx["stats"]), **solve_counts(mx["stats"], tol), "speedup_vs_fp64": t64 / tm,
-                             "error_vs_fp64": field_errors(mx, fp64),
-                             "gpu_launches": mx["launches"], "device_mem_gb": mx["device_mem_gb"],
-                             "roofline": r32, "kernel_share": share32}
-        except cg.CfdgbError as e:
-            line["mixed"] = {"value": None, "error": str(e)}
-    if "mixed_mg" in modes:
-        try:
-            mg = run_mode(cg, torch, dist, wl, args.steps, args.warmup, "jacobi", "mixed", maxit=args.maxit,
-                          keep_fields=True, precond="multigrid")
-            tm = dist.max(mg["ms"])
-            rg, shg = roofline(mg["kernels"], cells, 4, "32", hbm_peak, peak_kind, traffic_file)
-            line["mixed_mg"] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
-                                "solver": "jacobi bicgstab, FP32 sweeps right-preconditioned by a multigrid V-cycle",
-                                "iters_per_step": [r.iters for r in mg["stats"]],
-                                "outer_per_step": [r.outer for r in mg["stats"]],
-                                "relres": max(r.relres for r in mg["stats"]), **solve_counts(mg["stats"], tol), "speedup_vs_fp64": t64 / tm,
-                                "error_vs_fp64": field_errors(mg, fp64), "gpu_launches": mg["launches"],
-                                "device_mem_gb": mg["device_mem_gb"], "roofline": rg, "kernel_share": shg}
-        except cg.CfdgbError as e:
-            line["mixed_mg"] = {"value": None, "error": str(e)}
-    for key, solver, prec in (("cg", "cg", "fp64"), ("mixed_cg", "cg", "mixed")):
-        if key not in modes:
-            continue
-        try:
-            rm = run_mode(cg, torch, dist, wl, args.steps, args.warmup, solver, prec, maxit=args.maxit,
-                          keep_fields=True)
-            tm = dist.max(rm["ms"])
-            rf, shr = roofline(rm["kernels"], cells, 4 if prec == "mixed" else 8, "32" if prec == "mixed" else "64",
-                               hbm_peak, peak_kind, traffic_file)
-            line[key] = {"value": cells * args.steps * dist.world / (tm / 1e3), "ms_per_step": tm / args.steps,
-                         "solver": "cg (SPE operator)", "precision": prec,
-                         "iters_per_step": [r.iters for r in rm["stats"]],
-                         "outer_per_step": [r.outer for r in rm["stats"]],
-                         "relres": max(r.relres for r in rm["stats"]), **solve_counts(rm["stats"], tol), "speedup_vs_fp64": t64 / tm,
-                         "error_vs_fp64": field_errors(rm, fp64), "gpu_launches": rm["launches"],
-                         "device_mem_gb": rm["device_mem_gb"], "roofline": rf, "kernel_share": shr}
+            line[key], results[key] = measure_mode(cg, torch, dist, wl, key, args.steps, args.warmup, args.maxit,
+                                                   fp64, t64, hbm_peak, peak_kind, traffic_file)
         except cg.CfdgbError as e:
             line[key] = {"value": None, "error": str(e)}
+    line["precision_speedup"] = precision_speedups(line, t64, args.steps)
+    if args.c3_steps > 0 and wl != "c3":
+        try:
+            line["c3"] = subline(cg, torch, dist, "c3", args.c3_steps, args.warmup, args.maxit, hbm_peak, peak_kind)
+        except cg.CfdgbError as e:
+            line["c3"] = {"error": str(e)}
     if "rbsor" in modes:
-        sr = run_mode(cg, torch, dist, wl, args.sor_steps, args.warmup, "rbsor", "fp64", maxit=args.sor_maxit,
-                      profile=False)
-        ts = dist.max(sr["ms"])
-        line["rbsor"] = {"value": cells * args.sor_steps * dist.world / (ts / 1e3), "steps": args.sor_steps,
-                         "omega": 1.7, "sweeps_per_step": [r.iters for r in sr["stats"]],
-                         "relres": [r.relres for r in sr["stats"]], "status": [r.status for r in sr["stats"]]}
+        line["rbsor"] = sor_legs(cg, torch, dist, wl, args, cells, tol)
     if "e2e" in modes:
         ms, nbytes, _ = e2e_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64")
         te = dist.max(ms)

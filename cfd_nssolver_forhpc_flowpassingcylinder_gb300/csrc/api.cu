@@ -60,14 +60,16 @@ enum KId {
   K_CONVDIFF, K_RHS, K_SETUP64, K_AP64, K_S64, K_AS64, K_XR64, K_P64, K_PAP32, K_SAS32, K_XR32,
   K_RESID64, K_SETUP32, K_CORRECT64, K_TRANSFORM, K_UPDATE, K_BC, K_RBSOR, K_RNORM, K_NANRESET, K_ETA,
   K_CGQ64, K_CGXR64, K_CGP64, K_CGPQ32, K_CGXR32, K_CFL, K_LES,
-  K_PP32, K_MG, K_PV32, K_PS32, K_PT32, K_PXR32, K_MIRROR, K_COUNT
+  K_PP32, K_MG, K_PV32, K_PS32, K_PT32, K_PXR32, K_MIRROR,
+  K_PP64, K_MG64, K_PV64, K_PS64, K_PT64, K_PXR64, K_COUNT
 };
 const char *const kKernelNames[K_COUNT] = {
     "convection_diffusion", "rhs", "bicg_setup64", "bicg_ap64", "bicg_s64", "bicg_as64", "bicg_xr64",
     "bicg_p64", "bicg_pap32", "bicg_sas32", "bicg_xr32", "residual64", "refine32",
     "correct64", "transform", "update_uf", "bc", "rbsor_sweep", "residual_norm64", "nan_reset", "solid_fraction",
     "cg_q64", "cg_xr64", "cg_p64", "cg_pq32", "cg_xr32", "cfl", "smagorinsky",
-    "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32", "mirror32"};
+    "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32", "mirror32",
+    "bicgp_p64", "mg_vcycle64", "bicgp_v64", "bicgp_s64", "bicgp_t64", "bicgp_xr64"};
 
 struct PendingEv {
   int id;
@@ -100,6 +102,10 @@ struct cfdgb_ctx {
   bool use_mg = false;
   MgPlan mg{};
   float *ph32 = nullptr, *sh32 = nullptr;
+  // the same preconditioner in FP64 for the FP64 BiCGSTAB (precision FP64, precond multigrid)
+  bool use_mg64 = false;
+  MgPlanT<double> mg64{};
+  double *ph64 = nullptr, *sh64 = nullptr;
   // MIXED QUICK: FP32 copies of the padded u, v, w that the FP32 stencil sweep reads
   float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;
   double *part = nullptr;
@@ -111,6 +117,10 @@ struct cfdgb_ctx {
   // chunk graphs of solver iterations
   cudaGraphExec_t chunk64 = nullptr, chunk32 = nullptr;
   int chunk_len = 16;
+  double omega = 0.0;  // SOR relaxation in use (cfg.omega, or the optimal one when that is 0)
+  // test switch (environment CFDGB_TEST_WAIT_FAULT at create): the next MIXED solve makes one
+  // bounded wait of the FP32 bulk-copy pipeline run out, to exercise that failure path
+  bool test_wait_fault = false;
   // scratch for the per-function entry points (allocated on first use)
   double *op[10] = {nullptr};
   // Plot3D staging: five float32 arrays on the device and a pinned host copy
@@ -326,6 +336,24 @@ std::vector<float> build_tab32(const cfdgb_ctx *c, int L) {
   return t;
 }
 
+// The optimal SOR relaxation for the uniform-grid Neumann operator: 2 / (1 + sqrt(1 - mu^2))
+// with mu the spectral radius of the Jacobi iteration on the non-constant modes, the mode
+// with one half-wave along the axis where c_a (1 - cos(pi / n_a)) is least (c_a = 1/h_a^2):
+// mu = 1 - min_a c_a (1 - cos(pi / n_a)) / (c_x + c_y + c_z)  (Young's theorem for red-black
+// ordering, which is consistently ordered).
+double sor_omega_opt(const cfdgb_config *c) {
+  const double h[3] = {c->lx / c->nx, c->ly / c->ny, c->lz / c->nz};
+  const int n[3] = {c->nx, c->ny, c->nz};
+  double sum = 0.0, low = 1e300;
+  for (int a = 0; a < 3; ++a) {
+    const double w = 1.0 / (h[a] * h[a]);
+    sum += w;
+    if (n[a] > 1) low = std::min(low, w * (1.0 - std::cos(3.14159265358979323846 / n[a])));
+  }
+  const double mu = 1.0 - low / sum;
+  return 2.0 / (1.0 + std::sqrt(std::max(0.0, 1.0 - mu * mu)));
+}
+
 int validate(const cfdgb_config *c) {
   if (!c) return fail(CFDGB_EINVAL, "null config");
   if (c->nx < 3 || c->ny < 3 || c->nz < 3) return fail(CFDGB_EINVAL, "grid must be at least 3x3x3 interior cells");
@@ -337,7 +365,7 @@ int validate(const cfdgb_config *c) {
   if (c->precision < 0 || c->precision > 1) return fail(CFDGB_EINVAL, "unknown precision %d", c->precision);
   if (!(c->tol > 0)) return fail(CFDGB_EINVAL, "tol must be positive");
   if (c->maxit < 1) return fail(CFDGB_EINVAL, "maxit must be >= 1");
-  if (c->solver == CFDGB_RBSOR && !(c->omega > 0 && c->omega < 2)) return fail(CFDGB_EINVAL, "omega outside (0,2)");
+  if (c->solver == CFDGB_RBSOR && !(c->omega >= 0 && c->omega < 2)) return fail(CFDGB_EINVAL, "omega outside [0,2)");
   if (c->precision == CFDGB_MIXED && c->solver == CFDGB_RBSOR)
     return fail(CFDGB_EINVAL, "MIXED precision is implemented for the Krylov solvers");
   if (c->precision == CFDGB_MIXED && !(c->inner_tol >= 0 && c->inner_tol < 1))
@@ -351,9 +379,8 @@ int validate(const cfdgb_config *c) {
   if (c->precond != CFDGB_PRECOND_NONE && c->precond != CFDGB_PRECOND_MULTIGRID)
     return fail(CFDGB_EINVAL, "unknown precond %d", c->precond);
   if (c->precond == CFDGB_PRECOND_MULTIGRID) {
-    if (c->precision != CFDGB_MIXED || (c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI) ||
-        c->grid != CFDGB_GRID_UNIFORM)
-      return fail(CFDGB_EINVAL, "the multigrid preconditioner is for the MIXED BiCGSTAB solvers on a uniform grid");
+    if ((c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI) || c->grid != CFDGB_GRID_UNIFORM)
+      return fail(CFDGB_EINVAL, "the multigrid preconditioner is for the BiCGSTAB solvers on a uniform grid");
     MgPlan mg;
     if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, false, &mg))
       return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
@@ -379,32 +406,50 @@ int validate(const cfdgb_config *c) {
 // The multigrid-preconditioned FP32 iteration: p, M p, v = A M p, s, M s, t = A M s, x/r
 constexpr int kPrecParts = 7;
 const int kPrecKid[kPrecParts] = {K_PP32, K_MG, K_PV32, K_PS32, K_MG, K_PT32, K_PXR32};
+const int kPrecKid64[kPrecParts] = {K_PP64, K_MG64, K_PV64, K_PS64, K_MG64, K_PT64, K_PXR64};
+
+// the iteration of this precision is the multigrid-preconditioned one
+bool prec_iter(const cfdgb_ctx *c, bool fp32) { return fp32 ? c->use_mg : c->use_mg64; }
 
 int iter_kernels(const cfdgb_ctx *c, bool fp32) {
-  if (fp32 && c->use_mg) return kPrecParts;
+  if (prec_iter(c, fp32)) return kPrecParts;
   if (c->cfg.solver == CFDGB_CG) return fp32 ? 2 : 3;
   return fp32 ? 3 : 5;
 }
 int iter_kid(const cfdgb_ctx *c, bool fp32, int part) {
-  if (fp32 && c->use_mg) return kPrecKid[part];
+  if (prec_iter(c, fp32)) return (fp32 ? kPrecKid : kPrecKid64)[part];
   if (c->cfg.solver == CFDGB_CG) return (fp32 ? K_CGPQ32 : K_CGQ64) + part;
   return (fp32 ? K_PAP32 : K_AP64) + part;
 }
 // kernels one part launches (a V-cycle is many)
 int iter_part_launches(const cfdgb_ctx *c, bool fp32, int part) {
-  return iter_kid(c, fp32, part) == K_MG ? mg_vcycle_launches(c->mg) : 1;
+  const int k = iter_kid(c, fp32, part);
+  return k == K_MG ? mg_vcycle_launches(c->mg) : k == K_MG64 ? mg_vcycle_launches(c->mg64) : 1;
 }
 // iterations per captured chunk: the preconditioned iteration is long and needs few
-int chunk_iters(const cfdgb_ctx *c, bool fp32) { return fp32 && c->use_mg ? 2 : c->chunk_len; }
+int chunk_iters(const cfdgb_ctx *c, bool fp32) { return prec_iter(c, fp32) ? 2 : c->chunk_len; }
 void launch_iter_kernel(cfdgb_ctx *c, bool fp32, int part) {
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  if (!fp32 && c->use_mg64) {
+    PrecVecsT<double> v{c->k64.x, c->k64.r0, c->k64.r1, c->k64.p1, c->k64.ap, c->k64.s, c->k64.as, c->ph64, c->sh64,
+                        nullptr};
+    const int jf = jac ? 1 : 0;
+    switch (part) {
+      case 1: launch_mg_vcycle(c->stream, c->mg64, jf, (const double *)v.p, v.ph, c->sc); break;
+      case 4: launch_mg_vcycle(c->stream, c->mg64, jf, (const double *)v.s, v.sh, c->sc); break;
+      default:
+        launch_bicgp64_part(c->stream, part == 0 ? 0 : part == 2 ? 1 : part == 3 ? 2 : part == 5 ? 3 : 4, c->g,
+                            jac ? c->jac64 : c->spe64, v, c->part, c->sc);
+    }
+    return;
+  }
   if (fp32 && c->use_mg) {
     PrecVecs v{c->k32.x, c->k32.r0, c->k32.r1, c->p32[0], c->ap32[0], c->k32.s, c->k32.as, c->ph32, c->sh32,
                c->k32.xb};
     const int jf = jac ? 1 : 0;
     switch (part) {
-      case 1: launch_mg_vcycle(c->stream, c->mg, jf, v.p, v.ph, c->sc32); break;
-      case 4: launch_mg_vcycle(c->stream, c->mg, jf, v.s, v.sh, c->sc32); break;
+      case 1: launch_mg_vcycle(c->stream, c->mg, jf, (const float *)v.p, v.ph, c->sc32); break;
+      case 4: launch_mg_vcycle(c->stream, c->mg, jf, (const float *)v.s, v.sh, c->sc32); break;
       default:
         launch_bicgp32_part(c->stream, part == 0 ? 0 : part == 2 ? 1 : part == 3 ? 2 : part == 5 ? 3 : 4, c->g,
                             jac ? c->jac32 : c->spe32, v, c->part, c->sc32);
@@ -518,7 +563,8 @@ void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
   if (c->cfg.solver == CFDGB_CG)
     launch_cg_setup64(c->stream, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc);
   else
-    launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc);
+    launch_bicg_setup64(c->stream, c->nblk, c->g, st64, c->k64, c->b, c->px1, c->px2, c->part, c->sc,
+                        c->use_mg64 ? 1 : 0);
 }
 
 // createBMatrix + solve + (caller) transform, on the current u*.  Fills iters/relres.
@@ -526,7 +572,10 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
   L(c, K_RHS, 1, [&] {
-    launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, c->us, c->vs, c->ws, jac, c->jac64, c->b);
+    if (c->cfg.precision == CFDGB_MIXED)
+      launch_rhs_fast(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, c->us, c->vs, c->ws, jac, c->jac64, c->b);
+    else
+      launch_rhs_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, c->us, c->vs, c->ws, jac, c->jac64, c->b);
   });
   if (c->cfg.project_rhs)
     L(c, K_RHS, 2, [&] { launch_project_rhs(c->stream, c->g, st64, jac ? 1 : 0, c->b, c->part, c->ss); });
@@ -547,7 +596,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
         break;
       }
       for (int q = 0; q < c->cfg.check_every; ++q)
-        L(c, K_RBSOR, 2, [&] { launch_rbsor_sweep(c->stream, c->nblk, c->g, c->spe64, c->b, c->x, c->cfg.omega); });
+        L(c, K_RBSOR, 2, [&] { launch_rbsor_sweep(c->stream, c->nblk, c->g, c->spe64, c->b, c->x, c->omega); });
       sweeps += c->cfg.check_every;
     }
     *iters = sweeps;
@@ -595,6 +644,11 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   }
   if (rel < c->cfg.tol) return 0;
   TRY(set_solver_params(c, c->sc32, c->cfg.tol, c->cfg.maxit));
+  if (c->test_wait_fault) {  // one shot
+    static const int one = 1;
+    CK(cudaMemcpyAsync(&c->sc32->test_wait, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->test_wait_fault = false;
+  }
   L(c, K_SETUP32, 1, [&] {
     launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), sweep_peak(c), 1,
                           c->part, c->sc32);
@@ -798,6 +852,19 @@ int ensure_op_buffers(cfdgb_ctx *c) {
   return 0;
 }
 
+// the coarsest level's dense pseudo-inverse, when it is small enough
+template <typename T>
+int upload_dense_coarse(cfdgb_ctx *c, MgPlanT<T> &mg) {
+  std::vector<T> M;
+  mg.cinv = nullptr;
+  if (!mg_dense_inverse(mg, M)) return 0;
+  T *d = nullptr;
+  TRY(dalloc(c, &d, M.size()));
+  CK(cudaMemcpy(d, M.data(), M.size() * sizeof(T), cudaMemcpyHostToDevice));
+  mg.cinv = d;
+  return 0;
+}
+
 int h2d(cfdgb_ctx *c, double *d, const double *h, size_t n) {
   CK(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   return 0;
@@ -880,6 +947,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   // reduction grid: a fixed number of resident blocks
   c->nblk = (int)std::min<long long>((c->ncell + kBlock - 1) / kBlock, (long long)c->nsm * 8);
   c->chunk_len = c->ncell > (1LL << 22) ? 8 : 32;
+  c->omega = cfg->omega > 0.0 ? cfg->omega : sor_omega_opt(cfg);
+  c->test_wait_fault = std::getenv("CFDGB_TEST_WAIT_FAULT") != nullptr;
   int rc = 0;
   const int nmet = nx + ny + nz;
   if ((rc = dalloc(c, &c->metric, 2 * (size_t)nmet))) return bail(rc);
@@ -1016,9 +1085,24 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     if ((rc = dalloc(c, &c->u32, c->npad)) || (rc = dalloc(c, &c->v32, c->npad)) || (rc = dalloc(c, &c->w32, c->npad)))
       return bail(rc);
   }
-  if (cfg->precond == CFDGB_PRECOND_MULTIGRID) {  // levels >= 1 and the vectors M p, M s
+  if (cfg->precond == CFDGB_PRECOND_MULTIGRID && cfg->precision == CFDGB_FP64) {  // the FP64 hierarchy
+    mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm, false,
+            &c->mg64);
+    mg_prepare<double>();
+    if ((rc = upload_dense_coarse(c, c->mg64))) return bail(rc);
+    if ((rc = dalloc(c, &c->ph64, c->ncell)) || (rc = dalloc(c, &c->sh64, c->ncell))) return bail(rc);
+    for (int l = 1; l < c->mg64.nlev; ++l) {
+      MgLevelT<double> &L = c->mg64.lev[l];
+      const size_t n = (size_t)L.nx * L.ny * L.nz;
+      if ((rc = dalloc(c, &L.x, n)) || (rc = dalloc(c, &L.b, n))) return bail(rc);
+    }
+    c->use_mg64 = true;
+  }
+  if (cfg->precond == CFDGB_PRECOND_MULTIGRID && cfg->precision == CFDGB_MIXED) {  // levels >= 1, M p, M s
     mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm,
             !std::getenv("CFDGB_SCALAR_FP32"), &c->mg);
+    mg_prepare<float>();
+    if ((rc = upload_dense_coarse(c, c->mg))) return bail(rc);
     if ((rc = dalloc(c, &c->ph32, c->ncell)) || (rc = dalloc(c, &c->sh32, c->ncell))) return bail(rc);
     for (int l = 1; l < c->mg.nlev; ++l) {
       MgLevel &L = c->mg.lev[l];

@@ -236,6 +236,8 @@ struct SolverScal {
   int iter, maxit, done, status, timestep, restart;
   int par;                   // FP32: p[par], ap[par] hold the previous iteration's vectors
   int fault;                 // FP32: a pipeline wait of a stencil kernel gave up (never expected)
+  int test_wait;             // FP32: one-shot test request: the next pipelined launch makes
+                             // one of its waits run out (CFDGB_TEST_WAIT_FAULT; tests only)
   unsigned cnt[8];           // last-block counters, one per kernel kind
 };
 // status of an FP32 solve that stopped for an FP64 refinement (never returned to callers)

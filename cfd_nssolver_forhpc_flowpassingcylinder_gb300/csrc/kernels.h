@@ -1,6 +1,8 @@
 // Kernel launchers shared between the translation units (all enqueue on stream s).
 #pragma once
 
+#include <vector>
+
 #include "cfdgb_internal.cuh"
 
 namespace cfdgb {
@@ -54,6 +56,9 @@ void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const d
 void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
                          const double *u, const double *v, const double *w, const float *u32, const float *v32,
                          const float *w32, double *us, double *vs, double *ws, const StepCtl &sc);
+// MIXED: createBMatrix with the reciprocal metrics (multiplications)
+void launch_rhs_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, const double *us,
+                     const double *vs, const double *ws, int jacobi, const Stencil<double> &st, double *b);
 // padded FP32 copies of u, v, w (rounded to nearest)
 void launch_mirror32(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w, float *u32,
                      float *v32, float *w32);
@@ -70,7 +75,7 @@ void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out);
 // FP64 BiCGSTAB (bicgstabRe2) set-up: r0 = b - A x, r1 = p1 = r0, history px2 <- px1 <- x
 void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st,
                          KrylovVecs<double> v, const double *b, double *px1, double *px2, double *part,
-                         SolverScal *sc);
+                         SolverScal *sc, int restart = 0);
 // FP64 iteration, kernel `part` 0..4 (ap, s, as, xr, p); each a no-op once sc->done is set
 void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
                         double *part_buf, SolverScal *sc);
@@ -135,39 +140,67 @@ void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st,
 constexpr int kMgMaxLevels = 16;
 constexpr int kMgCoarseCells = 64;      // coarsening stops at or below this many cells
 constexpr int kMgSharedCells = 4096;    // largest coarsest level solved in one block
-struct MgLevel {
+constexpr int kMgDenseCells = 256;      // largest coarsest level solved by its dense pseudo-inverse
+template <typename T>
+struct MgLevelT {
   int nx, ny, nz;          // cells
-  float wx, wy, wz;        // 1/h^2 per axis
+  T wx, wy, wz;            // 1/h^2 per axis
   int fx, fy, fz;          // cells of this level per cell of the next one, per axis (1, 2)
-  float *x, *b;            // correction and right-hand side (levels >= 1)
+  T *x, *b;                // correction and right-hand side (levels >= 1)
   int bx, by, gx, gy, gz;  // launch geometry: bx along k, by along j, gz planes strided over i
-  int qgrid;               // blocks of the quad smoother (nz % 4 == 0), 0: the scalar one
+  int qgrid;               // blocks of the quad smoother (FP32, nz % 4 == 0), 0: the scalar one
+  // 1/diag of a row by its neighbour counts along x, y, z (each 0..2): idg[9 cx + 3 cy + cz]
+  // (0 where a row has no neighbour); the smoother multiplies instead of dividing
+  T idg[27];
 };
-struct MgPlan {
+template <typename T>
+struct MgPlanT {
   int nlev;
   int coarse_sweeps;  // red-black sweeps of the coarsest solve
   int tail;           // levels tail..nlev-1 run in one block's shared memory (tail >= 1); nlev: none
-  MgLevel lev[kMgMaxLevels];
+  const T *cinv;      // the coarsest level's dense pseudo-inverse (device), or null: red-black sweeps
+  MgLevelT<T> lev[kMgMaxLevels];
 };
+using MgLevel = MgLevelT<float>;
+using MgPlan = MgPlanT<float>;
 // levels of an nx x ny x nz grid with spacing hx, hy, hz (arrays left null); false when
-// the grid has a single level too large for the one-block coarsest solve
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlan *mg);
+// the grid has a single level too large for the one-block coarsest solve.  T: the element
+// type of the hierarchy (float: the MIXED sweeps' preconditioner; double: FP64's)
+template <typename T>
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg);
 // kernels one V-cycle launches
-int mg_vcycle_launches(const MgPlan &mg);
+template <typename T>
+int mg_vcycle_launches(const MgPlanT<T> &mg);
+// the pseudo-inverse of the coarsest level's operator, row-major, when that level has at
+// most kMgDenseCells cells (the caller uploads it and sets mg.cinv)
+template <typename T>
+bool mg_dense_inverse(const MgPlanT<T> &mg, std::vector<T> &M);
+// kernel attributes the hierarchy needs (shared memory of the one-block kernels); once,
+// before the first V-cycle
+template <typename T>
+void mg_prepare();
 // x0 = M b0, one V(1,1) cycle: red-black Gauss-Seidel smoothing from a zero start,
 // averaging restriction, cell-centred trilinear prolongation, a one-block red-black solve
 // on the coarsest level.  jacobi: b0 holds Jacobi-scaled rows (jp = 1/diag), so M applies
 // to diag * b0.  Every kernel returns at once when sc->done is set.
-void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float *b0, float *x0, const SolverScal *sc);
+template <typename T>
+void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T *b0, T *x0, const SolverScal *sc);
 
 // FP32 BiCGSTAB with a right preconditioner M (the V-cycle), kernel `part` 0..4:
 // 0 p = r1 + beta (p - omega v) (or r1 on restart, r0 = r1); 1 v = A ph, alpha;
 // 2 s = r1 - alpha v; 3 t = A sh, omega; 4 x += alpha ph + omega sh, r1 = s - omega t,
 // stop test and beta.  ph = M p and sh = M s come from the V-cycles between them.
-struct PrecVecs {
-  float *x, *r0, *r1, *p, *v, *s, *t, *ph, *sh, *xb;
+template <typename T>
+struct PrecVecsT {
+  T *x, *r0, *r1, *p, *v, *s, *t, *ph, *sh, *xb;
 };
+using PrecVecs = PrecVecsT<float>;
 void launch_bicgp32_part(cudaStream_t s, int part, const Geo &g, const Stencil<float> &st, PrecVecs v,
+                         double *part_buf, SolverScal *sc);
+// The FP64 iteration with the FP64 V-cycle as right preconditioner (the same five kernels
+// and order; xb unused): the like-for-like FP64 counterpart of the MIXED multigrid sweep.
+// It stops on the tolerance or the cap and restarts only on a Lanczos breakdown.
+void launch_bicgp64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, PrecVecsT<double> v,
                          double *part_buf, SolverScal *sc);
 
 // red-black SOR on the same operator (FP64)

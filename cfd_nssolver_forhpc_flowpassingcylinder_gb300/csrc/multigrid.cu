@@ -14,6 +14,8 @@
 // level and reads sc->done first, so a captured chunk of iterations idles once the sweep
 // has stopped.
 #include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include "cfdgb_internal.cuh"
 #include "kernels.h"
@@ -26,20 +28,29 @@ namespace cfdgb {
   const bool on_ = (k < (L).nz) && (j < (L).ny);       \
   for (int i = blockIdx.z; on_ && i < (L).nx; i += gridDim.z)
 
-__device__ __forceinline__ long long lrow(const MgLevel &L, int i, int j, int k) {
+template <typename T>
+__device__ __forceinline__ long long lrow(const MgLevelT<T> &L, int i, int j, int k) {
   return ((long long)i * L.ny + j) * L.nz + k;
 }
 
 // diagonal of a Neumann row: the weights of the neighbours that exist
-__device__ __forceinline__ float ldiag(const MgLevel &L, int i, int j, int k) {
-  return L.wx * (float)((i > 0) + (i < L.nx - 1)) + L.wy * (float)((j > 0) + (j < L.ny - 1)) +
-         L.wz * (float)((k > 0) + (k < L.nz - 1));
+template <typename T>
+__device__ __forceinline__ T ldiag(const MgLevelT<T> &L, int i, int j, int k) {
+  return L.wx * (T)((i > 0) + (i < L.nx - 1)) + L.wy * (T)((j > 0) + (j < L.ny - 1)) +
+         L.wz * (T)((k > 0) + (k < L.nz - 1));
+}
+
+// 1/diag of the row (ldiag's reciprocal, from the level's table)
+template <typename T>
+__device__ __forceinline__ T linv(const MgLevelT<T> &L, int i, int j, int k) {
+  return L.idg[9 * ((i > 0) + (i < L.nx - 1)) + 3 * ((j > 0) + (j < L.ny - 1)) + ((k > 0) + (k < L.nz - 1))];
 }
 
 // weighted sum of the neighbours' values (minus the off-diagonal part of the row)
-__device__ __forceinline__ float lnb(const MgLevel &L, const float *x, int i, int j, int k, long long r) {
+template <typename T>
+__device__ __forceinline__ T lnb(const MgLevelT<T> &L, const T *x, int i, int j, int k, long long r) {
   const long long sx = (long long)L.ny * L.nz;
-  float a = 0.f, b = 0.f, c = 0.f;
+  T a = T(0), b = T(0), c = T(0);
   if (i > 0) a += x[r - sx];
   if (i < L.nx - 1) a += x[r + sx];
   if (j > 0) b += x[r - L.nz];
@@ -52,20 +63,20 @@ __device__ __forceinline__ float lnb(const MgLevel &L, const float *x, int i, in
 // One colour of a red-black Gauss-Seidel sweep (colour = (i + j + k) & 1).  zero: x starts
 // at zero, so the cells of this colour take b / diag and the others are set to zero.
 // bscale: b holds Jacobi-scaled rows (b / diag), which are unscaled first.
-__global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, int colour, int zero, int bscale,
-                                                      const float *__restrict__ b, float *x, const SolverScal *sc) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevelT<T> L, int colour, int zero, int bscale,
+                                                      const T *__restrict__ b, T *x, const SolverScal *sc) {
   if (sc->done) return;
   FOR_LEVEL(L) {
     const long long r = lrow(L, i, j, k);
     if (((i + j + k) & 1) != colour) {
-      if (zero) x[r] = 0.f;
+      if (zero) x[r] = T(0);
       continue;
     }
-    const float d = ldiag(L, i, j, k);
-    float bb = b[r];
-    if (bscale) bb *= d;
-    const float num = zero ? bb : bb + lnb(L, x, i, j, k, r);
-    x[r] = d > 0.f ? num / d : 0.f;
+    T bb = b[r];
+    if (bscale) bb *= ldiag(L, i, j, k);
+    const T num = zero ? bb : bb + lnb(L, x, i, j, k, r);
+    x[r] = num * linv(L, i, j, k);
   }
 }
 
@@ -93,9 +104,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
           o[c] = 0.f;
           continue;
         }
-        const float d = ldiag(L, (int)i, (int)j, k0 + c);
-        const float bb = bscale ? bv[c] * d : bv[c];
-        o[c] = d > 0.f ? bb / d : 0.f;
+        const float bb = bscale ? bv[c] * ldiag(L, (int)i, (int)j, k0 + c) : bv[c];
+        o[c] = bb * linv(L, (int)i, (int)j, k0 + c);
       }
     } else {
       const float4 xq = *reinterpret_cast<const float4 *>(x + r);
@@ -121,9 +131,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
         if (jp) e += ypv[c];
         if (k > 0) f += c == 0 ? kl : xv[c - 1];
         if (k < L.nz - 1) f += c == 3 ? kr : xv[c + 1];
-        const float d = ldiag(L, (int)i, (int)j, k);
-        const float bb = bscale ? bv[c] * d : bv[c];
-        o[c] = d > 0.f ? (bb + (L.wx * a + L.wy * e + L.wz * f)) / d : 0.f;
+        const float bb = bscale ? bv[c] * ldiag(L, (int)i, (int)j, k) : bv[c];
+        o[c] = (bb + (L.wx * a + L.wy * e + L.wz * f)) * linv(L, (int)i, (int)j, k);
       }
     }
     *reinterpret_cast<float4 *>(x + r) = make_float4(o[0], o[1], o[2], o[3]);
@@ -131,20 +140,21 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
 }
 
 // bc = average over each coarse cell's children of the fine residual b - A x
-__global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel Cl, int bscale, const float *__restrict__ bf,
-                                                        const float *__restrict__ xf, float *__restrict__ bc,
-                                                        const SolverScal *sc) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevelT<T> F, MgLevelT<T> Cl, int bscale,
+                                                        const T *__restrict__ bf, const T *__restrict__ xf,
+                                                        T *__restrict__ bc, const SolverScal *sc) {
   if (sc->done) return;
-  const float inv = 1.0f / (float)(F.fx * F.fy * F.fz);
+  const T inv = T(1) / (T)(F.fx * F.fy * F.fz);
   FOR_LEVEL(Cl) {
-    float sum = 0.f;
+    T sum = T(0);
     for (int a = 0; a < F.fx; ++a)
       for (int e = 0; e < F.fy; ++e)
         for (int c = 0; c < F.fz; ++c) {
           const int fi = i * F.fx + a, fj = j * F.fy + e, fk = k * F.fz + c;
           const long long r = lrow(F, fi, fj, fk);
-          const float d = ldiag(F, fi, fj, fk);
-          float bb = bf[r];
+          const T d = ldiag(F, fi, fj, fk);
+          T bb = bf[r];
           if (bscale) bb *= d;
           sum += bb - d * xf[r] + lnb(F, xf, fi, fj, fk, r);
         }
@@ -153,11 +163,12 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel Cl, i
 }
 
 // the two coarse cells a fine cell interpolates from along one axis, and their weights
-__device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], float (&w)[2]) {
+template <typename T>
+__device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], T (&w)[2]) {
   if (f == 1) {
     c[0] = c[1] = i;
-    w[0] = 1.f;
-    w[1] = 0.f;
+    w[0] = T(1);
+    w[1] = T(0);
     return;
   }
   const int p = i >> 1;
@@ -165,104 +176,262 @@ __device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], floa
   if (q < 0 || q >= n) q = p;  // beyond a wall: the parent's value (zero normal gradient)
   c[0] = p;
   c[1] = q;
-  w[0] = 0.75f;
-  w[1] = 0.25f;
+  w[0] = T(0.75);
+  w[1] = T(0.25);
+}
+
+// (P xc) at fine cell (i, j, k): cell-centred trilinear interpolation
+template <typename T>
+__device__ __forceinline__ T prolong_at(const MgLevelT<T> &F, const MgLevelT<T> &Cl, const T *__restrict__ xc, int i,
+                                        int j, int k) {
+  int ci[2], cj[2], ck[2];
+  T wi[2], wj[2], wk[2];
+  axis_taps(i, F.fx, Cl.nx, ci, wi);
+  axis_taps(j, F.fy, Cl.ny, cj, wj);
+  axis_taps(k, F.fz, Cl.nz, ck, wk);
+  T v = T(0);
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const T w = wi[a] * wj[e] * wk[c];
+        if (w != T(0)) v += w * xc[lrow(Cl, ci[a], cj[e], ck[c])];
+      }
+  return v;
 }
 
 // xf += P xc
-__global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel Cl, const float *__restrict__ xc,
-                                                       float *__restrict__ xf, const SolverScal *sc) {
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevelT<T> F, MgLevelT<T> Cl, const T *__restrict__ xc,
+                                                       T *__restrict__ xf, const SolverScal *sc) {
   if (sc->done) return;
   FOR_LEVEL(F) {
-    int ci[2], cj[2], ck[2];
-    float wi[2], wj[2], wk[2];
-    axis_taps(i, F.fx, Cl.nx, ci, wi);
-    axis_taps(j, F.fy, Cl.ny, cj, wj);
-    axis_taps(k, F.fz, Cl.nz, ck, wk);
-    float v = 0.f;
+    xf[lrow(F, i, j, k)] += prolong_at(F, Cl, xc, i, j, k);
+  }
+}
+
+// ---- transfers when every axis halves (fx = fy = fz = 2): one thread per coarse cell,
+// its eight children loaded once (pairs along k as one vector load) and their neighbours
+// shared, the arithmetic and summation order of k_mg_restrict / k_mg_prolong ----
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+template <typename T>
+__device__ __forceinline__ void ld2(const T *p, T &a, T &b) {
+  const typename Vec2<T>::type v = *reinterpret_cast<const typename Vec2<T>::type *>(p);
+  a = v.x;
+  b = v.y;
+}
+template <typename T>
+__device__ __forceinline__ void st2(T *p, T a, T b) {
+  typename Vec2<T>::type v;
+  v.x = a;
+  v.y = b;
+  *reinterpret_cast<typename Vec2<T>::type *>(p) = v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT<T> Cl, int bscale,
+                                                         const T *__restrict__ bf, const T *__restrict__ xf,
+                                                         T *__restrict__ bc, const SolverScal *sc) {
+  if (sc->done) return;
+  const T inv = T(1) / T(8);
+  const long long sx = (long long)F.ny * F.nz, sy = F.nz;
+  FOR_LEVEL(Cl) {
+    const int i0 = 2 * i, j0 = 2 * j, k0 = 2 * k;
+    const long long r0 = lrow(F, i0, j0, k0);
+    T xv[2][2][2], bv[2][2][2], xim[2][2], xip[2][2], xjm[2][2], xjp[2][2], xkm[2][2], xkp[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const long long r = r0 + a * sx + e * sy;
+        ld2(xf + r, xv[a][e][0], xv[a][e][1]);
+        ld2(bf + r, bv[a][e][0], bv[a][e][1]);
+        xkm[a][e] = k0 > 0 ? xf[r - 1] : T(0);
+        xkp[a][e] = k0 + 2 < F.nz ? xf[r + 2] : T(0);
+      }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {  // x neighbours of the i0 and i0+1 planes
+      if (i0 > 0) ld2(xf + r0 - sx + e * sy, xim[e][0], xim[e][1]);
+      else xim[e][0] = xim[e][1] = T(0);
+      if (i0 + 2 < F.nx) ld2(xf + r0 + 2 * sx + e * sy, xip[e][0], xip[e][1]);
+      else xip[e][0] = xip[e][1] = T(0);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {  // y neighbours
+      if (j0 > 0) ld2(xf + r0 + a * sx - sy, xjm[a][0], xjm[a][1]);
+      else xjm[a][0] = xjm[a][1] = T(0);
+      if (j0 + 2 < F.ny) ld2(xf + r0 + a * sx + 2 * sy, xjp[a][0], xjp[a][1]);
+      else xjp[a][0] = xjp[a][1] = T(0);
+    }
+    T sum = T(0);
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
       for (int e = 0; e < 2; ++e)
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
-          const float w = wi[a] * wj[e] * wk[c];
-          if (w != 0.f) v += w * xc[lrow(Cl, ci[a], cj[e], ck[c])];
+          const int fi = i0 + a, fj = j0 + e, fk = k0 + c;
+          T ax = T(0), ay = T(0), az = T(0);  // lnb's terms in its order
+          if (fi > 0) ax += a ? xv[0][e][c] : xim[e][c];
+          if (fi < F.nx - 1) ax += a ? xip[e][c] : xv[1][e][c];
+          if (fj > 0) ay += e ? xv[a][0][c] : xjm[a][c];
+          if (fj < F.ny - 1) ay += e ? xjp[a][c] : xv[a][1][c];
+          if (fk > 0) az += c ? xv[a][e][0] : xkm[a][e];
+          if (fk < F.nz - 1) az += c ? xkp[a][e] : xv[a][e][1];
+          const T d = ldiag(F, fi, fj, fk);
+          T bb = bv[a][e][c];
+          if (bscale) bb *= d;
+          sum += bb - d * xv[a][e][c] + (F.wx * ax + F.wy * ay + F.wz * az);
         }
-    xf[lrow(F, i, j, k)] += v;
+    bc[lrow(Cl, i, j, k)] = sum * inv;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_mg_prolong8(MgLevelT<T> F, MgLevelT<T> Cl, const T *__restrict__ xc,
+                                                        T *__restrict__ xf, const SolverScal *sc) {
+  if (sc->done) return;
+  const long long sx = (long long)F.ny * F.nz, sy = F.nz;
+  FOR_LEVEL(Cl) {
+    // the 3 x 3 x 3 coarse neighbourhood; beyond a wall the parent's value (axis_taps)
+    T cv[3][3][3];
+    const int ci[3] = {i > 0 ? i - 1 : i, i, i < Cl.nx - 1 ? i + 1 : i};
+    const int cj[3] = {j > 0 ? j - 1 : j, j, j < Cl.ny - 1 ? j + 1 : j};
+    const int ck[3] = {k > 0 ? k - 1 : k, k, k < Cl.nz - 1 ? k + 1 : k};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cv[a][e][c] = xc[lrow(Cl, ci[a], cj[e], ck[c])];
+    const T w0 = T(0.75), w1 = T(0.25);
+    const long long r0 = lrow(F, 2 * i, 2 * j, 2 * k);
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        T out[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          // taps: the parent (index 1) and the neighbour on the child's side (0 or 2), in
+          // k_mg_prolong's order (parent first on every axis) and weights
+          const int ti[2] = {1, a ? 2 : 0}, tj[2] = {1, e ? 2 : 0}, tk[2] = {1, c ? 2 : 0};
+          const T wa[2] = {w0, w1};
+          T v = T(0);
+#pragma unroll
+          for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+#pragma unroll
+              for (int t = 0; t < 2; ++t) v += wa[p] * wa[q] * wa[t] * cv[ti[p]][tj[q]][tk[t]];
+          out[c] = v;
+        }
+        T *dst = xf + r0 + a * sx + e * sy;
+        T x0, x1;
+        ld2(dst, x0, x1);
+        st2(dst, x0 + out[0], x1 + out[1]);
+      }
   }
 }
 
 // coarsest level: x = 0, then `sweeps` red-black sweeps in shared memory, one block
-__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevel L, int sweeps, int bscale, const float *__restrict__ b,
-                                                    float *__restrict__ x, const SolverScal *sc) {
-  if (sc->done) return;
-  extern __shared__ float sm[];
-  const int n = L.nx * L.ny * L.nz;
-  float *xs = sm, *bs = sm + n;
+// x = M b on the coarsest level with the precomputed pseudo-inverse M (n x n, row-major):
+// one dot product of length n per cell (the block's shared copies of b, x)
+template <typename T>
+__device__ void blk_dense(int n, const T *__restrict__ M, const T *bs, T *xs) {
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int k = q % L.nz, t = q / L.nz, j = t % L.ny, i = t / L.ny;
-    float bb = b[q];
-    if (bscale) bb *= ldiag(L, i, j, k);
-    bs[q] = bb;
-    xs[q] = 0.f;
+    const T *row = M + (long long)q * n;
+    T v = T(0);
+    for (int c = 0; c < n; ++c) v += row[c] * bs[c];
+    xs[q] = v;
   }
   __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_coarse(MgLevelT<T> L, int sweeps, const T *__restrict__ M, int bscale,
+                                                    const T *__restrict__ b, T *__restrict__ x, const SolverScal *sc) {
+  if (sc->done) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T *sm = reinterpret_cast<T *>(smraw);
+  const int n = L.nx * L.ny * L.nz;
+  T *xs = sm, *bs = sm + n;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int k = q % L.nz, t = q / L.nz, j = t % L.ny, i = t / L.ny;
+    T bb = b[q];
+    if (bscale) bb *= ldiag(L, i, j, k);
+    bs[q] = bb;
+    xs[q] = T(0);
+  }
+  __syncthreads();
+  if (M) {
+    blk_dense(n, M, bs, xs);
+    sweeps = 0;
+  }
   for (int s = 0; s < sweeps; ++s)
     for (int colour = 0; colour < 2; ++colour) {
       for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int k = q % L.nz, t = q / L.nz, j = t % L.ny, i = t / L.ny;
         if (((i + j + k) & 1) != colour) continue;
-        const float d = ldiag(L, i, j, k);
-        xs[q] = d > 0.f ? (bs[q] + lnb(L, xs, i, j, k, q)) / d : 0.f;
+        xs[q] = (bs[q] + lnb(L, xs, i, j, k, q)) * linv(L, i, j, k);
       }
       __syncthreads();
     }
   for (int q = threadIdx.x; q < n; q += blockDim.x) x[q] = xs[q];
 }
 
-// ---- the small levels in one block: levels t..nlev-1 together hold at most kMgTailCells
-// cells, x and b of each in shared memory; the same smoothing, transfers and coarsest solve
-// as the per-level kernels (same arithmetic, same order), a barrier between phases where
-// the per-level path has a launch ----
-constexpr int kMgTailCells = 6144;  // 2 arrays of floats: 48 KB of shared memory
+// ---- the small levels in one block: levels t..nlev-1 together hold at most
+// kMgTailBytes / (2 sizeof(T)) cells, x and b of each in shared memory; the same smoothing,
+// transfers and coarsest solve as the per-level kernels (same arithmetic, same order), a
+// barrier between phases where the per-level path has a launch ----
+// 48 KB: one block working on more cells per barrier (a 16K-cell level, 192 KB) ran slower
+// than the same level's launched kernels (measured on 512x256x64)
+constexpr int kMgTailBytes = 48 * 1024;
+template <typename T>
+constexpr int tail_cells_max() { return kMgTailBytes / (2 * (int)sizeof(T)); }
 
-__device__ __forceinline__ void cell_ijk(const MgLevel &L, int q, int &i, int &j, int &k) {
+template <typename T>
+__device__ __forceinline__ void cell_ijk(const MgLevelT<T> &L, int q, int &i, int &j, int &k) {
   k = q % L.nz;
   const int t = q / L.nz;
   j = t % L.ny;
   i = t / L.ny;
 }
 
-__device__ void blk_smooth(const MgLevel &L, int colour, int zero, const float *b, float *x) {
+template <typename T>
+__device__ void blk_smooth(const MgLevelT<T> &L, int colour, int zero, const T *b, T *x) {
   const int n = L.nx * L.ny * L.nz;
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     int i, j, k;
     cell_ijk(L, q, i, j, k);
     if (((i + j + k) & 1) != colour) {
-      if (zero) x[q] = 0.f;
+      if (zero) x[q] = T(0);
       continue;
     }
-    const float d = ldiag(L, i, j, k);
-    const float num = zero ? b[q] : b[q] + lnb(L, x, i, j, k, q);
-    x[q] = d > 0.f ? num / d : 0.f;
+    const T num = zero ? b[q] : b[q] + lnb(L, x, i, j, k, q);
+    x[q] = num * linv(L, i, j, k);
   }
   __syncthreads();
 }
 
-__device__ void blk_restrict(const MgLevel &F, const MgLevel &Cl, const float *bf, const float *xf, float *bc) {
-  const float inv = 1.0f / (float)(F.fx * F.fy * F.fz);
+template <typename T>
+__device__ void blk_restrict(const MgLevelT<T> &F, const MgLevelT<T> &Cl, const T *bf, const T *xf, T *bc) {
+  const T inv = T(1) / (T)(F.fx * F.fy * F.fz);
   const int n = Cl.nx * Cl.ny * Cl.nz;
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     int i, j, k;
     cell_ijk(Cl, q, i, j, k);
-    float sum = 0.f;
+    T sum = T(0);
     for (int a = 0; a < F.fx; ++a)
       for (int e = 0; e < F.fy; ++e)
         for (int c = 0; c < F.fz; ++c) {
           const int fi = i * F.fx + a, fj = j * F.fy + e, fk = k * F.fz + c;
           const long long r = lrow(F, fi, fj, fk);
-          const float d = ldiag(F, fi, fj, fk);
+          const T d = ldiag(F, fi, fj, fk);
           sum += bf[r] - d * xf[r] + lnb(F, xf, fi, fj, fk, r);
         }
     bc[q] = sum * inv;
@@ -270,37 +439,25 @@ __device__ void blk_restrict(const MgLevel &F, const MgLevel &Cl, const float *b
   __syncthreads();
 }
 
-__device__ void blk_prolong(const MgLevel &F, const MgLevel &Cl, const float *xc, float *xf) {
+template <typename T>
+__device__ void blk_prolong(const MgLevelT<T> &F, const MgLevelT<T> &Cl, const T *xc, T *xf) {
   const int n = F.nx * F.ny * F.nz;
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     int i, j, k;
     cell_ijk(F, q, i, j, k);
-    int ci[2], cj[2], ck[2];
-    float wi[2], wj[2], wk[2];
-    axis_taps(i, F.fx, Cl.nx, ci, wi);
-    axis_taps(j, F.fy, Cl.ny, cj, wj);
-    axis_taps(k, F.fz, Cl.nz, ck, wk);
-    float v = 0.f;
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int e = 0; e < 2; ++e)
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          const float w = wi[a] * wj[e] * wk[c];
-          if (w != 0.f) v += w * xc[lrow(Cl, ci[a], cj[e], ck[c])];
-        }
-    xf[q] += v;
+    xf[q] += prolong_at(F, Cl, xc, i, j, k);
   }
   __syncthreads();
 }
 
 // x_t = V-cycle of levels t..nlev-1 on b_t (both in global memory, level t >= 1)
-__global__ void __launch_bounds__(1024) k_mg_tail(MgPlan mg, int t, const SolverScal *sc) {
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_tail(MgPlanT<T> mg, int t, const SolverScal *sc) {
   if (sc->done) return;
-  extern __shared__ float sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T *sm = reinterpret_cast<T *>(smraw);
   const int n = mg.nlev;
-  float *xs[kMgMaxLevels], *bs[kMgMaxLevels];
+  T *xs[kMgMaxLevels], *bs[kMgMaxLevels];
   int off = 0;
   for (int l = t; l < n; ++l) {
     const int c = mg.lev[l].nx * mg.lev[l].ny * mg.lev[l].nz;
@@ -316,14 +473,18 @@ __global__ void __launch_bounds__(1024) k_mg_tail(MgPlan mg, int t, const Solver
     blk_smooth(mg.lev[l], 1, 0, bs[l], xs[l]);
     blk_restrict(mg.lev[l], mg.lev[l + 1], bs[l], xs[l], bs[l + 1]);
   }
-  {  // coarsest: x = 0, then red-black sweeps (k_mg_coarse)
-    const MgLevel &C = mg.lev[n - 1];
+  {  // coarsest: the dense pseudo-inverse, or x = 0 and red-black sweeps (k_mg_coarse)
+    const MgLevelT<T> &C = mg.lev[n - 1];
     const int nc = C.nx * C.ny * C.nz;
-    for (int q = threadIdx.x; q < nc; q += blockDim.x) xs[n - 1][q] = 0.f;
-    __syncthreads();
-    for (int s = 0; s < mg.coarse_sweeps; ++s) {
-      blk_smooth(C, 0, 0, bs[n - 1], xs[n - 1]);
-      blk_smooth(C, 1, 0, bs[n - 1], xs[n - 1]);
+    if (mg.cinv) {
+      blk_dense(nc, mg.cinv, bs[n - 1], xs[n - 1]);
+    } else {
+      for (int q = threadIdx.x; q < nc; q += blockDim.x) xs[n - 1][q] = T(0);
+      __syncthreads();
+      for (int s = 0; s < mg.coarse_sweeps; ++s) {
+        blk_smooth(C, 0, 0, bs[n - 1], xs[n - 1]);
+        blk_smooth(C, 1, 0, bs[n - 1], xs[n - 1]);
+      }
     }
   }
   for (int l = n - 2; l >= t; --l) {
@@ -334,7 +495,8 @@ __global__ void __launch_bounds__(1024) k_mg_tail(MgPlan mg, int t, const Solver
   for (int q = threadIdx.x; q < nt; q += blockDim.x) mg.lev[t].x[q] = xs[t][q];
 }
 
-static void level_geometry(MgLevel &L, int nsm, bool quads) {
+template <typename T>
+static void level_geometry(MgLevelT<T> &L, int nsm, bool quads) {
   L.bx = 1;
   while (L.bx < L.nz && L.bx < 32) L.bx *= 2;
   L.by = kBlock / L.bx;
@@ -342,20 +504,28 @@ static void level_geometry(MgLevel &L, int nsm, bool quads) {
   L.gy = (L.ny + L.by - 1) / L.by;
   L.gz = std::max(1, std::min(L.nx, nsm * 8 / std::max(1, L.gx * L.gy)));
   const long long nquads = (long long)L.nx * L.ny * (L.nz / 4);
-  L.qgrid = quads && L.nz % 4 == 0 ? (int)std::max(1LL, std::min((nquads + kBlock - 1) / kBlock, 8LL * nsm)) : 0;
+  // the quad smoother is FP32 (float4 loads)
+  L.qgrid = quads && sizeof(T) == sizeof(float) && L.nz % 4 == 0
+                ? (int)std::max(1LL, std::min((nquads + kBlock - 1) / kBlock, 8LL * nsm))
+                : 0;
 }
 
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlan *mg) {
-  *mg = MgPlan{};
+template <typename T>
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg) {
+  *mg = MgPlanT<T>{};
   int l = 0;
   for (;;) {
-    MgLevel &L = mg->lev[l];
+    MgLevelT<T> &L = mg->lev[l];
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
-    L.wx = (float)(1.0 / (hx * hx));
-    L.wy = (float)(1.0 / (hy * hy));
-    L.wz = (float)(1.0 / (hz * hz));
+    L.wx = (T)(1.0 / (hx * hx));
+    L.wy = (T)(1.0 / (hy * hy));
+    L.wz = (T)(1.0 / (hz * hz));
+    for (int q = 0; q < 27; ++q) {  // the diagonal as ldiag sums it, then its reciprocal
+      const T d = L.wx * (T)(q / 9) + L.wy * (T)((q / 3) % 3) + L.wz * (T)(q % 3);
+      L.idg[q] = d > T(0) ? T(1) / d : T(0);
+    }
     level_geometry(L, nsm, quads);
     const long long cells = (long long)nx * ny * nz;
     const int fx = nx % 2 == 0 ? 2 : 1, fy = ny % 2 == 0 ? 2 : 1, fz = nz % 2 == 0 ? 2 : 1;
@@ -380,58 +550,149 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
   long long tail_cells = 0;
   for (int t = mg->nlev - 1; t >= 1; --t) {
     tail_cells += (long long)mg->lev[t].nx * mg->lev[t].ny * mg->lev[t].nz;
-    if (tail_cells > kMgTailCells) break;
+    if (tail_cells > tail_cells_max<T>()) break;
     mg->tail = t;
   }
-  const MgLevel &C = mg->lev[l];
+  const MgLevelT<T> &C = mg->lev[l];
   mg->coarse_sweeps = std::min(256, 16 + 2 * std::max(C.nx, std::max(C.ny, C.nz)));
   return (long long)C.nx * C.ny * C.nz <= kMgSharedCells;
 }
 
 // per level above the tail (or the coarsest): 2 smooths + restrict, prolong + 2 smooths;
 // then one tail (or coarsest) kernel
-int mg_vcycle_launches(const MgPlan &mg) {
+template <typename T>
+int mg_vcycle_launches(const MgPlanT<T> &mg) {
   return mg.tail < mg.nlev ? 6 * mg.tail + 1 : 6 * (mg.nlev - 1) + 1;
 }
 
-void launch_mg_vcycle(cudaStream_t s, const MgPlan &mg, int jacobi, const float *b0, float *x0, const SolverScal *sc) {
+// The pseudo-inverse of the coarsest level's operator (symmetric, singular on constants
+// only): A+ = (A + J/n)^-1 - J/n with J the all-ones matrix, inverted by Gauss-Jordan with
+// partial pivoting in double.  False when the level is larger than kMgDenseCells.
+template <typename T>
+bool mg_dense_inverse(const MgPlanT<T> &mg, std::vector<T> &M) {
+  const MgLevelT<T> &C = mg.lev[mg.nlev - 1];
+  const int n = C.nx * C.ny * C.nz;
+  if (n > kMgDenseCells) return false;
+  std::vector<double> A((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
+  const double wx = (double)C.wx, wy = (double)C.wy, wz = (double)C.wz;
+  for (int i = 0; i < C.nx; ++i)
+    for (int j = 0; j < C.ny; ++j)
+      for (int k = 0; k < C.nz; ++k) {
+        const int r = (i * C.ny + j) * C.nz + k;
+        auto link = [&](int q, double w) {
+          A[(size_t)r * n + q] -= w;
+          A[(size_t)r * n + r] += w;
+        };
+        if (i > 0) link(r - C.ny * C.nz, wx);
+        if (i < C.nx - 1) link(r + C.ny * C.nz, wx);
+        if (j > 0) link(r - C.nz, wy);
+        if (j < C.ny - 1) link(r + C.nz, wy);
+        if (k > 0) link(r - 1, wz);
+        if (k < C.nz - 1) link(r + 1, wz);
+      }
+  for (size_t q = 0; q < A.size(); ++q) A[q] += 1.0 / n;
+  for (int r = 0; r < n; ++r) I[(size_t)r * n + r] = 1.0;
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < n; ++r)
+      if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+    if (!(std::fabs(A[(size_t)piv * n + col]) > 0.0)) return false;
+    if (piv != col)
+      for (int c = 0; c < n; ++c) {
+        std::swap(A[(size_t)piv * n + c], A[(size_t)col * n + c]);
+        std::swap(I[(size_t)piv * n + c], I[(size_t)col * n + c]);
+      }
+    const double inv = 1.0 / A[(size_t)col * n + col];
+    for (int c = 0; c < n; ++c) {
+      A[(size_t)col * n + c] *= inv;
+      I[(size_t)col * n + c] *= inv;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      const double f = A[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int c = 0; c < n; ++c) {
+        A[(size_t)r * n + c] -= f * A[(size_t)col * n + c];
+        I[(size_t)r * n + c] -= f * I[(size_t)col * n + c];
+      }
+    }
+  }
+  M.resize((size_t)n * n);
+  for (size_t q = 0; q < M.size(); ++q) M[q] = (T)(I[q] - 1.0 / n);
+  return true;
+}
+
+template <typename T>
+void mg_prepare() {
+  // the one-block kernels of the FP64 hierarchy need more than the default 48 KB
+  cudaFuncSetAttribute(k_mg_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(2 * sizeof(T) * kMgSharedCells));
+  cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgTailBytes);
+}
+
+template <typename T>
+void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T *b0, T *x0, const SolverScal *sc) {
   const int n = mg.nlev;
-  auto B = [&](int l) -> const float * { return l == 0 ? b0 : mg.lev[l].b; };
-  auto X = [&](int l) -> float * { return l == 0 ? x0 : mg.lev[l].x; };
+  auto B = [&](int l) -> const T * { return l == 0 ? b0 : mg.lev[l].b; };
+  auto X = [&](int l) -> T * { return l == 0 ? x0 : mg.lev[l].x; };
   auto grid = [&](int l) { return dim3(mg.lev[l].gx, mg.lev[l].gy, mg.lev[l].gz); };
   auto block = [&](int l) { return dim3(mg.lev[l].bx, mg.lev[l].by, 1); };
   auto smooth = [&](int l, int colour, int zero) {
-    if (mg.lev[l].qgrid > 0)
-      k_mg_smooth4<<<mg.lev[l].qgrid, kBlock, 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
-    else
-      k_mg_smooth<<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+    if constexpr (sizeof(T) == sizeof(float)) {
+      if (mg.lev[l].qgrid > 0) {
+        k_mg_smooth4<<<mg.lev[l].qgrid, kBlock, 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+        return;
+      }
+    }
+    k_mg_smooth<T><<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
   };
-  const int m = std::min(mg.tail, n);  // levels m..n-1 run in one block (m < n), or none
-  for (int l = 0; l + 1 < m; ++l) {
+  // pre-smoothing from zero and restriction to level l + 1.  (Both colour passes in one
+  // kernel, each black cell recomputing its red neighbours' start values, was measured at
+  // 80 us on the 512x256x64 level against 36 us for the two quad passes: not kept.)
+  auto down = [&](int l) {
+    const int bs = l == 0 ? jacobi : 0;
     smooth(l, 0, 1);
     smooth(l, 1, 0);
-    k_mg_restrict<<<grid(l + 1), block(l + 1), 0, s>>>(mg.lev[l], mg.lev[l + 1], l == 0 ? jacobi : 0, B(l), X(l),
-                                                         mg.lev[l + 1].b, sc);
-  }
+    const MgLevelT<T> &F = mg.lev[l];
+    if (F.fx == 2 && F.fy == 2 && F.fz == 2)
+      k_mg_restrict8<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], bs, B(l), X(l), mg.lev[l + 1].b, sc);
+    else
+      k_mg_restrict<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], bs, B(l), X(l), mg.lev[l + 1].b, sc);
+  };
+  const int m = std::min(mg.tail, n);  // levels m..n-1 run in one block (m < n), or none
+  for (int l = 0; l + 1 < m; ++l) down(l);
   if (m < n) {
-    // levels m-1 -> m: smooth and restrict as above, then the tail
-    smooth(m - 1, 0, 1);
-    smooth(m - 1, 1, 0);
-    k_mg_restrict<<<grid(m), block(m), 0, s>>>(mg.lev[m - 1], mg.lev[m], m == 1 ? jacobi : 0, B(m - 1), X(m - 1),
-                                                 mg.lev[m].b, sc);
+    down(m - 1);  // levels m-1 -> m as above, then the tail
     size_t cells = 0;
     for (int l = m; l < n; ++l) cells += (size_t)mg.lev[l].nx * mg.lev[l].ny * mg.lev[l].nz;
-    k_mg_tail<<<1, 1024, 2 * sizeof(float) * cells, s>>>(mg, m, sc);
+    k_mg_tail<T><<<1, 1024, 2 * sizeof(T) * cells, s>>>(mg, m, sc);
   } else {
-    const MgLevel &C = mg.lev[n - 1];
-    const size_t smem = 2 * sizeof(float) * (size_t)C.nx * C.ny * C.nz;
-    k_mg_coarse<<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
+    const MgLevelT<T> &C = mg.lev[n - 1];
+    const size_t smem = 2 * sizeof(T) * (size_t)C.nx * C.ny * C.nz;
+    k_mg_coarse<T><<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, mg.cinv, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
   }
   for (int l = (m < n ? m : n - 1) - 1; l >= 0; --l) {
-    k_mg_prolong<<<grid(l), block(l), 0, s>>>(mg.lev[l], mg.lev[l + 1], X(l + 1), X(l), sc);
+    const MgLevelT<T> &F = mg.lev[l];
+    if (F.fx == 2 && F.fy == 2 && F.fz == 2)
+      k_mg_prolong8<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], X(l + 1), X(l), sc);
+    else
+      k_mg_prolong<T><<<grid(l), block(l), 0, s>>>(F, mg.lev[l + 1], X(l + 1), X(l), sc);
     smooth(l, 1, 0);
     smooth(l, 0, 0);
   }
 }
+
+template bool mg_plan<float>(int, int, int, double, double, double, int, bool, MgPlanT<float> *);
+template bool mg_plan<double>(int, int, int, double, double, double, int, bool, MgPlanT<double> *);
+template int mg_vcycle_launches<float>(const MgPlanT<float> &);
+template bool mg_dense_inverse<float>(const MgPlanT<float> &, std::vector<float> &);
+template bool mg_dense_inverse<double>(const MgPlanT<double> &, std::vector<double> &);
+template int mg_vcycle_launches<double>(const MgPlanT<double> &);
+template void mg_prepare<float>();
+template void mg_prepare<double>();
+template void launch_mg_vcycle<float>(cudaStream_t, const MgPlanT<float> &, int, const float *, float *,
+                                      const SolverScal *);
+template void launch_mg_vcycle<double>(cudaStream_t, const MgPlanT<double> &, int, const double *, double *,
+                                       const SolverScal *);
 
 }  // namespace cfdgb

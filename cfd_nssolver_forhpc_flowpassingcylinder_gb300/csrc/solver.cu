@@ -99,9 +99,10 @@ __device__ __forceinline__ T spmv_at(const Geo &g, const Stencil<T> &st, const T
 }
 
 // ---- FP64 set-up: bicgstabRe2.hpp:86-106 ----
+// restart: 1 for the preconditioned iteration, whose first p kernel then takes p = r0 = r1
 __global__ void __launch_bounds__(kBlock) k_bicg_setup64(Geo g, Stencil<double> st, KrylovVecs<double> v,
                                                           const double *__restrict__ b, double *px1, double *px2,
-                                                          double *part, SolverScal *sc) {
+                                                          double *part, SolverScal *sc, int restart) {
   double acc[2] = {0.0, 0.0};
   FOR_CELLS(g) {
     const long long row = ROW(g);
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_setup64(Geo g, Stencil<double> 
     sc->iter = 0;
     sc->done = 0;
     sc->status = 0;
-    sc->restart = 0;
+    sc->restart = restart;
     sc->relres = 0.0;
   }
 }
@@ -449,6 +450,109 @@ __global__ void __launch_bounds__(kBlock) k32p_xr(Geo g, PrecVecs v, double *par
   if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_iteration<true>(sc, out[0], out[1]);
 }
 
+// ---- FP64 BiCGSTAB with the FP64 V-cycle as right preconditioner ----
+// The FP32 preconditioned iteration above in FP64 (the like-for-like FP64 counterpart of
+// the MIXED multigrid sweep): same kernels and order, FP64 vectors and dots.  Not the
+// reference's iteration, so no rho-restart rule: it stops on the tolerance, the cap or a
+// non-finite residual, and restarts only on a Lanczos breakdown.
+__device__ __forceinline__ void finish_prec64(SolverScal *sc, double n2, double rr) {
+  const double relres = sqrt(n2) / sc->norm0;
+  sc->relres = relres;
+  sc->iter += 1;
+  if (!isfinite(relres)) {
+    sc->done = 1;
+    sc->status = CFDGB_ENAN;
+  } else if (relres < sc->tol) {
+    sc->done = 1;
+  } else if (sc->iter >= sc->maxit) {
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+  } else {
+    const double rho_old = sc->rho;
+    sc->rho = rr;
+    sc->beta = (sc->alpha / sc->omega) * (rr / rho_old);
+    sc->restart = 0;
+    if (!(isfinite(sc->beta) && sc->omega != 0.0 && rr != 0.0)) {
+      sc->restart = 1;
+      sc->rho = n2;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k64p_p(Geo g, PrecVecsT<double> v, const SolverScal *sc) {
+  if (sc->done) return;
+  const double b = sc->beta, w = sc->omega;
+  const bool rst = sc->restart != 0;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double r1 = v.r1[row];
+    if (rst) {
+      v.r0[row] = r1;
+      v.p[row] = r1;
+    } else {
+      v.p[row] = fma(b, fma(-w, v.v[row], v.p[row]), r1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k64p_v(Geo g, Stencil<double> st, PrecVecsT<double> v, double *part,
+                                                 SolverScal *sc) {
+  if (sc->done) return;
+  double a[1] = {0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double y = spmv_at<double>(g, st, v.ph, ic, jc, kc, row);
+    v.v[row] = y;
+    a[0] = fma(y, v.r0[row], a[0]);
+  }
+  double out[1];
+  if (grid_sum<1>(a, part, &sc->cnt[1], out) && lin_tid() == 0) sc->alpha = sc->rho / out[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k64p_s(Geo g, PrecVecsT<double> v, const SolverScal *sc) {
+  if (sc->done) return;
+  const double a = sc->alpha;
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.s[row] = fma(-a, v.v[row], v.r1[row]);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k64p_t(Geo g, Stencil<double> st, PrecVecsT<double> v, double *part,
+                                                 SolverScal *sc) {
+  if (sc->done) return;
+  double a[2] = {0.0, 0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    const double y = spmv_at<double>(g, st, v.sh, ic, jc, kc, row);
+    v.t[row] = y;
+    a[0] = fma(y, v.s[row], a[0]);
+    a[1] = fma(y, y, a[1]);
+  }
+  double out[2];
+  if (grid_sum<2>(a, part, &sc->cnt[2], out) && lin_tid() == 0) {
+    double wv = out[0] / out[1];
+    if (!(out[1] > 0.0 && isfinite(wv))) wv = 0.0;
+    sc->omega = wv;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k64p_xr(Geo g, PrecVecsT<double> v, double *part, SolverScal *sc) {
+  if (sc->done) return;
+  const double a = sc->alpha, w = sc->omega;
+  double acc[2] = {0.0, 0.0};
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    v.x[row] = fma(w, v.sh[row], fma(a, v.ph[row], v.x[row]));
+    const double r1 = fma(-w, v.t[row], v.s[row]);
+    v.r1[row] = r1;
+    acc[0] = fma(r1, r1, acc[0]);
+    acc[1] = fma(r1, v.r0[row], acc[1]);
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &sc->cnt[3], out) && lin_tid() == 0) finish_prec64(sc, out[0], out[1]);
+}
+
 // ---- FP32 iteration, vectorised: four consecutive k cells per thread (nzc % 4 == 0) ----
 // One float4 load per vector and stencil point instead of four scalar loads; the k
 // neighbours inside the quad come from registers.  Dot partials stay FP32 over the few
@@ -740,6 +844,7 @@ __global__ void __launch_bounds__(kBlock) k32pv_xr(Geo g, PrecVecs v, double *pa
 // own copies in flight and still joins the reduction.
 constexpr int kStages = 4;
 constexpr long long kWaitCycles = 1LL << 32;  // ~2 s at 2 GHz
+constexpr long long kTestWaitCycles = 1LL << 20;  // ~0.5 ms: the wait limit of the test request
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
@@ -760,11 +865,12 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// wait for the phase with the given parity to complete; false if it did not within kWaitCycles
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// wait for the phase with the given parity to complete; false if it did not within `limit`
+// cycles
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = kWaitCycles) {
   const long long t0 = clock64();
   while (!mbar_test(bar, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void bulk_load(float *dst, const float *src, uint32_t bytes, uint64_t *bar) {
@@ -793,7 +899,7 @@ template <class Fv, class F1, class Body>
 __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st, const StageSrc &src, SolverScal *sc,
                                           Fv &&fval, F1 &&f1, Body &&body) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ int bad;
+  __shared__ int bad, test_wait;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + kStages;
   float *stage0 = reinterpret_cast<float *>(smem + 128);
@@ -816,7 +922,9 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     const int s = k % kStages;
     float *dst = stage0 + s * SS;
     const long long plane = (long long)(lo + k) * nyz;
-    mbar_expect_tx(&full[s], txb);
+    // the test request announces 16 bytes more than plane 0's copies bring, so that wait
+    // runs out (every copy issued still lands; nothing is left in flight)
+    mbar_expect_tx(&full[s], txb + (k == 0 && test_wait ? 16u : 0u));
     for (int a = 0; a < src.na; ++a)
       bulk_load(dst + a * SA + (long long)(jlo - (jt - 1)) * nz, src.a[a] + plane + (long long)jlo * nz, hbytes,
                 &full[s]);
@@ -830,8 +938,16 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     bad = 0;
+    // a one-shot request (SolverScal::test_wait, set only by the host's test switch):
+    // block (0,0) of the next pipelined launch takes it
+    test_wait = 0;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && sc->test_wait) {
+      sc->test_wait = 0;
+      test_wait = 1;
+    }
   }
   __syncthreads();
+  const long long wait_limit = test_wait ? kTestWaitCycles : kWaitCycles;
   if (tid == 0)
     for (int k = 0; k <= min(khi, kStages - 1); ++k) issue(k);
   auto fail = [&]() {
@@ -839,7 +955,7 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     atomicExch(&sc->fault, 1);
   };
   auto wait_full = [&](int k) {
-    if (mbar_wait(&full[k % kStages], (k / kStages) & 1)) return true;
+    if (mbar_wait(&full[k % kStages], (k / kStages) & 1, wait_limit)) return true;
     fail();
     return false;
   };
@@ -850,7 +966,7 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
   };
   auto refill = [&](int k) {  // thread 0: plane k was released by every warp -> load plane k + kStages
     if (tid != 0 || k < 0 || k + kStages > khi) return;
-    if (!mbar_wait(&empty[k % kStages], (k / kStages) & 1)) {
+    if (!mbar_wait(&empty[k % kStages], (k / kStages) & 1, wait_limit)) {
       fail();
       return;
     }
@@ -922,7 +1038,7 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     fc = fp;
   }
   if (!ok && tid == 0)  // stopped early: let this block's copies land before it exits
-    for (int k = waited + 1; k <= issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1);
+    for (int k = waited + 1; k <= issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1, wait_limit);
 }
 
 __device__ __forceinline__ F4 lds4(const float *p) {
@@ -1539,7 +1655,7 @@ __global__ void __launch_bounds__(kBlock) k_rbsor(Geo g, Stencil<double> st, con
     if (kc < g.nzc - 1) off += c[4] * x[row + 1];
     if (jc < g.nyc - 1) off += c[5] * x[row + g.nzc];
     if (ic < g.nxc - 1) off += c[6] * x[row + nyz];
-    const double xn = (b[row] - off) / c[3];
+    const double xn = (b[row] - off) * c[7];  // c[7] = 1/diag (no division in the sweep)
     x[row] += omega * (xn - x[row]);
   }
 }
@@ -1596,8 +1712,19 @@ void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out) {
 }
 
 void launch_bicg_setup64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,
-                         const double *b, double *px1, double *px2, double *part, SolverScal *sc) {
-  k_bicg_setup64<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, b, px1, px2, part, sc);
+                         const double *b, double *px1, double *px2, double *part, SolverScal *sc, int restart) {
+  k_bicg_setup64<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, b, px1, px2, part, sc, restart);
+}
+
+void launch_bicgp64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, PrecVecsT<double> v,
+                         double *part_buf, SolverScal *sc) {
+  switch (part) {
+    case 0: k64p_p<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+    case 1: k64p_v<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    case 2: k64p_s<<<cgrid(g), cblock(g), 0, s>>>(g, v, sc); break;
+    case 3: k64p_t<<<cgrid(g), cblock(g), 0, s>>>(g, st, v, part_buf, sc); break;
+    default: k64p_xr<<<cgrid(g), cblock(g), 0, s>>>(g, v, part_buf, sc); break;
+  }
 }
 
 void launch_bicg64_part(cudaStream_t s, int part, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,

@@ -5,6 +5,7 @@
 // the results are bit-identical to the reference (checked against its golden vectors).
 // One thread per interior cell (grid-stride over compact rows, k fastest, so a warp
 // reads contiguous k runs of each padded array).
+#include <algorithm>
 #include <cmath>
 
 #include "cfdgb_internal.cuh"
@@ -132,8 +133,10 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
 // reference's division and order (c = u/Dxs + v/Dys + w/Dzs, a term left out on the last
 // face of its axis), so the CFL number and extremes are those of get_Cfl bit for bit; the
 // maxima are exact in any order.  The last block also sets the next dt (StepCtl).
+// Two resident blocks per SM (at most 128 registers a thread): the kernel is bound by the
+// FP64 pipe, and one block of 8 warps per SM leaves it waiting on latency.
 template <int S>
-__global__ void __launch_bounds__(kBlock) k_convdiff_exact(Geo g, double dt_arg, double nu0,
+__global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_arg, double nu0,
                                                            const double *__restrict__ nut,
                                                            const double *__restrict__ u,
                                                            const double *__restrict__ v,
@@ -524,13 +527,17 @@ __global__ void __launch_bounds__(kBlock) k_bc_z(Geo g, BcTable t, double *u, do
 }
 
 // inc/dfib/setEta.hpp:136-198: per (i,j) column, solid fraction at k = 0 by 100x100
-// sub-sampling of cells within half a cell diagonal of the circle.
+// sub-sampling of cells within half a cell diagonal of the circle.  One warp per column:
+// the lanes split the 100 sub-rows and the warp adds their integer counts (exact in any
+// order), so a band column costs 400 sample tests per lane instead of 10000 in one thread.
 __global__ void __launch_bounds__(kBlock) k_eta_plane(Geo g, const double *__restrict__ X,
                                                       const double *__restrict__ Y, double cx, double cy,
                                                       double R, double *__restrict__ eta) {
   const int nxc = g.nxc, nyc = g.nyc;
-  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nyc; q += gridDim.x * kBlock) {
-    const int i = q / nyc + 2, j = q % nyc + 2;
+  const int lane = threadIdx.x & 31, wpb = kBlock / 32;
+  for (long long q = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); q < (long long)nxc * nyc;
+       q += (long long)gridDim.x * wpb) {
+    const int i = (int)(q / nyc) + 2, j = (int)(q % nyc) + 2;
     const long long icel = pidx(g, i, j, 0);
     const double Diagonal = sqrt(g.Dx[i] * g.Dx[i] + g.Dy[j] * g.Dy[j]) * 0.5;
     const double ddx = ((X[i] + X[i + 1]) * 0.5) - cx;
@@ -540,8 +547,8 @@ __global__ void __launch_bounds__(kBlock) k_eta_plane(Geo g, const double *__res
       const int nsub = 100;
       const double dyg = g.Dy[j] / (double)nsub;
       const double dxg = g.Dx[i] / (double)nsub;
-      long long xi = 0;
-      for (int ii = 0; ii < nsub; ++ii) {
+      unsigned xi = 0;
+      for (int ii = lane; ii < nsub; ii += 32) {
         const double sx0 = X[i] + (double)ii * dxg, sx1 = X[i] + (double)(ii + 1) * dxg;
         const double a = (sx0 + sx1) * 0.5 - cx;
         for (int jj = 0; jj < nsub; ++jj) {
@@ -550,11 +557,10 @@ __global__ void __launch_bounds__(kBlock) k_eta_plane(Geo g, const double *__res
           if (sqrt(a * a + b * b) <= R) ++xi;
         }
       }
-      eta[icel] = (double)xi * (1.0 / ((double)nsub * (double)nsub));
-    } else if (Distance > R) {
-      eta[icel] = 0.;
-    } else {
-      eta[icel] = 1.;
+      xi = __reduce_add_sync(0xffffffffu, xi);
+      if (lane == 0) eta[icel] = (double)xi * (1.0 / ((double)nsub * (double)nsub));
+    } else if (lane == 0) {
+      eta[icel] = Distance > R ? 0. : 1.;
     }
   }
 }
@@ -628,7 +634,10 @@ void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, do
 }
 void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
                 double R, double *eta) {
-  k_eta_plane<<<nblk, kBlock, 0, s>>>(g, X, Y, cx, cy, R, eta);
+  const long long cols = (long long)g.nxc * g.nyc;
+  const int wpb = kBlock / 32;
+  const int blocks = (int)std::min<long long>((cols + wpb - 1) / wpb, 65535LL * 8);
+  k_eta_plane<<<blocks, kBlock, 0, s>>>(g, X, Y, cx, cy, R, eta);
   k_eta_extrude<<<nblk, kBlock, 0, s>>>(g, eta);
 }
 

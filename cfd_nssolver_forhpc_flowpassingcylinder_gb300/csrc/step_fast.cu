@@ -250,6 +250,29 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
   }
 }
 
+// createBMatrix_omp (inc/matrix/b_matrix.hpp:35-98) for the MIXED mode: b = -(jp)(1/dt)
+// div(u*) with the reciprocal metrics (multiplications, not the reference's divisions)
+__global__ void __launch_bounds__(kBlock) k_rhs_fast(Geo g, double dt_arg, const double *dtp,
+                                                     const double *__restrict__ us, const double *__restrict__ vs,
+                                                     const double *__restrict__ ws, int jacobi, Stencil<double> st,
+                                                     double *__restrict__ b) {
+  const double ndt = -1.0 / (dtp ? *dtp : dt_arg);
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long ic = pidx(g, i, j, k);
+    const double div = fma(us[ic] - us[ic - g.sx], g.rDx[i],
+                           fma(vs[ic] - vs[ic - g.sy], g.rDy[j], (ws[ic] - ws[ic - 1]) * g.rDz[k]));
+    b[row] = (jacobi ? row_jp(g, st, i - 2, j - 2, k - 2, row) * ndt : ndt) * div;
+  }
+}
+
+void launch_rhs_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, const double *us,
+                     const double *vs, const double *ws, int jacobi, const Stencil<double> &st, double *b) {
+  k_rhs_fast<<<nblk, kBlock, 0, s>>>(g, dt, dtp, us, vs, ws, jacobi, st, b);
+}
+
 void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
                          const double *u, const double *v, const double *w, const float *u32, const float *v32,
                          const float *w32, double *us, double *vs, double *ws, const StepCtl &sc) {

@@ -75,16 +75,19 @@ typedef enum cfdgb_scheme {
   CFDGB_UD = 2      /* first-order upwind, UdUnit (:150-168) */
 } cfdgb_scheme;
 
-/* Preconditioner of the FP32 BiCGSTAB sweeps of the MIXED precision mode (the reference
-   has none; its FP64 BiCGSTAB stays unpreconditioned in every mode). */
+/* Preconditioner of the BiCGSTAB solvers (the reference has none: its bicgstabRe2 is
+   unpreconditioned, and so is CFDGB_PRECOND_NONE here). */
 typedef enum cfdgb_precond {
   CFDGB_PRECOND_NONE = 0,      /* the plain sweep (default) */
-  CFDGB_PRECOND_MULTIGRID = 1  /* one FP32 geometric multigrid V-cycle per application (right
+  CFDGB_PRECOND_MULTIGRID = 1  /* one geometric multigrid V-cycle per application (right
                                   preconditioning): red-black Gauss-Seidel smoothing, cell-
                                   centred transfers, the uniform-grid Laplacian rediscretised
-                                  per level.  MIXED, BICGSTAB or BICGSTAB_JACOBI, uniform grid;
-                                  the grid must coarsen (by halving its even extents) to at
-                                  most 4096 cells */
+                                  per level.  MIXED: an FP32 V-cycle in the FP32 sweeps; FP64:
+                                  the same V-cycle in FP64 in an FP64 BiCGSTAB that stops on the
+                                  tolerance or the cap and restarts only on breakdown (not the
+                                  reference's iteration).  BICGSTAB or BICGSTAB_JACOBI, uniform
+                                  grid; the grid must coarsen (by halving its even extents) to
+                                  at most 4096 cells */
 } cfdgb_precond;
 
 /* How dt changes from step to step.  The reference keeps dt fixed: its adaptive
@@ -115,7 +118,9 @@ typedef struct cfdgb_config {
   int maxit;                 /* iteration cap per solve (5000: bicgstabRe2.hpp:47); MIXED caps
                                 its FP32 iterations over all sweeps at maxit, and an FP64
                                 finish, when one runs, at maxit again */
-  double omega;              /* SOR relaxation */
+  double omega;              /* SOR relaxation; 0: the optimal one for the grid, 2 / (1 + sqrt(1 -
+                                mu^2)) with mu the Jacobi iteration's spectral radius on the
+                                non-constant modes of the uniform-grid operator */
   double inner_tol;          /* MIXED: residual reduction of each FP32 sweep; 0 (default):
                                 0.3 for the BiCGSTAB solvers, 3e-4 for CG */
   int max_outer;             /* MIXED: cap on FP64 refinements per solve */

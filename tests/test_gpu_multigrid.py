@@ -86,8 +86,31 @@ def test_multigrid_small_and_ragged_grids(shape):
     assert all(r.status == 0 and r.relres < 1e-8 for r in st[1:]), (shape, st)
 
 
+@pytest.mark.parametrize("case", ["96x48x4", "128x64x16"])
+@pytest.mark.parametrize("solver", ["bicgstab", "jacobi"])
+def test_fp64_multigrid_reaches_the_fp64_solution(solver, case):
+    """The FP64 BiCGSTAB preconditioned by the same V-cycle in FP64 (the like-for-like FP64
+    counterpart of the MIXED multigrid sweep): every solve below the tolerance in a few
+    dozen iterations, fields within 1e-6 of the plain FP64 BiCGSTAB, and the MIXED multigrid
+    run within 1e-6 of it."""
+    dom = CASES[case]
+    runs = {}
+    for key, kw in (("mg64", dict(precond="multigrid")), ("plain", {}),
+                    ("mg32", dict(precond="multigrid", precision="mixed"))):
+        with cg.Solver(solver=solver, **kw, **dom) as s:
+            s.init_fields()
+            st = s.step(5)
+            runs[key] = (s.get_fields(), st)
+    st = runs["mg64"][1]
+    assert all(r.status == 0 and r.relres < 1e-8 for r in st[1:]), [(r.status, r.relres) for r in st]
+    assert all(r.iters <= 100 for r in st[1:]), [r.iters for r in st]
+    for ref in ("plain", "mg32"):
+        for k, e in vel_err(runs["mg64"][0], runs[ref][0]).items():
+            assert e <= 1e-6, (solver, case, ref, k, e)
+
+
 @pytest.mark.parametrize("bad", [
-    dict(precond="multigrid"),                                      # FP64
+    dict(precond="multigrid", solver="cg"),                         # not BiCGSTAB (FP64)
     dict(precond="multigrid", precision="mixed", solver="cg"),      # not BiCGSTAB
     dict(precond="multigrid", precision="mixed", solver="rbsor"),
     dict(precond=7, precision="mixed"),                             # unknown value
