@@ -71,6 +71,18 @@ const char *const kKernelNames[K_COUNT] = {
     "bicgp_p32", "mg_vcycle", "bicgp_v32", "bicgp_s32", "bicgp_t32", "bicgp_xr32", "mirror32",
     "bicgp_p64", "mg_vcycle64", "bicgp_v64", "bicgp_s64", "bicgp_t64", "bicgp_xr64"};
 
+// Scalars of one time step run as a graph, appended on the device (k_step_record)
+struct StepRec {
+  double relres, cd, cl, cfl, dt, time;
+  int iters, status, nan, bodies;
+};
+constexpr int kRing = 1024;  // steps per read-back
+struct StepRing {
+  int n;       // records written since the last read-back
+  int bodies;  // WHILE-body executions of the running step
+  StepRec rec[kRing];
+};
+
 struct PendingEv {
   int id;
   cudaEvent_t a, b;
@@ -121,6 +133,16 @@ struct cfdgb_ctx {
   // test switch (environment CFDGB_TEST_WAIT_FAULT at create): the next MIXED solve makes one
   // bounded wait of the FP32 bulk-copy pipeline run out, to exercise that failure path
   bool test_wait_fault = false;
+  // one CUDA graph per time step (FP64 Krylov solvers, after the first step, kernel timing
+  // off): the whole step with its convergence loop as a conditional WHILE node; each step
+  // appends its scalars to a device ring read back once per cfdgb_step call
+  cudaGraphExec_t step_graph = nullptr;
+  bool no_step_graph = false;   // CFDGB_NO_STEP_GRAPH at create: the host-driven step instead
+  cudaStream_t side = nullptr;  // the WHILE body is captured on it
+  bool capturing = false;       // L() neither counts nor times while a graph is captured
+  long long graph_fixed = 0;    // kernels of one step graph outside the WHILE body
+  long long graph_fixed_kn[64] = {0};
+  StepRing *ring = nullptr, *h_ring = nullptr;
   // scratch for the per-function entry points (allocated on first use)
   double *op[10] = {nullptr};
   // Plot3D staging: five float32 arrays on the device and a pinned host copy
@@ -182,6 +204,12 @@ void resolve_events(cfdgb_ctx *c) {
 // on, brackets the launch with a CUDA-event pair on the context's stream.
 template <class F>
 void L(cfdgb_ctx *c, int id, int nkernels, F &&launch) {
+  if (c->capturing) {  // counted per replay instead (run_step_graphs)
+    c->graph_fixed += nkernels;
+    c->graph_fixed_kn[id] += nkernels;
+    launch();
+    return;
+  }
   c->launches += nkernels;
   c->kn[id] += nkernels;
   if (!c->timing) {
@@ -568,7 +596,8 @@ void launch_setup64(cfdgb_ctx *c, const Stencil<double> &st64) {
 }
 
 // createBMatrix + solve + (caller) transform, on the current u*.  Fills iters/relres.
-int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *status) {
+// createBMatrix_omp on u* (and, project_rhs, the null-space projection)
+void enqueue_rhs(cfdgb_ctx *c) {
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
   L(c, K_RHS, 1, [&] {
@@ -579,6 +608,12 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
   });
   if (c->cfg.project_rhs)
     L(c, K_RHS, 2, [&] { launch_project_rhs(c->stream, c->g, st64, jac ? 1 : 0, c->b, c->part, c->ss); });
+}
+
+int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *status) {
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
+  enqueue_rhs(c);
   *iters = 0;
   *outer = 0;
   *status = 0;
@@ -843,6 +878,200 @@ void convdiff(cfdgb_ctx *c, const double *u, const double *v, const double *w, d
   }
 }
 
+// 3. correction + DFIB + drag, written straight into T0 (copyVel, RUN_CPU.cpp:369-391);
+// 4. ghost fill of T0 and p, copy into T1 (RUN_CPU.cpp:399-400)
+void enqueue_update_bc(cfdgb_ctx *c) {
+  L(c, K_UPDATE, 1, [&] {
+    if (c->cfg.precision == CFDGB_MIXED)
+      launch_update_uf_fast(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta, c->p,
+                            c->us, c->vs, c->ws, c->u, c->v, c->w, c->ui, c->vi, c->wi, c->part, c->ss);
+    else
+      launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta,
+                             c->p, c->us, c->vs, c->ws, c->u, c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part,
+                             c->ss);
+  });
+  L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet); });
+}
+
+// ---- one CUDA graph per time step ----
+// The WHILE node's condition: another chunk of iterations while the solver has not decided.
+// Bounded twice over: the solver decides at its iteration cap, and the body count stops
+// the loop (with ENOCONV) a few chunks past the cap should that ever fail.
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, SolverScal *sc, StepRing *ring, int max_bodies) {
+  const int b = ++ring->bodies;
+  bool more = !sc->done;
+  if (more && b >= max_bodies) {
+    sc->done = 1;
+    sc->status = CFDGB_ENOCONV;
+    more = false;
+  }
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// The solve parameters (bicgstabRe2's tol, restart threshold tol * 1e-7, cap) at the start
+// of every graph step: cfdgb_init_fields clears the solver scalars
+__global__ void k_solver_params(SolverScal *sc, double tol, int maxit) {
+  sc->tol = tol;
+  sc->restart_thr = tol * 1e-7;  // bicgstabRe2.hpp:53 (pRestartFactor_)
+  sc->maxit = maxit;
+}
+
+// The step's scalars into the ring (what the host path reads back after each step)
+__global__ void k_step_record(StepRing *ring, const SolverScal *sc, const StepScal *ss) {
+  const int n = ring->n;
+  if (n >= kRing) return;  // the host reads back before the ring fills
+  StepRec &r = ring->rec[n];
+  r.relres = sc->relres;
+  r.iters = sc->iter;
+  r.status = sc->status;
+  r.cd = ss->cd;
+  r.cl = ss->cl;
+  r.cfl = ss->cfl[0];
+  r.dt = ss->dt_step;
+  r.time = ss->time;
+  r.nan = ss->nan_flag;
+  r.bodies = ring->bodies;
+  ring->bodies = 0;
+  ring->n = n + 1;
+}
+
+// the steps after the first run as one graph each: FP64 Krylov solvers (their loop is the
+// device's own decision), kernel timing off (it times launches one by one)
+bool use_step_graph(const cfdgb_ctx *c) {
+  return !c->no_step_graph && !c->timing && c->cfg.precision == CFDGB_FP64 && c->cfg.solver != CFDGB_RBSOR;
+}
+
+void drop_step_graph(cfdgb_ctx *c) {
+  if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+  c->step_graph = nullptr;
+}
+
+int capture_step_graph(cfdgb_ctx *c) {
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
+  if (!c->side) CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  if (!c->ring) {
+    TRY(dalloc(c, &c->ring, 1));
+    CK(cudaMallocHost(&c->h_ring, sizeof(StepRing)));
+    CK(cudaMemsetAsync(c->ring, 0, sizeof(StepRing), c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->graph_fixed = 0;
+  std::fill(std::begin(c->graph_fixed_kn), std::end(c->graph_fixed_kn), 0LL);
+  const int len = chunk_iters(c, false), nk = iter_kernels(c, false);
+  cudaGraph_t graph = nullptr;
+  c->capturing = true;
+  auto done = [&](cudaError_t e) -> int {
+    c->capturing = false;
+    if (e != cudaSuccess) {
+      cudaGraph_t g2 = nullptr;
+      cudaStreamEndCapture(c->stream, &g2);  // leave no capture open on an error
+      if (g2) cudaGraphDestroy(g2);
+      cudaGetLastError();
+      return fail(CFDGB_ECUDA, "step graph capture: %s", cudaGetErrorString(e));
+    }
+    return 0;
+  };
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return done(e);
+  convdiff(c, c->u, c->v, c->w, c->us, c->vs, c->ws, true);
+  enqueue_rhs(c);
+  L(c, K_SETUP64, 1, [&] { k_solver_params<<<1, 1, 0, c->stream>>>(c->sc, c->cfg.tol, c->cfg.maxit); });
+  L(c, K_SETUP64, 1, [&] { launch_setup64(c, st64); });
+  // the convergence loop: a WHILE node whose body is a chunk of iterations and k_loop_cond
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return done(e);
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return done(e);
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t loop_node;
+  e = cudaGraphAddNode(&loop_node, g, deps, nullptr, nd, &np);
+  if (e != cudaSuccess) return done(e);
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return done(e);
+  std::swap(c->stream, c->side);  // the iteration launchers enqueue on c->stream
+  for (int m = 0; m < len; ++m)
+    for (int part = 0; part < nk; ++part) launch_iter_kernel(c, false, part);
+  const int max_bodies = c->cfg.maxit / len + 4;
+  k_loop_cond<<<1, 1, 0, c->stream>>>(h, c->sc, c->ring, max_bodies);
+  std::swap(c->stream, c->side);
+  cudaGraph_t body_out = nullptr;
+  e = cudaStreamEndCapture(c->side, &body_out);
+  if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(c->stream, &loop_node, nullptr, 1,
+                                                                cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return done(e);
+  // bicgstabRe2's NaN recovery after a capped solve (the kernels check the status)
+  L(c, K_NANRESET, 2, [&] { launch_bicg_nan_reset(c->stream, c->nblk, c->g, c->x, c->px1, c->px2, c->part, c->sc); });
+  L(c, K_TRANSFORM, 1, [&] { launch_transform(c->stream, c->nblk, c->g, c->x, c->p); });
+  enqueue_update_bc(c);
+  k_step_record<<<1, 1, 0, c->stream>>>(c->ring, c->sc, c->ss);
+  e = cudaStreamEndCapture(c->stream, &graph);
+  c->capturing = false;
+  if (e != cudaSuccess) return fail(CFDGB_ECUDA, "step graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&c->step_graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    c->step_graph = nullptr;
+    return fail(CFDGB_ECUDA, "step graph instantiate: %s", cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+// n steps (each after the first of the run) as graph launches, one read-back per kRing
+// steps; fills stats[0..n) and returns the worst status
+int run_step_graphs(cfdgb_ctx *c, int n, cfdgb_step_stats *stats, int *worst) {
+  if (!c->step_graph) TRY(capture_step_graph(c));
+  const int len = chunk_iters(c, false), nk = iter_kernels(c, false);
+  long long per_body = 1;  // k_loop_cond
+  for (int part = 0; part < nk; ++part) per_body += (long long)iter_part_launches(c, false, part) * len;
+  for (int done = 0; done < n;) {
+    const int b = std::min(n - done, kRing);
+    CK(cudaMemsetAsync(&c->ring->n, 0, sizeof(int), c->stream));
+    for (int q = 0; q < b; ++q) CK(cudaGraphLaunch(c->step_graph, c->stream));
+    CK(cudaMemcpyAsync(c->h_ring, c->ring, offsetof(StepRing, rec) + b * sizeof(StepRec), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->h_ring->n != b) return fail(CFDGB_ECUDA, "step graph: %d of %d step records", c->h_ring->n, b);
+    for (int q = 0; q < b; ++q) {
+      const StepRec &r = c->h_ring->rec[q];
+      const int loop = ++c->loop;
+      int status = r.status;
+      if (r.nan && status == 0) status = CFDGB_ENAN;
+      c->launches += c->graph_fixed + 1 + r.bodies * per_body;
+      for (int k = 0; k < K_COUNT; ++k) c->kn[k] += c->graph_fixed_kn[k];
+      for (int part = 0; part < nk; ++part)
+        c->kn[iter_kid(c, false, part)] += (long long)r.bodies * len * iter_part_launches(c, false, part);
+      if (stats) {
+        cfdgb_step_stats &st = stats[done + q];
+        st.step = loop;
+        st.iters = r.iters;
+        st.outer = 0;
+        st.status = status;
+        st.relres = r.relres;
+        st.cd = r.cd;
+        st.cl = r.cl;
+        st.cfl = r.cfl;
+        st.dt = r.dt;
+        st.time = r.time;
+      }
+      if (status < *worst) *worst = status;
+    }
+    done += b;
+  }
+  return 0;
+}
+
 int ensure_op_buffers(cfdgb_ctx *c) {
   if (c->op[0]) return 0;
   for (int q = 0; q < 7; ++q) TRY(dalloc(c, &c->op[q], c->npad));
@@ -884,6 +1113,7 @@ int sync(cfdgb_ctx *c) {
 extern "C" {
 
 int cfdgb_abi_version(void) { return CFDGB_ABI_VERSION; }
+static_assert(K_COUNT <= 64, "graph_fixed_kn holds every kernel id");
 const char *cfdgb_last_error(void) { return g_last_error.c_str(); }
 
 int cfdgb_config_default(cfdgb_config *c) {
@@ -949,6 +1179,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   c->chunk_len = c->ncell > (1LL << 22) ? 8 : 32;
   c->omega = cfg->omega > 0.0 ? cfg->omega : sor_omega_opt(cfg);
   c->test_wait_fault = std::getenv("CFDGB_TEST_WAIT_FAULT") != nullptr;
+  c->no_step_graph = std::getenv("CFDGB_NO_STEP_GRAPH") != nullptr;
   int rc = 0;
   const int nmet = nx + ny + nz;
   if ((rc = dalloc(c, &c->metric, 2 * (size_t)nmet))) return bail(rc);
@@ -1136,6 +1367,9 @@ int cfdgb_destroy(cfdgb_ctx *c) {
   for (auto e : c->ev_free) cudaEventDestroy(e);
   if (c->chunk64) cudaGraphExecDestroy(c->chunk64);
   if (c->chunk32) cudaGraphExecDestroy(c->chunk32);
+  drop_step_graph(c);
+  if (c->h_ring) cudaFreeHost(c->h_ring);
+  if (c->side) cudaStreamDestroy(c->side);
   for (void *q : c->allocs) cudaFree(q);
   if (c->h_p3d) cudaFreeHost(c->h_p3d);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -1235,6 +1469,10 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
   const double nu = 1.0 / c->cfg.Re;  // 0_1_SimulationVariable.hpp:26-31
   int worst = 0;
   for (int s = 0; s < nsteps; ++s) {
+    if (c->loop >= 1 && use_step_graph(c)) {  // the remaining steps, one graph each
+      TRY(run_step_graphs(c, nsteps - s, stats ? stats + s : nullptr, &worst));
+      break;
+    }
     const int loop = ++c->loop;
     // 1. u* (RUN_CPU.cpp:268) and, from the same kernel, the CFL diagnostic on u* (get_Cfl,
     // RUN_CPU.cpp:274) with the next dt of an adaptive rule (timestepper, :275)
@@ -1246,18 +1484,8 @@ int cfdgb_step(cfdgb_ctx *c, int nsteps, cfdgb_step_stats *stats) {
       TRY(solve_pressure(c, &iters, &outer, &relres, &status));
       L(c, K_TRANSFORM, 1, [&] { launch_transform(c->stream, c->nblk, c->g, c->x, c->p); });
     }
-    // 3. correction + DFIB + drag, written straight into T0 (copyVel, RUN_CPU.cpp:369-391)
-    L(c, K_UPDATE, 1, [&] {
-      if (c->cfg.precision == CFDGB_MIXED)
-        launch_update_uf_fast(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta, c->p,
-                              c->us, c->vs, c->ws, c->u, c->v, c->w, c->ui, c->vi, c->wi, c->part, c->ss);
-      else
-        launch_update_uf_exact(c->stream, c->nblk, c->g, c->cfg.dt, &c->ss->dt, step_mode(c), c->cfg.lz, c->eta,
-                               c->p, c->us, c->vs, c->ws, c->u, c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part,
-                               c->ss);
-    });
-    // 4. ghost fill of T0 and p, copy into T1 (RUN_CPU.cpp:399-400)
-    L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet); });
+    // 3. correction + DFIB + drag into T0, 4. ghost fill and copy into T1
+    enqueue_update_bc(c);
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
     resolve_events(c);
@@ -1497,6 +1725,7 @@ int cfdgb_set_dt(cfdgb_ctx *c, double dt) {
   if (!c) return fail(CFDGB_EINVAL, "null context");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(CFDGB_EINVAL, "dt must be positive");
   c->cfg.dt = dt;
+  drop_step_graph(c);  // a graph holds the CFL rule's dt bound, taken from dt
   // the step kernels read dt from the step scalars
   const double h[2] = {dt, dt};
   CK(cudaMemcpyAsync(&c->ss->dt, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
@@ -1595,6 +1824,7 @@ int cfdgb_read_plot3d(cfdgb_ctx *c, const char *qpath, double *head) {
 
 int cfdgb_set_inlet(cfdgb_ctx *c, const double *u_in) {
   if (!c) return fail(CFDGB_EINVAL, "null context");
+  drop_step_graph(c);  // the ghost fill's inlet pointer is part of a step graph
   if (!u_in) {
     c->inlet = nullptr;
     return 0;
