@@ -427,18 +427,20 @@ def roofline(prof, cells, word_bytes, suffix, hbm_peak, peak_kind, traffic_file)
     return r, share
 
 
-# the modes beside the FP64 value: (solver, precision, preconditioner, what it is).  Each
+# the modes beside the FP64 value: (solver (None: the case's own FP64 solver), precision,
+# preconditioner, what it is).  Each
 # MIXED mode has an FP64 counterpart with the same solver (PRECISION_PAIR), so that its
 # speed-up over that one isolates the precision; against `value` it also includes the
 # change of solver.
 MODES = {
     "cg": ("cg", "fp64", "none", "cg (SPE operator), FP64"),
-    "fp64_mg": ("jacobi", "fp64", "multigrid",
-                "jacobi bicgstab right-preconditioned by an FP64 multigrid V-cycle, FP64"),
-    "mixed": ("jacobi", "mixed", "none", "jacobi bicgstab, FP32 sweeps in FP64 refinement"),
+    "fp64_mg": (None, "fp64", "multigrid",
+                "the case's bicgstab right-preconditioned by an FP64 multigrid V-cycle, FP64"),
+    "mixed": (None, "mixed", "none", "the case's bicgstab, FP32 sweeps in FP64 refinement"),
     "mixed_cg": ("cg", "mixed", "none", "cg (SPE operator), FP32 sweeps in FP64 refinement"),
-    "mixed_mg": ("jacobi", "mixed", "multigrid",
-                 "jacobi bicgstab, FP32 sweeps right-preconditioned by an FP32 multigrid V-cycle, in FP64 refinement"),
+    "mixed_mg": (None, "mixed", "multigrid",
+                 "the case's bicgstab, FP32 sweeps right-preconditioned by an FP32 multigrid V-cycle, in FP64 "
+                 "refinement"),
 }
 PRECISION_PAIR = {"mixed": "fp64", "mixed_cg": "cg", "mixed_mg": "fp64_mg"}
 

@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 7  # CFDGB_ABI_VERSION
+ABI_VERSION = 8  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -53,7 +53,8 @@ class Config(C.Structure):
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
                 ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int),
-                ("precond", C.c_int), ("dt_mode", C.c_int), ("cfl_target", C.c_double), ("dt_max", C.c_double)]
+                ("precond", C.c_int), ("dt_mode", C.c_int), ("cfl_target", C.c_double), ("dt_max", C.c_double),
+                ("time_order", C.c_int)]
 
 
 class Objective(C.Structure):

@@ -120,6 +120,8 @@ struct cfdgb_ctx {
   double *ph64 = nullptr, *sh64 = nullptr;
   // MIXED QUICK: FP32 copies of the padded u, v, w that the FP32 stencil sweep reads
   float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;
+  // Adams-Bashforth history (time_order 2, 3): increments of the last two steps
+  double *hb[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   double *part = nullptr;
   SolverScal *sc = nullptr, *sc32 = nullptr;
   StepScal *ss = nullptr;
@@ -415,6 +417,9 @@ int validate(const cfdgb_config *c) {
                   c->ny, c->nz, kMgSharedCells);
   }
   if (c->dt_mode < CFDGB_DT_FIXED || c->dt_mode > CFDGB_DT_CFL) return fail(CFDGB_EINVAL, "unknown dt_mode %d", c->dt_mode);
+  if (c->time_order < 0 || c->time_order > 3) return fail(CFDGB_EINVAL, "time_order must be 1, 2 or 3");
+  if (c->time_order == 3 && c->dt_mode != CFDGB_DT_FIXED)
+    return fail(CFDGB_EINVAL, "third-order Adams-Bashforth is the constant-step form: it needs CFDGB_DT_FIXED");
   if (c->dt_mode == CFDGB_DT_CFL && !(c->cfl_target > 0 && c->dt_max >= 0))
     return fail(CFDGB_EINVAL, "CFDGB_DT_CFL needs cfl_target > 0 and dt_max >= 0");
   if (c->grid == CFDGB_GRID_SML) {
@@ -422,8 +427,8 @@ int validate(const cfdgb_config *c) {
     // cells) and in y, an even number of coarse ones on both sides
     if (c->nx % 2 || c->nx <= 108 || c->ny % 2 || c->ny <= 100)
       return fail(CFDGB_EINVAL, "the SML grid needs nx even > 108 and ny even > 100");
-    if (c->precision != CFDGB_FP64 || (c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI))
-      return fail(CFDGB_EINVAL, "the SML grid is implemented for the FP64 BiCGSTAB solvers");
+    if (c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI)
+      return fail(CFDGB_EINVAL, "the SML grid is implemented for the BiCGSTAB solvers (its operator is not symmetric)");
     if (c->project_rhs)
       return fail(CFDGB_EINVAL, "project_rhs removes the mean, not the stretched operator's null-space part");
   }
@@ -777,6 +782,8 @@ int reset_time(cfdgb_ctx *c) {
                     offsetof(StepScal, urun) == offsetof(StepScal, dt) + 24,
                 "StepScal time-step fields are contiguous");
   CK(cudaMemcpyAsync(&c->ss->dt, h, 9 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(&c->ss->hist, 0, 2 * sizeof(int), c->stream));  // Adams-Bashforth history empty
+  static_assert(offsetof(StepScal, hslot) == offsetof(StepScal, hist) + sizeof(int), "hist, hslot adjacent");
   CK(cudaStreamSynchronize(c->stream));  // h is reused by the next call
   return 0;
 }
@@ -846,13 +853,16 @@ StepCtl step_ctl(const cfdgb_ctx *c, bool in_step) {
   sc.Re = c->cfg.Re;
   sc.cfl_target = c->cfg.cfl_target;
   sc.dt_max = c->cfg.dt_max > 0.0 ? c->cfg.dt_max : c->cfg.dt;
+  sc.time_order = in_step && c->cfg.time_order > 1 ? c->cfg.time_order : 1;
+  for (int q = 0; q < 2; ++q)
+    for (int a = 0; a < 3; ++a) sc.hb[q][a] = c->hb[q][a];
   return sc;
 }
 // step_end mode of the velocity correction (launch_update_uf_exact)
 int step_mode(const cfdgb_ctx *c) { return c->cfg.dt_mode == CFDGB_DT_FIXED ? 1 : 2; }
 
 bool fast_convdiff(const cfdgb_ctx *c) {
-  return c->cfg.precision == CFDGB_MIXED && c->cfg.scheme == CFDGB_QUICK && !c->cfg.les;
+  return c->cfg.precision == CFDGB_MIXED && c->cfg.scheme == CFDGB_QUICK && !c->cfg.les && c->cfg.time_order <= 1;
 }
 
 // u* of the step, with the CFL number of u* (get_Cfl, src/RUN_CPU.cpp:274) from the same
@@ -1137,6 +1147,7 @@ int cfdgb_config_default(cfdgb_config *c) {
   c->dt_mode = CFDGB_DT_FIXED;
   c->cfl_target = 0.5;
   c->dt_max = 0.0;  // 0: the configured dt
+  c->time_order = 1;
   return 0;
 }
 
@@ -1264,7 +1275,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.lgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.lgx * g.lgy)));
   int nblk3 = g.lgx * g.lgy * g.lgz;
   // vectorised FP32 kernels: quads of four k cells per thread when nz % 4 == 0
-  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32")) {
+  // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows)
+  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML) {
     const int nq = cfg->nz / 4;
     g.vbx = 1;
     while (g.vbx < nq && g.vbx < 32) g.vbx *= 2;
@@ -1290,6 +1302,13 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   if (g.nonuni) {  // the stored rows, from the same per-axis factors and jpv
     launch_build_rows(c->stream, g, 0, const_cast<double *>(g.cof[0]));
     launch_build_rows(c->stream, g, 1, const_cast<double *>(g.cof[1]));
+    if (cfg->precision == CFDGB_MIXED) {
+      float *r32 = nullptr;
+      if ((rc = dalloc(c, &r32, 14 * (size_t)c->ncell))) return bail(rc);
+      launch_rows_f32(c->stream, 14 * c->ncell, g.cof[0], r32);  // cof[1] follows cof[0]
+      g.cof32[0] = r32;
+      g.cof32[1] = r32 + 7 * c->ncell;
+    }
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(fail(CFDGB_ECUDA, "stretched-grid rows"));
   }
   // fields and solver vectors
@@ -1312,7 +1331,14 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     for (auto **q : kv)
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
-  if (cfg->precision == CFDGB_MIXED && cfg->scheme == CFDGB_QUICK && !cfg->les) {  // FP32 copies of u, v, w
+  if (cfg->time_order > 1) {  // Adams-Bashforth history
+    for (int q = 0; q < (cfg->time_order == 3 ? 2 : 1); ++q)
+      for (int a = 0; a < 3; ++a)
+        if ((rc = dalloc(c, &c->hb[q][a], c->npad))) return bail(rc);
+    if (cfg->time_order == 2)
+      for (int a = 0; a < 3; ++a) c->hb[1][a] = c->hb[0][a];
+  }
+  if (cfg->precision == CFDGB_MIXED && cfg->scheme == CFDGB_QUICK && !cfg->les && cfg->time_order <= 1) {
     if ((rc = dalloc(c, &c->u32, c->npad)) || (rc = dalloc(c, &c->v32, c->npad)) || (rc = dalloc(c, &c->w32, c->npad)))
       return bail(rc);
   }
@@ -1726,6 +1752,8 @@ int cfdgb_set_dt(cfdgb_ctx *c, double dt) {
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(CFDGB_EINVAL, "dt must be positive");
   c->cfg.dt = dt;
   drop_step_graph(c);  // a graph holds the CFL rule's dt bound, taken from dt
+  if (c->cfg.time_order == 3 && c->ss)  // the constant-step history is of the old dt
+    CK(cudaMemsetAsync(&c->ss->hist, 0, 2 * sizeof(int), c->stream));
   // the step kernels read dt from the step scalars
   const double h[2] = {dt, dt};
   CK(cudaMemcpyAsync(&c->ss->dt, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
@@ -1876,6 +1904,8 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
     return fail(CFDGB_EINVAL, "the adjoint is implemented for QUICK without the Smagorinsky model");
   if (c->cfg.dt_mode != CFDGB_DT_FIXED)  // its reverse sweep replays the steps at one dt
     return fail(CFDGB_EINVAL, "the adjoint needs a fixed dt (CFDGB_DT_FIXED)");
+  if (c->cfg.time_order > 1)  // its transposed step is the Euler step's
+    return fail(CFDGB_EINVAL, "the adjoint is implemented for the Euler step (time_order 1)");
   if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
     return fail(CFDGB_EINVAL, "bad objective window");
   if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");

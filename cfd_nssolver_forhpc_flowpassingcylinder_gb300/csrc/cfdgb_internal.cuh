@@ -46,6 +46,8 @@ struct Geo {
   // cof[0] the SPE rows and cof[1] the Jacobi-scaled CSR rows: built by nonuni_row, so the
   // solver kernels read the bits they would otherwise recompute at every application
   const double *cof[2];
+  // MIXED on the stretched grid: the same rows rounded to FP32 (the FP32 sweeps' operator)
+  const float *cof32[2];
   int walls;  // a cfdgb_walls value (the boundary table's y-wall rows)
   // per-index reciprocals RN(1/D), RN(1/Ds) of the metrics (padded lengths) for div_by, and
   // the DFIB face-fraction factors (Ds * 0.5) / D of updateUandF.hpp, each one IEEE division
@@ -257,6 +259,8 @@ struct StepScal {
   double dt, dt_next, time;
   double urun[6];
   double dt_step;  // dt of the last step (set with time at its end)
+  int hist;        // Adams-Bashforth: increments stored by the steps since init (at most 2)
+  int hslot;       // Adams-Bashforth order 3: the history slot that holds the last increment
   int nan_flag, pad;
   unsigned cnt[8];
 };
@@ -271,6 +275,10 @@ struct StepCtl {
   int in_step;        // 1: a time step (running extremes and dt_next are kept); 0: a single call
   int dt_mode;        // a cfdgb_dt_mode value
   double Re, cfl_target, dt_max;
+  // Adams-Bashforth time stepping (cfdgb_config.time_order 2 or 3; 1: the reference's Euler
+  // step): increments convection + diffusion of the last two steps, in slots hb[0], hb[1]
+  int time_order;
+  double *hb[2][3];
 };
 
 // Dir/Num boundary table of inc/BoundaryCondition/FLOWpassing.hpp:6-40 as

@@ -72,6 +72,8 @@ struct KrylovVecs {
 
 // stretched grid: store the SPE (jac 0) or Jacobi-scaled CSR (jac 1) rows into out[7][ncell]
 void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out);
+// out[q] = (float)in[q], q < n (the stored rows for the MIXED sweeps)
+void launch_rows_f32(cudaStream_t s, long long n, const double *in, float *out);
 // FP64 BiCGSTAB (bicgstabRe2) set-up: r0 = b - A x, r1 = p1 = r0, history px2 <- px1 <- x
 void launch_bicg_setup64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st,
                          KrylovVecs<double> v, const double *b, double *px1, double *px2, double *part,

@@ -15,6 +15,8 @@
 // recomputation.  FP32 (inner solve of the mixed path, bound by HBM): three kernels per
 // iteration; the p update is fused into the next SpMV and s into its SpMV by
 // recomputing them at the stencil points (L1-resident), 17 instead of 19 words per cell.
+#include <algorithm>
+
 #include "cfdgb_internal.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -78,10 +80,21 @@ template <class F>
 __device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<float> &st, int ic, int jc, int kc,
                                                     long long row, F &&f, float &center) {
   const long long nyz = (long long)g.nyc * g.nzc;
-  const float *c = st.c[cls_of(g, ic, jc, kc)];
   const float fc = f(row);
   center = fc;
   float sum = 0.0f;
+  if (g.nonuni) {  // stretched grid (MIXED): its rows stored in FP32, [7][ncell]
+    const float *__restrict__ cs = g.cof32[st.jac] + row;
+    const long long n = g.ncell;
+    if (ic > 0) sum = fmaf(cs[0], f(row - nyz) - fc, sum);
+    if (jc > 0) sum = fmaf(cs[n], f(row - g.nzc) - fc, sum);
+    if (kc > 0) sum = fmaf(cs[2 * n], f(row - 1) - fc, sum);
+    if (kc < g.nzc - 1) sum = fmaf(cs[4 * n], f(row + 1) - fc, sum);
+    if (jc < g.nyc - 1) sum = fmaf(cs[5 * n], f(row + g.nzc) - fc, sum);
+    if (ic < g.nxc - 1) sum = fmaf(cs[6 * n], f(row + nyz) - fc, sum);
+    return sum;
+  }
+  const float *c = st.c[cls_of(g, ic, jc, kc)];
   if (ic > 0) sum = fmaf(c[0], f(row - nyz) - fc, sum);
   if (jc > 0) sum = fmaf(c[1], f(row - g.nzc) - fc, sum);
   if (kc > 0) sum = fmaf(c[2], f(row - 1) - fc, sum);
@@ -1558,7 +1571,10 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
                                                             double delta, double peak, int first, double *part,
                                                             SolverScal *sc) {
   const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
-  const double m = ss->rsum / (double)g.ncell;
+  // the null-space part is the mean on the uniform grid (a symmetric operator); on the
+  // stretched grid the operator's left null vector is not constant, and the FP64 residual,
+  // in range(A) for a consistent system, is taken as it is
+  const double m = g.nonuni ? 0.0 : ss->rsum / (double)g.ncell;
   Dot2F acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
@@ -1709,6 +1725,16 @@ __global__ void __launch_bounds__(kBlock) k_build_rows(Geo g, int jac, double *_
 
 void launch_build_rows(cudaStream_t s, const Geo &g, int jac, double *out) {
   k_build_rows<<<cgrid(g), cblock(g), 0, s>>>(g, jac, out);
+}
+
+// the stored rows rounded to FP32 (MIXED on the stretched grid)
+__global__ void __launch_bounds__(kBlock) k_rows_f32(long long n, const double *__restrict__ in,
+                                                     float *__restrict__ out) {
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock)
+    out[q] = (float)in[q];
+}
+void launch_rows_f32(cudaStream_t s, long long n, const double *in, float *out) {
+  k_rows_f32<<<(int)std::min<long long>((n + kBlock - 1) / kBlock, 4096), kBlock, 0, s>>>(n, in, out);
 }
 
 void launch_bicg_setup64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, KrylovVecs<double> v,

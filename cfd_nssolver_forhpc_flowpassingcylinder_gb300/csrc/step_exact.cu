@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
 // maxima are exact in any order.  The last block also sets the next dt (StepCtl).
 // Two resident blocks per SM (at most 128 registers a thread): the kernel is bound by the
 // FP64 pipe, and one block of 8 warps per SM leaves it waiting on latency.
-template <int S>
+template <int S, bool AB>
 __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_arg, double nu0,
                                                            const double *__restrict__ nut,
                                                            const double *__restrict__ u,
@@ -146,6 +146,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
                                                            double *__restrict__ ws, StepCtl sc) {
   const double dt = step_dt(sc, dt_arg);
   CflAcc cfl;
+  AbStep ab;
+  if (AB) ab.init(sc, dt);
   const long long sx = g.sx, sy = g.sy, sz = 1;
   const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
   const double *rDx = g.rDx, *rDy = g.rDy, *rDz = g.rDz, *rDxs = g.rDxs, *rDys = g.rDys, *rDzs = g.rDzs;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
           (oxs(ox(uxp - uc, i + 1) - ox(uc - uxm, i), i) +
            oy(oys(u[yp] - uc, j) - oys(uc - u[ym], j - 1), j) +
            oz(ozs(u[zp] - uc, k) - ozs(uc - u[zm], k - 1), k));
-      const double r = uc + convection + difussion;
+      const double r = AB ? ab.value(0, ic, uc, convection, difussion) : uc + convection + difussion;
       us[ic] = r;
       ccfl += oxs(r, i);
       cfl.comp(0, r);
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
           (ox(oxs(v[xp] - vc, i) - oxs(vc - v[xm], i - 1), i) +
            oys(oy(vyp - vc, j + 1) - oy(vc - vym, j), j) +
            oz(ozs(v[zp] - vc, k) - ozs(vc - v[zm], k - 1), k));
-      const double r = vc + convection + difussion;
+      const double r = AB ? ab.value(1, ic, vc, convection, difussion) : vc + convection + difussion;
       vs[ic] = r;
       ccfl += oys(r, j);
       cfl.comp(1, r);
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
           (ox(oxs(w[xp] - wc, i) - oxs(wc - w[xm], i - 1), i) +
            oy(oys(w[yp] - wc, j) - oys(wc - w[ym], j - 1), j) +
            ozs(oz(wzp - wc, k + 1) - oz(wc - wzm, k), k));
-      const double r = wc + convection + difussion;
+      const double r = AB ? ab.value(2, ic, wc, convection, difussion) : wc + convection + difussion;
       ws[ic] = r;
       ccfl += ozs(r, k);
       cfl.comp(2, r);
@@ -577,15 +579,24 @@ __global__ void __launch_bounds__(kBlock) k_eta_extrude(Geo g, double *__restric
 }
 
 // ---- launchers ----
+template <bool AB>
+static void convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu, const double *nut,
+                           const double *u, const double *v, const double *w, double *us, double *vs, double *ws,
+                           const StepCtl &sc) {
+  if (scheme == CFDGB_LUD)
+    k_convdiff_exact<CFDGB_LUD, AB><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
+  else if (scheme == CFDGB_UD)
+    k_convdiff_exact<CFDGB_UD, AB><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
+  else
+    k_convdiff_exact<CFDGB_QUICK, AB><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
+}
 void launch_convdiff_exact(cudaStream_t s, int nblk, const Geo &g, int scheme, double dt, double nu,
                            const double *nut, const double *u, const double *v, const double *w, double *us,
                            double *vs, double *ws, const StepCtl &sc) {
-  if (scheme == CFDGB_LUD)
-    k_convdiff_exact<CFDGB_LUD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
-  else if (scheme == CFDGB_UD)
-    k_convdiff_exact<CFDGB_UD><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
+  if (sc.time_order > 1)
+    convdiff_exact<true>(s, nblk, g, scheme, dt, nu, nut, u, v, w, us, vs, ws, sc);
   else
-    k_convdiff_exact<CFDGB_QUICK><<<nblk, kBlock, 0, s>>>(g, dt, nu, nut, u, v, w, us, vs, ws, sc);
+    convdiff_exact<false>(s, nblk, g, scheme, dt, nu, nut, u, v, w, us, vs, ws, sc);
 }
 void launch_smagorinsky(cudaStream_t s, int nblk, const Geo &g, const double *l2, const double *u, const double *v,
                         const double *w, double *nut) {

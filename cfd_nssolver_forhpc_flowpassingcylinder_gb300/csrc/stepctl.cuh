@@ -62,6 +62,10 @@ __device__ __forceinline__ void cfl_finish(CflAcc &acc, double dt, const StepCtl
     if (sc.in_step) {
       for (int q = 0; q < 6; ++q) ss->urun[q] = fmax(ss->urun[q], out[1 + q]);
       ss->dt_next = next_dt(sc, ss, out[0], dt);
+      if (sc.time_order > 1) {  // this step's increment is stored: the history grows
+        if (ss->hist < 2) ss->hist += 1;
+        if (sc.time_order == 3) ss->hslot ^= 1;
+      }
     }
   }
 }
@@ -75,5 +79,41 @@ __device__ __forceinline__ void step_end(StepScal *ss, double dt, int mode) {
   ss->dt_step = dt;
   if (mode == 2) ss->dt = ss->dt_next;
 }
+
+// The new value of a velocity component from this step's convection and diffusion terms:
+// the reference's Euler step u + convection + diffusion (Convection_Difussion.hpp:269), or
+// with Adams-Bashforth (not in the reference) inc = convection + diffusion and
+//   order 2: u + (inc + (r/2) (inc - r h1)),  r = dt_n / dt_(n-1) (variable step);
+//   order 3: u + ((23 inc - 16 h1) + 5 h2) / 12 (constant step);
+// h1, h2 the increments of the two steps before; the order in effect grows from 1 as the
+// history fills after init.  inc is stored for the next steps.
+struct AbStep {
+  int ord;   // order in effect this step (1: Euler)
+  double r;  // dt_n / dt_(n-1)
+  double *h1[3], *h2[3], *hn[3];
+  __device__ __forceinline__ void init(const StepCtl &sc, double dt) {
+    const int hist = sc.ss ? sc.ss->hist : 0;
+    ord = sc.time_order > 1 ? (hist + 1 < sc.time_order ? hist + 1 : sc.time_order) : 1;
+    r = ord == 2 ? dt / sc.ss->dt_step : 1.0;
+    const int s = sc.ss ? sc.ss->hslot : 0;
+    for (int c = 0; c < 3; ++c) {
+      h1[c] = sc.hb[s][c];
+      h2[c] = sc.hb[1 - s][c];
+      hn[c] = sc.time_order == 2 ? sc.hb[s][c] : sc.hb[1 - s][c];
+    }
+  }
+  __device__ __forceinline__ double value(int c, long long ic, double uc, double convection, double difussion) const {
+    const double inc = convection + difussion;
+    double out;
+    if (ord <= 1)
+      out = uc + convection + difussion;
+    else if (ord == 2)
+      out = uc + (inc + (0.5 * r) * (inc - r * h1[c][ic]));
+    else
+      out = uc + ((23.0 * inc - 16.0 * h1[c][ic]) + 5.0 * h2[c][ic]) / 12.0;
+    hn[c][ic] = inc;
+    return out;
+  }
+};
 
 }  // namespace cfdgb

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 7
+#define CFDGB_ABI_VERSION 8
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -58,7 +58,8 @@ typedef enum cfdgb_grid {
   CFDGB_GRID_SML = 1       /* the reference's default stretched grid, "non_uniform-SML"
                               (structureGrid.hpp:250-329): 100 fine cells over 30 % of x
                               (shifted 4 cells upstream) and of y, coarse cells outside, z
-                              uniform; FP64 BiCGSTAB solvers; nx even > 108, ny even > 100 */
+                              uniform; the BiCGSTAB solvers, FP64 or MIXED (the FP32 sweeps
+                              on its stored rows rounded to FP32); nx even > 108, ny even > 100 */
 } cfdgb_grid;
 
 /* The y-wall rows of the reference's boundary table (inc/BoundaryCondition/FLOWpassing.hpp). */
@@ -145,6 +146,14 @@ typedef struct cfdgb_config {
   int dt_mode;               /* a cfdgb_dt_mode value; default fixed */
   double cfl_target;         /* CFDGB_DT_CFL: the CFL number each step aims at (default 0.5) */
   double dt_max;             /* CFDGB_DT_CFL: upper bound of dt (default: cfdgb_config.dt) */
+  int time_order;            /* time stepping of u*: 1 the reference's explicit Euler step
+                                (default); 2 Adams-Bashforth, variable step; 3 Adams-Bashforth,
+                                constant step (CFDGB_DT_FIXED).  Not a drop-in: the reference's
+                                2nd/3rd-order branch (inc/source/sourceTerm.hpp:9-108) does not
+                                compile, and as written it would overwrite the stored increment
+                                before reading it.  The order builds up from 1 over the first
+                                steps after init (cfdgb_set_dt restarts order 3); MIXED then
+                                uses the FP64 convection-diffusion kernel; no adjoint */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {

@@ -239,6 +239,31 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
  * Smagorinsky model added to nu per cell (Convection_Difussion.hpp:251-256) */
 void og_convection_diffusion_ex(const og_grid *g, double dt, double nu0, const double *nut, const double *u,
                                 const double *v, const double *w, double *us, double *vs, double *ws) {
+  og_convection_diffusion_ab(g, dt, nu0, nut, NULL, u, v, w, us, vs, ws);
+}
+
+/* the new value of a component: the reference's u + convection + diffusion (ab NULL or
+ * order 1), else the Adams-Bashforth combination of og_ab */
+static double ab_value(const og_ab *ab, int c, long ic, double uc, double convection, double difussion) {
+  if (!ab || ab->order <= 1) {
+    if (ab && ab->hnew[c]) ab->hnew[c][ic] = convection + difussion;
+    return uc + convection + difussion;
+  }
+  const double inc = convection + difussion;
+  const double h1 = ab->h1[c][ic];
+  double r;
+  if (ab->order == 2) {
+    r = uc + (inc + (0.5 * ab->r) * (inc - ab->r * h1));
+  } else {
+    r = uc + ((23.0 * inc - 16.0 * h1) + 5.0 * ab->h2[c][ic]) / 12.0;
+  }
+  ab->hnew[c][ic] = inc;
+  return r;
+}
+
+void og_convection_diffusion_ab(const og_grid *g, double dt, double nu0, const double *nut, const og_ab *ab,
+                                const double *u, const double *v, const double *w, double *us, double *vs,
+                                double *ws) {
   const long sx = (long)g->ny * g->nz, sy = g->nz, sz = 1;
   const int sc = g->scheme;
 #define NU_AT(i, j, k) (nut ? nu0 + nut[((long)((i) - GC) * g->nyc + ((j) - GC)) * g->nzc + ((k) - GC)] : nu0)
@@ -270,7 +295,7 @@ void og_convection_diffusion_ex(const og_grid *g, double dt, double nu0, const d
             (((u[xp] - u[ic]) / g->Dx[i + 1] - (u[ic] - u[xm]) / g->Dx[i]) / g->Dxs[i] +
              ((u[yp] - u[ic]) / g->Dys[j] - (u[ic] - u[ym]) / g->Dys[j - 1]) / g->Dy[j] +
              ((u[zp] - u[ic]) / g->Dzs[k] - (u[ic] - u[zm]) / g->Dzs[k - 1]) / g->Dz[k]);
-        us[ic] = u[ic] + convection + difussion;
+        us[ic] = ab_value(ab, 0, ic, u[ic], convection, difussion);
       }
   /* v: :276-355 */
   for (int i = GC; i < nx - GC; ++i)
@@ -299,7 +324,7 @@ void og_convection_diffusion_ex(const og_grid *g, double dt, double nu0, const d
             (((v[xp] - v[ic]) / g->Dxs[i] - (v[ic] - v[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
              ((v[yp] - v[ic]) / g->Dy[j + 1] - (v[ic] - v[ym]) / g->Dy[j]) / g->Dys[j] +
              ((v[zp] - v[ic]) / g->Dzs[k] - (v[ic] - v[zm]) / g->Dzs[k - 1]) / g->Dz[k]);
-        vs[ic] = v[ic] + convection + difussion;
+        vs[ic] = ab_value(ab, 1, ic, v[ic], convection, difussion);
       }
   /* w: :359-438 */
   for (int i = GC; i < nx - GC; ++i)
@@ -328,7 +353,7 @@ void og_convection_diffusion_ex(const og_grid *g, double dt, double nu0, const d
             (((w[xp] - w[ic]) / g->Dxs[i] - (w[ic] - w[xm]) / g->Dxs[i - 1]) / g->Dx[i] +
              ((w[yp] - w[ic]) / g->Dys[j] - (w[ic] - w[ym]) / g->Dys[j - 1]) / g->Dy[j] +
              ((w[zp] - w[ic]) / g->Dz[k + 1] - (w[ic] - w[zm]) / g->Dz[k]) / g->Dzs[k]);
-        ws[ic] = w[ic] + convection + difussion;
+        ws[ic] = ab_value(ab, 2, ic, w[ic], convection, difussion);
       }
 #undef NU_AT
 }
@@ -1019,9 +1044,31 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
     og_dfib_cylinder_z(g, eta);
   }
   double *nut = g->les ? dalloc(n) : NULL;
+  /* Adams-Bashforth history (time_order 2, 3): increments of the last two steps, slots
+   * hs[0], hs[1] swapping roles each step */
+  const int order = g->time_order > 1 ? g->time_order : 1;
+  double *hs[2][3] = {{NULL, NULL, NULL}, {NULL, NULL, NULL}};
+  if (order > 1)
+    for (int q = 0; q < 2; ++q)
+      for (int c = 0; c < 3; ++c) hs[q][c] = dalloc(tot);
+  int nhist = 0, slot = 0;
   for (int s = 1; s <= steps; ++s) {
     if (nut) og_smagorinsky(g, u, v, w, nut); /* RUN_CPU.cpp:261-263, on T0 */
-    og_convection_diffusion_ex(g, dt, nu, nut, u, v, w, us, vs, ws);
+    if (order > 1) {
+      og_ab ab;
+      ab.order = nhist + 1 < order ? nhist + 1 : order;
+      ab.r = 1.0; /* constant dt here */
+      for (int c = 0; c < 3; ++c) {
+        ab.h1[c] = hs[slot][c];
+        ab.h2[c] = hs[1 - slot][c];
+        ab.hnew[c] = order == 2 ? hs[slot][c] : hs[1 - slot][c];
+      }
+      og_convection_diffusion_ab(g, dt, nu, nut, &ab, u, v, w, us, vs, ws);
+      if (nhist < 2) ++nhist;
+      if (order == 3) slot = 1 - slot;
+    } else {
+      og_convection_diffusion_ex(g, dt, nu, nut, u, v, w, us, vs, ws);
+    }
     int iters = 0;
     double err = 0.0;
     if (s > 1) { /* RUN_CPU.cpp:287/:303: no pressure solve at the first step */
@@ -1055,6 +1102,8 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
   if (solver == 0 || solver == 1) og_bicg_free(&bs);
   free(val7);
   free(nut);
+  for (int q = 0; q < 2; ++q)
+    for (int c = 0; c < 3; ++c) free(hs[q][c]);
   free(us); free(vs); free(ws); free(u3); free(v3); free(w3); free(f); free(b); free(x);
   return rc;
 }

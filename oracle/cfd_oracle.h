@@ -27,7 +27,21 @@ typedef struct og_grid {
   int scheme;                  /* convection scheme: OG_SCHEME_* (0 after init: QUICK) */
   int les;                     /* != 0: Smagorinsky eddy viscosity in og_run_ex */
   int walls;                   /* y walls: OG_WALLS_* (0 after init: zero-gradient) */
+  int time_order;              /* og_run_ex's time stepping: 0 or 1 explicit Euler (the
+                                  reference), 2 or 3 Adams-Bashforth (not in the reference) */
 } og_grid;
+
+/* Adams-Bashforth history of og_convection_diffusion_ab (no counterpart in the reference,
+ * whose 2nd/3rd-order branch does not compile): order 1 is the reference's Euler step;
+ * order 2 takes u* = u + (inc + (0.5 r) (inc - r h1)) with r = dt_n / dt_(n-1); order 3
+ * (constant dt) u* = u + ((23 inc - 16 h1) + 5 h2) / 12; inc = convection + diffusion of
+ * this step, h1 and h2 those of the two steps before.  hnew (may alias h1 for order 2, h2
+ * for order 3) receives inc. */
+typedef struct og_ab {
+  int order;
+  double r;
+  double *h1[3], *h2[3], *hnew[3];
+} og_ab;
 
 /* the y-wall rows of the Dir/Num table (inc/BoundaryCondition/FLOWpassing.hpp): the active
  * zero-gradient rows (:23-29) or the free-slip rows left commented out there (:14-21) */
@@ -53,6 +67,9 @@ void og_convection_diffusion(const og_grid *g, double dt, double nu, const doubl
 /* with g->scheme and, nut != NULL (compact, og_smagorinsky), nu + nut per cell */
 void og_convection_diffusion_ex(const og_grid *g, double dt, double nu, const double *nut, const double *u,
                                 const double *v, const double *w, double *us, double *vs, double *ws);
+void og_convection_diffusion_ab(const og_grid *g, double dt, double nu, const double *nut, const og_ab *ab,
+                                const double *u, const double *v, const double *w, double *us, double *vs,
+                                double *ws);
 /* SmagorinskyModel (inc/source/SmagorinskyModel.hpp:30): compact eddy viscosity of T0 */
 void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *nut);
 void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p);

@@ -41,7 +41,7 @@ class _Grid(C.Structure):
                 ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)] + [
         (n, C.POINTER(C.c_double)) for n in
         ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")] + [
-        ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int)]
+        ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int), ("time_order", C.c_int)]
 
 
 # the reference's compile-time convection switch (0_General.hpp:114-118)
@@ -101,10 +101,12 @@ class Grid:
     """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
 
     def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform", scheme="quick",
-                 les=False, walls="zero_gradient"):
+                 les=False, walls="zero_gradient", time_order=1):
         """gridder: "uniform" (init_uniform) or "sml" (the reference's default stretched
         non_uniform-SML grid); scheme: "quick", "lud" or "ud" (the convection switch);
-        les: the Smagorinsky eddy viscosity in run(); walls: the y walls' boundary rows."""
+        les: the Smagorinsky eddy viscosity in run(); walls: the y walls' boundary rows;
+        time_order: run()'s time stepping, 1 the reference's Euler step, 2 or 3
+        Adams-Bashforth (constant dt; not in the reference)."""
         self._g = _Grid()
         init = {"uniform": lib().og_grid_init_uniform, "sml": lib().og_grid_init_sml}[gridder]
         rc = init(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx, ly / 2.0, radius)
@@ -113,6 +115,7 @@ class Grid:
         self._g.scheme = SCHEMES[scheme]
         self._g.les = 1 if les else 0
         self._g.walls = WALLS[walls]
+        self._g.time_order = int(time_order)
         self.shape = (nxc + 4, nyc + 4, nzc + 4)
         self.cells = nxc * nyc * nzc
 

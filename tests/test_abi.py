@@ -42,15 +42,15 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 7
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 8
     assert cfg.scheme == cg.QUICK and cfg.les == 0 and cfg.walls == cg.WALLS_ZERO_GRADIENT
-    assert cfg.dt_mode == cg.DT_FIXED and cfg.cfl_target == 0.5 and cfg.dt_max == 0.0
+    assert cfg.dt_mode == cg.DT_FIXED and cfg.cfl_target == 0.5 and cfg.dt_max == 0.0 and cfg.time_order == 1
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
                                          ("precision", 3), ("tol", 0.0), ("maxit", 0), ("scheme", 3),
                                          ("scheme", -1), ("les", 2), ("walls", 2), ("dt_mode", 3),
-                                         ("dt_mode", -1)])
+                                         ("dt_mode", -1), ("time_order", 4)])
 def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     cfg = cg.default_config()
     setattr(cfg, field, value)
@@ -97,10 +97,11 @@ def test_perturbation_generator_matches_oracle():
 
 
 @pytest.mark.parametrize("kw", [dict(nx=96, ny=110), dict(nx=121, ny=110), dict(nx=120, ny=100),
-                                dict(precision="mixed"), dict(solver="cg"), dict(solver="rbsor"),
-                                dict(project_rhs=1)])
+                                dict(solver="cg"), dict(solver="rbsor"), dict(precision="mixed", solver="cg"),
+                                dict(precision="mixed", precond="multigrid"), dict(project_rhs=1)])
 def test_stretched_grid_limits_rejected(lib, kw):
-    """The SML grid needs unit_SML's sizes and runs the FP64 BiCGSTAB solvers only."""
+    """The SML grid needs unit_SML's sizes and runs the BiCGSTAB solvers (FP64 or MIXED,
+    unpreconditioned): its operator is not symmetric and the V-cycle is the uniform grid's."""
     base = dict(nx=120, ny=110, nz=4, lx=17.0, ly=12.0, lz=3.0, cx=6.5, cy=6.0, grid="sml")
     base.update(kw)
     cfg = cg.default_config(**base)
