@@ -312,12 +312,16 @@ def e2e_mode(cg, torch, dist, wl, steps, warmup, solver, precision):
         return ms, nbytes, s.cells
 
 
-def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4", first=0):
+def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4", first=0, precision="fp64", solver="jacobi",
+                 precond="none"):
     """Forward run with checkpoints and the adjoint sweep (gradient of the drag averaged
-    over the last third of the window w.r.t. the inlet profile and eta) on the adjoint
-    case; returns both wall times (CUDA events on the library's stream) and their ratio."""
+    over the last third of the window, or from step `first`, w.r.t. the inlet profile and
+    eta) on the adjoint case; returns both wall times (CUDA events on the library's stream)
+    and their ratio.  precision/solver/precond: the forward's (MIXED: FP32 sweeps in FP64
+    refinement; the transposed solve stays FP64, with the FP64 V-cycle under precond
+    multigrid)."""
     cfg = dict(WORKLOADS[wl])
-    with cg.Solver(solver="jacobi", precision="fp64", tol=TOL, **cfg) as s:
+    with cg.Solver(solver=solver, precision=precision, precond=precond, tol=TOL, **cfg) as s:
         stream = torch.cuda.ExternalStream(s.stream)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         s.init_fields()
@@ -332,7 +336,9 @@ def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4", first=0):
         tf, tb = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
         free, total = torch.cuda.mem_get_info()
         import numpy as np
-        return {"workload": wl, "device_mem_gb": round((total - free) / 1e9, 2), "steps": nsteps, "objective_steps": [first, nsteps], "ckpt_every": ckpt,
+        return {"workload": wl, "precision": precision, "solver": solver, "precond": precond,
+                "device_mem_gb": round((total - free) / 1e9, 2), "steps": nsteps,
+                "objective_steps": [first, nsteps], "ckpt_every": ckpt,
                 "J": J, "forward_ms": tf, "backward_ms": tb, "adjoint_over_forward": tb / tf,
                 "forward_cell_steps_per_s": s.cells * nsteps / (tf / 1e3),
                 "grad_inlet_norm": float(np.linalg.norm(g_in)), "grad_eta_norm": float(np.linalg.norm(g_eta))}
@@ -693,6 +699,9 @@ def main(argv=None):
     ap.add_argument("--adj-workload", default="c4", choices=sorted(WORKLOADS))
     ap.add_argument("--adj-first", type=int, default=0,
                     help="first step of the drag average (0: the last third of --adj-steps)")
+    ap.add_argument("--adj-precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--adj-solver", default="jacobi", choices=["jacobi", "bicgstab", "cg"])
+    ap.add_argument("--adj-precond", default="none", choices=["none", "multigrid"])
     ap.add_argument("--maxit", type=int, default=5000,
                     help="Krylov iteration cap per solve (the reference's 5000; MIXED: FP32 iterations)")
     ap.add_argument("--fd-steps", type=int, default=21, help="adjoint_fd mode: steps of each forward run")
@@ -766,7 +775,7 @@ def main(argv=None):
     if "adjoint" in modes:
         try:
             line["adjoint"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt, args.adj_workload,
-                                           args.adj_first)
+                                           args.adj_first, args.adj_precision, args.adj_solver, args.adj_precond)
         except cg.CfdgbError as e:
             line["adjoint"] = {"value": None, "error": str(e)}
     if "adjoint_fd" in modes:  # not in the default modes: ~4 * fd_dirs forward runs

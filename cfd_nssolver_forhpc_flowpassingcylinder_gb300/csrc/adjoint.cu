@@ -15,6 +15,8 @@
 // upwind branches of the forward state held fixed (the scheme is piecewise linear in the
 // transported field and bilinear in the face velocities).  CD^T scatters with FP64
 // atomics; every other kernel gathers.
+#include <algorithm>
+
 #include "cfdgb_internal.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -396,6 +398,22 @@ void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, doub
                          const double *w, const double *lus, const double *lvs, const double *lws, double *lu,
                          double *lv, double *lw) {
   k_adj_convdiff<<<nblk, kBlock, 0, s>>>(g, dt, nu, u, v, w, lus, lvs, lws, lu, lv, lw);
+}
+
+// window storage of the adjoint: the pressure rounded to FP32 and back
+__global__ void __launch_bounds__(kBlock) k_f64_to_f32(long long n, const double *__restrict__ a, float *__restrict__ b) {
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock)
+    b[q] = (float)a[q];
+}
+__global__ void __launch_bounds__(kBlock) k_f32_to_f64(long long n, const float *__restrict__ a, double *__restrict__ b) {
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock)
+    b[q] = (double)a[q];
+}
+void launch_f64_to_f32(cudaStream_t s, long long n, const double *a, float *b) {
+  k_f64_to_f32<<<(int)std::min<long long>((n + kBlock - 1) / kBlock, 4096), kBlock, 0, s>>>(n, a, b);
+}
+void launch_f32_to_f64(cudaStream_t s, long long n, const float *a, double *b) {
+  k_f32_to_f64<<<(int)std::min<long long>((n + kBlock - 1) / kBlock, 4096), kBlock, 0, s>>>(n, a, b);
 }
 
 }  // namespace cfdgb

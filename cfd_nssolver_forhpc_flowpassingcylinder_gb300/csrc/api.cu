@@ -171,7 +171,11 @@ struct cfdgb_ctx {
   std::vector<double *> ck_f;  // 5 buffers per checkpoint: u, v, w, p (padded), x (compact)
   std::vector<SolverScal> ck_sc;
   std::vector<int> ck_loop;
-  std::vector<double *> win;  // 4 padded buffers per window step: u, v, w, p
+  std::vector<double *> win;  // 3 padded buffers per window step: u, v, w
+  std::vector<float *> winp;  // the window steps' pressure, padded, rounded to FP32
+  // the adjoint's transposed solve preconditioned by an FP64 V-cycle (contexts with the
+  // multigrid preconditioner; built on the first backward)
+  bool adj_mg = false;
   double *lA[3] = {nullptr}, *lB[3] = {nullptr}, *lus[3] = {nullptr}, *le[3] = {nullptr};
   double *leta = nullptr, *lx = nullptr, *linlet = nullptr;
   KrylovVecs<double> ka{};
@@ -1873,15 +1877,51 @@ int dd_copy(cfdgb_ctx *c, double *dst, const double *src, size_t n) {
 
 // Adjoint Poisson solve A y = rhs with the unscaled operator, zero start, its own scalars
 // (no restarts: a fresh solver object each time).
+// The FP64 V-cycle of the transposed solve (contexts with the multigrid preconditioner)
+int build_adjoint_mg(cfdgb_ctx *c) {
+  if (!c->use_mg64) {  // a MIXED context has only the FP32 hierarchy
+    const cfdgb_config &cf = c->cfg;
+    mg_plan(cf.nx, cf.ny, cf.nz, cf.lx / cf.nx, cf.ly / cf.ny, cf.lz / cf.nz, c->nsm, false, &c->mg64);
+    mg_prepare<double>();
+    TRY(upload_dense_coarse(c, c->mg64));
+    for (int l = 1; l < c->mg64.nlev; ++l) {
+      MgLevelT<double> &Lv = c->mg64.lev[l];
+      const size_t n = (size_t)Lv.nx * Lv.ny * Lv.nz;
+      TRY(dalloc(c, &Lv.x, n));
+      TRY(dalloc(c, &Lv.b, n));
+    }
+  }
+  c->adj_mg = true;
+  return 0;
+}
+
 int adjoint_solve(cfdgb_ctx *c, const double *rhs, double tol, int *iters) {
   CK(cudaMemsetAsync(c->sca, 0, sizeof(SolverScal), c->stream));
   CK(cudaMemsetAsync(c->ka.x, 0, c->ncell * sizeof(double), c->stream));
   TRY(set_solver_params(c, c->sca, tol, c->cfg.maxit));
-  launch_bicg_setup64(c->stream, c->nblk, c->g, c->spe64, c->ka, rhs, c->kapx[0], c->kapx[1], c->part, c->sca);
+  // with the multigrid preconditioner the transposed system (the same symmetric operator)
+  // gets the FP64 V-cycle; M p, M s in the two history vectors, free during the solve
+  const bool mg = c->adj_mg;
+  launch_bicg_setup64(c->stream, c->nblk, c->g, c->spe64, c->ka, rhs, c->kapx[0], c->kapx[1], c->part, c->sca,
+                      mg ? 1 : 0);
+  const PrecVecsT<double> pv{c->ka.x, c->ka.r0, c->ka.r1, c->ka.p1, c->ka.ap, c->ka.s, c->ka.as, c->kapx[0],
+                             c->kapx[1], nullptr};
   for (long long q = 0; q < (long long)c->cfg.maxit / 8 + 3; ++q) {
-    for (int m = 0; m < 8; ++m)
+    for (int m = 0; m < 8; ++m) {
+      if (mg) {
+        for (int part = 0; part < kPrecParts; ++part) {
+          L(c, kPrecKid64[part], part == 1 || part == 4 ? mg_vcycle_launches(c->mg64) : 1, [&] {
+            if (part == 1) launch_mg_vcycle(c->stream, c->mg64, 0, (const double *)pv.p, pv.ph, c->sca);
+            else if (part == 4) launch_mg_vcycle(c->stream, c->mg64, 0, (const double *)pv.s, pv.sh, c->sca);
+            else launch_bicgp64_part(c->stream, part == 0 ? 0 : part == 2 ? 1 : part == 3 ? 2 : part == 5 ? 3 : 4,
+                                     c->g, c->spe64, pv, c->part, c->sca);
+          });
+        }
+        continue;
+      }
       for (int part = 0; part < 5; ++part)
         L(c, K_AP64 + part, 1, [&] { launch_bicg64_part(c->stream, part, c->g, c->spe64, c->ka, c->part, c->sca); });
+    }
     CK(cudaMemcpyAsync(c->h_sc, c->sca, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
     TRY(sync(c));
     if (c->h_sc->done) {
@@ -1896,8 +1936,8 @@ int adjoint_solve(cfdgb_ctx *c, const double *rhs, double tol, int *iters) {
 
 int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
   if (!c || !obj) return fail(CFDGB_EINVAL, "null argument");
-  if (c->cfg.precision != CFDGB_FP64 || c->cfg.solver == CFDGB_RBSOR)
-    return fail(CFDGB_EINVAL, "the adjoint needs an FP64 BiCGSTAB context");
+  if (c->cfg.solver == CFDGB_RBSOR)  // the replay and the transposed solve are the Krylov solvers'
+    return fail(CFDGB_EINVAL, "the adjoint needs a Krylov-solver context (FP64 or MIXED)");
   if (c->g.nonuni)  // its transposed solve relies on the symmetric uniform-grid operator
     return fail(CFDGB_EINVAL, "the adjoint is implemented on the uniform grid");
   if (c->cfg.scheme != CFDGB_QUICK || c->cfg.les)  // its transposed stencil is QUICK's
@@ -1912,9 +1952,12 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
   c->obj = *obj;
   c->fwd_done = false;
   const int K = obj->ckpt_every, nck = (obj->nsteps + K - 1) / K;
+  // checkpoint q: u, v, w (padded), p (padded; only q = 0: later ones rebuild it from x, which
+  // holds p's interior after the step before, the ghosts being the boundary fill's), x
   while ((int)c->ck_f.size() < 5 * nck) {
+    const int slot = (int)(c->ck_f.size() % 5), q = (int)(c->ck_f.size() / 5);
     double *d = nullptr;
-    TRY(dalloc(c, &d, ((c->ck_f.size() % 5) == 4) ? c->ncell : c->npad));
+    if (slot != 3 || q == 0) TRY(dalloc(c, &d, slot == 4 ? c->ncell : c->npad));
     c->ck_f.push_back(d);
   }
   c->ck_sc.assign(nck, SolverScal{});
@@ -1927,7 +1970,7 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
       TRY(dd_copy(c, f[0], c->u, c->npad));
       TRY(dd_copy(c, f[1], c->v, c->npad));
       TRY(dd_copy(c, f[2], c->w, c->npad));
-      TRY(dd_copy(c, f[3], c->p, c->npad));
+      if (f[3]) TRY(dd_copy(c, f[3], c->p, c->npad));
       TRY(dd_copy(c, f[4], c->x, c->ncell));
       CK(cudaMemcpyAsync(&c->ck_sc[q], c->sc, sizeof(SolverScal), cudaMemcpyDeviceToHost, c->stream));
       c->ck_loop[q] = c->loop;
@@ -1963,11 +2006,17 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
     for (auto **q : kv) TRY(dalloc(c, q, c->ncell));
     TRY(dalloc(c, &c->sca, 1));
   }
-  while ((int)c->win.size() < 4 * K) {
+  while ((int)c->win.size() < 3 * K) {
     double *d = nullptr;
     TRY(dalloc(c, &d, np));
     c->win.push_back(d);
   }
+  while ((int)c->winp.size() < K) {
+    float *d = nullptr;
+    TRY(dalloc(c, &d, np));
+    c->winp.push_back(d);
+  }
+  if (c->cfg.precond == CFDGB_PRECOND_MULTIGRID && !c->adj_mg) TRY(build_adjoint_mg(c));
   for (int a = 0; a < 3; ++a) {
     CK(cudaMemsetAsync(c->lA[a], 0, np * sizeof(double), c->stream));
     CK(cudaMemsetAsync(c->lus[a], 0, np * sizeof(double), c->stream));
@@ -1985,30 +2034,38 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
     TRY(dd_copy(c, c->u, f[0], np));
     TRY(dd_copy(c, c->v, f[1], np));
     TRY(dd_copy(c, c->w, f[2], np));
-    TRY(dd_copy(c, c->p, f[3], np));
     TRY(dd_copy(c, c->x, f[4], c->ncell));
     CK(cudaMemcpyAsync(c->sc, &c->ck_sc[q], sizeof(SolverScal), cudaMemcpyHostToDevice, c->stream));
-    launch_bc(c->stream, c->g, c->u, c->v, c->w, nullptr, c->us, c->vs, c->ws, 0);  // T1's copies of T0
+    if (f[3]) {
+      TRY(dd_copy(c, c->p, f[3], np));
+      launch_bc(c->stream, c->g, c->u, c->v, c->w, nullptr, c->us, c->vs, c->ws, 0);  // T1's copies of T0
+    } else {
+      // p = its interior from x, then the ghost fill (which rewrites u, v, w's ghosts with the
+      // values they hold) and T1's copies
+      launch_transform(c->stream, c->nblk, c->g, c->x, c->p);
+      launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet);
+    }
     c->loop = c->ck_loop[q];
     for (int n = n0; n <= n1; ++n) {
-      double **wv = &c->win[4 * (n - n0)];
+      double **wv = &c->win[3 * (n - n0)];
       TRY(dd_copy(c, wv[0], c->u, np));
       TRY(dd_copy(c, wv[1], c->v, np));
       TRY(dd_copy(c, wv[2], c->w, np));
       cfdgb_step_stats st{};
       const int rc = cfdgb_step(c, 1, &st);
       if (rc < 0 && rc != CFDGB_ENOCONV) return rc;
-      TRY(dd_copy(c, wv[3], c->p, np));
+      launch_f64_to_f32(c->stream, (long long)np, c->p, c->winp[n - n0]);
     }
-    // reverse sweep over the window
+    // reverse sweep over the window (p^n back to FP64 in the context's p, free here)
     for (int n = n1; n >= n0; --n) {
-      double **wv = &c->win[4 * (n - n0)];
+      double **wv = &c->win[3 * (n - n0)];
+      launch_f32_to_f64(c->stream, (long long)np, c->winp[n - n0], c->p);
       launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
       // u* of step n (interior faces), from U^n
       launch_convdiff_exact(c->stream, c->nblk, c->g, CFDGB_QUICK, dt, nu, nullptr, wv[0], wv[1], wv[2], c->us, c->vs,
                             c->ws, StepCtl{});
       const double cw = (n >= obj.first && n <= obj.last) ? cw_in : 0.0;
-      launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, wv[3], c->us, c->vs, c->ws, c->lA[0], c->lA[1],
+      launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, c->p, c->us, c->vs, c->ws, c->lA[0], c->lA[1],
                       c->lA[2], c->lus[0], c->lus[1], c->lus[2], c->le[0], c->le[1], c->le[2], c->lx, c->leta,
                       c->part, c->ss);
       for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(c->lB[a], 0, np * sizeof(double), c->stream));

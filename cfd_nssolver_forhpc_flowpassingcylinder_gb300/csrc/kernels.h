@@ -124,6 +124,9 @@ void launch_adj_corr(cudaStream_t s, int nblk, const Geo &g, double dt, double c
                      double *lx, double *leta, double *part, StepScal *ss);
 // y -= mean(y); sum_known: the previous kernel left sum(y) in ss->fsum[0]
 void launch_remove_mean(cudaStream_t s, int nblk, const Geo &g, double *y, double *part, StepScal *ss, bool sum_known);
+// padded field conversions of the adjoint's window storage
+void launch_f64_to_f32(cudaStream_t s, long long n, const double *a, float *b);
+void launch_f32_to_f64(cudaStream_t s, long long n, const float *a, double *b);
 void launch_adj_rhs(cudaStream_t s, int nblk, const Geo &g, double dt, const double *lb, double *lus, double *lvs,
                     double *lws, double *lu, double *lv, double *lw);
 void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, double nu, const double *u, const double *v,

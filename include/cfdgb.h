@@ -206,13 +206,17 @@ int cfdgb_step(cfdgb_ctx *ctx, int nsteps, cfdgb_step_stats *stats);
 
 /* ---- discrete adjoint (no reference counterpart: the reference has no gradients) ----
  * Objective J: drag coefficient averaged over steps first..last of an nsteps run that
- * starts from the state cfdgb_init_fields set.  cfdgb_forward runs it (FP64 context, a
- * BiCGSTAB solver), keeping a checkpoint (T0, p, solver warm start and scalars) every
- * ckpt_every steps, and returns J.  cfdgb_backward sweeps the steps in reverse,
- * recomputing each checkpoint window forward first, and returns dJ/d(inlet u profile)
- * (ny*nz values, the inlet ghost value of BC_staggered_main's face 0 per (j,k)) and
- * dJ/d(solid fraction eta) (padded field).  Memory: (5 + 4*ckpt_every) padded FP64 fields
- * beyond the forward ones. */
+ * starts from the state cfdgb_init_fields set.  cfdgb_forward runs it (a Krylov solver,
+ * FP64 or MIXED, fixed dt, the Euler step, QUICK without the Smagorinsky model, uniform
+ * grid), keeping a checkpoint every ckpt_every steps, and returns J.  cfdgb_backward sweeps
+ * the steps in reverse, recomputing each checkpoint window forward first (in the context's
+ * precision), and returns dJ/d(inlet u profile) (ny*nz values, the inlet ghost value of
+ * BC_staggered_main's face 0 per (j,k)) and dJ/d(solid fraction eta) (padded field).  The
+ * transposed Poisson solve is FP64 BiCGSTAB, preconditioned by the FP64 V-cycle when the
+ * context has the multigrid preconditioner.  Memory beyond the forward's: per checkpoint
+ * u, v, w (padded FP64) and the solver's warm start (compact; p is rebuilt from it), plus
+ * p for the first; per window step u, v, w (padded FP64) and p (padded FP32); about 14
+ * padded FP64 fields and 9 compact ones of adjoint state. */
 typedef struct cfdgb_objective {
   int nsteps;      /* forward steps */
   int first, last; /* drag averaged over these steps (1-based, inclusive) */

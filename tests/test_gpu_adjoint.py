@@ -137,3 +137,24 @@ def test_free_slip_walls_gradients_match_central_fd():
         assert abs(float(np.sum(g_eta * de)) - fd) <= 1e-4 * abs(fd) + 1e-9
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("kw", [dict(precond="multigrid"), dict(precision="mixed", precond="multigrid"),
+                                dict(precision="mixed", solver="cg")],
+                         ids=["fp64_multigrid", "mixed_multigrid", "mixed_cg"])
+def test_adjoint_of_other_contexts_matches_fp64(adj, kw):
+    """The adjoint from a context whose forward runs the multigrid-preconditioned FP64
+    solver, or MIXED precision (FP32 sweeps in FP64 refinement; the transposed solve stays
+    FP64, with the FP64 V-cycle where the context has the multigrid preconditioner): the
+    same objective and gradients as the plain FP64 context's, which the finite-difference
+    tests above check.  The MIXED forward differs from FP64 by its FP32 rounding."""
+    s0, eta0, J0, g_in0, g_eta0 = adj
+    with cg.Solver(tol=TOL, project_rhs=PROJECT, **kw, **CASE) as s:
+        s.set_inlet(None)
+        s.init_fields()
+        J = s.forward(NSTEPS, FIRST, LAST, K)
+        g_in, g_eta = s.backward()
+    bar = 1e-9 if "precision" not in kw else 1e-6
+    assert abs(J - J0) <= bar * abs(J0), (J, J0)
+    assert np.linalg.norm(g_in - g_in0) <= 1e2 * bar * np.linalg.norm(g_in0)
+    assert np.linalg.norm(g_eta - g_eta0) <= 1e2 * bar * np.linalg.norm(g_eta0)
