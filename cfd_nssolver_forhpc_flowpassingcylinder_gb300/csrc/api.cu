@@ -388,6 +388,17 @@ double sor_omega_opt(const cfdgb_config *c) {
   return 2.0 / (1.0 + std::sqrt(std::max(0.0, 1.0 - mu * mu)));
 }
 
+// The step kernels' divisors are the metric arrays and dt: the single correction of div_by
+// is proven only for certified divisors (div_certified); any other one, or a dt that an
+// adaptive rule chooses on the device, selects the double correction
+bool division_twice(const cfdgb_ctx *c) {
+  if (c->cfg.dt_mode != CFDGB_DT_FIXED || !div_certified(c->cfg.dt)) return true;
+  for (auto *v : {&c->Dx, &c->Dy, &c->Dz, &c->Dxs, &c->Dys, &c->Dzs})
+    for (double d : *v)
+      if (!div_certified(d)) return true;
+  return false;
+}
+
 int validate(const cfdgb_config *c) {
   if (!c) return fail(CFDGB_EINVAL, "null config");
   if (c->nx < 3 || c->ny < 3 || c->nz < 3) return fail(CFDGB_EINVAL, "grid must be at least 3x3x3 interior cells");
@@ -1232,6 +1243,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.rDxs = g.rDz + nz; g.rDys = g.rDxs + nx; g.rDzs = g.rDys + ny;
     g.hfx = g.rDzs + nz; g.hfy = g.hfx + nx; g.hfz = g.hfy + ny;
   }
+  g.div2 = division_twice(c) ? 1 : 0;
   if (cfg->grid == CFDGB_GRID_SML) {
     // per-axis operator factors and the Jacobi scale of every row (createPressureMatrixCSR)
     const Coef C{c};
@@ -1756,6 +1768,7 @@ int cfdgb_set_dt(cfdgb_ctx *c, double dt) {
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(CFDGB_EINVAL, "dt must be positive");
   c->cfg.dt = dt;
   drop_step_graph(c);  // a graph holds the CFL rule's dt bound, taken from dt
+  c->g.div2 = division_twice(c) ? 1 : 0;  // dt is a divisor too
   if (c->cfg.time_order == 3 && c->ss)  // the constant-step history is of the old dt
     CK(cudaMemsetAsync(&c->ss->hist, 0, 2 * sizeof(int), c->stream));
   // the step kernels read dt from the step scalars

@@ -52,6 +52,7 @@ struct Geo {
   // per-index reciprocals RN(1/D), RN(1/Ds) of the metrics (padded lengths) for div_by, and
   // the DFIB face-fraction factors (Ds * 0.5) / D of updateUandF.hpp, each one IEEE division
   const double *rDx, *rDy, *rDz, *rDxs, *rDys, *rDzs, *hfx, *hfy, *hfz;
+  int div2;  // 1: div_by applies its correction twice (a divisor lacks the certificate)
 };
 
 // Width along k of the 3-D solver blocks (host side; the context driver and the
@@ -68,16 +69,36 @@ inline int k_block_width(int nz) {
   return w;
 }
 
-// a / b correctly rounded, given y = RN(1/b): q = RN(a y) lies within an ulp of a / b, so
-// the remainder a - b q is exact in one FMA and RN(q + (a - b q) y) = RN(a / b) (Markstein's
-// theorem: P. Markstein, IBM J. Res. Develop. 34(1), 1990; J.-M. Muller et al., Handbook of
-// Floating-Point Arithmetic, the chapter on division by FMA).  It holds while a / b and the
-// intermediates are normal numbers; a = +-0 returns the zero of IEEE division's sign.
-__device__ __forceinline__ double div_by(double a, double b, double y) {
+// a / b correctly rounded, given y = RN(1/b), by Markstein's FMA correction.  Markstein's
+// theorem (P. Markstein, IBM J. Res. Develop. 34(1), 1990; J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, the chapter on division by FMA): if y is within half an ulp of
+// 1/b and q within one ulp of a/b, then r = a - b q is exact and RN(q + r y) = RN(a/b),
+// while a/b and the intermediates are normal numbers.  q = RN(a y) is within
+// 1/2 ulp + |a/b| |b y - 1| of a/b: within one ulp for every a when the divisor's
+// certificate |b y - 1| < 2^-54 holds (div_certified, checked on the host for every
+// divisor a context uploads), but only within 1.5 ulp in general.  two = true (some
+// divisor of the context lacks the certificate) applies the correction twice: the first
+// brings q within 1/2 ulp plus a few 2^-53 of an ulp of a/b (its r is exact or nearly so),
+// after which the theorem applies to the second.  a = +-0 returns the zero of IEEE
+// division's sign.
+__device__ __forceinline__ double div_by(double a, double b, double y, bool two) {
   const double q = __dmul_rn(a, y);
-  const double r = fma(-q, b, a);
-  const double q1 = fma(r, y, q);
+  double r = fma(-q, b, a);
+  double q1 = fma(r, y, q);
+  if (two) {
+    r = fma(-q1, b, a);
+    q1 = fma(r, y, q1);
+  }
   return a == 0.0 ? q : q1;
+}
+
+// Host: whether b's reciprocal y = RN(1/b) carries Markstein's certificate |b y - 1| < 2^-54
+// (the product b y - 1 is computed exactly by one FMA: its 106-bit product lies within
+// 2^-52 of 1, so the difference fits a double).
+inline bool div_certified(double b) {
+  const double y = 1.0 / b;
+  const double e = __builtin_fma(b, y, -1.0);
+  return __builtin_fabs(e) < 0x1.0p-54;
 }
 
 // compact row -> padded (i,j,k).  Grids below 2^31 cells divide in 32 bits: a 64-bit

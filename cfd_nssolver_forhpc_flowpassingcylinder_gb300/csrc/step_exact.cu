@@ -16,14 +16,14 @@
 namespace cfdgb {
 
 // inc/source/Convection_Difussion.hpp:20-51 (QuickUnitA)
-__device__ __forceinline__ void quick_a(double Up, double Un, long long pp, long long p, long long ic,
+__device__ __forceinline__ void quick_a(bool two, double Up, double Un, long long pp, long long p, long long ic,
                                         long long n, long long nn, const double *__restrict__ Di,
                                         const double *__restrict__ Ds, const double *__restrict__ rDi,
                                         const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
-  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
-  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q]); };  // a / Ds[q]
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q], two); };  // a / Di[q]
+  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q], two); };  // a / Ds[q]
   if (Up > 0.0)
     P = 0.5 * (fc + fp) - os(0.125 * Di[I + 1] * Di[I + 1], I) * (oi(fp - fc, I + 1) - oi(fc - fn, I));
   else
@@ -37,14 +37,14 @@ __device__ __forceinline__ void quick_a(double Up, double Un, long long pp, long
 }
 
 // inc/source/Convection_Difussion.hpp:55-90 (QuickUnitB)
-__device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long long p, long long ic,
+__device__ __forceinline__ void quick_b(bool two, double Up, double Un, long long pp, long long p, long long ic,
                                         long long n, long long nn, const double *__restrict__ Di,
                                         const double *__restrict__ Ds, const double *__restrict__ rDi,
                                         const double *__restrict__ rDs, int I,
                                         const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
-  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
-  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q]); };  // a / Ds[q]
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q], two); };  // a / Di[q]
+  auto os = [&](double a, int q) { return div_by(a, Ds[q], rDs[q], two); };  // a / Ds[q]
   if (Up > 0.0)
     P = 0.5 * (fc + fp) - oi(0.125 * Ds[I] * Ds[I], I) * (os(fp - fc, I) - os(fc - fn, I - 1));
   else
@@ -58,12 +58,12 @@ __device__ __forceinline__ void quick_b(double Up, double Un, long long pp, long
 }
 
 // inc/source/Convection_Difussion.hpp:96-147 (LudUnitA; LudUnitB has the same body)
-__device__ __forceinline__ void lud(double Up, double Un, long long pp, long long p, long long ic, long long n,
+__device__ __forceinline__ void lud(bool two, double Up, double Un, long long pp, long long p, long long ic, long long n,
                                     long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
                                     const double *__restrict__ rDi, const double *__restrict__ rDs, int I,
                                     const double *__restrict__ phi, double &P, double &N) {
   const double fc = phi[ic], fp = phi[p], fn = phi[n];
-  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q]); };  // a / Di[q]
+  auto oi = [&](double a, int q) { return div_by(a, Di[q], rDi[q], two); };  // a / Di[q]
   if (Up > 0.0)
     P = (fc + oi(0.5 * Ds[I] * (fc - fn), I));
   else
@@ -77,19 +77,19 @@ __device__ __forceinline__ void lud(double Up, double Un, long long pp, long lon
 // face values of one axis under the convection switch (inc/0_General.hpp:114-118): QUICK,
 // LUD or UD (UdUnit, :150-168); OWN: the component's own axis (the "A" units)
 template <int S, bool OWN>
-__device__ __forceinline__ void face(double Up, double Un, long long pp, long long p, long long ic, long long n,
+__device__ __forceinline__ void face(bool two, double Up, double Un, long long pp, long long p, long long ic, long long n,
                                      long long nn, const double *__restrict__ Di, const double *__restrict__ Ds,
                                      const double *__restrict__ rDi, const double *__restrict__ rDs, int I,
                                      const double *__restrict__ phi, double &P, double &N) {
   if (S == CFDGB_LUD) {
-    lud(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
+    lud(two, Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   } else if (S == CFDGB_UD) {
     P = Up > 0.0 ? phi[ic] : phi[p];
     N = Un > 0.0 ? phi[n] : phi[ic];
   } else if (OWN) {
-    quick_a(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
+    quick_a(two, Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   } else {
-    quick_b(Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
+    quick_b(two, Up, Un, pp, p, ic, n, nn, Di, Ds, rDi, rDs, I, phi, P, N);
   }
 }
 
@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(kBlock) k_smagorinsky(Geo g, const double *__r
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
-    auto h = [&](double d, double r) { return div_by(0.5, d, r); };  // 0.5 / d
+    const bool two = g.div2 != 0;
+    auto h = [&](double d, double r) { return div_by(0.5, d, r, two); };  // 0.5 / d
     const double ux = h(g.Dxs[i], g.rDxs[i]) * (u[c - sx] - u[c + sx]);
     const double uy = h(g.Dy[j], g.rDy[j]) * (u[c - sy] - u[c + sy]);
     const double uz = h(g.Dz[k], g.rDz[k]) * (u[c - 1] - u[c + 1]);
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
                                                            double *__restrict__ vs,
                                                            double *__restrict__ ws, StepCtl sc) {
   const double dt = step_dt(sc, dt_arg);
+  const bool two = g.div2 != 0;
   CflAcc cfl;
   AbStep ab;
   if (AB) ab.init(sc, dt);
@@ -152,12 +154,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
   const double *Dx = g.Dx, *Dy = g.Dy, *Dz = g.Dz, *Dxs = g.Dxs, *Dys = g.Dys, *Dzs = g.Dzs;
   const double *rDx = g.rDx, *rDy = g.rDy, *rDz = g.rDz, *rDxs = g.rDxs, *rDys = g.rDys, *rDzs = g.rDzs;
   // a / D[q] of each metric array (div_by with the array's reciprocals)
-  auto ox = [&](double a, int q) { return div_by(a, Dx[q], rDx[q]); };
-  auto oy = [&](double a, int q) { return div_by(a, Dy[q], rDy[q]); };
-  auto oz = [&](double a, int q) { return div_by(a, Dz[q], rDz[q]); };
-  auto oxs = [&](double a, int q) { return div_by(a, Dxs[q], rDxs[q]); };
-  auto oys = [&](double a, int q) { return div_by(a, Dys[q], rDys[q]); };
-  auto ozs = [&](double a, int q) { return div_by(a, Dzs[q], rDzs[q]); };
+  auto ox = [&](double a, int q) { return div_by(a, Dx[q], rDx[q], two); };
+  auto oy = [&](double a, int q) { return div_by(a, Dy[q], rDy[q], two); };
+  auto oz = [&](double a, int q) { return div_by(a, Dz[q], rDz[q], two); };
+  auto oxs = [&](double a, int q) { return div_by(a, Dxs[q], rDxs[q], two); };
+  auto oys = [&](double a, int q) { return div_by(a, Dys[q], rDys[q], two); };
+  auto ozs = [&](double a, int q) { return div_by(a, Dzs[q], rDzs[q], two); };
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
@@ -176,9 +178,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
       const double Wp = w[ic] + (w[xp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + xp - ic] - w[zm]) * IT;
       double uPx, uNx, uPy, uNy, uPz, uNz;
-      face<S, true>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, u, uPx, uNx);
-      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, u, uPy, uNy);
-      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, u, uPz, uNz);
+      face<S, true>(two, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, u, uPx, uNx);
+      face<S, false>(two, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, u, uPy, uNy);
+      face<S, false>(two, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, u, uPz, uNz);
       const double convection = -dt * (oxs(uPx * uPx - uNx * uNx, i) + oy(uPy * Vp - uNy * Vn, j) +
                                        oz(uPz * Wp - uNz * Wn, k));
       const double difussion =
@@ -201,9 +203,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
       const double Wp = w[ic] + (w[yp] - w[ic]) * IT;
       const double Wn = w[zm] + (w[zm + yp - ic] - w[zm]) * IT;
       double vPx, vNx, vPy, vNy, vPz, vNz;
-      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, v, vPx, vNx);
-      face<S, true>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, v, vPy, vNy);
-      face<S, false>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, v, vPz, vNz);
+      face<S, false>(two, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, v, vPx, vNx);
+      face<S, true>(two, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, v, vPy, vNy);
+      face<S, false>(two, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, v, vPz, vNz);
       const double convection = -dt * (ox(Up * vPx - Un * vNx, i) + oys(vPy * vPy - vNy * vNy, j) +
                                        oz(Wp * vPz - Wn * vNz, k));
       const double difussion =
@@ -226,9 +228,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
       const double Vp = v[ic] + (v[zp] - v[ic]) * IT;
       const double Vn = v[ym] + (v[ym + zp - ic] - v[ym]) * IT;
       double wPx, wNx, wPy, wNy, wPz, wNz;
-      face<S, false>(Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, w, wPx, wNx);
-      face<S, false>(Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, w, wPy, wNy);
-      face<S, true>(Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, w, wPz, wNz);
+      face<S, false>(two, Up, Un, ic + 2 * sx, xp, ic, xm, ic - 2 * sx, Dx, Dxs, rDx, rDxs, i, w, wPx, wNx);
+      face<S, false>(two, Vp, Vn, ic + 2 * sy, yp, ic, ym, ic - 2 * sy, Dy, Dys, rDy, rDys, j, w, wPy, wNy);
+      face<S, true>(two, Wp, Wn, ic + 2 * sz, zp, ic, zm, ic - 2 * sz, Dz, Dzs, rDz, rDzs, k, w, wPz, wNz);
       const double convection = -dt * (ox(Up * wPx - Un * wNx, i) + oy(Vp * wPy - Vn * wNy, j) +
                                        ozs(wPz * wPz - wNz * wNz, k));
       const double difussion =
@@ -253,14 +255,15 @@ __global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt_arg, cons
                                                       const double *__restrict__ ws, int jacobi,
                                                       Stencil<double> st, double *__restrict__ b) {
   const double ddt = 1.0 / (dtp ? *dtp : dt_arg);
+  const bool two = g.div2 != 0;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
-    const double div = div_by(us[ic] - us[ic - g.sx], g.Dx[i], g.rDx[i]) +
-                       div_by(vs[ic] - vs[ic - g.sy], g.Dy[j], g.rDy[j]) +
-                       div_by(ws[ic] - ws[ic - 1], g.Dz[k], g.rDz[k]);
+    const double div = div_by(us[ic] - us[ic - g.sx], g.Dx[i], g.rDx[i], two) +
+                       div_by(vs[ic] - vs[ic - g.sy], g.Dy[j], g.rDy[j], two) +
+                       div_by(ws[ic] - ws[ic - 1], g.Dz[k], g.rDz[k], two);
     if (jacobi) {
       b[row] = -row_jp(g, st, i - 2, j - 2, k - 2, row) * ddt * div;
     } else {
@@ -287,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_exact(Geo g, Stencil<double> st
 __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *__restrict__ us,
                                                  const double *__restrict__ vs, const double *__restrict__ ws,
                                                  StepCtl sc) {
+  const bool two = g.div2 != 0;
   CflAcc cfl;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
@@ -295,15 +299,15 @@ __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *
     const long long ic = pidx(g, i, j, k);
     double c = 0.0;
     if (i < g.nx - 3) {
-      c += div_by(us[ic], g.Dxs[i], g.rDxs[i]);
+      c += div_by(us[ic], g.Dxs[i], g.rDxs[i], two);
       cfl.comp(0, us[ic]);
     }
     if (j < g.ny - 3) {
-      c += div_by(vs[ic], g.Dys[j], g.rDys[j]);
+      c += div_by(vs[ic], g.Dys[j], g.rDys[j], two);
       cfl.comp(1, vs[ic]);
     }
     if (k < g.nz - 3) {
-      c += div_by(ws[ic], g.Dzs[k], g.rDzs[k]);
+      c += div_by(ws[ic], g.Dzs[k], g.rDzs[k], two);
       cfl.comp(2, ws[ic]);
     }
     cfl.cell(c);
@@ -375,6 +379,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     double *__restrict__ f, const double *__restrict__ ui, const double *__restrict__ vi,
     const double *__restrict__ wi, double *part, StepScal *ss) {
   const double dt = dtp ? *dtp : dt_arg;
+  const bool two = g.div2 != 0;
   const long long tot = (long long)g.nx * g.ny * g.nz;
   const double uS = 0.0, vS = 0.0, wS = 0.0;
   const double rdt = 1.0 / dt;
@@ -388,10 +393,10 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     const double ec = eta[ic];
     if (i < g.nx - 3) {
       const long long icP = ic + g.sx;
-      const double T2u = us[ic] - div_by(dt * (p[icP] - p[ic]), g.Dxs[i], g.rDxs[i]);
+      const double T2u = us[ic] - div_by(dt * (p[icP] - p[ic]), g.Dxs[i], g.rDxs[i], two);
       const double e = ec + (eta[icP] - ec) * g.hfx[i];
       const double nu3 = ec * uS + (1.0 - e) * T2u;
-      const double fx = div_by(nu3 - T2u, dt, rdt);
+      const double fx = div_by(nu3 - T2u, dt, rdt, two);
       u3[ic] = nu3;
       if (f) f[ic] = fx;
       acc[0] += fx * vol;
@@ -400,10 +405,10 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     }
     if (j < g.ny - 3) {
       const long long icP = ic + g.sy;
-      const double T2v = vs[ic] - div_by(dt * (p[icP] - p[ic]), g.Dys[j], g.rDys[j]);
+      const double T2v = vs[ic] - div_by(dt * (p[icP] - p[ic]), g.Dys[j], g.rDys[j], two);
       const double e = ec + (eta[icP] - ec) * g.hfy[j];
       const double nv3 = ec * vS + (1.0 - e) * T2v;
-      const double fy = div_by(nv3 - T2v, dt, rdt);
+      const double fy = div_by(nv3 - T2v, dt, rdt, two);
       v3[ic] = nv3;
       if (f) f[ic + tot] = fy;
       acc[1] += fy * vol;
@@ -412,11 +417,11 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     }
     if (k < g.nz - 3) {
       const long long icP = ic + 1;
-      const double T2w = ws[ic] - div_by(dt * (p[icP] - p[ic]), g.Dzs[k], g.rDzs[k]);
+      const double T2w = ws[ic] - div_by(dt * (p[icP] - p[ic]), g.Dzs[k], g.rDzs[k], two);
       const double e = ec + (eta[icP] - ec) * g.hfz[k];
       const double nw3 = ec * wS + (1.0 - e) * T2w;
       w3[ic] = nw3;
-      if (f) f[ic + 2 * tot] = div_by(nw3 - T2w, dt, rdt);
+      if (f) f[ic + 2 * tot] = div_by(nw3 - T2w, dt, rdt, two);
     } else if (wi) {
       w3[ic] = wi[ic];
     }
@@ -663,7 +668,7 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 __global__ void __launch_bounds__(kBlock) k_check_div(long long n, unsigned long long seed, double b, double y,
-                                                      unsigned long long *bad) {
+                                                      bool two, unsigned long long *bad) {
   unsigned long long miss = 0;
   for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < n; q += (long long)gridDim.x * kBlock) {
     const unsigned long long h1 = mix64(seed ^ (unsigned long long)q), h2 = mix64(h1);
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(kBlock) k_check_div(long long n, unsigned long
       const double m = 1.0 + (double)(h1 >> 12) * 0x1.0p-52;  // [1, 2), 52 random bits
       a = scalbn(m, (int)(h2 % 81) - 40) * ((h2 >> 40) & 1 ? -1.0 : 1.0);
     }
-    if (__double_as_longlong(a / b) != __double_as_longlong(div_by(a, b, y))) ++miss;
+    if (__double_as_longlong(a / b) != __double_as_longlong(div_by(a, b, y, two))) ++miss;
   }
   if (miss) atomicAdd(bad, miss);
 }
@@ -688,7 +693,8 @@ extern "C" int cfdgb_check_division(long long n, uint64_t seed, double b, unsign
   unsigned long long *d = nullptr;
   if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return CFDGB_ECUDA;
   cudaMemset(d, 0, sizeof(*d));
-  k_check_div<<<1216, kBlock>>>(n, seed, b, 1.0 / b, d);
+  // the form the library uses for a context whose only divisor is b
+  k_check_div<<<1216, kBlock>>>(n, seed, b, 1.0 / b, !div_certified(b), d);
   const cudaError_t e = cudaMemcpy(mismatches, d, sizeof(*d), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess && cudaGetLastError() == cudaSuccess ? CFDGB_OK : CFDGB_ECUDA;

@@ -327,9 +327,12 @@ int cfdgb_pressure_solve(cfdgb_ctx *ctx, int *iters, double *relres);
 
 /* ---- self-check ---- */
 /* The step kernels divide by a metric or dt through its reciprocal (Markstein's FMA
- * correction, correctly rounded like IEEE division).  On the current GPU: n seeded dividends
+ * correction, correctly rounded like IEEE division): once for a divisor b whose reciprocal
+ * y = RN(1/b) satisfies |b y - 1| < 2^-54 (then Markstein's theorem covers every dividend),
+ * twice in a context where some divisor does not.  On the current GPU: n seeded dividends
  * (random sign, significand and exponent in [2^-40, 2^40], a tenth of them exact multiples
- * of b, and zeros) divided by b both ways; *mismatches counts results whose bits differ. */
+ * of b, and zeros) divided by b both ways, with the form a context whose only divisor is b
+ * would use; *mismatches counts results whose bits differ. */
 int cfdgb_check_division(long long n, uint64_t seed, double b, unsigned long long *mismatches);
 
 #ifdef __cplusplus
