@@ -17,7 +17,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libcfdgb.so"
 
-ABI_VERSION = 8  # CFDGB_ABI_VERSION
+ABI_VERSION = 9  # CFDGB_ABI_VERSION
 OK, EINVAL, ECUDA, ENOCONV, ENAN, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5, -6
 BICGSTAB, BICGSTAB_JACOBI, RBSOR, CG = 0, 1, 2, 3
 FP64, MIXED = 0, 1
@@ -34,6 +34,13 @@ PRECOND_NONE, PRECOND_MULTIGRID = 0, 1
 PRECONDS = {"none": PRECOND_NONE, "multigrid": PRECOND_MULTIGRID}
 DT_FIXED, DT_REFERENCE, DT_CFL = 0, 1, 2
 DT_MODES = {"fixed": DT_FIXED, "reference": DT_REFERENCE, "cfl": DT_CFL}
+Z_ZERO_GRADIENT, Z_PERIODIC = 0, 1
+BC_Z = {"zero_gradient": Z_ZERO_GRADIENT, "periodic": Z_PERIODIC}
+OUTFLOW_ZERO_GRADIENT, OUTFLOW_CONVECTIVE = 0, 1
+OUTFLOWS = {"zero_gradient": OUTFLOW_ZERO_GRADIENT, "convective": OUTFLOW_CONVECTIVE}
+# the boundary set of the plain FP64 cylinder case (uniform inflow, convective outflow,
+# free-slip y walls, periodic z): default_config(**BOUNDARY_SET) or Solver(**BOUNDARY_SET, ...)
+BOUNDARY_SET = {"walls": "free_slip", "bc_z": "periodic", "outflow": "convective"}
 
 
 class CfdgbError(RuntimeError):
@@ -54,7 +61,7 @@ class Config(C.Structure):
                 ("dfib", C.c_int), ("seed", C.c_uint64), ("amp", C.c_double), ("project_rhs", C.c_int),
                 ("grid", C.c_int), ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int),
                 ("precond", C.c_int), ("dt_mode", C.c_int), ("cfl_target", C.c_double), ("dt_max", C.c_double),
-                ("time_order", C.c_int)]
+                ("time_order", C.c_int), ("bc_z", C.c_int), ("outflow", C.c_int)]
 
 
 class Objective(C.Structure):
@@ -178,6 +185,10 @@ def default_config(**kw) -> Config:
             v = PRECONDS[v]
         if k == "dt_mode" and isinstance(v, str):
             v = DT_MODES[v]
+        if k == "bc_z" and isinstance(v, str):
+            v = BC_Z[v]
+        if k == "outflow" and isinstance(v, str):
+            v = OUTFLOWS[v]
         if k == "les":
             v = int(bool(v))
         setattr(cfg, k, v)

@@ -370,6 +370,19 @@ std::vector<float> build_tab32(const cfdgb_ctx *c, int L) {
   return t;
 }
 
+// The convective outflow's velocity: the area-weighted mean of the inlet u over the inlet
+// face (in NULL: the reference's constant 1.0, whose mean is exactly 1)
+double inlet_mean(const cfdgb_ctx *c, const double *in) {
+  double q = 0.0, a = 0.0;
+  for (int j = 2; j < c->cfg.ny + 2; ++j)
+    for (int k = 2; k < c->cfg.nz + 2; ++k) {
+      const double da = c->Dy[j] * c->Dz[k];
+      q += (in ? in[(size_t)(j - 2) * c->cfg.nz + (k - 2)] : 1.0) * da;
+      a += da;
+    }
+  return q / a;
+}
+
 // The optimal SOR relaxation for the uniform-grid Neumann operator: 2 / (1 + sqrt(1 - mu^2))
 // with mu the spectral radius of the Jacobi iteration on the non-constant modes, the mode
 // with one half-wave along the axis where c_a (1 - cos(pi / n_a)) is least (c_a = 1/h_a^2):
@@ -430,6 +443,16 @@ int validate(const cfdgb_config *c) {
     if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, false, &mg))
       return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
                   c->ny, c->nz, kMgSharedCells);
+  }
+  if (c->bc_z != CFDGB_Z_ZERO_GRADIENT && c->bc_z != CFDGB_Z_PERIODIC)
+    return fail(CFDGB_EINVAL, "unknown bc_z %d", c->bc_z);
+  if (c->outflow != CFDGB_OUTFLOW_ZERO_GRADIENT && c->outflow != CFDGB_OUTFLOW_CONVECTIVE)
+    return fail(CFDGB_EINVAL, "unknown outflow %d", c->outflow);
+  if (c->bc_z == CFDGB_Z_PERIODIC) {
+    if (c->precond == CFDGB_PRECOND_MULTIGRID)  // its coarse levels are Neumann in z
+      return fail(CFDGB_EINVAL, "the multigrid preconditioner is implemented for zero-gradient z faces");
+    if (c->solver == CFDGB_RBSOR && c->nz % 2)  // the cells across the wrap must differ in colour
+      return fail(CFDGB_EINVAL, "red-black SOR with periodic z needs nz even");
   }
   if (c->dt_mode < CFDGB_DT_FIXED || c->dt_mode > CFDGB_DT_CFL) return fail(CFDGB_EINVAL, "unknown dt_mode %d", c->dt_mode);
   if (c->time_order < 0 || c->time_order > 3) return fail(CFDGB_EINVAL, "time_order must be 1, 2 or 3");
@@ -812,7 +835,7 @@ int apply_init_bc(cfdgb_ctx *c) {
   CK(cudaMemcpyAsync(c->us, c->u, bytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->vs, c->v, bytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->ws, c->w, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet);
+  launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet, 0, c->part, c->ss, c->nblk);
   CK(cudaMemsetAsync(c->x, 0, c->ncell * sizeof(double), c->stream));  // X_result = 0
   CK(cudaMemsetAsync(c->px1, 0, c->ncell * sizeof(double), c->stream));
   CK(cudaMemsetAsync(c->px2, 0, c->ncell * sizeof(double), c->stream));
@@ -915,7 +938,9 @@ void enqueue_update_bc(cfdgb_ctx *c) {
                              c->p, c->us, c->vs, c->ws, c->u, c->v, c->w, nullptr, c->ui, c->vi, c->wi, c->part,
                              c->ss);
   });
-  L(c, K_BC, 3, [&] { launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet); });
+  L(c, K_BC, 3 + c->g.outflow, [&] {
+    launch_bc(c->stream, c->g, c->u, c->v, c->w, c->p, c->us, c->vs, c->ws, 1, c->inlet, 1, c->part, c->ss, c->nblk);
+  });
 }
 
 // ---- one CUDA graph per time step ----
@@ -1223,6 +1248,9 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   Geo &g = c->g;
   g.nxc = cfg->nx; g.nyc = cfg->ny; g.nzc = cfg->nz;
   g.walls = cfg->walls;
+  g.pz = cfg->bc_z == CFDGB_Z_PERIODIC ? 1 : 0;
+  g.outflow = cfg->outflow == CFDGB_OUTFLOW_CONVECTIVE ? 1 : 0;
+  g.uconv = inlet_mean(c, nullptr);
   g.nx = nx; g.ny = ny; g.nz = nz;
   g.sx = (long long)ny * nz; g.sy = nz;
   g.ncell = c->ncell;
@@ -1263,8 +1291,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
           if (i == cfg->nx - 1) aa = -C.xp(i);
           if (j == 0) bb = -C.ym(j);
           if (j == cfg->ny - 1) bb = -C.yp(j);
-          if (k == 0) cc = -C.zm(k);
-          if (k == cfg->nz - 1) cc = -C.zp(k);
+          if (k == 0 && !g.pz) cc = -C.zm(k);
+          if (k == cfg->nz - 1 && !g.pz) cc = -C.zp(k);
           const double dj = C.xm(i) + C.ym(j) + C.zm(k) + C.xp(i) + C.yp(j) + C.zp(k) + aa + bb + cc;
           jp[((size_t)i * cfg->ny + j) * cfg->nz + k] = 1.0 / dj;
         }
@@ -1291,8 +1319,9 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.lgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.lgx * g.lgy)));
   int nblk3 = g.lgx * g.lgy * g.lgz;
   // vectorised FP32 kernels: quads of four k cells per thread when nz % 4 == 0
-  // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows)
-  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML) {
+  // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows, and
+  // so does periodic z, whose wrapped neighbours the quad and bulk-copy kernels do not read)
+  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML && !g.pz) {
     const int nq = cfg->nz / 4;
     g.vbx = 1;
     while (g.vbx < nq && g.vbx < 32) g.vbx *= 2;
@@ -1631,7 +1660,8 @@ int cfdgb_op_bc_main(cfdgb_ctx *c, double *u, double *v, double *w, double *p) {
   const size_t n = c->npad;
   double **o = c->op;
   TRY(h2d(c, o[0], u, n)); TRY(h2d(c, o[1], v, n)); TRY(h2d(c, o[2], w, n)); TRY(h2d(c, o[6], p, n));
-  launch_bc(c->stream, c->g, o[0], o[1], o[2], o[6], nullptr, nullptr, nullptr, 1);
+  launch_bc(c->stream, c->g, o[0], o[1], o[2], o[6], nullptr, nullptr, nullptr, 1, nullptr, 0, c->part, c->ss,
+            c->nblk);
   TRY(d2h(c, u, o[0], n)); TRY(d2h(c, v, o[1], n)); TRY(d2h(c, w, o[2], n)); TRY(d2h(c, p, o[6], n));
   return sync(c);
 }
@@ -1872,11 +1902,13 @@ int cfdgb_set_inlet(cfdgb_ctx *c, const double *u_in) {
   drop_step_graph(c);  // the ghost fill's inlet pointer is part of a step graph
   if (!u_in) {
     c->inlet = nullptr;
+    c->g.uconv = inlet_mean(c, nullptr);
     return 0;
   }
   const size_t n = (size_t)c->cfg.ny * c->cfg.nz;
   if (!c->inlet_buf) TRY(dalloc(c, &c->inlet_buf, n));
   c->inlet = c->inlet_buf;
+  c->g.uconv = inlet_mean(c, u_in);  // the convective outflow's velocity
   TRY(h2d(c, c->inlet, u_in, n));
   return sync(c);
 }
@@ -1959,6 +1991,9 @@ int cfdgb_forward(cfdgb_ctx *c, const cfdgb_objective *obj, double *J) {
     return fail(CFDGB_EINVAL, "the adjoint needs a fixed dt (CFDGB_DT_FIXED)");
   if (c->cfg.time_order > 1)  // its transposed step is the Euler step's
     return fail(CFDGB_EINVAL, "the adjoint is implemented for the Euler step (time_order 1)");
+  if (c->g.pz || c->g.outflow)  // its transposed ghost fill is the reference's table
+    return fail(CFDGB_EINVAL, "the adjoint is implemented for the reference's boundary rows (no periodic z or "
+                              "convective outflow)");
   if (obj->nsteps < 1 || obj->first < 1 || obj->last < obj->first || obj->last > obj->nsteps || obj->ckpt_every < 1)
     return fail(CFDGB_EINVAL, "bad objective window");
   if (!c->have_fields || c->loop != 0) return fail(CFDGB_ESTATE, "cfdgb_init_fields must come right before");

@@ -49,6 +49,13 @@ struct Geo {
   // MIXED on the stretched grid: the same rows rounded to FP32 (the FP32 sweeps' operator)
   const float *cof32[2];
   int walls;  // a cfdgb_walls value (the boundary table's y-wall rows)
+  // periodic z (cfdgb_config.bc_z): z ghosts wrap, the top w face nz-3 is an unknown (face 1
+  // its image), every Poisson row keeps both z terms and rows k = 0, nzc-1 couple
+  int pz;
+  // convective outflow (cfdgb_config.outflow) and its convective velocity: the
+  // area-weighted mean inlet u
+  int outflow;
+  double uconv;
   // per-index reciprocals RN(1/D), RN(1/Ds) of the metrics (padded lengths) for div_by, and
   // the DFIB face-fraction factors (Ds * 0.5) / D of updateUandF.hpp, each one IEEE division
   const double *rDx, *rDy, *rDz, *rDxs, *rDys, *rDzs, *hfx, *hfy, *hfz;
@@ -137,6 +144,18 @@ struct Stencil {
 };
 
 __device__ __forceinline__ int axis_class(int a, int n) { return a == 0 ? 0 : (a == n - 1 ? 2 : 1); }
+// the class of a row: periodic z has no first or last cell along z
+__device__ __forceinline__ int row_class(const Geo &g, int ic, int jc, int kc) {
+  return axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + (g.pz ? 1 : axis_class(kc, g.nzc));
+}
+// compact rows of the z neighbours: across the ends of a periodic z the wrapped cell;
+// -1 where a Neumann row has none
+__device__ __forceinline__ long long z_minus(const Geo &g, int kc, long long row) {
+  return kc > 0 ? row - 1 : (g.pz ? row + g.nzc - 1 : -1);
+}
+__device__ __forceinline__ long long z_plus(const Geo &g, int kc, long long row) {
+  return kc < g.nzc - 1 ? row + 1 : (g.pz ? row - (g.nzc - 1) : -1);
+}
 
 // Coefficients of row (ic, jc, kc) on a stretched grid, computed from the per-axis factors
 // with the reference's arithmetic: SPE_sparseMatrix.hpp:66-85 (c[1] the j-1 neighbour with
@@ -145,8 +164,8 @@ __device__ __forceinline__ int axis_class(int a, int n) { return a == 0 ? 0 : (a
 __device__ __forceinline__ void nonuni_row(const Geo &g, int jac, int ic, int jc, int kc, long long row,
                                            double (&c)[8]) {
   const double xm = g.fxm[ic], xp = g.fxp[ic], ym = g.fym[jc], yp = g.fyp[jc], zm = g.fzm[kc], zp = g.fzp[kc];
-  const bool i0 = ic == 0, i1 = ic == g.nxc - 1, j0 = jc == 0, j1 = jc == g.nyc - 1, k0 = kc == 0,
-             k1 = kc == g.nzc - 1;
+  const bool i0 = ic == 0, i1 = ic == g.nxc - 1, j0 = jc == 0, j1 = jc == g.nyc - 1, k0 = kc == 0 && !g.pz,
+             k1 = kc == g.nzc - 1 && !g.pz;
   if (!jac) {
     double ijk = xm + ym + zm + xp + yp + zp;
     if (i0) ijk -= xm;
@@ -179,18 +198,20 @@ __device__ __forceinline__ void nonuni_row(const Geo &g, int jac, int ic, int jc
 }
 
 // y = (A x)[row] for compact row with compact coordinates (ic,jc,kc); bounds on the
-// coordinates, terms accumulated in SPE column order.
+// coordinates, terms accumulated in SPE column order; pz: periodic z (the z terms wrap)
 template <typename T>
 __device__ __forceinline__ T stencil_row(const Stencil<T> &st, const T *__restrict__ x, long long row,
-                                         int ic, int jc, int kc, int nxc, int nyc, int nzc) {
+                                         int ic, int jc, int kc, int nxc, int nyc, int nzc, bool pz = false) {
   const long long nyz = (long long)nyc * nzc;
-  const T *c = st.c[axis_class(ic, nxc) * 9 + axis_class(jc, nyc) * 3 + axis_class(kc, nzc)];
+  const T *c = st.c[axis_class(ic, nxc) * 9 + axis_class(jc, nyc) * 3 + (pz ? 1 : axis_class(kc, nzc))];
   T sum = T(0);
   if (ic > 0) sum += c[0] * x[row - nyz];
   if (jc > 0) sum += c[1] * x[row - nzc];
   if (kc > 0) sum += c[2] * x[row - 1];
+  else if (pz) sum += c[2] * x[row + nzc - 1];
   sum += c[3] * x[row];
   if (kc < nzc - 1) sum += c[4] * x[row + 1];
+  else if (pz) sum += c[4] * x[row - (nzc - 1)];
   if (jc < nyc - 1) sum += c[5] * x[row + nzc];
   if (ic < nxc - 1) sum += c[6] * x[row + nyz];
   return sum;
@@ -199,15 +220,16 @@ __device__ __forceinline__ T stencil_row(const Stencil<T> &st, const T *__restri
 // the same on any grid (the class table on a uniform one)
 __device__ __forceinline__ double stencil_row_g(const Geo &g, const Stencil<double> &st, const double *__restrict__ x,
                                                 long long row, int ic, int jc, int kc) {
-  if (!g.nonuni) return stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc);
+  if (!g.nonuni) return stencil_row<double>(st, x, row, ic, jc, kc, g.nxc, g.nyc, g.nzc, g.pz != 0);
   const double *__restrict__ c = g.cof[st.jac] + row;
   const long long n = g.ncell, nyz = (long long)g.nyc * g.nzc;
+  const long long zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
   double sum = 0.0;
   if (ic > 0) sum += c[0] * x[row - nyz];
   if (jc > 0) sum += c[n] * x[row - g.nzc];
-  if (kc > 0) sum += c[2 * n] * x[row - 1];
+  if (zm >= 0) sum += c[2 * n] * x[zm];
   sum += c[3 * n] * x[row];
-  if (kc < g.nzc - 1) sum += c[4 * n] * x[row + 1];
+  if (zp >= 0) sum += c[4 * n] * x[zp];
   if (jc < g.nyc - 1) sum += c[5 * n] * x[row + g.nzc];
   if (ic < g.nxc - 1) sum += c[6 * n] * x[row + nyz];
   return sum;
@@ -216,7 +238,7 @@ __device__ __forceinline__ double stencil_row_g(const Geo &g, const Stencil<doub
 __device__ __forceinline__ double row_jp(const Geo &g, const Stencil<double> &st, int ic, int jc, int kc,
                                          long long row) {
   if (g.nonuni) return g.jpv[row];
-  return st.c[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)][7];
+  return st.c[row_class(g, ic, jc, kc)][7];
 }
 
 // the unscaled diagonal of a row (class table, or column 3 of the stored SPE rows): maps a
@@ -224,7 +246,7 @@ __device__ __forceinline__ double row_jp(const Geo &g, const Stencil<double> &st
 __device__ __forceinline__ double row_diag(const Geo &g, const Stencil<double> &st, int ic, int jc, int kc,
                                            long long row) {
   if (g.nonuni) return g.cof[0][3 * g.ncell + row];
-  return st.dg[axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc)];
+  return st.dg[row_class(g, ic, jc, kc)];
 }
 
 __device__ __forceinline__ void row_cijk(long long row, int nyc, int nzc, int &ic, int &jc, int &kc) {
@@ -280,10 +302,11 @@ struct StepScal {
   double dt, dt_next, time;
   double urun[6];
   double dt_step;  // dt of the last step (set with time at its end)
+  double oflux;    // convective outflow: the outlet correction (net boundary flux / outlet area)
   int hist;        // Adams-Bashforth: increments stored by the steps since init (at most 2)
   int hslot;       // Adams-Bashforth order 3: the history slot that holds the last increment
   int nan_flag, pad;
-  unsigned cnt[8];
+  unsigned cnt[10];
 };
 
 // What the step kernels need beside their fields: where dt lives (device memory, so an

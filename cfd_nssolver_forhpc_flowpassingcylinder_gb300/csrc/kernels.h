@@ -44,9 +44,13 @@ void launch_update_uf_fast(cudaStream_t s, int nblk, const Geo &g, double dt, co
                            double lz, const double *eta, const double *p, const double *us, const double *vs,
                            const double *ws, double *u3, double *v3, double *w3, const double *ui, const double *vi,
                            const double *wi, double *part, StepScal *ss);
-// inlet: nyc*nzc inlet u values (NULL: the reference's constant Dir[0][0] = 1)
+// inlet: nyc*nzc inlet u values (NULL: the reference's constant Dir[0][0] = 1).
+// Convective outflow (g.outflow): conv = 1 in a time step (the outlet advances from the
+// last step's values in us, vs, ws, with the step's dt in ss->dt_step), 0 at init; the
+// flux reduction uses part (nblk blocks at most) and ss.
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
-               double *vs, double *ws, int do_main, const double *inlet = nullptr);
+               double *vs, double *ws, int do_main, const double *inlet = nullptr, int conv = 0,
+               double *part = nullptr, StepScal *ss = nullptr, int nblk = 1);
 void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
                 double R, double *eta);
 

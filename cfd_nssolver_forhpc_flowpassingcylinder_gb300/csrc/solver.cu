@@ -32,9 +32,7 @@ namespace cfdgb {
 
 #define ROW(g) ((((long long)ic * (g).nyc + jc) * (g).nzc) + kc)
 
-__device__ __forceinline__ int cls_of(const Geo &g, int ic, int jc, int kc) {
-  return axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3 + axis_class(kc, g.nzc);
-}
+__device__ __forceinline__ int cls_of(const Geo &g, int ic, int jc, int kc) { return row_class(g, ic, jc, kc); }
 
 // y = (A f)(row) where f(q) is evaluated on demand at the stencil points
 template <typename T, class F>
@@ -44,27 +42,28 @@ __device__ __forceinline__ T stencil_apply(const Geo &g, const Stencil<T> &st, i
   if constexpr (sizeof(T) == sizeof(double)) {
     if (g.nonuni) {  // stretched grid (FP64 solvers only): the rows stored per context
       const double *__restrict__ cs = g.cof[st.jac] + row;
-      const long long n = g.ncell;
+      const long long n = g.ncell, zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
       T sum = T(0);
       if (ic > 0) sum += cs[0] * f(row - nyz);
       if (jc > 0) sum += cs[n] * f(row - g.nzc);
-      if (kc > 0) sum += cs[2 * n] * f(row - 1);
+      if (zm >= 0) sum += cs[2 * n] * f(zm);
       center = f(row);
       sum += cs[3 * n] * center;
-      if (kc < g.nzc - 1) sum += cs[4 * n] * f(row + 1);
+      if (zp >= 0) sum += cs[4 * n] * f(zp);
       if (jc < g.nyc - 1) sum += cs[5 * n] * f(row + g.nzc);
       if (ic < g.nxc - 1) sum += cs[6 * n] * f(row + nyz);
       return sum;
     }
   }
   const T *c = st.c[cls_of(g, ic, jc, kc)];
+  const long long zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
   T sum = T(0);
   if (ic > 0) sum += c[0] * f(row - nyz);
   if (jc > 0) sum += c[1] * f(row - g.nzc);
-  if (kc > 0) sum += c[2] * f(row - 1);
+  if (zm >= 0) sum += c[2] * f(zm);
   center = f(row);
   sum += c[3] * center;
-  if (kc < g.nzc - 1) sum += c[4] * f(row + 1);
+  if (zp >= 0) sum += c[4] * f(zp);
   if (jc < g.nyc - 1) sum += c[5] * f(row + g.nzc);
   if (ic < g.nxc - 1) sum += c[6] * f(row + nyz);
   return sum;
@@ -80,6 +79,7 @@ template <class F>
 __device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<float> &st, int ic, int jc, int kc,
                                                     long long row, F &&f, float &center) {
   const long long nyz = (long long)g.nyc * g.nzc;
+  const long long zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
   const float fc = f(row);
   center = fc;
   float sum = 0.0f;
@@ -88,8 +88,8 @@ __device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<
     const long long n = g.ncell;
     if (ic > 0) sum = fmaf(cs[0], f(row - nyz) - fc, sum);
     if (jc > 0) sum = fmaf(cs[n], f(row - g.nzc) - fc, sum);
-    if (kc > 0) sum = fmaf(cs[2 * n], f(row - 1) - fc, sum);
-    if (kc < g.nzc - 1) sum = fmaf(cs[4 * n], f(row + 1) - fc, sum);
+    if (zm >= 0) sum = fmaf(cs[2 * n], f(zm) - fc, sum);
+    if (zp >= 0) sum = fmaf(cs[4 * n], f(zp) - fc, sum);
     if (jc < g.nyc - 1) sum = fmaf(cs[5 * n], f(row + g.nzc) - fc, sum);
     if (ic < g.nxc - 1) sum = fmaf(cs[6 * n], f(row + nyz) - fc, sum);
     return sum;
@@ -97,8 +97,8 @@ __device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<
   const float *c = st.c[cls_of(g, ic, jc, kc)];
   if (ic > 0) sum = fmaf(c[0], f(row - nyz) - fc, sum);
   if (jc > 0) sum = fmaf(c[1], f(row - g.nzc) - fc, sum);
-  if (kc > 0) sum = fmaf(c[2], f(row - 1) - fc, sum);
-  if (kc < g.nzc - 1) sum = fmaf(c[4], f(row + 1) - fc, sum);
+  if (zm >= 0) sum = fmaf(c[2], f(zm) - fc, sum);
+  if (zp >= 0) sum = fmaf(c[4], f(zp) - fc, sum);
   if (jc < g.nyc - 1) sum = fmaf(c[5], f(row + g.nzc) - fc, sum);
   if (ic < g.nxc - 1) sum = fmaf(c[6], f(row + nyz) - fc, sum);
   return sum;
@@ -1656,7 +1656,8 @@ __global__ void __launch_bounds__(kBlock) k_rhs_subtract(Geo g, Stencil<double> 
 
 // ---- red-black SOR (FP64) on the exact Neumann rows ----
 // One colour per launch: cells with (i+j+k) even, then odd, so each half-sweep updates
-// cells whose neighbours all have the other colour (no race, order independent).
+// cells whose neighbours all have the other colour (no race, order independent; periodic z
+// needs an even nzc for the cells across the wrap to differ in colour).
 __global__ void __launch_bounds__(kBlock) k_rbsor(Geo g, Stencil<double> st, const double *__restrict__ b,
                                                    double *__restrict__ x, double omega, int color) {
   const long long nyz = (long long)g.nyc * g.nzc;
@@ -1667,8 +1668,9 @@ __global__ void __launch_bounds__(kBlock) k_rbsor(Geo g, Stencil<double> st, con
     double off = 0.0;
     if (ic > 0) off += c[0] * x[row - nyz];
     if (jc > 0) off += c[1] * x[row - g.nzc];
-    if (kc > 0) off += c[2] * x[row - 1];
-    if (kc < g.nzc - 1) off += c[4] * x[row + 1];
+    const long long zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
+    if (zm >= 0) off += c[2] * x[zm];
+    if (zp >= 0) off += c[4] * x[zp];
     if (jc < g.nyc - 1) off += c[5] * x[row + g.nzc];
     if (ic < g.nxc - 1) off += c[6] * x[row + nyz];
     const double xn = (b[row] - off) * c[7];  // c[7] = 1/diag (no division in the sweep)

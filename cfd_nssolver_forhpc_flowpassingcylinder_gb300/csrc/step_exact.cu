@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_convdiff_exact(Geo g, double dt_a
       ccfl += oys(r, j);
       cfl.comp(1, r);
     }
-    if (k < g.nz - 3) {  // w
+    if (k < g.nz - 3 + g.pz) {  // w (periodic z: the top face too)
       const double IT = oz(Dzs[k] * 0.5, k);
       const double wc = w[ic], wzp = w[zp], wzm = w[zm];
       const double Wp = 0.5 * (wzp + wc);
@@ -261,9 +261,11 @@ __global__ void __launch_bounds__(kBlock) k_rhs_exact(Geo g, double dt_arg, cons
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
+    // periodic z: the bottom face of the first cell is the top face nz-3
+    const long long zb = (g.pz && k == 2) ? ic + g.nzc - 1 : ic - 1;
     const double div = div_by(us[ic] - us[ic - g.sx], g.Dx[i], g.rDx[i], two) +
                        div_by(vs[ic] - vs[ic - g.sy], g.Dy[j], g.rDy[j], two) +
-                       div_by(ws[ic] - ws[ic - 1], g.Dz[k], g.rDz[k], two);
+                       div_by(ws[ic] - ws[zb], g.Dz[k], g.rDz[k], two);
     if (jacobi) {
       b[row] = -row_jp(g, st, i - 2, j - 2, k - 2, row) * ddt * div;
     } else {
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(kBlock) k_cfl(Geo g, double dt, const double *
       c += div_by(vs[ic], g.Dys[j], g.rDys[j], two);
       cfl.comp(1, vs[ic]);
     }
-    if (k < g.nz - 3) {
+    if (k < g.nz - 3 + g.pz) {
       c += div_by(ws[ic], g.Dzs[k], g.rDzs[k], two);
       cfl.comp(2, ws[ic]);
     }
@@ -415,8 +417,8 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
     } else if (vi) {
       v3[ic] = vi[ic];
     }
-    if (k < g.nz - 3) {
-      const long long icP = ic + 1;
+    if (k < g.nz - 3 + g.pz) {  // periodic z: the top face, its upper cell the first one
+      const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
       const double T2w = ws[ic] - div_by(dt * (p[icP] - p[ic]), g.Dzs[k], g.rDzs[k], two);
       const double e = ec + (eta[icP] - ec) * g.hfz[k];
       const double nw3 = ec * wS + (1.0 - e) * T2w;
@@ -443,11 +445,83 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_exact(
 // (updateBC.hpp:6-108), whose cells no later phase touches.  bc: Dir/Num table
 // (FLOWpassing.hpp:6-40, BcTable).  inlet: optional per-(j,k) inlet velocity taking the
 // place of Dir[0][0] (all 1.0 reproduces the reference).
+// Two options that are not in the reference: a convective outflow in place of face 1's
+// rows (k_outflow_flux first, then k_bc_x), and periodic z in place of faces 4 and 5.
+
+// Convective outflow at the x+ face: d(phi)/dt + Uc d(phi)/dx = 0 for the outlet u face and
+// the v, w ghost cells beyond it, implicit upwind in time.  In a step (conv) the outlet u
+// before the flux correction is (u_b + cu u_(nx-4)) / (1 + cu), u_b the last step's value
+// (the copy in us, which no kernel of the step writes), cu = Uc dt / Dx[nx-3]; at init the
+// zero-gradient value u_(nx-4).  The ghosts: (phi_g + cv phi_(nx-3)) / (1 + cv), cv =
+// Uc dt / Dxs[nx-3], or phi_(nx-3) at init.
+__device__ __forceinline__ double outlet_u(const Geo &g, const double *u, const double *us, double cu, int j,
+                                           int k) {
+  const double un = u[pidx(g, g.nx - 4, j, k)];
+  return us ? (us[pidx(g, g.nx - 3, j, k)] + cu * un) / (1.0 + cu) : un;
+}
+__device__ __forceinline__ double outlet_ghost(const Geo &g, const double *f, const double *fs, double cv, int j,
+                                               int k) {
+  const double fn = f[pidx(g, g.nx - 3, j, k)];
+  return fs ? (fs[pidx(g, g.nx - 2, j, k)] + cv * fn) / (1.0 + cv) : fn;
+}
+// cu, cv of a step: dt is the step's (set by the velocity correction's step_end)
+__device__ __forceinline__ void outlet_coeffs(const Geo &g, const StepScal *ss, bool conv, double &cu,
+                                              double &cv) {
+  cu = cv = 0.0;
+  if (!conv) return;
+  const double dt = ss->dt_step;
+  cu = g.uconv * dt / g.Dx[g.nx - 3];
+  cv = g.uconv * dt / g.Dxs[g.nx - 3];
+}
+
+// The outlet correction: the net flux through the boundary with the outlet faces at
+// outlet_u -- inlet u faces, outlet faces, the y-wall v faces and (not periodic) the z-wall
+// w faces at the values the ghost fill gives them, each times its face area -- divided by
+// the outlet's area, into ss->oflux.  One grid-stride pass over the three face sets.
+__global__ void __launch_bounds__(kBlock) k_outflow_flux(Geo g, BcTable t, const double *__restrict__ inlet,
+                                                         const double *__restrict__ u, const double *__restrict__ v,
+                                                         const double *__restrict__ w, const double *__restrict__ us,
+                                                         double *part, StepScal *ss) {
+  double cu, cv;
+  outlet_coeffs(g, ss, us != nullptr, cu, cv);
+  const long long nx_ = g.nyc * (long long)g.nzc, ny_ = g.nxc * (long long)g.nzc,
+                  nz_ = g.pz ? 0 : g.nxc * (long long)g.nyc;
+  double acc[2] = {0.0, 0.0};  // flux, outlet area
+  for (long long q = blockIdx.x * (long long)kBlock + threadIdx.x; q < nx_ + ny_ + nz_;
+       q += (long long)gridDim.x * kBlock) {
+    if (q < nx_) {
+      const int j = (int)(q / g.nzc) + 2, k = (int)(q % g.nzc) + 2;
+      const double a = g.Dy[j] * g.Dz[k];
+      const double uin = (inlet ? inlet[q] : t.dir[0][0]) + t.num[0][0] * u[pidx(g, 2, j, k)];
+      acc[0] += (uin - outlet_u(g, u, us, cu, j, k)) * a;
+      acc[1] += a;
+    } else if (q < nx_ + ny_) {
+      const long long r = q - nx_;
+      const int i = (int)(r / g.nzc) + 2, k = (int)(r % g.nzc) + 2;
+      const double vb = t.dir[2][1] + t.num[2][1] * v[pidx(g, i, 2, k)];
+      const double vt = t.dir[3][1] + t.num[3][1] * v[pidx(g, i, g.ny - 4, k)];
+      acc[0] += (vb - vt) * (g.Dx[i] * g.Dz[k]);
+    } else {
+      const long long r = q - nx_ - ny_;
+      const int i = (int)(r / g.nyc) + 2, j = (int)(r % g.nyc) + 2;
+      const double wb = t.dir[4][2] + t.num[4][2] * w[pidx(g, i, j, 2)];
+      const double wt = t.dir[5][2] + t.num[5][2] * w[pidx(g, i, j, g.nz - 4)];
+      acc[0] += (wb - wt) * (g.Dx[i] * g.Dy[j]);
+    }
+  }
+  double out[2];
+  if (grid_sum<2>(acc, part, &ss->cnt[8], out) && threadIdx.x == 0) ss->oflux = out[0] / out[1];
+}
 
 __global__ void __launch_bounds__(kBlock) k_bc_x(Geo g, BcTable t, const double *__restrict__ inlet, double *u,
                                                  double *v, double *w, double *p, double *us, double *vs, double *ws,
-                                                 int do_main) {
+                                                 int do_main, int conv, const StepScal *ss) {
   const int nyc = g.nyc, nzc = g.nzc, nx = g.nx;
+  double cu = 0.0, cv = 0.0, corr = 0.0;
+  if (do_main && g.outflow) {
+    outlet_coeffs(g, ss, conv != 0, cu, cv);
+    corr = ss->oflux;
+  }
   for (int q = blockIdx.x * kBlock + threadIdx.x; q < nyc * nzc; q += gridDim.x * kBlock) {
     const int j = q / nzc + 2, k = q % nzc + 2;
     auto I = [&](int i) { return pidx(g, i, j, k); };
@@ -456,9 +530,19 @@ __global__ void __launch_bounds__(kBlock) k_bc_x(Geo g, BcTable t, const double 
       u[I(1)] = u[I(0)] = din + t.num[0][0] * u[I(2)];
       v[I(1)] = v[I(0)] = t.dir[0][1] * 2. + (2.0 * t.num[0][1] - 1.0) * v[I(2)];
       w[I(1)] = w[I(0)] = t.dir[0][2] * 2. + (2.0 * t.num[0][2] - 1.0) * w[I(2)];
-      u[I(nx - 1)] = u[I(nx - 2)] = u[I(nx - 3)] = t.dir[1][0] + t.num[1][0] * u[I(nx - 4)];
-      v[I(nx - 1)] = v[I(nx - 2)] = t.dir[1][1] * 2. + (2.0 * t.num[1][1] - 1.0) * v[I(nx - 3)];
-      w[I(nx - 1)] = w[I(nx - 2)] = t.dir[1][2] * 2. + (2.0 * t.num[1][2] - 1.0) * w[I(nx - 3)];
+      if (g.outflow) {
+        const double *os = conv ? us : nullptr;
+        const double ub = outlet_u(g, u, os, cu, j, k) + corr;
+        const double vg = outlet_ghost(g, v, conv ? vs : nullptr, cv, j, k);
+        const double wg = outlet_ghost(g, w, conv ? ws : nullptr, cv, j, k);
+        u[I(nx - 1)] = u[I(nx - 2)] = u[I(nx - 3)] = ub;
+        v[I(nx - 1)] = v[I(nx - 2)] = vg;
+        w[I(nx - 1)] = w[I(nx - 2)] = wg;
+      } else {
+        u[I(nx - 1)] = u[I(nx - 2)] = u[I(nx - 3)] = t.dir[1][0] + t.num[1][0] * u[I(nx - 4)];
+        v[I(nx - 1)] = v[I(nx - 2)] = t.dir[1][1] * 2. + (2.0 * t.num[1][1] - 1.0) * v[I(nx - 3)];
+        w[I(nx - 1)] = w[I(nx - 2)] = t.dir[1][2] * 2. + (2.0 * t.num[1][2] - 1.0) * w[I(nx - 3)];
+      }
       if (p) {
         p[I(1)] = p[I(0)] = p[I(2)];
         p[I(nx - 2)] = p[I(nx - 1)] = p[I(nx - 3)];
@@ -500,6 +584,38 @@ __global__ void __launch_bounds__(kBlock) k_bc_y(Geo g, BcTable t, double *u, do
       const int jv[5] = {0, 1, ny - 3, ny - 2, ny - 1};
 #pragma unroll
       for (int a = 0; a < 5; ++a) vs[J(jv[a])] = v[J(jv[a])];
+    }
+  }
+}
+
+// periodic z: the two ghost layers on each side take the images nzc cells away (w's face
+// 1 is the image of the top face nz-3), over the whole padded (i, j) plane so that the
+// edges and corners next to the z ghosts are periodic too; the copy into T1 as the
+// reference's (interior (i, j), the z ghosts and w's face nz-3)
+__global__ void __launch_bounds__(kBlock) k_bc_zp(Geo g, double *u, double *v, double *w, double *p, double *us,
+                                                  double *vs, double *ws, int do_main) {
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < nx * ny; q += gridDim.x * kBlock) {
+    const int i = q / ny, j = q % ny;
+    const long long base = pidx(g, i, j, 0);
+    if (do_main) {
+      double *f[4] = {u, v, w, p};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        if (!f[a]) continue;
+        f[a][base + 0] = f[a][base + nz - 4];
+        f[a][base + 1] = f[a][base + nz - 3];
+        f[a][base + nz - 2] = f[a][base + 2];
+        f[a][base + nz - 1] = f[a][base + 3];
+      }
+    }
+    if (us && i >= 2 && i < nx - 2 && j >= 2 && j < ny - 2) {
+      const int ku[4] = {0, 1, nz - 2, nz - 1};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) { us[base + ku[a]] = u[base + ku[a]]; vs[base + ku[a]] = v[base + ku[a]]; }
+      const int kw[5] = {0, 1, nz - 3, nz - 2, nz - 1};
+#pragma unroll
+      for (int a = 0; a < 5; ++a) ws[base + kw[a]] = w[base + kw[a]];
     }
   }
 }
@@ -641,12 +757,22 @@ void launch_update_uf_exact(cudaStream_t s, int nblk, const Geo &g, double dt, c
                                             wi, part, ss);
 }
 void launch_bc(cudaStream_t s, const Geo &g, double *u, double *v, double *w, double *p, double *us,
-               double *vs, double *ws, int do_main, const double *inlet) {
+               double *vs, double *ws, int do_main, const double *inlet, int conv, double *part, StepScal *ss,
+               int nblk) {
   const BcTable t = flowpassing_table(g.walls);
   auto blocks = [](long long n) { return (int)((n + kBlock - 1) / kBlock < 1024 ? (n + kBlock - 1) / kBlock : 1024); };
-  k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, inlet, u, v, w, p, us, vs, ws, do_main);
+  conv = conv && us;  // the last step's outlet values live in T1
+  if (do_main && g.outflow) {
+    const long long nf = (long long)g.nyc * g.nzc + (long long)g.nxc * g.nzc + (g.pz ? 0LL : (long long)g.nxc * g.nyc);
+    const int fb = (int)std::min<long long>((nf + kBlock - 1) / kBlock, (long long)nblk);
+    k_outflow_flux<<<fb, kBlock, 0, s>>>(g, t, inlet, u, v, w, conv ? us : nullptr, part, ss);
+  }
+  k_bc_x<<<blocks((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, t, inlet, u, v, w, p, us, vs, ws, do_main, conv, ss);
   k_bc_y<<<blocks((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
-  k_bc_z<<<blocks((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
+  if (g.pz)
+    k_bc_zp<<<blocks((long long)g.nx * g.ny), kBlock, 0, s>>>(g, u, v, w, p, us, vs, ws, do_main);
+  else
+    k_bc_z<<<blocks((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, t, u, v, w, p, us, vs, ws, do_main);
 }
 void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const double *Y, double cx, double cy,
                 double R, double *eta) {

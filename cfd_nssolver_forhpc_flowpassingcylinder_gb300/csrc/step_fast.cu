@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, dou
       c += r * tb(tab, fa.L, 1, T_IDS, j);
       cfl.comp(1, r);
     }
-    if (k < g.nz - 3) {
+    if (k < g.nz - 3 + g.pz) {  // periodic z: the top face too
       const float d = component<2>(g, fa, tab, vel, ic, I);
       ws[ic] = w[ic] + f2d_int(d);
       const float r = w32[ic] + d;
@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     } else if (vi) {
       v3[ic] = vi[ic];
     }
-    if (k < g.nz - 3) {
-      const long long icP = ic + 1;
+    if (k < g.nz - 3 + g.pz) {  // periodic z: the top face, its upper cell the first one
+      const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
       const double T2 = fma(-(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
       const double en = eta[icP];
       w3[ic] = (bc || nonzero(en)) ? (1.0 - fma(en - ec, g.hfz[k], ec)) * T2 : T2;
@@ -262,8 +262,9 @@ __global__ void __launch_bounds__(kBlock) k_rhs_fast(Geo g, double dt_arg, const
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
+    const long long zb = (g.pz && k == 2) ? ic + g.nzc - 1 : ic - 1;  // periodic z: face nz-3
     const double div = fma(us[ic] - us[ic - g.sx], g.rDx[i],
-                           fma(vs[ic] - vs[ic - g.sy], g.rDy[j], (ws[ic] - ws[ic - 1]) * g.rDz[k]));
+                           fma(vs[ic] - vs[ic - g.sy], g.rDy[j], (ws[ic] - ws[zb]) * g.rDz[k]));
     b[row] = (jacobi ? row_jp(g, st, i - 2, j - 2, k - 2, row) * ndt : ndt) * div;
   }
 }

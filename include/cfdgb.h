@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CFDGB_ABI_VERSION 8
+#define CFDGB_ABI_VERSION 9
 
 typedef enum cfdgb_status {
   CFDGB_OK = 0,
@@ -68,6 +68,30 @@ typedef enum cfdgb_walls {
   CFDGB_WALLS_FREE_SLIP = 1       /* the rows left commented out there (:14-21): v = 0 on the
                                      walls, u and w zero-gradient */
 } cfdgb_walls;
+
+/* The z faces.  The reference has only its zero-gradient rows (FLOWpassing.hpp:30-39); its
+   periodic Poisson terms (inc/matrix/PressureMatrix.hpp:83-101) are unused. */
+typedef enum cfdgb_bc_z {
+  CFDGB_Z_ZERO_GRADIENT = 0,  /* the reference's rows (default) */
+  CFDGB_Z_PERIODIC = 1        /* periodic in z (not in the reference): the ghost layers wrap over
+                                 the whole padded (i, j) plane, w has nz unknown faces (face 0 is
+                                 the image of the top face), every Poisson row keeps both z terms
+                                 and rows k = 0 and nz-1 couple.  No multigrid preconditioner;
+                                 RBSOR needs nz even; no adjoint */
+} cfdgb_bc_z;
+
+/* The x+ (outlet) face. */
+typedef enum cfdgb_outflow {
+  CFDGB_OUTFLOW_ZERO_GRADIENT = 0,  /* the reference's row (FLOWpassing.hpp:23-29), default */
+  CFDGB_OUTFLOW_CONVECTIVE = 1      /* convective outflow (not in the reference): d(phi)/dt +
+                                       Uc d(phi)/dx = 0 for the outlet u face and the v, w ghost
+                                       cells beyond it, implicit upwind in time, Uc the area-
+                                       weighted mean inlet u; then a uniform correction of the
+                                       outlet u that makes the net flux through the domain's
+                                       boundary zero, so the Neumann Poisson problem is
+                                       consistent.  At init the outlet starts from the
+                                       zero-gradient values (corrected).  No adjoint */
+} cfdgb_outflow;
 
 /* The reference's compile-time convection switch (inc/0_General.hpp:114-118). */
 typedef enum cfdgb_scheme {
@@ -154,6 +178,8 @@ typedef struct cfdgb_config {
                                 before reading it.  The order builds up from 1 over the first
                                 steps after init (cfdgb_set_dt restarts order 3); MIXED then
                                 uses the FP64 convection-diffusion kernel; no adjoint */
+  int bc_z;                  /* a cfdgb_bc_z value; default zero-gradient */
+  int outflow;               /* a cfdgb_outflow value; default zero-gradient */
 } cfdgb_config;
 
 typedef struct cfdgb_step_stats {

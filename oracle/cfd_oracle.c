@@ -326,10 +326,11 @@ void og_convection_diffusion_ab(const og_grid *g, double dt, double nu0, const d
              ((v[zp] - v[ic]) / g->Dzs[k] - (v[ic] - v[zm]) / g->Dzs[k - 1]) / g->Dz[k]);
         vs[ic] = ab_value(ab, 1, ic, v[ic], convection, difussion);
       }
-  /* w: :359-438 */
+  /* w: :359-438; periodic z adds the top face nz-3 (the image of face 1) as an unknown */
+  const int kw_end = nz - GC - 1 + (g->periodic_z != 0);
   for (int i = GC; i < nx - GC; ++i)
     for (int j = GC; j < ny - GC; ++j)
-      for (int k = GC; k < nz - GC - 1; ++k) {
+      for (int k = GC; k < kw_end; ++k) {
         const long ic = IC(g, i, j, k);
         const long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz,
                    zp = ic + sz;
@@ -371,13 +372,98 @@ static void num_table(const og_grid *g, double N[6][3]) {
   if (g->walls == OG_WALLS_FREE_SLIP) N[2][1] = N[3][1] = 0.0;
 }
 
+double og_inlet_mean(const og_grid *g, const double *inlet) {
+  double q = 0.0, a = 0.0;
+  for (int j = GC; j < g->ny - GC; ++j)
+    for (int k = GC; k < g->nz - GC; ++k) {
+      const double da = g->Dy[j] * g->Dz[k];
+      q += (inlet ? inlet[(j - GC) * g->nzc + (k - GC)] : kDir[0][0]) * da;
+      a += da;
+    }
+  return q / a;
+}
+
+/* convective outflow: the outlet u face before the flux correction -- at init (us NULL) the
+ * zero-gradient value, in a step (u_b + cu u_(nx-4)) / (1 + cu) with u_b the last step's
+ * outlet value (kept in us by og_bc_copy) and cu = Uc dt / Dx of the last cell */
+static double outlet_u(const og_grid *g, const double *u, const double *us, double cu, int j, int k) {
+  const int nx = g->nx;
+  if (!us) return u[IC(g, nx - 4, j, k)];
+  return (us[IC(g, nx - 3, j, k)] + cu * u[IC(g, nx - 4, j, k)]) / (1.0 + cu);
+}
+/* the v or w ghost cell beyond the outlet, the same way from the last cell (cv = Uc dt / Dxs) */
+static double outlet_ghost(const og_grid *g, const double *f, const double *fs, double cv, int j, int k) {
+  const int nx = g->nx;
+  if (!fs) return f[IC(g, nx - 3, j, k)];
+  return (fs[IC(g, nx - 2, j, k)] + cv * f[IC(g, nx - 3, j, k)]) / (1.0 + cv);
+}
+
+/* the uniform correction of the outlet u that makes the net boundary flux zero: inlet u
+ * face, outlet faces (outlet_u), and, with the values the ghost fill gives them, the y-wall
+ * v faces and (not periodic) the z-wall w faces, each times its face area; divided by the
+ * outlet's area */
+static double outflow_correction(const og_grid *g, const double kN[6][3], const double *u, const double *v,
+                                 const double *w, const double *inlet, const double *us, double cu) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  double F = 0.0, A = 0.0;
+  for (int j = GC; j < ny - GC; ++j)
+    for (int k = GC; k < nz - GC; ++k) {
+      const double a = g->Dy[j] * g->Dz[k];
+      const double uin = (inlet ? inlet[(j - GC) * g->nzc + (k - GC)] : kDir[0][0]) + kN[0][0] * u[IC(g, 2, j, k)];
+      F += (uin - outlet_u(g, u, us, cu, j, k)) * a;
+      A += a;
+    }
+  for (int i = GC; i < nx - GC; ++i)
+    for (int k = GC; k < nz - GC; ++k) {
+      const double vb = kDir[2][1] + kN[2][1] * v[IC(g, i, 2, k)];
+      const double vt = kDir[3][1] + kN[3][1] * v[IC(g, i, ny - 4, k)];
+      F += (vb - vt) * (g->Dx[i] * g->Dz[k]);
+    }
+  if (!g->periodic_z)
+    for (int i = GC; i < nx - GC; ++i)
+      for (int j = GC; j < ny - GC; ++j) {
+        const double wb = kDir[4][2] + kN[4][2] * w[IC(g, i, j, 2)];
+        const double wt = kDir[5][2] + kN[5][2] * w[IC(g, i, j, nz - 4)];
+        F += (wb - wt) * (g->Dx[i] * g->Dy[j]);
+      }
+  return F / A;
+}
+
+/* periodic z: the two ghost layers on each side take the images of the cells nzc away
+ * (for w, face 1 is the image of the top face nz-3), over every (i, j) of the padded plane
+ * so that edges and corners next to the z ghosts are periodic too */
+static void periodic_z_fill(const og_grid *g, double *f) {
+  const int nz = g->nz;
+  for (int i = 0; i < g->nx; ++i)
+    for (int j = 0; j < g->ny; ++j) {
+      const long b = IC(g, i, j, 0);
+      f[b + 0] = f[b + nz - 4];
+      f[b + 1] = f[b + nz - 3];
+      f[b + nz - 2] = f[b + 2];
+      f[b + nz - 1] = f[b + 3];
+    }
+}
+
 /* inc/BoundaryCondition/Boundary_Condition.hpp:37-176 (BC_staggered_main), in the
- * order one thread executes it: faces 0..5 for u,v,w, then pressure. */
-static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet) {
+ * order one thread executes it: faces 0..5 for u,v,w, then pressure.  With the grid's
+ * options (not in the reference): the convective outflow in place of face 1's rows, and
+ * periodic z in place of faces 4 and 5 and of the pressure's z rows. */
+static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet,
+                       const double *us, const double *vs, const double *ws, double dt) {
   double kN[6][3];
   num_table(g, kN);
   const int nx = g->nx, ny = g->ny, nz = g->nz;
   double *vel[3] = {u, v, w};
+  const int conv = g->outflow == OG_OUTFLOW_CONVECTIVE;
+  double cu = 0.0, cv = 0.0, corr = 0.0;
+  if (conv) {
+    if (us) {
+      const double uc = og_inlet_mean(g, inlet);
+      cu = uc * dt / g->Dx[nx - 3];
+      cv = uc * dt / g->Dxs[nx - 3];
+    }
+    corr = outflow_correction(g, (const double(*)[3])kN, u, v, w, inlet, us, cu);
+  }
   for (int j = GC; j < ny - GC; ++j)
     for (int k = GC; k < nz - GC; ++k) { /* BC_0 */
       const double din = inlet ? inlet[(j - GC) * g->nzc + (k - GC)] : kDir[0][0];
@@ -387,7 +473,14 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
       w[IC(g, 1, j, k)] = w[IC(g, 0, j, k)] =
           kDir[0][2] * 2. + (2.0 * kN[0][2] - 1.0) * w[IC(g, 2, j, k)];
     }
-  for (int j = GC; j < ny - GC; ++j)
+  for (int j = GC; j < ny - GC && conv; ++j)
+    for (int k = GC; k < nz - GC; ++k) { /* convective outflow */
+      u[IC(g, nx - 1, j, k)] = u[IC(g, nx - 2, j, k)] = u[IC(g, nx - 3, j, k)] =
+          outlet_u(g, u, us, cu, j, k) + corr;
+      v[IC(g, nx - 1, j, k)] = v[IC(g, nx - 2, j, k)] = outlet_ghost(g, v, vs, cv, j, k);
+      w[IC(g, nx - 1, j, k)] = w[IC(g, nx - 2, j, k)] = outlet_ghost(g, w, ws, cv, j, k);
+    }
+  for (int j = GC; j < ny - GC && !conv; ++j)
     for (int k = GC; k < nz - GC; ++k) { /* BC_1 */
       u[IC(g, nx - 1, j, k)] = u[IC(g, nx - 2, j, k)] = u[IC(g, nx - 3, j, k)] =
           kDir[1][0] + kN[1][0] * u[IC(g, nx - 4, j, k)];
@@ -413,7 +506,9 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
       w[IC(g, i, ny - 1, k)] = w[IC(g, i, ny - 2, k)] =
           kDir[3][2] * 2. + (2.0 * kN[3][2] - 1.0) * w[IC(g, i, ny - 3, k)];
     }
-  for (int i = GC; i < nx - GC; ++i)
+  if (g->periodic_z)
+    for (int c = 0; c < 3; ++c) periodic_z_fill(g, vel[c]);
+  for (int i = GC; i < nx - GC && !g->periodic_z; ++i)
     for (int j = GC; j < ny - GC; ++j) { /* BC_4 */
       u[IC(g, i, j, 1)] = u[IC(g, i, j, 0)] =
           kDir[4][0] * 2. + (2.0 * kN[4][0] - 1.0) * u[IC(g, i, j, 2)];
@@ -421,7 +516,7 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
           kDir[4][1] * 2. + (2.0 * kN[4][1] - 1.0) * v[IC(g, i, j, 2)];
       w[IC(g, i, j, 1)] = w[IC(g, i, j, 0)] = kDir[4][2] + kN[4][2] * w[IC(g, i, j, 2)];
     }
-  for (int i = GC; i < nx - GC; ++i)
+  for (int i = GC; i < nx - GC && !g->periodic_z; ++i)
     for (int j = GC; j < ny - GC; ++j) { /* BC_5 */
       w[IC(g, i, j, nz - 1)] = w[IC(g, i, j, nz - 2)] = w[IC(g, i, j, nz - 3)] =
           kDir[5][2] + kN[5][2] * w[IC(g, i, j, nz - 4)];
@@ -430,7 +525,6 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
       v[IC(g, i, j, nz - 1)] = v[IC(g, i, j, nz - 2)] =
           kDir[5][1] * 2. + (2.0 * kN[5][1] - 1.0) * v[IC(g, i, j, nz - 3)];
     }
-  (void)vel;
   /* pressure: homogeneous Neumann, :148-172 */
   for (int j = GC; j < ny - GC; ++j)
     for (int k = GC; k < nz - GC; ++k) {
@@ -442,6 +536,10 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
       p[IC(g, i, 1, k)] = p[IC(g, i, 0, k)] = p[IC(g, i, 2, k)];
       p[IC(g, i, ny - 2, k)] = p[IC(g, i, ny - 1, k)] = p[IC(g, i, ny - 3, k)];
     }
+  if (g->periodic_z) {
+    periodic_z_fill(g, p);
+    return;
+  }
   for (int i = GC; i < nx - GC; ++i)
     for (int j = GC; j < ny - GC; ++j) {
       p[IC(g, i, j, 1)] = p[IC(g, i, j, 0)] = p[IC(g, i, j, 2)];
@@ -450,7 +548,12 @@ static void bc_main_in(const og_grid *g, double *u, double *v, double *w, double
 }
 
 void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p) {
-  bc_main_in(g, u, v, w, p, NULL);
+  bc_main_in(g, u, v, w, p, NULL, NULL, NULL, NULL, 0.0);
+}
+
+void og_bc_main_ex(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet,
+                   const double *us, const double *vs, const double *ws, double dt) {
+  bc_main_in(g, u, v, w, p, inlet, us, vs, ws, dt);
 }
 
 /* inc/BoundaryCondition/updateBC.hpp:6-108 (BC_staggered_copy) */
@@ -492,8 +595,10 @@ void og_rhs(const og_grid *g, double dt, const double *us, const double *vs,
     for (int j = GC; j < g->ny - GC; ++j)
       for (int k = GC; k < g->nz - GC; ++k, ++row) {
         const long ic = IC(g, i, j, k);
+        /* periodic z: the bottom face of the first cell is the top face nz-3 */
+        const long zb = (g->periodic_z && k == GC) ? IC(g, i, j, g->nz - 3) : ic - 1;
         const double div = (us[ic] - us[ic - sx]) / g->Dx[i] + (vs[ic] - vs[ic - sy]) / g->Dy[j] +
-                           (ws[ic] - ws[ic - 1]) / g->Dz[k];
+                           (ws[ic] - ws[zb]) / g->Dz[k];
         if (jp)
           b[row] = -jp[row] * ddt * div;
         else
@@ -520,8 +625,8 @@ void og_jacobi_scale(const og_grid *g, double *jp) {
         if (i == g->nxc - 1) aa = -cxp(g, i);
         if (j == 0) bb = -cym(g, j);
         if (j == g->nyc - 1) bb = -cyp(g, j);
-        if (k == 0) cc = -czm(g, k);
-        if (k == g->nzc - 1) cc = -czp(g, k);
+        if (k == 0 && !g->periodic_z) cc = -czm(g, k);
+        if (k == g->nzc - 1 && !g->periodic_z) cc = -czp(g, k);
         const double ijk = cxm(g, i) + cym(g, j) + czm(g, k) + cxp(g, i) + cyp(g, j) +
                            czp(g, k) + aa + bb + cc;
         jp[row] = 1.0 / ijk;
@@ -529,9 +634,10 @@ void og_jacobi_scale(const og_grid *g, double *jp) {
 }
 
 /* inc/matrix/SPE_sparseMatrix.hpp:42-88 (setupPressure), including the swapped
- * y-coefficients of :79/:83 (identical on a uniform grid) */
+ * y-coefficients of :79/:83 (identical on a uniform grid).  Periodic z: every row keeps
+ * both z terms, the k = 0 and nzc-1 rows' outer ones coupling them (og_spe_multiply). */
 void og_spe_setup(const og_grid *g, double *val) {
-  const int nx = g->nxc, ny = g->nyc, nz = g->nzc;
+  const int nx = g->nxc, ny = g->nyc, nz = g->nzc, pz = g->periodic_z != 0;
   memset(val, 0, sizeof(double) * 7 * (size_t)og_cells(g));
   for (int i = 0; i < nx; ++i)
     for (int j = 0; j < ny; ++j)
@@ -542,13 +648,13 @@ void og_spe_setup(const og_grid *g, double *val) {
         if (i == nx - 1) ijk -= cxp(g, i);
         if (j == 0) ijk -= cym(g, j);
         if (j == ny - 1) ijk -= cyp(g, j);
-        if (k == 0) ijk -= czm(g, k);
-        if (k == nz - 1) ijk -= czp(g, k);
+        if (k == 0 && !pz) ijk -= czm(g, k);
+        if (k == nz - 1 && !pz) ijk -= czp(g, k);
         if (i != 0) val[ic7 + 0] = -cxm(g, i);
         if (j != 0) val[ic7 + 1] = -cyp(g, j);
-        if (k != 0) val[ic7 + 2] = -czm(g, k);
+        if (k != 0 || pz) val[ic7 + 2] = -czm(g, k);
         val[ic7 + 3] = ijk;
-        if (k != nz - 1) val[ic7 + 4] = -czp(g, k);
+        if (k != nz - 1 || pz) val[ic7 + 4] = -czp(g, k);
         if (j != ny - 1) val[ic7 + 5] = -cym(g, j);
         if (i != nx - 1) val[ic7 + 6] = -cxp(g, i);
       }
@@ -557,6 +663,21 @@ void og_spe_setup(const og_grid *g, double *val) {
 /* inc/matrix/SPE_sparseMatrix.hpp:92-108 (multiply_omp; bounds tested on the row index) */
 void og_spe_multiply(const og_grid *g, const double *val, const double *x, double *r) {
   const long n = og_cells(g), nz = g->nzc, nynz = (long)g->nyc * g->nzc;
+  if (g->periodic_z) { /* z neighbours by the cell's k, wrapping at the ends */
+    for (long i = 0; i < n; ++i) {
+      const long k = i % nz, i7 = i * 7;
+      double sum = 0.0;
+      if (i - nynz >= 0) sum += val[i7 + 0] * x[i - nynz];
+      if (i - nz >= 0) sum += val[i7 + 1] * x[i - nz];
+      sum += val[i7 + 2] * x[k == 0 ? i + nz - 1 : i - 1];
+      sum += val[i7 + 3] * x[i];
+      sum += val[i7 + 4] * x[k == nz - 1 ? i - (nz - 1) : i + 1];
+      if (i + nz < n) sum += val[i7 + 5] * x[i + nz];
+      if (i + nynz < n) sum += val[i7 + 6] * x[i + nynz];
+      r[i] = sum;
+    }
+    return;
+  }
   for (long i = 0; i < n; ++i) {
     double sum = 0.0;
     const long i7 = i * 7;
@@ -574,7 +695,7 @@ void og_spe_multiply(const og_grid *g, const double *val, const double *x, doubl
 /* Jacobi-scaled CSR rows of inc/grid/structureGrid.hpp:557-654 multiplied as in
  * inc/matrix/CSR_sparseMatrix.hpp:232-243; entries in the builder's order. */
 void og_csr_multiply(const og_grid *g, const double *jp, const double *x, double *r) {
-  const int nx = g->nxc, ny = g->nyc, nz = g->nzc;
+  const int nx = g->nxc, ny = g->nyc, nz = g->nzc, pz = g->periodic_z != 0;
   const long nyz = (long)ny * nz;
   long row = 0;
   for (int i = 0; i < nx; ++i)
@@ -585,8 +706,8 @@ void og_csr_multiply(const og_grid *g, const double *jp, const double *x, double
         if (i == nx - 1) aa = -cxp(g, i);
         if (j == 0) bb = -cym(g, j);
         if (j == ny - 1) bb = -cyp(g, j);
-        if (k == 0) cc = -czm(g, k);
-        if (k == nz - 1) cc = -czp(g, k);
+        if (k == 0 && !pz) cc = -czm(g, k);
+        if (k == nz - 1 && !pz) cc = -czp(g, k);
         const double ijk = cxm(g, i) + cym(g, j) + czm(g, k) + cxp(g, i) + cyp(g, j) +
                            czp(g, k) + aa + bb + cc;
         const double s = jp[row];
@@ -594,8 +715,10 @@ void og_csr_multiply(const og_grid *g, const double *jp, const double *x, double
         if (i != 0) acc += (-cxm(g, i) * s) * x[row - nyz];
         if (j != 0) acc += (-cym(g, j) * s) * x[row - nz];
         if (k != 0) acc += (-czm(g, k) * s) * x[row - 1];
+        else if (pz) acc += (-czm(g, k) * s) * x[row + nz - 1];
         acc += (ijk * s) * x[row];
         if (k != nz - 1) acc += (-czp(g, k) * s) * x[row + 1];
+        else if (pz) acc += (-czp(g, k) * s) * x[row - (nz - 1)];
         if (j != ny - 1) acc += (-cyp(g, j) * s) * x[row + nz];
         if (i != nx - 1) acc += (-cxp(g, i) * s) * x[row + nyz];
         r[row] = acc;
@@ -718,9 +841,10 @@ int og_sor(const og_grid *g, double dt, double omega, double tol, int itmax,
                             Dx[i] * Dy[j] / g->Dzs[k] + Dx[i] * Dy[j] / g->Dzs[k - 1];
         c[7] = -1.0 / coef;
         const long ic = IC(g, i, j, k);
+        const long zb = (g->periodic_z && k == GC) ? IC(g, i, j, g->nz - 3) : ic - 1;
         const double mChange = (us[ic] - us[ic - sx]) * Dy[j] * Dz[k] +
                                (vs[ic] - vs[ic - sy]) * Dx[i] * Dz[k] +
-                               (ws[ic] - ws[ic - 1]) * Dx[i] * Dy[j];
+                               (ws[ic] - ws[zb]) * Dx[i] * Dy[j];
         c[6] = mChange * rdt;
         norm_rhs += (mChange * rdt) * (mChange * rdt);
       }
@@ -735,8 +859,11 @@ int og_sor(const og_grid *g, double dt, double omega, double tol, int itmax,
         for (int k = GC; k < g->nz - GC; ++k, ++row) {
           const long ic = IC(g, i, j, k);
           const double *c = cf + 8 * row;
+          /* periodic z: the neighbours across the ends are the wrapped cells */
+          const long zm = (g->periodic_z && k == GC) ? ic + g->nzc - 1 : ic - 1;
+          const long zp = (g->periodic_z && k == g->nz - 3) ? ic - (g->nzc - 1) : ic + 1;
           const double pNEW = (-p[ic + sx] * c[0] - p[ic - sx] * c[1] - p[ic + sy] * c[2] -
-                               p[ic - sy] * c[3] - p[ic + 1] * c[4] - p[ic - 1] * c[5] + c[6]) *
+                               p[ic - sy] * c[3] - p[zp] * c[4] - p[zm] * c[5] + c[6]) *
                               c[7];
           const double pChange = fabs(pNEW - p[ic]);
           p[ic] += omega * (pNEW - p[ic]);
@@ -782,10 +909,12 @@ void og_update_uf(const og_grid *g, double dt, const double *eta, const double *
         v3[ic] = eta[ic] * vS + (1.0 - e) * T2v;
         f[ic + tot] = (v3[ic] - T2v) / dt;
       }
+  /* periodic z: the top face nz-3 too, its upper cell the first one (k = 2) */
+  const int pz = g->periodic_z != 0;
   for (int i = GC; i < g->nx - GC; ++i)
     for (int j = GC; j < g->ny - GC; ++j)
-      for (int k = GC; k < g->nz - GC - 1; ++k) {
-        const long ic = IC(g, i, j, k), icP = ic + 1;
+      for (int k = GC; k < g->nz - GC - 1 + pz; ++k) {
+        const long ic = IC(g, i, j, k), icP = (pz && k == g->nz - 3) ? ic - (g->nzc - 1) : ic + 1;
         const double T2w = ws[ic] - dt * (p[icP] - p[ic]) / g->Dzs[k];
         const double e = eta[ic] + (eta[icP] - eta[ic]) * ((g->Dzs[k] * 0.5) / g->Dz[k]);
         w3[ic] = eta[ic] * wS + (1.0 - e) * T2w;
@@ -861,7 +990,7 @@ void og_cfl(const og_grid *g, double dt, const double *us, const double *vs, con
   for (int a = 0; a < 3; ++a)
     for (int i = GC; i < g->nx - GC - (a == 0); ++i)
       for (int j = GC; j < g->ny - GC - (a == 1); ++j)
-        for (int k = GC; k < g->nz - GC - (a == 2); ++k) {
+        for (int k = GC; k < g->nz - GC - (a == 2 && !g->periodic_z); ++k) {
           const long ic = IC(g, i, j, k);
           const long r = ((long)(i - GC) * g->nyc + (j - GC)) * g->nzc + (k - GC);
           const int d = a == 0 ? i : (a == 1 ? j : k);
@@ -1032,7 +1161,7 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
   memcpy(us, u, sizeof(double) * tot); memcpy(u3, u, sizeof(double) * tot);
   memcpy(vs, v, sizeof(double) * tot); memcpy(v3, v, sizeof(double) * tot);
   memcpy(ws, w, sizeof(double) * tot); memcpy(w3, w, sizeof(double) * tot);
-  bc_main_in(g, u, v, w, p, inlet);
+  bc_main_in(g, u, v, w, p, inlet, NULL, NULL, NULL, dt);
   og_bc_copy(g, u, v, w, us, vs, ws);
   if (solver == 0 || solver == 1) og_bicg_init(&bs, g, solver, tol);
   double *val7 = solver == 3 ? dalloc(7 * n) : NULL;
@@ -1090,7 +1219,7 @@ int og_run_ex(const og_grid *g, int steps, double Re, double dt, double tol, int
     memcpy(u, u3, sizeof(double) * tot); /* copyVel */
     memcpy(v, v3, sizeof(double) * tot);
     memcpy(w, w3, sizeof(double) * tot);
-    bc_main_in(g, u, v, w, p, inlet);
+    bc_main_in(g, u, v, w, p, inlet, us, vs, ws, dt);
     og_bc_copy(g, u, v, w, us, vs, ws);
     if (stats) {
       stats[4 * (s - 1) + 0] = iters;

@@ -29,7 +29,19 @@ typedef struct og_grid {
   int walls;                   /* y walls: OG_WALLS_* (0 after init: zero-gradient) */
   int time_order;              /* og_run_ex's time stepping: 0 or 1 explicit Euler (the
                                   reference), 2 or 3 Adams-Bashforth (not in the reference) */
+  int periodic_z;              /* != 0: periodic in z (not in the reference, whose periodic
+                                  Poisson terms, inc/matrix/PressureMatrix.hpp:83-101, are
+                                  unused): ghosts wrap, w has nzc unknown faces (face nzc is
+                                  the image of face 0), Poisson rows k = 0 and nzc-1 couple */
+  int outflow;                 /* OG_OUTFLOW_*: the x+ face (0 after init: zero-gradient) */
 } og_grid;
+
+/* the x+ (outlet) face: the reference's zero-gradient row (FLOWpassing.hpp:23-29), or a
+ * convective outflow (not in the reference): d(phi)/dt + Uc d(phi)/dx = 0 for the outlet
+ * u face and the v, w ghost cells beyond it, implicit upwind in time, Uc the mean inlet
+ * velocity, followed by a uniform correction of the outlet u that makes the net flux
+ * through the domain boundary zero (the Neumann Poisson problem then is consistent) */
+enum { OG_OUTFLOW_ZERO_GRADIENT = 0, OG_OUTFLOW_CONVECTIVE = 1 };
 
 /* Adams-Bashforth history of og_convection_diffusion_ab (no counterpart in the reference,
  * whose 2nd/3rd-order branch does not compile): order 1 is the reference's Euler step;
@@ -73,6 +85,14 @@ void og_convection_diffusion_ab(const og_grid *g, double dt, double nu, const do
 /* SmagorinskyModel (inc/source/SmagorinskyModel.hpp:30): compact eddy viscosity of T0 */
 void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *nut);
 void og_bc_main(const og_grid *g, double *u, double *v, double *w, double *p);
+/* the ghost fill of a time step with the grid's outflow and z options: us, vs, ws (may be
+ * NULL: the fill at init, where the outlet starts from the zero-gradient values) hold the
+ * last step's outlet values (the copies og_bc_copy made), dt the step, inlet the inlet u
+ * per (j, k) or NULL (1.0) */
+void og_bc_main_ex(const og_grid *g, double *u, double *v, double *w, double *p, const double *inlet,
+                   const double *us, const double *vs, const double *ws, double dt);
+/* the convective velocity of the outflow: the area-weighted mean of the inlet u */
+double og_inlet_mean(const og_grid *g, const double *inlet);
 void og_bc_copy(const og_grid *g, const double *u, const double *v, const double *w,
                 double *us, double *vs, double *ws);
 void og_rhs(const og_grid *g, double dt, const double *us, const double *vs,

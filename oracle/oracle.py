@@ -41,13 +41,17 @@ class _Grid(C.Structure):
                 ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)] + [
         (n, C.POINTER(C.c_double)) for n in
         ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")] + [
-        ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int), ("time_order", C.c_int)]
+        ("scheme", C.c_int), ("les", C.c_int), ("walls", C.c_int), ("time_order", C.c_int),
+        ("periodic_z", C.c_int), ("outflow", C.c_int)]
 
 
 # the reference's compile-time convection switch (0_General.hpp:114-118)
 SCHEMES = {"quick": 0, "lud": 1, "ud": 2}
 # the y-wall rows of its boundary table (FLOWpassing.hpp: active, and the commented-out ones)
 WALLS = {"zero_gradient": 0, "free_slip": 1}
+# the z faces and the outlet (neither option is in the reference)
+BC_Z = {"zero_gradient": 0, "periodic": 1}
+OUTFLOWS = {"zero_gradient": 0, "convective": 1}
 
 
 class _Bicg(C.Structure):
@@ -101,12 +105,14 @@ class Grid:
     """Uniform MAC grid of the reference (structureGrid.hpp:336), cylinder at (cx, ly/2)."""
 
     def __init__(self, nxc, nyc, nzc, lx, ly, lz, cx, radius=0.5, gridder="uniform", scheme="quick",
-                 les=False, walls="zero_gradient", time_order=1):
+                 les=False, walls="zero_gradient", time_order=1, bc_z="zero_gradient", outflow="zero_gradient"):
         """gridder: "uniform" (init_uniform) or "sml" (the reference's default stretched
         non_uniform-SML grid); scheme: "quick", "lud" or "ud" (the convection switch);
         les: the Smagorinsky eddy viscosity in run(); walls: the y walls' boundary rows;
         time_order: run()'s time stepping, 1 the reference's Euler step, 2 or 3
-        Adams-Bashforth (constant dt; not in the reference)."""
+        Adams-Bashforth (constant dt; not in the reference); bc_z: "periodic" wraps z;
+        outflow: "convective" (with the flux correction) in place of the zero-gradient
+        outlet."""
         self._g = _Grid()
         init = {"uniform": lib().og_grid_init_uniform, "sml": lib().og_grid_init_sml}[gridder]
         rc = init(C.byref(self._g), nxc, nyc, nzc, lx, ly, lz, cx, ly / 2.0, radius)
@@ -116,6 +122,8 @@ class Grid:
         self._g.les = 1 if les else 0
         self._g.walls = WALLS[walls]
         self._g.time_order = int(time_order)
+        self._g.periodic_z = BC_Z[bc_z]
+        self._g.outflow = OUTFLOWS[outflow]
         self.shape = (nxc + 4, nyc + 4, nzc + 4)
         self.cells = nxc * nyc * nzc
 
@@ -162,6 +170,23 @@ def smagorinsky(g: Grid, u, v, w):
 
 def bc_main(g, u, v, w, p):
     lib().og_bc_main(g.ptr, u, v, w, p)
+
+
+def bc_main_ex(g, u, v, w, p, inlet=None, us=None, vs=None, ws=None, dt=0.0):
+    """The ghost fill of a time step (us, vs, ws: the last step's copies; None at init)."""
+    L = lib()
+    vp = C.c_void_p
+    L.og_bc_main_ex.argtypes = [vp] + [_dp] * 4 + [vp] * 4 + [C.c_double]
+    keep = [None if a is None else _c(a) for a in (inlet, us, vs, ws)]
+    L.og_bc_main_ex(g.ptr, u, v, w, p, *[None if a is None else a.ctypes.data_as(vp) for a in keep], dt)
+
+
+def inlet_mean(g, inlet=None):
+    L = lib()
+    L.og_inlet_mean.argtypes = [C.c_void_p, C.c_void_p]
+    L.og_inlet_mean.restype = C.c_double
+    a = None if inlet is None else _c(inlet).reshape(-1)
+    return L.og_inlet_mean(g.ptr, None if a is None else a.ctypes.data_as(C.c_void_p))
 
 
 def bc_copy(g, u, v, w, us, vs, ws):
@@ -291,14 +316,17 @@ SOLVERS = {"spe": 0, "bicgstab": 0, "jacobi": 1, "csr": 1, "sor": 2, "cg": 3}
 
 
 def run(g: Grid, steps, Re, dt, tol, solver="spe", omega=1.8, seed=0, amp=0.0, eta_in=None,
-        inlet=None, project=False):
+        inlet=None, project=False, init=None):
     """Whole run (src/RUN_CPU.cpp:257-436 order); returns dict of final fields + stats.
     eta_in (padded) replaces the cylinder's solid fraction, inlet (ny, nz) the inlet u;
-    project removes the Poisson rhs's mean before each BiCGSTAB solve (not in the reference)."""
+    project removes the Poisson rhs's mean before each BiCGSTAB solve (not in the reference);
+    init: padded (u, v, w) to start from in place of u = 1, v = w = 0 (+ the perturbation)."""
     u = np.ones(g.shape)
     v = g.zeros()
     w = g.zeros()
-    if amp:
+    if init is not None:
+        u, v, w = (np.array(a, dtype=np.float64, copy=True) for a in init)
+    elif amp:
         perturb(g, u, v, w, seed, amp)
     p = g.zeros()
     eta = g.zeros()

@@ -42,15 +42,17 @@ def test_defaults_are_the_reference_case(lib):
     assert (cfg.lx, cfg.ly, cfg.lz, cfg.cx, cfg.cy, cfg.radius) == (24.0, 12.0, 1.0, 6.0, 6.0, 0.5)
     assert (cfg.Re, cfg.dt, cfg.maxit) == (100.0, 0.005, 5000)
     assert cfg.solver == cg.BICGSTAB and cfg.precision == cg.FP64
-    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 8
+    assert lib.cfdgb_abi_version() == cg.ABI_VERSION == 9
     assert cfg.scheme == cg.QUICK and cfg.les == 0 and cfg.walls == cg.WALLS_ZERO_GRADIENT
     assert cfg.dt_mode == cg.DT_FIXED and cfg.cfl_target == 0.5 and cfg.dt_max == 0.0 and cfg.time_order == 1
+    assert cfg.bc_z == cg.Z_ZERO_GRADIENT and cfg.outflow == cg.OUTFLOW_ZERO_GRADIENT
 
 
 @pytest.mark.parametrize("field,value", [("nx", 2), ("dt", 0.0), ("Re", -1.0), ("solver", 7),
                                          ("precision", 3), ("tol", 0.0), ("maxit", 0), ("scheme", 3),
                                          ("scheme", -1), ("les", 2), ("walls", 2), ("dt_mode", 3),
-                                         ("dt_mode", -1), ("time_order", 4)])
+                                         ("dt_mode", -1), ("time_order", 4), ("bc_z", 2), ("bc_z", -1),
+                                         ("outflow", 2), ("outflow", -1)])
 def test_invalid_config_is_rejected_before_any_device_work(lib, field, value):
     cfg = cg.default_config()
     setattr(cfg, field, value)
@@ -78,6 +80,18 @@ def test_mixed_sor_combination_rejected(lib):
     cfg = cg.default_config(solver="rbsor", precision="mixed")
     h = C.c_void_p()
     assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
+
+
+@pytest.mark.parametrize("kw", [dict(precond="multigrid", precision="mixed"), dict(precond="multigrid"),
+                                dict(solver="rbsor", nz=5)])
+def test_periodic_z_limits_rejected(lib, kw):
+    """Periodic z: the V-cycle's coarse levels are Neumann in z, and red-black SOR needs the
+    cells across the wrap to differ in colour (nz even)."""
+    base = dict(nx=32, ny=16, nz=8, lx=8.0, ly=4.0, lz=2.0, cx=2.0, cy=2.0, bc_z="periodic")
+    cfg = cg.default_config(**{**base, **kw})
+    h = C.c_void_p()
+    assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
+    assert h.value is None
 
 
 def test_null_arguments_are_errors(lib):

@@ -1,0 +1,210 @@
+"""Periodic z and the convective outflow (the boundary set of the plain FP64 cylinder
+case: uniform inflow, convective outflow, free-slip y walls, periodic z, seeded
+perturbation) on the GPU against the oracle's restatement of them.
+
+Neither option is in the reference (its table is zero-gradient on every face but the
+inlet, inc/BoundaryCondition/FLOWpassing.hpp:6-40); tests/test_oracle_boundary_set.py pins
+the oracle's versions by their defining properties.  Here: the step kernels and the
+operators bit for bit (the FP64 kernels keep the oracle's operation order), the ghost fill
+to 1e-15 (its flux correction sums on the GPU in another order), whole runs within 1e-10 at
+tol 1e-12 through the step graphs, the FP32+FP64-refined paths within 1e-8 of FP64, and
+every solve consistent (the corrected net flux is zero, so each one reaches 1e-12).
+
+The grid has nz = 8 so that, without periodic z, the MIXED sweeps would run their quad
+and bulk-copy kernels: periodic z must select the scalar ones, whose z neighbours wrap."""
+import numpy as np
+import pytest
+
+import cfd_nssolver_forhpc_flowpassingcylinder_gb300 as cg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SET = dict(walls="free_slip", bc_z="periodic", outflow="convective")
+CASE = dict(nx=24, ny=12, nz=8, lx=6.0, ly=3.0, lz=2.0, cx=1.5, cy=1.5, Re=100.0, dt=0.01)
+SEED, AMP = 11, 1e-3
+CORE = (slice(2, -2),) * 3
+
+
+def ogrid(**kw):
+    return O.Grid(24, 12, 8, 6.0, 3.0, 2.0, 1.5, **{**SET, **kw})
+
+
+def vel_err(f, ref):
+    scale = np.sqrt(sum(np.linalg.norm(ref[k][CORE]) ** 2 for k in "uvw"))
+    return {k: float(np.linalg.norm(f[k][CORE] - ref[k][CORE]) / scale) for k in "uvw"}
+
+
+def p_err(a, b):
+    a, b = a[CORE] - a[CORE].mean(), b[CORE] - b[CORE].mean()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _fields(rng, shape):
+    return (1.0 + 0.1 * rng.standard_normal(shape), 0.1 * rng.standard_normal(shape),
+            0.1 * rng.standard_normal(shape))
+
+
+@pytest.fixture(scope="module")
+def pair():
+    s = cg.Solver(**CASE, **SET)
+    yield ogrid(), s
+    s.close()
+
+
+def test_step_kernels_bit_exact(pair):
+    """Convection-diffusion (the top w face an unknown), the right-hand side (face 1 read
+    as face nz-3), the velocity correction (the top face's upper cell the first one) and the
+    CFL reduction (the top face included), each against the oracle's function."""
+    g, s = pair
+    rng = np.random.default_rng(1)
+    u, v, w = _fields(rng, s.shape)
+    O.bc_main(g, u, v, w, s.zeros())
+    ref = [a.copy() for a in (u, v, w)]
+    O.convection_diffusion(g, CASE["dt"], 1.0 / CASE["Re"], u, v, w, *ref)
+    got = [a.copy() for a in (u, v, w)]
+    s.convection_diffusion(u, v, w, *got)
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
+    for jac in (False, True):
+        jp = O.jacobi_scale(g) if jac else None
+        np.testing.assert_array_equal(s.rhs(*got, jacobi=jac), O.rhs(g, CASE["dt"], *got, jp))
+    np.testing.assert_array_equal(s.cfl(*got), O.cfl(g, CASE["dt"], *got))
+    eta = s.solid_fraction()
+    p = rng.standard_normal(s.shape)
+    o3 = [s.zeros() for _ in range(3)]
+    fo = np.zeros(3 * int(np.prod(s.shape)))
+    O.update_uf(g, CASE["dt"], eta, p, *got, *o3, fo)
+    g3 = [s.zeros() for _ in range(3)]
+    s.update_uf(eta, p, *got, *g3)
+    for a, b in zip(g3, o3):
+        np.testing.assert_array_equal(a[CORE], b[CORE])
+
+
+@pytest.mark.parametrize("grid", ["uniform", "sml"])
+def test_periodic_operators_bit_exact(grid):
+    if grid == "sml":
+        kw = dict(nx=120, ny=110, nz=4, lx=17.0, ly=12.0, lz=3.0, cx=6.5, cy=6.0, grid="sml")
+        g = O.Grid(120, 110, 4, 17.0, 12.0, 3.0, 6.5, gridder="sml", bc_z="periodic")
+    else:
+        kw = {k: CASE[k] for k in ("nx", "ny", "nz", "lx", "ly", "lz", "cx", "cy")}
+        g = ogrid()
+    with cg.Solver(bc_z="periodic", **kw) as s:
+        x = np.random.default_rng(2).standard_normal(s.cells)
+        np.testing.assert_array_equal(s.spmv(x), O.spe_multiply(g, x))
+        np.testing.assert_array_equal(s.spmv(x, jacobi=True), O.csr_multiply(g, x))
+
+
+def test_ghost_fill_matches_oracle(pair):
+    """The fill at init: the outlet from its zero-gradient values plus the flux correction,
+    free-slip walls, periodic z over the whole padded plane (pressure too)."""
+    g, s = pair
+    rng = np.random.default_rng(3)
+    u, v, w = _fields(rng, s.shape)
+    p = rng.standard_normal(s.shape)
+    ref = [a.copy() for a in (u, v, w, p)]
+    O.bc_main(g, *ref)
+    s.bc_main(u, v, w, p)
+    for a, b in zip((u, v, w, p), ref):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-15)
+    for a in (u, v, w, p):
+        assert np.array_equal(a[:, :, 1], a[:, :, -3]) and np.array_equal(a[:, :, -2], a[:, :, 2])
+
+
+@pytest.mark.parametrize("solver,osolver", [("bicgstab", "spe"), ("jacobi", "csr"), ("cg", "cg")])
+def test_run_matches_oracle(solver, osolver):
+    """Eight steps of the boundary set from the seeded perturbation, both sides at 1e-12;
+    the GPU's FP64 steps after the first run as one CUDA graph each."""
+    ref = O.run(ogrid(), 8, CASE["Re"], CASE["dt"], 1e-12, osolver, seed=SEED, amp=AMP)
+    with cg.Solver(solver=solver, tol=1e-12, seed=SEED, amp=AMP, **CASE, **SET) as s:
+        s.init_fields()
+        st = s.step(8)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 8
+    assert all(r.relres < 1e-12 for r in st[1:])
+    for k, e in vel_err(f, ref).items():
+        assert e <= 1e-10, (solver, k, e)
+    assert p_err(f["p"], ref["p"]) <= 1e-10
+    np.testing.assert_allclose([r.cd for r in st], ref["cd"], rtol=1e-10)
+    # the flux correction's fill: the outlet carries what the inlet brings in
+    X, Y, Z = (np.diff(a)[2:-2] for a in ogrid().coords())
+    nx = f["u"].shape[0]
+    q = np.sum((f["u"][1, 2:-2, 2:-2] - f["u"][nx - 3, 2:-2, 2:-2]) * np.outer(Y, Z))
+    assert abs(q) <= 1e-13
+
+
+def test_inlet_profile_sets_the_convective_velocity():
+    """A non-uniform inlet: Uc is its area-weighted mean; three steps against the oracle."""
+    inlet = 1.0 + 0.2 * np.sin(np.linspace(0, np.pi, 12))[:, None] * np.ones((1, 8))
+    ref = O.run(ogrid(), 3, CASE["Re"], CASE["dt"], 1e-12, "spe", seed=SEED, amp=AMP, inlet=inlet)
+    with cg.Solver(tol=1e-12, seed=SEED, amp=AMP, **CASE, **SET) as s:
+        s.set_inlet(inlet)
+        s.init_fields()
+        st = s.step(3)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 3
+    for k, e in vel_err(f, ref).items():
+        assert e <= 1e-10, (k, e)
+    np.testing.assert_allclose([r.cd for r in st], ref["cd"], rtol=1e-10)
+
+
+@pytest.fixture(scope="module")
+def fp64_run():
+    with cg.Solver(tol=1e-12, seed=SEED, amp=AMP, **CASE, **SET) as s:
+        s.init_fields()
+        st = s.step(6)
+        return st, s.get_fields()
+
+
+@pytest.mark.parametrize("kw", [dict(solver="bicgstab"), dict(solver="jacobi"), dict(solver="cg")],
+                         ids=["bicgstab", "jacobi", "cg"])
+def test_mixed_matches_fp64(fp64_run, kw):
+    """MIXED (FP32 sweeps on the scalar kernels, FP64 refinement) at 1e-10 against FP64."""
+    st64, f64 = fp64_run
+    with cg.Solver(precision="mixed", tol=1e-10, seed=SEED, amp=AMP, **kw, **CASE, **SET) as s:
+        s.init_fields()
+        st = s.step(6)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 6
+    assert all(r.relres < 1e-10 for r in st[1:])
+    for k, e in vel_err(f, f64).items():
+        assert e <= 1e-8, (kw, k, e)
+    assert p_err(f["p"], f64["p"]) <= 1e-6
+    np.testing.assert_allclose([r.cd for r in st], [r.cd for r in st64], rtol=1e-8)
+
+
+def test_rbsor_matches_fp64(fp64_run):
+    """Red-black SOR on the periodic operator (nz even: the wrap joins cells of two colours)."""
+    st64, f64 = fp64_run
+    with cg.Solver(solver="rbsor", tol=1e-11, maxit=200000, seed=SEED, amp=AMP, **CASE, **SET) as s:
+        s.init_fields()
+        st = s.step(6)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 6
+    for k, e in vel_err(f, f64).items():
+        assert e <= 1e-8, (k, e)
+    np.testing.assert_allclose([r.cd for r in st], [r.cd for r in st64], rtol=1e-8)
+
+
+def test_adaptive_dt_keeps_the_flux_balanced():
+    """The CFL-target dt changes every step; the outlet's convective coefficient uses each
+    step's own dt and every solve stays consistent."""
+    with cg.Solver(tol=1e-12, seed=SEED, amp=AMP, dt_mode="cfl", cfl_target=0.1, dt_max=0.05, **CASE, **SET) as s:
+        s.init_fields()
+        st = s.step(6)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 6
+    assert all(r.relres < 1e-12 for r in st[1:])
+    assert len({r.dt for r in st}) > 1
+    X, Y, Z = (np.diff(a)[2:-2] for a in ogrid().coords())
+    nx = f["u"].shape[0]
+    assert abs(np.sum((f["u"][1, 2:-2, 2:-2] - f["u"][nx - 3, 2:-2, 2:-2]) * np.outer(Y, Z))) <= 1e-13
+
+
+def test_adjoint_rejects_the_boundary_options():
+    for kw in (dict(bc_z="periodic"), dict(outflow="convective")):
+        with cg.Solver(**CASE, **kw) as s:
+            s.init_fields()
+            with pytest.raises(cg.CfdgbError) as e:
+                s.forward(4, 2, 4, 2)
+            assert e.value.status == cg.EINVAL
