@@ -440,20 +440,19 @@ int validate(const cfdgb_config *c) {
     if ((c->solver != CFDGB_BICGSTAB && c->solver != CFDGB_BICGSTAB_JACOBI) || c->grid != CFDGB_GRID_UNIFORM)
       return fail(CFDGB_EINVAL, "the multigrid preconditioner is for the BiCGSTAB solvers on a uniform grid");
     MgPlan mg;
-    if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, false, &mg))
-      return fail(CFDGB_EINVAL, "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents", c->nx,
-                  c->ny, c->nz, kMgSharedCells);
+    if (!mg_plan(c->nx, c->ny, c->nz, c->lx / c->nx, c->ly / c->ny, c->lz / c->nz, 1, false, &mg,
+                 c->bc_z == CFDGB_Z_PERIODIC))
+      return fail(CFDGB_EINVAL,
+                  "multigrid: %dx%dx%d does not coarsen to %d cells by halving even extents (periodic z: with an "
+                  "even nz on every level)",
+                  c->nx, c->ny, c->nz, kMgSharedCells);
   }
   if (c->bc_z != CFDGB_Z_ZERO_GRADIENT && c->bc_z != CFDGB_Z_PERIODIC)
     return fail(CFDGB_EINVAL, "unknown bc_z %d", c->bc_z);
   if (c->outflow != CFDGB_OUTFLOW_ZERO_GRADIENT && c->outflow != CFDGB_OUTFLOW_CONVECTIVE)
     return fail(CFDGB_EINVAL, "unknown outflow %d", c->outflow);
-  if (c->bc_z == CFDGB_Z_PERIODIC) {
-    if (c->precond == CFDGB_PRECOND_MULTIGRID)  // its coarse levels are Neumann in z
-      return fail(CFDGB_EINVAL, "the multigrid preconditioner is implemented for zero-gradient z faces");
-    if (c->solver == CFDGB_RBSOR && c->nz % 2)  // the cells across the wrap must differ in colour
-      return fail(CFDGB_EINVAL, "red-black SOR with periodic z needs nz even");
-  }
+  if (c->bc_z == CFDGB_Z_PERIODIC && c->solver == CFDGB_RBSOR && c->nz % 2)  // the cells across the wrap
+    return fail(CFDGB_EINVAL, "red-black SOR with periodic z needs nz even");  // must differ in colour
   if (c->dt_mode < CFDGB_DT_FIXED || c->dt_mode > CFDGB_DT_CFL) return fail(CFDGB_EINVAL, "unknown dt_mode %d", c->dt_mode);
   if (c->time_order < 0 || c->time_order > 3) return fail(CFDGB_EINVAL, "time_order must be 1, 2 or 3");
   if (c->time_order == 3 && c->dt_mode != CFDGB_DT_FIXED)
@@ -1389,7 +1388,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   }
   if (cfg->precond == CFDGB_PRECOND_MULTIGRID && cfg->precision == CFDGB_FP64) {  // the FP64 hierarchy
     mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm, false,
-            &c->mg64);
+            &c->mg64, g.pz != 0);
     mg_prepare<double>();
     if ((rc = upload_dense_coarse(c, c->mg64))) return bail(rc);
     if ((rc = dalloc(c, &c->ph64, c->ncell)) || (rc = dalloc(c, &c->sh64, c->ncell))) return bail(rc);
@@ -1402,7 +1401,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   }
   if (cfg->precond == CFDGB_PRECOND_MULTIGRID && cfg->precision == CFDGB_MIXED) {  // levels >= 1, M p, M s
     mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm,
-            !std::getenv("CFDGB_SCALAR_FP32"), &c->mg);
+            !std::getenv("CFDGB_SCALAR_FP32"), &c->mg, g.pz != 0);
     mg_prepare<float>();
     if ((rc = upload_dense_coarse(c, c->mg))) return bail(rc);
     if ((rc = dalloc(c, &c->ph32, c->ncell)) || (rc = dalloc(c, &c->sh32, c->ncell))) return bail(rc);
@@ -1926,7 +1925,7 @@ int dd_copy(cfdgb_ctx *c, double *dst, const double *src, size_t n) {
 int build_adjoint_mg(cfdgb_ctx *c) {
   if (!c->use_mg64) {  // a MIXED context has only the FP32 hierarchy
     const cfdgb_config &cf = c->cfg;
-    mg_plan(cf.nx, cf.ny, cf.nz, cf.lx / cf.nx, cf.ly / cf.ny, cf.lz / cf.nz, c->nsm, false, &c->mg64);
+    mg_plan(cf.nx, cf.ny, cf.nz, cf.lx / cf.nx, cf.ly / cf.ny, cf.lz / cf.nz, c->nsm, false, &c->mg64, c->g.pz != 0);
     mg_prepare<double>();
     TRY(upload_dense_coarse(c, c->mg64));
     for (int l = 1; l < c->mg64.nlev; ++l) {

@@ -145,7 +145,8 @@ void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st,
 // Level 0 is the Poisson grid; each coarser level halves every even extent (cell-centred
 // agglomeration of two cells per halved axis) until at most kMgCoarseCells cells remain
 // or no extent is even.  Operator on every level: the unscaled 7-point Neumann Laplacian
-// of that level's spacing (1/h^2 per axis), the uniform-grid SPE rows rediscretised.
+// of that level's spacing (1/h^2 per axis), the uniform-grid SPE rows rediscretised;
+// periodic in z on every level when the grid is (the z ends coupled, nz even on each).
 constexpr int kMgMaxLevels = 16;
 constexpr int kMgCoarseCells = 64;      // coarsening stops at or below this many cells
 constexpr int kMgSharedCells = 4096;    // largest coarsest level solved in one block
@@ -158,6 +159,7 @@ struct MgLevelT {
   T *x, *b;                // correction and right-hand side (levels >= 1)
   int bx, by, gx, gy, gz;  // launch geometry: bx along k, by along j, gz planes strided over i
   int qgrid;               // blocks of the quad smoother (FP32, nz % 4 == 0), 0: the scalar one
+  int pz;                  // periodic z (every level; nz even or 1 on each)
   // 1/diag of a row by its neighbour counts along x, y, z (each 0..2): idg[9 cx + 3 cy + cz]
   // (0 where a row has no neighbour); the smoother multiplies instead of dividing
   T idg[27];
@@ -173,10 +175,12 @@ struct MgPlanT {
 using MgLevel = MgLevelT<float>;
 using MgPlan = MgPlanT<float>;
 // levels of an nx x ny x nz grid with spacing hx, hy, hz (arrays left null); false when
-// the grid has a single level too large for the one-block coarsest solve.  T: the element
-// type of the hierarchy (float: the MIXED sweeps' preconditioner; double: FP64's)
+// the grid has a single level too large for the one-block coarsest solve, or (pz: periodic
+// z on every level) a level with an odd nz above 1.  T: the element type of the hierarchy
+// (float: the MIXED sweeps' preconditioner; double: FP64's)
 template <typename T>
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg);
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg,
+             bool pz = false);
 // kernels one V-cycle launches
 template <typename T>
 int mg_vcycle_launches(const MgPlanT<T> &mg);

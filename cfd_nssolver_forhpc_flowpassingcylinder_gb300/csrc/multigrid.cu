@@ -6,7 +6,8 @@
 // Cell-centred hierarchy: a coarse cell is the union of 2 cells along each halved axis.
 // Restriction averages the fine residual over a coarse cell's children; prolongation is
 // the cell-centred trilinear interpolation (weights 3/4 and 1/4 per halved axis, the
-// parent's value standing in for a neighbour beyond a Neumann wall); the smoother is
+// parent's value standing in for a neighbour beyond a Neumann wall, the wrapped cell
+// across a periodic z end); the smoother is
 // red-black Gauss-Seidel, one sweep before and one after the coarse correction; the
 // coarsest level (at most kMgSharedCells cells) is solved by red-black sweeps in the
 // shared memory of one block.  The V-cycle is a fixed linear map, as a right
@@ -33,17 +34,23 @@ __device__ __forceinline__ long long lrow(const MgLevelT<T> &L, int i, int j, in
   return ((long long)i * L.ny + j) * L.nz + k;
 }
 
-// diagonal of a Neumann row: the weights of the neighbours that exist
+// z neighbours of a cell: those that exist (Neumann), or both across the wrap (periodic z,
+// none on a level one cell thick, whose wrapped neighbours are the cell itself)
+template <typename T>
+__device__ __forceinline__ int zcount(const MgLevelT<T> &L, int k) {
+  return L.pz ? (L.nz > 1 ? 2 : 0) : (k > 0) + (k < L.nz - 1);
+}
+
+// diagonal of a row: the weights of the neighbours that exist
 template <typename T>
 __device__ __forceinline__ T ldiag(const MgLevelT<T> &L, int i, int j, int k) {
-  return L.wx * (T)((i > 0) + (i < L.nx - 1)) + L.wy * (T)((j > 0) + (j < L.ny - 1)) +
-         L.wz * (T)((k > 0) + (k < L.nz - 1));
+  return L.wx * (T)((i > 0) + (i < L.nx - 1)) + L.wy * (T)((j > 0) + (j < L.ny - 1)) + L.wz * (T)zcount(L, k);
 }
 
 // 1/diag of the row (ldiag's reciprocal, from the level's table)
 template <typename T>
 __device__ __forceinline__ T linv(const MgLevelT<T> &L, int i, int j, int k) {
-  return L.idg[9 * ((i > 0) + (i < L.nx - 1)) + 3 * ((j > 0) + (j < L.ny - 1)) + ((k > 0) + (k < L.nz - 1))];
+  return L.idg[9 * ((i > 0) + (i < L.nx - 1)) + 3 * ((j > 0) + (j < L.ny - 1)) + zcount(L, k)];
 }
 
 // weighted sum of the neighbours' values (minus the off-diagonal part of the row)
@@ -55,8 +62,15 @@ __device__ __forceinline__ T lnb(const MgLevelT<T> &L, const T *x, int i, int j,
   if (i < L.nx - 1) a += x[r + sx];
   if (j > 0) b += x[r - L.nz];
   if (j < L.ny - 1) b += x[r + L.nz];
-  if (k > 0) c += x[r - 1];
-  if (k < L.nz - 1) c += x[r + 1];
+  if (L.pz) {
+    if (L.nz > 1) {
+      c += x[k > 0 ? r - 1 : r + L.nz - 1];
+      c += x[k < L.nz - 1 ? r + 1 : r + 1 - L.nz];
+    }
+  } else {
+    if (k > 0) c += x[r - 1];
+    if (k < L.nz - 1) c += x[r + 1];
+  }
   return L.wx * a + L.wy * b + L.wz * c;
 }
 
@@ -118,7 +132,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
       const float4 yp = jp ? *reinterpret_cast<const float4 *>(x + r + L.nz) : z4;
       const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
       const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
-      const float kl = k0 > 0 ? x[r - 1] : 0.f, kr = k0 + 4 < L.nz ? x[r + 4] : 0.f;
+      // the cells left and right of the quad (periodic z: across the wrap)
+      const float kl = k0 > 0 ? x[r - 1] : (L.pz ? x[r + L.nz - 1] : 0.f);
+      const float kr = k0 + 4 < L.nz ? x[r + 4] : (L.pz ? x[r + 4 - L.nz] : 0.f);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         o[c] = xv[c];
@@ -129,8 +145,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
         if (ip) a += xpv[c];
         if (jm) e += ymv[c];
         if (jp) e += ypv[c];
-        if (k > 0) f += c == 0 ? kl : xv[c - 1];
-        if (k < L.nz - 1) f += c == 3 ? kr : xv[c + 1];
+        if (k > 0 || L.pz) f += c == 0 ? kl : xv[c - 1];
+        if (k < L.nz - 1 || L.pz) f += c == 3 ? kr : xv[c + 1];
         const float bb = bscale ? bv[c] * ldiag(L, (int)i, (int)j, k) : bv[c];
         o[c] = (bb + (L.wx * a + L.wy * e + L.wz * f)) * linv(L, (int)i, (int)j, k);
       }
@@ -162,9 +178,10 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevelT<T> F, MgLevelT<
   }
 }
 
-// the two coarse cells a fine cell interpolates from along one axis, and their weights
+// the two coarse cells a fine cell interpolates from along one axis, and their weights;
+// per: the axis is periodic
 template <typename T>
-__device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], T (&w)[2]) {
+__device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], T (&w)[2], bool per = false) {
   if (f == 1) {
     c[0] = c[1] = i;
     w[0] = T(1);
@@ -173,7 +190,8 @@ __device__ __forceinline__ void axis_taps(int i, int f, int n, int (&c)[2], T (&
   }
   const int p = i >> 1;
   int q = p + ((i & 1) ? 1 : -1);
-  if (q < 0 || q >= n) q = p;  // beyond a wall: the parent's value (zero normal gradient)
+  // beyond a wall: the parent's value (zero normal gradient); periodic: the wrapped cell
+  if (q < 0 || q >= n) q = per ? (q + n) % n : p;
   c[0] = p;
   c[1] = q;
   w[0] = T(0.75);
@@ -188,7 +206,7 @@ __device__ __forceinline__ T prolong_at(const MgLevelT<T> &F, const MgLevelT<T> 
   T wi[2], wj[2], wk[2];
   axis_taps(i, F.fx, Cl.nx, ci, wi);
   axis_taps(j, F.fy, Cl.ny, cj, wj);
-  axis_taps(k, F.fz, Cl.nz, ck, wk);
+  axis_taps(k, F.fz, Cl.nz, ck, wk, F.pz != 0);
   T v = T(0);
 #pragma unroll
   for (int a = 0; a < 2; ++a)
@@ -250,8 +268,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT
         const long long r = r0 + a * sx + e * sy;
         ld2(xf + r, xv[a][e][0], xv[a][e][1]);
         ld2(bf + r, bv[a][e][0], bv[a][e][1]);
-        xkm[a][e] = k0 > 0 ? xf[r - 1] : T(0);
-        xkp[a][e] = k0 + 2 < F.nz ? xf[r + 2] : T(0);
+        xkm[a][e] = k0 > 0 ? xf[r - 1] : (F.pz ? xf[r + F.nz - 1] : T(0));
+        xkp[a][e] = k0 + 2 < F.nz ? xf[r + 2] : (F.pz ? xf[r + 2 - F.nz] : T(0));
       }
 #pragma unroll
     for (int e = 0; e < 2; ++e) {  // x neighbours of the i0 and i0+1 planes
@@ -280,8 +298,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT
           if (fi < F.nx - 1) ax += a ? xip[e][c] : xv[1][e][c];
           if (fj > 0) ay += e ? xv[a][0][c] : xjm[a][c];
           if (fj < F.ny - 1) ay += e ? xjp[a][c] : xv[a][1][c];
-          if (fk > 0) az += c ? xv[a][e][0] : xkm[a][e];
-          if (fk < F.nz - 1) az += c ? xkp[a][e] : xv[a][e][1];
+          if (fk > 0 || F.pz) az += c ? xv[a][e][0] : xkm[a][e];
+          if (fk < F.nz - 1 || F.pz) az += c ? xkp[a][e] : xv[a][e][1];
           const T d = ldiag(F, fi, fj, fk);
           T bb = bv[a][e][c];
           if (bscale) bb *= d;
@@ -301,7 +319,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong8(MgLevelT<T> F, MgLevelT<
     T cv[3][3][3];
     const int ci[3] = {i > 0 ? i - 1 : i, i, i < Cl.nx - 1 ? i + 1 : i};
     const int cj[3] = {j > 0 ? j - 1 : j, j, j < Cl.ny - 1 ? j + 1 : j};
-    const int ck[3] = {k > 0 ? k - 1 : k, k, k < Cl.nz - 1 ? k + 1 : k};
+    const int ck[3] = {k > 0 ? k - 1 : (Cl.pz ? Cl.nz - 1 : k), k, k < Cl.nz - 1 ? k + 1 : (Cl.pz ? 0 : k)};
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -511,7 +529,8 @@ static void level_geometry(MgLevelT<T> &L, int nsm, bool quads) {
 }
 
 template <typename T>
-bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg) {
+bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, bool quads, MgPlanT<T> *mg,
+             bool pz) {
   *mg = MgPlanT<T>{};
   int l = 0;
   for (;;) {
@@ -519,6 +538,10 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
     L.nx = nx;
     L.ny = ny;
     L.nz = nz;
+    L.pz = pz ? 1 : 0;
+    // periodic z: red-black colouring holds across the wrap only for an even nz (or one
+    // cell, which has no z neighbours)
+    if (pz && nz % 2 && nz > 1) return false;
     L.wx = (T)(1.0 / (hx * hx));
     L.wy = (T)(1.0 / (hy * hy));
     L.wz = (T)(1.0 / (hz * hz));
@@ -587,8 +610,15 @@ bool mg_dense_inverse(const MgPlanT<T> &mg, std::vector<T> &M) {
         if (i < C.nx - 1) link(r + C.ny * C.nz, wx);
         if (j > 0) link(r - C.nz, wy);
         if (j < C.ny - 1) link(r + C.nz, wy);
-        if (k > 0) link(r - 1, wz);
-        if (k < C.nz - 1) link(r + 1, wz);
+        if (C.pz) {
+          if (C.nz > 1) {
+            link(k > 0 ? r - 1 : r + C.nz - 1, wz);
+            link(k < C.nz - 1 ? r + 1 : r + 1 - C.nz, wz);
+          }
+        } else {
+          if (k > 0) link(r - 1, wz);
+          if (k < C.nz - 1) link(r + 1, wz);
+        }
       }
   for (size_t q = 0; q < A.size(); ++q) A[q] += 1.0 / n;
   for (int r = 0; r < n; ++r) I[(size_t)r * n + r] = 1.0;
@@ -682,8 +712,8 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
   }
 }
 
-template bool mg_plan<float>(int, int, int, double, double, double, int, bool, MgPlanT<float> *);
-template bool mg_plan<double>(int, int, int, double, double, double, int, bool, MgPlanT<double> *);
+template bool mg_plan<float>(int, int, int, double, double, double, int, bool, MgPlanT<float> *, bool);
+template bool mg_plan<double>(int, int, int, double, double, double, int, bool, MgPlanT<double> *, bool);
 template int mg_vcycle_launches<float>(const MgPlanT<float> &);
 template bool mg_dense_inverse<float>(const MgPlanT<float> &, std::vector<float> &);
 template bool mg_dense_inverse<double>(const MgPlanT<double> &, std::vector<double> &);

@@ -82,11 +82,12 @@ def test_mixed_sor_combination_rejected(lib):
     assert lib.cfdgb_create(C.byref(cfg), C.byref(h)) == cg.EINVAL
 
 
-@pytest.mark.parametrize("kw", [dict(precond="multigrid", precision="mixed"), dict(precond="multigrid"),
+@pytest.mark.parametrize("kw", [dict(precond="multigrid", precision="mixed", nz=6), dict(precond="multigrid", nz=6),
                                 dict(solver="rbsor", nz=5)])
 def test_periodic_z_limits_rejected(lib, kw):
-    """Periodic z: the V-cycle's coarse levels are Neumann in z, and red-black SOR needs the
-    cells across the wrap to differ in colour (nz even)."""
+    """Periodic z: red-black smoothing and red-black SOR need the cells across the wrap to
+    differ in colour, so an even nz on the grid and on every multigrid level (6 coarsens to
+    3)."""
     base = dict(nx=32, ny=16, nz=8, lx=8.0, ly=4.0, lz=2.0, cx=2.0, cy=2.0, bc_z="periodic")
     cfg = cg.default_config(**{**base, **kw})
     h = C.c_void_p()
