@@ -14,7 +14,10 @@
 // A^+ lambda_x for both solvers), RHS^T, and CD^T, the transposed QUICK stencil with the
 // upwind branches of the forward state held fixed (the scheme is piecewise linear in the
 // transported field and bilinear in the face velocities).  CD^T scatters with FP64
-// atomics; every other kernel gathers.
+// atomics (one per target and thread: a thread sums its contributions per target first);
+// every other kernel gathers.  Divisions by the metrics are multiplications by their
+// reciprocal tables (RN(1/D)) and the DFIB face factors come from their table: the
+// transpose holds to an ulp per term, and the FP64 pipe is spared the division sequence.
 #include <algorithm>
 
 #include "cfdgb_internal.cuh"
@@ -130,8 +133,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_corr(Geo g, double dt, double cw
     const double ec = eta[c];
     if (i < g.nx - 3) {
       const long long cp = c + g.sx;
-      const double T2 = us[c] - dt * (p[cp] - p[c]) / g.Dxs[i];
-      const double e = ec + (eta[cp] - ec) * ((g.Dxs[i] * 0.5) / g.Dx[i]);
+      const double T2 = us[c] - dt * (p[cp] - p[c]) * g.rDxs[i];
+      const double e = ec + (eta[cp] - ec) * g.hfx[i];
       const double vol = g.Dx[i] * g.Dy[j] * g.Dz[k];
       lus[c] = (1.0 - e) * lu[c] + cw * e * vol;
       lex[c] = -T2 * lu[c] + cw * T2 * vol;
@@ -141,8 +144,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_corr(Geo g, double dt, double cw
     }
     if (j < g.ny - 3) {
       const long long cp = c + g.sy;
-      const double T2 = vs[c] - dt * (p[cp] - p[c]) / g.Dys[j];
-      const double e = ec + (eta[cp] - ec) * ((g.Dys[j] * 0.5) / g.Dy[j]);
+      const double T2 = vs[c] - dt * (p[cp] - p[c]) * g.rDys[j];
+      const double e = ec + (eta[cp] - ec) * g.hfy[j];
       lvs[c] = (1.0 - e) * lv[c];
       ley[c] = -T2 * lv[c];
     } else {
@@ -151,8 +154,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_corr(Geo g, double dt, double cw
     }
     if (k < g.nz - 3) {
       const long long cp = c + 1;
-      const double T2 = ws[c] - dt * (p[cp] - p[c]) / g.Dzs[k];
-      const double e = ec + (eta[cp] - ec) * ((g.Dzs[k] * 0.5) / g.Dz[k]);
+      const double T2 = ws[c] - dt * (p[cp] - p[c]) * g.rDzs[k];
+      const double e = ec + (eta[cp] - ec) * g.hfz[k];
       lws[c] = (1.0 - e) * lw[c];
       lez[c] = -T2 * lw[c];
     } else {
@@ -176,13 +179,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_corr_gather(Geo g, double dt, co
     int i, j, k;
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
-    const double l = dt * (lus[c] / g.Dxs[i] - lus[c - g.sx] / g.Dxs[i - 1] + lvs[c] / g.Dys[j] -
-                           lvs[c - g.sy] / g.Dys[j - 1] + lws[c] / g.Dzs[k] - lws[c - 1] / g.Dzs[k - 1]);
+    const double l = dt * (lus[c] * g.rDxs[i] - lus[c - g.sx] * g.rDxs[i - 1] + lvs[c] * g.rDys[j] -
+                           lvs[c - g.sy] * g.rDys[j - 1] + lws[c] * g.rDzs[k] - lws[c - 1] * g.rDzs[k - 1]);
     lx[row] = l;
     acc[0] += l;
-    const double itx = (g.Dxs[i] * 0.5) / g.Dx[i], itx1 = (g.Dxs[i - 1] * 0.5) / g.Dx[i - 1];
-    const double ity = (g.Dys[j] * 0.5) / g.Dy[j], ity1 = (g.Dys[j - 1] * 0.5) / g.Dy[j - 1];
-    const double itz = (g.Dzs[k] * 0.5) / g.Dz[k], itz1 = (g.Dzs[k - 1] * 0.5) / g.Dz[k - 1];
+    const double itx = g.hfx[i], itx1 = g.hfx[i - 1], ity = g.hfy[j], ity1 = g.hfy[j - 1];
+    const double itz = g.hfz[k], itz1 = g.hfz[k - 1];
     leta[c] += (1.0 - itx) * lex[c] + itx1 * lex[c - g.sx] + (1.0 - ity) * ley[c] + ity1 * ley[c - g.sy] +
                (1.0 - itz) * lez[c] + itz1 * lez[c - 1];
   }
@@ -214,133 +216,152 @@ __global__ void __launch_bounds__(kBlock) k_adj_rhs(Geo g, double dt, const doub
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
     const double l = lb[row];
-    if (i < g.nx - 3) lus[c] += -ddt / g.Dx[i] * l + ddt / g.Dx[i + 1] * lb[row + nyz];
-    else lu[c] += -ddt / g.Dx[i] * l;
-    if (i == 2) lu[c - g.sx] += ddt / g.Dx[i] * l;
-    if (j < g.ny - 3) lvs[c] += -ddt / g.Dy[j] * l + ddt / g.Dy[j + 1] * lb[row + g.nzc];
-    else lv[c] += -ddt / g.Dy[j] * l;
-    if (j == 2) lv[c - g.sy] += ddt / g.Dy[j] * l;
-    if (k < g.nz - 3) lws[c] += -ddt / g.Dz[k] * l + ddt / g.Dz[k + 1] * lb[row + 1];
-    else lw[c] += -ddt / g.Dz[k] * l;
-    if (k == 2) lw[c - 1] += ddt / g.Dz[k] * l;
+    if (i < g.nx - 3) lus[c] += -ddt * g.rDx[i] * l + ddt * g.rDx[i + 1] * lb[row + nyz];
+    else lu[c] += -ddt * g.rDx[i] * l;
+    if (i == 2) lu[c - g.sx] += ddt * g.rDx[i] * l;
+    if (j < g.ny - 3) lvs[c] += -ddt * g.rDy[j] * l + ddt * g.rDy[j + 1] * lb[row + g.nzc];
+    else lv[c] += -ddt * g.rDy[j] * l;
+    if (j == 2) lv[c - g.sy] += ddt * g.rDy[j] * l;
+    if (k < g.nz - 3) lws[c] += -ddt * g.rDz[k] * l + ddt * g.rDz[k + 1] * lb[row + 1];
+    else lw[c] += -ddt * g.rDz[k] * l;
+    if (k == 2) lw[c - 1] += ddt * g.rDz[k] * l;
   }
 }
 
 // ---- CD^T: transposed QUICK convection-diffusion ---------------------------------------
 // A face value of QuickUnitA/B (inc/source/Convection_Difussion.hpp:20-90) is, for the
-// branch the face velocity selects, a fixed combination of three transported values.
-struct Lin3 {
-  long long q[3];
-  double c[3];
+// branch the face velocity selects, a fixed combination of three transported values: the
+// cell's own and two along the axis (offsets -2..+2).  Divisions by the metrics are
+// multiplications by their reciprocal tables (RN(1/D): the adjoint is the transpose of the
+// step to within an ulp per term, which no gradient check resolves), so the kernel is not
+// held to the FP64 division sequence.
+// A face: its coefficients on the transported values at offsets -2..+2 along the axis
+// (two of them zero, by branch) and its value.
+struct Face {
+  double c[5];
   double val;
 };
 
-__device__ __forceinline__ void lin_set(Lin3 &L, long long q0, double c0, long long q1, double c1, long long q2,
-                                        double c2, const double *phi) {
-  L.q[0] = q0; L.q[1] = q1; L.q[2] = q2;
-  L.c[0] = c0; L.c[1] = c1; L.c[2] = c2;
-  L.val = c0 * phi[q0] + c1 * phi[q1] + c2 * phi[q2];
+__device__ __forceinline__ void face_set(Face &F, int lo, double c0, double c1, double c2, const double *phi,
+                                         long long sb) {
+  // the three coefficients sit at offsets lo, lo + 1, lo + 2 (lo in -2..0)
+#pragma unroll
+  for (int o = 0; o < 5; ++o) F.c[o] = 0.0;
+  F.c[lo + 2] = c0;
+  F.c[lo + 3] = c1;
+  F.c[lo + 4] = c2;
+  F.val = c0 * phi[lo * sb] + c1 * phi[(lo + 1) * sb] + c2 * phi[(lo + 2) * sb];
 }
 
-// QuickUnitA (the component's own axis)
-__device__ __forceinline__ void qa_lin(double Up, double Un, long long pp, long long p, long long ic, long long n,
-                                       long long nn, const double *Di, const double *Ds, int I, const double *phi,
-                                       Lin3 &P, Lin3 &N) {
+// QuickUnitA (the component's own axis); phi points at the cell, rDi / rDs the reciprocals
+__device__ __forceinline__ void qa_lin(double Up, double Un, long long sb, const double *Di, const double *rDi,
+                                       const double *rDs, int I, const double *phi, Face &P, Face &N) {
   if (Up > 0.0) {
-    const double k1 = 0.125 * Di[I + 1] * Di[I + 1] / Ds[I], a = 1.0 / Di[I + 1], b = 1.0 / Di[I];
-    lin_set(P, p, 0.5 - k1 * a, ic, 0.5 + k1 * a + k1 * b, n, -k1 * b, phi);
+    const double k1 = 0.125 * Di[I + 1] * Di[I + 1] * rDs[I], a = rDi[I + 1], b = rDi[I];
+    face_set(P, -1, -k1 * b, 0.5 + k1 * a + k1 * b, 0.5 - k1 * a, phi, sb);
   } else {
-    const double k2 = 0.125 * Di[I + 1] * Di[I + 1] / Ds[I + 1], a2 = 1.0 / Di[I + 2], a1 = 1.0 / Di[I + 1];
-    lin_set(P, pp, -k2 * a2, p, 0.5 + k2 * a2 + k2 * a1, ic, 0.5 - k2 * a1, phi);
+    const double k2 = 0.125 * Di[I + 1] * Di[I + 1] * rDs[I + 1], a2 = rDi[I + 2], a1 = rDi[I + 1];
+    face_set(P, 0, 0.5 - k2 * a1, 0.5 + k2 * a2 + k2 * a1, -k2 * a2, phi, sb);
   }
   if (Un > 0.0) {
-    const double k3 = 0.125 * Di[I] * Di[I] / Ds[I - 1], a = 1.0 / Di[I], b = 1.0 / Di[I - 1];
-    lin_set(N, ic, 0.5 - k3 * a, n, 0.5 + k3 * a + k3 * b, nn, -k3 * b, phi);
+    const double k3 = 0.125 * Di[I] * Di[I] * rDs[I - 1], a = rDi[I], b = rDi[I - 1];
+    face_set(N, -2, -k3 * b, 0.5 + k3 * a + k3 * b, 0.5 - k3 * a, phi, sb);
   } else {
-    const double k4 = 0.125 * Di[I] * Di[I] / Ds[I], a1 = 1.0 / Di[I + 1], a0 = 1.0 / Di[I];
-    lin_set(N, p, -k4 * a1, ic, 0.5 + k4 * a1 + k4 * a0, n, 0.5 - k4 * a0, phi);
+    const double k4 = 0.125 * Di[I] * Di[I] * rDs[I], a1 = rDi[I + 1], a0 = rDi[I];
+    face_set(N, -1, 0.5 - k4 * a0, 0.5 + k4 * a1 + k4 * a0, -k4 * a1, phi, sb);
   }
 }
 
 // QuickUnitB (across)
-__device__ __forceinline__ void qb_lin(double Up, double Un, long long pp, long long p, long long ic, long long n,
-                                       long long nn, const double *Di, const double *Ds, int I, const double *phi,
-                                       Lin3 &P, Lin3 &N) {
+__device__ __forceinline__ void qb_lin(double Up, double Un, long long sb, const double *Ds, const double *rDi,
+                                       const double *rDs, int I, const double *phi, Face &P, Face &N) {
   if (Up > 0.0) {
-    const double k = 0.125 * Ds[I] * Ds[I] / Di[I], a = 1.0 / Ds[I], b = 1.0 / Ds[I - 1];
-    lin_set(P, p, 0.5 - k * a, ic, 0.5 + k * a + k * b, n, -k * b, phi);
+    const double k = 0.125 * Ds[I] * Ds[I] * rDi[I], a = rDs[I], b = rDs[I - 1];
+    face_set(P, -1, -k * b, 0.5 + k * a + k * b, 0.5 - k * a, phi, sb);
   } else {
-    const double k = 0.125 * Ds[I] * Ds[I] / Di[I + 1], a2 = 1.0 / Ds[I + 1], a1 = 1.0 / Ds[I];
-    lin_set(P, pp, -k * a2, p, 0.5 + k * a2 + k * a1, ic, 0.5 - k * a1, phi);
+    const double k = 0.125 * Ds[I] * Ds[I] * rDi[I + 1], a2 = rDs[I + 1], a1 = rDs[I];
+    face_set(P, 0, 0.5 - k * a1, 0.5 + k * a2 + k * a1, -k * a2, phi, sb);
   }
   if (Un > 0.0) {
-    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I - 1], a = 1.0 / Ds[I - 1], b = 1.0 / Ds[I - 2];
-    lin_set(N, ic, 0.5 - k * a, n, 0.5 + k * a + k * b, nn, -k * b, phi);
+    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] * rDi[I - 1], a = rDs[I - 1], b = rDs[I - 2];
+    face_set(N, -2, -k * b, 0.5 + k * a + k * b, 0.5 - k * a, phi, sb);
   } else {
-    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] / Di[I], a1 = 1.0 / Ds[I], a0 = 1.0 / Ds[I - 1];
-    lin_set(N, p, -k * a1, ic, 0.5 + k * a1 + k * a0, n, 0.5 - k * a0, phi);
+    const double k = 0.125 * Ds[I - 1] * Ds[I - 1] * rDi[I], a1 = rDs[I], a0 = rDs[I - 1];
+    face_set(N, -1, 0.5 - k * a0, 0.5 + k * a1 + k * a0, -k * a1, phi, sb);
   }
 }
 
-__device__ __forceinline__ void scatter(double *lam, const Lin3 &L, double w) {
+// w times a face's coefficients into the per-offset accumulators
+__device__ __forceinline__ void gather_lin(double (&acc)[5], const Face &F, double w) {
 #pragma unroll
-  for (int t = 0; t < 3; ++t) atomicAdd(lam + L.q[t], w * L.c[t]);
+  for (int o = 0; o < 5; ++o) acc[o] = fma(w, F.c[o], acc[o]);
 }
 
 // Adjoint of one component (own axis A) of ConvectionDifussion at face c:
-// u*_c = u_c - dt * sum_b conv_b + nu dt * sum_b diff_b.
+// u*_c = u_c - dt * sum_b conv_b + nu dt * sum_b diff_b.  Contributions to the three
+// fields at the cell itself go to own[0..2] (the caller adds them once); the others are
+// summed per target in registers and added with one atomic each.
 template <int A>
 __device__ __forceinline__ void adj_component(const Geo &g, double dt, double nu, const double *const *vel,
-                                              double *const *lam, long long c, const int (&I)[3], double L) {
+                                              double *const *lam, long long c, const int (&I)[3], double L,
+                                              double (&own)[3]) {
   const long long s[3] = {g.sx, g.sy, 1};
   const double *D[3] = {g.Dx, g.Dy, g.Dz};
   const double *S[3] = {g.Dxs, g.Dys, g.Dzs};
-  const double *phi = vel[A];
-  double *lphi = lam[A];
-  atomicAdd(lphi + c, L);  // u*_c = u_c + ...
+  const double *rD[3] = {g.rDx, g.rDy, g.rDz};
+  const double *rS[3] = {g.rDxs, g.rDys, g.rDzs};
+  const double *hf[3] = {g.hfx, g.hfy, g.hfz};
+  const double *phi = vel[A] + c;
+  double *lphi = lam[A] + c;
+  own[A] += L;  // u*_c = u_c + ...
   const double gc = -dt * L, h = nu * dt * L;
-  const double IT = (S[A][I[A]] * 0.5) / D[A][I[A]];
+  const double IT = hf[A][I[A]];  // (Ds * 0.5) / D
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
     const long long sb = s[b];
     const int Ib = I[b];
-    const double *Db = D[b], *Sb = S[b];
+    const double *Db = D[b], *Sb = S[b], *rDb = rD[b], *rSb = rS[b];
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // lam[A] at offsets -2..+2 along b
     // diffusion
     double ap, an;
     if (b == A) {
-      ap = 1.0 / (Db[Ib + 1] * Sb[Ib]);
-      an = 1.0 / (Db[Ib] * Sb[Ib]);
+      ap = rDb[Ib + 1] * rSb[Ib];
+      an = rDb[Ib] * rSb[Ib];
     } else {
-      ap = 1.0 / (Sb[Ib] * Db[Ib]);
-      an = 1.0 / (Sb[Ib - 1] * Db[Ib]);
+      ap = rSb[Ib] * rDb[Ib];
+      an = rSb[Ib - 1] * rDb[Ib];
     }
-    atomicAdd(lphi + c + sb, h * ap);
-    atomicAdd(lphi + c - sb, h * an);
-    atomicAdd(lphi + c, -h * (ap + an));
+    acc[3] += h * ap;
+    acc[1] += h * an;
+    acc[2] -= h * (ap + an);
     // convection
-    Lin3 P, N;
+    Face P, N;
     if (b == A) {
-      const double Up = 0.5 * (phi[c + sb] + phi[c]), Un = 0.5 * (phi[c - sb] + phi[c]);
-      qa_lin(Up, Un, c + 2 * sb, c + sb, c, c - sb, c - 2 * sb, Db, Sb, Ib, phi, P, N);
-      const double w = gc / Sb[Ib];  // (P^2 - N^2) / Ds
-      scatter(lphi, P, w * 2.0 * P.val);
-      scatter(lphi, N, -w * 2.0 * N.val);
+      const double Up = 0.5 * (phi[sb] + phi[0]), Un = 0.5 * (phi[-sb] + phi[0]);
+      qa_lin(Up, Un, sb, Db, rDb, rSb, Ib, phi, P, N);
+      const double w = gc * rSb[Ib];  // (P^2 - N^2) / Ds
+      gather_lin(acc, P, w * 2.0 * P.val);
+      gather_lin(acc, N, -w * 2.0 * N.val);
     } else {
-      const double *vb = vel[b];
-      double *lvb = lam[b];
+      const double *vb = vel[b] + c;
+      double *lvb = lam[b] + c;
       const long long sA = s[A];
-      const double b0 = vb[c], bA = vb[c + sA], bm = vb[c - sb], bmA = vb[c - sb + sA];
+      const double b0 = vb[0], bA = vb[sA], bm = vb[-sb], bmA = vb[-sb + sA];
       const double Bp = b0 + (bA - b0) * IT, Bn = bm + (bmA - bm) * IT;
-      qb_lin(Bp, Bn, c + 2 * sb, c + sb, c, c - sb, c - 2 * sb, Db, Sb, Ib, phi, P, N);
-      const double w = gc / Db[Ib];  // (P Bp - N Bn) / D
-      scatter(lphi, P, w * Bp);
-      scatter(lphi, N, -w * Bn);
+      qb_lin(Bp, Bn, sb, Sb, rDb, rSb, Ib, phi, P, N);
+      const double w = gc * rDb[Ib];  // (P Bp - N Bn) / D
+      gather_lin(acc, P, w * Bp);
+      gather_lin(acc, N, -w * Bn);
       const double lBp = w * P.val, lBn = -w * N.val;
-      atomicAdd(lvb + c, (1.0 - IT) * lBp);
-      atomicAdd(lvb + c + sA, IT * lBp);
-      atomicAdd(lvb + c - sb, (1.0 - IT) * lBn);
-      atomicAdd(lvb + c - sb + sA, IT * lBn);
+      own[b] += (1.0 - IT) * lBp;
+      atomicAdd(lvb + sA, IT * lBp);
+      atomicAdd(lvb - sb, (1.0 - IT) * lBn);
+      atomicAdd(lvb - sb + sA, IT * lBn);
     }
+    own[A] += acc[2];
+#pragma unroll
+    for (int o = 0; o < 5; ++o)
+      if (o != 2 && acc[o] != 0.0) atomicAdd(lphi + (o - 2) * sb, acc[o]);
   }
 }
 
@@ -356,9 +377,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_convdiff(Geo g, double dt, doubl
     row_ijk(g, row, i, j, k);
     const long long c = pidx(g, i, j, k);
     const int I[3] = {i, j, k};
-    if (i < g.nx - 3 && lus[c] != 0.0) adj_component<0>(g, dt, nu, vel, lam, c, I, lus[c]);
-    if (j < g.ny - 3 && lvs[c] != 0.0) adj_component<1>(g, dt, nu, vel, lam, c, I, lvs[c]);
-    if (k < g.nz - 3 && lws[c] != 0.0) adj_component<2>(g, dt, nu, vel, lam, c, I, lws[c]);
+    double own[3] = {0.0, 0.0, 0.0};
+    if (i < g.nx - 3 && lus[c] != 0.0) adj_component<0>(g, dt, nu, vel, lam, c, I, lus[c], own);
+    if (j < g.ny - 3 && lvs[c] != 0.0) adj_component<1>(g, dt, nu, vel, lam, c, I, lvs[c], own);
+    if (k < g.nz - 3 && lws[c] != 0.0) adj_component<2>(g, dt, nu, vel, lam, c, I, lws[c], own);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      if (own[a] != 0.0) atomicAdd(lam[a] + c, own[a]);
   }
 }
 

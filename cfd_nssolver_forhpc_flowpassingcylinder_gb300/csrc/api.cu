@@ -103,6 +103,7 @@ struct cfdgb_ctx {
   // device buffers
   double *metric = nullptr, *Xd = nullptr, *Yd = nullptr;
   float *tab32 = nullptr;
+  std::vector<float> tab32_uni;  // a uniform grid's table rows, one value each (3 x 11); empty otherwise
   double *u = nullptr, *v = nullptr, *w = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
   double *ui = nullptr, *vi = nullptr, *wi = nullptr, *p = nullptr, *eta = nullptr;
   double *b = nullptr, *x = nullptr, *px1 = nullptr, *px2 = nullptr, *r64 = nullptr;
@@ -652,6 +653,8 @@ void enqueue_rhs(cfdgb_ctx *c) {
     L(c, K_RHS, 2, [&] { launch_project_rhs(c->stream, c->g, st64, jac ? 1 : 0, c->b, c->part, c->ss); });
 }
 
+int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres, int *status);
+
 int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *status) {
   const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
   const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
@@ -691,6 +694,17 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     *status = r.status;
     return 0;
   }
+  return solve_mixed(c, c->cfg.tol, iters, outer, relres, status);
+}
+
+// MIXED solve of the context's system on b (rows of the context's solver) from the warm
+// start x, to relative residual tol; iters, outer, relres and status as solve_pressure's
+int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres, int *status) {
+  const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+  const Stencil<double> &st64 = jac ? c->jac64 : c->spe64;
+  *iters = 0;
+  *outer = 0;
+  *status = 0;
   // MIXED: FP32 BiCGSTAB sweeps inside FP64 iterative refinement (defect correction).
   // Each sweep starts afresh from the FP64 residual and stops once its own residual has
   // dropped by inner_tol (or looks converged); the refinement adds its correction to the
@@ -719,8 +733,8 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     *status = CFDGB_ENAN;
     return 0;
   }
-  if (rel < c->cfg.tol) return 0;
-  TRY(set_solver_params(c, c->sc32, c->cfg.tol, c->cfg.maxit));
+  if (rel < tol) return 0;
+  TRY(set_solver_params(c, c->sc32, tol, c->cfg.maxit));
   if (c->test_wait_fault) {  // one shot
     static const int one = 1;
     CK(cudaMemcpyAsync(&c->sc32->test_wait, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -779,7 +793,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     rel = rn;
     best = std::min(best, rn);
     *relres = rn;
-    if (rn < c->cfg.tol) break;
+    if (rn < tol) break;
     if (r.status == CFDGB_ENOCONV && !broke) {  // iteration cap
       *status = CFDGB_ENOCONV;
       break;
@@ -794,7 +808,7 @@ int solve_pressure(cfdgb_ctx *c, int *iters, int *outer, double *relres, int *st
     });
   }
   if (finish64) {
-    TRY(set_solver_params(c, c->sc, c->cfg.tol, c->cfg.maxit));
+    TRY(set_solver_params(c, c->sc, tol, c->cfg.maxit));
     L(c, K_SETUP64, 1, [&] { launch_setup64(c, st64); });
     SolverScal r;
     TRY(run_chunks(c, false, &r));
@@ -914,7 +928,8 @@ void convdiff(cfdgb_ctx *c, const double *u, const double *v, const double *w, d
   if (fast_convdiff(c)) {
     L(c, K_MIRROR, 1, [&] { launch_mirror32(c->stream, c->g, u, v, w, c->u32, c->v32, c->w32); });
     L(c, K_CONVDIFF, 1, [&] {
-      launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->cfg.dt, nu, u, v, w, c->u32, c->v32, c->w32, us, vs,
+      launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->tab32_uni.empty() ? nullptr : c->tab32_uni.data(),
+                          c->cfg.dt, nu, u, v, w, c->u32, c->v32, c->w32, us, vs,
                           ws, sc);
     });
   } else {
@@ -1244,6 +1259,19 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   std::vector<float> tab = build_tab32(c, L);
   if ((rc = dalloc(c, &c->tab32, tab.size()))) return bail(rc);
   cudaMemcpy(c->tab32, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice);
+  {  // every row one value along its axis (a uniform grid): the kernel takes them as parameters
+    const int ext[3] = {nx, ny, nz};
+    bool uni = true;
+    std::vector<float> u1(3 * 11);
+    for (int a = 0; a < 3 && uni; ++a)
+      for (int r = 0; r < 11 && uni; ++r) {
+        const float *row = tab.data() + ((size_t)a * 11 + r) * L;
+        u1[a * 11 + r] = row[0];
+        for (int q = 1; q < ext[a]; ++q)
+          if (row[q] != row[0]) uni = false;
+      }
+    if (uni) c->tab32_uni = u1;
+  }
   Geo &g = c->g;
   g.nxc = cfg->nx; g.nyc = cfg->ny; g.nzc = cfg->nz;
   g.walls = cfg->walls;
@@ -1271,6 +1299,10 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     g.hfx = g.rDzs + nz; g.hfy = g.hfx + nx; g.hfz = g.hfy + ny;
   }
   g.div2 = division_twice(c) ? 1 : 0;
+  g.uni = 1;
+  for (auto *v : {&c->Dx, &c->Dy, &c->Dz, &c->Dxs, &c->Dys, &c->Dzs})
+    for (double d : *v)
+      if (d != v->front()) g.uni = 0;
   if (cfg->grid == CFDGB_GRID_SML) {
     // per-axis operator factors and the Jacobi scale of every row (createPressureMatrixCSR)
     const Coef C{c};
@@ -1919,27 +1951,24 @@ int dd_copy(cfdgb_ctx *c, double *dst, const double *src, size_t n) {
   return 0;
 }
 
-// Adjoint Poisson solve A y = rhs with the unscaled operator, zero start, its own scalars
-// (no restarts: a fresh solver object each time).
-// The FP64 V-cycle of the transposed solve (contexts with the multigrid preconditioner)
-int build_adjoint_mg(cfdgb_ctx *c) {
-  if (!c->use_mg64) {  // a MIXED context has only the FP32 hierarchy
-    const cfdgb_config &cf = c->cfg;
-    mg_plan(cf.nx, cf.ny, cf.nz, cf.lx / cf.nx, cf.ly / cf.ny, cf.lz / cf.nz, c->nsm, false, &c->mg64, c->g.pz != 0);
-    mg_prepare<double>();
-    TRY(upload_dense_coarse(c, c->mg64));
-    for (int l = 1; l < c->mg64.nlev; ++l) {
-      MgLevelT<double> &Lv = c->mg64.lev[l];
-      const size_t n = (size_t)Lv.nx * Lv.ny * Lv.nz;
-      TRY(dalloc(c, &Lv.x, n));
-      TRY(dalloc(c, &Lv.b, n));
-    }
-  }
-  c->adj_mg = true;
-  return 0;
-}
-
+// Adjoint Poisson solve A y = rhs with the unscaled operator (symmetric on the uniform
+// grid), zero start.  FP64 contexts: its own scalars (no restarts: a fresh solver object
+// each time), with the context's FP64 V-cycle where it has the multigrid preconditioner.
 int adjoint_solve(cfdgb_ctx *c, const double *rhs, double tol, int *iters) {
+  if (c->cfg.precision == CFDGB_MIXED) {
+    // a MIXED context solves as its forward does (FP32 sweeps in FP64 refinement, its
+    // solver and preconditioner), on the forward's b and x: free here, as every step rebuilds
+    // b and each recompute window restores x from its checkpoint.  The Jacobi rows take
+    // jp * rhs (the same solution).  The answer goes to ka.x, zero start.
+    const bool jac = c->cfg.solver == CFDGB_BICGSTAB_JACOBI;
+    launch_scale_rows(c->stream, c->g, c->jac64, jac ? 1 : 0, rhs, c->b);
+    CK(cudaMemsetAsync(c->x, 0, c->ncell * sizeof(double), c->stream));
+    int outer = 0, status = 0;
+    double rr = 0.0;
+    TRY(solve_mixed(c, tol, iters, &outer, &rr, &status));
+    CK(cudaMemcpyAsync(c->ka.x, c->x, c->ncell * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return status;
+  }
   CK(cudaMemsetAsync(c->sca, 0, sizeof(SolverScal), c->stream));
   CK(cudaMemsetAsync(c->ka.x, 0, c->ncell * sizeof(double), c->stream));
   TRY(set_solver_params(c, c->sca, tol, c->cfg.maxit));
@@ -2049,8 +2078,11 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
     TRY(dalloc(c, &c->leta, np));
     TRY(dalloc(c, &c->lx, c->ncell));
     TRY(dalloc(c, &c->linlet, (size_t)c->cfg.ny * c->cfg.nz));
-    double **kv[] = {&c->ka.x, &c->ka.r0, &c->ka.r1, &c->ka.p1, &c->ka.s, &c->ka.ap, &c->ka.as, &c->kapx[0], &c->kapx[1]};
-    for (auto **q : kv) TRY(dalloc(c, q, c->ncell));
+    TRY(dalloc(c, &c->ka.x, c->ncell));
+    if (c->cfg.precision == CFDGB_FP64) {  // the FP64 transposed solve's vectors (MIXED solves as its forward)
+      double **kv[] = {&c->ka.r0, &c->ka.r1, &c->ka.p1, &c->ka.s, &c->ka.ap, &c->ka.as, &c->kapx[0], &c->kapx[1]};
+      for (auto **q : kv) TRY(dalloc(c, q, c->ncell));
+    }
     TRY(dalloc(c, &c->sca, 1));
   }
   while ((int)c->win.size() < 3 * K) {
@@ -2063,7 +2095,7 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
     TRY(dalloc(c, &d, np));
     c->winp.push_back(d);
   }
-  if (c->cfg.precond == CFDGB_PRECOND_MULTIGRID && !c->adj_mg) TRY(build_adjoint_mg(c));
+  c->adj_mg = c->use_mg64;  // FP64 multigrid contexts: the transposed solve takes their V-cycle
   for (int a = 0; a < 3; ++a) {
     CK(cudaMemsetAsync(c->lA[a], 0, np * sizeof(double), c->stream));
     CK(cudaMemsetAsync(c->lus[a], 0, np * sizeof(double), c->stream));
@@ -2108,9 +2140,16 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
       double **wv = &c->win[3 * (n - n0)];
       launch_f32_to_f64(c->stream, (long long)np, c->winp[n - n0], c->p);
       launch_adj_bc(c->stream, c->g, c->lA[0], c->lA[1], c->lA[2], c->linlet);
-      // u* of step n (interior faces), from U^n
-      launch_convdiff_exact(c->stream, c->nblk, c->g, CFDGB_QUICK, dt, nu, nullptr, wv[0], wv[1], wv[2], c->us, c->vs,
-                            c->ws, StepCtl{});
+      // u* of step n (interior faces), from U^n, by the kernel the forward step ran (MIXED:
+      // the FP32 stencil on FP32 copies, which reproduces the forward's u* bit for bit)
+      if (fast_convdiff(c)) {
+        launch_mirror32(c->stream, c->g, wv[0], wv[1], wv[2], c->u32, c->v32, c->w32);
+        launch_convdiff_f32(c->stream, c->nblk, c->g, c->tab32, c->tab32_uni.empty() ? nullptr : c->tab32_uni.data(),
+                            dt, nu, wv[0], wv[1], wv[2], c->u32, c->v32, c->w32, c->us, c->vs, c->ws, StepCtl{});
+      } else {
+        launch_convdiff_exact(c->stream, c->nblk, c->g, CFDGB_QUICK, dt, nu, nullptr, wv[0], wv[1], wv[2], c->us,
+                              c->vs, c->ws, StepCtl{});
+      }
       const double cw = (n >= obj.first && n <= obj.last) ? cw_in : 0.0;
       launch_adj_corr(c->stream, c->nblk, c->g, dt, cw, c->eta, c->p, c->us, c->vs, c->ws, c->lA[0], c->lA[1],
                       c->lA[2], c->lus[0], c->lus[1], c->lus[2], c->le[0], c->le[1], c->le[2], c->lx, c->leta,
@@ -2126,8 +2165,13 @@ int cfdgb_backward(cfdgb_ctx *c, double *dJ_dinlet, double *dJ_deta) {
         launch_adj_rhs(c->stream, c->nblk, c->g, dt, c->ka.x, c->lus[0], c->lus[1], c->lus[2], c->lB[0], c->lB[1],
                        c->lB[2]);
       }
-      launch_adj_convdiff(c->stream, c->nblk, c->g, dt, nu, wv[0], wv[1], wv[2], c->lus[0], c->lus[1], c->lus[2],
-                          c->lB[0], c->lB[1], c->lB[2]);
+      if (fast_convdiff(c))  // the transpose of the FP32 stencil the forward ran (u32.. hold U^n)
+        launch_adj_convdiff_f32(c->stream, c->nblk, c->g, c->tab32,
+                                c->tab32_uni.empty() ? nullptr : c->tab32_uni.data(), dt, nu, c->u32, c->v32, c->w32,
+                                c->lus[0], c->lus[1], c->lus[2], c->lB[0], c->lB[1], c->lB[2]);
+      else
+        launch_adj_convdiff(c->stream, c->nblk, c->g, dt, nu, wv[0], wv[1], wv[2], c->lus[0], c->lus[1],
+                            c->lus[2], c->lB[0], c->lB[1], c->lB[2]);
       for (int a = 0; a < 3; ++a) std::swap(c->lA[a], c->lB[a]);
     }
   }

@@ -60,6 +60,7 @@ struct Geo {
   // the DFIB face-fraction factors (Ds * 0.5) / D of updateUandF.hpp, each one IEEE division
   const double *rDx, *rDy, *rDz, *rDxs, *rDys, *rDzs, *hfx, *hfy, *hfz;
   int div2;  // 1: div_by applies its correction twice (a divisor lacks the certificate)
+  int uni;   // 1: every metric array holds one value (a uniform grid): per-axis factors hoist
 };
 
 // Width along k of the 3-D solver blocks (host side; the context driver and the

@@ -10,6 +10,8 @@
 //             [scheme=quick|lud|ud: the convection switch (inc/0_General.hpp:114-118);
 //              les=1: the Smagorinsky model (TERBULENCE_SMAGORINSKY);
 //              walls=free_slip: the free-slip y-wall rows of the boundary table;
+//              bc_z=periodic: periodic z; outflow=convective: the convective outflow with
+//              the mass-flux correction (neither is in the reference);
 //              precond=multigrid: the FP32 multigrid V-cycle preconditioning the MIXED
 //              BiCGSTAB sweeps]
 //             [restart=<file.q>: start from a Plot3D solution file of this grid (QfileRead,
@@ -55,6 +57,9 @@ int main(int argc, char **argv) {
   cfg.les = (int)num("les", 0.0);
   cfg.walls = (kv.count("walls") && kv["walls"] == "free_slip") ? CFDGB_WALLS_FREE_SLIP : CFDGB_WALLS_ZERO_GRADIENT;
   cfg.precond = (kv.count("precond") && kv["precond"] == "multigrid") ? CFDGB_PRECOND_MULTIGRID : CFDGB_PRECOND_NONE;
+  cfg.bc_z = (kv.count("bc_z") && kv["bc_z"] == "periodic") ? CFDGB_Z_PERIODIC : CFDGB_Z_ZERO_GRADIENT;
+  cfg.outflow = (kv.count("outflow") && kv["outflow"] == "convective") ? CFDGB_OUTFLOW_CONVECTIVE
+                                                                         : CFDGB_OUTFLOW_ZERO_GRADIENT;
   const std::string solver = kv.count("solver") ? kv["solver"] : "bicgstab";
   cfg.solver = solver == "jacobi" ? CFDGB_BICGSTAB_JACOBI
                : solver == "rbsor"  ? CFDGB_RBSOR

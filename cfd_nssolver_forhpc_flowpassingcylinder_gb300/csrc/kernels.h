@@ -56,10 +56,18 @@ void launch_eta(cudaStream_t s, int nblk, const Geo &g, const double *X, const d
 
 // step_fast.cu (MIXED: FP32 arithmetic on the FP64 state)
 // u32, v32, w32: FP32 copies of the padded u, v, w (launch_mirror32), which the stencil
-// reads; u, v, w (FP64) give u* = u + increment.  Fused CFL reduction into sc.ss.
-void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
-                         const double *u, const double *v, const double *w, const float *u32, const float *v32,
-                         const float *w32, double *us, double *vs, double *ws, const StepCtl &sc);
+// reads; u, v, w (FP64) give u* = u + increment.  Fused CFL reduction into sc.ss.  tab: the
+// per-axis FP32 tables (device); uni: on a uniform grid, the one value of each of their
+// rows (host, 3 x 11), which the kernel then takes as parameters; NULL otherwise.
+void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, const float *uni, double dt,
+                         double nu, const double *u, const double *v, const double *w, const float *u32,
+                         const float *v32, const float *w32, double *us, double *vs, double *ws, const StepCtl &sc);
+// the adjoint of launch_convdiff_f32 (MIXED contexts): lambda of u*, v*, w* (lus, lvs,
+// lws) into lambda of U^n (lu, lv, lw, accumulated), with u32, v32, w32 the FP32 copies of
+// U^n the forward's stencil read
+void launch_adj_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, const float *uni, double dt,
+                             double nu, const float *u32, const float *v32, const float *w32, const double *lus,
+                             const double *lvs, const double *lws, double *lu, double *lv, double *lw);
 // MIXED: createBMatrix with the reciprocal metrics (multiplications)
 void launch_rhs_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const double *dtp, const double *us,
                      const double *vs, const double *ws, int jacobi, const Stencil<double> &st, double *b);
@@ -137,6 +145,10 @@ void launch_adj_convdiff(cudaStream_t s, int nblk, const Geo &g, double dt, doub
                          const double *w, const double *lus, const double *lvs, const double *lws, double *lu,
                          double *lv, double *lw);
 
+// out = jp * in for the Jacobi-scaled rows, in otherwise (a right-hand side in the rows of
+// the context's solver)
+void launch_scale_rows(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, const double *in,
+                       double *out);
 // b -= its null-space part (mean of the unscaled rhs; jp-weighted for the Jacobi rows)
 void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
                         StepScal *ss);

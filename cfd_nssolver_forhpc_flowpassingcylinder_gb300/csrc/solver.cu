@@ -1654,6 +1654,15 @@ __global__ void __launch_bounds__(kBlock) k_rhs_subtract(Geo g, Stencil<double> 
   }
 }
 
+// out = in scaled to the rows of the system: by jp (Jacobi-scaled rows) or unchanged
+__global__ void __launch_bounds__(kBlock) k_scale_rows(Geo g, Stencil<double> st, int jacobi,
+                                                        const double *__restrict__ in, double *__restrict__ out) {
+  FOR_CELLS(g) {
+    const long long row = ROW(g);
+    out[row] = jacobi ? row_jp(g, st, ic, jc, kc, row) * in[row] : in[row];
+  }
+}
+
 // ---- red-black SOR (FP64) on the exact Neumann rows ----
 // One colour per launch: cells with (i+j+k) even, then odd, so each half-sweep updates
 // cells whose neighbours all have the other colour (no race, order independent; periodic z
@@ -1868,6 +1877,10 @@ void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st,
                         StepScal *ss) {
   k_rhs_sum<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, part, ss);
   k_rhs_subtract<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, ss);
+}
+void launch_scale_rows(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, const double *in,
+                       double *out) {
+  k_scale_rows<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, in, out);
 }
 void launch_rbsor_sweep(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, const double *b, double *x,
                         double omega) {

@@ -620,23 +620,45 @@ __global__ void __launch_bounds__(kBlock) k_bc_zp(Geo g, double *u, double *v, d
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_bc_z(Geo g, BcTable t, double *u, double *v, double *w, double *p,
-                                                 double *us, double *vs, double *ws, int do_main) {
+__global__ void __launch_bounds__(kBlock) k_bc_z(Geo g, BcTable t, double *__restrict__ u, double *__restrict__ v,
+                                                 double *__restrict__ w, double *__restrict__ p,
+                                                 double *__restrict__ us, double *__restrict__ vs,
+                                                 double *__restrict__ ws, int do_main) {
   const int nxc = g.nxc, nyc = g.nyc, nz = g.nz;
   for (int q = blockIdx.x * kBlock + threadIdx.x; q < nxc * nyc; q += gridDim.x * kBlock) {
     const int i = q / nyc + 2, j = q % nyc + 2;
     const long long base = pidx(g, i, j, 0);
     if (do_main) {
-      u[base + 1] = u[base + 0] = t.dir[4][0] * 2. + (2.0 * t.num[4][0] - 1.0) * u[base + 2];
-      v[base + 1] = v[base + 0] = t.dir[4][1] * 2. + (2.0 * t.num[4][1] - 1.0) * v[base + 2];
-      w[base + 1] = w[base + 0] = t.dir[4][2] + t.num[4][2] * w[base + 2];
-      w[base + nz - 1] = w[base + nz - 2] = w[base + nz - 3] = t.dir[5][2] + t.num[5][2] * w[base + nz - 4];
-      u[base + nz - 1] = u[base + nz - 2] = t.dir[5][0] * 2. + (2.0 * t.num[5][0] - 1.0) * u[base + nz - 3];
-      v[base + nz - 1] = v[base + nz - 2] = t.dir[5][1] * 2. + (2.0 * t.num[5][1] - 1.0) * v[base + nz - 3];
+      // every source value first (each line's ends lie 8 B x nz apart: the loads of all
+      // four fields are in flight together), then the ghosts
+      const double u2 = u[base + 2], v2 = v[base + 2], w2 = w[base + 2];
+      const double uT = u[base + nz - 3], vT = v[base + nz - 3], wT = w[base + nz - 4];
+      const double p2 = p ? p[base + 2] : 0.0, pT = p ? p[base + nz - 3] : 0.0;
+      const double ub = t.dir[4][0] * 2. + (2.0 * t.num[4][0] - 1.0) * u2;
+      const double vb = t.dir[4][1] * 2. + (2.0 * t.num[4][1] - 1.0) * v2;
+      const double wb = t.dir[4][2] + t.num[4][2] * w2;
+      const double wt = t.dir[5][2] + t.num[5][2] * wT;
+      const double ut = t.dir[5][0] * 2. + (2.0 * t.num[5][0] - 1.0) * uT;
+      const double vt = t.dir[5][1] * 2. + (2.0 * t.num[5][1] - 1.0) * vT;
+      u[base + 1] = u[base + 0] = ub;
+      v[base + 1] = v[base + 0] = vb;
+      w[base + 1] = w[base + 0] = wb;
+      w[base + nz - 1] = w[base + nz - 2] = w[base + nz - 3] = wt;
+      u[base + nz - 1] = u[base + nz - 2] = ut;
+      v[base + nz - 1] = v[base + nz - 2] = vt;
       if (p) {
-        p[base + 1] = p[base + 0] = p[base + 2];
-        p[base + nz - 2] = p[base + nz - 1] = p[base + nz - 3];
+        p[base + 1] = p[base + 0] = p2;
+        p[base + nz - 2] = p[base + nz - 1] = pT;
       }
+      if (us) {  // the copies of what this thread just wrote
+        us[base + 0] = us[base + 1] = ub;
+        us[base + nz - 2] = us[base + nz - 1] = ut;
+        vs[base + 0] = vs[base + 1] = vb;
+        vs[base + nz - 2] = vs[base + nz - 1] = vt;
+        ws[base + 0] = ws[base + 1] = wb;
+        ws[base + nz - 3] = ws[base + nz - 2] = ws[base + nz - 1] = wt;
+      }
+      continue;
     }
     if (us) {
       const int ku[4] = {0, 1, nz - 2, nz - 1};

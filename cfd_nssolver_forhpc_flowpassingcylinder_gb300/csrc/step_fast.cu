@@ -59,66 +59,74 @@ enum TabRow { T_ID = 0, T_IDS, T_IT, T_AP1, T_AP2, T_AN1, T_AN2, T_BP1, T_BP2, T
 struct FastArgs {
   int L;  // table row length
   float dt, nu;
+  // a uniform grid's tables: every row is one value per axis, passed as kernel parameters
+  // (the UNI kernel reads these instead of loading the table at every term)
+  float uni[3][T_NROW];
 };
 
-__device__ __forceinline__ float tb(const float *__restrict__ tab, int L, int axis, int row, int I) {
-  return __ldg(tab + ((axis * T_NROW + row) * L + I));
+// table entry (axis, row, I): the parameter of a uniform grid, else a load
+template <bool UNI>
+__device__ __forceinline__ float tb(const FastArgs &fa, const float *__restrict__ tab, int axis, int row, int I) {
+  if (UNI) return fa.uni[axis][row];
+  return __ldg(tab + ((axis * T_NROW + row) * fa.L + I));
 }
 
 // QUICK along the component's own axis (QuickUnitA, :20-51)
+template <bool UNI>
 __device__ __forceinline__ void qa(float Up, float Un, float pp, float p, float c, float n, float nn,
-                                   const float *tab, int L, int ax, int I, float &P, float &N) {
-  const float iDm1 = tb(tab, L, ax, T_ID, I - 1), iD0 = tb(tab, L, ax, T_ID, I), iD1 = tb(tab, L, ax, T_ID, I + 1),
-              iD2 = tb(tab, L, ax, T_ID, I + 2);
-  P = 0.5f * (c + p) - (Up > 0.0f ? tb(tab, L, ax, T_AP1, I) * ((p - c) * iD1 - (c - n) * iD0)
-                                  : tb(tab, L, ax, T_AP2, I) * ((pp - p) * iD2 - (p - c) * iD1));
-  N = 0.5f * (n + c) - (Un > 0.0f ? tb(tab, L, ax, T_AN1, I) * ((c - n) * iD0 - (n - nn) * iDm1)
-                                  : tb(tab, L, ax, T_AN2, I) * ((p - c) * iD1 - (c - n) * iD0));
+                                   const FastArgs &fa, const float *tab, int ax, int I, float &P, float &N) {
+  const float iDm1 = tb<UNI>(fa, tab, ax, T_ID, I - 1), iD0 = tb<UNI>(fa, tab, ax, T_ID, I),
+              iD1 = tb<UNI>(fa, tab, ax, T_ID, I + 1), iD2 = tb<UNI>(fa, tab, ax, T_ID, I + 2);
+  P = 0.5f * (c + p) - (Up > 0.0f ? tb<UNI>(fa, tab, ax, T_AP1, I) * ((p - c) * iD1 - (c - n) * iD0)
+                                  : tb<UNI>(fa, tab, ax, T_AP2, I) * ((pp - p) * iD2 - (p - c) * iD1));
+  N = 0.5f * (n + c) - (Un > 0.0f ? tb<UNI>(fa, tab, ax, T_AN1, I) * ((c - n) * iD0 - (n - nn) * iDm1)
+                                  : tb<UNI>(fa, tab, ax, T_AN2, I) * ((p - c) * iD1 - (c - n) * iD0));
 }
 // QUICK across (QuickUnitB, :55-90)
+template <bool UNI>
 __device__ __forceinline__ void qb(float Up, float Un, float pp, float p, float c, float n, float nn,
-                                   const float *tab, int L, int ax, int I, float &P, float &N) {
-  const float iSm2 = tb(tab, L, ax, T_IDS, I - 2), iSm1 = tb(tab, L, ax, T_IDS, I - 1),
-              iS0 = tb(tab, L, ax, T_IDS, I), iS1 = tb(tab, L, ax, T_IDS, I + 1);
-  P = 0.5f * (c + p) - (Up > 0.0f ? tb(tab, L, ax, T_BP1, I) * ((p - c) * iS0 - (c - n) * iSm1)
-                                  : tb(tab, L, ax, T_BP2, I) * ((pp - p) * iS1 - (p - c) * iS0));
-  N = 0.5f * (n + c) - (Un > 0.0f ? tb(tab, L, ax, T_BN1, I) * ((c - n) * iSm1 - (n - nn) * iSm2)
-                                  : tb(tab, L, ax, T_BN2, I) * ((p - c) * iS0 - (c - n) * iSm1));
+                                   const FastArgs &fa, const float *tab, int ax, int I, float &P, float &N) {
+  const float iSm2 = tb<UNI>(fa, tab, ax, T_IDS, I - 2), iSm1 = tb<UNI>(fa, tab, ax, T_IDS, I - 1),
+              iS0 = tb<UNI>(fa, tab, ax, T_IDS, I), iS1 = tb<UNI>(fa, tab, ax, T_IDS, I + 1);
+  P = 0.5f * (c + p) - (Up > 0.0f ? tb<UNI>(fa, tab, ax, T_BP1, I) * ((p - c) * iS0 - (c - n) * iSm1)
+                                  : tb<UNI>(fa, tab, ax, T_BP2, I) * ((pp - p) * iS1 - (p - c) * iS0));
+  N = 0.5f * (n + c) - (Un > 0.0f ? tb<UNI>(fa, tab, ax, T_BN1, I) * ((c - n) * iSm1 - (n - nn) * iSm2)
+                                  : tb<UNI>(fa, tab, ax, T_BN2, I) * ((p - c) * iS0 - (c - n) * iSm1));
 }
 
 // The FP32 increment of one staggered component whose own axis is A.  vel[0..2] = the FP32
-// copies of u, v, w.
-template <int A>
-__device__ __forceinline__ float component(const Geo &g, const FastArgs &fa, const float *__restrict__ tab,
-                                           const float *__restrict__ const *vel, long long ic, const int (&I)[3]) {
-  const long long s[3] = {g.sx, g.sy, 1};
+// copies of u, v, w, each already offset to the cell; sx, sy the padded strides (the
+// padded field is below 2^31 entries, so neighbour offsets are 32-bit).
+template <int A, bool UNI>
+__device__ __forceinline__ float component(const FastArgs &fa, const float *__restrict__ tab,
+                                           const float *__restrict__ const *vel, int sx, int sy, const int (&I)[3]) {
+  const int s[3] = {sx, sy, 1};
   const float *phi = vel[A];
-  auto ld = [&](long long q) { return __ldg(phi + q); };
-  const float c = ld(ic);
+  const float c = __ldg(phi);
   float conv = 0.0f, diff = 0.0f;
-  const float IT = tb(tab, fa.L, A, T_IT, I[A]);
+  const float IT = tb<UNI>(fa, tab, A, T_IT, I[A]);
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
-    const long long sb = s[b];
+    const int sb = s[b];
     const int Ib = I[b];
-    const float p = ld(ic + sb), n = ld(ic - sb), pp = ld(ic + 2 * sb), nn = ld(ic - 2 * sb);
+    const float p = __ldg(phi + sb), n = __ldg(phi - sb), pp = __ldg(phi + 2 * sb), nn = __ldg(phi - 2 * sb);
     float P, N;
     if (b == A) {
       const float Up = 0.5f * (p + c), Un = 0.5f * (n + c);
-      qa(Up, Un, pp, p, c, n, nn, tab, fa.L, b, Ib, P, N);
-      conv += (P - N) * (P + N) * tb(tab, fa.L, b, T_IDS, Ib);
-      diff += ((p - c) * tb(tab, fa.L, b, T_ID, Ib + 1) - (c - n) * tb(tab, fa.L, b, T_ID, Ib)) *
-              tb(tab, fa.L, b, T_IDS, Ib);
+      qa<UNI>(Up, Un, pp, p, c, n, nn, fa, tab, b, Ib, P, N);
+      conv += (P - N) * (P + N) * tb<UNI>(fa, tab, b, T_IDS, Ib);
+      diff += ((p - c) * tb<UNI>(fa, tab, b, T_ID, Ib + 1) - (c - n) * tb<UNI>(fa, tab, b, T_ID, Ib)) *
+              tb<UNI>(fa, tab, b, T_IDS, Ib);
     } else {
       // velocity normal to the b-faces of this control volume, interpolated along A
       const float *vb = vel[b];
-      const float b0 = __ldg(vb + ic), bA = __ldg(vb + ic + s[A]);
-      const float bm = __ldg(vb + ic - sb), bmA = __ldg(vb + ic - sb + s[A]);
+      const float b0 = __ldg(vb), bA = __ldg(vb + s[A]);
+      const float bm = __ldg(vb - sb), bmA = __ldg(vb - sb + s[A]);
       const float Bp = b0 + (bA - b0) * IT, Bn = bm + (bmA - bm) * IT;
-      qb(Bp, Bn, pp, p, c, n, nn, tab, fa.L, b, Ib, P, N);
-      conv += (P * Bp - N * Bn) * tb(tab, fa.L, b, T_ID, Ib);
-      diff += ((p - c) * tb(tab, fa.L, b, T_IDS, Ib) - (c - n) * tb(tab, fa.L, b, T_IDS, Ib - 1)) *
-              tb(tab, fa.L, b, T_ID, Ib);
+      qb<UNI>(Bp, Bn, pp, p, c, n, nn, fa, tab, b, Ib, P, N);
+      conv += (P * Bp - N * Bn) * tb<UNI>(fa, tab, b, T_ID, Ib);
+      diff += ((p - c) * tb<UNI>(fa, tab, b, T_IDS, Ib) - (c - n) * tb<UNI>(fa, tab, b, T_IDS, Ib - 1)) *
+              tb<UNI>(fa, tab, b, T_ID, Ib);
     }
   }
   return fa.nu * fa.dt * diff - fa.dt * conv;
@@ -134,6 +142,7 @@ struct CflAccF {
   }
 };
 
+template <bool UNI>
 __global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, double dt_arg, const float *__restrict__ tab,
                                                          const double *__restrict__ u, const double *__restrict__ v,
                                                          const double *__restrict__ w, const float *__restrict__ u32,
@@ -142,7 +151,7 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, dou
                                                          double *__restrict__ ws, StepCtl sc) {
   const double dt = step_dt(sc, dt_arg);
   fa.dt = (float)dt;
-  const float *vel[3] = {u32, v32, w32};
+  const int sx = (int)g.sx, sy = (int)g.sy;
   CflAccF cfl;
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
@@ -150,26 +159,27 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, dou
     row_ijk(g, row, i, j, k);
     const long long ic = pidx(g, i, j, k);
     const int I[3] = {i, j, k};
+    const float *vel[3] = {u32 + ic, v32 + ic, w32 + ic};
     float c = 0.0f;
     if (i < g.nx - 3) {
-      const float d = component<0>(g, fa, tab, vel, ic, I);
+      const float d = component<0, UNI>(fa, tab, vel, sx, sy, I);
       us[ic] = u[ic] + f2d_int(d);
       const float r = u32[ic] + d;
-      c += r * tb(tab, fa.L, 0, T_IDS, i);
+      c += r * tb<UNI>(fa, tab, 0, T_IDS, i);
       cfl.comp(0, r);
     }
     if (j < g.ny - 3) {
-      const float d = component<1>(g, fa, tab, vel, ic, I);
+      const float d = component<1, UNI>(fa, tab, vel, sx, sy, I);
       vs[ic] = v[ic] + f2d_int(d);
       const float r = v32[ic] + d;
-      c += r * tb(tab, fa.L, 1, T_IDS, j);
+      c += r * tb<UNI>(fa, tab, 1, T_IDS, j);
       cfl.comp(1, r);
     }
     if (k < g.nz - 3 + g.pz) {  // periodic z: the top face too
-      const float d = component<2>(g, fa, tab, vel, ic, I);
+      const float d = component<2, UNI>(fa, tab, vel, sx, sy, I);
       ws[ic] = w[ic] + f2d_int(d);
       const float r = w32[ic] + d;
-      c += r * tb(tab, fa.L, 2, T_IDS, k);
+      c += r * tb<UNI>(fa, tab, 2, T_IDS, k);
       cfl.comp(2, r);
     }
     cfl.m[0] = fmaxf(cfl.m[0], c);
@@ -178,6 +188,158 @@ __global__ void __launch_bounds__(kBlock) k_convdiff_f32(Geo g, FastArgs fa, dou
     CflAcc acc;
     for (int q = 0; q < 7; ++q) acc.m[q] = (double)cfl.m[q];
     cfl_finish(acc, dt, sc);
+  }
+}
+
+// ---- transpose of k_convdiff_f32, for the adjoint of a MIXED context ----
+// The FP32 stencil above, transposed with its own FP32 coefficients and upwind branches
+// (the face velocities of the same FP32 copies), so that the adjoint is that of the step
+// the MIXED forward ran.  The identity part of u* = u + increment adds lambda in FP64; the
+// increment's part is computed in FP32 (dt times the stencil: ~0.1 of lambda per step),
+// summed per target in registers and added to the FP64 adjoint fields with one FP64 atomic
+// per target (converted exactly, by integer operations).
+struct Face32 {
+  float c[5];  // coefficients on offsets -2..+2 along the axis (two of them zero)
+  float val;
+};
+__device__ __forceinline__ void face32(Face32 &F, int lo, float c0, float c1, float c2, const float *phi, int sb) {
+#pragma unroll
+  for (int o = 0; o < 5; ++o) F.c[o] = 0.0f;
+  F.c[lo + 2] = c0;
+  F.c[lo + 3] = c1;
+  F.c[lo + 4] = c2;
+  F.val = c0 * __ldg(phi + lo * sb) + c1 * __ldg(phi + (lo + 1) * sb) + c2 * __ldg(phi + (lo + 2) * sb);
+}
+
+template <int A, bool UNI>
+__device__ __forceinline__ void adj_component32(const FastArgs &fa, const float *__restrict__ tab,
+                                                const float *const *vel, double *const *lam, int sx, int sy,
+                                                const int (&I)[3], float L, float (&own)[3]) {
+  const int s[3] = {sx, sy, 1};
+  const float *phi = vel[A];
+  const float gc = -fa.dt * L, h = fa.nu * fa.dt * L;
+  const float IT = tb<UNI>(fa, tab, A, T_IT, I[A]);
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const int sb = s[b], Ib = I[b];
+    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    Face32 P, N;
+    if (b == A) {
+      const float iDm1 = tb<UNI>(fa, tab, b, T_ID, Ib - 1), iD0 = tb<UNI>(fa, tab, b, T_ID, Ib),
+                  iD1 = tb<UNI>(fa, tab, b, T_ID, Ib + 1), iD2 = tb<UNI>(fa, tab, b, T_ID, Ib + 2);
+      const float iS = tb<UNI>(fa, tab, b, T_IDS, Ib);
+      const float ap = iD1 * iS, an = iD0 * iS;  // diffusion
+      acc[3] += h * ap;
+      acc[1] += h * an;
+      acc[2] -= h * (ap + an);
+      const float c = __ldg(phi), Up = 0.5f * (__ldg(phi + sb) + c), Un = 0.5f * (__ldg(phi - sb) + c);
+      if (Up > 0.0f) {
+        const float k = tb<UNI>(fa, tab, b, T_AP1, Ib);
+        face32(P, -1, -k * iD0, 0.5f + k * iD1 + k * iD0, 0.5f - k * iD1, phi, sb);
+      } else {
+        const float k = tb<UNI>(fa, tab, b, T_AP2, Ib);
+        face32(P, 0, 0.5f - k * iD1, 0.5f + k * iD2 + k * iD1, -k * iD2, phi, sb);
+      }
+      if (Un > 0.0f) {
+        const float k = tb<UNI>(fa, tab, b, T_AN1, Ib);
+        face32(N, -2, -k * iDm1, 0.5f + k * iD0 + k * iDm1, 0.5f - k * iD0, phi, sb);
+      } else {
+        const float k = tb<UNI>(fa, tab, b, T_AN2, Ib);
+        face32(N, -1, 0.5f - k * iD0, 0.5f + k * iD1 + k * iD0, -k * iD1, phi, sb);
+      }
+      const float w = gc * iS;  // (P^2 - N^2) / Ds
+      const float wP = w * 2.0f * P.val, wN = -w * 2.0f * N.val;
+#pragma unroll
+      for (int o = 0; o < 5; ++o) acc[o] = fmaf(wP, P.c[o], fmaf(wN, N.c[o], acc[o]));
+    } else {
+      const float iSm2 = tb<UNI>(fa, tab, b, T_IDS, Ib - 2), iSm1 = tb<UNI>(fa, tab, b, T_IDS, Ib - 1),
+                  iS0 = tb<UNI>(fa, tab, b, T_IDS, Ib), iS1 = tb<UNI>(fa, tab, b, T_IDS, Ib + 1);
+      const float iD = tb<UNI>(fa, tab, b, T_ID, Ib);
+      const float ap = iS0 * iD, an = iSm1 * iD;  // diffusion
+      acc[3] += h * ap;
+      acc[1] += h * an;
+      acc[2] -= h * (ap + an);
+      const float *vb = vel[b];
+      const int sA = s[A];
+      const float b0 = __ldg(vb), bA = __ldg(vb + sA), bm = __ldg(vb - sb), bmA = __ldg(vb - sb + sA);
+      const float Bp = b0 + (bA - b0) * IT, Bn = bm + (bmA - bm) * IT;
+      if (Bp > 0.0f) {
+        const float k = tb<UNI>(fa, tab, b, T_BP1, Ib);
+        face32(P, -1, -k * iSm1, 0.5f + k * iS0 + k * iSm1, 0.5f - k * iS0, phi, sb);
+      } else {
+        const float k = tb<UNI>(fa, tab, b, T_BP2, Ib);
+        face32(P, 0, 0.5f - k * iS0, 0.5f + k * iS1 + k * iS0, -k * iS1, phi, sb);
+      }
+      if (Bn > 0.0f) {
+        const float k = tb<UNI>(fa, tab, b, T_BN1, Ib);
+        face32(N, -2, -k * iSm2, 0.5f + k * iSm1 + k * iSm2, 0.5f - k * iSm1, phi, sb);
+      } else {
+        const float k = tb<UNI>(fa, tab, b, T_BN2, Ib);
+        face32(N, -1, 0.5f - k * iSm1, 0.5f + k * iS0 + k * iSm1, -k * iS0, phi, sb);
+      }
+      const float w = gc * iD;  // (P Bp - N Bn) / D
+      const float wP = w * Bp, wN = -w * Bn;
+#pragma unroll
+      for (int o = 0; o < 5; ++o) acc[o] = fmaf(wP, P.c[o], fmaf(wN, N.c[o], acc[o]));
+      const float lBp = w * P.val, lBn = -w * N.val;  // the face velocities, interpolated along A
+      own[b] += (1.0f - IT) * lBp;
+      double *lvb = lam[b];
+      atomicAdd(lvb + sA, f2d_int(IT * lBp));
+      atomicAdd(lvb - sb, f2d_int((1.0f - IT) * lBn));
+      atomicAdd(lvb - sb + sA, f2d_int(IT * lBn));
+    }
+    own[A] += acc[2];
+#pragma unroll
+    for (int o = 0; o < 5; ++o)
+      if (o != 2 && acc[o] != 0.0f) atomicAdd(lam[A] + (o - 2) * sb, f2d_int(acc[o]));
+  }
+}
+
+template <bool UNI>
+__global__ void __launch_bounds__(kBlock) k_adj_convdiff_f32(Geo g, FastArgs fa, const float *__restrict__ tab,
+                                                             const float *__restrict__ u32,
+                                                             const float *__restrict__ v32,
+                                                             const float *__restrict__ w32,
+                                                             const double *__restrict__ lus,
+                                                             const double *__restrict__ lvs,
+                                                             const double *__restrict__ lws, double *lu, double *lv,
+                                                             double *lw) {
+  const int sx = (int)g.sx, sy = (int)g.sy;
+  for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
+       row += (long long)gridDim.x * kBlock) {
+    int i, j, k;
+    row_ijk(g, row, i, j, k);
+    const long long c = pidx(g, i, j, k);
+    const int I[3] = {i, j, k};
+    const float *vel[3] = {u32 + c, v32 + c, w32 + c};
+    double *lam[3] = {lu + c, lv + c, lw + c};
+    const double L64[3] = {i < g.nx - 3 ? lus[c] : 0.0, j < g.ny - 3 ? lvs[c] : 0.0,
+                           k < g.nz - 3 + g.pz ? lws[c] : 0.0};
+    float own[3] = {0.0f, 0.0f, 0.0f};
+    if (L64[0] != 0.0) adj_component32<0, UNI>(fa, tab, vel, lam, sx, sy, I, d2f_int(L64[0]), own);
+    if (L64[1] != 0.0) adj_component32<1, UNI>(fa, tab, vel, lam, sx, sy, I, d2f_int(L64[1]), own);
+    if (L64[2] != 0.0) adj_component32<2, UNI>(fa, tab, vel, lam, sx, sy, I, d2f_int(L64[2]), own);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double t = L64[a] + f2d_int(own[a]);  // u*_c = u_c + ...: lambda in FP64
+      if (t != 0.0) atomicAdd(lam[a], t);
+    }
+  }
+}
+
+void launch_adj_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, const float *uni, double dt,
+                             double nu, const float *u32, const float *v32, const float *w32, const double *lus,
+                             const double *lvs, const double *lws, double *lu, double *lv, double *lw) {
+  FastArgs fa{};
+  fa.L = (g.nx > g.ny ? (g.nx > g.nz ? g.nx : g.nz) : (g.ny > g.nz ? g.ny : g.nz)) + 1;
+  fa.dt = (float)dt;
+  fa.nu = (float)nu;
+  if (uni) {
+    for (int a = 0; a < 3; ++a)
+      for (int r = 0; r < T_NROW; ++r) fa.uni[a][r] = uni[a * T_NROW + r];
+    k_adj_convdiff_f32<true><<<nblk, kBlock, 0, s>>>(g, fa, tab, u32, v32, w32, lus, lvs, lws, lu, lv, lw);
+  } else {
+    k_adj_convdiff_f32<false><<<nblk, kBlock, 0, s>>>(g, fa, tab, u32, v32, w32, lus, lvs, lws, lu, lv, lw);
   }
 }
 
@@ -194,6 +356,8 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
   const double dt = dtp ? *dtp : dt_arg;
   const double rdt = 1.0 / dt;
   auto nonzero = [](double e) { return (__double_as_longlong(e) << 1) != 0; };  // +-0 is zero
+  // -dt / Ds per axis: once per thread on a uniform grid (the same product at every index)
+  const double gx = -(dt * g.rDxs[2]), gy = -(dt * g.rDys[2]), gz = -(dt * g.rDzs[2]);
   double acc[2] = {0.0, 0.0};
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
@@ -204,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     const bool bc = nonzero(ec);
     if (i < g.nx - 3) {
       const long long icP = ic + g.sx;
-      const double T2 = fma(-(dt * g.rDxs[i]), p[icP] - p[ic], us[ic]);
+      const double T2 = fma(g.uni ? gx : -(dt * g.rDxs[i]), p[icP] - p[ic], us[ic]);
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
@@ -218,7 +382,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     }
     if (j < g.ny - 3) {
       const long long icP = ic + g.sy;
-      const double T2 = fma(-(dt * g.rDys[j]), p[icP] - p[ic], vs[ic]);
+      const double T2 = fma(g.uni ? gy : -(dt * g.rDys[j]), p[icP] - p[ic], vs[ic]);
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
@@ -232,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     }
     if (k < g.nz - 3 + g.pz) {  // periodic z: the top face, its upper cell the first one
       const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
-      const double T2 = fma(-(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
+      const double T2 = fma(g.uni ? gz : -(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
       const double en = eta[icP];
       w3[ic] = (bc || nonzero(en)) ? (1.0 - fma(en - ec, g.hfz[k], ec)) * T2 : T2;
     } else if (wi) {
@@ -274,14 +438,20 @@ void launch_rhs_fast(cudaStream_t s, int nblk, const Geo &g, double dt, const do
   k_rhs_fast<<<nblk, kBlock, 0, s>>>(g, dt, dtp, us, vs, ws, jacobi, st, b);
 }
 
-void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, double dt, double nu,
-                         const double *u, const double *v, const double *w, const float *u32, const float *v32,
-                         const float *w32, double *us, double *vs, double *ws, const StepCtl &sc) {
-  FastArgs fa;
+void launch_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float *tab, const float *uni, double dt,
+                         double nu, const double *u, const double *v, const double *w, const float *u32,
+                         const float *v32, const float *w32, double *us, double *vs, double *ws, const StepCtl &sc) {
+  FastArgs fa{};
   fa.L = (g.nx > g.ny ? (g.nx > g.nz ? g.nx : g.nz) : (g.ny > g.nz ? g.ny : g.nz)) + 1;
   fa.dt = (float)dt;
   fa.nu = (float)nu;
-  k_convdiff_f32<<<nblk, kBlock, 0, s>>>(g, fa, dt, tab, u, v, w, u32, v32, w32, us, vs, ws, sc);
+  if (uni) {
+    for (int a = 0; a < 3; ++a)
+      for (int r = 0; r < T_NROW; ++r) fa.uni[a][r] = uni[a * T_NROW + r];
+    k_convdiff_f32<true><<<nblk, kBlock, 0, s>>>(g, fa, dt, tab, u, v, w, u32, v32, w32, us, vs, ws, sc);
+  } else {
+    k_convdiff_f32<false><<<nblk, kBlock, 0, s>>>(g, fa, dt, tab, u, v, w, u32, v32, w32, us, vs, ws, sc);
+  }
 }
 
 void launch_mirror32(cudaStream_t s, const Geo &g, const double *u, const double *v, const double *w, float *u32,

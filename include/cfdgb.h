@@ -238,11 +238,14 @@ int cfdgb_step(cfdgb_ctx *ctx, int nsteps, cfdgb_step_stats *stats);
  * the steps in reverse, recomputing each checkpoint window forward first (in the context's
  * precision), and returns dJ/d(inlet u profile) (ny*nz values, the inlet ghost value of
  * BC_staggered_main's face 0 per (j,k)) and dJ/d(solid fraction eta) (padded field).  The
- * transposed Poisson solve is FP64 BiCGSTAB, preconditioned by the FP64 V-cycle when the
- * context has the multigrid preconditioner.  Memory beyond the forward's: per checkpoint
- * u, v, w (padded FP64) and the solver's warm start (compact; p is rebuilt from it), plus
- * p for the first; per window step u, v, w (padded FP64) and p (padded FP32); about 14
- * padded FP64 fields and 9 compact ones of adjoint state. */
+ * transposed Poisson solve (the operator is symmetric on the uniform grid) is the
+ * context's own: FP64 BiCGSTAB (preconditioned by the FP64 V-cycle when the context has
+ * the multigrid preconditioner), or for a MIXED context the same FP32 sweeps in FP64
+ * refinement as its forward solves, to the same FP64 tolerance.  Memory beyond the
+ * forward's: per checkpoint u, v, w (padded FP64) and the solver's warm start (compact; p
+ * is rebuilt from it), plus p for the first; per window step u, v, w (padded FP64) and p
+ * (padded FP32); about 14 padded FP64 fields of adjoint state, and 1 compact one (MIXED)
+ * or 9 (FP64). */
 typedef struct cfdgb_objective {
   int nsteps;      /* forward steps */
   int first, last; /* drag averaged over these steps (1-based, inclusive) */

@@ -144,10 +144,10 @@ def test_free_slip_walls_gradients_match_central_fd():
                          ids=["fp64_multigrid", "mixed_multigrid", "mixed_cg"])
 def test_adjoint_of_other_contexts_matches_fp64(adj, kw):
     """The adjoint from a context whose forward runs the multigrid-preconditioned FP64
-    solver, or MIXED precision (FP32 sweeps in FP64 refinement; the transposed solve stays
-    FP64, with the FP64 V-cycle where the context has the multigrid preconditioner): the
+    solver (its transposed solve with the FP64 V-cycle), or MIXED precision (FP32 sweeps in
+    FP64 refinement, forward and transposed solves alike, to the same FP64 tolerance): the
     same objective and gradients as the plain FP64 context's, which the finite-difference
-    tests above check.  The MIXED forward differs from FP64 by its FP32 rounding."""
+    tests above check.  The MIXED runs differ from FP64 by their FP32 rounding."""
     s0, eta0, J0, g_in0, g_eta0 = adj
     with cg.Solver(tol=TOL, project_rhs=PROJECT, **kw, **CASE) as s:
         s.set_inlet(None)
