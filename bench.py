@@ -157,6 +157,44 @@ def alu_roofline(prof, cells, fp_peak):
             "peak_kind": "measured (bench_fp_peak FMA chains)"}
 
 
+# The MIXED step's kernels beside the Krylov sweeps: algorithmic bytes per interior cell
+# and launch (one word per array read or written, neighbours cached) and the FP64
+# instructions per cell counted in their source (an FMA is one instruction).  Each is set
+# against the HBM peak and the measured FP64 instruction rate; the larger fraction names
+# its bound.  correct64 pairs two launches (the correction's mean, then x += e).
+STEP_KERNELS = {
+    "convection_diffusion": (60, 3),  # read u32, v32, w32 (FP32) and u, v, w; write us, vs, ws; 3 DADD
+    "update_uf": (64, 6),             # read eta, p, us, vs, ws; write u, v, w; 3 DADD + 3 DFMA (uniform grid)
+    "rhs": (32, 8),                   # read us, vs, ws; write b
+    "residual64": (24, 9),            # read b, x; write r; 7-point stencil, subtraction, norm
+    "correct64": (24, 2),             # read e (mean), then x, e; write x
+    "mirror32": (36, 0),              # read u, v, w; write u32, v32, w32 (integer rounding; padded fields)
+}
+
+
+def step_roofline(prof, cells, npad, hbm_peak, fp_peak):
+    """Per MIXED step kernel: average launch, achieved GB/s and FP64 instruction rate, each
+    as a fraction of its peak, and the bound the larger one names."""
+    f64 = (fp_peak or {}).get("fp64_tflops")
+    inst_peak = f64 * 1e12 / 2 if f64 else None  # FMA instructions per second
+    out = {}
+    for k, (bpc, fpc) in STEP_KERNELS.items():
+        ms, n = prof.get(k, (0.0, 0))
+        if not n or ms <= 0:
+            continue
+        n = n / 2 if k == "correct64" else n
+        per = ms / n / 1e3
+        units = npad if k == "mirror32" else cells
+        gbs = bpc * units / per / 1e9
+        hf = gbs / hbm_peak
+        ff = fpc * cells / per / inst_peak if inst_peak else None
+        out[k] = {"avg_launch_us": round(per * 1e6, 2), "launches": n, "achieved_gbs": round(gbs, 1),
+                  "hbm_frac": round(hf, 4), "fp64_inst_per_cell": fpc,
+                  "fp64_frac": round(ff, 4) if ff is not None else None,
+                  "bound": "fp64" if ff is not None and ff > hf else "hbm"}
+    return out
+
+
 def peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -317,9 +355,9 @@ def adjoint_mode(cg, torch, dist, nsteps, ckpt, wl="c4", first=0, precision="fp6
     """Forward run with checkpoints and the adjoint sweep (gradient of the drag averaged
     over the last third of the window, or from step `first`, w.r.t. the inlet profile and
     eta) on the adjoint case; returns both wall times (CUDA events on the library's stream)
-    and their ratio.  precision/solver/precond: the forward's (MIXED: FP32 sweeps in FP64
-    refinement; the transposed solve stays FP64, with the FP64 V-cycle under precond
-    multigrid)."""
+    and their ratio.  precision/solver/precond: the forward's; the backward recomputes and
+    solves as the forward does (MIXED: FP32 sweeps in FP64 refinement, the FP32 stencil's
+    transpose; FP64 multigrid: the FP64 V-cycle)."""
     cfg = dict(WORKLOADS[wl])
     with cg.Solver(solver=solver, precision=precision, precond=precond, tol=TOL, **cfg) as s:
         stream = torch.cuda.ExternalStream(s.stream)
@@ -451,6 +489,9 @@ MODES = {
 PRECISION_PAIR = {"mixed": "fp64", "mixed_cg": "cg", "mixed_mg": "fp64_mg"}
 
 
+FP_PEAK_CACHE = {}  # the measured FMA rates of this run (alu_peaks), for step_roofline
+
+
 def measure_mode(cg, torch, dist, wl, key, steps, warmup, maxit, fp64, t64, hbm_peak, peak_kind, traffic_file,
                  keep_fields=True, profile=True):
     """One mode of MODES on the workload: its timed window, solve record, errors against the
@@ -472,6 +513,10 @@ def measure_mode(cg, torch, dist, wl, key, steps, warmup, maxit, fp64, t64, hbm_
         word, suffix = (4, "32") if prec == "mixed" else (8, "64")
         out["roofline"], out["kernel_share"] = roofline(rm["kernels"], cells, word, suffix, hbm_peak, peak_kind,
                                                         traffic_file)
+        if prec == "mixed":
+            c = WORKLOADS[wl]
+            npad = (c["nx"] + 4) * (c["ny"] + 4) * (c["nz"] + 4)
+            out["step_kernels"] = step_roofline(rm["kernels"], cells, npad, hbm_peak, FP_PEAK_CACHE.get("peaks"))
     rm.pop("fields", None)
     return out, rm
 
@@ -777,6 +822,7 @@ def main(argv=None):
     traffic_file = ROOT / "profiles" / f"traffic_{wl}.json"
 
     fp_peak = alu_peaks()
+    FP_PEAK_CACHE["peaks"] = fp_peak
     with Clocks(dist.local) as clk:
         fp64 = run_mode(cg, torch, dist, wl, args.steps, args.warmup, None, "fp64", maxit=args.maxit,
                         keep_fields=bool(modes & set(MODES)))
@@ -834,6 +880,15 @@ def main(argv=None):
                                            args.adj_first, args.adj_precision, args.adj_solver, args.adj_precond)
         except cg.CfdgbError as e:
             line["adjoint"] = {"value": None, "error": str(e)}
+        if (args.adj_precision, args.adj_precond) != ("mixed", "multigrid"):
+            # the 1536x768x96 case's recipe (MIXED multigrid forward, then the adjoint) on the
+            # adjoint case's grid
+            try:
+                line["adjoint"]["mixed_multigrid"] = adjoint_mode(cg, torch, dist, args.adj_steps, args.adj_ckpt,
+                                                                  args.adj_workload, args.adj_first, "mixed",
+                                                                  args.adj_solver, "multigrid")
+            except cg.CfdgbError as e:
+                line["adjoint"]["mixed_multigrid"] = {"error": str(e)}
     if "adjoint_fd" in modes:  # not in the default modes: ~4 * fd_dirs forward runs
         try:
             line["adjoint_fd"] = adjoint_fd_mode(cg, args.fd_steps, args.adj_ckpt, args.fd_dirs)

@@ -1350,9 +1350,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   g.lgz = std::max(1, std::min(cfg->nx, c->nsm * 8 / std::max(1, g.lgx * g.lgy)));
   int nblk3 = g.lgx * g.lgy * g.lgz;
   // vectorised FP32 kernels: quads of four k cells per thread when nz % 4 == 0
-  // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows, and
-  // so does periodic z, whose wrapped neighbours the quad and bulk-copy kernels do not read)
-  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML && !g.pz) {
+  // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows)
+  if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML) {
     const int nq = cfg->nz / 4;
     g.vbx = 1;
     while (g.vbx < nq && g.vbx < 32) g.vbx *= 2;

@@ -607,8 +607,11 @@ __device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &
   const int i0 = min(g.nxc, (int)blockIdx.z * chunk), i1 = min(g.nxc, i0 + chunk);
   const long long nyz = (long long)g.nyc * g.nzc;
   const bool hy0 = jc > 0, hy1 = jc + 1 < g.nyc;
-  const bool kl = kc0 > 0, kr = kc0 + 4 < g.nzc;                       // cells left / right exist
-  const bool sl = threadIdx.x > 0, sr = threadIdx.x + 1 < blockDim.x;  // ... and are in this warp
+  // cells left / right exist (periodic z: always, across the wrap at the line's ends)...
+  const bool kl = kc0 > 0 || g.pz, kr = kc0 + 4 < g.nzc || g.pz;
+  // ... and are held by the neighbouring lane (within the line)
+  const bool sl = threadIdx.x > 0 && kc0 > 0, sr = threadIdx.x + 1 < blockDim.x && kc0 + 4 < g.nzc;
+  const long long wl = kc0 > 0 ? -1 : g.nzc - 1, wr = kc0 + 4 < g.nzc ? 4 : 4 - g.nzc;  // their offsets
   long long row = ((long long)i0 * g.nyc + jc) * g.nzc + kc0;
   F4 fm{}, fc{};
   if (on && i0 < i1) {
@@ -624,12 +627,12 @@ __device__ __forceinline__ void march_quads(const Geo &g, const Stencil<float> &
     }
     const float l = __shfl_up_sync(0xffffffffu, fc.v[3], 1);
     const float r = __shfl_down_sync(0xffffffffu, fc.v[0], 1);
-    const float zl = !kl ? 0.0f : (sl ? l : (on ? f1(row - 1) : 0.0f));
-    const float zr = !kr ? 0.0f : (sr ? r : (on ? f1(row + 4) : 0.0f));
+    const float zl = !kl ? 0.0f : (sl ? l : (on ? f1(row + wl) : 0.0f));
+    const float zr = !kr ? 0.0f : (sr ? r : (on ? f1(row + wr) : 0.0f));
     // difference form (stencil_apply_diff); a missing neighbour has coefficient 0
     const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
-    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 ? 0 : 1)],
-                *clast = st.c[cxy + (kc0 + 4 == g.nzc ? 2 : 1)];
+    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 && !g.pz ? 0 : 1)],
+                *clast = st.c[cxy + (kc0 + 4 == g.nzc && !g.pz ? 2 : 1)];
     F4 y;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -1025,11 +1028,16 @@ __device__ __forceinline__ void tma_march(const Geo &g, const Stencil<float> &st
     }
     const float l = __shfl_up_sync(0xffffffffu, fc.v[3], 1);
     const float r = __shfl_down_sync(0xffffffffu, fc.v[0], 1);
-    const float zl = tq == 0 ? 0.0f : (lane > 0 ? l : (on ? f1(arr, own, kc0 - 1) : 0.0f));
-    const float zr = tq == nq - 1 ? 0.0f : (lane < 31 ? r : (on ? f1(arr, own, kc0 + 4) : 0.0f));
+    // the cells left and right of the quad: from the neighbouring lane within the row, from
+    // the stage at a warp's edge, across the wrap at the row's ends (periodic z), else none
+    const float zl = (tq == 0 && !g.pz) ? 0.0f
+                                       : ((lane > 0 && tq > 0) ? l : (on ? f1(arr, own, tq > 0 ? kc0 - 1 : nz - 1) : 0.0f));
+    const float zr = (tq == nq - 1 && !g.pz)
+                         ? 0.0f
+                         : ((lane < 31 && tq < nq - 1) ? r : (on ? f1(arr, own, tq < nq - 1 ? kc0 + 4 : 0) : 0.0f));
     const int cxy = axis_class(ic, g.nxc) * 9 + axis_class(jc, g.nyc) * 3;
-    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 ? 0 : 1)],
-                *clast = st.c[cxy + (kc0 + 4 == nz ? 2 : 1)];
+    const float *cmid = st.c[cxy + 1], *cfirst = st.c[cxy + (kc0 == 0 && !g.pz ? 0 : 1)],
+                *clast = st.c[cxy + (kc0 + 4 == nz && !g.pz ? 2 : 1)];
     F4 y;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {

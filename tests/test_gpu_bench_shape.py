@@ -20,6 +20,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 CASE = dict(nx=128, ny=64, nz=64, lx=8.0, ly=4.0, lz=4.0, cx=2.0, cy=2.0, Re=200.0, dt=0.002)
+BSET = dict(walls="free_slip", bc_z="periodic", outflow="convective")
 STEPS = 3
 
 
@@ -58,6 +59,38 @@ def test_fp64_matches_oracle_at_nz64(fp64_run):
     # iteration counts: two correct solvers near the rounding floor agree to a few percent
     it, rit = np.array([r.iters for r in st]), np.asarray(ref["iters"])
     assert np.all(np.abs(it[1:] - rit[1:]) <= 0.1 * rit[1:]), (it, rit)
+
+
+@pytest.fixture(scope="module")
+def fp64_set_run():
+    with cg.Solver(solver="jacobi", tol=1e-12, amp=1e-3, seed=5, **BSET, **CASE) as s:
+        s.init_fields()
+        st = s.step(STEPS)
+        f = s.get_fields()
+    return st, f
+
+
+@pytest.mark.parametrize("kw", [dict(solver="jacobi"), dict(solver="cg"),
+                                dict(solver="jacobi", precond="multigrid")],
+                         ids=["bicgstab", "cg", "multigrid"])
+def test_mixed_paths_on_the_boundary_set_at_nz64(fp64_set_run, kw):
+    """The boundary set (convective outflow, free-slip walls, periodic z) at this shape: the
+    bulk-copy and quad kernels take the cells across the wrap at each line's ends (16 quads
+    a line, two lines a warp).  Every FP64 solve reaches 1e-12 (the flux-corrected problem
+    is consistent); the MIXED runs end below 1e-10 and agree with FP64 as above."""
+    st64, f64 = fp64_set_run
+    assert [r.status for r in st64] == [0] * STEPS
+    assert all(r.relres < 1e-12 for r in st64[1:]), [r.relres for r in st64]
+    with cg.Solver(precision="mixed", tol=1e-10, amp=1e-3, seed=5, **kw, **BSET, **CASE) as s:
+        s.init_fields()
+        st = s.step(STEPS)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * STEPS
+    assert all(r.relres < 1e-10 for r in st[1:]), [r.relres for r in st]
+    for k, e in vel_err(f, f64).items():
+        assert e <= 1e-8, (kw, k, e)
+    assert p_err(f["p"], f64["p"]) <= 1e-6, kw
+    np.testing.assert_allclose([r.cd for r in st], [r.cd for r in st64], rtol=1e-8)
 
 
 @pytest.mark.parametrize("kw", [dict(solver="jacobi"), dict(solver="cg"),

@@ -10,8 +10,9 @@ to 1e-15 (its flux correction sums on the GPU in another order), whole runs with
 tol 1e-12 through the step graphs, the FP32+FP64-refined paths within 1e-8 of FP64, and
 every solve consistent (the corrected net flux is zero, so each one reaches 1e-12).
 
-The grid has nz = 8 so that, without periodic z, the MIXED sweeps would run their quad
-and bulk-copy kernels: periodic z must select the scalar ones, whose z neighbours wrap."""
+The grid has nz = 8, so the MIXED sweeps run their quad and bulk-copy kernels (and the
+V-cycle its quad smoother), which take the cells across the wrap at each line's ends;
+tests/test_gpu_bench_shape.py runs the same at nz = 64."""
 import numpy as np
 import pytest
 
