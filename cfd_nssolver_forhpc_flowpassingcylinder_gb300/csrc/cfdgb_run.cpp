@@ -17,10 +17,15 @@
 //             [restart=<file.q>: start from a Plot3D solution file of this grid (QfileRead,
 //              the restart the reference leaves commented out at src/RUN_CPU.cpp:88-99);
 //              the simulated time continues from the file's header]
+//             [adjoint=first:last:ckpt: instead of the step loop, cfdgb_forward over `steps`
+//              steps (drag averaged over steps first..last, a checkpoint every ckpt steps)
+//              and cfdgb_backward; prints J, the gradients' norms and both wall times]
 //
 // Per step it prints the reference's lines ("[SPE (BICG)] iter:...", "[cD, cL] : ...")
 // and appends the drag/lift series to <out>/Time_cDcL.dat in the reference's Tecplot
 // layout (inc/dfib/virtualForceIntergrator.hpp:113-145).
+#include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -82,6 +87,30 @@ int main(int argc, char **argv) {
       double head[5];
       cfdgb::check(cfdgb_read_plot3d(ctx.handle(), kv["restart"].c_str(), head));
       time = head[4];
+    }
+    if (kv.count("adjoint")) {  // first:last:ckpt
+      cfdgb_objective obj{};
+      obj.nsteps = steps;
+      if (std::sscanf(kv["adjoint"].c_str(), "%d:%d:%d", &obj.first, &obj.last, &obj.ckpt_every) != 3) {
+        std::fprintf(stderr, "adjoint=first:last:ckpt expected\n");
+        return 2;
+      }
+      double J = 0.0;
+      const auto t0 = std::chrono::steady_clock::now();
+      const int rf = cfdgb_forward(ctx.handle(), &obj, &J);
+      if (rf != CFDGB_OK && rf != CFDGB_ENOCONV) cfdgb::check(rf);
+      const auto t1 = std::chrono::steady_clock::now();
+      std::vector<double> gin((size_t)cfg.ny * cfg.nz), geta((size_t)(cfg.nx + 4) * (cfg.ny + 4) * (cfg.nz + 4));
+      const int rb = cfdgb_backward(ctx.handle(), gin.data(), geta.data());
+      if (rb != CFDGB_OK && rb != CFDGB_ENOCONV) cfdgb::check(rb);
+      const auto t2 = std::chrono::steady_clock::now();
+      double ni = 0.0, ne = 0.0;
+      for (double x : gin) ni += x * x;
+      for (double x : geta) ne += x * x;
+      const double tf = std::chrono::duration<double>(t1 - t0).count(), tb = std::chrono::duration<double>(t2 - t1).count();
+      std::printf("J %.12g |dJ/dinlet| %.9g |dJ/deta| %.9g forward %.3f s backward %.3f s ratio %.3f\n", J,
+                  std::sqrt(ni), std::sqrt(ne), tf, tb, tb / tf);
+      return rf == CFDGB_OK && rb == CFDGB_OK ? 0 : 3;
     }
     mkdir(out.c_str(), 0755);
     FILE *f = std::fopen((out + "/Time_cDcL.dat").c_str(), "w");

@@ -347,6 +347,7 @@ void launch_adj_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float
 // T2 = u* - (dt / Ds) (p+ - p) with the reciprocal metric, and the DFIB fraction, velocity
 // and force only on faces where eta is non-zero on either side (elsewhere u = T2 and the
 // force is zero); drag and lift summed as the exact kernel does.
+template <bool UNI>
 __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     Geo g, double dt_arg, const double *dtp, int step_mode, double lz, const double *__restrict__ eta,
     const double *__restrict__ p, const double *__restrict__ us, const double *__restrict__ vs,
@@ -356,8 +357,13 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
   const double dt = dtp ? *dtp : dt_arg;
   const double rdt = 1.0 / dt;
   auto nonzero = [](double e) { return (__double_as_longlong(e) << 1) != 0; };  // +-0 is zero
-  // -dt / Ds per axis: once per thread on a uniform grid (the same product at every index)
-  const double gx = -(dt * g.rDxs[2]), gy = -(dt * g.rDys[2]), gz = -(dt * g.rDzs[2]);
+  // UNI: -dt / Ds per axis once per thread (a uniform grid: the same product at every index)
+  double gx = 0.0, gy = 0.0, gz = 0.0;
+  if (UNI) {
+    gx = -(dt * g.rDxs[2]);
+    gy = -(dt * g.rDys[2]);
+    gz = -(dt * g.rDzs[2]);
+  }
   double acc[2] = {0.0, 0.0};
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
@@ -368,7 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     const bool bc = nonzero(ec);
     if (i < g.nx - 3) {
       const long long icP = ic + g.sx;
-      const double T2 = fma(g.uni ? gx : -(dt * g.rDxs[i]), p[icP] - p[ic], us[ic]);
+      const double T2 = fma(UNI ? gx : -(dt * g.rDxs[i]), p[icP] - p[ic], us[ic]);
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
@@ -382,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     }
     if (j < g.ny - 3) {
       const long long icP = ic + g.sy;
-      const double T2 = fma(g.uni ? gy : -(dt * g.rDys[j]), p[icP] - p[ic], vs[ic]);
+      const double T2 = fma(UNI ? gy : -(dt * g.rDys[j]), p[icP] - p[ic], vs[ic]);
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     }
     if (k < g.nz - 3 + g.pz) {  // periodic z: the top face, its upper cell the first one
       const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
-      const double T2 = fma(g.uni ? gz : -(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
+      const double T2 = fma(UNI ? gz : -(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
       const double en = eta[icP];
       w3[ic] = (bc || nonzero(en)) ? (1.0 - fma(en - ec, g.hfz[k], ec)) * T2 : T2;
     } else if (wi) {
@@ -468,8 +474,12 @@ void launch_update_uf_fast(cudaStream_t s, int nblk, const Geo &g, double dt, co
                            double lz, const double *eta, const double *p, const double *us, const double *vs,
                            const double *ws, double *u3, double *v3, double *w3, const double *ui, const double *vi,
                            const double *wi, double *part, StepScal *ss) {
-  k_update_uf_fast<<<nblk, kBlock, 0, s>>>(g, dt, dtp, step_mode, lz, eta, p, us, vs, ws, u3, v3, w3, ui, vi, wi,
-                                           part, ss);
+  if (g.uni)
+    k_update_uf_fast<true><<<nblk, kBlock, 0, s>>>(g, dt, dtp, step_mode, lz, eta, p, us, vs, ws, u3, v3, w3, ui, vi,
+                                                   wi, part, ss);
+  else
+    k_update_uf_fast<false><<<nblk, kBlock, 0, s>>>(g, dt, dtp, step_mode, lz, eta, p, us, vs, ws, u3, v3, w3, ui,
+                                                    vi, wi, part, ss);
 }
 
 }  // namespace cfdgb
