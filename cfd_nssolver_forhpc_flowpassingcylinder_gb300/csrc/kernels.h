@@ -170,7 +170,8 @@ struct MgLevelT {
   int fx, fy, fz;          // cells of this level per cell of the next one, per axis (1, 2)
   T *x, *b;                // correction and right-hand side (levels >= 1)
   int bx, by, gx, gy, gz;  // launch geometry: bx along k, by along j, gz planes strided over i
-  int qgrid;               // blocks of the quad smoother (FP32, nz % 4 == 0), 0: the scalar one
+  int qgrid;               // 1: the quad smoother (FP32, nz % 4 == 0), 0: the scalar one
+  int qbx, qby, qgx, qgy, qgz;  // its launch: quads along x, rows along y, planes strided over z
   int pz;                  // periodic z (every level; nz even or 1 on each)
   // 1/diag of a row by its neighbour counts along x, y, z (each 0..2): idg[9 cx + 3 cy + cz]
   // (0 where a row has no neighbour); the smoother multiplies instead of dividing

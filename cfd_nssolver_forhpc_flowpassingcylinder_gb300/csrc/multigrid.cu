@@ -97,17 +97,27 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevelT<T> L, int colour,
 // The same colour pass on quads of four consecutive k cells (nz % 4 == 0): a thread updates
 // the two cells of the colour in its quad and stores the whole quad, the other two
 // unchanged (no thread writes them in this pass, so rewriting them races with nothing).
-// Neighbour sums in the order of lnb.
+// 3-D launch (quads along x, rows along y, planes strided over z: no index division), the
+// row's neighbour counts along x and y taken once per quad.  Neighbour sums in the order
+// of lnb, diagonals as ldiag / linv form them.
 __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, int zero, int bscale,
                                                        const float *__restrict__ b, float *x, const SolverScal *sc) {
   if (sc->done) return;
-  const unsigned nq = (unsigned)L.nz >> 2, nquads = (unsigned)L.nx * L.ny * nq;
+  const int kq = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (kq >= (L.nz >> 2) || j >= L.ny) return;  // no barrier below
   const long long sx = (long long)L.ny * L.nz;
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nquads; q += gridDim.x * blockDim.x) {
-    const unsigned t = q / nq, kq = q - t * nq, j = t % (unsigned)L.ny, i = t / (unsigned)L.ny;
-    const int k0 = (int)(4 * kq);
-    const long long r = lrow(L, (int)i, (int)j, k0);
-    const int t0 = ((int)i + (int)j + k0 + colour) & 1;  // first cell of the colour in the quad
+  const int k0 = 4 * kq;
+  const bool jm = j > 0, jp = j < L.ny - 1;
+  const int cy = (int)jm + (int)jp;
+  int cz[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) cz[c] = zcount(L, k0 + c);
+  for (int i = blockIdx.z; i < L.nx; i += gridDim.z) {
+    const long long r = lrow(L, i, j, k0);
+    const bool im = i > 0, ip = i < L.nx - 1;
+    const int cx = (int)im + (int)ip, cxy = 9 * cx + 3 * cy;
+    const float dxy = L.wx * (float)cx + L.wy * (float)cy;  // ldiag's first two terms, in its order
+    const int t0 = (i + j + k0 + colour) & 1;  // first cell of the colour in the quad
     const float4 bq = *reinterpret_cast<const float4 *>(b + r);
     const float bv[4] = {bq.x, bq.y, bq.z, bq.w};
     float o[4];
@@ -118,13 +128,12 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
           o[c] = 0.f;
           continue;
         }
-        const float bb = bscale ? bv[c] * ldiag(L, (int)i, (int)j, k0 + c) : bv[c];
-        o[c] = bb * linv(L, (int)i, (int)j, k0 + c);
+        const float bb = bscale ? bv[c] * (dxy + L.wz * (float)cz[c]) : bv[c];
+        o[c] = bb * L.idg[cxy + cz[c]];
       }
     } else {
       const float4 xq = *reinterpret_cast<const float4 *>(x + r);
       const float xv[4] = {xq.x, xq.y, xq.z, xq.w};
-      const bool im = i > 0, ip = (int)i < L.nx - 1, jm = j > 0, jp = (int)j < L.ny - 1;
       const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
       const float4 xm = im ? *reinterpret_cast<const float4 *>(x + r - sx) : z4;
       const float4 xp = ip ? *reinterpret_cast<const float4 *>(x + r + sx) : z4;
@@ -147,8 +156,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
         if (jp) e += ypv[c];
         if (k > 0 || L.pz) f += c == 0 ? kl : xv[c - 1];
         if (k < L.nz - 1 || L.pz) f += c == 3 ? kr : xv[c + 1];
-        const float bb = bscale ? bv[c] * ldiag(L, (int)i, (int)j, k) : bv[c];
-        o[c] = (bb + (L.wx * a + L.wy * e + L.wz * f)) * linv(L, (int)i, (int)j, k);
+        const float bb = bscale ? bv[c] * (dxy + L.wz * (float)cz[c]) : bv[c];
+        o[c] = (bb + (L.wx * a + L.wy * e + L.wz * f)) * L.idg[cxy + cz[c]];
       }
     }
     *reinterpret_cast<float4 *>(x + r) = make_float4(o[0], o[1], o[2], o[3]);
@@ -521,11 +530,17 @@ static void level_geometry(MgLevelT<T> &L, int nsm, bool quads) {
   L.gx = (L.nz + L.bx - 1) / L.bx;
   L.gy = (L.ny + L.by - 1) / L.by;
   L.gz = std::max(1, std::min(L.nx, nsm * 8 / std::max(1, L.gx * L.gy)));
-  const long long nquads = (long long)L.nx * L.ny * (L.nz / 4);
-  // the quad smoother is FP32 (float4 loads)
-  L.qgrid = quads && sizeof(T) == sizeof(float) && L.nz % 4 == 0
-                ? (int)std::max(1LL, std::min((nquads + kBlock - 1) / kBlock, 8LL * nsm))
-                : 0;
+  // the quad smoother is FP32 (float4 loads): quads along x, rows along y, planes over z
+  L.qgrid = quads && sizeof(T) == sizeof(float) && L.nz % 4 == 0 ? 1 : 0;
+  if (L.qgrid) {
+    const int nq = L.nz / 4;
+    L.qbx = 1;
+    while (L.qbx < nq && L.qbx < 32) L.qbx *= 2;
+    L.qby = kBlock / L.qbx;
+    L.qgx = (nq + L.qbx - 1) / L.qbx;
+    L.qgy = (L.ny + L.qby - 1) / L.qby;
+    L.qgz = std::max(1, std::min(L.nx, nsm * 8 / std::max(1, L.qgx * L.qgy)));
+  }
 }
 
 template <typename T>
@@ -670,7 +685,9 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
   auto smooth = [&](int l, int colour, int zero) {
     if constexpr (sizeof(T) == sizeof(float)) {
       if (mg.lev[l].qgrid > 0) {
-        k_mg_smooth4<<<mg.lev[l].qgrid, kBlock, 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+        const MgLevelT<T> &Q = mg.lev[l];
+        k_mg_smooth4<<<dim3(Q.qgx, Q.qgy, Q.qgz), dim3(Q.qbx, Q.qby, 1), 0, s>>>(Q, colour, zero, l == 0 ? jacobi : 0,
+                                                                               B(l), X(l), sc);
         return;
       }
     }
