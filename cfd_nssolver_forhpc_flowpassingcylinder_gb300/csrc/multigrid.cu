@@ -16,12 +16,36 @@
 // has stopped.
 #include <algorithm>
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "cfdgb_internal.cuh"
 #include "kernels.h"
 
 namespace cfdgb {
+
+// Programmatic dependent launch (griddepcontrol): a V-cycle kernel is launched so that it
+// may be scheduled while its predecessor finishes.  It waits for the predecessor's
+// completion and memory (pdl_wait) before reading anything, and lets its successor be
+// scheduled once its own results are stored (pdl_trigger); a block that returns early
+// counts as triggered.  The small levels' kernels are launch-latency-bound.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 #define FOR_LEVEL(L)                                   \
   const int k = blockIdx.x * blockDim.x + threadIdx.x; \
@@ -80,7 +104,9 @@ __device__ __forceinline__ T lnb(const MgLevelT<T> &L, const T *x, int i, int j,
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevelT<T> L, int colour, int zero, int bscale,
                                                       const T *__restrict__ b, T *x, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   FOR_LEVEL(L) {
     const long long r = lrow(L, i, j, k);
     if (((i + j + k) & 1) != colour) {
@@ -102,7 +128,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevelT<T> L, int colour,
 // of lnb, diagonals as ldiag / linv form them.
 __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, int zero, int bscale,
                                                        const float *__restrict__ b, float *x, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   const int kq = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (kq >= (L.nz >> 2) || j >= L.ny) return;  // no barrier below
   const long long sx = (long long)L.ny * L.nz;
@@ -169,7 +197,9 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevelT<T> F, MgLevelT<T> Cl, int bscale,
                                                         const T *__restrict__ bf, const T *__restrict__ xf,
                                                         T *__restrict__ bc, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   const T inv = T(1) / (T)(F.fx * F.fy * F.fz);
   FOR_LEVEL(Cl) {
     T sum = T(0);
@@ -233,7 +263,9 @@ __device__ __forceinline__ T prolong_at(const MgLevelT<T> &F, const MgLevelT<T> 
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevelT<T> F, MgLevelT<T> Cl, const T *__restrict__ xc,
                                                        T *__restrict__ xf, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   FOR_LEVEL(F) {
     xf[lrow(F, i, j, k)] += prolong_at(F, Cl, xc, i, j, k);
   }
@@ -263,7 +295,9 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT<T> Cl, int bscale,
                                                          const T *__restrict__ bf, const T *__restrict__ xf,
                                                          T *__restrict__ bc, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   const T inv = T(1) / T(8);
   const long long sx = (long long)F.ny * F.nz, sy = F.nz;
   FOR_LEVEL(Cl) {
@@ -321,7 +355,9 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mg_prolong8(MgLevelT<T> F, MgLevelT<T> Cl, const T *__restrict__ xc,
                                                         T *__restrict__ xf, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   const long long sx = (long long)F.ny * F.nz, sy = F.nz;
   FOR_LEVEL(Cl) {
     // the 3 x 3 x 3 coarse neighbourhood; beyond a wall the parent's value (axis_taps)
@@ -382,7 +418,9 @@ __device__ void blk_dense(int n, const T *__restrict__ M, const T *bs, T *xs) {
 template <typename T>
 __global__ void __launch_bounds__(1024) k_mg_coarse(MgLevelT<T> L, int sweeps, const T *__restrict__ M, int bscale,
                                                     const T *__restrict__ b, T *__restrict__ x, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smraw[];
   T *sm = reinterpret_cast<T *>(smraw);
   const int n = L.nx * L.ny * L.nz;
@@ -480,7 +518,9 @@ __device__ void blk_prolong(const MgLevelT<T> &F, const MgLevelT<T> &Cl, const T
 // x_t = V-cycle of levels t..nlev-1 on b_t (both in global memory, level t >= 1)
 template <typename T>
 __global__ void __launch_bounds__(1024) k_mg_tail(MgPlanT<T> mg, int t, const SolverScal *sc) {
+  pdl_wait();
   if (sc->done) return;
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smraw[];
   T *sm = reinterpret_cast<T *>(smraw);
   const int n = mg.nlev;
@@ -686,12 +726,12 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
     if constexpr (sizeof(T) == sizeof(float)) {
       if (mg.lev[l].qgrid > 0) {
         const MgLevelT<T> &Q = mg.lev[l];
-        k_mg_smooth4<<<dim3(Q.qgx, Q.qgy, Q.qgz), dim3(Q.qbx, Q.qby, 1), 0, s>>>(Q, colour, zero, l == 0 ? jacobi : 0,
-                                                                               B(l), X(l), sc);
+        launch_pdl(k_mg_smooth4, dim3(Q.qgx, Q.qgy, Q.qgz), dim3(Q.qbx, Q.qby, 1), 0, s, Q, colour, zero,
+                   l == 0 ? jacobi : 0, B(l), X(l), sc);
         return;
       }
     }
-    k_mg_smooth<T><<<grid(l), block(l), 0, s>>>(mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
+    launch_pdl(k_mg_smooth<T>, grid(l), block(l), 0, s, mg.lev[l], colour, zero, l == 0 ? jacobi : 0, B(l), X(l), sc);
   };
   // pre-smoothing from zero and restriction to level l + 1.  (Both colour passes in one
   // kernel, each black cell recomputing its red neighbours' start values, was measured at
@@ -702,9 +742,11 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
     smooth(l, 1, 0);
     const MgLevelT<T> &F = mg.lev[l];
     if (F.fx == 2 && F.fy == 2 && F.fz == 2)
-      k_mg_restrict8<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], bs, B(l), X(l), mg.lev[l + 1].b, sc);
+      launch_pdl(k_mg_restrict8<T>, grid(l + 1), block(l + 1), 0, s, F, mg.lev[l + 1], bs, B(l), X(l),
+                 mg.lev[l + 1].b, sc);
     else
-      k_mg_restrict<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], bs, B(l), X(l), mg.lev[l + 1].b, sc);
+      launch_pdl(k_mg_restrict<T>, grid(l + 1), block(l + 1), 0, s, F, mg.lev[l + 1], bs, B(l), X(l),
+                 mg.lev[l + 1].b, sc);
   };
   const int m = std::min(mg.tail, n);  // levels m..n-1 run in one block (m < n), or none
   for (int l = 0; l + 1 < m; ++l) down(l);
@@ -712,18 +754,19 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
     down(m - 1);  // levels m-1 -> m as above, then the tail
     size_t cells = 0;
     for (int l = m; l < n; ++l) cells += (size_t)mg.lev[l].nx * mg.lev[l].ny * mg.lev[l].nz;
-    k_mg_tail<T><<<1, 1024, 2 * sizeof(T) * cells, s>>>(mg, m, sc);
+    launch_pdl(k_mg_tail<T>, dim3(1), dim3(1024), 2 * sizeof(T) * cells, s, mg, m, sc);
   } else {
     const MgLevelT<T> &C = mg.lev[n - 1];
     const size_t smem = 2 * sizeof(T) * (size_t)C.nx * C.ny * C.nz;
-    k_mg_coarse<T><<<1, 1024, smem, s>>>(C, mg.coarse_sweeps, mg.cinv, n == 1 ? jacobi : 0, B(n - 1), X(n - 1), sc);
+    launch_pdl(k_mg_coarse<T>, dim3(1), dim3(1024), smem, s, C, mg.coarse_sweeps, mg.cinv, n == 1 ? jacobi : 0,
+               B(n - 1), X(n - 1), sc);
   }
   for (int l = (m < n ? m : n - 1) - 1; l >= 0; --l) {
     const MgLevelT<T> &F = mg.lev[l];
     if (F.fx == 2 && F.fy == 2 && F.fz == 2)
-      k_mg_prolong8<T><<<grid(l + 1), block(l + 1), 0, s>>>(F, mg.lev[l + 1], X(l + 1), X(l), sc);
+      launch_pdl(k_mg_prolong8<T>, grid(l + 1), block(l + 1), 0, s, F, mg.lev[l + 1], (const T *)X(l + 1), X(l), sc);
     else
-      k_mg_prolong<T><<<grid(l), block(l), 0, s>>>(F, mg.lev[l + 1], X(l + 1), X(l), sc);
+      launch_pdl(k_mg_prolong<T>, grid(l), block(l), 0, s, F, mg.lev[l + 1], (const T *)X(l + 1), X(l), sc);
     smooth(l, 1, 0);
     smooth(l, 0, 0);
   }
