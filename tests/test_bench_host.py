@@ -80,3 +80,21 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setenv("RANK", "1")
     assert bench.main(["--impl", "reference"]) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_step_kernel_roofline_names_the_bound():
+    """Each MIXED step kernel against both measured roofs: a kernel whose FP64 instruction
+    rate is the larger fraction is FP64-bound, else HBM-bound; correct64's two launches
+    count as one pass, mirror32 runs over the padded field."""
+    cells, npad = 1_000_000, 1_200_000
+    fp = {"fp64_tflops": 1.0}  # 5e11 FMA instructions per second
+    prof = {"residual64": (2 * 0.1, 2),  # 100 us a launch
+            "mirror32": (0.05, 1), "correct64": (0.1, 4)}
+    r = bench.step_roofline(prof, cells, npad, 5000.0, fp)
+    res = r["residual64"]
+    assert res["avg_launch_us"] == 100.0
+    assert res["achieved_gbs"] == round(24 * cells / 1e-4 / 1e9, 1)
+    assert res["fp64_frac"] == round(9 * cells / 1e-4 / 5e11, 4) and res["bound"] == "fp64"
+    assert r["mirror32"]["achieved_gbs"] == round(36 * npad / 5e-5 / 1e9, 1) and r["mirror32"]["bound"] == "hbm"
+    assert r["correct64"]["launches"] == 2 and r["correct64"]["avg_launch_us"] == 50.0
+    assert "update_uf" not in r
