@@ -213,3 +213,27 @@ def test_adjoint_rejects_the_boundary_options():
             with pytest.raises(cg.CfdgbError) as e:
                 s.forward(4, 2, 4, 2)
             assert e.value.status == cg.EINVAL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_stretched_grid_boundary_set_is_consistent_with_the_csr_rows(precision):
+    """The reference's stretched SML grid with the boundary set.  The flux correction makes
+    the Jacobi-scaled CSR rows' problem consistent (those rows are the finite-volume
+    operator, whose left null vector is the cell volumes): every solve reaches 1e-12, and
+    the GPU run matches the oracle's.  (The SPE rows' y-coefficient swap,
+    SPE_sparseMatrix.hpp:79,83, leaves their problem inconsistent on this grid: the
+    oracle's SPE solves stall between 1e-2 and 1e-4.)  MIXED reaches 1e-10 and agrees."""
+    g = O.Grid(120, 110, 4, 17.0, 12.0, 3.0, 6.5, gridder="sml", **SET)
+    ref = O.run(g, 4, 100.0, 0.005, 1e-12, "csr", seed=SEED, amp=AMP)
+    tol = 1e-12 if precision == "fp64" else 1e-10
+    with cg.Solver(nx=120, ny=110, nz=4, lx=17.0, ly=12.0, lz=3.0, cx=6.5, cy=6.0, grid="sml", Re=100.0,
+                   dt=0.005, solver="jacobi", precision=precision, tol=tol, seed=SEED, amp=AMP, **SET) as s:
+        s.init_fields()
+        st = s.step(4)
+        f = s.get_fields()
+    assert [r.status for r in st] == [0] * 4
+    assert all(r.relres < tol for r in st[1:]), [r.relres for r in st]
+    bar = 1e-10 if precision == "fp64" else 1e-7
+    for k, e in vel_err(f, ref).items():
+        assert e <= bar, (precision, k, e)
+    np.testing.assert_allclose([r.cd for r in st], ref["cd"], rtol=bar)
