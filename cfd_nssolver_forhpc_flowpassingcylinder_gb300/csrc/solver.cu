@@ -1535,20 +1535,25 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
 
 // r64 = b - A x (FP64); ||r||, ||b|| (flags & 1) and the scale (flags & 2).
 // jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose unscaled residual is r / jp.
+// FIRST: also ||b|| (a solve's first residual).  The kernel is bound by the FP64 pipe, so
+// the terms a call does not need are left out: ||b|| after the first, the null-space sum on
+// the stretched grid (whose residual is taken as it is).
+template <bool FIRST>
 __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st, int jacobi,
                                                         const double *__restrict__ b, const double *__restrict__ x,
                                                         double *__restrict__ r64, double *part, StepScal *ss,
                                                         SolverScal *inner, int flags) {
   double acc[3] = {0.0, 0.0, 0.0};
+  const bool nsum = !g.nonuni;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const double bb = b[row];
     const double r = bb - spmv_at<double>(g, st, x, ic, jc, kc, row);
     r64[row] = r;
     acc[0] += r * r;
-    acc[1] += bb * bb;
+    if (FIRST) acc[1] += bb * bb;
     // the unscaled residual's sum: its component along the operator's null space
-    acc[2] += jacobi ? r * row_diag(g, st, ic, jc, kc, row) : r;
+    if (nsum) acc[2] += jacobi ? r * row_diag(g, st, ic, jc, kc, row) : r;
   }
   double out[3];
   if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
@@ -1566,8 +1571,8 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
 __device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<double> &st, int jacobi,
                                                  const double *__restrict__ r64, double m, double inv, int ic, int jc,
                                                  int kc, long long row) {
-  const double wgt = jacobi ? row_jp(g, st, ic, jc, kc, row) : 1.0;
-  return (float)((r64[row] - m * wgt) * inv);
+  const double c = jacobi ? r64[row] - m * row_jp(g, st, ic, jc, kc, row) : r64[row] - m;
+  return d2f_int(c * inv);
 }
 
 // start of a sweep: x = 0, r0 = r1 = scaled residual, rho = <r1, r1>; restart = 1 makes the
@@ -1618,12 +1623,15 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
 }
 
 // sum of the inner correction e (FP64)
+// sum of e: FP32 per thread (its only use is the constant mode, which the operator
+// annihilates, so its rounding changes x by a constant), FP64 over threads
 __global__ void __launch_bounds__(kBlock) k_sum32(Geo g, const float *__restrict__ e, double *part, StepScal *ss) {
-  double acc[1] = {0.0};
+  float f = 0.0f;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    acc[0] += (double)e[row];
+    f += e[row];
   }
+  double acc[1] = {f2d_int(f)};
   double out[1];
   if (grid_sum<1>(acc, part, &ss->cnt[5], out) && lin_tid() == 0) ss->esum = out[0];
 }
@@ -1635,7 +1643,7 @@ __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict_
   const double m = ss->esum / (double)g.ncell;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    x[row] += s * ((double)e[row] - m);
+    x[row] += s * (f2d_int(e[row]) - m);
   }
 }
 
@@ -1866,7 +1874,10 @@ void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const d
 
 void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
                        const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags) {
-  k_residual64<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
+  if (flags & 1)
+    k_residual64<true><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
+  else
+    k_residual64<false><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
 }
 void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
                            float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,

@@ -19,29 +19,6 @@
 
 namespace cfdgb {
 
-// double -> float, rounded to nearest (ties to even), by integer operations.  Results
-// below the normal FP32 range flush to a signed zero, above it to infinity; NaN stays NaN.
-__device__ __forceinline__ float d2f_int(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const unsigned long long a = b & 0x7fffffffffffffffULL;
-  if ((a >> 52) == 0x7ffULL) return __uint_as_float(sign | 0x7f800000u | ((a << 12) ? 0x400000u : 0u));
-  const unsigned long long r = a + 0x0fffffffULL + ((a >> 29) & 1ULL);  // drop 29 bits: nearest, even
-  const int e = (int)(r >> 52) - 896;                                     // FP32 exponent field
-  if (e <= 0) return __uint_as_float(sign);
-  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-  return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((r >> 29) & 0x7fffffULL));
-}
-
-// float -> double, exact, by integer operations (FP32 subnormals, never met here, read as zero)
-__device__ __forceinline__ double f2d_int(float x) {
-  const unsigned b = __float_as_uint(x);
-  const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-  const unsigned eh = e == 0xffu ? 0x7ffu : e + 896u;
-  return __hiloint2double((int)((b & 0x80000000u) | (eh << 20) | ((b >> 3) & 0xfffffu)), (int)(b << 29));
-}
-
 __global__ void __launch_bounds__(kBlock) k_mirror32(long long n, const double *__restrict__ u,
                                                      const double *__restrict__ v, const double *__restrict__ w,
                                                      float *__restrict__ u32, float *__restrict__ v32,
