@@ -1433,6 +1433,8 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   if (cfg->precond == CFDGB_PRECOND_MULTIGRID && cfg->precision == CFDGB_MIXED) {  // levels >= 1, M p, M s
     mg_plan(cfg->nx, cfg->ny, cfg->nz, cfg->lx / cfg->nx, cfg->ly / cfg->ny, cfg->lz / cfg->nz, c->nsm,
             !std::getenv("CFDGB_SCALAR_FP32"), &c->mg, g.pz != 0);
+    if (std::getenv("CFDGB_MG_PER_PASS"))  // every level on the per-pass kernels (tests compare)
+      for (int l = 0; l < c->mg.nlev; ++l) c->mg.lev[l].march = 0;
     mg_prepare<float>();
     if ((rc = upload_dense_coarse(c, c->mg))) return bail(rc);
     if ((rc = dalloc(c, &c->ph32, c->ncell)) || (rc = dalloc(c, &c->sh32, c->ncell))) return bail(rc);

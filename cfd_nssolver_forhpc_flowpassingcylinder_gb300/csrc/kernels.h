@@ -173,6 +173,10 @@ struct MgLevelT {
   int qgrid;               // 1: the quad smoother (FP32, nz % 4 == 0), 0: the scalar one
   int qbx, qby, qgx, qgy, qgz;  // its launch: quads along x, rows along y, planes strided over z
   int pz;                  // periodic z (every level; nz even or 1 on each)
+  // 1: the level's V-cycle work runs as two marching kernels (k_mg_down4, k_mg_up4; FP32
+  // quads, every axis halves, nz / 4 a power of two up to 16): a block of nz / 4 x (mty + 4)
+  // threads owns a band of mty rows and marches over a segment of msx planes; mgx x mgy blocks
+  int march, mty, msx, mgx, mgy;
   // 1/diag of a row by its neighbour counts along x, y, z (each 0..2): idg[9 cx + 3 cy + cz]
   // (0 where a row has no neighbour); the smoother multiplies instead of dividing
   T idg[27];

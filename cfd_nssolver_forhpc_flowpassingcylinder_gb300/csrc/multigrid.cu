@@ -58,6 +58,24 @@ __device__ __forceinline__ long long lrow(const MgLevelT<T> &L, int i, int j, in
   return ((long long)i * L.ny + j) * L.nz + k;
 }
 
+// Rounded operations the compiler does not contract: the quad smoother, the pair transfers
+// and the marching kernels form each value by the same explicit sequence, so that they give
+// identical results.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+// wx a + wy e + wz f (the weighted neighbour sums of lnb's three axes)
+template <typename T>
+__device__ __forceinline__ T wsum(const MgLevelT<T> &L, T a, T e, T f) {
+  return fma_rn(L.wz, f, fma_rn(L.wy, e, mul_rn(L.wx, a)));
+}
+// one child's residual b - d x + (neighbour sum), b already scaled
+template <typename T>
+__device__ __forceinline__ T resid(T bb, T d, T x, T nb) { return add_rn(fma_rn(-d, x, bb), nb); }
+
 // z neighbours of a cell: those that exist (Neumann), or both across the wrap (periodic z,
 // none on a level one cell thick, whose wrapped neighbours are the cell itself)
 template <typename T>
@@ -156,8 +174,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
           o[c] = 0.f;
           continue;
         }
-        const float bb = bscale ? bv[c] * (dxy + L.wz * (float)cz[c]) : bv[c];
-        o[c] = bb * L.idg[cxy + cz[c]];
+        const float bb = bscale ? mul_rn(bv[c], dxy + L.wz * (float)cz[c]) : bv[c];
+        o[c] = mul_rn(bb, L.idg[cxy + cz[c]]);
       }
     } else {
       const float4 xq = *reinterpret_cast<const float4 *>(x + r);
@@ -184,8 +202,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, int colour, in
         if (jp) e += ypv[c];
         if (k > 0 || L.pz) f += c == 0 ? kl : xv[c - 1];
         if (k < L.nz - 1 || L.pz) f += c == 3 ? kr : xv[c + 1];
-        const float bb = bscale ? bv[c] * (dxy + L.wz * (float)cz[c]) : bv[c];
-        o[c] = (bb + (L.wx * a + L.wy * e + L.wz * f)) * L.idg[cxy + cz[c]];
+        const float bb = bscale ? mul_rn(bv[c], dxy + L.wz * (float)cz[c]) : bv[c];
+        o[c] = mul_rn(add_rn(bb, wsum(L, a, e, f)), L.idg[cxy + cz[c]]);
       }
     }
     *reinterpret_cast<float4 *>(x + r) = make_float4(o[0], o[1], o[2], o[3]);
@@ -344,11 +362,10 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict8(MgLevelT<T> F, MgLevelT
           if (fk > 0 || F.pz) az += c ? xv[a][e][0] : xkm[a][e];
           if (fk < F.nz - 1 || F.pz) az += c ? xkp[a][e] : xv[a][e][1];
           const T d = ldiag(F, fi, fj, fk);
-          T bb = bv[a][e][c];
-          if (bscale) bb *= d;
-          sum += bb - d * xv[a][e][c] + (F.wx * ax + F.wy * ay + F.wz * az);
+          const T bb = bscale ? mul_rn(bv[a][e][c], d) : bv[a][e][c];
+          sum = add_rn(sum, resid(bb, d, xv[a][e][c], wsum(F, ax, ay, az)));
         }
-    bc[lrow(Cl, i, j, k)] = sum * inv;
+    bc[lrow(Cl, i, j, k)] = mul_rn(sum, inv);
   }
 }
 
@@ -390,14 +407,403 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong8(MgLevelT<T> F, MgLevelT<
 #pragma unroll
             for (int q = 0; q < 2; ++q)
 #pragma unroll
-              for (int t = 0; t < 2; ++t) v += wa[p] * wa[q] * wa[t] * cv[ti[p]][tj[q]][tk[t]];
+              for (int t = 0; t < 2; ++t) v = fma_rn(wa[p] * wa[q] * wa[t], cv[ti[p]][tj[q]][tk[t]], v);
           out[c] = v;
         }
         T *dst = xf + r0 + a * sx + e * sy;
         T x0, x1;
         ld2(dst, x0, x1);
-        st2(dst, x0 + out[0], x1 + out[1]);
+        st2(dst, add_rn(x0, out[0]), add_rn(x1, out[1]));
       }
+  }
+}
+
+// ---- a level whose every axis halves, FP32 quads (nz / 4 a power of two up to 16): its
+// V-cycle work in two marching kernels instead of six per-pass launches.  A block of
+// nz / 4 x (mty + 4) threads owns a band of mty rows and two halo rows on each side (a
+// thread: one quad of one row) and marches along x over a segment of msx planes and two halo
+// planes on each side.  A thread keeps its planes in registers (rings of three, rotated by
+// unrolling); each stage's plane passes through shared memory for the y neighbours (three
+// buffers per stage, so one barrier a plane; rows outside the level hold zeros there) and
+// the z neighbours across quads by shuffles.  The arithmetic runs on cell pairs (FP32x2).
+//   k_mg_down4: the pre-smoothing from zero (colour 0: b / diag; colour 1 from those), the
+//     residual and its restriction to the next level's b.  The level's x is not stored: the
+//     only part of it read later, colour 0's, is b / diag again.
+//   k_mg_up4: colour 0 = b / diag + P xc, then the colour-1 and colour-0 passes of the
+//     post-smoothing; x stored.
+// Neighbours beyond a wall enter as zeros (the registers of planes and the shared rows
+// outside the level hold zeros).  Each value is otherwise formed by the rounded sequence of
+// k_mg_smooth4, k_mg_restrict8 or k_mg_prolong8 (the pair operations round each component
+// as the scalar ones do), so a V-cycle gives the per-pass kernels' result (equal as
+// numbers: a sum of two zeros may differ in sign).
+constexpr int kMgMarchThreads = 320;
+
+__device__ __forceinline__ float2 pr(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+// wsum of two cells
+__device__ __forceinline__ float2 wsum2(const MgLevel &L, float2 a, float2 e, float2 f) {
+  return __ffma2_rn(bc2(L.wz), f, __ffma2_rn(bc2(L.wy), e, __fmul2_rn(bc2(L.wx), a)));
+}
+
+// a thread's row and quad, and what does not change along the march
+struct MarchRow {
+  unsigned mask;      // the lanes of this warp that exist
+  int left, right;    // lanes of the quads before and after this one in its row (wrapping)
+  int q, tj, j, k0;
+  bool jin, jm, jp;   // the row exists; its neighbours along y exist
+  bool zl, zr;        // the quad has a z neighbour before / after it (or across the wrap)
+  float wycy;         // wy cy (exact: cy in 0..2)
+  float2 wz01, wz23;  // wz cz of the quad's cells (exact)
+  int cy3, cz0, cz3;  // 3 cy; cz of the end cells (the middle ones have cz = 2)
+  // 1/diag of the quad's cells on a plane with 9 cx = c9
+  __device__ __forceinline__ float2 idg01(const MgLevel &L, int c9) const {
+    return pr(L.idg[c9 + cy3 + cz0], L.idg[c9 + cy3 + 2]);
+  }
+  __device__ __forceinline__ float2 idg23(const MgLevel &L, int c9) const {
+    return pr(L.idg[c9 + cy3 + 2], L.idg[c9 + cy3 + cz3]);
+  }
+};
+
+template <int NQ>
+__device__ __forceinline__ MarchRow march_row(const MgLevel &L) {
+  MarchRow R;
+  const int w0 = threadIdx.x & ~31, n = min(32, (int)blockDim.x - w0);
+  R.mask = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+  R.q = threadIdx.x % NQ;
+  R.tj = threadIdx.x / NQ;
+  R.k0 = 4 * R.q;
+  const int row0 = (threadIdx.x & 31) - R.q;  // a row's NQ lanes lie in one warp (NQ divides 32)
+  R.left = row0 + ((R.q - 1) & (NQ - 1));
+  R.right = row0 + ((R.q + 1) & (NQ - 1));
+  R.j = blockIdx.y * L.mty - 2 + R.tj;
+  R.jin = R.j >= 0 && R.j < L.ny;
+  R.jm = R.j > 0;
+  R.jp = R.j < L.ny - 1;
+  R.zl = R.q > 0 || L.pz;
+  R.zr = R.q < NQ - 1 || L.pz;
+  const int cy = (int)R.jm + (int)R.jp;
+  R.wycy = L.wy * (float)cy;
+  R.cy3 = 3 * cy;
+  R.cz0 = zcount(L, R.k0);
+  R.cz3 = zcount(L, R.k0 + 3);
+  R.wz01 = pr(L.wz * (float)R.cz0, 2.f * L.wz);
+  R.wz23 = pr(2.f * L.wz, L.wz * (float)R.cz3);
+  return R;
+}
+
+__device__ __forceinline__ void unq(const float4 v, float (&o)[4]) {
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+__device__ __forceinline__ float4 mkq(const float (&o)[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
+
+// wx cx + wy cy of plane i (the diagonal less its z part) and 9 cx
+__device__ __forceinline__ float march_dxy(const MgLevel &L, const MarchRow &R, int i, int &c9) {
+  const int cx = (int)(i > 0) + (int)(i < L.nx - 1);
+  c9 = 9 * cx;
+  return fma_rn(L.wx, (float)cx, R.wycy);
+}
+
+// the z neighbours of a quad's end cells from the neighbouring lanes (every lane calls it)
+__device__ __forceinline__ void march_kz(const MarchRow &R, const float (&v)[4], float &kl, float &kr) {
+  const float l = __shfl_sync(R.mask, v[3], R.left), r = __shfl_sync(R.mask, v[0], R.right);
+  kl = R.zl ? l : 0.f;
+  kr = R.zr ? r : 0.f;
+}
+
+// b of a quad's cell pairs, times the diagonal for Jacobi-scaled rows (BS)
+template <bool BS>
+__device__ __forceinline__ void march_bb(const MarchRow &R, float dxy, const float (&bv)[4], float2 &b01,
+                                         float2 &b23) {
+  if (BS) {
+    b01 = pr(mul_rn(bv[0], dxy + R.wz01.x), mul_rn(bv[1], dxy + R.wz01.y));
+    b23 = pr(mul_rn(bv[2], dxy + R.wz23.x), mul_rn(bv[3], dxy + R.wz23.y));
+  } else {
+    b01 = pr(bv[0], bv[1]);
+    b23 = pr(bv[2], bv[3]);
+  }
+}
+
+// colour 0 of a quad after the pre-smoothing from zero (k_mg_smooth4's zero pass): b / diag
+// on colour 0, zero on colour 1
+template <bool BS>
+__device__ __forceinline__ void march_zero(const MgLevel &L, const MarchRow &R, float dxy, int c9, int t0,
+                                           const float (&bv)[4], float (&o)[4]) {
+  float2 b01, b23;
+  march_bb<BS>(R, dxy, bv, b01, b23);
+  const float2 v01 = __fmul2_rn(b01, R.idg01(L, c9)), v23 = __fmul2_rn(b23, R.idg23(L, c9));
+  o[0] = t0 ? 0.f : v01.x;
+  o[1] = t0 ? v01.y : 0.f;
+  o[2] = t0 ? 0.f : v23.x;
+  o[3] = t0 ? v23.y : 0.f;
+}
+
+// One colour pass of k_mg_smooth4 on a quad (its non-zero form): the cells of colour t0's
+// parity (t0: the first such cell) from the neighbours' values, the others kept.  xm, xp:
+// the quad on the planes before and after; ym, yp: rows j -1, j + 1; kl, kr: the cells
+// beyond the quad's ends.
+template <bool BS>
+__device__ __forceinline__ void march_pass(const MgLevel &L, const MarchRow &R, float dxy, int c9, int t0,
+                                           const float (&bv)[4], const float (&xv)[4], const float (&xm)[4],
+                                           const float (&xp)[4], const float4 ym, const float4 yp, float kl, float kr,
+                                           float (&o)[4]) {
+  float2 b01, b23;
+  march_bb<BS>(R, dxy, bv, b01, b23);
+  const float2 s01 = wsum2(L, __fadd2_rn(pr(xm[0], xm[1]), pr(xp[0], xp[1])), __fadd2_rn(pr(ym.x, ym.y), pr(yp.x, yp.y)),
+                           __fadd2_rn(pr(kl, xv[0]), pr(xv[1], xv[2])));
+  const float2 s23 = wsum2(L, __fadd2_rn(pr(xm[2], xm[3]), pr(xp[2], xp[3])), __fadd2_rn(pr(ym.z, ym.w), pr(yp.z, yp.w)),
+                           __fadd2_rn(pr(xv[1], xv[2]), pr(xv[3], kr)));
+  const float2 v01 = __fmul2_rn(__fadd2_rn(b01, s01), R.idg01(L, c9));
+  const float2 v23 = __fmul2_rn(__fadd2_rn(b23, s23), R.idg23(L, c9));
+  o[0] = t0 ? xv[0] : v01.x;
+  o[1] = t0 ? v01.y : xv[1];
+  o[2] = t0 ? xv[2] : v23.x;
+  o[3] = t0 ? v23.y : xv[3];
+}
+
+template <int NQ, bool BS>
+__global__ void __launch_bounds__(kMgMarchThreads, 2)
+    k_mg_down4(MgLevel F, MgLevel Cl, const float *__restrict__ b, float *__restrict__ bc, const SolverScal *sc) {
+  pdl_wait();
+  if (sc->done) return;
+  pdl_trigger();
+  constexpr int NZ = 4 * NQ;
+  const int RY = F.mty + 4, PL = RY * NQ;
+  extern __shared__ float4 msm[];
+  float4 *const sa = msm + threadIdx.x, *const sb = msm + 3 * PL + threadIdx.x;  // colour 0 / both
+  const MarchRow R = march_row<NQ>(F);
+  const int is = blockIdx.x * F.msx, ie = min(F.nx, is + F.msx);
+  const bool blk = R.jin && R.tj >= 1 && R.tj < RY - 1;  // colour 1: the band and one halo row
+  const bool res = R.jin && R.tj >= 2 && R.tj < RY - 2;  // residual: the band
+  const bool even = !(R.j & 1);
+  const int sx = F.ny * NZ, o = (R.jin ? R.j : 0) * NZ + R.k0;  // 32-bit: under 2^31 cells
+  auto ldb = [&](int p) -> float4 {
+    return R.jin && p >= 0 && p < F.nx ? __ldg(reinterpret_cast<const float4 *>(b + (o + p * sx)))
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  float4 bn1 = ldb(is - 2), bn2 = ldb(is - 1);
+  float bA[4] = {}, bB[4] = {}, bC[4] = {};  // b of planes p, p-1, p-2 (rotating)
+  float xA[4] = {}, xB[4] = {}, xC[4] = {};  // colour 0 from zero, planes p, p-1, p-2
+  float fA[4] = {}, fB[4] = {}, fC[4] = {};  // both colours, planes p-1, p-2, p-3
+  float sA = 0.f, sB = 0.f;  // the restriction sums of the quad's two coarse cells (even rows)
+  // s0, s1, s2: the shared slots of planes p, p - 1, p - 2
+  auto step = [&](int p, float(&b0)[4], float(&b1)[4], float(&b2)[4], float(&x0)[4], float(&x1)[4],
+                  float(&x2)[4], float(&f1)[4], float(&f2)[4], float(&f3)[4], int s0, int s1, int s2) {
+    // plane p: b, and colour 0 from zero (zeros outside the level)
+    unq(bn1, b0);
+    bn1 = bn2;
+    bn2 = ldb(p + 2);
+    {
+      int c9;
+      const float dxy = march_dxy(F, R, p, c9);
+      march_zero<BS>(F, R, dxy, c9, (p + R.j) & 1, b0, x0);
+      sa[s0 * PL] = mkq(x0);
+    }
+    __syncthreads();
+    {  // plane p - 1: colour 1 from colour 0
+      const int i = p - 1;
+      float kl, kr;
+      march_kz(R, x1, kl, kr);
+      if (blk && i >= 0 && i < F.nx) {
+        int c9;
+        const float dxy = march_dxy(F, R, i, c9);
+        const float4 *s = sa + s1 * PL;
+        march_pass<BS>(F, R, dxy, c9, (i + R.j + 1) & 1, b1, x1, x2, x0, s[-NQ], s[NQ], kl, kr, f1);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) f1[c] = x1[c];
+      }
+      sb[s1 * PL] = mkq(f1);
+    }
+    {  // plane p - 2: the residual b - A x, restricted (k_mg_restrict8's sums)
+      const int i = p - 2;
+      float kl, kr;
+      march_kz(R, f2, kl, kr);
+      const bool act = res && i >= is && i < ie;
+      float2 r01 = make_float2(0.f, 0.f), r23 = r01;
+      if (act) {
+        int c9;
+        const float dxy = march_dxy(F, R, i, c9);
+        const float4 *s = sb + s2 * PL;
+        const float4 ym = s[-NQ], yp = s[NQ];
+        float2 b01, b23;
+        march_bb<BS>(R, dxy, b2, b01, b23);
+        const float2 d01 = __fadd2_rn(bc2(dxy), R.wz01), d23 = __fadd2_rn(bc2(dxy), R.wz23);  // ldiag
+        const float2 s01 = wsum2(F, __fadd2_rn(pr(f3[0], f3[1]), pr(f1[0], f1[1])),
+                                 __fadd2_rn(pr(ym.x, ym.y), pr(yp.x, yp.y)), __fadd2_rn(pr(kl, f2[0]), pr(f2[1], f2[2])));
+        const float2 s23 = wsum2(F, __fadd2_rn(pr(f3[2], f3[3]), pr(f1[2], f1[3])),
+                                 __fadd2_rn(pr(ym.z, ym.w), pr(yp.z, yp.w)), __fadd2_rn(pr(f2[1], f2[2]), pr(f2[3], kr)));
+        r01 = __fadd2_rn(__ffma2_rn(pr(-d01.x, -d01.y), pr(f2[0], f2[1]), b01), s01);
+        r23 = __fadd2_rn(__ffma2_rn(pr(-d23.x, -d23.y), pr(f2[2], f2[3]), b23), s23);
+      }
+      // children (a, e, c) of a coarse cell summed in k_mg_restrict8's order: the odd row's
+      // residuals by shuffle
+      const float o0 = __shfl_down_sync(R.mask, r01.x, NQ), o1 = __shfl_down_sync(R.mask, r01.y, NQ);
+      const float o2 = __shfl_down_sync(R.mask, r23.x, NQ), o3 = __shfl_down_sync(R.mask, r23.y, NQ);
+      if (act && even) {
+        if (!(i & 1)) {
+          sA = 0.f;
+          sB = 0.f;
+        }
+        sA = add_rn(add_rn(add_rn(add_rn(sA, r01.x), r01.y), o0), o1);
+        sB = add_rn(add_rn(add_rn(add_rn(sB, r23.x), r23.y), o2), o3);
+        if (i & 1) {
+          const float inv = 1.f / 8.f;
+          *reinterpret_cast<float2 *>(bc + lrow(Cl, i >> 1, R.j >> 1, 2 * R.q)) =
+              make_float2(mul_rn(sA, inv), mul_rn(sB, inv));
+        }
+      }
+    }
+  };
+  for (int p = is - 2;;) {
+    step(p, bA, bC, bB, xA, xC, xB, fA, fC, fB, 0, 2, 1);
+    if (++p > ie + 1) break;
+    step(p, bB, bA, bC, xB, xA, xC, fB, fA, fC, 1, 0, 2);
+    if (++p > ie + 1) break;
+    step(p, bC, bB, bA, xC, xB, xA, fC, fB, fA, 2, 1, 0);
+    if (++p > ie + 1) break;
+  }
+}
+
+// a coarse plane's values for a quad's prolongation: rows pj, nj (the parent row and the
+// neighbour on the child's side) x coarse z 2q - 1, 2q, 2q + 1, 2q + 2, the ends the parent
+// beyond a wall or wrapped (k_mg_prolong8's taps); raw: the float2 pairs of the two rows
+__device__ __forceinline__ void march_zext(const MarchRow &R, float4 raw, float (&o)[2][4]) {
+  const float l0 = __shfl_sync(R.mask, raw.y, R.left), l1 = __shfl_sync(R.mask, raw.w, R.left);
+  const float r0 = __shfl_sync(R.mask, raw.x, R.right), r1 = __shfl_sync(R.mask, raw.z, R.right);
+  o[0][0] = R.zl ? l0 : raw.x;
+  o[0][1] = raw.x;
+  o[0][2] = raw.y;
+  o[0][3] = R.zr ? r0 : raw.y;
+  o[1][0] = R.zl ? l1 : raw.z;
+  o[1][1] = raw.z;
+  o[1][2] = raw.w;
+  o[1][3] = R.zr ? r1 : raw.w;
+}
+
+template <int NQ, bool BS>
+__global__ void __launch_bounds__(kMgMarchThreads, 2)
+    k_mg_up4(MgLevel F, MgLevel Cl, const float *__restrict__ b, const float *__restrict__ xc, float *__restrict__ x,
+             const SolverScal *sc) {
+  pdl_wait();
+  if (sc->done) return;
+  pdl_trigger();
+  constexpr int NZ = 4 * NQ;
+  const int RY = F.mty + 4, PL = RY * NQ;
+  extern __shared__ float4 msm[];
+  float4 *const sa = msm + threadIdx.x, *const sb = msm + 3 * PL + threadIdx.x;  // colour 0 / both
+  const MarchRow R = march_row<NQ>(F);
+  const int is = blockIdx.x * F.msx, ie = min(F.nx, is + F.msx);
+  const bool one = R.jin && R.tj >= 1 && R.tj < RY - 1;   // colour 1: the band and one halo row
+  const bool zero = R.jin && R.tj >= 2 && R.tj < RY - 2;  // colour 0, stored: the band
+  // 32-bit offsets: a marching level has fewer than 2^31 cells (mg_plan)
+  const int sx = F.ny * NZ, o = (R.jin ? R.j : 0) * NZ + R.k0;
+  auto ldb = [&](int p) -> float4 {
+    return R.jin && p >= 0 && p < F.nx ? __ldg(reinterpret_cast<const float4 *>(b + (o + p * sx)))
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  // prolongation taps along y: the parent row and the neighbour on the child's side
+  const int jc = min(max(R.j, 0), F.ny - 1), pj = jc >> 1;
+  const int nj = (jc & 1) ? min(pj + 1, Cl.ny - 1) : max(pj - 1, 0);
+  const int co = pj * Cl.nz + 2 * R.q, cd = (nj - pj) * Cl.nz, csx = Cl.ny * Cl.nz;
+  auto ldc = [&](int m) -> float4 {  // coarse plane m (clamped to the level), rows pj and nj
+    const int r = min(max(m, 0), Cl.nx - 1) * csx + co;
+    const float2 u = __ldg(reinterpret_cast<const float2 *>(xc + r));
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(xc + (r + cd)));
+    return make_float4(u.x, u.y, v.x, v.y);
+  };
+  // coarse planes m - 1 and m around the parent plane m = p / 2 of the fine plane p (raw
+  // pairs, extended at each use), and m + 1 in flight during the parent's first child (is - 2
+  // is even: the march starts on a first child)
+  const int m0 = (is - 2) >> 1;
+  float4 ca = ldc(m0 - 1), cb = ldc(m0), cn = cb;
+  float4 bn1 = ldb(is - 2), bn2 = ldb(is - 1);
+  float bA[4] = {}, bB[4] = {}, bC[4] = {};  // b of planes p, p-1, p-2 (rotating)
+  float xA[4] = {}, xB[4] = {}, xC[4] = {};  // colour 0 + P xc, planes p, p-1, p-2
+  float yA[4] = {}, yB[4] = {}, yC[4] = {};  // after colour 1, planes p-1, p-2, p-3
+  auto step = [&](int p, float(&b0)[4], float(&b1)[4], float(&b2)[4], float(&x0)[4], float(&x1)[4],
+                  float(&x2)[4], float(&y1)[4], float(&y2)[4], float(&y3)[4], int s0, int s1, int s2) {
+    const bool odd = p & 1;
+    // plane p: colour 0 = b / diag + P xc (k_mg_prolong8: parent first on every axis)
+    unq(bn1, b0);
+    bn1 = bn2;
+    bn2 = ldb(p + 2);
+    {
+      int c9;
+      const float dxy = march_dxy(F, R, p, c9);
+      const int t0 = (p + R.j) & 1;
+      march_zero<BS>(F, R, dxy, c9, t0, b0, x0);
+      // cells (0, 1) and (2, 3): z taps parent (1, 1), (2, 2), child's side (0, 2), (1, 3);
+      // the parent plane (a = 0), then the plane on the child's side
+      const float wa[2] = {0.75f, 0.25f};
+      float2 v01 = make_float2(0.f, 0.f), v23 = v01;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        float cv[2][4];
+        march_zext(R, a == 0 ? cb : (odd ? cn : ca), cv);
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+          for (int t = 0; t < 2; ++t) {
+            const float2 w = bc2(wa[a] * wa[e] * wa[t]);
+            v01 = __ffma2_rn(w, t == 0 ? pr(cv[e][1], cv[e][1]) : pr(cv[e][0], cv[e][2]), v01);
+            v23 = __ffma2_rn(w, t == 0 ? pr(cv[e][2], cv[e][2]) : pr(cv[e][1], cv[e][3]), v23);
+          }
+      }
+      const float2 s01 = __fadd2_rn(pr(x0[0], x0[1]), v01), s23 = __fadd2_rn(pr(x0[2], x0[3]), v23);
+      // outside the level: zeros, as the neighbours beyond a wall
+      const bool in = R.jin && p >= 0 && p < F.nx;
+      x0[0] = in && !t0 ? s01.x : 0.f;
+      x0[1] = in && t0 ? s01.y : 0.f;
+      x0[2] = in && !t0 ? s23.x : 0.f;
+      x0[3] = in && t0 ? s23.y : 0.f;
+      sa[s0 * PL] = mkq(x0);
+      if (odd) {  // the next plane has the next parent
+        ca = cb;
+        cb = cn;
+      } else {
+        cn = ldc((p >> 1) + 1);
+      }
+    }
+    __syncthreads();
+    {  // plane p - 1: colour 1 of the post-smoothing
+      const int i = p - 1;
+      float kl, kr;
+      march_kz(R, x1, kl, kr);
+      if (one && i >= 0 && i < F.nx) {
+        int c9;
+        const float dxy = march_dxy(F, R, i, c9);
+        const float4 *s = sa + s1 * PL;
+        march_pass<BS>(F, R, dxy, c9, (i + R.j + 1) & 1, b1, x1, x2, x0, s[-NQ], s[NQ], kl, kr, y1);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) y1[c] = x1[c];
+      }
+      sb[s1 * PL] = mkq(y1);
+    }
+    {  // plane p - 2: colour 0, stored
+      const int i = p - 2;
+      float kl, kr;
+      march_kz(R, y2, kl, kr);
+      if (zero && i >= is && i < ie) {
+        int c9;
+        const float dxy = march_dxy(F, R, i, c9);
+        const float4 *s = sb + s2 * PL;
+        float ov[4];
+        march_pass<BS>(F, R, dxy, c9, (i + R.j) & 1, b2, y2, y3, y1, s[-NQ], s[NQ], kl, kr, ov);
+        *reinterpret_cast<float4 *>(x + (o + i * sx)) = mkq(ov);
+      }
+    }
+  };
+  for (int p = is - 2;;) {
+    step(p, bA, bC, bB, xA, xC, xB, yA, yC, yB, 0, 2, 1);
+    if (++p > ie + 1) break;
+    step(p, bB, bA, bC, xB, xA, xC, yB, yA, yC, 1, 0, 2);
+    if (++p > ie + 1) break;
+    step(p, bC, bB, bA, xC, xB, xA, yC, yB, yA, 2, 1, 0);
+    if (++p > ie + 1) break;
   }
 }
 
@@ -614,6 +1020,17 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
     L.fx = fx;
     L.fy = fy;
     L.fz = fz;
+    // the marching kernels: a band of 256 / (nz / 4) rows (at most ny), the segments sized so
+    // that about two blocks per SM run
+    const int nq = nz / 4;
+    if (L.qgrid && fx == 2 && fy == 2 && fz == 2 && nq <= 16 && (nq & (nq - 1)) == 0 && cells < (1LL << 31)) {
+      L.march = 1;
+      L.mty = std::min(256 / nq, ny);
+      L.mgy = (ny + L.mty - 1) / L.mty;
+      const long long want = 2LL * nsm;
+      L.msx = 2 * (int)std::max(1LL, ((long long)nx * L.mgy + 2 * want - 1) / (2 * want));
+      L.mgx = (nx + L.msx - 1) / L.msx;
+    }
     nx /= fx;
     ny /= fy;
     nz /= fz;
@@ -636,11 +1053,14 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
   return (long long)C.nx * C.ny * C.nz <= kMgSharedCells;
 }
 
-// per level above the tail (or the coarsest): 2 smooths + restrict, prolong + 2 smooths;
-// then one tail (or coarsest) kernel
+// per level above the tail (or the coarsest): 2 smooths + restrict, prolong + 2 smooths, or
+// the two marching kernels; then one tail (or coarsest) kernel
 template <typename T>
 int mg_vcycle_launches(const MgPlanT<T> &mg) {
-  return mg.tail < mg.nlev ? 6 * mg.tail + 1 : 6 * (mg.nlev - 1) + 1;
+  const int m = mg.tail < mg.nlev ? mg.tail : mg.nlev - 1;
+  int n = 1;
+  for (int l = 0; l < m; ++l) n += mg.lev[l].march ? 2 : 6;
+  return n;
 }
 
 // The pseudo-inverse of the coarsest level's operator (symmetric, singular on constants
@@ -736,7 +1156,39 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
   // pre-smoothing from zero and restriction to level l + 1.  (Both colour passes in one
   // kernel, each black cell recomputing its red neighbours' start values, was measured at
   // 80 us on the 512x256x64 level against 36 us for the two quad passes: not kept.)
+  // the marching kernels of a level (FP32 only; nz / 4 a power of two up to 16)
+  auto march = [&](int l, bool up) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+      const MgLevelT<T> &F = mg.lev[l], &Cl = mg.lev[l + 1];
+      const int bs = l == 0 ? jacobi : 0, nq = F.nz / 4;
+      const dim3 grid(F.mgx, F.mgy), block(nq * (F.mty + 4));
+      const size_t smem = 6 * sizeof(float4) * (size_t)block.x;
+#define CFDGB_MARCH(NQ)                                                                                      \
+  case NQ:                                                                                                 \
+    if (up && bs)                                                                                          \
+      launch_pdl(k_mg_up4<NQ, true>, grid, block, smem, s, F, Cl, B(l), (const T *)X(l + 1), X(l), sc);     \
+    else if (up)                                                                                           \
+      launch_pdl(k_mg_up4<NQ, false>, grid, block, smem, s, F, Cl, B(l), (const T *)X(l + 1), X(l), sc);    \
+    else if (bs)                                                                                           \
+      launch_pdl(k_mg_down4<NQ, true>, grid, block, smem, s, F, Cl, B(l), Cl.b, sc);                        \
+    else                                                                                                   \
+      launch_pdl(k_mg_down4<NQ, false>, grid, block, smem, s, F, Cl, B(l), Cl.b, sc);                       \
+    break;
+      switch (nq) {
+        CFDGB_MARCH(1)
+        CFDGB_MARCH(2)
+        CFDGB_MARCH(4)
+        CFDGB_MARCH(8)
+        CFDGB_MARCH(16)
+      }
+#undef CFDGB_MARCH
+    }
+  };
   auto down = [&](int l) {
+    if (mg.lev[l].march) {
+      march(l, false);
+      return;
+    }
     const int bs = l == 0 ? jacobi : 0;
     smooth(l, 0, 1);
     smooth(l, 1, 0);
@@ -763,6 +1215,10 @@ void launch_mg_vcycle(cudaStream_t s, const MgPlanT<T> &mg, int jacobi, const T 
   }
   for (int l = (m < n ? m : n - 1) - 1; l >= 0; --l) {
     const MgLevelT<T> &F = mg.lev[l];
+    if (F.march) {
+      march(l, true);
+      continue;
+    }
     if (F.fx == 2 && F.fy == 2 && F.fz == 2)
       launch_pdl(k_mg_prolong8<T>, grid(l + 1), block(l + 1), 0, s, F, mg.lev[l + 1], (const T *)X(l + 1), X(l), sc);
     else

@@ -59,6 +59,42 @@ def test_multigrid_quad_and_scalar_kernels_agree(env, monkeypatch):
         assert e <= 1e-6, (env, k, e)
 
 
+MARCH_CASES = {
+    # levels 128x64x16 and 64x32x8 above the one-block tail: nz / 4 = 4 and 2
+    "128x64x16": CASES["128x64x16"],
+    # four marching levels (nz / 4 = 16, 8, 4, 2), several bands and segments on each
+    "256x128x64": dict(nx=256, ny=128, nz=64, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0),
+    # a ragged band (ny not a multiple of the band), one segment per level
+    "64x40x8": dict(nx=64, ny=40, nz=8, lx=16.0, ly=10.0, lz=2.0, cx=4.0, cy=5.0, project_rhs=1),
+    # the stated boundary set: periodic z on every level, the seeded perturbation
+    "set 128x64x16": dict(CASES["128x64x16"], seed=7, amp=1e-3, **cg.BOUNDARY_SET),
+}
+
+
+@pytest.mark.parametrize("case", sorted(MARCH_CASES))
+@pytest.mark.parametrize("solver", ["bicgstab", "jacobi"])
+def test_multigrid_marching_kernels_match_the_per_pass_kernels(solver, case, monkeypatch):
+    """The two marching kernels a level (pre-smoothing + restriction, prolongation +
+    post-smoothing) form every value by the per-pass kernels' expressions in their order:
+    the whole run, fields and iteration counts, is identical bit for bit."""
+    dom = MARCH_CASES[case]
+    runs = []
+    for per_pass in (False, True):
+        if per_pass:
+            monkeypatch.setenv("CFDGB_MG_PER_PASS", "1")
+        else:
+            monkeypatch.delenv("CFDGB_MG_PER_PASS", raising=False)
+        with cg.Solver(solver=solver, precision="mixed", precond="multigrid", **dom) as s:
+            s.init_fields()
+            st = s.step(3)
+            runs.append((s.get_fields(), [(r.iters, r.outer, r.relres) for r in st]))
+    (fa, sa), (fb, sb) = runs
+    assert sa == sb, (sa, sb)
+    assert all(r[2] < 1e-8 for r in sa[1:]), sa
+    for k in "uvwp":
+        assert np.array_equal(fa[k], fb[k]), (case, k, float(np.abs(fa[k] - fb[k]).max()))
+
+
 def test_multigrid_with_perturbation_and_projection():
     """The seeded-perturbation case over 20 steps."""
     res = {}
