@@ -106,7 +106,8 @@ struct cfdgb_ctx {
   std::vector<float> tab32_uni;  // a uniform grid's table rows, one value each (3 x 11); empty otherwise
   double *u = nullptr, *v = nullptr, *w = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
   double *ui = nullptr, *vi = nullptr, *wi = nullptr, *p = nullptr, *eta = nullptr;
-  double *b = nullptr, *x = nullptr, *px1 = nullptr, *px2 = nullptr, *r64 = nullptr;
+  double *b = nullptr, *x = nullptr, *px1 = nullptr, *px2 = nullptr;
+  float *rf = nullptr;  // MIXED: the FP64 residual rounded to FP32
   KrylovVecs<double> k64{};
   KrylovVecs<float> k32{};
   float *p32[2] = {nullptr, nullptr}, *ap32[2] = {nullptr, nullptr};  // FP32 double buffers
@@ -717,7 +718,7 @@ int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres
   const int jacf = jac ? 1 : 0;
   auto residual = [&](int flags, double *rel) -> int {
     L(c, K_RESID64, 1, [&] {
-      launch_residual64(c->stream, c->nblk, c->g, st64, jacf, c->b, c->x, c->r64, c->part, c->ss, c->sc32, flags);
+      launch_residual64(c->stream, c->nblk, c->g, st64, jacf, c->b, c->x, c->rf, c->part, c->ss, c->sc32, flags);
     });
     CK(cudaMemcpyAsync(c->h_ss, c->ss, sizeof(StepScal), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -726,7 +727,7 @@ int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres
   };
   double rel = 0.0;
   TRY(residual(3, &rel));
-  const double scale = c->h_ss->rnorm;
+  const double scale = sweep_scale(c->h_ss->rnorm);  // as the residual kernel set it
   *relres = rel;
   if (trace) std::fprintf(stderr, "[cfdgb] step %d relres %.3e\n", c->loop, rel);
   if (!std::isfinite(rel)) {
@@ -741,7 +742,7 @@ int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres
     c->test_wait_fault = false;
   }
   L(c, K_SETUP32, 1, [&] {
-    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), sweep_peak(c), 1,
+    launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->rf, c->ss, sweep_reduction(c), sweep_peak(c), 1,
                           c->part, c->sc32);
   });
   bool finish64 = false;
@@ -803,7 +804,7 @@ int solve_mixed(cfdgb_ctx *c, double tol, int *iters, int *outer, double *relres
       break;
     }
     L(c, K_SETUP32, 1, [&] {
-      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->r64, c->ss, sweep_reduction(c), sweep_peak(c), 0,
+      launch_refine_start32(c->stream, c->g, st64, jacf, c->k32, c->p32, c->ap32, c->rf, c->ss, sweep_reduction(c), sweep_peak(c), 0,
                             c->part, c->sc32);
     });
   }
@@ -1400,7 +1401,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
       if ((rc = dalloc(c, q, c->ncell))) return bail(rc);
   }
   if (cfg->precision == CFDGB_MIXED) {
-    if ((rc = dalloc(c, &c->r64, c->ncell))) return bail(rc);
+    if ((rc = dalloc(c, &c->rf, c->ncell))) return bail(rc);
     float **kv[] = {&c->k32.x, &c->k32.r0, &c->k32.r1, &c->k32.s, &c->k32.as, &c->p32[0], &c->p32[1],
                     &c->ap32[0], &c->ap32[1], &c->k32.xb};
     for (auto **q : kv)

@@ -114,6 +114,12 @@ inline bool div_certified(double b) {
 // the integer pipes instead.
 // double -> float, rounded to nearest (ties to even), by integer operations.  Results
 // below the normal FP32 range flush to a signed zero, above it to infinity; NaN stays NaN.
+// the scale of a MIXED solve's FP32 sweeps for a residual norm r: the power of two at or
+// below r (a multiplication by it, or by its inverse, is exact)
+__host__ __device__ __forceinline__ double sweep_scale(double r) {
+  return r > 0.0 && r <= 1.7e308 ? ldexp(1.0, ilogb(r)) : r;
+}
+
 __device__ __forceinline__ float d2f_int(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;

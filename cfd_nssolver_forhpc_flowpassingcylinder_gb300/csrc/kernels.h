@@ -116,15 +116,17 @@ void launch_cg32_part(cudaStream_t s, int part, const Geo &g, const Stencil<floa
 void launch_bicg_nan_reset(cudaStream_t s, int nblk, const Geo &g, double *x, const double *px1,
                            const double *px2, double *part, SolverScal *sc);
 
-// MIXED refinement pieces: FP64 residual (flags: 1 = also ||b||, 2 = also the FP32 scale)
-// and the start of an FP32 sweep on it (first: also the solve's set-up)
+// MIXED refinement pieces: FP64 residual, stored rounded to FP32 in rf (flags: 1 = also
+// ||b||, 2 = also the sweep scale) and the start of an FP32 sweep on it (first: also the
+// solve's set-up)
 void launch_residual64(cudaStream_t s, int nblk, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
-                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags);
+                       const double *x, float *rf, double *part, StepScal *ss, SolverScal *inner, int flags);
 void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
-                           float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
+                           float *const p2[2], float *const ap2[2], const float *rf, const StepScal *ss,
                            double delta, double peak, int first, double *part, SolverScal *sc);
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss);
-// x += factor (e - mean e), the mean taken from the preceding launch_sum32
+// x += factor (e - mean e), the mean taken from the preceding launch_sum32; factor = +-2^k
+// (sweep_scale)
 void launch_correct64(cudaStream_t s, int nblk, const Geo &g, double *x, const float *e, double factor,
                       const StepScal *ss);
 

@@ -1524,55 +1524,61 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
 }
 
 // ---- mixed precision: FP32 BiCGSTAB inside FP64 iterative refinement ----
-// Each sweep runs FP32 BiCGSTAB from a fresh start on r1 = (r64 - null-space part) / scale
+// Each sweep runs FP32 BiCGSTAB from a fresh start on r1 = (r - null-space part) / scale
 // (scale fixed for the whole solve) until its residual has dropped by delta; its
 // correction accumulates in the FP32 x.  The refinement adds scale * x to the FP64
-// solution and recomputes r64 = b - A x in FP64, which starts the next sweep.  Keeping the
+// solution and recomputes r = b - A x in FP64, which starts the next sweep.  Keeping the
 // Krylov space across refinements (reliable updates) was measured too: on the 512-cell
 // axis the FP32 iteration then breaks down near 1e-3 (with compensated dot products as
 // well: the FP32 vectors and stencil are the limit), while short restarted sweeps
 // converge to the FP64 tolerance.
 
-// r64 = b - A x (FP64); ||r||, ||b|| (flags & 1) and the scale (flags & 2).
-// jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose unscaled residual is r / jp.
-// FIRST: also ||b|| (a solve's first residual).  The kernel is bound by the FP64 pipe, so
-// the terms a call does not need are left out: ||b|| after the first, the null-space sum on
-// the stretched grid (whose residual is taken as it is).
+// r = b - A x in FP64, stored rounded to FP32 (rf); ||r||, ||b|| (flags & 1) and the sweep
+// scale (flags & 2): the power of two at or below ||r||, so that scaling by it, here and in
+// k_correct64, is exact.  jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose
+// unscaled residual is r / jp.  FIRST: also ||b|| (a solve's first residual).  The kernel
+// is bound by the FP64 pipe, so only the residual and the two norms are FP64; the
+// null-space sum (whose only use is to keep the FP32 system consistent) is summed in FP32
+// per thread, and is left out on the stretched grid (whose residual is taken as it is).
 template <bool FIRST>
 __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st, int jacobi,
                                                         const double *__restrict__ b, const double *__restrict__ x,
-                                                        double *__restrict__ r64, double *part, StepScal *ss,
+                                                        float *__restrict__ rf, double *part, StepScal *ss,
                                                         SolverScal *inner, int flags) {
   double acc[3] = {0.0, 0.0, 0.0};
+  float ns = 0.0f;
   const bool nsum = !g.nonuni;
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const double bb = b[row];
     const double r = bb - spmv_at<double>(g, st, x, ic, jc, kc, row);
-    r64[row] = r;
+    const float r32 = d2f_int(r);
+    rf[row] = r32;
     acc[0] += r * r;
     if (FIRST) acc[1] += bb * bb;
     // the unscaled residual's sum: its component along the operator's null space
-    if (nsum) acc[2] += jacobi ? r * row_diag(g, st, ic, jc, kc, row) : r;
+    if (nsum) ns += jacobi ? r32 * d2f_int(row_diag(g, st, ic, jc, kc, row)) : r32;
   }
+  acc[2] = f2d_int(ns);
   double out[3];
   if (grid_sum<3>(acc, part, &ss->cnt[1], out) && lin_tid() == 0) {
     if (flags & 1) ss->bnorm = sqrt(out[1]);
     ss->rnorm = sqrt(out[0]);
     ss->relres = ss->rnorm / ss->bnorm;
     ss->rsum = out[2];
-    if (flags & 2) inner->scale = ss->rnorm;
+    if (flags & 2) inner->scale = sweep_scale(ss->rnorm);
   }
 }
 
-// r64 minus its null-space part (the mean of the unscaled residual; for the Jacobi rows its
-// image jp * mean), scaled to FP32.  Removing it keeps the FP32 system consistent, so the
-// iteration cannot drift along the constant mode.
+// rf minus its null-space part (the mean of the unscaled residual; for the Jacobi rows its
+// image jp * mean), divided by the sweep scale, in FP32 (the division by a power of two is
+// exact).  Removing it keeps the FP32 system consistent, so the iteration cannot drift
+// along the constant mode.
 __device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<double> &st, int jacobi,
-                                                 const double *__restrict__ r64, double m, double inv, int ic, int jc,
+                                                 const float *__restrict__ rf, float mi, float inv, int ic, int jc,
                                                  int kc, long long row) {
-  const double c = jacobi ? r64[row] - m * row_jp(g, st, ic, jc, kc, row) : r64[row] - m;
-  return d2f_int(c * inv);
+  const float r = rf[row] * inv;
+  return jacobi ? fmaf(-mi, d2f_int(row_jp(g, st, ic, jc, kc, row)), r) : r - mi;
 }
 
 // start of a sweep: x = 0, r0 = r1 = scaled residual, rho = <r1, r1>; restart = 1 makes the
@@ -1580,18 +1586,19 @@ __device__ __forceinline__ float scaled_residual(const Geo &g, const Stencil<dou
 // reductions (against its start and its largest residual).  first: also the solve's set-up
 // (iteration count, the FP32 estimate's normalisation).
 __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double> st, int jacobi, Vec32 v,
-                                                            const double *__restrict__ r64, const StepScal *ss,
+                                                            const float *__restrict__ rf, const StepScal *ss,
                                                             double delta, double peak, int first, double *part,
                                                             SolverScal *sc) {
-  const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;
+  const double inv = sc->scale > 0.0 ? 1.0 / sc->scale : 0.0;  // a power of two
   // the null-space part is the mean on the uniform grid (a symmetric operator); on the
   // stretched grid the operator's left null vector is not constant, and the FP64 residual,
   // in range(A) for a consistent system, is taken as it is
   const double m = g.nonuni ? 0.0 : ss->rsum / (double)g.ncell;
+  const float inv32 = d2f_int(inv), mi = d2f_int(m * inv);
   Dot2F acc;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    const float r = scaled_residual(g, st, jacobi, r64, m, inv, ic, jc, kc, row);
+    const float r = scaled_residual(g, st, jacobi, rf, mi, inv32, ic, jc, kc, row);
     v.x[row] = 0.0f;
     v.r0[row] = r;
     v.r1[row] = r;
@@ -1636,14 +1643,19 @@ __global__ void __launch_bounds__(kBlock) k_sum32(Geo g, const float *__restrict
   if (grid_sum<1>(acc, part, &ss->cnt[5], out) && lin_tid() == 0) ss->esum = out[0];
 }
 
-// x += factor (e - mean e): factor = ||r|| applies an inner correction, -||r|| takes it
-// back; the mean (the constant mode, which the pressure leaves free) is dropped
+// x += factor (e - mean e): factor = +-2^k, the sweep scale, applies an inner correction
+// (+) or takes it back (-); the mean (the constant mode, which the pressure leaves free) is
+// dropped.  e - mean in FP32, widened exactly, scaled by 2^k and signed in its bits: one
+// FP64 addition a cell.
 __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict__ x, const float *__restrict__ e,
-                                                       double s, const StepScal *ss) {
-  const double m = ss->esum / (double)g.ncell;
+                                                       int k, int neg, const StepScal *ss) {
+  const float m = d2f_int(ss->esum / (double)g.ncell);
+  const long long shift = (long long)k << 52, sign = neg ? (long long)0x8000000000000000ULL : 0LL;
   FOR_CELLS(g) {
     const long long row = ROW(g);
-    x[row] += s * (f2d_int(e[row]) - m);
+    const long long d = __double_as_longlong(f2d_int(e[row] - m));
+    // a zero stays zero; any other value is an FP32 normal, far from the FP64 limits
+    x[row] += __longlong_as_double((d << 1) == 0 ? 0LL : (d + shift) ^ sign);
   }
 }
 
@@ -1873,16 +1885,16 @@ void launch_bicg_nan_reset(cudaStream_t s, int, const Geo &g, double *x, const d
 }
 
 void launch_residual64(cudaStream_t s, int, const Geo &g, const Stencil<double> &st, int jacobi, const double *b,
-                       const double *x, double *r64, double *part, StepScal *ss, SolverScal *inner, int flags) {
+                       const double *x, float *rf, double *part, StepScal *ss, SolverScal *inner, int flags) {
   if (flags & 1)
-    k_residual64<true><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
+    k_residual64<true><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, rf, part, ss, inner, flags);
   else
-    k_residual64<false><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, r64, part, ss, inner, flags);
+    k_residual64<false><<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, b, x, rf, part, ss, inner, flags);
 }
 void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, KrylovVecs<float> v,
-                           float *const p2[2], float *const ap2[2], const double *r64, const StepScal *ss,
+                           float *const p2[2], float *const ap2[2], const float *rf, const StepScal *ss,
                            double delta, double peak, int first, double *part, SolverScal *sc) {
-  k_refine_start32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), r64, ss, delta, peak, first, part,
+  k_refine_start32<<<cgrid(g), cblock(g), 0, s>>>(g, st, jacobi, v32(v, p2, ap2), rf, ss, delta, peak, first, part,
                                                    sc);
 }
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss) {
@@ -1890,7 +1902,8 @@ void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, St
 }
 void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor,
                       const StepScal *ss) {
-  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, factor, ss);
+  // factor = +-2^k (sweep_scale)
+  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, std::ilogb(factor), factor < 0.0 ? 1 : 0, ss);
 }
 void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
                         StepScal *ss) {

@@ -324,6 +324,21 @@ void launch_adj_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float
 // T2 = u* - (dt / Ds) (p+ - p) with the reciprocal metric, and the DFIB fraction, velocity
 // and force only on faces where eta is non-zero on either side (elsewhere u = T2 and the
 // force is zero); drag and lift summed as the exact kernel does.
+// DFIB on a face next to the body (eta non-zero on either side): the forced value
+// (1 - e) T2 and, when f is wanted, the face's force (n3 - T2) / dt dV.  Out of line, so
+// that the branch stays a branch: the faces away from the body (all but a few per mille)
+// then carry none of this FP64 work.
+struct DfibFace {
+  double n3, f;
+};
+__device__ __noinline__ DfibFace dfib_face(double T2, double en, double ec, double hf, double rdt, double vol) {
+  DfibFace r;
+  const double e = fma(en - ec, hf, ec);
+  r.n3 = (1.0 - e) * T2;
+  r.f = (r.n3 - T2) * rdt * vol;
+  return r;
+}
+
 template <bool UNI>
 __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     Geo g, double dt_arg, const double *dtp, int step_mode, double lz, const double *__restrict__ eta,
@@ -355,9 +370,9 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
-        const double e = fma(en - ec, g.hfx[i], ec);
-        n3 = (1.0 - e) * T2;
-        acc[0] += (n3 - T2) * rdt * (g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        const DfibFace d = dfib_face(T2, en, ec, g.hfx[i], rdt, g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        n3 = d.n3;
+        acc[0] += d.f;
       }
       u3[ic] = n3;
     } else if (ui) {
@@ -369,9 +384,9 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
-        const double e = fma(en - ec, g.hfy[j], ec);
-        n3 = (1.0 - e) * T2;
-        acc[1] += (n3 - T2) * rdt * (g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        const DfibFace d = dfib_face(T2, en, ec, g.hfy[j], rdt, g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        n3 = d.n3;
+        acc[1] += d.f;
       }
       v3[ic] = n3;
     } else if (vi) {
@@ -381,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
       const double T2 = fma(UNI ? gz : -(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
       const double en = eta[icP];
-      w3[ic] = (bc || nonzero(en)) ? (1.0 - fma(en - ec, g.hfz[k], ec)) * T2 : T2;
+      w3[ic] = (bc || nonzero(en)) ? dfib_face(T2, en, ec, g.hfz[k], rdt, 0.0).n3 : T2;
     } else if (wi) {
       w3[ic] = wi[ic];
     }
