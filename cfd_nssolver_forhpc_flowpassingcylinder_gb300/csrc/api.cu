@@ -1352,6 +1352,10 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
   int nblk3 = g.lgx * g.lgy * g.lgz;
   // vectorised FP32 kernels: quads of four k cells per thread when nz % 4 == 0
   // (the stretched grid's MIXED sweeps run the scalar kernels, on its stored FP32 rows)
+  // the flat pointwise kernels (every SM filled): the FP32 quad kernels and the MIXED
+  // refinement's sum and correction on any grid
+  g.xgrid = c->nsm * fp32_pointwise_blocks_per_sm();
+  nblk3 = std::max(nblk3, g.xgrid);
   if (cfg->nz % 4 == 0 && !std::getenv("CFDGB_SCALAR_FP32") && cfg->grid != CFDGB_GRID_SML) {
     const int nq = cfg->nz / 4;
     g.vbx = 1;
@@ -1364,8 +1368,7 @@ int cfdgb_create(const cfdgb_config *cfg, cfdgb_ctx **out) {
     const char *bps = std::getenv("CFDGB_FP32_BLOCKS_PER_SM");
     const int per_sm = bps ? std::max(1, std::atoi(bps)) : 4;
     g.vgz = std::max(1, std::min(cfg->nx, c->nsm * per_sm / std::max(1, g.vgx * g.vgy)));
-    g.xgrid = c->nsm * fp32_pointwise_blocks_per_sm();
-    nblk3 = std::max(nblk3, std::max(g.vgx * g.vgy * g.vgz, g.xgrid));
+    nblk3 = std::max(nblk3, g.vgx * g.vgy * g.vgz);
     int tbps = 0, tbps2 = 0;
     if (!std::getenv("CFDGB_NO_TMA") && fp32_stage_plan(cfg->nz, &g.tj, &g.tsmem, &tbps, &g.tsmem2, &tbps2)) {
       g.tma = 1;

@@ -721,11 +721,16 @@ __global__ void __launch_bounds__(kMgMarchThreads, 2)
   float4 ca = ldc(m0 - 1), cb = ldc(m0), cn = cb;
   float4 bn1 = ldb(is - 2), bn2 = ldb(is - 1);
   float bA[4] = {}, bB[4] = {}, bC[4] = {};  // b of planes p, p-1, p-2 (rotating)
-  float xA[4] = {}, xB[4] = {}, xC[4] = {};  // colour 0 + P xc, planes p, p-1, p-2
-  float yA[4] = {}, yB[4] = {}, yC[4] = {};  // after colour 1, planes p-1, p-2, p-3
-  auto step = [&](int p, float(&b0)[4], float(&b1)[4], float(&b2)[4], float(&x0)[4], float(&x1)[4],
-                  float(&x2)[4], float(&y1)[4], float(&y2)[4], float(&y3)[4], int s0, int s1, int s2) {
+  // the earlier planes of both stages are read back from this thread's own shared slots
+  // (registers are this kernel's limit); zeros before the march, as the planes before it
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    sa[q * PL] = make_float4(0.f, 0.f, 0.f, 0.f);
+    sb[q * PL] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  auto step = [&](int p, float(&b0)[4], float(&b1)[4], float(&b2)[4], int s0, int s1, int s2) {
     const bool odd = p & 1;
+    float x0[4], x1[4], x2[4], y1[4], y2[4], y3[4];  // colour 0 + P xc of p, p-1, p-2; after colour 1, p-1..p-3
     // plane p: colour 0 = b / diag + P xc (k_mg_prolong8: parent first on every axis)
     unq(bn1, b0);
     bn1 = bn2;
@@ -768,6 +773,10 @@ __global__ void __launch_bounds__(kMgMarchThreads, 2)
       }
     }
     __syncthreads();
+    unq(sa[s1 * PL], x1);
+    unq(sa[s2 * PL], x2);
+    unq(sb[s2 * PL], y2);
+    unq(sb[s0 * PL], y3);  // plane p - 3 (the slot that takes plane p in the next step)
     {  // plane p - 1: colour 1 of the post-smoothing
       const int i = p - 1;
       float kl, kr;
@@ -798,11 +807,11 @@ __global__ void __launch_bounds__(kMgMarchThreads, 2)
     }
   };
   for (int p = is - 2;;) {
-    step(p, bA, bC, bB, xA, xC, xB, yA, yC, yB, 0, 2, 1);
+    step(p, bA, bC, bB, 0, 2, 1);
     if (++p > ie + 1) break;
-    step(p, bB, bA, bC, xB, xA, xC, yB, yA, yC, 1, 0, 2);
+    step(p, bB, bA, bC, 1, 0, 2);
     if (++p > ie + 1) break;
-    step(p, bC, bB, bA, xC, xB, xA, yC, yB, yA, 2, 1, 0);
+    step(p, bC, bB, bA, 2, 1, 0);
     if (++p > ie + 1) break;
   }
 }

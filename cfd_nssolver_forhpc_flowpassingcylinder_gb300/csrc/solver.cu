@@ -30,6 +30,13 @@ namespace cfdgb {
   const bool on_ = (kc < (g).nzc) && (jc < (g).nyc);               \
   for (int ic = blockIdx.z; on_ && ic < (g).nxc; ic += gridDim.z)
 
+// the same, four planes of a thread's column in flight at once (short bodies that stream)
+#define FOR_CELLS4(g)                                              \
+  const int kc = blockIdx.x * blockDim.x + threadIdx.x;            \
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y;            \
+  const bool on_ = (kc < (g).nzc) && (jc < (g).nyc);               \
+  _Pragma("unroll 4") for (int ic = blockIdx.z; on_ && ic < (g).nxc; ic += gridDim.z)
+
 #define ROW(g) ((((long long)ic * (g).nyc + jc) * (g).nzc) + kc)
 
 __device__ __forceinline__ int cls_of(const Geo &g, int ic, int jc, int kc) { return row_class(g, ic, jc, kc); }
@@ -1596,7 +1603,7 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
   const double m = g.nonuni ? 0.0 : ss->rsum / (double)g.ncell;
   const float inv32 = d2f_int(inv), mi = d2f_int(m * inv);
   Dot2F acc;
-  FOR_CELLS(g) {
+  FOR_CELLS4(g) {
     const long long row = ROW(g);
     const float r = scaled_residual(g, st, jacobi, rf, mi, inv32, ic, jc, kc, row);
     v.x[row] = 0.0f;
@@ -1629,15 +1636,19 @@ __global__ void __launch_bounds__(kBlock) k_refine_start32(Geo g, Stencil<double
   }
 }
 
-// sum of the inner correction e (FP64)
 // sum of e: FP32 per thread (its only use is the constant mode, which the operator
-// annihilates, so its rounding changes x by a constant), FP64 over threads
+// annihilates, so its rounding changes x by a constant), FP64 over threads.  Pointwise on
+// the compact vector: quads over a flat grid-stride loop (g.xgrid blocks), the tail cells
+// of a cell count that is not a multiple of 4 by the first threads.
 __global__ void __launch_bounds__(kBlock) k_sum32(Geo g, const float *__restrict__ e, double *part, StepScal *ss) {
   float f = 0.0f;
-  FOR_CELLS(g) {
-    const long long row = ROW(g);
-    f += e[row];
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long q = t0; q < nq; q += stride) {
+    const float4 v = *reinterpret_cast<const float4 *>(e + 4 * q);
+    f += (v.x + v.y) + (v.z + v.w);
   }
+  if (t0 < g.ncell - 4 * nq) f += e[4 * nq + t0];
   double acc[1] = {f2d_int(f)};
   double out[1];
   if (grid_sum<1>(acc, part, &ss->cnt[5], out) && lin_tid() == 0) ss->esum = out[0];
@@ -1646,17 +1657,30 @@ __global__ void __launch_bounds__(kBlock) k_sum32(Geo g, const float *__restrict
 // x += factor (e - mean e): factor = +-2^k, the sweep scale, applies an inner correction
 // (+) or takes it back (-); the mean (the constant mode, which the pressure leaves free) is
 // dropped.  e - mean in FP32, widened exactly, scaled by 2^k and signed in its bits: one
-// FP64 addition a cell.
+// FP64 addition a cell.  Pointwise, quads as k_sum32.
+__device__ __forceinline__ double correction(float e, float m, long long shift, long long sign) {
+  const long long d = __double_as_longlong(f2d_int(e - m));
+  // a zero stays zero; any other value is an FP32 normal, far from the FP64 limits
+  return __longlong_as_double((d << 1) == 0 ? 0LL : (d + shift) ^ sign);
+}
 __global__ void __launch_bounds__(kBlock) k_correct64(Geo g, double *__restrict__ x, const float *__restrict__ e,
                                                        int k, int neg, const StepScal *ss) {
   const float m = d2f_int(ss->esum / (double)g.ncell);
   const long long shift = (long long)k << 52, sign = neg ? (long long)0x8000000000000000ULL : 0LL;
-  FOR_CELLS(g) {
-    const long long row = ROW(g);
-    const long long d = __double_as_longlong(f2d_int(e[row] - m));
-    // a zero stays zero; any other value is an FP32 normal, far from the FP64 limits
-    x[row] += __longlong_as_double((d << 1) == 0 ? 0LL : (d + shift) ^ sign);
+  const long long nq = g.ncell / 4, stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long q = t0; q < nq; q += stride) {
+    const float4 v = *reinterpret_cast<const float4 *>(e + 4 * q);
+    double2 *xp = reinterpret_cast<double2 *>(x + 4 * q);
+    double2 a = xp[0], b = xp[1];
+    a.x += correction(v.x, m, shift, sign);
+    a.y += correction(v.y, m, shift, sign);
+    b.x += correction(v.z, m, shift, sign);
+    b.y += correction(v.w, m, shift, sign);
+    xp[0] = a;
+    xp[1] = b;
   }
+  if (t0 < g.ncell - 4 * nq) x[4 * nq + t0] += correction(e[4 * nq + t0], m, shift, sign);
 }
 
 // ---- null-space projection of the right-hand side (project_rhs) ----
@@ -1898,12 +1922,12 @@ void launch_refine_start32(cudaStream_t s, const Geo &g, const Stencil<double> &
                                                    sc);
 }
 void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, StepScal *ss) {
-  k_sum32<<<cgrid(g), cblock(g), 0, s>>>(g, e, part, ss);
+  k_sum32<<<g.xgrid, kBlock, 0, s>>>(g, e, part, ss);
 }
 void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor,
                       const StepScal *ss) {
   // factor = +-2^k (sweep_scale)
-  k_correct64<<<cgrid(g), cblock(g), 0, s>>>(g, x, e, std::ilogb(factor), factor < 0.0 ? 1 : 0, ss);
+  k_correct64<<<g.xgrid, kBlock, 0, s>>>(g, x, e, std::ilogb(factor), factor < 0.0 ? 1 : 0, ss);
 }
 void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
                         StepScal *ss) {

@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
     gz = -(dt * g.rDzs[2]);
   }
   double acc[2] = {0.0, 0.0};
+#pragma unroll 2
   for (long long row = blockIdx.x * (long long)kBlock + threadIdx.x; row < g.ncell;
        row += (long long)gridDim.x * kBlock) {
     int i, j, k;
