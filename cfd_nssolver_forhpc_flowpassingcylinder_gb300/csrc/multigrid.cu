@@ -513,7 +513,10 @@ __device__ __forceinline__ void march_kz(const MarchRow &R, const float (&v)[4],
   kr = R.zr ? r : 0.f;
 }
 
-// b of a quad's cell pairs, times the diagonal for Jacobi-scaled rows (BS)
+// b of a quad's cell pairs, times the diagonal for Jacobi-scaled rows (BS).  The product
+// stays scalar: its FP32x2 form gave results different from the per-pass kernels on the
+// Jacobi-scaled runs (measured; the pair operations alone round as the scalar ones do, and
+// the cause was not found), the scalar form gives identical ones.
 template <bool BS>
 __device__ __forceinline__ void march_bb(const MarchRow &R, float dxy, const float (&bv)[4], float2 &b01,
                                          float2 &b23) {
