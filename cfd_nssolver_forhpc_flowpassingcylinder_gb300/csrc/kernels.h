@@ -179,6 +179,10 @@ struct MgLevelT {
   // quads, every axis halves, nz / 4 a power of two up to 16): a block of nz / 4 x (mty + 4)
   // threads owns a band of mty rows and marches over a segment of msx planes; mgx x mgy blocks
   int march, mty, msx, mgx, mgy;
+  // division of a cell index by nz, ny and nz / 2 (the one-block kernels' cell loops): the
+  // multiplier and shift of a division by an invariant integer (div_magic in multigrid.cu)
+  unsigned dz_m, dy_m, dh_m;
+  int dz_l, dy_l, dh_l;
   // 1/diag of a row by its neighbour counts along x, y, z (each 0..2): idg[9 cx + 3 cy + cz]
   // (0 where a row has no neighbour); the smoother multiplies instead of dividing
   T idg[27];

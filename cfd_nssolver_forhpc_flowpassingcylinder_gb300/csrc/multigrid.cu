@@ -877,17 +877,48 @@ constexpr int kMgTailBytes = 48 * 1024;
 template <typename T>
 constexpr int tail_cells_max() { return kMgTailBytes / (2 * (int)sizeof(T)); }
 
+// Unsigned division by an invariant d >= 1 (Granlund and Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994, the round-up method): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (t + ((n - t) >> 1)) >> (l - 1), t = mulhi(m, n),
+// for every 32-bit n (d = 1: l = 0 and the quotient is n).
+static inline void div_magic(unsigned d, unsigned *m, int *l) {
+  int ll = 0;
+  while ((1ull << ll) < d) ++ll;
+  *l = ll;
+  *m = (unsigned)((((1ull << ll) - d) << 32) / d + 1);
+}
+__device__ __forceinline__ unsigned udiv_inv(unsigned n, unsigned m, int l) {
+  if (l == 0) return n;
+  const unsigned t = __umulhi(m, n);
+  return (t + ((n - t) >> 1)) >> (l - 1);
+}
+
 template <typename T>
 __device__ __forceinline__ void cell_ijk(const MgLevelT<T> &L, int q, int &i, int &j, int &k) {
-  k = q % L.nz;
-  const int t = q / L.nz;
-  j = t % L.ny;
-  i = t / L.ny;
+  const unsigned t = udiv_inv((unsigned)q, L.dz_m, L.dz_l), u = udiv_inv(t, L.dy_m, L.dy_l);
+  k = q - (int)t * L.nz;
+  j = (int)t - (int)u * L.ny;
+  i = (int)u;
 }
 
 template <typename T>
 __device__ void blk_smooth(const MgLevelT<T> &L, int colour, int zero, const T *b, T *x) {
   const int n = L.nx * L.ny * L.nz;
+  if (L.nz % 2 == 0) {
+    // the cells of a row pair up along k, one of each colour: a thread per pair updates the
+    // one of the colour (and, from zero, clears the other)
+    const int half = L.nz / 2, np = n / 2;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+      const unsigned r = udiv_inv((unsigned)p, L.dh_m, L.dh_l), ii = udiv_inv(r, L.dy_m, L.dy_l);
+      const int i = (int)ii, j = (int)r - i * L.ny, d = (i + j + colour) & 1;
+      const int k = 2 * (p - (int)r * half) + d, q = (int)r * L.nz + k;
+      if (zero) x[q + 1 - 2 * d] = T(0);
+      const T num = zero ? b[q] : b[q] + lnb(L, x, i, j, k, q);
+      x[q] = num * linv(L, i, j, k);
+    }
+    __syncthreads();
+    return;
+  }
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     int i, j, k;
     cell_ijk(L, q, i, j, k);
@@ -1023,6 +1054,9 @@ bool mg_plan(int nx, int ny, int nz, double hx, double hy, double hz, int nsm, b
       L.idg[q] = d > T(0) ? T(1) / d : T(0);
     }
     level_geometry(L, nsm, quads);
+    div_magic((unsigned)nz, &L.dz_m, &L.dz_l);
+    div_magic((unsigned)ny, &L.dy_m, &L.dy_l);
+    div_magic((unsigned)std::max(1, nz / 2), &L.dh_m, &L.dh_l);
     const long long cells = (long long)nx * ny * nz;
     const int fx = nx % 2 == 0 ? 2 : 1, fy = ny % 2 == 0 ? 2 : 1, fz = nz % 2 == 0 ? 2 : 1;
     if (cells <= kMgCoarseCells || fx * fy * fz == 1 || l + 1 == kMgMaxLevels) {
