@@ -64,8 +64,10 @@ MARCH_CASES = {
     "128x64x16": CASES["128x64x16"],
     # four marching levels (nz / 4 = 16, 8, 4, 2), several bands and segments on each
     "256x128x64": dict(nx=256, ny=128, nz=64, lx=32.0, ly=16.0, lz=4.0, cx=8.0, cy=8.0),
-    # a ragged band (ny not a multiple of the band), one segment per level
-    "64x40x8": dict(nx=64, ny=40, nz=8, lx=16.0, ly=10.0, lz=2.0, cx=4.0, cy=5.0, project_rhs=1),
+    # a ragged band on level 0 (40 rows: bands of 32 and 8), one band on level 1
+    "64x40x32": dict(nx=64, ny=40, nz=32, lx=16.0, ly=10.0, lz=8.0, cx=4.0, cy=5.0, project_rhs=1),
+    # level 0 on the per-pass kernels (nz / 4 = 32), level 1 marching: the two paths meet
+    "64x32x128": dict(nx=64, ny=32, nz=128, lx=16.0, ly=8.0, lz=32.0, cx=4.0, cy=4.0, project_rhs=1),
     # the stated boundary set: periodic z on every level, the seeded perturbation
     "set 128x64x16": dict(CASES["128x64x16"], seed=7, amp=1e-3, **cg.BOUNDARY_SET),
 }
