@@ -331,11 +331,14 @@ void launch_adj_convdiff_f32(cudaStream_t s, int nblk, const Geo &g, const float
 struct DfibFace {
   double n3, f;
 };
-__device__ __noinline__ DfibFace dfib_face(double T2, double en, double ec, double hf, double rdt, double vol) {
+// (the cell volume is formed inside, from the metric entries, so that none of it is
+// evaluated ahead of the branch; dz null: no force wanted)
+__device__ __noinline__ DfibFace dfib_face(double T2, double en, double ec, double hf, double rdt,
+                                           const double *dx, const double *dy, const double *dz) {
   DfibFace r;
   const double e = fma(en - ec, hf, ec);
   r.n3 = (1.0 - e) * T2;
-  r.f = (r.n3 - T2) * rdt * vol;
+  r.f = dz ? (r.n3 - T2) * rdt * (*dx * *dy * *dz) : 0.0;
   return r;
 }
 
@@ -371,7 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
-        const DfibFace d = dfib_face(T2, en, ec, g.hfx[i], rdt, g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        const DfibFace d = dfib_face(T2, en, ec, g.hfx[i], rdt, g.Dx + i, g.Dy + j, g.Dz + k);
         n3 = d.n3;
         acc[0] += d.f;
       }
@@ -385,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const double en = eta[icP];
       double n3 = T2;
       if (bc || nonzero(en)) {
-        const DfibFace d = dfib_face(T2, en, ec, g.hfy[j], rdt, g.Dx[i] * g.Dy[j] * g.Dz[k]);
+        const DfibFace d = dfib_face(T2, en, ec, g.hfy[j], rdt, g.Dx + i, g.Dy + j, g.Dz + k);
         n3 = d.n3;
         acc[1] += d.f;
       }
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(kBlock) k_update_uf_fast(
       const long long icP = (g.pz && k == g.nz - 3) ? ic - (g.nzc - 1) : ic + 1;
       const double T2 = fma(UNI ? gz : -(dt * g.rDzs[k]), p[icP] - p[ic], ws[ic]);
       const double en = eta[icP];
-      w3[ic] = (bc || nonzero(en)) ? dfib_face(T2, en, ec, g.hfz[k], rdt, 0.0).n3 : T2;
+      w3[ic] = (bc || nonzero(en)) ? dfib_face(T2, en, ec, g.hfz[k], rdt, nullptr, nullptr, nullptr).n3 : T2;
     } else if (wi) {
       w3[ic] = wi[ic];
     }
