@@ -166,8 +166,8 @@ STEP_KERNELS = {
     "convection_diffusion": (60, 3),  # read u32, v32, w32 (FP32) and u, v, w; write us, vs, ws; 3 DADD
     "update_uf": (64, 6),             # read eta, p, us, vs, ws; write u, v, w; 3 DADD + 3 DFMA (uniform grid)
     "rhs": (32, 8),                   # read us, vs, ws; write b
-    "residual64": (24, 9),            # read b, x; write r; 7-point stencil, subtraction, norm
-    "correct64": (24, 2),             # read e (mean), then x, e; write x
+    "residual64": (20, 8),            # read b, x; write r (FP32); 7 DFMA from b, the norm's DFMA
+    "correct64": (24, 1),             # read e (mean), then x, e; write x; 1 DADD (the scaling in integers)
     "mirror32": (36, 0),              # read u, v, w; write u32, v32, w32 (integer rounding; padded fields)
 }
 

@@ -111,6 +111,36 @@ __device__ __forceinline__ float stencil_apply_diff(const Geo &g, const Stencil<
   return sum;
 }
 
+// b - (A x)(row) as one FMA chain from b, the terms in stencil_apply's order (the MIXED
+// refinement's residual: FP64-pipe-bound, so the subtraction folds into the chain)
+__device__ __forceinline__ double resid_at(const Geo &g, const Stencil<double> &st, const double *__restrict__ x, int ic,
+                                          int jc, int kc, long long row, double bb) {
+  const long long nyz = (long long)g.nyc * g.nzc;
+  const long long zm = z_minus(g, kc, row), zp = z_plus(g, kc, row);
+  double r = bb;
+  if (g.nonuni) {  // stretched grid: the rows stored per context
+    const double *__restrict__ cs = g.cof[st.jac] + row;
+    const long long n = g.ncell;
+    if (ic > 0) r = fma(-cs[0], x[row - nyz], r);
+    if (jc > 0) r = fma(-cs[n], x[row - g.nzc], r);
+    if (zm >= 0) r = fma(-cs[2 * n], x[zm], r);
+    r = fma(-cs[3 * n], x[row], r);
+    if (zp >= 0) r = fma(-cs[4 * n], x[zp], r);
+    if (jc < g.nyc - 1) r = fma(-cs[5 * n], x[row + g.nzc], r);
+    if (ic < g.nxc - 1) r = fma(-cs[6 * n], x[row + nyz], r);
+    return r;
+  }
+  const double *c = st.c[cls_of(g, ic, jc, kc)];
+  if (ic > 0) r = fma(-c[0], x[row - nyz], r);
+  if (jc > 0) r = fma(-c[1], x[row - g.nzc], r);
+  if (zm >= 0) r = fma(-c[2], x[zm], r);
+  r = fma(-c[3], x[row], r);
+  if (zp >= 0) r = fma(-c[4], x[zp], r);
+  if (jc < g.nyc - 1) r = fma(-c[5], x[row + g.nzc], r);
+  if (ic < g.nxc - 1) r = fma(-c[6], x[row + nyz], r);
+  return r;
+}
+
 template <typename T>
 __device__ __forceinline__ T spmv_at(const Geo &g, const Stencil<T> &st, const T *__restrict__ x, int ic, int jc,
                                      int kc, long long row) {
@@ -1544,7 +1574,7 @@ __global__ void __launch_bounds__(kBlock) k_nan_restore(Geo g, double *x, const 
 // scale (flags & 2): the power of two at or below ||r||, so that scaling by it, here and in
 // k_correct64, is exact.  jacobi: st holds the jp-scaled rows (st.c[.][7] = jp), whose
 // unscaled residual is r / jp.  FIRST: also ||b|| (a solve's first residual).  The kernel
-// is bound by the FP64 pipe, so only the residual and the two norms are FP64; the
+// is bound by the FP64 pipe, so only the residual (7 FMA from b) and the norms are FP64; the
 // null-space sum (whose only use is to keep the FP32 system consistent) is summed in FP32
 // per thread, and is left out on the stretched grid (whose residual is taken as it is).
 template <bool FIRST>
@@ -1558,7 +1588,7 @@ __global__ void __launch_bounds__(kBlock) k_residual64(Geo g, Stencil<double> st
   FOR_CELLS(g) {
     const long long row = ROW(g);
     const double bb = b[row];
-    const double r = bb - spmv_at<double>(g, st, x, ic, jc, kc, row);
+    const double r = resid_at(g, st, x, ic, jc, kc, row, bb);
     const float r32 = d2f_int(r);
     rf[row] = r32;
     acc[0] += r * r;
