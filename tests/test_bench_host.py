@@ -92,9 +92,10 @@ def test_step_kernel_roofline_names_the_bound():
             "mirror32": (0.05, 1), "correct64": (0.1, 4)}
     r = bench.step_roofline(prof, cells, npad, 5000.0, fp)
     res = r["residual64"]
+    nbytes, ninst = bench.STEP_KERNELS["residual64"]
     assert res["avg_launch_us"] == 100.0
-    assert res["achieved_gbs"] == round(24 * cells / 1e-4 / 1e9, 1)
-    assert res["fp64_frac"] == round(9 * cells / 1e-4 / 5e11, 4) and res["bound"] == "fp64"
+    assert res["achieved_gbs"] == round(nbytes * cells / 1e-4 / 1e9, 1)
+    assert res["fp64_frac"] == round(ninst * cells / 1e-4 / 5e11, 4) and res["bound"] == "fp64"
     assert r["mirror32"]["achieved_gbs"] == round(36 * npad / 5e-5 / 1e9, 1) and r["mirror32"]["bound"] == "hbm"
     assert r["correct64"]["launches"] == 2 and r["correct64"]["avg_launch_us"] == 50.0
     assert "update_uf" not in r
