@@ -20,6 +20,17 @@ def test_reference_window_beyond_the_record_is_refused():
         bench.reference_window_iters(rec, warmup=2, steps=4)
 
 
+def test_committed_record_covers_the_default_and_the_twenty_step_windows():
+    """The reference's own recorded run spans the windows the bench times by default (3
+    warm-up steps, 10 timed) and with 5 warm-up steps and 20 timed, each solve to 1e-8."""
+    rec = bench.reference_iteration_record("c2")
+    assert rec["tol"] == 1e-8 and len(rec["iters"]) >= 25
+    for warmup, steps in ((3, 10), (5, 20)):
+        its = bench.reference_window_iters(rec, warmup=warmup, steps=steps)
+        assert len(its) == steps and all(n > 0 for n in its)
+    assert all(r < 1e-8 for r in rec["relres"][1:])
+
+
 def test_reference_arm_unavailable_when_the_record_is_short(capsys, monkeypatch):
     monkeypatch.setattr(bench, "reference_iteration_record", lambda wl: {"iters": [0, 1, 2]})
     assert bench.main(["--impl", "reference", "--steps", "20", "--warmup", "5"]) == 0
