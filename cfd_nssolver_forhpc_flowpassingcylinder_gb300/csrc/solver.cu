@@ -1956,7 +1956,8 @@ void launch_sum32(cudaStream_t s, const Geo &g, const float *e, double *part, St
 }
 void launch_correct64(cudaStream_t s, int, const Geo &g, double *x, const float *e, double factor,
                       const StepScal *ss) {
-  // factor = +-2^k (sweep_scale)
+  // factor = +-2^k (sweep_scale); a zero factor (a zero residual, never corrected) adds nothing
+  if (!(std::fabs(factor) > 0.0) || !std::isfinite(factor)) return;
   k_correct64<<<g.xgrid, kBlock, 0, s>>>(g, x, e, std::ilogb(factor), factor < 0.0 ? 1 : 0, ss);
 }
 void launch_project_rhs(cudaStream_t s, const Geo &g, const Stencil<double> &st, int jacobi, double *b, double *part,
